@@ -1,0 +1,143 @@
+/*
+ * spice_gb300.h -- C ABI of the GB300-native snn::step engine.
+ *
+ * The reference (denniskb/spice2) has no C ABI: its boundary is the C++20 template API of
+ * spice/include/spice/snn.h plus the two virtual interfaces NeuronPopulation
+ * (spice/include/spice/detail/neuron_population.h:17-25) and SynapsePopulation
+ * (spice/include/spice/detail/synapse_population.h:17-24).  Each entry point below replaces one
+ * member of that boundary (cited beside it) with plain pointers and sizes, so a C, Python
+ * (ctypes), Go (cgo) or Java (JNI) host can drive the engine.  The C++ front end in
+ * include/spice/ re-exposes the reference's own names on top of these calls.
+ *
+ * Conventions
+ *   - Every call returns an int status: SPICE_OK (0) or one of the SPICE_E* codes below.  The
+ *     message of the last failure on the calling thread is spice_last_error().  Failed
+ *     preconditions carry the reference's wording ("Assertion failed (file:line): cond",
+ *     spice/src/util/assert.cpp:8-15).  No C++ exception crosses the ABI.
+ *   - A spice_net owns all of its populations and connections (snn.h:72-74).  Population and
+ *     connection ids are small integers in add order.
+ *   - One CUDA stream per net; a net is not thread-safe.  Host buffers are plain host memory;
+ *     calls that return data synchronise the net's stream.
+ *   - All device work runs on the current CUDA device at spice_net_create time.
+ */
+#ifndef SPICE_GB300_H
+#define SPICE_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPICE_OK 0
+#define SPICE_EINVAL 1    /* a precondition failed (SPICE_PRE in the reference)            */
+#define SPICE_ECUDA 2     /* a CUDA runtime call failed                                     */
+#define SPICE_ENOMEM 3    /* device or host allocation failed                               */
+#define SPICE_ESTATE 4    /* the call is not valid in the net's current state              */
+#define SPICE_EOVERFLOW 5 /* a caller buffer is too small; the needed size is returned      */
+
+/* Neuron models (the user-model structs of samples/brunel.cpp, samples/vogels.cpp and
+ * samples/external_input.cpp, built in so non-C++ hosts can use them). */
+enum {
+	SPICE_NEURON_POISSON  = 0, /* stateless; params {rate_hz=20}; one draw per neuron and step  */
+	SPICE_NEURON_LIF      = 1, /* {V, Tref}; params {Vthres=0.02, Tref=20, TmemInv=50}          */
+	SPICE_NEURON_LIF_COND = 2, /* {V, Gex, Gin, Tref}; samples/vogels.cpp constants             */
+	SPICE_NEURON_EXTERNAL = 3, /* per-population update replaying a cyclic spike train          */
+};
+
+/* Synapse models. */
+enum {
+	/* fixed_weight (samples/brunel.cpp:67-70): deliver adds params[0] (weight) to state field
+	 * params[1] of the target (0 = V, 1 = Gex, 2 = Gin; default 0). */
+	SPICE_SYNAPSE_FIXED_WEIGHT = 0,
+};
+
+/* Delivery modes. */
+enum {
+	SPICE_MODE_DETERMINISTIC = 0, /* bit-exact with the reference's sequential delivery order */
+	SPICE_MODE_ATOMIC        = 1, /* float atomics: fastest, order-dependent rounding          */
+};
+
+/* State fields for spice_get_state / spice_set_state. */
+enum { SPICE_FIELD_V = 0, SPICE_FIELD_GEX = 1, SPICE_FIELD_GIN = 2, SPICE_FIELD_TREF = 3 };
+
+typedef struct spice_net spice_net;
+
+/* snn::snn(dt, max_delay, seed) -- spice/include/spice/snn.h:18-19.  seeds: the
+ * std::initializer_list<UInt32> of util::seed_seq (spice/include/spice/util/random.h:149-152). */
+int spice_net_create(float dt, float max_delay, const uint32_t* seeds, int nseeds, spice_net** out);
+int spice_net_destroy(spice_net* net);
+
+/* snn::add_population<Neur>(size, neur) -- snn.h:21-27 (neuron_population.h:106-112).  Stateful
+ * models consume one seed, as stateful_neuron_adapter does (neuron_population.h:56-60). */
+int spice_add_population(spice_net* net, int model, int64_t size, const float* params, int nparams,
+                         int* pop_out);
+
+/* snn::connect<Syn>(src, dst, fixed_probability(p), delay, syn) -- snn.h:29-48, with the
+ * adjacency of fixed_probability::generate (spice/src/topology.cpp:78-112) generated on the GPU,
+ * bit-identical to the reference's for the same seed. */
+int spice_connect_fixed_probability(spice_net* net, int src, int dst, double p, float delay,
+                                    int synapse, const float* params, int nparams, int* conn_out);
+
+/* snn::connect<Syn>(src, dst, adj_list, delay, syn) -- snn.h:29-48 with adj_list
+ * (topology.cpp:56-71); pairs holds npairs (src, dst) int32 pairs. */
+int spice_connect_adj_list(spice_net* net, int src, int dst, const int32_t* pairs, int64_t npairs,
+                           float delay, int synapse, const float* params, int nparams,
+                           int* conn_out);
+
+/* The per-population update of samples/external_input.cpp:17-30: population `pop` (model
+ * SPICE_NEURON_EXTERNAL) emits the spikes of train step (i mod nsteps) at its i-th update. */
+int spice_set_external_input(spice_net* net, int pop, int nsteps, const int32_t* counts,
+                             const int32_t* indices);
+
+int spice_set_mode(spice_net* net, int mode);
+/* Upper bound on the steps fused into one neuron-update launch (default: the network's
+ * minimum connection delay, the largest value that keeps the reference's semantics). */
+int spice_set_window(spice_net* net, int max_window);
+
+/* snn::step() -- spice/src/snn.cpp:7-28. */
+int spice_step(spice_net* net);
+/* `steps` calls of snn::step(), fused into windows of up to min-delay steps. */
+int spice_run(spice_net* net, int64_t steps);
+/* spice_run that also records every step's spikes (the raster that samples/matplot.cpp:96-134
+ * prints): counts_out[steps][npop] and the ascending spike indices, step-major then population
+ * order, into spikes_out (capacity entries).  *total_out = number of spikes recorded. */
+int spice_run_record(spice_net* net, int64_t steps, int64_t* counts_out, int32_t* spikes_out,
+                     int64_t capacity, int64_t* total_out);
+
+/* NeuronPopulation::spikes(age) -- neuron_population.h:147-153: ascending indices of the
+ * neurons of `pop` that fired `age` steps ago, 0 <= age < min(steps run, max_delay). */
+int spice_spike_count(spice_net* net, int pop, int64_t age, int64_t* n_out);
+int spice_spikes(spice_net* net, int pop, int64_t age, int32_t* out, int64_t capacity,
+                 int64_t* n_out);
+
+/* neuron_population::get_neurons() -- neuron_population.h:139-145, one SoA field at a time
+ * (float fields V/Gex/Gin, int32 field Tref), into or from a host buffer of size() elements. */
+int spice_get_state(spice_net* net, int pop, int field, void* host_out);
+int spice_set_state(spice_net* net, int pop, int field, const void* host_in);
+
+int spice_pop_size(spice_net* net, int pop, int64_t* size_out);
+int spice_time(spice_net* net, int64_t* time_out);
+/* Synaptic events delivered so far (sum over delivered spikes of their CSR row lengths). */
+int spice_events(spice_net* net, uint64_t* events_out);
+
+/* csr<T> of a connection -- spice/include/spice/detail/csr.h:69-99: offsets (src+1 int64) and
+ * neighbors (synapses int32), copied to host buffers. */
+int spice_conn_size(spice_net* net, int conn, int64_t* src_out, int64_t* synapses_out);
+int spice_get_csr(spice_net* net, int conn, int64_t* offsets_out, int32_t* neighbors_out);
+
+/* Per-kernel timing with CUDA events recorded on the net's stream around every launch. */
+int spice_set_profiling(spice_net* net, int on);
+/* kind: 0 = neuron update, 1 = spike delivery, 2 = raster extraction.  Returns the number of
+ * launches and their summed device time (ms) since profiling was switched on. */
+int spice_kernel_stats(spice_net* net, int kind, int64_t* launches_out, double* ms_out);
+/* Number of kernels this library launched on the net's stream so far. */
+int spice_launch_count(spice_net* net, int64_t* launches_out);
+
+int spice_synchronize(spice_net* net);
+const char* spice_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,269 @@
+// ref_driver.cpp -- runs the spice2 reference itself (TEST INFRASTRUCTURE ONLY).
+//
+// Compiled by oracle/Makefile against the reference's own headers and its three source files
+// (spice/src/{snn,topology,util/assert}.cpp) with the reference's Release flags
+// (CMakeLists.txt:42-54, configure.sh:8), into oracle/_ref/ref_driver.  The models below are
+// the ones of samples/brunel.cpp:23-70, with the Poisson rate as a member.  Tests use the
+// output to pin the CPU restatement (oracle/spice_oracle.c) and the GPU engine to the
+// reference; bench.py may time it as the CPU baseline where it was built.
+//
+// usage:
+//   ref_driver net  SPEC OUT     run the network described in SPEC, write results to OUT
+//   ref_driver gen  SRC DST P SEED OUT    one fixed_probability CSR (seed_seq{SEED})
+//   ref_driver rng  SEED N OUT   seed chain and xoroshiro128+ draws of seed_seq{SEED}
+//   ref_driver bcsr N P SEED     checksums of the six Brunel CSRs, seeded as snn seeds them:
+//                                seed_seq{SEED}, one seed per stateful population (E, I), then
+//                                one per connection (snn.h:21-48, neuron_population.h:56-60)
+//
+// SPEC (text):  dt max_delay seed steps dump_csr
+//               pop poisson SIZE RATE | pop lif SIZE
+//               conn SRC DST P DELAY WEIGHT        (fixed_probability + fixed_weight)
+//               adj SRC DST DELAY WEIGHT M s0 d0 s1 d1 ...   (adj_list + fixed_weight)
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+#include "spice/snn.h"
+
+using namespace spice;
+
+struct poisson {
+	float rate = 20;
+	bool update(float dt, auto& rng) const { return util::generate_canonical<float>(rng) < (rate * dt); }
+};
+
+struct lif {
+	struct neuron {
+		float V   = 0;
+		int Twait = 0;
+	};
+	bool update(neuron& n, float dt, auto) const {
+		float const TmemInv = 1.0 / 0.02;
+		float const Vrest   = 0.0;
+		int const Tref      = 20;
+		float const Vthres  = 0.02;
+		if (--n.Twait <= 0) {
+			if (n.V > Vthres) {
+				n.V     = Vrest;
+				n.Twait = Tref;
+				return true;
+			}
+			n.V += (Vrest - n.V) * (dt * TmemInv);
+		}
+		return false;
+	}
+};
+
+struct fixed_weight {
+	float weight;
+	void deliver(lif::neuron& to) const { to.V += weight; }
+};
+
+std::vector<float> g_dt;
+struct dt_probe {
+	bool update(float dt, auto&) const {
+		g_dt.push_back(dt);
+		return false;
+	}
+};
+
+template <class T>
+static void put(FILE* f, T const& v) { fwrite(&v, sizeof(T), 1, f); }
+
+static int run_gen(int argc, char** argv) {
+	if (argc < 7) return 2;
+	Int src = atoll(argv[2]), dst = atoll(argv[3]);
+	double p = atof(argv[4]);
+	unsigned seed = (unsigned)atoll(argv[5]);
+	fixed_probability fp(p);
+	fp(src, dst);
+	std::vector<Int> off(src + 1);
+	std::vector<Int32> nb(fp.size());
+	fp.generate(off, nb, util::seed_seq{seed});
+	FILE* f = fopen(argv[6], "wb");
+	Int md = src > 0 ? fp.size() / src : 0;
+	put(f, md);
+	put(f, off[src]);
+	fwrite(off.data(), sizeof(Int), off.size(), f);
+	fwrite(nb.data(), sizeof(Int32), off[src], f);
+	fclose(f);
+	return 0;
+}
+
+// Order-sensitive checksum of a CSR with wrapping 64-bit arithmetic (the same function as
+// oracle.csr_checksum in oracle/oracle.py).
+static UInt csr_checksum(std::vector<Int> const& off, std::vector<Int32> const& nb, Int n) {
+	UInt h1 = 0, h2 = 0;
+	for (size_t i = 0; i < off.size(); i++)
+		h1 += (UInt(off[i]) + 1) * ((UInt(i) * 0x9E3779B97F4A7C15ull + 0x632BE59BD9B4E019ull) | 1);
+	for (Int j = 0; j < n; j++)
+		h2 += (UInt(UInt32(nb[j])) + 1) * ((UInt(j) * 0xD1B54A32D192ED03ull + 0x8CB92BA72F3D8DD7ull) | 1);
+	return h1 ^ ((h2 << 1) | (h2 >> 63));
+}
+
+static int run_bcsr(int argc, char** argv) {
+	if (argc < 5) return 2;
+	Int const N = atoll(argv[2]);
+	double const p = atof(argv[3]);
+	unsigned const seed = (unsigned)atoll(argv[4]);
+	util::seed_seq s{seed};
+	s++;  // E (stateful)
+	s++;  // I (stateful)
+	Int const sz[3] = {N / 2, N * 4 / 10, N / 10};
+	int const pr[6][2] = {{0, 1}, {0, 2}, {1, 1}, {1, 2}, {2, 1}, {2, 2}};
+	for (auto& q : pr) {
+		fixed_probability fp(p);
+		fp(sz[q[0]], sz[q[1]]);
+		std::vector<Int> off(sz[q[0]] + 1);
+		std::vector<Int32> nb(fp.size());
+		fp.generate(off, nb, s++);
+		printf("%d %d %lld %llu\n", q[0], q[1], (long long)off.back(),
+		       (unsigned long long)csr_checksum(off, nb, off.back()));
+	}
+	return 0;
+}
+
+static int run_rng(int argc, char** argv) {
+	if (argc < 5) return 2;
+	unsigned seed = (unsigned)atoll(argv[2]);
+	Int n = atoll(argv[3]);
+	util::seed_seq s{seed};
+	FILE* f = fopen(argv[4], "wb");
+	for (Int i = 0; i < n; i++) {  // seed chain
+		UInt128 v = s++.seed();
+		put(f, v.lo);
+		put(f, v.hi);
+	}
+	util::xoroshiro64_128p rng(util::seed_seq{seed});
+	for (Int i = 0; i < n; i++) put(f, rng());
+	util::xoroshiro64_128p rng2(util::seed_seq{seed});
+	util::exponential_distribution<double> ex(499.0);
+	for (Int i = 0; i < n; i++) put(f, ex(rng2));
+	util::xoroshiro64_128p rng3(util::seed_seq{seed});
+	for (Int i = 0; i < n; i++) put(f, util::generate_canonical<float>(rng3));
+	util::kahan_sum<float> k;
+	for (Int i = 0; i < n; i++) {
+		float y = k += 1e-4f;
+		if (k >= 1) k.reset();
+		put(f, y);
+	}
+	fclose(f);
+	return 0;
+}
+
+struct pop_rec {
+	bool is_lif;
+	Int size;
+	detail::NeuronPopulation* base;
+	detail::neuron_population<lif>* L;
+};
+
+static int run_net(int argc, char** argv) {
+	if (argc < 4) return 2;
+	std::ifstream in(argv[2]);
+	float dt, max_delay;
+	unsigned seed;
+	Int steps;
+	int dump_csr;
+	in >> dt >> max_delay >> seed >> steps >> dump_csr;
+	auto t0 = std::chrono::steady_clock::now();
+	snn net(dt, max_delay, {seed});
+	std::vector<pop_rec> pops;
+	std::string kw;
+	while (in >> kw) {
+		if (kw == "pop") {
+			std::string kind;
+			Int size;
+			in >> kind >> size;
+			if (kind == "poisson") {
+				float rate;
+				in >> rate;
+				auto* P = net.add_population<poisson>(size, {rate});
+				pops.push_back({false, size, P, nullptr});
+			} else {
+				auto* L = net.add_population<lif>(size);
+				pops.push_back({true, size, L, L});
+			}
+		} else if (kw == "conn" || kw == "adj") {
+			Int s, d;
+			in >> s >> d;
+			double p = 0;
+			if (kw == "conn") in >> p;
+			float delay, w;
+			in >> delay >> w;
+			auto* L = pops[d].L;
+			if (kw == "conn") {
+				if (pops[s].is_lif)
+					net.connect<fixed_weight>(pops[s].L, L, fixed_probability(p), delay, {w});
+				else
+					net.connect<fixed_weight>(static_cast<detail::neuron_population<poisson>*>(pops[s].base), L,
+					                             fixed_probability(p), delay, {w});
+			} else {
+				Int m;
+				in >> m;
+				adj_list adj;
+				for (Int i = 0; i < m; i++) {
+					Int a, b;
+					in >> a >> b;
+					adj.connect(a, b);
+				}
+				if (pops[s].is_lif)
+					net.connect<fixed_weight>(pops[s].L, L, adj, delay, {w});
+				else
+					net.connect<fixed_weight>(static_cast<detail::neuron_population<poisson>*>(pops[s].base), L, adj,
+					                             delay, {w});
+			}
+		}
+	}
+	net.add_population<dt_probe>(1);  // stateless: consumes no seed and no draw
+	auto t1 = std::chrono::steady_clock::now();
+	FILE* f = fopen(argv[3], "wb");
+	put(f, (Int)pops.size());
+	for (auto& p : pops) put(f, p.size);
+	put(f, steps);
+	std::vector<std::vector<std::vector<Int32>>> raster(steps);
+	for (Int t = 0; t < steps; t++) {
+		net.step();
+		raster[t].resize(pops.size());
+		for (size_t k = 0; k < pops.size(); k++) {
+			auto sp = pops[k].base->spikes(0);
+			raster[t][k].assign(sp.begin(), sp.end());
+		}
+	}
+	auto t2 = std::chrono::steady_clock::now();
+	fwrite(g_dt.data(), sizeof(float), g_dt.size(), f);
+	for (Int t = 0; t < steps; t++)
+		for (size_t k = 0; k < pops.size(); k++) {
+			put(f, (Int)raster[t][k].size());
+			fwrite(raster[t][k].data(), sizeof(Int32), raster[t][k].size(), f);
+		}
+	for (auto& p : pops)
+		if (p.is_lif)
+			for (auto& n : p.L->get_neurons()) {
+				put(f, n.V);
+				put(f, (Int32)n.Twait);
+			}
+	put(f, std::chrono::duration<double>(t1 - t0).count());
+	put(f, std::chrono::duration<double>(t2 - t1).count());
+	fclose(f);
+	(void)dump_csr;  // reserved
+	return 0;
+}
+
+int main(int argc, char** argv) {
+	if (argc < 2) return 2;
+	try {
+		if (!strcmp(argv[1], "net")) return run_net(argc, argv);
+		if (!strcmp(argv[1], "gen")) return run_gen(argc, argv);
+		if (!strcmp(argv[1], "rng")) return run_rng(argc, argv);
+		if (!strcmp(argv[1], "bcsr")) return run_bcsr(argc, argv);
+	} catch (std::exception const& e) {
+		fprintf(stderr, "%s\n", e.what());
+		return 3;
+	}
+	return 2;
+}

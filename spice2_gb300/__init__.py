@@ -1,0 +1,407 @@
+"""spice2_gb300 -- the GB300-native snn::step engine, driven from Python.
+
+This mirrors the reference's user API (spice/include/spice/snn.h and the sample models of
+samples/brunel.cpp, samples/vogels.cpp, samples/external_input.cpp) over the C ABI declared in
+include/spice_gb300.h:
+
+    from spice2_gb300 import snn, poisson, lif, fixed_weight, fixed_probability
+    brunel = snn(1e-4, 15e-4, [1337])                       # snn(dt, max_delay, seed)
+    P = brunel.add_population(poisson(20), N // 2)           # add_population<poisson>(N/2)
+    E = brunel.add_population(lif(), N * 4 // 10)
+    brunel.connect(P, E, fixed_probability(0.1), 15e-4, fixed_weight(2 / N))
+    brunel.step()                                            # snn::step()
+    P.spikes(0)                                              # NeuronPopulation::spikes(age)
+
+Every call runs on the GPU through libspice_gb300.so.  There is no CPU fallback: importing the
+package fails loudly when the library has not been built (``python -m spice2_gb300.build``).
+Failed preconditions raise LogicError with the reference's message
+("Assertion failed (file:line): cond", spice/src/util/assert.cpp:8-15).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field as dc_field
+from typing import Iterable, Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libspice_gb300.so")
+
+OK, EINVAL, ECUDA, ENOMEM, ESTATE, EOVERFLOW = 0, 1, 2, 3, 4, 5
+NEURON_POISSON, NEURON_LIF, NEURON_LIF_COND, NEURON_EXTERNAL = 0, 1, 2, 3
+SYNAPSE_FIXED_WEIGHT = 0
+MODE_DETERMINISTIC, MODE_ATOMIC = 0, 1
+FIELD_V, FIELD_GEX, FIELD_GIN, FIELD_TREF = 0, 1, 2, 3
+
+
+class SpiceError(RuntimeError):
+    """A failed call into libspice_gb300; .code is the SPICE_E* status."""
+
+    def __init__(self, code: int, msg: str):
+        super().__init__(msg)
+        self.code = code
+
+
+class LogicError(SpiceError, ValueError):
+    """A violated precondition -- the reference throws std::logic_error for these."""
+
+
+class CudaError(SpiceError):
+    pass
+
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(
+            f"{LIB_PATH} is missing: build the CUDA engine first (python -m spice2_gb300.build); "
+            "spice2_gb300 has no CPU fallback")
+    L = C.CDLL(LIB_PATH)
+    vp, i32, i64, u32, f32, f64 = C.c_void_p, C.c_int, C.c_int64, C.c_uint32, C.c_float, C.c_double
+    P = C.POINTER
+    sig = {
+        "spice_net_create": [f32, f32, P(u32), i32, P(vp)],
+        "spice_net_destroy": [vp],
+        "spice_add_population": [vp, i32, i64, P(f32), i32, P(i32)],
+        "spice_connect_fixed_probability": [vp, i32, i32, f64, f32, i32, P(f32), i32, P(i32)],
+        "spice_connect_adj_list": [vp, i32, i32, vp, i64, f32, i32, P(f32), i32, P(i32)],
+        "spice_set_external_input": [vp, i32, i32, vp, vp],
+        "spice_set_mode": [vp, i32],
+        "spice_set_window": [vp, i32],
+        "spice_step": [vp],
+        "spice_run": [vp, i64],
+        "spice_run_record": [vp, i64, vp, vp, i64, P(i64)],
+        "spice_spike_count": [vp, i32, i64, P(i64)],
+        "spice_spikes": [vp, i32, i64, vp, i64, P(i64)],
+        "spice_get_state": [vp, i32, i32, vp],
+        "spice_set_state": [vp, i32, i32, vp],
+        "spice_pop_size": [vp, i32, P(i64)],
+        "spice_time": [vp, P(i64)],
+        "spice_events": [vp, P(C.c_uint64)],
+        "spice_conn_size": [vp, i32, P(i64), P(i64)],
+        "spice_get_csr": [vp, i32, vp, vp],
+        "spice_set_profiling": [vp, i32],
+        "spice_kernel_stats": [vp, i32, P(i64), P(f64)],
+        "spice_launch_count": [vp, P(i64)],
+        "spice_synchronize": [vp],
+    }
+    for name, args in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = C.c_int
+    L.spice_last_error.argtypes = []
+    L.spice_last_error.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def lib():
+    return _load()
+
+
+def _check(rc: int):
+    if rc == OK:
+        return
+    msg = (_load().spice_last_error() or b"").decode()
+    if rc == EINVAL:
+        raise LogicError(rc, msg)
+    if rc == ECUDA:
+        raise CudaError(rc, msg)
+    raise SpiceError(rc, msg)
+
+
+# ---- models ---------------------------------------------------------------------------------
+@dataclass(frozen=True)
+class poisson:
+    """Stateless Poisson source: fires when canonical<float>(rng) < rate*dt (samples/brunel.cpp:23-31)."""
+    rate: float = 20.0
+    model = NEURON_POISSON
+
+    def params(self):
+        return [self.rate]
+
+
+@dataclass(frozen=True)
+class lif:
+    """Brunel LIF {V, Tref} (samples/brunel.cpp:39-62)."""
+    Vthres: float = 0.02
+    Tref: int = 20
+    TmemInv: float = 50.0
+    model = NEURON_LIF
+
+    def params(self):
+        return [self.Vthres, float(self.Tref), self.TmemInv]
+
+
+@dataclass(frozen=True)
+class lif_cond:
+    """Conductance LIF {V, Gex, Gin, Tref} with the constants of samples/vogels.cpp:10-46."""
+    model = NEURON_LIF_COND
+
+    def params(self):
+        return []
+
+
+@dataclass(frozen=True)
+class external_input:
+    """Per-population update replaying a cyclic spike train (samples/external_input.cpp:17-30)."""
+    trains: tuple = ()
+    model = NEURON_EXTERNAL
+
+    def params(self):
+        return []
+
+
+@dataclass(frozen=True)
+class fixed_weight:
+    """Adds `weight` to a target state field on every spike (samples/brunel.cpp:67-70)."""
+    weight: float
+    field: int = FIELD_V
+
+    def params(self):
+        return [self.weight, float(self.field)]
+
+
+def excitatory(weight: float) -> fixed_weight:
+    """samples/vogels.cpp:48-53: to.Gex += weight."""
+    return fixed_weight(weight, FIELD_GEX)
+
+
+def inhibitory(weight: float) -> fixed_weight:
+    """samples/vogels.cpp:55-60: to.Gin += weight."""
+    return fixed_weight(weight, FIELD_GIN)
+
+
+# ---- topologies -----------------------------------------------------------------------------
+@dataclass(frozen=True)
+class fixed_probability:
+    """fixed_probability(p) (spice/include/spice/topology.h:48-58)."""
+    p: float
+
+
+@dataclass
+class adj_list:
+    """adj_list (spice/include/spice/topology.h:37-46): connect(src, dst) edge by edge."""
+    edges: list = dc_field(default_factory=list)
+
+    def connect(self, src: int, dst: int):
+        self.edges.append((int(src), int(dst)))
+
+    def size(self) -> int:
+        return len(self.edges)
+
+
+# ---- network --------------------------------------------------------------------------------
+class Population:
+    """Handle returned by snn.add_population (the neuron_population<Neur>* of snn.h:21-27)."""
+
+    def __init__(self, net: "snn", idx: int, model):
+        self._net = net
+        self.id = idx
+        self.model = model
+
+    def size(self) -> int:
+        v = C.c_int64()
+        _check(lib().spice_pop_size(self._net._h, self.id, C.byref(v)))
+        return v.value
+
+    def spikes(self, age: int = 0) -> np.ndarray:
+        return self._net.spikes(self, age)
+
+    def get_neurons(self) -> dict:
+        """State of a stateful population as SoA numpy arrays (neuron_population.h:139-145)."""
+        fields = {"V": FIELD_V, "Tref": FIELD_TREF}
+        if self.model.model == NEURON_LIF_COND:
+            fields.update({"Gex": FIELD_GEX, "Gin": FIELD_GIN})
+        return {k: self._net.get_state(self, f) for k, f in fields.items()}
+
+    def __repr__(self):
+        return f"Population({self.id}, {self.model})"
+
+
+class snn:
+    """snn(dt, max_delay, seed) -- spice/include/spice/snn.h:16-75, running on the GPU."""
+
+    def __init__(self, dt: float, max_delay: float, seed: Sequence[int] | int):
+        seeds = [int(seed)] if isinstance(seed, (int, np.integer)) else [int(s) for s in seed]
+        arr = (C.c_uint32 * max(1, len(seeds)))(*seeds)
+        h = C.c_void_p()
+        _check(lib().spice_net_create(dt, max_delay, arr, len(seeds), C.byref(h)))
+        self._h = h
+        self._pops: list[Population] = []
+        self._conns: list[tuple] = []
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().spice_net_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # construction
+    def add_population(self, model, size: int) -> Population:
+        prm = model.params()
+        arr = (C.c_float * max(1, len(prm)))(*prm)
+        out = C.c_int()
+        _check(lib().spice_add_population(self._h, model.model, int(size), arr, len(prm), C.byref(out)))
+        pop = Population(self, out.value, model)
+        self._pops.append(pop)
+        if model.model == NEURON_EXTERNAL and model.trains:
+            self.set_external_input(pop, model.trains)
+        return pop
+
+    def set_external_input(self, pop: Population, trains: Iterable[Iterable[int]]):
+        trains = [np.asarray(list(t), dtype=np.int32) for t in trains]
+        counts = np.array([len(t) for t in trains], dtype=np.int32)
+        idx = np.concatenate(trains + [np.zeros(0, np.int32)]).astype(np.int32)
+        _check(lib().spice_set_external_input(self._h, pop.id, len(trains), counts.ctypes.data, idx.ctypes.data))
+
+    def connect(self, source: Population, target: Population, topology, delay: float, syn) -> int:
+        prm = syn.params()
+        arr = (C.c_float * len(prm))(*prm)
+        out = C.c_int()
+        if isinstance(topology, fixed_probability):
+            _check(lib().spice_connect_fixed_probability(self._h, source.id, target.id, float(topology.p),
+                                                         delay, SYNAPSE_FIXED_WEIGHT, arr, len(prm), C.byref(out)))
+        elif isinstance(topology, adj_list):
+            pairs = np.ascontiguousarray(np.asarray(topology.edges, dtype=np.int32).reshape(-1, 2))
+            _check(lib().spice_connect_adj_list(self._h, source.id, target.id, pairs.ctypes.data, len(pairs),
+                                                delay, SYNAPSE_FIXED_WEIGHT, arr, len(prm), C.byref(out)))
+        else:
+            raise TypeError("topology must be fixed_probability or adj_list")
+        self._conns.append((source, target, topology, delay, syn))
+        return out.value
+
+    def set_mode(self, mode: int):
+        _check(lib().spice_set_mode(self._h, mode))
+
+    def set_window(self, w: int):
+        _check(lib().spice_set_window(self._h, w))
+
+    # stepping
+    def step(self):
+        _check(lib().spice_step(self._h))
+
+    def run(self, steps: int):
+        _check(lib().spice_run(self._h, int(steps)))
+
+    def run_record(self, steps: int, capacity: int | None = None):
+        """Runs `steps` steps and returns the raster: list over steps of lists over populations."""
+        npop = len(self._pops)
+        counts = np.zeros((max(1, steps), max(1, npop)), dtype=np.int64)
+        if capacity is None:
+            capacity = max(1024, steps * sum(p.size() for p in self._pops) // 50)
+        while True:
+            buf = np.zeros(max(1, capacity), dtype=np.int32)
+            total = C.c_int64()
+            rc = lib().spice_run_record(self._h, int(steps), counts.ctypes.data, buf.ctypes.data, capacity,
+                                        C.byref(total))
+            if rc == EOVERFLOW:
+                # the steps ran; the raster did not fit -- the caller asked for too little room
+                raise SpiceError(rc, f"raster needs {total.value} entries (capacity {capacity})")
+            _check(rc)
+            break
+        out, pos = [], 0
+        for t in range(steps):
+            row = []
+            for k in range(npop):
+                c = int(counts[t, k])
+                row.append(buf[pos:pos + c].copy())
+                pos += c
+            out.append(row)
+        return out
+
+    @property
+    def time(self) -> int:
+        v = C.c_int64()
+        _check(lib().spice_time(self._h, C.byref(v)))
+        return v.value
+
+    @property
+    def events(self) -> int:
+        v = C.c_uint64()
+        _check(lib().spice_events(self._h, C.byref(v)))
+        return v.value
+
+    # readback
+    def spikes(self, pop: Population | int, age: int = 0) -> np.ndarray:
+        pid = pop.id if isinstance(pop, Population) else int(pop)
+        n = C.c_int64()
+        _check(lib().spice_spike_count(self._h, pid, int(age), C.byref(n)))
+        out = np.zeros(max(1, n.value), dtype=np.int32)
+        _check(lib().spice_spikes(self._h, pid, int(age), out.ctypes.data, len(out), C.byref(n)))
+        return out[:n.value]
+
+    def get_state(self, pop: Population, fld: int) -> np.ndarray:
+        out = np.zeros(pop.size(), dtype=np.int32 if fld == FIELD_TREF else np.float32)
+        _check(lib().spice_get_state(self._h, pop.id, fld, out.ctypes.data))
+        return out
+
+    def set_state(self, pop: Population, fld: int, values):
+        v = np.ascontiguousarray(values, dtype=np.int32 if fld == FIELD_TREF else np.float32)
+        if v.size != pop.size():
+            raise LogicError(EINVAL, "state array must have one entry per neuron")
+        _check(lib().spice_set_state(self._h, pop.id, fld, v.ctypes.data))
+
+    def csr(self, conn: int):
+        src, syn = C.c_int64(), C.c_int64()
+        _check(lib().spice_conn_size(self._h, conn, C.byref(src), C.byref(syn)))
+        off = np.zeros(src.value + 1, dtype=np.int64)
+        nb = np.zeros(max(1, syn.value), dtype=np.int32)
+        _check(lib().spice_get_csr(self._h, conn, off.ctypes.data, nb.ctypes.data))
+        return off, nb[:syn.value]
+
+    # profiling
+    def set_profiling(self, on: bool):
+        _check(lib().spice_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_stats(self, kind: int):
+        n, ms = C.c_int64(), C.c_double()
+        _check(lib().spice_kernel_stats(self._h, kind, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        _check(lib().spice_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def synchronize(self):
+        _check(lib().spice_synchronize(self._h))
+
+
+def brunel(N: int, p: float, seed: int = 1337, dt: float = 1e-4, delay: float = 15e-4, mode: int = MODE_DETERMINISTIC):
+    """The Brunel network of samples/brunel.cpp:75-103 (P = N/2 Poisson, E = 0.4 N and I = 0.1 N
+    LIF, six fixed_probability(p) projections) with weights scaled by 0.1/p so the mean input is
+    the same at any p.  Returns (net, (P, E, I))."""
+    net = snn(dt, delay, [seed])
+    net.set_mode(mode)
+    P = net.add_population(poisson(20.0), N // 2)
+    E = net.add_population(lif(), N * 4 // 10)
+    I = net.add_population(lif(), N // 10)
+    we = float(np.float32((2.0 / N) * (0.1 / p)))
+    wi = float(np.float32((-10.0 / N) * (0.1 / p)))
+    for s, d, w in ((P, E, we), (P, I, we), (E, E, we), (E, I, we), (I, E, wi), (I, I, wi)):
+        net.connect(s, d, fixed_probability(p), delay, fixed_weight(w))
+    return net, (P, E, I)
+
+
+__all__ = ["snn", "Population", "poisson", "lif", "lif_cond", "external_input", "fixed_weight", "excitatory",
+           "inhibitory", "fixed_probability", "adj_list", "brunel", "SpiceError", "LogicError", "CudaError",
+           "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib"]

@@ -1,0 +1,161 @@
+// internal.h -- engine data structures shared by the host runtime (net.cu) and the kernels.
+//
+// Device memory layout of one net (all SoA, one CUDA allocation per array):
+//   population p:  state fields V/Gex/Gin (f32[N]) and Tref (i32[N]);
+//                  spike bitmap ring   bits[Hb][ceil(N/32)]  (ascending order = bit order);
+//                  spike list ring     list[K][N] int32 (unordered, consumed by delivery);
+//                  input ring          deterministic: cnt[D][N][W] u32 packed per-group counts
+//                                      atomic:        acc[D][N][F] f32 per-field sums.
+//   connection c:  CSR offsets i64[src+1], neighbors i32[synapses].
+//   per run:       dt[t] (Kahan-compensated), per-step xoroshiro state basis T^i(s_t), i < 128.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "rng.h"
+
+namespace spice_gb300 {
+
+constexpr int kMaxPops    = 64;
+constexpr int kMaxConns   = 256;
+constexpr int kMaxGroups  = 8;   // distinct consecutive (field, weight) runs per target population
+constexpr int kMaxWindow  = 64;  // steps fused into one neuron-update launch
+constexpr int kBasis      = 128; // states per step basis
+constexpr int kPoissonChunk = 32; // consecutive Poisson neurons per thread (one jump each)
+
+enum Model { POISSON = 0, LIF = 1, LIF_COND = 2, EXTERNAL = 3 };
+
+struct Group {
+	int field;     // 0 V, 1 Gex, 2 Gin
+	float weight;  // the fixed_weight of every connection in the group
+};
+
+// Device-side view of one population, passed by value to kernels.
+struct PopDev {
+	int model;
+	int nwords;          // ceil(N / 32)
+	int64_t size;
+	int64_t draw_offset; // first draw of this population in each step's stream
+	float* V;
+	float* Gex;
+	float* Gin;
+	int32_t* T;
+	float p0, p1, p2;    // model parameters (POISSON: rate; LIF: Vthres, Tref, TmemInv)
+	uint32_t* bits;      // [Hb][nwords]
+	int32_t* list;       // [K][size]
+	// input ring
+	uint32_t* cnt;       // deterministic: [D][size][W]
+	float* acc;          // atomic:        [D][size][F]
+	int W;               // u32 words per neuron and slot (deterministic)
+	int F;               // fields per neuron and slot (atomic)
+	int ngroups;
+	int group_shift[kMaxGroups];  // bit offset of the group's counter in its word (0 or 16)
+	int group_word[kMaxGroups];
+	int group_bits[kMaxGroups];   // 16 or 32
+	int group_field[kMaxGroups];
+	float group_weight[kMaxGroups];
+	int field_slot[3];   // atomic mode: index of field f in the F per-neuron sums (-1: unused)
+	const u128* chunk_poly;  // POISSON: x^(draw_offset + 32 c) mod P for chunk c
+	// EXTERNAL: cyclic train
+	const int32_t* ext_counts;
+	const int64_t* ext_off;
+	const int32_t* ext_idx;
+	int ext_steps;
+};
+
+struct ConnDev {
+	int src, dst;
+	int delay;
+	int group;
+	float weight;
+	int field;
+	int64_t src_size;
+	int64_t dst_size;
+	const int64_t* off;
+	const int32_t* nb;
+	const int32_t* src_list;  // [K][src_size] spike lists of the source population
+	uint32_t* dst_cnt;        // deterministic input ring of the target: [D][dst_size][W]
+	float* dst_acc;           // atomic input ring of the target: [D][dst_size][F]
+	int W, word;              // words per neuron, word of this connection's group
+	uint32_t inc;             // 1 << group_shift
+	int F, fslot;             // atomic: sums per neuron, index of this connection's field
+};
+
+struct Pop {
+	PopDev d;
+	int64_t ext_pos0 = 0;  // train position at time 0
+	std::vector<int32_t> ext_counts_h;
+	std::vector<int64_t> ext_off_h;
+	bool stateful = false;
+};
+
+struct Conn {
+	ConnDev d;
+	int64_t synapses = 0;
+	bool adj         = false;
+};
+
+struct PendingGen {  // a fixed_probability connection whose adjacency is not generated yet
+	int conn;
+	u128 seed;
+	double p;
+};
+
+struct KernelStat {
+	int64_t launches = 0;
+	double ms        = 0;
+};
+
+}  // namespace spice_gb300
+
+struct spice_net {
+	float dt;
+	int64_t max_delay;   // D, in steps
+	int64_t time = 0;
+	spice_gb300::u128 seed;
+	float kahan_c = 0, kahan_sum = 0;
+	int mode      = 0;
+	int max_window = 0;  // 0 = auto
+	bool prepared  = false;
+	int device     = 0;
+	cudaStream_t stream = nullptr;
+	std::vector<spice_gb300::Pop> pops;
+	std::vector<spice_gb300::Conn> conns;
+	int K  = 1;          // window length used by run
+	int Hb = 1;          // bitmap ring length
+	int64_t total_draws = 0;  // draws per step over all populations
+	// device-wide buffers
+	unsigned long long* d_events = nullptr;
+	int32_t* d_counts  = nullptr;  // [K][npop] spikes per window step and population
+	float* d_dt        = nullptr;  // [run capacity]
+	spice_gb300::u128* d_seeds = nullptr;  // [run capacity]
+	spice_gb300::u128* d_basis = nullptr;  // [run capacity][128]
+	int64_t run_cap    = 0;
+	spice_gb300::PopDev* d_pops   = nullptr;
+	spice_gb300::ConnDev* d_conns = nullptr;
+	// host staging
+	float* h_dt        = nullptr;
+	spice_gb300::u128* h_seeds = nullptr;
+	// raster extraction
+	int32_t* d_raster  = nullptr;
+	int64_t raster_cap = 0;
+	int64_t* d_raster_tab = nullptr;  // [steps][npop][2] (offset, count)
+	unsigned long long* d_raster_cursor = nullptr;
+	int32_t* d_tmp     = nullptr;  // spikes(age) extraction
+	int64_t* d_tmp_n   = nullptr;
+	// profiling
+	bool profiling = false;
+	std::vector<cudaEvent_t> ev_pool;
+	std::vector<std::pair<int, int>> ev_pending;  // (kind, event index of the start)
+	size_t ev_used = 0;
+	spice_gb300::KernelStat stats[3];
+	int64_t launches = 0;
+	std::vector<void*> allocations;
+	std::vector<spice_gb300::PendingGen> gen_pending;
+	std::vector<int64_t> ext_t_set;  // per population: step at which its external train was set
+	int parity = 0;                  // which half of d_counts the next window writes
+};

@@ -1,0 +1,99 @@
+// kernels.h -- launch wrappers of the engine's CUDA kernels (gen.cu, step.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <vector>
+
+#include "internal.h"
+
+namespace spice_gb300 {
+
+// ---- gen.cu ----
+struct GenRequest {
+	int64_t src, dst;
+	double p;
+	u128 seed;
+	int64_t* offsets;   // out (device), src + 1
+	int32_t* neighbors; // out (device)
+	int64_t synapses;   // out
+};
+int64_t fp_max_degree(int64_t dst_count, double p);
+// Generates all requested projections (rows of every projection are chained concurrently).
+cudaError_t generate_fixed_probability(cudaStream_t stream, std::vector<GenRequest>& reqs);
+// Rows whose stop index was recomputed with the exact sequential loop (near-tie sums), process-wide.
+extern unsigned long long g_gen_fallbacks;
+
+// ---- step.cu ----
+// Exclusive scan of n int32 row lengths into n + 1 int64 offsets.
+cudaError_t scan_row_lengths(cudaStream_t stream, const int32_t* lens, int64_t n, int64_t* offsets);
+
+// Maximum in-degree of target population neurons over the connections of one input group.
+cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const int64_t* nsyn, int nconn,
+                         int64_t dst_size, uint32_t* scratch, uint32_t* max_out);
+
+// basis[t][i] = T^i(seed_t) for t < nsteps.
+cudaError_t launch_basis(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* basis);
+
+struct WindowArgs {
+	int64_t t0;        // absolute step of the window's first step
+	int K;             // steps in this window
+	int slot0;         // (t0 - 1) mod D: input slot applied before the update of step t0
+	int hslot0;        // t0 mod Hb: bitmap slot of step t0
+	int64_t D;         // input ring length (max delay)
+	int Hb;            // bitmap ring length
+	int npop;
+	int mode;
+	const PopDev* pops;
+	const float* dts;     // dt of steps t0 .. t0+K-1
+	const u128* basis;    // basis of step t0 (then t0+1, ...)
+	int32_t* counts;      // [K][npop] spikes per step and population (window parity buffer)
+	int blk_begin[kMaxPops + 1];
+	int blk_kind[kMaxPops];      // 0: per-neuron window CTAs, 1: Poisson step CTAs, 2: external
+	int blk_per_step[kMaxPops];  // Poisson / external: CTAs per step
+	int64_t ext_pos[kMaxPops];   // external: train position of step t0
+};
+cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks);
+
+struct DeliverArgs {
+	int64_t t0;
+	int K;
+	int64_t D;
+	int nconn;
+	int npop;
+	int mode;
+	const ConnDev* conns;
+	const PopDev* pops;
+	const int32_t* counts;   // [K][npop] of this window
+	int32_t* counts_next;    // the other parity buffer, zeroed here
+	int counts_next_len;
+	unsigned long long* events;
+};
+cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int nblocks);
+
+// Applies the inputs waiting in ring slot (t - 1) to the state and clears them.
+cudaError_t launch_apply_pending(cudaStream_t stream, const PopDev* pops, int npop_dev, const int* stateful,
+                                 int nstateful, std::vector<PopDev> const& hpops, int64_t t, int64_t D,
+                                 int mode);
+
+// Ascending indices of the set bits of one bitmap step: out[0..n), *n_out.
+cudaError_t launch_extract(cudaStream_t stream, const uint32_t* bits, int nwords, int32_t* out, int64_t* n_out);
+
+// Raster of a window: for k < K and population p, the ascending spikes of step t0 + k are
+// written at an offset taken from *cursor; tab[(row0 + k) * npop + p] = {offset, count}.
+struct RasterArgs {
+	int64_t t0;
+	int K;
+	int Hb;
+	int npop;
+	const PopDev* pops;
+	int32_t* out;
+	int64_t capacity;
+	unsigned long long* cursor;
+	int64_t* tab;
+	int64_t row0;
+};
+cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a);
+
+}  // namespace spice_gb300

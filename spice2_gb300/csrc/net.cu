@@ -1,0 +1,901 @@
+// net.cu -- the C ABI (include/spice_gb300.h): network construction, the step loop, readback.
+//
+// Host-side order of the reference is kept exactly: seeds are consumed in the order of
+// snn::add_population (stateful populations, neuron_population.h:56-60), snn::connect (one per
+// connection, synapse_population.h:30-31) and snn::step (one per step, snn.cpp:12); the per-step
+// dt is the Kahan-compensated increment (numeric.h:9-15, snn.cpp:8-10).  Construction is lazy:
+// the adjacency of every fixed_probability connection is generated on the GPU together, the first
+// time the network steps or a CSR is read.
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/spice_gb300.h"
+#include "internal.h"
+#include "kernels.h"
+
+using namespace spice_gb300;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, std::string msg) {
+	g_err = std::move(msg);
+	return code;
+}
+
+// The reference's precondition failure text (spice/src/util/assert.cpp:8-15).
+int pre_failed(const char* file_line, const char* cond) {
+	return fail(SPICE_EINVAL, std::string("Assertion failed (") + file_line + "): " + cond);
+}
+
+#define CUDA_TRY(x)                                                                                  \
+	do {                                                                                             \
+		cudaError_t const e_ = (x);                                                                  \
+		if (e_ != cudaSuccess) return fail(SPICE_ECUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+	} while (0)
+
+#define TRY(x)                    \
+	do {                          \
+		int const r_ = (x);       \
+		if (r_ != SPICE_OK) return r_; \
+	} while (0)
+
+constexpr int64_t kRunCap = 8192;  // steps of dt / seed / basis prepared per chunk
+
+template <class T>
+int dalloc(spice_net* n, T** p, size_t count, bool zero = true) {
+	size_t const bytes = sizeof(T) * (count > 0 ? count : 1);
+	cudaError_t e      = cudaMalloc((void**)p, bytes);
+	if (e != cudaSuccess) {
+		*p = nullptr;
+		return fail(e == cudaErrorMemoryAllocation ? SPICE_ENOMEM : SPICE_ECUDA,
+		            std::string("cudaMalloc(") + std::to_string(bytes) + " bytes): " + cudaGetErrorString(e));
+	}
+	n->allocations.push_back(*p);
+	if (zero) CUDA_TRY(cudaMemsetAsync(*p, 0, bytes, n->stream));
+	return SPICE_OK;
+}
+
+bool stateful_model(int m) { return m == LIF || m == LIF_COND; }
+
+u128 seed_next(spice_net* n) {  // seed_seq::operator++(int) (random.h:163-167)
+	u128 const r = n->seed;
+	n->seed      = murmur3_u128(n->seed);
+	return r;
+}
+
+float kahan_next(spice_net* n) {  // kahan_sum<float>::operator+= then the reset at >= 1 s
+	volatile float y = n->dt - n->kahan_c;
+	volatile float t = n->kahan_sum + y;
+	n->kahan_c       = (t - n->kahan_sum) - y;
+	n->kahan_sum     = t;
+	if (n->kahan_sum >= 1) n->kahan_sum = 0;
+	return y;
+}
+
+// ---- profiling ----
+int ev_begin(spice_net* n, int kind, int* slot) {
+	*slot = -1;
+	if (!n->profiling) return SPICE_OK;
+	if (n->ev_used + 2 > n->ev_pool.size()) {
+		// harvest: every recorded pair is complete once the stream is idle
+		CUDA_TRY(cudaStreamSynchronize(n->stream));
+		for (auto const& pr : n->ev_pending) {
+			float ms = 0;
+			CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
+			n->stats[pr.first].ms += ms;
+			n->stats[pr.first].launches++;
+		}
+		n->ev_pending.clear();
+		n->ev_used = 0;
+		while (n->ev_pool.size() < 4096) {
+			cudaEvent_t e;
+			CUDA_TRY(cudaEventCreate(&e));
+			n->ev_pool.push_back(e);
+		}
+	}
+	*slot = (int)n->ev_used;
+	n->ev_used += 2;
+	n->ev_pending.push_back({kind, *slot});
+	CUDA_TRY(cudaEventRecord(n->ev_pool[*slot], n->stream));
+	return SPICE_OK;
+}
+
+int ev_end(spice_net* n, int slot) {
+	if (slot >= 0) CUDA_TRY(cudaEventRecord(n->ev_pool[slot + 1], n->stream));
+	return SPICE_OK;
+}
+
+int harvest(spice_net* n) {
+	if (n->ev_pending.empty()) return SPICE_OK;
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	for (auto const& pr : n->ev_pending) {
+		float ms = 0;
+		CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
+		n->stats[pr.first].ms += ms;
+		n->stats[pr.first].launches++;
+	}
+	n->ev_pending.clear();
+	n->ev_used = 0;
+	return SPICE_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// construction
+// ------------------------------------------------------------------------------------------------
+
+extern "C" const char* spice_last_error(void) { return g_err.c_str(); }
+
+extern "C" int spice_net_create(float dt, float max_delay, const uint32_t* seeds, int nseeds, spice_net** out) {
+	if (!out) return fail(SPICE_EINVAL, "out must not be NULL");
+	*out = nullptr;
+	if (nseeds <= 0 || !seeds)
+		return pre_failed("random.h:153", "il.size() > 0 && \"Please provide at least 1 seed to seed_seq\"");
+	auto* n = new spice_net();
+	n->dt   = dt;
+	// _max_delay(std::round(max_delay / dt)) (snn.h:18-19)
+	n->max_delay = (int64_t)roundf(max_delay / dt);
+	n->seed      = murmur3_bytes(seeds, 4ull * (uint64_t)nseeds);
+	cudaError_t e = cudaGetDevice(&n->device);
+	if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&n->stream, cudaStreamNonBlocking);
+	if (e != cudaSuccess) {
+		delete n;
+		return fail(SPICE_ECUDA, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+	}
+	int r = dalloc(n, &n->d_events, 1);
+	if (r != SPICE_OK) {
+		spice_net_destroy(n);
+		return r;
+	}
+	*out = n;
+	return SPICE_OK;
+}
+
+extern "C" int spice_net_destroy(spice_net* n) {
+	if (!n) return SPICE_OK;
+	if (n->stream) cudaStreamSynchronize(n->stream);
+	for (void* p : n->allocations) cudaFree(p);
+	for (auto& c : n->conns) {
+		cudaFree((void*)c.d.off);
+		cudaFree((void*)c.d.nb);
+	}
+	if (n->h_dt) cudaFreeHost(n->h_dt);
+	if (n->h_seeds) cudaFreeHost(n->h_seeds);
+	for (auto e : n->ev_pool) cudaEventDestroy(e);
+	if (n->stream) cudaStreamDestroy(n->stream);
+	delete n;
+	return SPICE_OK;
+}
+
+extern "C" int spice_add_population(spice_net* n, int model, int64_t size, const float* params, int np,
+                                    int* pop_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (n->prepared) return fail(SPICE_ESTATE, "populations must be added before the network first steps");
+	if (model < POISSON || model > EXTERNAL) return fail(SPICE_EINVAL, "unknown neuron model");
+	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
+	if (!(n->max_delay >= 1)) return pre_failed("neuron_population.h:108", "max_delay >= 1");
+	if (size >= INT32_MAX) return pre_failed("topology.cpp:51", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
+	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
+	if (np < 0 || (np > 0 && !params)) return fail(SPICE_EINVAL, "bad params");
+	Pop p{};
+	PopDev& d = p.d;
+	memset(&d, 0, sizeof d);
+	d.model  = model;
+	d.size   = size;
+	d.nwords = (int)((size + 31) / 32);
+	for (int f = 0; f < 3; f++) d.field_slot[f] = -1;
+	if (model == POISSON) {
+		d.p0 = np > 0 ? params[0] : 20.0f;
+	} else if (model == LIF) {
+		d.p0 = np > 0 ? params[0] : 0.02f;
+		d.p1 = np > 1 ? params[1] : 20.0f;
+		d.p2 = np > 2 ? params[2] : 50.0f;
+	}
+	p.stateful = stateful_model(model);
+	if (p.stateful) {
+		seed_next(n);  // stateful_neuron_adapter: rng(seed++) (neuron_population.h:56-60)
+		TRY(dalloc(n, &d.V, size));
+		TRY(dalloc(n, &d.T, size));
+		if (model == LIF_COND) {
+			TRY(dalloc(n, &d.Gex, size));
+			TRY(dalloc(n, &d.Gin, size));
+			std::vector<float> v0(size, -0.06f);  // samples/vogels.cpp:12
+			CUDA_TRY(cudaMemcpyAsync(d.V, v0.data(), sizeof(float) * size, cudaMemcpyHostToDevice, n->stream));
+			CUDA_TRY(cudaStreamSynchronize(n->stream));
+		}
+	}
+	n->pops.push_back(std::move(p));
+	n->ext_t_set.push_back(0);
+	if (pop_out) *pop_out = (int)n->pops.size() - 1;
+	return SPICE_OK;
+}
+
+namespace {
+int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int np, float* w, int* field) {
+	if (synapse != SPICE_SYNAPSE_FIXED_WEIGHT) return fail(SPICE_EINVAL, "unknown synapse model");
+	if (np < 1 || !params) return fail(SPICE_EINVAL, "fixed_weight needs params {weight[, field]}");
+	*w     = params[0];
+	*field = np > 1 ? (int)params[1] : 0;
+	int const m = n->pops[dst].d.model;
+	if (*field < 0 || *field > 2 || (m == LIF && *field != 0))
+		return fail(SPICE_EINVAL, "the synapse's target field does not exist in the target neuron model");
+	return SPICE_OK;
+}
+
+int conn_common(spice_net* n, int src, int dst, float delay, int* d_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (n->prepared) return fail(SPICE_ESTATE, "connections must be added before the network first steps");
+	if (src < 0 || src >= (int)n->pops.size() || dst < 0 || dst >= (int)n->pops.size())
+		return fail(SPICE_EINVAL, "population id out of range");
+	if (!n->pops[dst].stateful)
+		return fail(SPICE_EINVAL, "the target population of a connection must be stateful (StatefulNeuron<DstNeur>, snn.h:29-31)");
+	if ((int)n->conns.size() >= kMaxConns) return fail(SPICE_EINVAL, "too many connections");
+	// Int const d = std::round(delay / _dt) (snn.h:33-38)
+	int64_t const d = (int64_t)roundf(delay / n->dt);
+	if (!(d >= 1)) return pre_failed("snn.h:35", "d >= 1 && \"The delay must be at least 1dt.\"");
+	if (!(d <= n->max_delay))
+		return pre_failed("snn.h:36", "d <= _max_delay && \"The delay of a synapse population may not exceed the maximum delay of the network.\"");
+	*d_out = (int)d;
+	return SPICE_OK;
+}
+}  // namespace
+
+extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, double p, float delay, int synapse,
+                                               const float* params, int np, int* conn_out) {
+	int d = 0;
+	TRY(conn_common(n, src, dst, delay, &d));
+	if (!(0 <= p && p <= 1)) return pre_failed("topology.cpp:79", "0 <= p && p <= 1");
+	float w   = 0;
+	int field = 0;
+	TRY(parse_synapse(n, dst, synapse, params, np, &w, &field));
+	Conn c{};
+	memset(&c.d, 0, sizeof c.d);
+	c.d.src = src;
+	c.d.dst = dst;
+	c.d.delay  = d;
+	c.d.weight = w;
+	c.d.field  = field;
+	c.d.src_size = n->pops[src].d.size;
+	c.d.dst_size = n->pops[dst].d.size;
+	n->conns.push_back(c);
+	// synapse_population ctor: _graph(c, seed++) (synapse_population.h:30-31)
+	n->gen_pending.push_back({(int)n->conns.size() - 1, seed_next(n), p});
+	if (conn_out) *conn_out = (int)n->conns.size() - 1;
+	return SPICE_OK;
+}
+
+extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int32_t* pairs, int64_t npairs, float delay,
+                                      int synapse, const float* params, int np, int* conn_out) {
+	int d = 0;
+	TRY(conn_common(n, src, dst, delay, &d));
+	if (npairs < 0 || (npairs > 0 && !pairs)) return fail(SPICE_EINVAL, "bad pairs");
+	float w   = 0;
+	int field = 0;
+	TRY(parse_synapse(n, dst, synapse, params, np, &w, &field));
+	int64_t const S = n->pops[src].d.size, Dn = n->pops[dst].d.size;
+	// adj_list::generate: sort src<<32|dst, stream the edges (topology.cpp:56-71, 12-32)
+	std::vector<uint64_t> e((size_t)npairs);
+	for (int64_t i = 0; i < npairs; i++) {
+		int32_t const a = pairs[2 * i], b = pairs[2 * i + 1];
+		if (a < 0 || a >= S) return pre_failed("topology.cpp:15", "edge.first < _offsets.size()");
+		if (b < 0 || b >= Dn) return pre_failed("synapse_population.h:119", "edge.first < dst_neurons.size()");
+		e[i] = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
+	}
+	std::sort(e.begin(), e.end());
+	std::vector<int64_t> off((size_t)S + 1, 0);
+	std::vector<int32_t> nb((size_t)npairs);
+	int64_t s = 0;
+	for (int64_t i = 0; i < npairs; i++) {
+		int64_t const es = (int64_t)(e[i] >> 32);
+		while (s <= es) off[s++] = i;
+		nb[i] = (int32_t)(e[i] & 0xffffffffu);
+	}
+	while (s <= S) off[s++] = npairs;
+	Conn c{};
+	memset(&c.d, 0, sizeof c.d);
+	c.d.src = src;
+	c.d.dst = dst;
+	c.d.delay    = d;
+	c.d.weight   = w;
+	c.d.field    = field;
+	c.d.src_size = S;
+	c.d.dst_size = Dn;
+	c.synapses   = npairs;
+	c.adj        = true;
+	int64_t* doff = nullptr;
+	int32_t* dnb  = nullptr;
+	CUDA_TRY(cudaMalloc(&doff, sizeof(int64_t) * (S + 1)));
+	if (cudaMalloc(&dnb, sizeof(int32_t) * (npairs > 0 ? npairs : 1)) != cudaSuccess) {
+		cudaFree(doff);
+		return fail(SPICE_ENOMEM, "cudaMalloc failed for adjacency");
+	}
+	CUDA_TRY(cudaMemcpyAsync(doff, off.data(), sizeof(int64_t) * (S + 1), cudaMemcpyHostToDevice, n->stream));
+	if (npairs > 0)
+		CUDA_TRY(cudaMemcpyAsync(dnb, nb.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	c.d.off = doff;
+	c.d.nb  = dnb;
+	n->conns.push_back(c);
+	seed_next(n);  // the synapse_population ctor consumes a seed for every topology
+	if (conn_out) *conn_out = (int)n->conns.size() - 1;
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_external_input(spice_net* n, int pop, int nsteps, const int32_t* counts,
+                                        const int32_t* indices) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (pop < 0 || pop >= (int)n->pops.size() || n->pops[pop].d.model != EXTERNAL)
+		return fail(SPICE_EINVAL, "population is not an external-input population");
+	if (nsteps < 0 || (nsteps > 0 && !counts)) return fail(SPICE_EINVAL, "bad train");
+	Pop& P          = n->pops[pop];
+	int64_t const S = P.d.size;
+	std::vector<int64_t> off((size_t)nsteps + 1, 0);
+	for (int i = 0; i < nsteps; i++) {
+		if (counts[i] < 0 || counts[i] > S) return fail(SPICE_EINVAL, "train step has more spikes than neurons");
+		off[i + 1] = off[i] + counts[i];
+	}
+	for (int i = 0; i < nsteps; i++)
+		for (int64_t j = off[i]; j < off[i + 1]; j++) {
+			if (indices[j] < 0 || indices[j] >= S) return fail(SPICE_EINVAL, "train spike index out of range");
+			if (j > off[i] && indices[j] <= indices[j - 1])
+				return fail(SPICE_EINVAL, "each step of an external train must list strictly ascending neuron indices");
+		}
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	int32_t* dc = nullptr;
+	int64_t* doff = nullptr;
+	int32_t* di = nullptr;
+	TRY(dalloc(n, &dc, nsteps + 1, false));
+	TRY(dalloc(n, &doff, nsteps + 1, false));
+	TRY(dalloc(n, &di, off[nsteps] + 1, false));
+	if (nsteps > 0) CUDA_TRY(cudaMemcpy(dc, counts, sizeof(int32_t) * nsteps, cudaMemcpyHostToDevice));
+	CUDA_TRY(cudaMemcpy(doff, off.data(), sizeof(int64_t) * (nsteps + 1), cudaMemcpyHostToDevice));
+	if (off[nsteps] > 0) CUDA_TRY(cudaMemcpy(di, indices, sizeof(int32_t) * off[nsteps], cudaMemcpyHostToDevice));
+	P.d.ext_counts = dc;
+	P.d.ext_off    = doff;
+	P.d.ext_idx    = di;
+	P.d.ext_steps  = nsteps;
+	n->ext_t_set[pop] = n->time;
+	if (n->prepared) CUDA_TRY(cudaMemcpy(n->d_pops + pop, &P.d, sizeof(PopDev), cudaMemcpyHostToDevice));
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_mode(spice_net* n, int mode) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (mode != SPICE_MODE_DETERMINISTIC && mode != SPICE_MODE_ATOMIC) return fail(SPICE_EINVAL, "unknown mode");
+	if (n->prepared && mode != n->mode) return fail(SPICE_ESTATE, "the delivery mode is fixed once the network steps");
+	n->mode = mode;
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_window(spice_net* n, int w) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (w < 0) return fail(SPICE_EINVAL, "window must be >= 0");
+	if (n->prepared && w > n->K) return fail(SPICE_ESTATE, "the window can only shrink once the network steps");
+	n->max_window = w;
+	return SPICE_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// preparation
+// ------------------------------------------------------------------------------------------------
+namespace {
+
+int generate_pending(spice_net* n) {
+	auto& pend = n->gen_pending;
+	if (pend.empty()) return SPICE_OK;
+	std::vector<GenRequest> reqs;
+	for (auto const& g : pend) {
+		Conn const& c = n->conns[g.conn];
+		reqs.push_back({c.d.src_size, c.d.dst_size, g.p, g.seed, nullptr, nullptr, 0});
+	}
+	cudaError_t e = generate_fixed_probability(n->stream, reqs);
+	if (e != cudaSuccess)
+		return fail(e == cudaErrorMemoryAllocation ? SPICE_ENOMEM : SPICE_ECUDA,
+		            std::string("fixed_probability generation failed: ") + cudaGetErrorString(e));
+	for (size_t i = 0; i < pend.size(); i++) {
+		Conn& c     = n->conns[pend[i].conn];
+		c.d.off     = reqs[i].offsets;
+		c.d.nb      = reqs[i].neighbors;
+		c.synapses  = reqs[i].synapses;
+	}
+	n->launches += 8 * (int64_t)pend.size();
+	pend.clear();
+	return SPICE_OK;
+}
+
+int prepare(spice_net* n) {
+	if (n->prepared) return SPICE_OK;
+	TRY(generate_pending(n));
+	int const np = (int)n->pops.size();
+	int64_t const D = n->max_delay;
+	if (D < 1) return pre_failed("neuron_population.h:108", "max_delay >= 1");
+	// window: the minimum delay (every delay is >= 1)
+	int K = kMaxWindow;
+	for (auto const& c : n->conns) K = std::min<int>(K, c.d.delay);
+	if (n->max_window > 0) K = std::min(K, n->max_window);
+	// the delivery kernel keeps a (step, connection) prefix of K * nconn entries in shared memory
+	if (!n->conns.empty()) K = std::min<int>(K, std::max<int>(1, 4096 / (int)n->conns.size()));
+	n->K  = std::max(K, 1);
+	n->Hb = (int)std::max<int64_t>(D, n->K);
+	// draw offsets in the step's shared stream (populations in add order, snn.cpp:14-15)
+	int64_t draws = 0;
+	for (auto& p : n->pops) {
+		p.d.draw_offset = draws;
+		if (p.d.model == POISSON) draws += p.d.size;
+	}
+	n->total_draws = draws;
+	for (auto& p : n->pops) {
+		PopDev& d = p.d;
+		TRY(dalloc(n, &d.bits, (size_t)n->Hb * std::max(d.nwords, 1)));
+		TRY(dalloc(n, &d.list, (size_t)n->K * std::max<int64_t>(d.size, 1), false));
+		if (d.model == POISSON && d.nwords > 0) {
+			std::vector<u128> polys(d.nwords);
+			u128 const step = gf2_xpow(kPoissonChunk);
+			polys[0]        = gf2_xpow((uint64_t)d.draw_offset);
+			for (int c = 1; c < d.nwords; c++) polys[c] = gf2_mulmod(polys[c - 1], step);
+			u128* dp = nullptr;
+			TRY(dalloc(n, &dp, d.nwords, false));
+			CUDA_TRY(cudaMemcpy(dp, polys.data(), sizeof(u128) * d.nwords, cudaMemcpyHostToDevice));
+			d.chunk_poly = dp;
+		}
+	}
+	// input groups per target population: connections in connect order; a connection joins the
+	// latest group of its field when the weights are bit-identical (same sequence of adds)
+	std::vector<std::vector<int>> group_conns(np * kMaxGroups);
+	for (int pi = 0; pi < np; pi++) {
+		PopDev& d = n->pops[pi].d;
+		if (!n->pops[pi].stateful) continue;
+		int last_of_field[3] = {-1, -1, -1};
+		d.ngroups = 0;
+		for (int ci = 0; ci < (int)n->conns.size(); ci++) {
+			ConnDev& c = n->conns[ci].d;
+			if (c.dst != pi) continue;
+			int g = last_of_field[c.field];
+			if (g < 0 || memcmp(&d.group_weight[g], &c.weight, sizeof(float)) != 0) {
+				if (d.ngroups >= kMaxGroups)
+					return fail(SPICE_EINVAL, "too many distinct input weights into one population (max 8)");
+				g                 = d.ngroups++;
+				d.group_field[g]  = c.field;
+				d.group_weight[g] = c.weight;
+				last_of_field[c.field] = g;
+			}
+			c.group = g;
+			group_conns[pi * kMaxGroups + g].push_back(ci);
+		}
+		// counter widths from the maximum in-degree of each group
+		uint32_t* scratch = nullptr;
+		uint32_t* dmax    = nullptr;
+		CUDA_TRY(cudaMalloc(&scratch, sizeof(uint32_t) * (d.size > 0 ? d.size : 1)));
+		CUDA_TRY(cudaMalloc(&dmax, sizeof(uint32_t)));
+		int word = 0, half = 0;
+		for (int g = 0; g < d.ngroups; g++) {
+			std::vector<const int32_t*> nbs;
+			std::vector<int64_t> ns;
+			for (int ci : group_conns[pi * kMaxGroups + g]) {
+				nbs.push_back(n->conns[ci].d.nb);
+				ns.push_back(n->conns[ci].synapses);
+			}
+			uint32_t mx = 0;
+			cudaError_t e = max_indegree(n->stream, nbs.data(), ns.data(), (int)nbs.size(), d.size, scratch, dmax);
+			if (e == cudaSuccess) e = cudaMemcpyAsync(&mx, dmax, sizeof(uint32_t), cudaMemcpyDeviceToHost, n->stream);
+			if (e == cudaSuccess) e = cudaStreamSynchronize(n->stream);
+			n->launches += (int64_t)nbs.size() + 1;
+			if (e != cudaSuccess) {
+				cudaFree(scratch);
+				cudaFree(dmax);
+				return fail(SPICE_ECUDA, std::string("in-degree count failed: ") + cudaGetErrorString(e));
+			}
+			if (mx < 65536u) {
+				if (half == 1) {
+					d.group_word[g]  = word - 1;
+					d.group_shift[g] = 16;
+					half             = 0;
+				} else {
+					d.group_word[g]  = word++;
+					d.group_shift[g] = 0;
+					half             = 1;
+				}
+				d.group_bits[g] = 16;
+			} else {
+				d.group_word[g]  = word++;
+				d.group_shift[g] = 0;
+				d.group_bits[g]  = 32;
+				half             = 0;
+			}
+		}
+		cudaFree(scratch);
+		cudaFree(dmax);
+		d.W = std::max(word, 1);
+		int F = 0;
+		for (int g = 0; g < d.ngroups; g++)
+			if (d.field_slot[d.group_field[g]] < 0) d.field_slot[d.group_field[g]] = F++;
+		d.F = std::max(F, 1);
+		if (n->mode == SPICE_MODE_DETERMINISTIC)
+			TRY(dalloc(n, &d.cnt, (size_t)D * d.size * d.W));
+		else
+			TRY(dalloc(n, &d.acc, (size_t)D * d.size * d.F));
+	}
+	for (auto& c : n->conns) {
+		ConnDev& d      = c.d;
+		PopDev const& S = n->pops[d.src].d;
+		PopDev const& T = n->pops[d.dst].d;
+		d.src_list = S.list;
+		d.dst_cnt  = T.cnt;
+		d.dst_acc  = T.acc;
+		d.W        = T.W;
+		d.word     = T.group_word[d.group];
+		d.inc      = 1u << T.group_shift[d.group];
+		d.F        = T.F;
+		d.fslot    = T.field_slot[d.field];
+	}
+	TRY(dalloc(n, &n->d_counts, (size_t)2 * n->K * std::max(np, 1)));
+	TRY(dalloc(n, &n->d_pops, std::max(np, 1), false));
+	TRY(dalloc(n, &n->d_conns, std::max<size_t>(n->conns.size(), 1), false));
+	std::vector<PopDev> hp;
+	for (auto& p : n->pops) hp.push_back(p.d);
+	std::vector<ConnDev> hc;
+	for (auto& c : n->conns) hc.push_back(c.d);
+	if (np) CUDA_TRY(cudaMemcpy(n->d_pops, hp.data(), sizeof(PopDev) * np, cudaMemcpyHostToDevice));
+	if (!hc.empty()) CUDA_TRY(cudaMemcpy(n->d_conns, hc.data(), sizeof(ConnDev) * hc.size(), cudaMemcpyHostToDevice));
+	n->run_cap = kRunCap;
+	TRY(dalloc(n, &n->d_dt, kRunCap, false));
+	TRY(dalloc(n, &n->d_seeds, kRunCap, false));
+	if (n->total_draws > 0) TRY(dalloc(n, &n->d_basis, (size_t)kRunCap * kBasis, false));
+	CUDA_TRY(cudaMallocHost(&n->h_dt, sizeof(float) * kRunCap));
+	CUDA_TRY(cudaMallocHost(&n->h_seeds, sizeof(u128) * kRunCap));
+	int64_t maxN = 1;
+	for (auto& p : n->pops) maxN = std::max(maxN, p.d.size);
+	TRY(dalloc(n, &n->d_tmp, maxN, false));
+	TRY(dalloc(n, &n->d_tmp_n, 1));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	n->prepared = true;
+	return SPICE_OK;
+}
+
+int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) {
+	TRY(prepare(n));
+	int const np   = (int)n->pops.size();
+	int64_t rows   = 0;
+	while (steps > 0) {
+		int64_t const chunk = std::min<int64_t>(steps, n->run_cap);
+		CUDA_TRY(cudaStreamSynchronize(n->stream));  // the pinned staging is about to be rewritten
+		for (int64_t j = 0; j < chunk; j++) {
+			n->h_dt[j]    = kahan_next(n);
+			n->h_seeds[j] = seed_next(n);  // xoroshiro64_128p rng(_seed++) (snn.cpp:12)
+		}
+		CUDA_TRY(cudaMemcpyAsync(n->d_dt, n->h_dt, sizeof(float) * chunk, cudaMemcpyHostToDevice, n->stream));
+		if (n->total_draws > 0) {
+			CUDA_TRY(cudaMemcpyAsync(n->d_seeds, n->h_seeds, sizeof(u128) * chunk, cudaMemcpyHostToDevice, n->stream));
+			CUDA_TRY(launch_basis(n->stream, n->d_seeds, chunk, n->d_basis));
+			n->launches++;
+		}
+		int64_t j = 0;
+		while (j < chunk) {
+			int const k = (int)std::min<int64_t>(n->K, chunk - j);
+			WindowArgs wa{};
+			wa.t0     = n->time;
+			wa.K      = k;
+			wa.slot0  = (int)((n->time - 1 + n->max_delay) % n->max_delay);
+			wa.hslot0 = (int)(n->time % n->Hb);
+			wa.D      = n->max_delay;
+			wa.Hb     = n->Hb;
+			wa.npop   = np;
+			wa.mode   = n->mode;
+			wa.pops   = n->d_pops;
+			wa.dts    = n->d_dt + j;
+			wa.basis  = n->d_basis ? n->d_basis + j * kBasis : nullptr;
+			wa.counts = n->d_counts + (size_t)n->parity * n->K * np;
+			int nb = 0;
+			for (int p = 0; p < np; p++) {
+				PopDev const& P = n->pops[p].d;
+				wa.blk_begin[p] = nb;
+				if (P.model == POISSON) {
+					wa.blk_kind[p]     = 1;
+					wa.blk_per_step[p] = (P.nwords + 255) / 256;
+					nb += wa.blk_per_step[p] * k;
+				} else if (P.model == EXTERNAL) {
+					wa.blk_kind[p]     = 2;
+					wa.blk_per_step[p] = 1;
+					nb += k;
+					int64_t const ns = P.ext_steps;
+					wa.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
+				} else {
+					wa.blk_kind[p] = 0;
+					nb += (int)((P.size + 255) / 256);
+				}
+			}
+			wa.blk_begin[np] = nb;
+			int slot = -1;
+			TRY(ev_begin(n, 0, &slot));
+			CUDA_TRY(launch_window(n->stream, wa, nb));
+			TRY(ev_end(n, slot));
+			n->launches++;
+			DeliverArgs da{};
+			da.t0     = n->time;
+			da.K      = k;
+			da.D      = n->max_delay;
+			da.nconn  = (int)n->conns.size();
+			da.npop   = np;
+			da.mode   = n->mode;
+			da.conns  = n->d_conns;
+			da.pops   = n->d_pops;
+			da.counts = wa.counts;
+			da.counts_next     = n->d_counts + (size_t)(n->parity ^ 1) * n->K * np;
+			da.counts_next_len = n->K * np;
+			da.events = n->d_events;
+			TRY(ev_begin(n, 1, &slot));
+			CUDA_TRY(launch_deliver(n->stream, da, 1216));
+			TRY(ev_end(n, slot));
+			n->launches++;
+			if (record) {
+				RasterArgs ra{};
+				ra.t0       = n->time;
+				ra.K        = k;
+				ra.Hb       = n->Hb;
+				ra.npop     = np;
+				ra.pops     = n->d_pops;
+				ra.out      = n->d_raster;
+				ra.capacity = n->raster_cap;
+				ra.cursor   = n->d_raster_cursor;
+				ra.tab      = n->d_raster_tab;
+				ra.row0     = rows;
+				TRY(ev_begin(n, 2, &slot));
+				CUDA_TRY(launch_raster(n->stream, ra));
+				TRY(ev_end(n, slot));
+				n->launches++;
+			}
+			n->parity ^= 1;
+			n->time += k;
+			rows += k;
+			j += k;
+		}
+		steps -= chunk;
+	}
+	if (rows_done_out) *rows_done_out = rows;
+	return SPICE_OK;
+}
+
+// Applies inputs waiting for the next update so that state reads match the reference's state
+// after step() (which has already delivered them).
+int flush_pending(spice_net* n) {
+	if (!n->prepared || n->time == 0) return SPICE_OK;
+	std::vector<int> st;
+	std::vector<PopDev> hp;
+	for (int i = 0; i < (int)n->pops.size(); i++) {
+		hp.push_back(n->pops[i].d);
+		if (n->pops[i].stateful) st.push_back(i);
+	}
+	CUDA_TRY(launch_apply_pending(n->stream, n->d_pops, (int)hp.size(), st.data(), (int)st.size(), hp, n->time,
+	                              n->max_delay, n->mode));
+	n->launches += (int64_t)st.size();
+	return SPICE_OK;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------------------------------------
+// stepping and readback
+// ------------------------------------------------------------------------------------------------
+
+extern "C" int spice_step(spice_net* n) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	return run_steps(n, 1, false, nullptr);
+}
+
+extern "C" int spice_run(spice_net* n, int64_t steps) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (steps < 0) return fail(SPICE_EINVAL, "steps must be >= 0");
+	return run_steps(n, steps, false, nullptr);
+}
+
+extern "C" int spice_run_record(spice_net* n, int64_t steps, int64_t* counts_out, int32_t* spikes_out, int64_t capacity,
+                                int64_t* total_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (steps < 0 || capacity < 0) return fail(SPICE_EINVAL, "steps and capacity must be >= 0");
+	TRY(prepare(n));
+	int const np = (int)n->pops.size();
+	// device raster buffers (grown on demand)
+	if (n->raster_cap < capacity || !n->d_raster) {
+		if (n->d_raster) {
+			CUDA_TRY(cudaStreamSynchronize(n->stream));
+			cudaFree(n->d_raster);
+			n->allocations.erase(std::find(n->allocations.begin(), n->allocations.end(), (void*)n->d_raster));
+		}
+		TRY(dalloc(n, &n->d_raster, std::max<int64_t>(capacity, 1), false));
+		n->raster_cap = std::max<int64_t>(capacity, 1);
+	}
+	static thread_local std::vector<int64_t> tab;
+	if (n->d_raster_tab) {
+		CUDA_TRY(cudaStreamSynchronize(n->stream));
+		cudaFree(n->d_raster_tab);
+		n->allocations.erase(std::find(n->allocations.begin(), n->allocations.end(), (void*)n->d_raster_tab));
+		n->d_raster_tab = nullptr;
+	}
+	TRY(dalloc(n, &n->d_raster_tab, (size_t)std::max<int64_t>(steps, 1) * std::max(np, 1) * 2));
+	if (!n->d_raster_cursor) TRY(dalloc(n, &n->d_raster_cursor, 1));
+	CUDA_TRY(cudaMemsetAsync(n->d_raster_cursor, 0, sizeof(unsigned long long), n->stream));
+	int64_t rows = 0;
+	TRY(run_steps(n, steps, true, &rows));
+	unsigned long long total = 0;
+	CUDA_TRY(cudaMemcpyAsync(&total, n->d_raster_cursor, sizeof(total), cudaMemcpyDeviceToHost, n->stream));
+	tab.resize((size_t)steps * np * 2);
+	if (steps * np > 0)
+		CUDA_TRY(cudaMemcpyAsync(tab.data(), n->d_raster_tab, sizeof(int64_t) * tab.size(), cudaMemcpyDeviceToHost,
+		                         n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	if (total_out) *total_out = (int64_t)total;
+	if ((int64_t)total > capacity)
+		return fail(SPICE_EOVERFLOW, "raster needs " + std::to_string(total) + " entries, capacity is " +
+		                                 std::to_string(capacity));
+	static thread_local std::vector<int32_t> flat;
+	flat.resize(total);
+	if (total) CUDA_TRY(cudaMemcpy(flat.data(), n->d_raster, sizeof(int32_t) * total, cudaMemcpyDeviceToHost));
+	int64_t pos = 0;
+	for (int64_t t = 0; t < steps; t++)
+		for (int p = 0; p < np; p++) {
+			int64_t const o = tab[(t * np + p) * 2], c = tab[(t * np + p) * 2 + 1];
+			if (counts_out) counts_out[t * np + p] = c;
+			if (spikes_out && c) memcpy(spikes_out + pos, flat.data() + o, sizeof(int32_t) * c);
+			pos += c;
+		}
+	return SPICE_OK;
+}
+
+namespace {
+int age_check(spice_net* n, int pop, int64_t age) {
+	if (pop < 0 || pop >= (int)n->pops.size()) return fail(SPICE_EINVAL, "population id out of range");
+	int64_t const recorded = std::min<int64_t>(n->time, n->max_delay);
+	if (!(0 <= age && age < recorded))
+		return pre_failed("neuron_population.h:148", "0 <= age && age < _spike_counts.size()");
+	return SPICE_OK;
+}
+}  // namespace
+
+extern "C" int spice_spikes(spice_net* n, int pop, int64_t age, int32_t* out, int64_t capacity, int64_t* n_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	TRY(age_check(n, pop, age));
+	PopDev const& P   = n->pops[pop].d;
+	int64_t const t   = n->time - 1 - age;
+	const uint32_t* b = P.bits + (t % n->Hb) * P.nwords;
+	CUDA_TRY(launch_extract(n->stream, b, P.nwords, n->d_tmp, n->d_tmp_n));
+	n->launches++;
+	int64_t cnt = 0;
+	CUDA_TRY(cudaMemcpyAsync(&cnt, n->d_tmp_n, sizeof(int64_t), cudaMemcpyDeviceToHost, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	if (n_out) *n_out = cnt;
+	if (cnt > capacity) return fail(SPICE_EOVERFLOW, "spike buffer too small");
+	if (cnt && out) CUDA_TRY(cudaMemcpy(out, n->d_tmp, sizeof(int32_t) * cnt, cudaMemcpyDeviceToHost));
+	return SPICE_OK;
+}
+
+extern "C" int spice_spike_count(spice_net* n, int pop, int64_t age, int64_t* n_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	TRY(age_check(n, pop, age));
+	int64_t cnt = 0;
+	int const r = spice_spikes(n, pop, age, nullptr, INT64_MAX, &cnt);
+	if (n_out) *n_out = cnt;
+	return r;
+}
+
+namespace {
+int field_ptr(spice_net* n, int pop, int field, void** p) {
+	if (pop < 0 || pop >= (int)n->pops.size()) return fail(SPICE_EINVAL, "population id out of range");
+	PopDev const& P = n->pops[pop].d;
+	if (!n->pops[pop].stateful)
+		return fail(SPICE_EINVAL, "Can only return collections of stateful neurons. (neuron_population.h:143)");
+	void* f = nullptr;
+	switch (field) {
+		case SPICE_FIELD_V: f = P.V; break;
+		case SPICE_FIELD_GEX: f = P.Gex; break;
+		case SPICE_FIELD_GIN: f = P.Gin; break;
+		case SPICE_FIELD_TREF: f = P.T; break;
+	}
+	if (!f) return fail(SPICE_EINVAL, "the neuron model has no such state field");
+	*p = f;
+	return SPICE_OK;
+}
+}  // namespace
+
+extern "C" int spice_get_state(spice_net* n, int pop, int field, void* host_out) {
+	if (!n || !host_out) return fail(SPICE_EINVAL, "NULL argument");
+	void* f = nullptr;
+	TRY(field_ptr(n, pop, field, &f));
+	TRY(flush_pending(n));
+	CUDA_TRY(cudaMemcpyAsync(host_out, f, 4 * n->pops[pop].d.size, cudaMemcpyDeviceToHost, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_state(spice_net* n, int pop, int field, const void* host_in) {
+	if (!n || !host_in) return fail(SPICE_EINVAL, "NULL argument");
+	void* f = nullptr;
+	TRY(field_ptr(n, pop, field, &f));
+	TRY(flush_pending(n));
+	CUDA_TRY(cudaMemcpyAsync(f, host_in, 4 * n->pops[pop].d.size, cudaMemcpyHostToDevice, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}
+
+extern "C" int spice_pop_size(spice_net* n, int pop, int64_t* size_out) {
+	if (!n || !size_out) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop < 0 || pop >= (int)n->pops.size()) return fail(SPICE_EINVAL, "population id out of range");
+	*size_out = n->pops[pop].d.size;
+	return SPICE_OK;
+}
+
+extern "C" int spice_time(spice_net* n, int64_t* t) {
+	if (!n || !t) return fail(SPICE_EINVAL, "NULL argument");
+	*t = n->time;
+	return SPICE_OK;
+}
+
+extern "C" int spice_events(spice_net* n, uint64_t* ev) {
+	if (!n || !ev) return fail(SPICE_EINVAL, "NULL argument");
+	unsigned long long v = 0;
+	CUDA_TRY(cudaMemcpyAsync(&v, n->d_events, sizeof(v), cudaMemcpyDeviceToHost, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	*ev = v;
+	return SPICE_OK;
+}
+
+extern "C" int spice_conn_size(spice_net* n, int conn, int64_t* src_out, int64_t* syn_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	TRY(generate_pending(n));
+	if (src_out) *src_out = n->conns[conn].d.src_size;
+	if (syn_out) *syn_out = n->conns[conn].synapses;
+	return SPICE_OK;
+}
+
+extern "C" int spice_get_csr(spice_net* n, int conn, int64_t* off, int32_t* nb) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	TRY(generate_pending(n));
+	Conn const& c = n->conns[conn];
+	if (off) CUDA_TRY(cudaMemcpy(off, c.d.off, sizeof(int64_t) * (c.d.src_size + 1), cudaMemcpyDeviceToHost));
+	if (nb && c.synapses) CUDA_TRY(cudaMemcpy(nb, c.d.nb, sizeof(int32_t) * c.synapses, cudaMemcpyDeviceToHost));
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_profiling(spice_net* n, int on) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	TRY(harvest(n));
+	n->profiling = on != 0;
+	for (auto& s : n->stats) s = KernelStat{};
+	if (n->profiling)
+		while (n->ev_pool.size() < 4096) {
+			cudaEvent_t e;
+			CUDA_TRY(cudaEventCreate(&e));
+			n->ev_pool.push_back(e);
+		}
+	return SPICE_OK;
+}
+
+extern "C" int spice_kernel_stats(spice_net* n, int kind, int64_t* launches, double* ms) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (kind < 0 || kind > 2) return fail(SPICE_EINVAL, "unknown kernel kind");
+	TRY(harvest(n));
+	if (launches) *launches = n->stats[kind].launches;
+	if (ms) *ms = n->stats[kind].ms;
+	return SPICE_OK;
+}
+
+extern "C" int spice_launch_count(spice_net* n, int64_t* out) {
+	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
+	*out = n->launches;
+	return SPICE_OK;
+}
+
+extern "C" int spice_synchronize(spice_net* n) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}

@@ -1,0 +1,116 @@
+"""Regenerates the golden fixtures in tests/golden/ from the reference itself.
+
+Runs oracle/_ref/ref_driver -- spice2's own sources (spice/src/{snn,topology,util/assert}.cpp and
+headers) compiled by oracle/Makefile with the reference's Release flags -- and stores its outputs:
+
+  rng.npz                    seed chains, xoroshiro128+ draws, exponential draws, canonical floats
+                             and the Kahan dt sequence for seeds 1, 7, 1337
+  csr_small.npz              complete fixed_probability CSRs for small (src, dst, p, seed) cases
+  brunel_csr_checksums.json  checksums of the six Brunel CSRs at N=2e4 p=0.1 seed 1337 and at
+                             N=5e5 p=0.002 seeds 1..10, seeded exactly as snn seeds them
+  brunel_n20000.npz          N=2e4 p=0.1 seed 1337, 300 steps: raster (I, E, P) and final V/Tref
+  brunel_n5000.npz           N=5e3 p=0.05 seed 7, 500 steps: raster and final V/Tref
+  mixed_net.npz              mixed delays (2..7), adj_list edges, three input groups: raster/state
+  brunel_n500000_s1.json     N=5e5 p=0.002 seed 1, 300 steps: per-step spike counts and checksums
+
+usage: python tests/golden/make_golden.py   (needs the reference sources; run from the repo root)
+"""
+from __future__ import annotations
+
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+from oracle import oracle as O  # noqa: E402
+from oracle.oracle import raster_checksum, state_checksum  # noqa: E402
+
+
+def raster_arrays(res):
+    """Flattens a raster into (counts[steps][npop], indices)."""
+    counts = np.array([[len(x) for x in row] for row in res["raster"]], dtype=np.int32)
+    idx = np.concatenate([x for row in res["raster"] for x in row] + [np.zeros(0, np.int32)]).astype(np.int32)
+    return counts, idx
+
+
+def mixed_spec(steps: int):
+    """A network with mixed delays, an adj_list projection and three input groups into E."""
+    rng = np.random.default_rng(5)
+    pairs = sorted({(int(a), int(b)) for a, b in zip(rng.integers(0, 2000, 6000), rng.integers(0, 1000, 6000))})
+    lines = ["0.0001 0.0008 4242 %d 0" % steps,
+             "pop poisson 3000 50", "pop lif 2000", "pop lif 1000"]
+    lines += ["conn 0 1 0.05 0.0003 0.002",
+              "conn 1 1 0.05 0.0005 0.002",
+              "conn 2 1 0.1 0.0002 -0.005",
+              "conn 0 2 0.02 0.0004 0.004",
+              "adj 1 2 0.0006 0.003 %d %s" % (len(pairs), " ".join(f"{a} {b}" for a, b in pairs)),
+              "conn 2 2 0.02 0.0007 -0.004",
+              "conn 1 1 0.01 0.0008 0.003"]
+    return lines, pairs
+
+
+def main():
+    if not O.have_reference():
+        O.build(with_reference=True)
+    # rng
+    rng = {}
+    for seed in (1, 7, 1337):
+        r = O.run_reference_rng(seed, 2000)
+        for k, v in r.items():
+            rng[f"{k}_{seed}"] = v
+    np.savez_compressed(os.path.join(HERE, "rng.npz"), **rng)
+    # small CSRs
+    cases = [(1000, 800, 0.1, 1), (100, 5000, 0.002, 7), (50, 50, 1.0, 3), (10, 10, 0.0, 3), (3, 0, 0.5, 1),
+             (300, 600, 0.5, 9), (100, 70000, 0.01, 11), (5, 3, 0.9, 2), (1500, 200, 0.3, 5)]
+    csr = {}
+    for (s, d, p, sd) in cases:
+        md, off, nb = O.run_reference_gen(s, d, p, sd)
+        key = f"{s}_{d}_{p}_{sd}"
+        csr[f"off_{key}"] = off
+        csr[f"nb_{key}"] = nb
+        csr[f"md_{key}"] = np.array([md])
+    np.savez_compressed(os.path.join(HERE, "csr_small.npz"), **csr)
+    # full-size checksums
+    cs = {}
+    for (N, p, seeds) in ((20000, 0.1, [1337]), (500000, 0.002, list(range(1, 11)))):
+        key = f"N={N},p={p}"
+        cs[key] = {}
+        for sd in seeds:
+            txt = subprocess.run([O.REF_DRIVER, "bcsr", str(N), repr(p), str(sd)], check=True,
+                                 capture_output=True, text=True).stdout
+            cs[key][str(sd)] = [[int(x) for x in line.split()] for line in txt.strip().splitlines()]
+    json.dump(cs, open(os.path.join(HERE, "brunel_csr_checksums.json"), "w"), indent=1)
+    # Brunel rasters
+    for (N, p, sd, steps, name) in ((20000, 0.1, 1337, 300, "brunel_n20000"), (5000, 0.05, 7, 500, "brunel_n5000")):
+        res = O.run_reference_net(O.brunel_spec(N, p, sd, steps))
+        st, _, _ = O.reference_states(res, [1, 2])
+        counts, idx = raster_arrays(res)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), counts=counts, idx=idx, dt=res["dt"],
+                            V1=st[1][0], T1=st[1][1], V2=st[2][0], T2=st[2][1],
+                            meta=np.array([N, sd, steps]), p=np.array([p]))
+    # mixed network
+    lines, pairs = mixed_spec(400)
+    res = O.run_reference_net(lines)
+    st, _, _ = O.reference_states(res, [1, 2])
+    counts, idx = raster_arrays(res)
+    np.savez_compressed(os.path.join(HERE, "mixed_net.npz"), counts=counts, idx=idx, V1=st[1][0], T1=st[1][1],
+                        V2=st[2][0], T2=st[2][1], pairs=np.array(pairs, dtype=np.int32))
+    # N = 5e5: per-step counts and checksums only (the raster and state are megabytes)
+    res = O.run_reference_net(O.brunel_spec(500000, 0.002, 1, 300))
+    st, _, step_s = O.reference_states(res, [1, 2])
+    counts, idx = raster_arrays(res)
+    json.dump({"N": 500000, "p": 0.002, "seed": 1, "steps": 300, "counts": counts.tolist(),
+               "raster_checksum": raster_checksum(counts, idx),
+               "state_checksum_E": state_checksum(*st[1]), "state_checksum_I": state_checksum(*st[2]),
+               "reference_step_seconds": step_s},
+              open(os.path.join(HERE, "brunel_n500000_s1.json"), "w"))
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

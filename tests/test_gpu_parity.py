@@ -1,0 +1,293 @@
+"""GPU parity: the CUDA engine against the CPU oracle (and the reference's golden vectors).
+
+Integer/index results (CSR neighbour lists, spike rasters, Tref) and the float state V are
+compared bit for bit: the reference's deterministic path has a single valid answer.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _csr_cases():
+    return [
+        (1000, 800, 0.1, 1), (100, 5000, 0.002, 7), (50, 50, 1.0, 3), (10, 10, 0.0, 3),
+        (3, 0, 0.5, 1), (0, 10, 0.5, 1), (2000, 2000, 0.5, 9), (300, 70000, 0.01, 11),
+        (5, 3, 0.9, 2), (70000, 300, 0.3, 5),
+    ]
+
+
+@pytest.mark.parametrize("src,dst,p,seed", _csr_cases())
+def test_fixed_probability_csr_bit_exact(engine, oracle_lib, src, dst, p, seed):
+    sp, o = engine, oracle_lib
+    net = sp.snn(1e-4, 1e-4, [seed])
+    # two stateful populations would consume seeds; use stateless source + lif target and
+    # compare against the oracle generator fed the projection's own seed
+    S = net.add_population(sp.poisson(), src)
+    D = net.add_population(sp.lif(), dst)
+    c = net.connect(S, D, sp.fixed_probability(p), 1e-4, sp.fixed_weight(0.0))
+    off, nb = net.csr(c)
+    chain = o.seed_chain([seed], 2)  # seed 0 -> lif population, seed 1 -> the projection
+    roff, rnb, _ = o.fp_generate(src, dst, p, chain[1])
+    assert np.array_equal(off, roff)
+    assert np.array_equal(nb, rnb)
+
+
+def _compare_net(sp, o, N, p, seed, steps, use_run=False, mode=0):
+    net, pops = sp.brunel(N, p, seed, mode=mode)
+    ref, rpops = o.brunel(N, p, seed)
+    if use_run:
+        raster = net.run_record(steps)
+    for t in range(steps):
+        if not use_run:
+            net.step()
+        ref.step()
+        for k in range(3):
+            a = raster[t][k] if use_run else net.spikes(pops[k], 0)
+            b = ref.spikes(rpops[k], 0)
+            assert np.array_equal(a, b), f"step {t} pop {k}: {a[:10]} vs {b[:10]}"
+    for k in (1, 2):
+        st = pops[k].get_neurons()
+        assert np.array_equal(st["V"].view(np.uint32), ref.state(rpops[k], 0).view(np.uint32))
+        assert np.array_equal(st["Tref"], ref.state(rpops[k], 3))
+    return net, ref
+
+
+def test_brunel_step_bit_exact(engine, oracle_lib):
+    _compare_net(engine, oracle_lib, 4000, 0.05, 1337, 300)
+
+
+def test_brunel_run_windows_bit_exact(engine, oracle_lib):
+    _compare_net(engine, oracle_lib, 4000, 0.05, 42, 400, use_run=True)
+
+
+def test_brunel_readme_config(engine, oracle_lib):
+    """samples/brunel.cpp as published: N=2e4, p=0.1, seed 1337 (README.md:106-117)."""
+    net, ref = _compare_net(engine, oracle_lib, 20000, 0.1, 1337, 300, use_run=True)
+
+
+# ---- against the reference's golden vectors (independent of the oracle) ------------------------
+import json
+import os
+
+from conftest import GOLDEN
+
+
+def _raster_flat(raster):
+    counts = np.array([[len(x) for x in row] for row in raster], dtype=np.int32)
+    idx = np.concatenate([x for row in raster for x in row] + [np.zeros(0, np.int32)]).astype(np.int32)
+    return counts, idx
+
+
+@pytest.mark.parametrize("name", ["brunel_n20000.npz", "brunel_n5000.npz"])
+def test_brunel_golden_raster_and_state(engine, name):
+    g = np.load(os.path.join(GOLDEN, name))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    counts, idx = _raster_flat(net.run_record(steps))
+    assert np.array_equal(counts, g["counts"])
+    assert np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        st = pops[k].get_neurons()
+        assert np.array_equal(st["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+        assert np.array_equal(st["Tref"], g[f"T{k}"])
+
+
+def test_mixed_network_golden(engine, oracle_lib):
+    """Delays 2..8 steps (window = 2 steps), an adj_list projection, three input groups into E."""
+    sp = engine
+    g = np.load(os.path.join(GOLDEN, "mixed_net.npz"))
+    net = sp.snn(1e-4, 8e-4, [4242])
+    P = net.add_population(sp.poisson(50.0), 3000)
+    E = net.add_population(sp.lif(), 2000)
+    I = net.add_population(sp.lif(), 1000)
+    f = lambda x: float(np.float32(x))
+    net.connect(P, E, sp.fixed_probability(0.05), 3e-4, sp.fixed_weight(f(0.002)))
+    net.connect(E, E, sp.fixed_probability(0.05), 5e-4, sp.fixed_weight(f(0.002)))
+    net.connect(I, E, sp.fixed_probability(0.1), 2e-4, sp.fixed_weight(f(-0.005)))
+    net.connect(P, I, sp.fixed_probability(0.02), 4e-4, sp.fixed_weight(f(0.004)))
+    adj = sp.adj_list()
+    for a, b in g["pairs"]:
+        adj.connect(a, b)
+    net.connect(E, I, adj, 6e-4, sp.fixed_weight(f(0.003)))
+    net.connect(I, I, sp.fixed_probability(0.02), 7e-4, sp.fixed_weight(f(-0.004)))
+    net.connect(E, E, sp.fixed_probability(0.01), 8e-4, sp.fixed_weight(f(0.003)))
+    half = g["counts"].shape[0] // 2
+    r1 = net.run_record(half)        # windowed
+    r2 = [None] * (g["counts"].shape[0] - half)
+    for t in range(len(r2)):         # then single steps
+        net.step()
+        r2[t] = [net.spikes(p, 0) for p in (P, E, I)]
+    counts, idx = _raster_flat(r1 + r2)
+    assert np.array_equal(counts, g["counts"])
+    assert np.array_equal(idx, g["idx"])
+    for k, pop in ((1, E), (2, I)):
+        st = pop.get_neurons()
+        assert np.array_equal(st["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+        assert np.array_equal(st["Tref"], g[f"T{k}"])
+
+
+def _checksums_of(net, n):
+    from oracle.oracle import csr_checksum
+    out = []
+    for c in range(n):
+        off, nb = net.csr(c)
+        out.append((int(off[-1]), csr_checksum(off, nb)))
+    return out
+
+
+def test_csr_checksums_n20000(engine):
+    cs = json.load(open(os.path.join(GOLDEN, "brunel_csr_checksums.json")))["N=20000,p=0.1"]["1337"]
+    net, _ = engine.brunel(20000, 0.1, 1337)
+    assert _checksums_of(net, 6) == [(row[2], row[3]) for row in cs]
+
+
+@pytest.mark.parametrize("seed", list(range(1, 11)))
+def test_csr_checksums_full_size(engine, seed):
+    """Large Brunel, N=5e5, p=0.002 (2.5e8 synapses): all six CSRs equal the reference's."""
+    cs = json.load(open(os.path.join(GOLDEN, "brunel_csr_checksums.json")))["N=500000,p=0.002"][str(seed)]
+    net, _ = engine.brunel(500000, 0.002, seed)
+    assert _checksums_of(net, 6) == [(row[2], row[3]) for row in cs]
+
+
+@pytest.mark.parametrize("mode", [0])
+def test_large_brunel_300_steps_golden(engine, mode):
+    """N=5e5, p=0.002, seed 1: per-step spike counts, raster and state checksums equal the reference's."""
+    from oracle.oracle import raster_checksum, state_checksum
+    g = json.load(open(os.path.join(GOLDEN, "brunel_n500000_s1.json")))
+    net, pops = engine.brunel(500000, 0.002, 1, mode=mode)
+    counts, idx = _raster_flat(net.run_record(g["steps"]))
+    assert counts.tolist() == g["counts"]
+    assert raster_checksum(counts, idx) == g["raster_checksum"]
+    e, i = pops[1].get_neurons(), pops[2].get_neurons()
+    assert state_checksum(e["V"], e["Tref"]) == g["state_checksum_E"]
+    assert state_checksum(i["V"], i["Tref"]) == g["state_checksum_I"]
+
+
+# ---- the reference's own known-answer tests, restated ----------------------------------------------
+def test_external_input_sample(engine):
+    """samples/external_input.cpp: a per-population update replays a cyclic spike train."""
+    sp = engine
+    trains = [[4, 5, 8], [5], [7, 8], [5, 7]]
+    net = sp.snn(1, 1, [1337])
+    I = net.add_population(sp.external_input(tuple(map(tuple, trains))), 9)
+    for t in range(20):
+        net.step()
+        assert net.spikes(I, 0).tolist() == trains[t % 4]
+
+
+def test_deliver_counts_known_answer(engine):
+    """test/detail/synapse_population.cpp:28-57: edges 0->0, 0->1, 0->3, 1->3, 2->4; spikes {0, 1}
+    deliver 1, 1, 0, 2, 0 times."""
+    sp = engine
+    net = sp.snn(1, 1, [1337])
+    S = net.add_population(sp.external_input(((0, 1), ())), 3)
+    D = net.add_population(sp.lif(Vthres=1e9), 5)
+    adj = sp.adj_list()
+    for a, b in [(0, 0), (0, 1), (0, 3), (1, 3), (2, 4)]:
+        adj.connect(a, b)
+    net.connect(S, D, adj, 1, sp.fixed_weight(1.0))
+    net.step()
+    assert D.get_neurons()["V"].tolist() == [1.0, 1.0, 0.0, 2.0, 0.0]
+
+
+def test_csr_custom_adjacency(engine):
+    """test/detail/csr.cpp:25-58: a 3x10 adj_list keeps sorted neighbour lists per source."""
+    sp = engine
+    net = sp.snn(1, 1, [1337])
+    S = net.add_population(sp.poisson(), 3)
+    D = net.add_population(sp.lif(), 10)
+    adj = sp.adj_list()
+    for a, b in [(0, 9), (0, 0), (2, 2), (0, 7), (2, 1), (0, 2)]:
+        adj.connect(a, b)
+    c = net.connect(S, D, adj, 1, sp.fixed_weight(0.0))
+    off, nb = net.csr(c)
+    assert off.tolist() == [0, 4, 4, 6]
+    assert nb.tolist() == [0, 2, 7, 9, 1, 2]
+
+
+def test_empty_and_zero_sized(engine):
+    sp = engine
+    net = sp.snn(1e-4, 15e-4, [3])
+    P = net.add_population(sp.poisson(), 0)
+    E = net.add_population(sp.lif(), 0)
+    F = net.add_population(sp.lif(), 5)
+    net.connect(P, E, sp.fixed_probability(0.5), 15e-4, sp.fixed_weight(1.0))
+    net.connect(P, F, sp.fixed_probability(0.5), 15e-4, sp.fixed_weight(1.0))
+    net.run(40)
+    assert net.spikes(P, 0).size == 0 and net.spikes(F, 3).size == 0
+    assert net.events == 0
+
+
+def test_events_equal_row_lengths(engine):
+    """Synaptic events = sum over delivered spikes of their CSR row lengths."""
+    sp = engine
+    net, pops = sp.brunel(6000, 0.05, 5)
+    raster = net.run_record(200)
+    csr = [net.csr(c)[0] for c in range(6)]
+    src = [0, 0, 1, 1, 2, 2]
+    expect = 0
+    for row in raster:
+        for c in range(6):
+            s = row[src[c]]
+            expect += int(np.sum(csr[c][s + 1] - csr[c][s]))
+    assert net.events == expect
+
+
+def test_errors_follow_the_reference(engine):
+    sp = engine
+    net = sp.snn(1e-4, 15e-4, [1])
+    P = net.add_population(sp.poisson(), 10)
+    E = net.add_population(sp.lif(), 10)
+    with pytest.raises(sp.LogicError, match=r"Assertion failed \(snn.h:35\).*at least 1dt"):
+        net.connect(P, E, sp.fixed_probability(0.1), 0.0, sp.fixed_weight(1.0))
+    with pytest.raises(sp.LogicError, match="may not exceed the maximum delay"):
+        net.connect(P, E, sp.fixed_probability(0.1), 16e-4, sp.fixed_weight(1.0))
+    with pytest.raises(sp.LogicError, match=r"0 <= p && p <= 1"):
+        net.connect(P, E, sp.fixed_probability(1.5), 15e-4, sp.fixed_weight(1.0))
+    with pytest.raises(sp.LogicError, match="stateful"):
+        net.connect(E, P, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(1.0))
+    net.connect(P, E, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(1.0))
+    with pytest.raises(sp.LogicError, match="0 <= age"):
+        net.spikes(P, 0)
+    net.step()
+    with pytest.raises(sp.LogicError, match="0 <= age"):
+        net.spikes(P, 1)
+    with pytest.raises(sp.SpiceError):
+        net.set_mode(sp.MODE_ATOMIC)
+    with pytest.raises(sp.LogicError, match="stateful"):
+        P.get_neurons()
+    X = sp.snn(1, 1, [1])
+    ext = X.add_population(sp.external_input(), 4)
+    with pytest.raises(sp.LogicError, match="ascending"):
+        X.set_external_input(ext, [[2, 1]])
+
+
+def _rate_cv(raster, pop, size, dt):
+    spikes = [np.asarray(row[pop]) for row in raster]
+    total = sum(len(s) for s in spikes)
+    rate = total / (size * len(raster) * dt)
+    last = np.full(size, -1, dtype=np.int64)
+    isis = []
+    for t, s in enumerate(spikes):
+        prev = last[s]
+        ok = prev >= 0
+        isis.append(t - prev[ok])
+        last[s] = t
+    isi = np.concatenate(isis).astype(np.float64) if isis else np.zeros(1)
+    return rate, isi.std() / isi.mean()
+
+
+def test_atomic_mode_statistics(engine):
+    """Atomic mode (float atomics, order-dependent rounding) keeps the firing statistics: per-
+    population rate and ISI CV within 1% of the deterministic path over 10 seeds."""
+    sp = engine
+    res = {0: [], 1: []}
+    for mode in (0, 1):
+        for seed in range(1, 11):
+            net, pops = sp.brunel(20000, 0.1, seed, mode=mode)
+            raster = net.run_record(2000)
+            res[mode].append([_rate_cv(raster, k, pops[k].size(), 1e-4) for k in (1, 2)])
+    det, atom = np.array(res[0]).mean(axis=0), np.array(res[1]).mean(axis=0)
+    rel = np.abs(atom - det) / det
+    assert (rel < 0.01).all(), (det, atom, rel)

@@ -1,0 +1,230 @@
+"""CPU tests: the oracle against the reference's golden vectors (no GPU needed).
+
+The golden fixtures in tests/golden/ were produced by the reference itself (make_golden.py runs
+spice2's own sources compiled by oracle/Makefile).  These tests pin the CPU restatement to them;
+the GPU engine is then checked against the restatement and the same fixtures (test_gpu_*.py).
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def _golden(name):
+    return np.load(os.path.join(GOLDEN, name))
+
+
+@pytest.mark.parametrize("seed", [1, 7, 1337])
+def test_rng_and_seed_chain(oracle_lib, seed):
+    o = oracle_lib
+    g = _golden("rng.npz")
+    n = len(g[f"draws_{seed}"])
+    chain = np.array(o.seed_chain([seed], n), dtype=np.uint64)
+    assert np.array_equal(chain, g[f"chain_{seed}"])
+    s0 = tuple(int(x) for x in chain[0])
+    assert np.array_equal(o.xoroshiro_draws(s0, n), g[f"draws_{seed}"])
+    # exponential_distribution<double>(499) and generate_canonical<float> on the same stream
+    import ctypes as C
+    st = (C.c_uint64 * 2)(*s0)
+    ex = np.array([o.lib().spo_exponential(499.0, st) for _ in range(n)])
+    assert np.array_equal(ex.view(np.uint64), g[f"exp_{seed}"].view(np.uint64))
+    canon = np.array([o.lib().spo_canonical_f32(int(u)) for u in g[f"draws_{seed}"]], dtype=np.float32)
+    assert np.array_equal(canon.view(np.uint32), g[f"canon_{seed}"].view(np.uint32))
+
+
+def test_kahan_dt_sequence(oracle_lib):
+    g = _golden("rng.npz")
+    k = oracle_lib.kahan_dts(len(g["kahan_1337"]))
+    assert np.array_equal(k.view(np.uint32), g["kahan_1337"].view(np.uint32))
+
+
+def test_kahan_known_answer(oracle_lib):
+    """test/util/numeric.cpp:9-28: 1000 x 0.001 sums to exactly 1 with compensation."""
+    import ctypes as C
+    o = oracle_lib
+    k = o._Kahan(0.0, 0.0)
+    deltas = np.float32(0)
+    for _ in range(1000):
+        # no reset: the reference test uses kahan_sum directly
+        y = np.float32(0.001) - np.float32(k.c)
+        t = np.float32(k.sum) + y
+        k.c = float((t - np.float32(k.sum)) - y)
+        k.sum = float(t)
+        deltas += y
+    assert np.float32(k.sum) == np.float32(1.0)
+    assert deltas == np.float32(1.0)
+
+
+def test_csr_small_cases(oracle_lib):
+    o = oracle_lib
+    g = _golden("csr_small.npz")
+    keys = sorted({k[4:] for k in g.files if k.startswith("off_")})
+    assert len(keys) >= 8
+    for key in keys:
+        s, d, p, sd = key.split("_")
+        s, d, p, sd = int(s), int(d), float(p), int(sd)
+        off, nb, _ = o.fp_generate(s, d, p, o.seed_from_list([sd]))
+        assert np.array_equal(off, g["off_" + key]), key
+        assert np.array_equal(nb, g["nb_" + key]), key
+        if s:
+            assert o.fp_max_degree(d, p) == int(g["md_" + key][0]), key
+
+
+def test_csr_checksums_n20000(oracle_lib):
+    o = oracle_lib
+    cs = json.load(open(os.path.join(GOLDEN, "brunel_csr_checksums.json")))["N=20000,p=0.1"]["1337"]
+    net, _ = o.brunel(20000, 0.1, 1337)
+    sizes = [10000, 8000, 2000]
+    for c, (sp, dp, nsyn, h) in enumerate(cs):
+        n = net.csr(c)
+        off = np.zeros(sizes[sp] + 1, dtype=np.int64)
+        nb = np.zeros(n, dtype=np.int32)
+        o.lib().spo_conn_csr(net.h, c, off.ctypes.data, nb.ctypes.data)
+        assert n == nsyn
+        assert o.csr_checksum(off, nb) == h
+
+
+def _raster_matches(net, pops, counts, idx):
+    pos = 0
+    for t in range(counts.shape[0]):
+        net.step()
+        for k, pk in enumerate(pops):
+            c = counts[t, k]
+            got = net.spikes(pk, 0)
+            assert np.array_equal(got, idx[pos:pos + c]), f"step {t} population {k}"
+            pos += c
+
+
+@pytest.mark.parametrize("name", ["brunel_n20000.npz", "brunel_n5000.npz"])
+def test_brunel_raster_and_state(oracle_lib, name):
+    o = oracle_lib
+    g = _golden(name)
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = o.brunel(N, float(g["p"][0]), seed)
+    _raster_matches(net, pops, g["counts"], g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(net.state(pops[k], 0).view(np.uint32), g[f"V{k}"].view(np.uint32))
+        assert np.array_equal(net.state(pops[k], 3), g[f"T{k}"])
+
+
+def test_readme_raster_head():
+    """README.md:110-116 prints the JSON raster of samples/brunel.cpp (I, E, P with offsets):
+    the first two steps begin [10533,11015,11209,...] and [10310,11115,11884,...]."""
+    g = _golden("brunel_n20000.npz")
+    counts, idx = g["counts"], g["idx"]
+    rows, pos = [], 0
+    for t in range(2):
+        per = []
+        for k in range(3):
+            per.append(idx[pos:pos + counts[t, k]])
+            pos += counts[t, k]
+        P, E, I = per
+        rows.append(list(I) + [x + 2000 for x in E] + [x + 10000 for x in P])
+    assert rows[0][:3] == [10533, 11015, 11209]
+    assert rows[1][:3] == [10310, 11115, 11884]
+
+
+def test_mixed_network(oracle_lib):
+    o = oracle_lib
+    g = _golden("mixed_net.npz")
+    net, pops, pairs = o.mixed_net()
+    assert np.array_equal(np.array(pairs, dtype=np.int32), g["pairs"])
+    _raster_matches(net, pops, g["counts"], g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(net.state(pops[k], 0).view(np.uint32), g[f"V{k}"].view(np.uint32))
+        assert np.array_equal(net.state(pops[k], 3), g[f"T{k}"])
+
+
+def test_oracle_errors(oracle_lib):
+    o = oracle_lib
+    net = o.Net(1e-4, 15e-4, [1])
+    P = net.add_population(o.POISSON, 10, (20.0,))
+    E = net.add_population(o.LIF, 10)
+    with pytest.raises(RuntimeError, match="The delay must be at least 1dt"):
+        net.connect(P, E, 0.1, 0.0, 1.0)
+    with pytest.raises(RuntimeError, match="may not exceed the maximum delay"):
+        net.connect(P, E, 0.1, 16e-4, 1.0)
+    with pytest.raises(RuntimeError, match="0 <= age"):
+        net.spikes(P, 0)
+
+
+# ---- jump-ahead math (the method the GPU uses to reproduce serial streams in parallel) --------
+def _charpoly():
+    """Characteristic polynomial of the xoroshiro128+ transition via Berlekamp-Massey."""
+    M = (1 << 64) - 1
+    s0, s1 = 0x0123456789ABCDEF, 0xFEDCBA9876543210
+    bits = []
+    for _ in range(256):
+        bits.append(s0 & 1)
+        t = s0 ^ s1
+        s0 = (((s0 << 24) | (s0 >> 40)) & M) ^ t ^ ((t << 16) & M)
+        s1 = ((t << 37) | (t >> 27)) & M
+    C, B, L, m = [1] + [0] * 256, [1] + [0] * 256, 0, 1
+    for n in range(256):
+        d = bits[n]
+        for i in range(1, L + 1):
+            d ^= C[i] & bits[n - i]
+        if not d:
+            m += 1
+            continue
+        T = C[:]
+        for i in range(0, 257 - m):
+            C[i + m] ^= B[i]
+        if 2 * L <= n:
+            L, B, m = n + 1 - L, T, 1
+        else:
+            m += 1
+    assert L == 128
+    return sum(C[128 - k] << k for k in range(128))
+
+
+def _xpow_mod(n, P):
+    def mulmod(a, b):
+        r = 0
+        for i in range(127, -1, -1):
+            carry = r >> 127
+            r = (r << 1) & ((1 << 128) - 1)
+            if carry:
+                r ^= P
+            if (b >> i) & 1:
+                r ^= a
+        return r
+    res, base = 1, 2
+    while n:
+        if n & 1:
+            res = mulmod(res, base)
+        base = mulmod(base, base)
+        n >>= 1
+    return res
+
+
+@pytest.mark.parametrize("n", [1, 31, 32, 1000, 65536, 123457])
+def test_jump_ahead_equals_stepping(oracle_lib, n):
+    o = oracle_lib
+    P = _charpoly()
+    poly = _xpow_mod(n, P)
+    start = o.seed_from_list([1337])
+    jumped = o.xoroshiro_jump(start, (poly & ((1 << 64) - 1), poly >> 64))
+    # stepping n times: the (n+1)-th draw equals s0 + s1 of the jumped state
+    draws = o.xoroshiro_draws(start, n + 1)
+    assert (jumped[0] + jumped[1]) & ((1 << 64) - 1) == int(draws[n])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+def test_oracle_vs_live_reference(oracle_lib):
+    """The restatement against the reference binary on a fresh configuration."""
+    o = oracle_lib
+    res = o.run_reference_net(o.brunel_spec(3000, 0.07, 99, 400))
+    st, _, _ = o.reference_states(res, [1, 2])
+    net, pops = o.brunel(3000, 0.07, 99)
+    for t in range(400):
+        net.step()
+        for k in range(3):
+            assert np.array_equal(net.spikes(pops[k], 0), res["raster"][t][k])
+        assert net.last_dt == res["dt"][t]
+    for k in (1, 2):
+        assert np.array_equal(net.state(pops[k], 0).view(np.uint32), st[k][0].view(np.uint32))
