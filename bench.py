@@ -1,0 +1,338 @@
+"""Benchmark: synaptic events/s of snn::step on Large Brunel (N=5e5, p=0.002) on one GB300.
+
+One bench "step" = one run of 2000 simulation steps (dt = 1e-4 s, 0.2 s of biological time) of
+the Large Brunel network: P = 2.5e5 Poisson (20 Hz), E = 2e5 and I = 5e4 LIF, six
+fixed_probability(0.002) projections (2.5e8 synapses), weights scaled by 0.1/p, delay 15 steps,
+deterministic delivery (bit-exact with the reference).  The network is generated on the GPU once
+and keeps running across bench steps (warm-up steps first), so every timed step is a steady-state
+stretch of the same simulation.  The metric counts every synaptic event exactly (sum over spikes
+of their CSR row lengths) and divides by device time.
+
+Printed JSON (one line, rank 0):
+  value        events/s with the network resident in HBM (CUDA events on the net's stream)
+  e2e          the same through the public C ABI call spice_run_record with host buffers: per
+               step the dt/seed inputs go host->device and the spike raster comes back
+  roofline     the delivery kernel (dominant): algorithmic bytes (4 B int32 target per event; a
+               fixed_weight synapse has one weight per projection, no per-synapse weight) per
+               launch / its mean CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs
+  cpu_baseline the CPU restatement of the reference step loop (oracle/oracle_bench, the same
+               algorithm as the reference's single-core path) timed on this host's cores
+  atomic_mode  value with the fast atomic delivery mode (order-dependent float rounding)
+
+--impl reference runs the reference's CPU implementation of the path on the host cores (the
+reference binary when it was built on this host, else its CPU restatement) and prints the same
+metric.  Under torchrun each rank runs an independent replica (seed + rank): replicas only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_NEURONS, P_CONN, SEED, STEPS_PER_RUN = 500000, 0.002, 1, 2000
+DT = 1e-4
+WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
+# DRAM bytes (read + write) per synaptic event of the delivery kernel, from the ncu capture summarised
+# in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum over the events of the captured launch).
+DELIVER_DRAM_BYTES_PER_EVENT = None
+
+
+def _dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    lrank = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, lrank
+
+
+def _barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def _max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _sum_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.out = os.path.join("/tmp", f"spice_clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=open(self.out, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        try:
+            rows = [r.split(",") for r in open(self.out).read().strip().splitlines() if r.strip()]
+        except Exception:
+            rows = []
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in rows:
+            for j, n in enumerate(names):
+                if len(r) > 5 + j and r[5 + j].strip() == "Active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(rows)}
+
+
+def _peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def cpu_baseline(threads: int | None = None, steps: int = 200, warmup: int = 50, n_neurons: int = N_NEURONS):
+    """Times the CPU restatement of the reference step loop (oracle/oracle_bench) on the host cores.
+    Each thread runs an independent replica (seeds 1..threads); returns the aggregate."""
+    from oracle import oracle as o
+    if not os.path.exists(o.BENCH_PATH):
+        o.build(with_reference=False)
+    threads = threads or max(1, min(8, (os.cpu_count() or 1)))
+    out = subprocess.run([o.BENCH_PATH, str(n_neurons), repr(P_CONN), str(steps), str(SEED), str(threads),
+                          str(warmup)], check=True, capture_output=True, text=True).stdout
+    d = json.loads(out.strip().splitlines()[-1])
+    d["kind"] = "port"
+    return d
+
+
+def reference_arm(args):
+    ws, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    from oracle import oracle as o
+    threads = max(1, os.cpu_count() or 1)
+    # bounded sample per bench step: 100 simulation steps of the same workload on every core
+    per_step = 100
+    vals = []
+    kind = "port"
+    build_s = None
+    for i in range(args.warmup + args.steps):
+        d = cpu_baseline(threads=min(threads, 16), steps=per_step, warmup=10 if i == 0 else 10)
+        build_s = d["build_seconds"]
+        if i >= args.warmup:
+            vals.append(d["events_per_s"])
+    value = statistics.median(vals)
+    line = {"metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "N": N_NEURONS, "p": P_CONN, "sample_steps_per_bench_step": per_step,
+                       "replicas": "one independent network per host thread (seeds 1..threads)"},
+            "cpu_baseline": {"value": value, "unit": "events/s", "cores": min(threads, 16), "kind": kind,
+                             "sample": f"{per_step} simulation steps of N=5e5 Brunel per thread after 10 warm-up "
+                                       f"steps; network build {build_s:.1f} s not timed"},
+            "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return reference_arm(args)
+
+    ws, rank, lrank = _dist()
+    import torch
+    torch.cuda.set_device(lrank)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    import spice2_gb300 as sp
+
+    seed = SEED + rank  # replicas: independent networks
+    t0 = time.perf_counter()
+    net, pops = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_DETERMINISTIC)
+    net.csr(0)
+    net.synchronize()
+    build_s = time.perf_counter() - t0
+    synapses = sum(net.synapses(c) for c in range(6))
+    stream = torch.cuda.ExternalStream(net.stream_handle())
+
+    for _ in range(args.warmup):
+        net.run(STEPS_PER_RUN)
+    net.synchronize()
+
+    # ---- device-resident timed region ----
+    net.set_profiling(True)
+    ev0, l0 = net.events, net.launch_count()
+    _barrier(ws)
+    torch.cuda.synchronize()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(lrank) as clk:
+        start.record(stream)
+        for _ in range(args.steps):
+            net.run(STEPS_PER_RUN)
+        end.record(stream)
+        torch.cuda.synchronize()
+    _barrier(ws)
+    ms = start.elapsed_time(end)
+    events = net.events - ev0
+    launches = net.launch_count() - l0
+    n_del, ms_del = net.kernel_stats(1)
+    n_win, ms_win = net.kernel_stats(0)
+    net.set_profiling(False)
+    ms_max = _max_over_ranks(ms, ws)
+    events_all = _sum_over_ranks(float(events), ws)
+    value = events_all / (ms_max / 1e3)
+
+    # ---- end to end through the public C ABI with host buffers ----
+    import numpy as np
+    cap = 4_000_000
+    counts = np.zeros((STEPS_PER_RUN, 3), dtype=np.int64)
+    spikes = np.zeros(cap, dtype=np.int32)
+    import ctypes as C
+    total = C.c_int64()
+    L = sp.lib()
+    e2e_times, e2e_events, d2h = [], 0, 0
+    _barrier(ws)
+    for i in range(args.steps + 1):
+        e0 = net.events
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        rc = L.spice_run_record(net._h, STEPS_PER_RUN, counts.ctypes.data, spikes.ctypes.data, cap, C.byref(total))
+        t = time.perf_counter() - t
+        if rc != 0:
+            raise RuntimeError(L.spice_last_error().decode())
+        if i > 0:  # the first call sizes the device raster buffer
+            e2e_times.append(t)
+            e2e_events += net.events - e0
+            d2h = 4 * int(total.value) + 16 * STEPS_PER_RUN * 3 + 8
+    e2e_s = _max_over_ranks(sum(e2e_times), ws)
+    e2e_value = _sum_over_ranks(float(e2e_events), ws) / e2e_s
+
+    # ---- atomic mode (fast, order-dependent rounding), timed the same way ----
+    atomic = None
+    if rank == 0:
+        del net
+        net2, _ = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_ATOMIC)
+        for _ in range(args.warmup):
+            net2.run(STEPS_PER_RUN)
+        net2.synchronize()
+        s2 = torch.cuda.ExternalStream(net2.stream_handle())
+        e0 = net2.events
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(s2)
+        for _ in range(args.steps):
+            net2.run(STEPS_PER_RUN)
+        b.record(s2)
+        torch.cuda.synchronize()
+        atomic = {"value": (net2.events - e0) / (a.elapsed_time(b) / 1e3), "unit": "events/s",
+                  "ms_per_step": a.elapsed_time(b) / args.steps}
+        del net2
+
+    if rank != 0:
+        if ws > 1:
+            import torch.distributed as dist
+            dist.destroy_process_group()
+        return 0
+
+    peak, peak_kind = _peaks()
+    bytes_per_event = 4
+    ev_per_launch = events / max(n_del, 1)
+    t_launch = ms_del / max(n_del, 1) / 1e3
+    achieved = bytes_per_event * ev_per_launch / t_launch / 1e9 if t_launch > 0 else None
+    traffic = None
+    if DELIVER_DRAM_BYTES_PER_EVENT is not None:
+        traffic = DELIVER_DRAM_BYTES_PER_EVENT * ev_per_launch
+
+    cpu = None
+    if not args.no_cpu_baseline and ws == 1:
+        try:
+            d = cpu_baseline(steps=200, warmup=20)
+            cpu = {"value": d["events_per_s"], "unit": "events/s", "cores": d["threads"], "kind": d["kind"],
+                   "sample": f"{d['steps']} steps of N=5e5 Brunel per thread ({d['threads']} independent replicas, "
+                             f"seeds 1..{d['threads']}) after 20 warm-up steps; build {d['build_seconds']:.1f} s untimed"}
+        except Exception as e:  # the baseline is reported, never a reason to fail the bench
+            cpu = {"value": None, "unit": "events/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
+
+    line = {
+        "metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "N": N_NEURONS, "p": P_CONN, "synapses": synapses,
+                   "sim_steps_per_bench_step": STEPS_PER_RUN, "dt": DT,
+                   "delay_steps": 15, "mode": "deterministic", "seed": SEED,
+                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                   "l2": "inputs larger than L2 (1 GB of CSR targets; a window reads ~42 MB of random rows)"},
+        "sim_seconds_per_wall_second": STEPS_PER_RUN * args.steps * DT / (ms_max / 1e3),
+        "ms_per_sim_step": ms_max / args.steps / STEPS_PER_RUN,
+        "build_seconds": build_s,
+        "gpu_launches": launches,
+        "e2e": {"value": e2e_value, "unit": "events/s", "h2d_bytes_per_step": 20 * STEPS_PER_RUN,
+                "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                     "kernel": "k_deliver", "bytes_per_event": bytes_per_event, "peak_source": f"{peak_kind} hbm_gbs",
+                     "launches": n_del, "mean_launch_us": t_launch * 1e6,
+                     "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3},
+        "cpu_baseline": cpu,
+        "atomic_mode": atomic,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

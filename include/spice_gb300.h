@@ -91,6 +91,17 @@ int spice_set_external_input(spice_net* net, int pop, int nsteps, const int32_t*
                              const int32_t* indices);
 
 int spice_set_mode(spice_net* net, int mode);
+
+/* Launch-shape knobs of the delivery kernel (no counterpart in the reference; may be changed at
+ * any time between steps): shared memory per target tile in bytes, and threads per delivery CTA.
+ * Results do not depend on them; spice2_gb300.autotune picks them per network. */
+enum {
+	SPICE_TUNE_TILE_BYTES      = 0, /* shared memory per target tile                          */
+	SPICE_TUNE_DELIVER_THREADS = 1, /* threads per delivery CTA                               */
+	SPICE_TUNE_DELIVER_PARTS   = 2, /* CTAs sharing one (input slot, tile)                    */
+	SPICE_TUNE_DELIVER_ALGO    = 3, /* 0: warp-flattened sub-rows, 1: one thread per spike   */
+};
+int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's
  * minimum connection delay, the largest value that keeps the reference's semantics). */
 int spice_set_window(spice_net* net, int max_window);
@@ -134,6 +145,9 @@ int spice_kernel_stats(spice_net* net, int kind, int64_t* launches_out, double* 
 /* Number of kernels this library launched on the net's stream so far. */
 int spice_launch_count(spice_net* net, int64_t* launches_out);
 
+/* The cudaStream_t the net launches on (for callers that order their own work or time it with
+ * CUDA events on the same stream). */
+int spice_get_stream(spice_net* net, void** stream_out);
 int spice_synchronize(spice_net* net);
 const char* spice_last_error(void);
 

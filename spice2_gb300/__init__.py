@@ -90,6 +90,8 @@ def _load():
         "spice_set_profiling": [vp, i32],
         "spice_kernel_stats": [vp, i32, P(i64), P(f64)],
         "spice_launch_count": [vp, P(i64)],
+        "spice_get_stream": [vp, P(vp)],
+        "spice_set_tuning": [vp, i32, i64],
         "spice_synchronize": [vp],
     }
     for name, args in sig.items():
@@ -295,6 +297,18 @@ class snn:
     def set_window(self, w: int):
         _check(lib().spice_set_window(self._h, w))
 
+    def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
+                   deliver_parts: int | None = None, deliver_algo: int | None = None):
+        """Delivery launch shape (any time between steps); results are independent of it."""
+        if tile_bytes is not None:
+            _check(lib().spice_set_tuning(self._h, 0, int(tile_bytes)))
+        if deliver_threads is not None:
+            _check(lib().spice_set_tuning(self._h, 1, int(deliver_threads)))
+        if deliver_parts is not None:
+            _check(lib().spice_set_tuning(self._h, 2, int(deliver_parts)))
+        if deliver_algo is not None:
+            _check(lib().spice_set_tuning(self._h, 3, int(deliver_algo)))
+
     # stepping
     def step(self):
         _check(lib().spice_step(self._h))
@@ -360,6 +374,11 @@ class snn:
             raise LogicError(EINVAL, "state array must have one entry per neuron")
         _check(lib().spice_set_state(self._h, pop.id, fld, v.ctypes.data))
 
+    def synapses(self, conn: int) -> int:
+        src, syn = C.c_int64(), C.c_int64()
+        _check(lib().spice_conn_size(self._h, conn, C.byref(src), C.byref(syn)))
+        return syn.value
+
     def csr(self, conn: int):
         src, syn = C.c_int64(), C.c_int64()
         _check(lib().spice_conn_size(self._h, conn, C.byref(src), C.byref(syn)))
@@ -384,6 +403,12 @@ class snn:
 
     def synchronize(self):
         _check(lib().spice_synchronize(self._h))
+
+    def stream_handle(self) -> int:
+        """The raw cudaStream_t of the net (e.g. for torch.cuda.ExternalStream)."""
+        v = C.c_void_p()
+        _check(lib().spice_get_stream(self._h, C.byref(v)))
+        return v.value or 0
 
 
 def brunel(N: int, p: float, seed: int = 1337, dt: float = 1e-4, delay: float = 15e-4, mode: int = MODE_DETERMINISTIC):

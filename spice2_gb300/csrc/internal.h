@@ -22,9 +22,10 @@ namespace spice_gb300 {
 
 constexpr int kMaxPops    = 64;
 constexpr int kMaxConns   = 256;
-constexpr int kMaxGroups  = 8;   // distinct consecutive (field, weight) runs per target population
+constexpr int kMaxGroups  = 4;   // distinct consecutive (field, weight) runs per target population
 constexpr int kMaxWindow  = 64;  // steps fused into one neuron-update launch
 constexpr int kBasis      = 128; // states per step basis
+constexpr int kJumpTable  = 16 * 256;  // u128 entries of one step's jump table
 constexpr int kPoissonChunk = 32; // consecutive Poisson neurons per thread (one jump each)
 
 enum Model { POISSON = 0, LIF = 1, LIF_COND = 2, EXTERNAL = 3 };
@@ -59,6 +60,12 @@ struct PopDev {
 	int group_field[kMaxGroups];
 	float group_weight[kMaxGroups];
 	int field_slot[3];   // atomic mode: index of field f in the F per-neuron sums (-1: unused)
+	// tiled delivery: targets are accumulated in shared-memory tiles of `tile` neurons
+	int tile;            // neurons per tile
+	int ntiles;
+	int in_begin, in_end;  // this population's incoming connections in the by-target order
+	int zero_inputs;     // 1: the input ring is accumulated (mixed delays), consumers clear it;
+	                     // 0: each slot is fully overwritten by one delivery, no clearing needed
 	const u128* chunk_poly;  // POISSON: x^(draw_offset + 32 c) mod P for chunk c
 	// EXTERNAL: cyclic train
 	const int32_t* ext_counts;
@@ -83,6 +90,7 @@ struct ConnDev {
 	int W, word;              // words per neuron, word of this connection's group
 	uint32_t inc;             // 1 << group_shift
 	int F, fslot;             // atomic: sums per neuron, index of this connection's field
+	const int64_t* bounds;    // [src_size][ntiles of dst + 1]: row positions where each tile starts
 };
 
 struct Pop {
@@ -133,7 +141,7 @@ struct spice_net {
 	int32_t* d_counts  = nullptr;  // [K][npop] spikes per window step and population
 	float* d_dt        = nullptr;  // [run capacity]
 	spice_gb300::u128* d_seeds = nullptr;  // [run capacity]
-	spice_gb300::u128* d_basis = nullptr;  // [run capacity][128]
+	spice_gb300::u128* d_tables = nullptr;  // [run capacity][16][256] jump tables
 	int64_t run_cap    = 0;
 	spice_gb300::PopDev* d_pops   = nullptr;
 	spice_gb300::ConnDev* d_conns = nullptr;
@@ -158,4 +166,11 @@ struct spice_net {
 	std::vector<spice_gb300::PendingGen> gen_pending;
 	std::vector<int64_t> ext_t_set;  // per population: step at which its external train was set
 	int parity = 0;                  // which half of d_counts the next window writes
+	spice_gb300::ConnDev* d_conns_by_dst = nullptr;  // connections grouped by target population
+	std::vector<int> by_dst;         // connection ids in that order
+	int tile_bytes = 24 * 1024;      // shared memory per delivery tile (tunable)
+	int deliver_threads = 256;       // threads per delivery CTA (tunable)
+	int deliver_parts = 1;           // CTAs per (slot, tile) (tunable)
+	int deliver_algo = 1;            // delivery work mapping (tunable)
+	int dmin = 1, dmax = 1;          // connection delays in steps
 };

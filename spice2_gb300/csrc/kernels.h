@@ -33,8 +33,8 @@ cudaError_t scan_row_lengths(cudaStream_t stream, const int32_t* lens, int64_t n
 cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const int64_t* nsyn, int nconn,
                          int64_t dst_size, uint32_t* scratch, uint32_t* max_out);
 
-// basis[t][i] = T^i(seed_t) for t < nsteps.
-cudaError_t launch_basis(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* basis);
+// Jump tables of steps t < nsteps: tables[t][g][m] = XOR of T^(8g+q)(seed_t) over the bits q of m.
+cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* tables);
 
 struct WindowArgs {
 	int64_t t0;        // absolute step of the window's first step
@@ -47,10 +47,11 @@ struct WindowArgs {
 	int mode;
 	const PopDev* pops;
 	const float* dts;     // dt of steps t0 .. t0+K-1
-	const u128* basis;    // basis of step t0 (then t0+1, ...)
+	const u128* tables;   // jump tables of step t0 (then t0+1, ...)
 	int32_t* counts;      // [K][npop] spikes per step and population (window parity buffer)
 	int blk_begin[kMaxPops + 1];
-	int blk_kind[kMaxPops];      // 0: per-neuron window CTAs, 1: Poisson step CTAs, 2: external
+	int blk_kind[kMaxPops];      // 0: per-neuron window CTAs, 1: Poisson step CTAs, 2: external,
+	                             // 3: per-neuron CTAs of a LIF whose inputs all add to V (16-bit counts)
 	int blk_per_step[kMaxPops];  // Poisson / external: CTAs per step
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
 };
@@ -63,14 +64,25 @@ struct DeliverArgs {
 	int nconn;
 	int npop;
 	int mode;
-	const ConnDev* conns;
+	const ConnDev* conns;    // grouped by target population (PopDev::in_begin/in_end)
 	const PopDev* pops;
 	const int32_t* counts;   // [K][npop] of this window
 	int32_t* counts_next;    // the other parity buffer, zeroed here
 	int counts_next_len;
 	unsigned long long* events;
+	int64_t slot_lo;         // first input slot the window's spikes reach: t0 + dmin - 1
+	int nslots;              // K + dmax - dmin
+	int ntiles_total;
+	int tile_begin[kMaxPops + 1];  // prefix over populations of their tile counts
+	int smem_bytes;
+	int parts;               // CTAs sharing one (slot, tile); > 1 flushes with reductions
+	int algo;                // 0: warp-flattened sub-rows, 1: one thread per spike
 };
-cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int nblocks);
+// One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.
+cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int threads);
+// bounds[s][t] = position in row s of the first target >= t * tile (t = 0..ntiles).
+cudaError_t launch_tile_bounds(cudaStream_t stream, const int64_t* off, const int32_t* nb, int64_t rows, int tile,
+                               int ntiles, int64_t* bounds);
 
 // Applies the inputs waiting in ring slot (t - 1) to the state and clears them.
 cudaError_t launch_apply_pending(cudaStream_t stream, const PopDev* pops, int npop_dev, const int* stateful,

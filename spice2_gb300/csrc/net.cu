@@ -14,7 +14,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/spice_gb300.h"
+#include "spice_gb300.h"
 #include "internal.h"
 #include "kernels.h"
 
@@ -46,7 +46,7 @@ int pre_failed(const char* file_line, const char* cond) {
 		if (r_ != SPICE_OK) return r_; \
 	} while (0)
 
-constexpr int64_t kRunCap = 8192;  // steps of dt / seed / basis prepared per chunk
+constexpr int64_t kRunCap = 1024;  // steps of dt / seed / jump tables prepared per chunk
 
 template <class T>
 int dalloc(spice_net* n, T** p, size_t count, bool zero = true) {
@@ -411,6 +411,57 @@ int generate_pending(spice_net* n) {
 	return SPICE_OK;
 }
 
+// Tile sizes of the delivery kernel, the by-target connection order and the per-row positions
+// where each tile starts.  Called at preparation and again when the launch shape is re-tuned.
+int setup_tiles(spice_net* n, bool first) {
+	int const np = (int)n->pops.size();
+	// tiled delivery: tile sizes, the by-target connection order, per-row tile start positions
+	n->dmin = (int)n->max_delay;
+	n->dmax = 1;
+	for (auto const& c : n->conns) {
+		n->dmin = std::min(n->dmin, c.d.delay);
+		n->dmax = std::max(n->dmax, c.d.delay);
+	}
+	if (n->conns.empty()) n->dmin = n->dmax = 1;
+	std::vector<int> by_dst;
+	for (int pi = 0; pi < np; pi++) {
+		PopDev& d   = n->pops[pi].d;
+		d.in_begin  = (int)by_dst.size();
+		int dfirst = -1;
+		bool mixed = false;
+		for (int ci = 0; ci < (int)n->conns.size(); ci++)
+			if (n->conns[ci].d.dst == pi) {
+				by_dst.push_back(ci);
+				if (dfirst < 0) dfirst = n->conns[ci].d.delay;
+				mixed |= n->conns[ci].d.delay != dfirst;
+			}
+		d.in_end      = (int)by_dst.size();
+		// slots are overwritten by one delivery CTA unless delays differ or tiles are split
+		d.zero_inputs = (mixed || n->deliver_parts > 1) ? 1 : 0;
+		int const width = n->mode == SPICE_MODE_DETERMINISTIC ? d.W : d.F;
+		int tile        = n->tile_bytes / (4 * std::max(width, 1));
+		tile            = std::max(32, tile / 32 * 32);
+		d.tile          = tile;
+		d.ntiles        = (d.in_end > d.in_begin && d.size > 0) ? (int)((d.size + tile - 1) / tile) : 0;
+	}
+	for (auto& c : n->conns) {
+		ConnDev& d      = c.d;
+		PopDev const& T = n->pops[d.dst].d;
+		int64_t* bnd    = nullptr;
+		if (!first && d.bounds) {
+			CUDA_TRY(cudaStreamSynchronize(n->stream));
+			cudaFree((void*)d.bounds);
+			n->allocations.erase(std::find(n->allocations.begin(), n->allocations.end(), (void*)d.bounds));
+		}
+		TRY(dalloc(n, &bnd, (size_t)d.src_size * (T.ntiles + 1), false));
+		CUDA_TRY(launch_tile_bounds(n->stream, d.off, d.nb, d.src_size, T.tile, T.ntiles, bnd));
+		n->launches++;
+		d.bounds = bnd;
+	}
+	n->by_dst = by_dst;
+	return SPICE_OK;
+}
+
 int prepare(spice_net* n) {
 	if (n->prepared) return SPICE_OK;
 	TRY(generate_pending(n));
@@ -461,7 +512,7 @@ int prepare(spice_net* n) {
 			int g = last_of_field[c.field];
 			if (g < 0 || memcmp(&d.group_weight[g], &c.weight, sizeof(float)) != 0) {
 				if (d.ngroups >= kMaxGroups)
-					return fail(SPICE_EINVAL, "too many distinct input weights into one population (max 8)");
+					return fail(SPICE_EINVAL, "too many distinct input weights into one population (max 4)");
 				g                 = d.ngroups++;
 				d.group_field[g]  = c.field;
 				d.group_weight[g] = c.weight;
@@ -523,6 +574,7 @@ int prepare(spice_net* n) {
 		else
 			TRY(dalloc(n, &d.acc, (size_t)D * d.size * d.F));
 	}
+	TRY(setup_tiles(n, true));
 	for (auto& c : n->conns) {
 		ConnDev& d      = c.d;
 		PopDev const& S = n->pops[d.src].d;
@@ -545,10 +597,17 @@ int prepare(spice_net* n) {
 	for (auto& c : n->conns) hc.push_back(c.d);
 	if (np) CUDA_TRY(cudaMemcpy(n->d_pops, hp.data(), sizeof(PopDev) * np, cudaMemcpyHostToDevice));
 	if (!hc.empty()) CUDA_TRY(cudaMemcpy(n->d_conns, hc.data(), sizeof(ConnDev) * hc.size(), cudaMemcpyHostToDevice));
+	{
+		std::vector<ConnDev> hb;
+		for (int ci : n->by_dst) hb.push_back(n->conns[ci].d);
+		TRY(dalloc(n, &n->d_conns_by_dst, std::max<size_t>(hb.size(), 1), false));
+		if (!hb.empty())
+			CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
+	}
 	n->run_cap = kRunCap;
 	TRY(dalloc(n, &n->d_dt, kRunCap, false));
 	TRY(dalloc(n, &n->d_seeds, kRunCap, false));
-	if (n->total_draws > 0) TRY(dalloc(n, &n->d_basis, (size_t)kRunCap * kBasis, false));
+	if (n->total_draws > 0) TRY(dalloc(n, &n->d_tables, (size_t)kRunCap * kJumpTable, false));
 	CUDA_TRY(cudaMallocHost(&n->h_dt, sizeof(float) * kRunCap));
 	CUDA_TRY(cudaMallocHost(&n->h_seeds, sizeof(u128) * kRunCap));
 	int64_t maxN = 1;
@@ -574,7 +633,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 		CUDA_TRY(cudaMemcpyAsync(n->d_dt, n->h_dt, sizeof(float) * chunk, cudaMemcpyHostToDevice, n->stream));
 		if (n->total_draws > 0) {
 			CUDA_TRY(cudaMemcpyAsync(n->d_seeds, n->h_seeds, sizeof(u128) * chunk, cudaMemcpyHostToDevice, n->stream));
-			CUDA_TRY(launch_basis(n->stream, n->d_seeds, chunk, n->d_basis));
+			CUDA_TRY(launch_jump_tables(n->stream, n->d_seeds, chunk, n->d_tables));
 			n->launches++;
 		}
 		int64_t j = 0;
@@ -591,7 +650,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			wa.mode   = n->mode;
 			wa.pops   = n->d_pops;
 			wa.dts    = n->d_dt + j;
-			wa.basis  = n->d_basis ? n->d_basis + j * kBasis : nullptr;
+			wa.tables = n->d_tables ? n->d_tables + j * kJumpTable : nullptr;
 			wa.counts = n->d_counts + (size_t)n->parity * n->K * np;
 			int nb = 0;
 			for (int p = 0; p < np; p++) {
@@ -608,7 +667,12 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					int64_t const ns = P.ext_steps;
 					wa.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
 				} else {
-					wa.blk_kind[p] = 0;
+					// LIF with every input group adding to V through a 16-bit counter of word 0
+					bool fast = P.model == LIF && P.W == 1 && P.ngroups <= 2;
+					for (int g = 0; g < P.ngroups && fast; g++)
+						fast = P.group_field[g] == 0 && P.group_bits[g] == 16 && P.group_word[g] == 0 &&
+						       P.group_shift[g] == 16 * g;
+					wa.blk_kind[p] = fast ? 3 : 0;
 					nb += (int)((P.size + 255) / 256);
 				}
 			}
@@ -625,14 +689,28 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			da.nconn  = (int)n->conns.size();
 			da.npop   = np;
 			da.mode   = n->mode;
-			da.conns  = n->d_conns;
+			da.conns  = n->d_conns_by_dst;
 			da.pops   = n->d_pops;
 			da.counts = wa.counts;
 			da.counts_next     = n->d_counts + (size_t)(n->parity ^ 1) * n->K * np;
 			da.counts_next_len = n->K * np;
 			da.events = n->d_events;
+			da.slot_lo = n->time + n->dmin - 1;
+			da.nslots  = k + n->dmax - n->dmin;
+			int tb = 0, smem = 0;
+			for (int p = 0; p < np; p++) {
+				PopDev const& P = n->pops[p].d;
+				da.tile_begin[p] = tb;
+				tb += P.ntiles;
+				if (P.ntiles) smem = std::max(smem, 4 * P.tile * (n->mode == 0 ? P.W : P.F));
+			}
+			da.tile_begin[np] = tb;
+			da.ntiles_total   = tb;
+			da.smem_bytes     = std::max(smem, 4);
+			da.parts          = n->deliver_parts;
+			da.algo           = n->deliver_algo;
 			TRY(ev_begin(n, 1, &slot));
-			CUDA_TRY(launch_deliver(n->stream, da, 1216));
+			CUDA_TRY(launch_deliver(n->stream, da, n->deliver_threads));
 			TRY(ev_end(n, slot));
 			n->launches++;
 			if (record) {
@@ -891,6 +969,75 @@ extern "C" int spice_kernel_stats(spice_net* n, int kind, int64_t* launches, dou
 extern "C" int spice_launch_count(spice_net* n, int64_t* out) {
 	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
 	*out = n->launches;
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	switch (knob) {
+		case SPICE_TUNE_TILE_BYTES:
+			if (value < 1024 || value > 220 * 1024) return fail(SPICE_EINVAL, "tile bytes must be in [1 KiB, 220 KiB]");
+			if (n->tile_bytes == (int)value) return SPICE_OK;
+			n->tile_bytes = (int)value;
+			if (n->prepared) {  // re-tile: the input ring layout does not depend on the tile size
+				TRY(setup_tiles(n, false));
+				std::vector<PopDev> hp;
+				for (auto& p : n->pops) hp.push_back(p.d);
+				CUDA_TRY(cudaMemcpy(n->d_pops, hp.data(), sizeof(PopDev) * hp.size(), cudaMemcpyHostToDevice));
+				std::vector<ConnDev> hb;
+				for (int ci : n->by_dst) hb.push_back(n->conns[ci].d);
+				if (!hb.empty())
+					CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
+			}
+			return SPICE_OK;
+		case SPICE_TUNE_DELIVER_THREADS:
+			if (value < 32 || value > 1024 || value % 32) return fail(SPICE_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
+			n->deliver_threads = (int)value;
+			return SPICE_OK;
+		case SPICE_TUNE_DELIVER_ALGO:
+			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "delivery algorithm must be 0 or 1");
+			n->deliver_algo = (int)value;
+			return SPICE_OK;
+		case SPICE_TUNE_DELIVER_PARTS: {
+			if (value < 1 || value > 64) return fail(SPICE_EINVAL, "parts must be in [1, 64]");
+			if (n->deliver_parts == (int)value) return SPICE_OK;
+			bool const was_split = n->deliver_parts > 1;
+			n->deliver_parts      = (int)value;
+			if (n->prepared && was_split != (value > 1)) {
+				// Overwritten slots (one delivery CTA per tile) are not cleared after use; slots that
+				// several CTAs accumulate into must start at zero.  Going from the first to the second
+				// convention, clear every slot that holds no pending input: for a population whose
+				// inputs all have delay d, slots t+d-1 .. t+D-2 (mod D).
+				std::vector<int> was_zeroing;
+				for (auto& p : n->pops) was_zeroing.push_back(p.d.zero_inputs);
+				TRY(setup_tiles(n, false));
+				for (size_t pi = 0; pi < n->pops.size(); pi++) {
+					PopDev& d = n->pops[pi].d;
+					if (was_zeroing[pi] || !d.zero_inputs || d.in_end == d.in_begin) continue;
+					int const dl = n->conns[n->by_dst[d.in_begin]].d.delay;
+					for (int64_t sg = n->time + dl - 1; sg <= n->time + n->max_delay - 2; sg++) {
+						int64_t const sl = sg % n->max_delay;
+						if (d.cnt) CUDA_TRY(cudaMemsetAsync(d.cnt + sl * d.size * d.W, 0, sizeof(uint32_t) * d.size * d.W, n->stream));
+						if (d.acc) CUDA_TRY(cudaMemsetAsync(d.acc + sl * d.size * d.F, 0, sizeof(float) * d.size * d.F, n->stream));
+					}
+				}
+				std::vector<PopDev> hp;
+				for (auto& p : n->pops) hp.push_back(p.d);
+				CUDA_TRY(cudaMemcpy(n->d_pops, hp.data(), sizeof(PopDev) * hp.size(), cudaMemcpyHostToDevice));
+				std::vector<ConnDev> hb;
+				for (int ci : n->by_dst) hb.push_back(n->conns[ci].d);
+				if (!hb.empty())
+					CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
+			}
+			return SPICE_OK;
+		}
+	}
+	return fail(SPICE_EINVAL, "unknown tuning knob");
+}
+
+extern "C" int spice_get_stream(spice_net* n, void** out) {
+	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
+	*out = (void*)n->stream;
 	return SPICE_OK;
 }
 

@@ -115,17 +115,6 @@ __device__ __forceinline__ void apply_inputs(PopDev const& P, int mode, int64_t 
 	}
 }
 
-// Appends the warp's spikes of one step (mask over lanes) to the step's list.
-__device__ __forceinline__ void append_warp(unsigned mask, bool spike, int32_t idx, int32_t* count,
-                                            int32_t* list) {
-	if (!mask) return;
-	int const lane = threadIdx.x & 31;
-	int base       = 0;
-	if (lane == 0) base = atomicAdd(count, __popc(mask));
-	base = __shfl_sync(0xffffffffu, base, 0);
-	if (spike) list[base + __popc(mask & lanemask_lt())] = idx;
-}
-
 __device__ __forceinline__ void red_add_u32(uint32_t* p, uint32_t v) {
 	asm volatile("red.relaxed.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -133,48 +122,91 @@ __device__ __forceinline__ void red_add_f32(float* p, float v) {
 	asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
 }
 
-// Replays the counted inputs of one slot word set (deterministic mode) in group order.
-__device__ __forceinline__ void replay_groups(PopDev const& P, const uint32_t* x, float& V, float& Gex, float& Gin) {
-	for (int g = 0; g < P.ngroups; g++) {
-		uint32_t const word = x[P.group_word[g]];
-		uint32_t const n    = P.group_bits[g] == 32 ? word : ((word >> P.group_shift[g]) & 0xffffu);
-		if (n) {
-			float& f       = field_ref(P.group_field[g], V, Gex, Gin);
-			float const wt = P.group_weight[g];
-			float v        = f;
-			for (uint32_t r = 0; r < n; r++) v = __fadd_rn(v, wt);
-			f = v;
-		}
+// v += w, n times, one IEEE add at a time (the reference's n sequential deliver() calls), with the
+// loop overhead paid once per four adds.
+__device__ __forceinline__ float add_n(float v, float w, uint32_t n) {
+	for (; n >= 4; n -= 4) v = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, w), w), w), w);
+	if (n >= 2) {
+		v = __fadd_rn(__fadd_rn(v, w), w);
+		n -= 2;
 	}
+	if (n) v = __fadd_rn(v, w);
+	return v;
 }
 
-// Same, when every group lives in one word (no array indexing: keeps the words in registers).
-__device__ __forceinline__ void replay_groups1(PopDev const& P, uint32_t word, float& V, float& Gex, float& Gin) {
-	for (int g = 0; g < P.ngroups; g++) {
+// Replays the counted inputs of one slot (deterministic mode) in group order: group g adds its
+// weight n_g times, one IEEE add at a time, as the reference's sequential deliver() calls do.
+// All loops run over the compile-time bound kMaxGroups so every index is static (registers).
+__device__ __forceinline__ void replay_words(PopDev const& P, const uint32_t (&x)[kMaxGroups], float& V, float& Gex,
+                                             float& Gin) {
+#pragma unroll
+	for (int g = 0; g < kMaxGroups; g++) {
+		if (g >= P.ngroups) break;
+		uint32_t word = 0;
+#pragma unroll
+		for (int j = 0; j < kMaxGroups; j++)
+			if (j == P.group_word[g]) word = x[j];
 		uint32_t const n = P.group_bits[g] == 32 ? word : ((word >> P.group_shift[g]) & 0xffffu);
 		if (n) {
-			float& f       = field_ref(P.group_field[g], V, Gex, Gin);
 			float const wt = P.group_weight[g];
-			float v        = f;
-			for (uint32_t r = 0; r < n; r++) v = __fadd_rn(v, wt);
-			f = v;
+			int const f    = P.group_field[g];
+			float v        = add_n(f == 0 ? V : (f == 1 ? Gex : Gin), wt, n);
+			if (f == 0) V = v;
+			else if (f == 1) Gex = v;
+			else Gin = v;
 		}
 	}
 }
 
-template <int MODE>
-__device__ void window_neurons(WindowArgs const& a, PopDev const& P, int p, int b) {
-	int const N      = (int)P.size;
-	int const i      = b * kThreads + threadIdx.x;
-	bool const valid = i < N;
-	int const lane   = threadIdx.x & 31;
-	int const word   = i >> 5;
+// Per-neuron window of a LIF population.  The population descriptor is copied to registers (a
+// local copy cannot alias the global stores below, so its fields are not re-loaded).  The inputs
+// of all steps of the window are already complete, so the loads of 8 consecutive slots are issued
+// together.  FAST: W == 1, every group adds to V with a 16-bit counter in word 0 (Brunel).
+constexpr int kBufSteps = 16;  // window steps buffered in shared memory before the list flush
+
+// Shared-memory spike buffer of one per-neuron CTA: warp w's spikes of buffered step k, so the
+// step loop needs no global atomic and no barrier; the lists are appended once per step and CTA.
+struct SpikeBuf {
+	int32_t idx[kBufSteps][kThreads / 32][32];
+	int cnt[kBufSteps][kThreads / 32];
+	int off[kBufSteps][kThreads / 32];
+	int base[kBufSteps];
+};
+
+__device__ void flush_spike_buf(SpikeBuf& sb, WindowArgs const& a, int p, int32_t* list, int N, int k_first, int nk) {
+	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kThreads / 32;
+	__syncthreads();
+	if (threadIdx.x < nk) {
+		int tot = 0;
+		for (int w = 0; w < nw; w++) {
+			sb.off[threadIdx.x][w] = tot;
+			tot += sb.cnt[threadIdx.x][w];
+		}
+		sb.base[threadIdx.x] = tot ? atomicAdd(a.counts + (k_first + threadIdx.x) * a.npop + p, tot) : 0;
+	}
+	__syncthreads();
+	for (int kk = 0; kk < nk; kk++) {
+		int const c = sb.cnt[kk][warp];
+		if (lane < c) list[(int64_t)(k_first + kk) * N + sb.base[kk] + sb.off[kk][warp] + lane] = sb.idx[kk][warp][lane];
+	}
+	__syncthreads();
+}
+
+template <int MODE, bool FAST>
+__device__ void window_neurons(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int b, SpikeBuf& sb) {
+	PopDev const P    = *Pg;
+	int const N       = (int)P.size;
+	int const i       = b * kThreads + threadIdx.x;
+	bool const valid  = i < N;
+	int const lane    = threadIdx.x & 31;
+	int const word    = i >> 5;
+	bool const cond   = P.model == LIF_COND;
 	float V = 0, Gex = 0, Gin = 0;
 	int32_t T = 0;
 	if (valid) {
 		V = P.V[i];
 		T = P.T[i];
-		if (P.model == LIF_COND) {
+		if (cond) {
 			Gex = P.Gex[i];
 			Gin = P.Gin[i];
 		}
@@ -185,13 +217,17 @@ __device__ void window_neurons(WindowArgs const& a, PopDev const& P, int p, int 
 	int const D = (int)a.D, Hb = a.Hb;
 	int slot  = a.slot0;   // (t0 - 1) mod D: inputs applied before the update of step t0
 	int hslot = a.hslot0;  // t0 mod Hb
-	int32_t* count = a.counts + p;
-	int32_t* list  = P.list;
-	bool const W1  = MODE == 0 && P.W == 1;
+	int const warp = threadIdx.x >> 5;
+	int k_first    = 0;
+	float w16[2] = {0.f, 0.f};
+	if (FAST) {
+		w16[0] = P.group_weight[0];
+		w16[1] = P.ngroups > 1 ? P.group_weight[1] : 0.f;
+	}
+	bool const zero = P.zero_inputs != 0;
 	for (int k0 = 0; k0 < a.K; k0 += 8) {
-		// the inputs of the next 8 steps are complete already: issue their loads together
 		uint32_t xs[8];
-		if (W1) {
+		if (MODE == 0 && P.W == 1) {
 			int sl = slot;
 #pragma unroll
 			for (int u = 0; u < 8; u++) {
@@ -207,49 +243,66 @@ __device__ void window_neurons(WindowArgs const& a, PopDev const& P, int p, int 
 			bool spike     = false;
 			if (valid) {
 				if (MODE == 0) {
-					if (W1) {
-						if (xs[u]) {
-							replay_groups1(P, xs[u], V, Gex, Gin);
-							P.cnt[(int64_t)slot * N + i] = 0;
+					if (P.W == 1) {
+						uint32_t const x = xs[u];
+						if (x) {
+							if (FAST) {
+								V = add_n(add_n(V, w16[0], x & 0xffffu), w16[1], x >> 16);
+							} else {
+								uint32_t xw[kMaxGroups] = {x};
+								replay_words(P, xw, V, Gex, Gin);
+							}
+							if (zero) P.cnt[(int64_t)slot * N + i] = 0;
 						}
 					} else {
 						uint32_t* w = P.cnt + ((int64_t)slot * N + i) * P.W;
-						uint32_t x[kMaxGroups];
+						uint32_t xw[kMaxGroups];
 						bool any = false;
 #pragma unroll
-						for (int j = 0; j < kMaxGroups; j++)
-							if (j < P.W) {
-								x[j] = w[j];
-								any |= x[j] != 0;
-							}
+						for (int j = 0; j < kMaxGroups; j++) {
+							xw[j] = j < P.W ? w[j] : 0u;
+							any |= xw[j] != 0;
+						}
 						if (any) {
-							replay_groups(P, x, V, Gex, Gin);
+							replay_words(P, xw, V, Gex, Gin);
+							if (zero) {
 #pragma unroll
-							for (int j = 0; j < kMaxGroups; j++)
-								if (j < P.W) w[j] = 0;
+								for (int j = 0; j < kMaxGroups; j++)
+									if (j < P.W) w[j] = 0;
+							}
 						}
 					}
 				} else {
 					float* acc = P.acc + ((int64_t)slot * N + i) * P.F;
+#pragma unroll
 					for (int f = 0; f < 3; f++) {
 						int const sidx = P.field_slot[f];
 						if (sidx < 0) continue;
 						float const x = acc[sidx];
 						if (x != 0.0f) {
-							float& dst = field_ref(f, V, Gex, Gin);
-							dst        = __fadd_rn(dst, x);
-							acc[sidx]  = 0.0f;
+							if (f == 0) V = __fadd_rn(V, x);
+							else if (f == 1) Gex = __fadd_rn(Gex, x);
+							else Gin = __fadd_rn(Gin, x);
+							if (zero) acc[sidx] = 0.0f;
 						}
 					}
 				}
-				if (P.model == LIF)
+				if (!cond)
 					spike = lif_update(V, T, __fmaf_rn(-dt, tminv, 1.0f), vthres, tref);
 				else
 					spike = lifc_update(V, Gex, Gin, T, dt);
 			}
 			unsigned const mask = __ballot_sync(0xffffffffu, spike);
-			if (lane == 0 && word < P.nwords) P.bits[(int64_t)hslot * P.nwords + word] = mask;
-			append_warp(mask, spike, i, count + k * a.npop, list + (int64_t)k * N);
+			int const kb        = k - k_first;
+			if (lane == 0) {
+				if (word < P.nwords) P.bits[(int64_t)hslot * P.nwords + word] = mask;
+				sb.cnt[kb][warp] = __popc(mask);
+			}
+			if (spike) sb.idx[kb][warp][__popc(mask & lanemask_lt())] = i;
+			if (kb + 1 == kBufSteps || k + 1 == a.K) {
+				flush_spike_buf(sb, a, p, P.list, N, k_first, kb + 1);
+				k_first = k + 1;
+			}
 			slot  = slot + 1 == D ? 0 : slot + 1;
 			hslot = hslot + 1 == Hb ? 0 : hslot + 1;
 		}
@@ -257,7 +310,7 @@ __device__ void window_neurons(WindowArgs const& a, PopDev const& P, int p, int 
 	if (valid) {
 		P.V[i] = V;
 		P.T[i] = T;
-		if (P.model == LIF_COND) {
+		if (cond) {
 			P.Gex[i] = Gex;
 			P.Gin[i] = Gin;
 		}
@@ -266,61 +319,54 @@ __device__ void window_neurons(WindowArgs const& a, PopDev const& P, int p, int 
 
 // One step of a Poisson population (samples/brunel.cpp:27-30): thread c owns neurons
 // [32c, 32c + 32), jumps to draw draw_offset + 32c of the step's stream and draws 32 numbers.
-// The jump XORs the basis states T^i(s) selected by the 128 bits of x^(offset) mod P; the CTA
-// first tabulates, for each of the 32 nibbles of the polynomial, the XOR of all 16 subsets of its
-// 4 basis states, so a jump is 32 table lookups.
-__device__ void window_poisson(WindowArgs const& a, PopDev const& P, int p, int b, u128* tab) {
-	int const k      = b / a.blk_per_step[p];
-	int const cb     = b % a.blk_per_step[p];
-	int const hslot  = (a.hslot0 + k) % a.Hb;
-	const u128* bas  = a.basis + (int64_t)k * kBasis;
-	for (int e = threadIdx.x; e < 32 * 16; e += blockDim.x) {
-		int const g = e >> 4, m = e & 15;
-		uint64_t lo = 0, hi = 0;
-#pragma unroll
-		for (int q = 0; q < 4; q++)
-			if ((m >> q) & 1) {
-				lo ^= bas[4 * g + q].lo;
-				hi ^= bas[4 * g + q].hi;
-			}
-		tab[e] = {lo, hi};
-	}
-	__syncthreads();
-	int64_t const c = (int64_t)cb * kThreads + threadIdx.x;
-	float const thr = __fmul_rn(P.p0, a.dts[k]);
-	unsigned mask   = 0;
+// The jump XORs the states T^i(s), i < 128, selected by the 128 bits of x^(offset) mod P; the step's
+// jump table holds, for each byte of the polynomial, the XOR of every subset of its 8 states, so a
+// jump is 16 independent table loads.
+// canonical<float>(u) < thr with canonical = (u >> 40) * 2^-24 is evaluated exactly in integers:
+// for an integer m < 2^24, m < thr * 2^24  <=>  m < ceil(thr * 2^24), and m < c <=> hi32(u) < 256 c.
+__device__ void window_poisson(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int b, int* red) {
+	PopDev const P  = *Pg;
+	int const k     = b / a.blk_per_step[p];
+	int const cb    = b % a.blk_per_step[p];
+	int const hslot = (a.hslot0 + k) % a.Hb;
+	const u128* tab = a.tables + (int64_t)k * kJumpTable;
+	int64_t const c  = (int64_t)cb * kThreads + threadIdx.x;
+	float const thr  = __fmul_rn(P.p0, a.dts[k]);
+	float const cthr = ceilf(thr * 16777216.0f);  // exact: scaling by 2^24
+	uint64_t const lim = cthr <= 0.f ? 0ull : (cthr >= 16777216.f ? (1ull << 32) : (uint64_t)cthr << 8);
+	unsigned mask = 0;
 	if (c < P.nwords) {
 		u128 const poly = P.chunk_poly[c];
 		uint64_t s0 = 0, s1 = 0;
 #pragma unroll
-		for (int g = 0; g < 16; g++) {
-			u128 const v = tab[g * 16 + ((poly.lo >> (4 * g)) & 15)];
-			s0 ^= v.lo;
-			s1 ^= v.hi;
+		for (int g = 0; g < 8; g++) {
+			ulonglong2 const v = __ldg(reinterpret_cast<const ulonglong2*>(tab + g * 256 + ((poly.lo >> (8 * g)) & 255)));
+			s0 ^= v.x;
+			s1 ^= v.y;
 		}
 #pragma unroll
-		for (int g = 0; g < 16; g++) {
-			u128 const v = tab[(16 + g) * 16 + ((poly.hi >> (4 * g)) & 15)];
-			s0 ^= v.lo;
-			s1 ^= v.hi;
+		for (int g = 0; g < 8; g++) {
+			ulonglong2 const v = __ldg(reinterpret_cast<const ulonglong2*>(tab + (8 + g) * 256 + ((poly.hi >> (8 * g)) & 255)));
+			s0 ^= v.x;
+			s1 ^= v.y;
 		}
 		int const n = (int)(P.size - 32 * c < 32 ? P.size - 32 * c : 32);
 		if (n == 32) {
 #pragma unroll 8
 			for (int r = 0; r < 32; r++) {
 				uint64_t const u = xoro_next(s0, s1);
-				mask |= (unsigned)(canonical_f32(u) < thr) << r;
+				mask |= (unsigned)((u >> 32) < lim) << r;
 			}
 		} else {
 			for (int r = 0; r < n; r++) {
 				uint64_t const u = xoro_next(s0, s1);
-				mask |= (unsigned)(canonical_f32(u) < thr) << r;
+				mask |= (unsigned)((u >> 32) < lim) << r;
 			}
 		}
 		P.bits[(int64_t)hslot * P.nwords + c] = mask;
 	}
-	// ascending append: warp exclusive scan of the per-thread spike counts
-	int const lane = threadIdx.x & 31;
+	// ascending append: CTA exclusive scan of the per-thread spike counts, one reservation
+	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 	int const mine = __popc(mask);
 	int incl       = mine;
 #pragma unroll
@@ -328,12 +374,20 @@ __device__ void window_poisson(WindowArgs const& a, PopDev const& P, int p, int 
 		int const v = __shfl_up_sync(0xffffffffu, incl, d);
 		if (lane >= d) incl += v;
 	}
-	int const total = __shfl_sync(0xffffffffu, incl, 31);
-	if (total == 0) return;
-	int base = 0;
-	if (lane == 31) base = atomicAdd(a.counts + k * a.npop + p, total);
-	base = __shfl_sync(0xffffffffu, base, 31);
-	int32_t* out = P.list + (int64_t)k * P.size + base + (incl - mine);
+	if (lane == 31) red[warp] = incl;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		int tot = 0;
+		for (int w = 0; w < kThreads / 32; w++) {
+			int const v = red[w];
+			red[w]      = tot;
+			tot += v;
+		}
+		red[kThreads / 32] = tot ? atomicAdd(a.counts + k * a.npop + p, tot) : 0;
+	}
+	__syncthreads();
+	if (!mask) return;
+	int32_t* out = P.list + (int64_t)k * P.size + red[kThreads / 32] + red[warp] + (incl - mine);
 	unsigned m   = mask;
 	while (m) {
 		int const r = __ffs(m) - 1;
@@ -343,7 +397,8 @@ __device__ void window_poisson(WindowArgs const& a, PopDev const& P, int p, int 
 }
 
 // One step of an external population (samples/external_input.cpp:17-30).
-__device__ void window_external(WindowArgs const& a, PopDev const& P, int p, int k) {
+__device__ void window_external(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int k) {
+	PopDev const P  = *Pg;
 	uint32_t* bits  = P.bits + (int64_t)((a.hslot0 + k) % a.Hb) * P.nwords;
 	for (int j = threadIdx.x; j < P.nwords; j += blockDim.x) bits[j] = 0;
 	__syncthreads();
@@ -359,113 +414,272 @@ __device__ void window_external(WindowArgs const& a, PopDev const& P, int p, int
 	if (threadIdx.x == 0) a.counts[k * a.npop + p] = n;
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_window(const __grid_constant__ WindowArgs a) {
-	__shared__ PopDev sp;
-	__shared__ u128 tab[32 * 16];
+// ONLY_FAST: every per-neuron population of the launch takes the FAST path, so the generic input
+// replay is compiled out (fewer registers).
+template <int MODE, bool ONLY_FAST>
+__global__ void __launch_bounds__(kThreads, 3) k_window(const __grid_constant__ WindowArgs a) {
+	__shared__ SpikeBuf sb;
+	__shared__ int red[kThreads / 32 + 1];
 	int const b = blockIdx.x;
 	int p       = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
-	if (threadIdx.x == 0) sp = a.pops[p];
-	__syncthreads();
 	int const lb = b - a.blk_begin[p];
 	switch (a.blk_kind[p]) {
-		case 0: window_neurons<MODE>(a, sp, p, lb); break;
-		case 1: window_poisson(a, sp, p, lb, tab); break;
-		case 2: window_external(a, sp, p, lb); break;
+		case 0:
+			if (!ONLY_FAST) window_neurons<MODE, false>(a, a.pops + p, p, lb, sb);
+			break;
+		case 1: window_poisson(a, a.pops + p, p, lb, red); break;
+		case 2: window_external(a, a.pops + p, p, lb); break;
+		case 3: window_neurons<MODE, true>(a, a.pops + p, p, lb, sb); break;
 	}
 }
 
-constexpr int kDeliverThreads = 256;
-
-// Work queue: item = (window step k, connection c, j-th spike of c's source at step k); one warp
-// per item streams the CSR row with 8 loads in flight per lane and adds with fire-and-forget
-// reductions.  The (k, c) prefix of spike counts is built once per CTA (no per-step barriers).
 template <int MODE>
-__global__ void __launch_bounds__(kDeliverThreads) k_deliver(const __grid_constant__ DeliverArgs a) {
-	extern __shared__ int64_t pre[];  // [K * nconn + 1]
+__global__ void k_deliver(const __grid_constant__ DeliverArgs a) {
+	extern __shared__ uint32_t tile_sm[];
 	__shared__ unsigned long long ev_block;
-	int const C = a.nconn, KC = a.K * C;
-	for (int t = threadIdx.x; t < KC; t += blockDim.x) {
-		int const k = t / C, c = t - k * C;
-		pre[t + 1]  = a.counts[k * a.npop + a.conns[c].src];
-	}
-	if (threadIdx.x == 0) {
-		pre[0]   = 0;
-		ev_block = 0;
-	}
+	int const part = blockIdx.x % a.parts;
+	int const b    = blockIdx.x / a.parts;
+	int const si   = b / a.ntiles_total;
+	int const g    = b - si * a.ntiles_total;
+	int Q        = 0;
+	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
+	PopDev const& P = a.pops[Q];
+	int const t     = g - a.tile_begin[Q];
+	int const T     = P.tile;
+	int const tbase = t * T;
+	int const tn    = (int)min((int64_t)T, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
+	if (threadIdx.x == 0) ev_block = 0;
 	if (blockIdx.x == 0)
 		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
 	__syncthreads();
-	int const lane = threadIdx.x & 31;
-	if (threadIdx.x < 32) {
-		int64_t carry = 0;
-		for (int base = 1; base <= KC; base += 32) {
-			int64_t v = base + lane <= KC ? pre[base + lane] : 0;
+	int64_t const sigma = a.slot_lo + si;
+	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+	unsigned long long my_events = 0;
+	bool touched = false;
+	for (int ci = P.in_begin; ci < P.in_end; ci++) {
+		ConnDev const& C = a.conns[ci];
+		int64_t const k  = sigma - (a.t0 + C.delay - 1);
+		if (k < 0 || k >= a.K) continue;
+		touched = true;
+		int const n          = a.counts[k * a.npop + C.src];
+		const int32_t* lst   = C.src_list + k * C.src_size;
+		const int64_t* bnd   = C.bounds;
+		int const stride     = P.ntiles + 1;
+		const int32_t* nb    = C.nb;
+		int const word       = MODE == 0 ? C.word : C.fslot;
+		uint32_t const inc   = C.inc;
+		float const w        = C.weight;
+		int const jstride = a.parts * nwarps * 32;
+		int j0            = (part * nwarps + warp) * 32;
+		int s_next        = (j0 + lane < n) ? __ldg(lst + j0 + lane) : -1;
+		while (j0 < n) {
+			int const s = s_next;
+			int64_t start = 0;
+			int len       = 0;
+			if (s >= 0) {
+				const int64_t* bb = bnd + (int64_t)s * stride + t;
+				start             = __ldg(bb);
+				len               = (int)(__ldg(bb + 1) - start);
+			}
+			int const jn = j0 + jstride;  // prefetch the next batch's spike ids
+			s_next       = (jn + lane < n) ? __ldg(lst + jn + lane) : -1;
+			int incl = len;
 #pragma unroll
 			for (int d = 1; d < 32; d <<= 1) {
-				int64_t const o = __shfl_up_sync(0xffffffffu, v, d);
-				if (lane >= d) v += o;
+				int const o = __shfl_up_sync(0xffffffffu, incl, d);
+				if (lane >= d) incl += o;
 			}
-			if (base + lane <= KC) pre[base + lane] = carry + v;
-			carry += __shfl_sync(0xffffffffu, v, 31);
-		}
-	}
-	__syncthreads();
-	int64_t const total  = pre[KC];
-	int64_t const gwarp  = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-	int64_t const nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-	unsigned long long my_events = 0;
-	for (int64_t item = gwarp; item < total; item += nwarps) {
-		int lo = 0, hi = KC;  // largest kc with pre[kc] <= item
-		while (hi - lo > 1) {
-			int const mid = (lo + hi) >> 1;
-			if (pre[mid] <= item) lo = mid;
-			else hi = mid;
-		}
-		int const k = lo / C, c = lo - k * C;
-		ConnDev const* Cp = a.conns + c;
-		int64_t const ss  = __ldg(&Cp->src_size);
-		const int32_t* lst = (const int32_t*)__ldg((const unsigned long long*)&Cp->src_list);
-		const int64_t* off = (const int64_t*)__ldg((const unsigned long long*)&Cp->off);
-		const int32_t* nb  = (const int32_t*)__ldg((const unsigned long long*)&Cp->nb);
-		int const delay    = __ldg(&Cp->delay);
-		int const s        = __ldg(lst + (int64_t)k * ss + (item - pre[lo]));
-		int64_t const e0   = __ldg(off + s);
-		int64_t const e1   = __ldg(off + s + 1);
-		int64_t slot       = a.t0 + k + delay - 1;
-		slot               = slot % a.D;
-		int64_t const dsz  = __ldg(&Cp->dst_size);
-		if (MODE == 0) {
-			int const W        = __ldg(&Cp->W);
-			uint32_t* base     = (uint32_t*)__ldg((const unsigned long long*)&Cp->dst_cnt) + slot * dsz * W + __ldg(&Cp->word);
-			uint32_t const inc = __ldg(&Cp->inc);
-			for (int64_t e = e0 + lane; e < e1; e += 256) {
+			int const total = __shfl_sync(0xffffffffu, incl, 31);
+			int const excl  = incl - len;
+			if (lane == 0) my_events += (unsigned long long)total;
+			for (int base = 0; base < total; base += 32 * 8) {
 				int32_t d[8];
 #pragma unroll
-				for (int u = 0; u < 8; u++) d[u] = (e + 32 * u < e1) ? __ldg(nb + e + 32 * u) : -1;
+				for (int u = 0; u < 8; u++) {
+					int const e = base + u * 32 + lane;
+					d[u]        = -1;
+					// the spike q whose sub-row holds flattened event e: largest q with excl_q <= e
+					int q = 0;
+#pragma unroll
+					for (int st = 16; st; st >>= 1) {
+						int const cand = q + st;
+						int const ex   = __shfl_sync(0xffffffffu, excl, cand & 31);
+						if (cand < 32 && ex <= e) q = cand;
+					}
+					int64_t const sq = __shfl_sync(0xffffffffu, start, q);
+					int const eq     = __shfl_sync(0xffffffffu, excl, q);
+					if (e < total) d[u] = __ldg(nb + sq + (e - eq));
+				}
 #pragma unroll
 				for (int u = 0; u < 8; u++)
-					if (d[u] >= 0) red_add_u32(base + (int64_t)d[u] * W, inc);
+					if (d[u] >= 0) {
+						int const li = (d[u] - tbase) * width + word;
+						if (MODE == 0)
+							atomicAdd(tile_sm + li, inc);
+						else
+							atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+					}
 			}
-		} else {
-			int const F    = __ldg(&Cp->F);
-			float* base    = (float*)__ldg((const unsigned long long*)&Cp->dst_acc) + slot * dsz * F + __ldg(&Cp->fslot);
-			float const w  = __ldg(&Cp->weight);
-			for (int64_t e = e0 + lane; e < e1; e += 256) {
-				int32_t d[8];
-#pragma unroll
-				for (int u = 0; u < 8; u++) d[u] = (e + 32 * u < e1) ? __ldg(nb + e + 32 * u) : -1;
-#pragma unroll
-				for (int u = 0; u < 8; u++)
-					if (d[u] >= 0) red_add_f32(base + (int64_t)d[u] * F, w);
-			}
+			j0 = jn;
 		}
-		if (lane == 0) my_events += (unsigned long long)(e1 - e0);
 	}
 	if (lane == 0 && my_events) atomicAdd(&ev_block, my_events);
 	__syncthreads();
 	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+	if (!touched) return;
+	// flush the tile into ring slot sigma mod D
+	int64_t const slot = sigma % a.D;
+	if (MODE == 0) {
+		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
+		if (a.parts > 1) {  // several CTAs share the slot's tile: coalesced reductions
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) red_add_u32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) dst[i] += v;
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
+		}
+	} else {
+		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
+		const float* sm = reinterpret_cast<const float*>(tile_sm);
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) red_add_f32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
+		}
+	}
+}
+
+// Thread-per-spike variant of the tiled delivery: each thread walks the sub-row of one spike
+// within the CTA's tile (8 loads in flight), no cross-lane work distribution.
+template <int MODE>
+__global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	int const part = blockIdx.x % a.parts;
+	int const b    = blockIdx.x / a.parts;
+	int const si   = b / a.ntiles_total;
+	int const g    = b - si * a.ntiles_total;
+	int Q          = 0;
+	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
+	PopDev const& P = a.pops[Q];
+	int const t     = g - a.tile_begin[Q];
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
+	if (threadIdx.x == 0) ev_block = 0;
+	if (blockIdx.x == 0)
+		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
+	__syncthreads();
+	int64_t const sigma = a.slot_lo + si;
+	unsigned long long my_events = 0;
+	bool touched = false;
+	for (int ci = P.in_begin; ci < P.in_end; ci++) {
+		ConnDev const& C = a.conns[ci];
+		int64_t const k  = sigma - (a.t0 + C.delay - 1);
+		if (k < 0 || k >= a.K) continue;
+		touched = true;
+		int const n        = a.counts[k * a.npop + C.src];
+		const int32_t* lst = C.src_list + k * C.src_size;
+		const int64_t* bnd = C.bounds;
+		int const stride   = P.ntiles + 1;
+		const int32_t* nb  = C.nb;
+		int const word     = MODE == 0 ? C.word : C.fslot;
+		uint32_t const inc = C.inc;
+		float const w      = C.weight;
+		for (int j = part * blockDim.x + threadIdx.x; j < n; j += a.parts * blockDim.x) {
+			int const s        = __ldg(lst + j);
+			const int64_t* bb  = bnd + (int64_t)s * stride + t;
+			int64_t const e0   = __ldg(bb);
+			int64_t const e1   = __ldg(bb + 1);
+			my_events += (unsigned long long)(e1 - e0);
+			for (int64_t e = e0; e < e1; e += 8) {
+				int32_t d[8];
+#pragma unroll
+				for (int u = 0; u < 8; u++) d[u] = e + u < e1 ? __ldg(nb + e + u) : -1;
+#pragma unroll
+				for (int u = 0; u < 8; u++)
+					if (d[u] >= 0) {
+						int const li = (d[u] - tbase) * width + word;
+						if (MODE == 0)
+							atomicAdd(tile_sm + li, inc);
+						else
+							atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+					}
+			}
+		}
+	}
+	for (int d = 16; d; d >>= 1) my_events += __shfl_xor_sync(0xffffffffu, my_events, d);
+	if ((threadIdx.x & 31) == 0 && my_events) atomicAdd(&ev_block, my_events);
+	__syncthreads();
+	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+	if (!touched) return;
+	int64_t const slot = sigma % a.D;
+	if (MODE == 0) {
+		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) red_add_u32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) dst[i] += v;
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
+		}
+	} else {
+		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
+		const float* sm = reinterpret_cast<const float*>(tile_sm);
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) red_add_f32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
+		}
+	}
+}
+
+__global__ void k_tile_bounds(const int64_t* __restrict__ off, const int32_t* __restrict__ nb, int64_t rows, int tile,
+                              int ntiles, int64_t* __restrict__ bounds) {
+	int64_t const r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (r >= rows) return;
+	int64_t pos       = off[r];
+	int64_t const end = off[r + 1];
+	int64_t* out = bounds + r * (ntiles + 1);
+	for (int t = 0; t <= ntiles; t++) {
+		int64_t const lim = (int64_t)t * tile;
+		while (pos < end && nb[pos] < lim) pos++;
+		out[t] = t == ntiles ? end : pos;
+	}
 }
 
 __global__ void k_apply_pending(PopDev P, int64_t slot, int mode) {
@@ -484,14 +698,31 @@ __global__ void k_apply_pending(PopDev P, int64_t slot, int mode) {
 	}
 }
 
-__global__ void k_basis(const u128* __restrict__ seeds, int64_t nsteps, u128* __restrict__ basis) {
-	int64_t const t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+// Per step t: the states T^i(seed_t), i < 128, then for each of the 16 bytes of a jump polynomial
+// the XOR of every subset of the byte's 8 states: tables[t][g][m] = XOR_{q: bit q of m} T^(8g+q)(s).
+__global__ void k_jump_tables(const u128* __restrict__ seeds, int64_t nsteps, u128* __restrict__ tables) {
+	__shared__ u128 basis[kBasis];
+	int64_t const t = blockIdx.x;
 	if (t >= nsteps) return;
-	uint64_t s0 = seeds[t].lo, s1 = seeds[t].hi;
-	u128* out   = basis + t * kBasis;
-	for (int i = 0; i < kBasis; i++) {
-		out[i] = {s0, s1};
-		xoro_next(s0, s1);
+	if (threadIdx.x == 0) {
+		uint64_t s0 = seeds[t].lo, s1 = seeds[t].hi;
+		for (int i = 0; i < kBasis; i++) {
+			basis[i] = {s0, s1};
+			xoro_next(s0, s1);
+		}
+	}
+	__syncthreads();
+	u128* out = tables + t * kJumpTable;
+	for (int e = threadIdx.x; e < kJumpTable; e += blockDim.x) {
+		int const g = e >> 8, m = e & 255;
+		uint64_t lo = 0, hi = 0;
+#pragma unroll
+		for (int q = 0; q < 8; q++)
+			if ((m >> q) & 1) {
+				lo ^= basis[8 * g + q].lo;
+				hi ^= basis[8 * g + q].hi;
+			}
+		out[e] = {lo, hi};
 	}
 }
 
@@ -642,28 +873,54 @@ cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const i
 	return cudaGetLastError();
 }
 
-cudaError_t launch_basis(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* basis) {
+cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* tables) {
 	if (nsteps <= 0) return cudaSuccess;
-	k_basis<<<(unsigned)((nsteps + 127) / 128), 128, 0, stream>>>(seeds, nsteps, basis);
+	k_jump_tables<<<(unsigned)nsteps, 256, 0, stream>>>(seeds, nsteps, tables);
 	return cudaGetLastError();
 }
 
 cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks) {
 	if (nblocks <= 0) return cudaSuccess;
-	if (a.mode == 0)
-		k_window<0><<<nblocks, kThreads, 0, stream>>>(a);
-	else
-		k_window<1><<<nblocks, kThreads, 0, stream>>>(a);
+	bool only_fast = true;
+	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0;
+	if (a.mode == 0) {
+		if (only_fast) k_window<0, true><<<nblocks, kThreads, 0, stream>>>(a);
+		else k_window<0, false><<<nblocks, kThreads, 0, stream>>>(a);
+	} else {
+		if (only_fast) k_window<1, true><<<nblocks, kThreads, 0, stream>>>(a);
+		else k_window<1, false><<<nblocks, kThreads, 0, stream>>>(a);
+	}
 	return cudaGetLastError();
 }
 
-cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int nblocks) {
-	if (nblocks <= 0) return cudaSuccess;
-	size_t const smem = sizeof(int64_t) * ((size_t)a.K * a.nconn + 1);
-	if (a.mode == 0)
-		k_deliver<0><<<nblocks, kDeliverThreads, smem, stream>>>(a);
-	else
-		k_deliver<1><<<nblocks, kDeliverThreads, smem, stream>>>(a);
+cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int threads) {
+	int64_t const nblocks = (int64_t)a.nslots * a.ntiles_total * a.parts;
+	if (nblocks <= 0) {
+		if (a.counts_next_len > 0) return cudaMemsetAsync(a.counts_next, 0, sizeof(int32_t) * a.counts_next_len, stream);
+		return cudaSuccess;
+	}
+	static int configured[4] = {0, 0, 0, 0};
+	int const m = (a.mode == 0 ? 0 : 1) + 2 * (a.algo == 1);
+	void const* fn = m == 0 ? (void const*)k_deliver<0> : m == 1 ? (void const*)k_deliver<1>
+	               : m == 2 ? (void const*)k_deliver_tps<0> : (void const*)k_deliver_tps<1>;
+	if (configured[m] < a.smem_bytes) {
+		cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes);
+		if (e != cudaSuccess) return e;
+		configured[m] = a.smem_bytes;
+	}
+	switch (m) {
+		case 0: k_deliver<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 1: k_deliver<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 2: k_deliver_tps<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 3: k_deliver_tps<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_tile_bounds(cudaStream_t stream, const int64_t* off, const int32_t* nb, int64_t rows, int tile,
+                               int ntiles, int64_t* bounds) {
+	if (rows <= 0) return cudaSuccess;
+	k_tile_bounds<<<(unsigned)((rows + 255) / 256), 256, 0, stream>>>(off, nb, rows, tile, ntiles, bounds);
 	return cudaGetLastError();
 }
 

@@ -291,3 +291,41 @@ def test_atomic_mode_statistics(engine):
     det, atom = np.array(res[0]).mean(axis=0), np.array(res[1]).mean(axis=0)
     rel = np.abs(atom - det) / det
     assert (rel < 0.01).all(), (det, atom, rel)
+
+
+@pytest.mark.parametrize("tile_bytes,threads", [(1024, 32), (4096, 128), (48 * 1024, 512), (200 * 1024, 1024)])
+def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
+    """Delivery tiles and CTA sizes change how events are accumulated, never the result."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    for mode in (0, 1):
+        net, pops = engine.brunel(N, float(g["p"][0]), seed, mode=mode)
+        net.set_tuning(tile_bytes=tile_bytes, deliver_threads=threads)
+        counts, idx = _raster_flat(net.run_record(steps if mode == 0 else 50))
+        if mode == 0:
+            assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+            for k in (1, 2):
+                assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
+def test_retuning_mid_run_keeps_results(engine):
+    """Switching tile size, threads and parts between steps (including between overwritten and
+    accumulated input slots) leaves the raster and state bit-exact."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    shapes = [(48 * 1024, 512, 1), (8 * 1024, 256, 3), (16 * 1024, 128, 1), (96 * 1024, 1024, 2), (4096, 64, 5)]
+    raster = []
+    for i, (tb, th, parts) in enumerate(shapes):
+        net.set_tuning(tile_bytes=tb, deliver_threads=th, deliver_parts=parts)
+        n = steps // len(shapes) if i < len(shapes) - 1 else steps - len(raster)
+        if i % 2:
+            for _ in range(n):
+                net.step()
+                raster.append([net.spikes(p, 0) for p in pops])
+        else:
+            raster += net.run_record(n)
+    counts, idx = _raster_flat(raster)
+    assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
