@@ -99,7 +99,8 @@ enum {
 	SPICE_TUNE_TILE_BYTES      = 0, /* shared memory per target tile                          */
 	SPICE_TUNE_DELIVER_THREADS = 1, /* threads per delivery CTA                               */
 	SPICE_TUNE_DELIVER_PARTS   = 2, /* CTAs sharing one (input slot, tile)                    */
-	SPICE_TUNE_DELIVER_ALGO    = 3, /* 0: warp-flattened sub-rows, 1: one thread per spike   */
+	SPICE_TUNE_DELIVER_ALGO    = 3, /* 0: warp-flattened sub-rows, 1: one thread per spike,
+	                                   2: one warp per spike, 8 sub-rows in flight          */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's
@@ -139,8 +140,9 @@ int spice_get_csr(spice_net* net, int conn, int64_t* offsets_out, int32_t* neigh
 
 /* Per-kernel timing with CUDA events recorded on the net's stream around every launch. */
 int spice_set_profiling(spice_net* net, int on);
-/* kind: 0 = neuron update, 1 = spike delivery, 2 = raster extraction.  Returns the number of
- * launches and their summed device time (ms) since profiling was switched on. */
+/* kind: 0 = neuron update, 1 = spike delivery, 2 = raster extraction, 3 = source populations
+ * (Poisson / external trains).  Returns the number of launches and their summed device time (ms)
+ * since profiling was switched on. */
 int spice_kernel_stats(spice_net* net, int kind, int64_t* launches_out, double* ms_out);
 /* Number of kernels this library launched on the net's stream so far. */
 int spice_launch_count(spice_net* net, int64_t* launches_out);

@@ -130,7 +130,12 @@ struct spice_net {
 	int max_window = 0;  // 0 = auto
 	bool prepared  = false;
 	int device     = 0;
-	cudaStream_t stream = nullptr;
+	cudaStream_t stream = nullptr;       // main stream: neuron updates, deliveries, readback
+	cudaStream_t stream_src = nullptr;   // source populations (Poisson, external), one window ahead
+	cudaEvent_t ev_src[2] = {nullptr, nullptr};   // sources of a parity done
+	cudaEvent_t ev_free[2] = {nullptr, nullptr};  // lists/counts of a parity consumed and cleared
+	cudaEvent_t ev_tab = nullptr;        // dt and jump tables of the current chunk written
+	bool has_sources = false;
 	std::vector<spice_gb300::Pop> pops;
 	std::vector<spice_gb300::Conn> conns;
 	int K  = 1;          // window length used by run
@@ -138,7 +143,7 @@ struct spice_net {
 	int64_t total_draws = 0;  // draws per step over all populations
 	// device-wide buffers
 	unsigned long long* d_events = nullptr;
-	int32_t* d_counts  = nullptr;  // [K][npop] spikes per window step and population
+	int32_t* d_counts  = nullptr;  // [2][K][npop] spikes per window step and population, per parity
 	float* d_dt        = nullptr;  // [run capacity]
 	spice_gb300::u128* d_seeds = nullptr;  // [run capacity]
 	spice_gb300::u128* d_tables = nullptr;  // [run capacity][16][256] jump tables
@@ -160,7 +165,7 @@ struct spice_net {
 	std::vector<cudaEvent_t> ev_pool;
 	std::vector<std::pair<int, int>> ev_pending;  // (kind, event index of the start)
 	size_t ev_used = 0;
-	spice_gb300::KernelStat stats[3];
+	spice_gb300::KernelStat stats[4];
 	int64_t launches = 0;
 	std::vector<void*> allocations;
 	std::vector<spice_gb300::PendingGen> gen_pending;

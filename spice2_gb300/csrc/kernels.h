@@ -49,13 +49,16 @@ struct WindowArgs {
 	const float* dts;     // dt of steps t0 .. t0+K-1
 	const u128* tables;   // jump tables of step t0 (then t0+1, ...)
 	int32_t* counts;      // [K][npop] spikes per step and population (window parity buffer)
+	int list_k0;          // first list slot of this window's parity: lists are [2K][size]
 	int blk_begin[kMaxPops + 1];
 	int blk_kind[kMaxPops];      // 0: per-neuron window CTAs, 1: Poisson step CTAs, 2: external,
 	                             // 3: per-neuron CTAs of a LIF whose inputs all add to V (16-bit counts)
+	                             // (k_neurons launches kinds 0 and 3, k_sources kinds 1 and 2)
 	int blk_per_step[kMaxPops];  // Poisson / external: CTAs per step
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
 };
-cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks);
+cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks);
+cudaError_t launch_sources(cudaStream_t stream, WindowArgs const& a, int nblocks);
 
 struct DeliverArgs {
 	int64_t t0;
@@ -76,7 +79,8 @@ struct DeliverArgs {
 	int tile_begin[kMaxPops + 1];  // prefix over populations of their tile counts
 	int smem_bytes;
 	int parts;               // CTAs sharing one (slot, tile); > 1 flushes with reductions
-	int algo;                // 0: warp-flattened sub-rows, 1: one thread per spike
+	int algo;                // 0: warp-flattened sub-rows, 1: one thread per spike, 2: warp per spike
+	int list_k0;             // first list slot of this window's parity
 };
 // One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.
 cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int threads);

@@ -80,12 +80,13 @@ float kahan_next(spice_net* n) {  // kahan_sum<float>::operator+= then the reset
 }
 
 // ---- profiling ----
-int ev_begin(spice_net* n, int kind, int* slot) {
+int ev_begin(spice_net* n, int kind, int* slot, cudaStream_t st = nullptr) {
 	*slot = -1;
 	if (!n->profiling) return SPICE_OK;
 	if (n->ev_used + 2 > n->ev_pool.size()) {
-		// harvest: every recorded pair is complete once the stream is idle
+		// harvest: every recorded pair is complete once the streams are idle
 		CUDA_TRY(cudaStreamSynchronize(n->stream));
+		if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
 		for (auto const& pr : n->ev_pending) {
 			float ms = 0;
 			CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
@@ -103,18 +104,19 @@ int ev_begin(spice_net* n, int kind, int* slot) {
 	*slot = (int)n->ev_used;
 	n->ev_used += 2;
 	n->ev_pending.push_back({kind, *slot});
-	CUDA_TRY(cudaEventRecord(n->ev_pool[*slot], n->stream));
+	CUDA_TRY(cudaEventRecord(n->ev_pool[*slot], st ? st : n->stream));
 	return SPICE_OK;
 }
 
-int ev_end(spice_net* n, int slot) {
-	if (slot >= 0) CUDA_TRY(cudaEventRecord(n->ev_pool[slot + 1], n->stream));
+int ev_end(spice_net* n, int slot, cudaStream_t st = nullptr) {
+	if (slot >= 0) CUDA_TRY(cudaEventRecord(n->ev_pool[slot + 1], st ? st : n->stream));
 	return SPICE_OK;
 }
 
 int harvest(spice_net* n) {
 	if (n->ev_pending.empty()) return SPICE_OK;
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
 	for (auto const& pr : n->ev_pending) {
 		float ms = 0;
 		CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
@@ -170,6 +172,15 @@ extern "C" int spice_net_destroy(spice_net* n) {
 	if (n->h_dt) cudaFreeHost(n->h_dt);
 	if (n->h_seeds) cudaFreeHost(n->h_seeds);
 	for (auto e : n->ev_pool) cudaEventDestroy(e);
+	if (n->stream_src) {
+		cudaStreamSynchronize(n->stream_src);
+		cudaStreamDestroy(n->stream_src);
+	}
+	if (n->ev_tab) cudaEventDestroy(n->ev_tab);
+	for (int q = 0; q < 2; q++) {
+		if (n->ev_src[q]) cudaEventDestroy(n->ev_src[q]);
+		if (n->ev_free[q]) cudaEventDestroy(n->ev_free[q]);
+	}
 	if (n->stream) cudaStreamDestroy(n->stream);
 	delete n;
 	return SPICE_OK;
@@ -475,7 +486,8 @@ int prepare(spice_net* n) {
 	// the delivery kernel keeps a (step, connection) prefix of K * nconn entries in shared memory
 	if (!n->conns.empty()) K = std::min<int>(K, std::max<int>(1, 4096 / (int)n->conns.size()));
 	n->K  = std::max(K, 1);
-	n->Hb = (int)std::max<int64_t>(D, n->K);
+	// bitmaps: the last D steps for spikes(age), and two windows in flight (sources run ahead)
+	n->Hb = (int)std::max<int64_t>(D, 2 * n->K) + 1;
 	// draw offsets in the step's shared stream (populations in add order, snn.cpp:14-15)
 	int64_t draws = 0;
 	for (auto& p : n->pops) {
@@ -486,7 +498,7 @@ int prepare(spice_net* n) {
 	for (auto& p : n->pops) {
 		PopDev& d = p.d;
 		TRY(dalloc(n, &d.bits, (size_t)n->Hb * std::max(d.nwords, 1)));
-		TRY(dalloc(n, &d.list, (size_t)n->K * std::max<int64_t>(d.size, 1), false));
+		TRY(dalloc(n, &d.list, (size_t)2 * n->K * std::max<int64_t>(d.size, 1), false));
 		if (d.model == POISSON && d.nwords > 0) {
 			std::vector<u128> polys(d.nwords);
 			u128 const step = gf2_xpow(kPoissonChunk);
@@ -614,6 +626,14 @@ int prepare(spice_net* n) {
 	for (auto& p : n->pops) maxN = std::max(maxN, p.d.size);
 	TRY(dalloc(n, &n->d_tmp, maxN, false));
 	TRY(dalloc(n, &n->d_tmp_n, 1));
+	for (auto& p : n->pops) n->has_sources |= p.d.model == POISSON || p.d.model == EXTERNAL;
+	CUDA_TRY(cudaStreamCreateWithFlags(&n->stream_src, cudaStreamNonBlocking));
+	CUDA_TRY(cudaEventCreateWithFlags(&n->ev_tab, cudaEventDisableTiming));
+	for (int q = 0; q < 2; q++) {
+		CUDA_TRY(cudaEventCreateWithFlags(&n->ev_src[q], cudaEventDisableTiming));
+		CUDA_TRY(cudaEventCreateWithFlags(&n->ev_free[q], cudaEventDisableTiming));
+		CUDA_TRY(cudaEventRecord(n->ev_free[q], n->stream));
+	}
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
 	n->prepared = true;
 	return SPICE_OK;
@@ -625,7 +645,10 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 	int64_t rows   = 0;
 	while (steps > 0) {
 		int64_t const chunk = std::min<int64_t>(steps, n->run_cap);
-		CUDA_TRY(cudaStreamSynchronize(n->stream));  // the pinned staging is about to be rewritten
+		// the pinned staging and the device dt / seed / jump-table arrays are about to be rewritten:
+		// nothing of the previous chunk may still read them, on either stream
+		CUDA_TRY(cudaStreamSynchronize(n->stream));
+		CUDA_TRY(cudaStreamSynchronize(n->stream_src));
 		for (int64_t j = 0; j < chunk; j++) {
 			n->h_dt[j]    = kahan_next(n);
 			n->h_seeds[j] = seed_next(n);  // xoroshiro64_128p rng(_seed++) (snn.cpp:12)
@@ -636,36 +659,45 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			CUDA_TRY(launch_jump_tables(n->stream, n->d_seeds, chunk, n->d_tables));
 			n->launches++;
 		}
+		// the source kernels of this chunk read dt and the jump tables written above
+		CUDA_TRY(cudaEventRecord(n->ev_tab, n->stream));
+		CUDA_TRY(cudaStreamWaitEvent(n->stream_src, n->ev_tab, 0));
 		int64_t j = 0;
 		while (j < chunk) {
 			int const k = (int)std::min<int64_t>(n->K, chunk - j);
+			int const q = n->parity;
 			WindowArgs wa{};
-			wa.t0     = n->time;
-			wa.K      = k;
-			wa.slot0  = (int)((n->time - 1 + n->max_delay) % n->max_delay);
-			wa.hslot0 = (int)(n->time % n->Hb);
-			wa.D      = n->max_delay;
-			wa.Hb     = n->Hb;
-			wa.npop   = np;
-			wa.mode   = n->mode;
-			wa.pops   = n->d_pops;
-			wa.dts    = n->d_dt + j;
-			wa.tables = n->d_tables ? n->d_tables + j * kJumpTable : nullptr;
-			wa.counts = n->d_counts + (size_t)n->parity * n->K * np;
-			int nb = 0;
+			wa.t0      = n->time;
+			wa.K       = k;
+			wa.slot0   = (int)((n->time - 1 + n->max_delay) % n->max_delay);
+			wa.hslot0  = (int)(n->time % n->Hb);
+			wa.D       = n->max_delay;
+			wa.Hb      = n->Hb;
+			wa.npop    = np;
+			wa.mode    = n->mode;
+			wa.pops    = n->d_pops;
+			wa.dts     = n->d_dt + j;
+			wa.tables  = n->d_tables ? n->d_tables + j * kJumpTable : nullptr;
+			wa.counts  = n->d_counts + (size_t)q * n->K * np;
+			wa.list_k0 = q * n->K;
+			WindowArgs ws = wa;  // sources
+			int nb = 0, nbs = 0;
 			for (int p = 0; p < np; p++) {
 				PopDev const& P = n->pops[p].d;
 				wa.blk_begin[p] = nb;
+				ws.blk_begin[p] = nbs;
 				if (P.model == POISSON) {
-					wa.blk_kind[p]     = 1;
-					wa.blk_per_step[p] = (P.nwords + 255) / 256;
-					nb += wa.blk_per_step[p] * k;
+					ws.blk_kind[p]     = 1;
+					ws.blk_per_step[p] = (P.nwords + 255) / 256;
+					nbs += ws.blk_per_step[p] * k;
+					wa.blk_kind[p] = 1;
 				} else if (P.model == EXTERNAL) {
-					wa.blk_kind[p]     = 2;
-					wa.blk_per_step[p] = 1;
-					nb += k;
+					ws.blk_kind[p]     = 2;
+					ws.blk_per_step[p] = 1;
+					nbs += k;
 					int64_t const ns = P.ext_steps;
-					wa.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
+					ws.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
+					wa.blk_kind[p] = 2;
 				} else {
 					// LIF with every input group adding to V through a 16-bit counter of word 0
 					bool fast = P.model == LIF && P.W == 1 && P.ngroups <= 2;
@@ -673,15 +705,27 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 						fast = P.group_field[g] == 0 && P.group_bits[g] == 16 && P.group_word[g] == 0 &&
 						       P.group_shift[g] == 16 * g;
 					wa.blk_kind[p] = fast ? 3 : 0;
+					ws.blk_kind[p] = wa.blk_kind[p];
 					nb += (int)((P.size + 255) / 256);
 				}
 			}
 			wa.blk_begin[np] = nb;
+			ws.blk_begin[np] = nbs;
 			int slot = -1;
+			if (nbs > 0) {
+				// sources of this window may start once the lists of this parity are free
+				CUDA_TRY(cudaStreamWaitEvent(n->stream_src, n->ev_free[q], 0));
+				TRY(ev_begin(n, 3, &slot, n->stream_src));
+				CUDA_TRY(launch_sources(n->stream_src, ws, nbs));
+				TRY(ev_end(n, slot, n->stream_src));
+				CUDA_TRY(cudaEventRecord(n->ev_src[q], n->stream_src));
+				n->launches++;
+			}
 			TRY(ev_begin(n, 0, &slot));
-			CUDA_TRY(launch_window(n->stream, wa, nb));
+			CUDA_TRY(launch_neurons(n->stream, wa, nb));
 			TRY(ev_end(n, slot));
-			n->launches++;
+			if (nb > 0) n->launches++;
+			if (nbs > 0) CUDA_TRY(cudaStreamWaitEvent(n->stream, n->ev_src[q], 0));
 			DeliverArgs da{};
 			da.t0     = n->time;
 			da.K      = k;
@@ -692,8 +736,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			da.conns  = n->d_conns_by_dst;
 			da.pops   = n->d_pops;
 			da.counts = wa.counts;
-			da.counts_next     = n->d_counts + (size_t)(n->parity ^ 1) * n->K * np;
-			da.counts_next_len = n->K * np;
+			da.counts_next     = nullptr;
+			da.counts_next_len = 0;
+			da.list_k0         = q * n->K;
 			da.events = n->d_events;
 			da.slot_lo = n->time + n->dmin - 1;
 			da.nslots  = k + n->dmax - n->dmin;
@@ -730,6 +775,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				TRY(ev_end(n, slot));
 				n->launches++;
 			}
+			// this parity's counts are consumed: clear them for the window after next
+			CUDA_TRY(cudaMemsetAsync(wa.counts, 0, sizeof(int32_t) * n->K * np, n->stream));
+			CUDA_TRY(cudaEventRecord(n->ev_free[q], n->stream));
 			n->parity ^= 1;
 			n->time += k;
 			rows += k;
@@ -959,7 +1007,7 @@ extern "C" int spice_set_profiling(spice_net* n, int on) {
 
 extern "C" int spice_kernel_stats(spice_net* n, int kind, int64_t* launches, double* ms) {
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
-	if (kind < 0 || kind > 2) return fail(SPICE_EINVAL, "unknown kernel kind");
+	if (kind < 0 || kind > 3) return fail(SPICE_EINVAL, "unknown kernel kind");
 	TRY(harvest(n));
 	if (launches) *launches = n->stats[kind].launches;
 	if (ms) *ms = n->stats[kind].ms;
@@ -995,7 +1043,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->deliver_threads = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_ALGO:
-			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "delivery algorithm must be 0 or 1");
+			if (value < 0 || value > 2) return fail(SPICE_EINVAL, "delivery algorithm must be 0, 1 or 2");
 			n->deliver_algo = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_PARTS: {

@@ -158,132 +158,105 @@ __device__ __forceinline__ void replay_words(PopDev const& P, const uint32_t (&x
 	}
 }
 
-// Per-neuron window of a LIF population.  The population descriptor is copied to registers (a
-// local copy cannot alias the global stores below, so its fields are not re-loaded).  The inputs
-// of all steps of the window are already complete, so the loads of 8 consecutive slots are issued
-// together.  FAST: W == 1, every group adds to V with a 16-bit counter in word 0 (Brunel).
-constexpr int kBufSteps = 16;  // window steps buffered in shared memory before the list flush
-
-// Shared-memory spike buffer of one per-neuron CTA: warp w's spikes of buffered step k, so the
-// step loop needs no global atomic and no barrier; the lists are appended once per step and CTA.
-struct SpikeBuf {
-	int32_t idx[kBufSteps][kThreads / 32][32];
-	int cnt[kBufSteps][kThreads / 32];
-	int off[kBufSteps][kThreads / 32];
-	int base[kBufSteps];
-};
-
-__device__ void flush_spike_buf(SpikeBuf& sb, WindowArgs const& a, int p, int32_t* list, int N, int k_first, int nk) {
-	int const warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = kThreads / 32;
-	__syncthreads();
-	if (threadIdx.x < nk) {
-		int tot = 0;
-		for (int w = 0; w < nw; w++) {
-			sb.off[threadIdx.x][w] = tot;
-			tot += sb.cnt[threadIdx.x][w];
-		}
-		sb.base[threadIdx.x] = tot ? atomicAdd(a.counts + (k_first + threadIdx.x) * a.npop + p, tot) : 0;
-	}
-	__syncthreads();
-	for (int kk = 0; kk < nk; kk++) {
-		int const c = sb.cnt[kk][warp];
-		if (lane < c) list[(int64_t)(k_first + kk) * N + sb.base[kk] + sb.off[kk][warp] + lane] = sb.idx[kk][warp][lane];
-	}
-	__syncthreads();
-}
-
+// Per-neuron window of a LIF population.  The inputs of every step of the window are complete
+// already, so the input words of up to 16 consecutive slots are loaded together first; the step
+// loop itself is kept rolled and small (instruction-cache friendly).  FAST: every input group adds to
+// V through a 16-bit counter of word 0 (Brunel).
 template <int MODE, bool FAST>
-__device__ void window_neurons(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int b, SpikeBuf& sb) {
-	PopDev const P    = *Pg;
-	int const N       = (int)P.size;
+__device__ void window_neurons(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int b) {
+	int const N       = (int)Pg->size;
 	int const i       = b * kThreads + threadIdx.x;
 	bool const valid  = i < N;
 	int const lane    = threadIdx.x & 31;
 	int const word    = i >> 5;
-	bool const cond   = P.model == LIF_COND;
+	int const nwords  = Pg->nwords;
+	bool const cond   = Pg->model == LIF_COND;
+	float* const Vp   = Pg->V;
+	int32_t* const Tp = Pg->T;
+	uint32_t* const cnt = Pg->cnt;
+	float* const acc  = Pg->acc;
+	uint32_t* const bits = Pg->bits;
+	int32_t* const list  = Pg->list;
+	int const W = Pg->W, F = Pg->F;
+	bool const zero     = Pg->zero_inputs != 0;
+	float const vthres  = Pg->p0;
+	int32_t const tref  = (int32_t)Pg->p1;
+	float const tminv   = Pg->p2;
+	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
 	float V = 0, Gex = 0, Gin = 0;
 	int32_t T = 0;
 	if (valid) {
-		V = P.V[i];
-		T = P.T[i];
+		V = Vp[i];
+		T = Tp[i];
 		if (cond) {
-			Gex = P.Gex[i];
-			Gin = P.Gin[i];
+			Gex = Pg->Gex[i];
+			Gin = Pg->Gin[i];
 		}
 	}
-	float const vthres = P.p0;
-	int32_t const tref = (int32_t)P.p1;
-	float const tminv  = P.p2;
 	int const D = (int)a.D, Hb = a.Hb;
 	int slot  = a.slot0;   // (t0 - 1) mod D: inputs applied before the update of step t0
 	int hslot = a.hslot0;  // t0 mod Hb
-	int const warp = threadIdx.x >> 5;
-	int k_first    = 0;
-	float w16[2] = {0.f, 0.f};
-	if (FAST) {
-		w16[0] = P.group_weight[0];
-		w16[1] = P.ngroups > 1 ? P.group_weight[1] : 0.f;
-	}
-	bool const zero = P.zero_inputs != 0;
-	for (int k0 = 0; k0 < a.K; k0 += 8) {
-		uint32_t xs[8];
-		if (MODE == 0 && P.W == 1) {
+	int32_t* const count = a.counts + p;
+	bool const word_in = MODE == 0 && W == 1;
+	for (int k0 = 0; k0 < a.K; k0 += 16) {
+		int const nk = min(16, a.K - k0);
+		uint32_t xs[16];
+		if (word_in) {
 			int sl = slot;
 #pragma unroll
-			for (int u = 0; u < 8; u++) {
-				xs[u] = (valid && k0 + u < a.K) ? P.cnt[(int64_t)sl * N + i] : 0u;
+			for (int u = 0; u < 16; u++) {
+				xs[u] = (valid && u < nk) ? cnt[(int64_t)sl * N + i] : 0u;
 				sl    = sl + 1 == D ? 0 : sl + 1;
 			}
 		}
-#pragma unroll
-		for (int u = 0; u < 8; u++) {
-			int const k = k0 + u;
-			if (k >= a.K) break;
+#pragma unroll 1
+		for (int u = 0; u < nk; u++) {
+			int const k    = k0 + u;
 			float const dt = a.dts[k];
 			bool spike     = false;
 			if (valid) {
-				if (MODE == 0) {
-					if (P.W == 1) {
-						uint32_t const x = xs[u];
-						if (x) {
-							if (FAST) {
-								V = add_n(add_n(V, w16[0], x & 0xffffu), w16[1], x >> 16);
-							} else {
-								uint32_t xw[kMaxGroups] = {x};
-								replay_words(P, xw, V, Gex, Gin);
-							}
-							if (zero) P.cnt[(int64_t)slot * N + i] = 0;
+				if (word_in) {
+					uint32_t const x = xs[u];
+					if (x) {
+						if (FAST) {
+							uint32_t n0 = x & 0xffffu, n1 = x >> 16;
+							for (; n0; n0--) V = __fadd_rn(V, w0);
+							for (; n1; n1--) V = __fadd_rn(V, w1);
+						} else {
+							uint32_t xw[kMaxGroups] = {x};
+							replay_words(*Pg, xw, V, Gex, Gin);
 						}
-					} else {
-						uint32_t* w = P.cnt + ((int64_t)slot * N + i) * P.W;
-						uint32_t xw[kMaxGroups];
-						bool any = false;
+						if (zero) cnt[(int64_t)slot * N + i] = 0;
+					}
+				} else if (MODE == 0) {
+					uint32_t* w = cnt + ((int64_t)slot * N + i) * W;
+					uint32_t xw[kMaxGroups];
+					bool any = false;
 #pragma unroll
-						for (int j = 0; j < kMaxGroups; j++) {
-							xw[j] = j < P.W ? w[j] : 0u;
-							any |= xw[j] != 0;
-						}
-						if (any) {
-							replay_words(P, xw, V, Gex, Gin);
-							if (zero) {
+					for (int j = 0; j < kMaxGroups; j++) {
+						xw[j] = j < W ? w[j] : 0u;
+						any |= xw[j] != 0;
+					}
+					if (any) {
+						replay_words(*Pg, xw, V, Gex, Gin);
+						if (zero) {
 #pragma unroll
-								for (int j = 0; j < kMaxGroups; j++)
-									if (j < P.W) w[j] = 0;
-							}
+							for (int j = 0; j < kMaxGroups; j++)
+								if (j < W) w[j] = 0;
 						}
 					}
 				} else {
-					float* acc = P.acc + ((int64_t)slot * N + i) * P.F;
+					float* ac = acc + ((int64_t)slot * N + i) * F;
 #pragma unroll
 					for (int f = 0; f < 3; f++) {
-						int const sidx = P.field_slot[f];
+						int const sidx = Pg->field_slot[f];
 						if (sidx < 0) continue;
-						float const x = acc[sidx];
+						float const x = ac[sidx];
 						if (x != 0.0f) {
 							if (f == 0) V = __fadd_rn(V, x);
 							else if (f == 1) Gex = __fadd_rn(Gex, x);
 							else Gin = __fadd_rn(Gin, x);
-							if (zero) acc[sidx] = 0.0f;
+							if (zero) ac[sidx] = 0.0f;
 						}
 					}
 				}
@@ -293,26 +266,23 @@ __device__ void window_neurons(WindowArgs const& a, const PopDev* __restrict__ P
 					spike = lifc_update(V, Gex, Gin, T, dt);
 			}
 			unsigned const mask = __ballot_sync(0xffffffffu, spike);
-			int const kb        = k - k_first;
-			if (lane == 0) {
-				if (word < P.nwords) P.bits[(int64_t)hslot * P.nwords + word] = mask;
-				sb.cnt[kb][warp] = __popc(mask);
-			}
-			if (spike) sb.idx[kb][warp][__popc(mask & lanemask_lt())] = i;
-			if (kb + 1 == kBufSteps || k + 1 == a.K) {
-				flush_spike_buf(sb, a, p, P.list, N, k_first, kb + 1);
-				k_first = k + 1;
+			if (lane == 0 && word < nwords) bits[(int64_t)hslot * nwords + word] = mask;
+			if (mask) {  // one list reservation per warp with spikes
+				int base = 0;
+				if (lane == 0) base = atomicAdd(count + k * a.npop, __popc(mask));
+				base = __shfl_sync(0xffffffffu, base, 0);
+				if (spike) list[(int64_t)(a.list_k0 + k) * N + base + __popc(mask & lanemask_lt())] = i;
 			}
 			slot  = slot + 1 == D ? 0 : slot + 1;
 			hslot = hslot + 1 == Hb ? 0 : hslot + 1;
 		}
 	}
 	if (valid) {
-		P.V[i] = V;
-		P.T[i] = T;
+		Vp[i] = V;
+		Tp[i] = T;
 		if (cond) {
-			P.Gex[i] = Gex;
-			P.Gin[i] = Gin;
+			Pg->Gex[i] = Gex;
+			Pg->Gin[i] = Gin;
 		}
 	}
 }
@@ -387,7 +357,7 @@ __device__ void window_poisson(WindowArgs const& a, const PopDev* __restrict__ P
 	}
 	__syncthreads();
 	if (!mask) return;
-	int32_t* out = P.list + (int64_t)k * P.size + red[kThreads / 32] + red[warp] + (incl - mine);
+	int32_t* out = P.list + (int64_t)(a.list_k0 + k) * P.size + red[kThreads / 32] + red[warp] + (incl - mine);
 	unsigned m   = mask;
 	while (m) {
 		int const r = __ffs(m) - 1;
@@ -409,33 +379,39 @@ __device__ void window_external(WindowArgs const& a, const PopDev* __restrict__ 
 	for (int j = threadIdx.x; j < n; j += blockDim.x) {
 		int32_t const s = src[j];
 		atomicOr(bits + (s >> 5), 1u << (s & 31));
-		P.list[(int64_t)k * P.size + j] = s;
+		P.list[(int64_t)(a.list_k0 + k) * P.size + j] = s;
 	}
 	if (threadIdx.x == 0) a.counts[k * a.npop + p] = n;
 }
 
-// ONLY_FAST: every per-neuron population of the launch takes the FAST path, so the generic input
-// replay is compiled out (fewer registers).
+// Per-neuron populations: one thread per neuron, K steps with the state in registers.
+// ONLY_FAST: every population of the launch takes the FAST path, so the generic input replay is
+// compiled out (fewer registers).
 template <int MODE, bool ONLY_FAST>
-__global__ void __launch_bounds__(kThreads, 3) k_window(const __grid_constant__ WindowArgs a) {
-	__shared__ SpikeBuf sb;
+__global__ void __launch_bounds__(kThreads) k_neurons(const __grid_constant__ WindowArgs a) {
+	int const b = blockIdx.x;
+	int p       = 0;
+	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
+	int const lb = b - a.blk_begin[p];
+	if (a.blk_kind[p] == 3) window_neurons<MODE, true>(a, a.pops + p, p, lb);
+	else if (!ONLY_FAST) window_neurons<MODE, false>(a, a.pops + p, p, lb);
+}
+
+// Populations without inputs (Poisson, external trains): one CTA per (step, chunk).  They depend on
+// nothing but the step's random stream, so they run on a second stream, overlapped with the
+// neuron update and the delivery of the previous window.
+__global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ WindowArgs a) {
 	__shared__ int red[kThreads / 32 + 1];
 	int const b = blockIdx.x;
 	int p       = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb = b - a.blk_begin[p];
-	switch (a.blk_kind[p]) {
-		case 0:
-			if (!ONLY_FAST) window_neurons<MODE, false>(a, a.pops + p, p, lb, sb);
-			break;
-		case 1: window_poisson(a, a.pops + p, p, lb, red); break;
-		case 2: window_external(a, a.pops + p, p, lb); break;
-		case 3: window_neurons<MODE, true>(a, a.pops + p, p, lb, sb); break;
-	}
+	if (a.blk_kind[p] == 1) window_poisson(a, a.pops + p, p, lb, red);
+	else if (a.blk_kind[p] == 2) window_external(a, a.pops + p, p, lb);
 }
 
 template <int MODE>
-__global__ void k_deliver(const __grid_constant__ DeliverArgs a) {
+__global__ void __launch_bounds__(1024) k_deliver(const __grid_constant__ DeliverArgs a) {
 	extern __shared__ uint32_t tile_sm[];
 	__shared__ unsigned long long ev_block;
 	int const part = blockIdx.x % a.parts;
@@ -466,7 +442,7 @@ __global__ void k_deliver(const __grid_constant__ DeliverArgs a) {
 		if (k < 0 || k >= a.K) continue;
 		touched = true;
 		int const n          = a.counts[k * a.npop + C.src];
-		const int32_t* lst   = C.src_list + k * C.src_size;
+		const int32_t* lst   = C.src_list + (a.list_k0 + k) * C.src_size;
 		const int64_t* bnd   = C.bounds;
 		int const stride     = P.ntiles + 1;
 		const int32_t* nb    = C.nb;
@@ -599,7 +575,7 @@ __global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
 		if (k < 0 || k >= a.K) continue;
 		touched = true;
 		int const n        = a.counts[k * a.npop + C.src];
-		const int32_t* lst = C.src_list + k * C.src_size;
+		const int32_t* lst = C.src_list + (a.list_k0 + k) * C.src_size;
 		const int64_t* bnd = C.bounds;
 		int const stride   = P.ntiles + 1;
 		const int32_t* nb  = C.nb;
@@ -630,6 +606,126 @@ __global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
 	}
 	for (int d = 16; d; d >>= 1) my_events += __shfl_xor_sync(0xffffffffu, my_events, d);
 	if ((threadIdx.x & 31) == 0 && my_events) atomicAdd(&ev_block, my_events);
+	__syncthreads();
+	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+	if (!touched) return;
+	int64_t const slot = sigma % a.D;
+	if (MODE == 0) {
+		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) red_add_u32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) dst[i] += v;
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
+		}
+	} else {
+		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
+		const float* sm = reinterpret_cast<const float*>(tile_sm);
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) red_add_f32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
+		}
+	}
+}
+
+// Warp-per-spike variant of the tiled delivery: a warp takes 32 spikes, loads their sub-row bounds
+// lane-parallel, then streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced
+// loads, 8 in flight per lane, no cross-lane search).
+template <int MODE>
+__global__ void __launch_bounds__(1024) k_deliver_wps(const __grid_constant__ DeliverArgs a) {
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	int const part = blockIdx.x % a.parts;
+	int const b    = blockIdx.x / a.parts;
+	int const si   = b / a.ntiles_total;
+	int const g    = b - si * a.ntiles_total;
+	int Q          = 0;
+	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
+	PopDev const& P = a.pops[Q];
+	int const t     = g - a.tile_begin[Q];
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
+	if (threadIdx.x == 0) ev_block = 0;
+	__syncthreads();
+	int64_t const sigma = a.slot_lo + si;
+	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+	unsigned long long my_events = 0;
+	bool touched = false;
+	for (int ci = P.in_begin; ci < P.in_end; ci++) {
+		ConnDev const& C = a.conns[ci];
+		int64_t const k  = sigma - (a.t0 + C.delay - 1);
+		if (k < 0 || k >= a.K) continue;
+		touched = true;
+		int const n        = a.counts[k * a.npop + C.src];
+		const int32_t* lst = C.src_list + (a.list_k0 + k) * C.src_size;
+		const int64_t* bnd = C.bounds + t;
+		int const stride   = P.ntiles + 1;
+		const int32_t* nb  = C.nb;
+		int const word     = MODE == 0 ? C.word : C.fslot;
+		uint32_t const inc = C.inc;
+		float const w      = C.weight;
+		for (int j0 = (part * nwarps + warp) * 32; j0 < n; j0 += a.parts * nwarps * 32) {
+			int64_t start = 0;
+			int len       = 0;
+			if (j0 + lane < n) {
+				int const s       = __ldg(lst + j0 + lane);
+				const int64_t* bb = bnd + (int64_t)s * stride;
+				start             = __ldg(bb);
+				len               = (int)(__ldg(bb + 1) - start);
+			}
+			my_events += (unsigned long long)len;
+			int const nq = min(32, n - j0);
+			for (int q0 = 0; q0 < nq; q0 += 8) {
+				int32_t d[8];
+#pragma unroll
+				for (int u = 0; u < 8; u++) {
+					int64_t const st = __shfl_sync(0xffffffffu, start, (q0 + u) & 31);
+					int const ln     = __shfl_sync(0xffffffffu, len, (q0 + u) & 31);
+					d[u]             = (q0 + u < nq && lane < ln) ? __ldg(nb + st + lane) : -1;
+				}
+#pragma unroll
+				for (int u = 0; u < 8; u++)
+					if (d[u] >= 0) {
+						int const li = (d[u] - tbase) * width + word;
+						if (MODE == 0) atomicAdd(tile_sm + li, inc);
+						else atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+					}
+				// sub-rows longer than a warp (large tiles): the rest, spike by spike
+#pragma unroll 1
+				for (int u = 0; u < 8; u++) {
+					int64_t const st = __shfl_sync(0xffffffffu, start, (q0 + u) & 31);
+					int const ln     = __shfl_sync(0xffffffffu, len, (q0 + u) & 31);
+					if (q0 + u >= nq || ln <= 32) continue;
+					for (int e = 32 + lane; e < ln; e += 32) {
+						int const li = (__ldg(nb + st + e) - tbase) * width + word;
+						if (MODE == 0) atomicAdd(tile_sm + li, inc);
+						else atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+					}
+				}
+			}
+		}
+	}
+	for (int d = 16; d; d >>= 1) my_events += __shfl_xor_sync(0xffffffffu, my_events, d);
+	if (lane == 0 && my_events) atomicAdd(&ev_block, my_events);
 	__syncthreads();
 	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
 	if (!touched) return;
@@ -879,17 +975,23 @@ cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t n
 	return cudaGetLastError();
 }
 
-cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks) {
+cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks) {
 	if (nblocks <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0;
 	if (a.mode == 0) {
-		if (only_fast) k_window<0, true><<<nblocks, kThreads, 0, stream>>>(a);
-		else k_window<0, false><<<nblocks, kThreads, 0, stream>>>(a);
+		if (only_fast) k_neurons<0, true><<<nblocks, kThreads, 0, stream>>>(a);
+		else k_neurons<0, false><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
-		if (only_fast) k_window<1, true><<<nblocks, kThreads, 0, stream>>>(a);
-		else k_window<1, false><<<nblocks, kThreads, 0, stream>>>(a);
+		if (only_fast) k_neurons<1, true><<<nblocks, kThreads, 0, stream>>>(a);
+		else k_neurons<1, false><<<nblocks, kThreads, 0, stream>>>(a);
 	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_sources(cudaStream_t stream, WindowArgs const& a, int nblocks) {
+	if (nblocks <= 0) return cudaSuccess;
+	k_sources<<<nblocks, kThreads, 0, stream>>>(a);
 	return cudaGetLastError();
 }
 
@@ -899,10 +1001,15 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		if (a.counts_next_len > 0) return cudaMemsetAsync(a.counts_next, 0, sizeof(int32_t) * a.counts_next_len, stream);
 		return cudaSuccess;
 	}
-	static int configured[4] = {0, 0, 0, 0};
-	int const m = (a.mode == 0 ? 0 : 1) + 2 * (a.algo == 1);
-	void const* fn = m == 0 ? (void const*)k_deliver<0> : m == 1 ? (void const*)k_deliver<1>
-	               : m == 2 ? (void const*)k_deliver_tps<0> : (void const*)k_deliver_tps<1>;
+	static int configured[6] = {0, 0, 0, 0, 0, 0};
+	int const m = (a.mode == 0 ? 0 : 1) + 2 * a.algo;
+	void const* fns[6] = {(void const*)k_deliver<0>,     (void const*)k_deliver<1>,
+	                      (void const*)k_deliver_tps<0>, (void const*)k_deliver_tps<1>,
+	                      (void const*)k_deliver_wps<0>, (void const*)k_deliver_wps<1>};
+	void const* fn = fns[m];
+	cudaFuncAttributes fa;
+	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
+		threads = fa.maxThreadsPerBlock / 32 * 32;  // the launch shape never changes results
 	if (configured[m] < a.smem_bytes) {
 		cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, a.smem_bytes);
 		if (e != cudaSuccess) return e;
@@ -913,6 +1020,8 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		case 1: k_deliver<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 2: k_deliver_tps<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 3: k_deliver_tps<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 4: k_deliver_wps<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 5: k_deliver_wps<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 	}
 	return cudaGetLastError();
 }
