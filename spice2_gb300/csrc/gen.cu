@@ -379,3 +379,65 @@ fail:
 }
 
 }  // namespace spice_gb300
+
+namespace spice_gb300 {
+
+// The generator pipeline of generate_fixed_probability for one projection, with every scratch
+// buffer supplied by the caller (GenScratch) and the neighbours written to a caller buffer of
+// `capacity` entries.  Allocates nothing.  Synchronises `stream` once, to read the synapse count.
+cudaError_t generate_fixed_probability_into(cudaStream_t stream, int64_t src, int64_t dst, double p, u128 seed,
+                                            GenScratch const& sc, int64_t* offsets, int32_t* neighbors,
+                                            int64_t capacity, int64_t* synapses) {
+	*synapses = 0;
+	if (src == 0 || dst == 0 || p == 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t) * (src + 1), stream);
+	int64_t const md     = fp_max_degree(dst, p);
+	int64_t const nd     = src * (md + 1);
+	int64_t const nsuper = (nd + kSuper - 1) / kSuper;
+	int64_t const nchunk = (nd + kSubDraws - 1) / kSubDraws;
+	if (nd > sc.max_draws || src > sc.max_src || nsuper > sc.max_super) return cudaErrorInvalidValue;
+	// jump polynomials: x^(65536 m) and x^(256 j) mod P, computed once per process on the host
+	struct Polys {
+		u128 sub[kGenThreads];
+		u128 sup[64];
+	};
+	static Polys const polys = [] {  // thread-safe one-time initialisation
+		Polys q;
+		u128 const step = gf2_xpow(kSubDraws), stride = gf2_xpow(kSuper);
+		q.sub[0] = {1, 0};
+		for (int j = 1; j < kGenThreads; j++) q.sub[j] = gf2_mulmod(q.sub[j - 1], step);
+		q.sup[0] = {1, 0};
+		for (int m = 1; m < 64; m++) q.sup[m] = gf2_mulmod(q.sup[m - 1], stride);
+		return q;
+	}();
+	if (nsuper > 64) return cudaErrorInvalidValue;
+	cudaError_t e = cudaMemcpyAsync(sc.subpolys, polys.sub, sizeof(polys.sub), cudaMemcpyHostToDevice, stream);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(sc.polys, polys.sup, sizeof(u128) * nsuper, cudaMemcpyHostToDevice, stream);
+	if (e != cudaSuccess) return e;
+	double const bound = (double)dst + 36.75 * (1 / p - 1) + 4;
+	int shift          = 61 - (int)ceil(log2(bound));
+	shift              = std::min(40, std::max(shift, 8));
+	k_superstates<<<1, 256, 0, stream>>>(seed, sc.polys, nsuper, sc.superstates);
+	k_gaps<<<(unsigned)nsuper, kGenThreads, 0, stream>>>(sc.superstates, sc.subpolys, 1 / p - 1, ldexp(1.0, shift), nd,
+	                                                     sc.gaps, sc.fx, sc.tots);
+	k_scan_u64<<<1, 1024, 0, stream>>>(sc.tots, nchunk);
+	k_add_chunk_prefix<<<1216, 256, 0, stream>>>(sc.fx, sc.tots, nd);
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	RowJob const job = {sc.gaps, sc.fx, nd, src, dst, md, shift, sc.lens, sc.fallbacks};
+	if ((e = cudaMemsetAsync(sc.lens, 0, sizeof(int32_t) * src, stream)) != cudaSuccess) return e;
+	if ((e = cudaMemsetAsync(sc.fallbacks, 0, sizeof(unsigned long long), stream)) != cudaSuccess) return e;
+	if ((e = cudaMemcpyAsync(sc.job, &job, sizeof(RowJob), cudaMemcpyHostToDevice, stream)) != cudaSuccess) return e;
+	k_rows<<<1, 32, 0, stream>>>(reinterpret_cast<const RowJob*>(sc.job));
+	if ((e = cudaGetLastError()) != cudaSuccess) return e;
+	if ((e = scan_row_lengths_into(stream, sc.lens, src, offsets, sc.block_sums)) != cudaSuccess) return e;
+	int64_t total = 0;
+	if ((e = cudaMemcpyAsync(&total, offsets + src, sizeof(int64_t), cudaMemcpyDeviceToHost, stream)) != cudaSuccess) return e;
+	if ((e = cudaStreamSynchronize(stream)) != cudaSuccess) return e;
+	*synapses = total;
+	if (total > capacity) return cudaErrorInvalidValue;
+	k_fill<<<(unsigned)((src + 255) / 256), 256, 0, stream>>>(sc.gaps, offsets, src, neighbors);
+	return cudaGetLastError();
+}
+
+size_t gen_row_job_bytes() { return sizeof(RowJob); }
+
+}  // namespace spice_gb300

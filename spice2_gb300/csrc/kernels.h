@@ -25,9 +25,31 @@ cudaError_t generate_fixed_probability(cudaStream_t stream, std::vector<GenReque
 // Rows whose stop index was recomputed with the exact sequential loop (near-tie sums), process-wide.
 extern unsigned long long g_gen_fallbacks;
 
+// Scratch of one projection's generation (generate_fixed_probability_into).
+struct GenScratch {
+	double* gaps;          // [max_draws]
+	uint64_t* fx;          // [max_draws]
+	uint64_t* tots;        // [max_draws / 256]
+	int32_t* lens;         // [max_src]
+	u128* superstates;     // [max_super]
+	u128* polys;           // [max_super]
+	u128* subpolys;        // [256]
+	int64_t* block_sums;   // [max_src / 1024 + 1]
+	void* job;             // gen_row_job_bytes()
+	unsigned long long* fallbacks;
+	int64_t max_draws, max_src, max_super;
+};
+size_t gen_row_job_bytes();
+cudaError_t generate_fixed_probability_into(cudaStream_t stream, int64_t src, int64_t dst, double p, u128 seed,
+                                            GenScratch const& sc, int64_t* offsets, int32_t* neighbors,
+                                            int64_t capacity, int64_t* synapses);
+
 // ---- step.cu ----
 // Exclusive scan of n int32 row lengths into n + 1 int64 offsets.
 cudaError_t scan_row_lengths(cudaStream_t stream, const int32_t* lens, int64_t n, int64_t* offsets);
+// The same with caller-provided block sums (n / 1024 + 1 entries).
+cudaError_t scan_row_lengths_into(cudaStream_t stream, const int32_t* lens, int64_t n, int64_t* offsets,
+                                  int64_t* block_sums);
 
 // Maximum in-degree of target population neurons over the connections of one input group.
 cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const int64_t* nsyn, int nconn,

@@ -130,6 +130,11 @@ int harvest(spice_net* n) {
 
 }  // namespace
 
+namespace spice_gb300 {
+// Records the calling thread's last error for spice_last_error() (for other translation units).
+int set_last_error(int code, std::string const& msg) { return fail(code, msg); }
+}  // namespace spice_gb300
+
 // ------------------------------------------------------------------------------------------------
 // construction
 // ------------------------------------------------------------------------------------------------

@@ -957,6 +957,16 @@ cudaError_t scan_row_lengths(cudaStream_t stream, const int32_t* lens, int64_t n
 	return err;
 }
 
+cudaError_t scan_row_lengths_into(cudaStream_t stream, const int32_t* lens, int64_t n, int64_t* offsets,
+                                  int64_t* block_sums) {
+	if (n <= 0) return cudaMemsetAsync(offsets, 0, sizeof(int64_t), stream);
+	int64_t const nb = (n + kScanItems - 1) / kScanItems;
+	k_scan_local<<<(unsigned)nb, kScanItems, 0, stream>>>(lens, n, offsets, block_sums);
+	k_scan_sums<<<1, kScanItems, 0, stream>>>(block_sums, nb);
+	k_scan_add<<<(unsigned)nb, kScanItems, 0, stream>>>(offsets, n, block_sums);
+	return cudaGetLastError();
+}
+
 cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const int64_t* nsyn, int nconn,
                          int64_t dst_size, uint32_t* scratch, uint32_t* max_out) {
 	cudaError_t err = cudaMemsetAsync(scratch, 0, sizeof(uint32_t) * (dst_size > 0 ? dst_size : 1), stream);
