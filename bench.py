@@ -205,6 +205,10 @@ def main():
     synapses = sum(net.synapses(c) for c in range(6))
     stream = torch.cuda.ExternalStream(net.stream_handle())
 
+    # launch shape of the delivery kernel, measured on this network (results do not depend on it)
+    from spice2_gb300.autotune import autotune
+    tuned = autotune(net, steps=300, warm=30)["best"]
+
     for _ in range(args.warmup):
         net.run(STEPS_PER_RUN)
     net.synchronize()
@@ -262,6 +266,7 @@ def main():
     if rank == 0:
         del net
         net2, _ = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_ATOMIC)
+        autotune(net2, steps=300, warm=30)
         for _ in range(args.warmup):
             net2.run(STEPS_PER_RUN)
         net2.synchronize()
@@ -311,6 +316,7 @@ def main():
                    "sim_steps_per_bench_step": STEPS_PER_RUN, "dt": DT,
                    "delay_steps": 15, "mode": "deterministic", "seed": SEED,
                    "parallelism": f"replicas{ws}" if ws > 1 else "single",
+                   "delivery_shape": tuned,
                    "l2": "inputs larger than L2 (1 GB of CSR targets; a window reads ~42 MB of random rows)"},
         "sim_seconds_per_wall_second": STEPS_PER_RUN * args.steps * DT / (ms_max / 1e3),
         "ms_per_sim_step": ms_max / args.steps / STEPS_PER_RUN,

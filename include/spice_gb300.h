@@ -100,7 +100,9 @@ enum {
 	SPICE_TUNE_DELIVER_THREADS = 1, /* threads per delivery CTA                               */
 	SPICE_TUNE_DELIVER_PARTS   = 2, /* CTAs sharing one (input slot, tile)                    */
 	SPICE_TUNE_DELIVER_ALGO    = 3, /* 0: warp-flattened sub-rows, 1: one thread per spike,
-	                                   2: one warp per spike, 8 sub-rows in flight          */
+	                                   2: one warp per spike, 8 sub-rows in flight,
+	                                   3: one thread per spike with 16-byte loads           */
+	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

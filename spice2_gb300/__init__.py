@@ -298,7 +298,8 @@ class snn:
         _check(lib().spice_set_window(self._h, w))
 
     def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
-                   deliver_parts: int | None = None, deliver_algo: int | None = None):
+                   deliver_parts: int | None = None, deliver_algo: int | None = None,
+                   overlap_sources: bool | None = None):
         """Delivery launch shape (any time between steps); results are independent of it."""
         if tile_bytes is not None:
             _check(lib().spice_set_tuning(self._h, 0, int(tile_bytes)))
@@ -308,6 +309,8 @@ class snn:
             _check(lib().spice_set_tuning(self._h, 2, int(deliver_parts)))
         if deliver_algo is not None:
             _check(lib().spice_set_tuning(self._h, 3, int(deliver_algo)))
+        if overlap_sources is not None:
+            _check(lib().spice_set_tuning(self._h, 4, int(bool(overlap_sources))))
 
     # stepping
     def step(self):

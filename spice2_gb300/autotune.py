@@ -1,0 +1,69 @@
+"""Launch-shape autotuner for the delivery kernel of a network.
+
+The delivery kernel accumulates events per (input slot, target tile) in shared memory; its tile
+size, CTA size and work mapping change its speed but never its results (the parity tests run every
+shape).  The best shape depends on the network (population sizes, out-degree, firing rate), so it
+is measured on the network itself: each candidate runs a stretch of simulation steps with per-kernel
+CUDA-event timing, the source populations serialised onto the main stream so the delivery timing
+is not shared with the overlapped source kernel.  The simulation state advances during tuning (the
+steps are real steps of the network).
+
+usage:  python -m spice2_gb300.autotune --brunel 500000 0.002 [--steps 600]
+"""
+from __future__ import annotations
+
+import argparse
+import itertools
+import json
+import sys
+
+DEFAULT_CANDIDATES = [
+    # (tile bytes, threads per CTA, parts per (slot, tile), work mapping)
+    (12 * 1024, 256, 1, 1), (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1),
+    (48 * 1024, 1024, 1, 1), (96 * 1024, 1024, 1, 1), (24 * 1024, 256, 2, 1), (24 * 1024, 256, 1, 0),
+    (48 * 1024, 512, 1, 3),
+]
+
+
+def autotune(net, steps: int = 600, warm: int = 60, candidates=None, verbose: bool = False) -> dict:
+    """Times the delivery kernel of `net` for each candidate shape; applies and returns the best."""
+    cands = candidates or DEFAULT_CANDIDATES
+    results = []
+    net.set_tuning(overlap_sources=False)
+    for tb, th, parts, algo in cands:
+        net.set_tuning(tile_bytes=tb, deliver_threads=th, deliver_parts=parts, deliver_algo=algo)
+        net.run(warm)
+        net.synchronize()
+        net.set_profiling(True)
+        net.run(steps)
+        net.synchronize()
+        n, ms = net.kernel_stats(1)
+        net.set_profiling(False)
+        us = 1e3 * ms / max(n, 1)
+        results.append({"tile_bytes": tb, "threads": th, "parts": parts, "algo": algo, "deliver_us": us})
+        if verbose:
+            print(f"tile {tb // 1024:4d} KiB  threads {th:5d}  parts {parts}  algo {algo}:  deliver {us:8.2f} us",
+                  flush=True)
+    best = min(results, key=lambda r: r["deliver_us"])
+    net.set_tuning(tile_bytes=best["tile_bytes"], deliver_threads=best["threads"], deliver_parts=best["parts"],
+                   deliver_algo=best["algo"], overlap_sources=True)
+    return {"best": best, "results": results}
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--brunel", nargs=2, metavar=("N", "P"), default=["500000", "0.002"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--mode", type=int, default=0)
+    args = ap.parse_args(argv)
+    import spice2_gb300 as sp
+    net, _ = sp.brunel(int(args.brunel[0]), float(args.brunel[1]), args.seed, mode=args.mode)
+    net.run(300)
+    rep = autotune(net, steps=args.steps, verbose=True)
+    print(json.dumps(rep["best"]))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -177,5 +177,6 @@ struct spice_net {
 	int deliver_threads = 256;       // threads per delivery CTA (tunable)
 	int deliver_parts = 1;           // CTAs per (slot, tile) (tunable)
 	int deliver_algo = 1;            // delivery work mapping (tunable)
+	int overlap_sources = 1;         // source kernels on their own stream (tunable)
 	int dmin = 1, dmax = 1;          // connection delays in steps
 };

@@ -717,13 +717,14 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			wa.blk_begin[np] = nb;
 			ws.blk_begin[np] = nbs;
 			int slot = -1;
+			cudaStream_t const ss = n->overlap_sources ? n->stream_src : n->stream;
 			if (nbs > 0) {
 				// sources of this window may start once the lists of this parity are free
-				CUDA_TRY(cudaStreamWaitEvent(n->stream_src, n->ev_free[q], 0));
-				TRY(ev_begin(n, 3, &slot, n->stream_src));
-				CUDA_TRY(launch_sources(n->stream_src, ws, nbs));
-				TRY(ev_end(n, slot, n->stream_src));
-				CUDA_TRY(cudaEventRecord(n->ev_src[q], n->stream_src));
+				CUDA_TRY(cudaStreamWaitEvent(ss, n->ev_free[q], 0));
+				TRY(ev_begin(n, 3, &slot, ss));
+				CUDA_TRY(launch_sources(ss, ws, nbs));
+				TRY(ev_end(n, slot, ss));
+				CUDA_TRY(cudaEventRecord(n->ev_src[q], ss));
 				n->launches++;
 			}
 			TRY(ev_begin(n, 0, &slot));
@@ -1048,8 +1049,16 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->deliver_threads = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_ALGO:
-			if (value < 0 || value > 2) return fail(SPICE_EINVAL, "delivery algorithm must be 0, 1 or 2");
+			if (value < 0 || value > 3) return fail(SPICE_EINVAL, "delivery algorithm must be 0, 1, 2 or 3");
 			n->deliver_algo = (int)value;
+			return SPICE_OK;
+		case SPICE_TUNE_OVERLAP_SOURCES:
+			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "overlap must be 0 or 1");
+			if (n->prepared) {
+				CUDA_TRY(cudaStreamSynchronize(n->stream));
+				if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
+			}
+			n->overlap_sources = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_PARTS: {
 			if (value < 1 || value > 64) return fail(SPICE_EINVAL, "parts must be in [1, 64]");
