@@ -39,9 +39,14 @@ sys.path.insert(0, ROOT)
 N_NEURONS, P_CONN, SEED, STEPS_PER_RUN = 500000, 0.002, 1, 2000
 DT = 1e-4
 WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
-# DRAM bytes (read + write) per synaptic event of the delivery kernel, from the ncu capture summarised
-# in profiles/ (dram__bytes_read.sum + dram__bytes_write.sum over the events of the captured launch).
-DELIVER_DRAM_BYTES_PER_EVENT = None
+# DRAM bytes (read + write) per synaptic event of the delivery kernel: dram__bytes_read.sum +
+# dram__bytes_write.sum of one captured k_deliver_tps launch (Brunel N=2e5, p=0.005, the 16th window,
+# 4,235,947 events; profiles/k_deliver_tps_k_neurons_k_sources_brunel_N2e5_p0.005.md) divided by its
+# events.  The bench's traffic per launch is this figure times the launch's mean events (the capture
+# runs on a smaller network than the bench so that the ncu replay stays small; the traffic per
+# event does not depend on the network size as long as the rows do not fit in L2).
+DELIVER_DRAM_BYTES_PER_EVENT = (22.117120e6 + 1.792e3) / 4235947
+DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>"}
 
 
 def _dist():
@@ -326,7 +331,7 @@ def main():
                 "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                     "kernel": "k_deliver", "bytes_per_event": bytes_per_event, "peak_source": f"{peak_kind} hbm_gbs",
+                     "kernel": DELIVER_KERNELS.get(tuned["algo"], "k_deliver"), "bytes_per_event": bytes_per_event, "peak_source": f"{peak_kind} hbm_gbs",
                      "launches": n_del, "mean_launch_us": t_launch * 1e6,
                      "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3},
         "cpu_baseline": cpu,

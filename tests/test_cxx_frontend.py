@@ -1,0 +1,74 @@
+"""The C++ front end (include/spice/snn.h): the reference's Brunel sample, unchanged in its calls,
+compiled with g++ -std=c++20 against the header and run on the GPU; its JSON raster equals the
+reference's (tests/golden/brunel_n20000.npz, README.md:110-116)."""
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+HEADER_USE = r"""
+#include "spice/snn.h"
+using namespace spice;
+int main() {
+	snn net(1e-4f, 8e-4f, {1337});
+	auto P = net.add_population<poisson>(10);
+	auto E = net.add_population<lif_cond>(10);
+	auto L = net.add_population<lif>(5);
+	auto X = net.add_population<external_input>(3, {{{1, 2}, {0}}});
+	adj_list a;
+	a.connect(0, 1);
+	net.connect<excitatory>(E, E, a, 8e-4f, {0.1f});
+	net.connect<inhibitory>(E, L, fixed_probability(0.5), 8e-4f, {0.1f});
+	net.connect<fixed_weight>(P, L, fixed_probability(0.5), 8e-4f, {1.f});
+	net.step();
+	auto s = X->spikes(0);
+	auto v = E->get_neurons();
+	auto w = L->get_neurons();
+	return int(s.size() + v.size() + w.size() + P->size()) & 0;
+}
+"""
+
+
+def test_cxx_header_compiles(tmp_path):
+    """Every model, synapse and topology of the header instantiates under g++ -std=c++20 -Wall."""
+    src = tmp_path / "use.cpp"
+    src.write_text(HEADER_USE)
+    subprocess.run(["g++", "-std=c++20", "-Wall", "-Wextra", "-Werror", "-fsyntax-only", "-I",
+                    os.path.join(ROOT, "include"), str(src)], check=True)
+
+
+@pytest.mark.gpu
+def test_cxx_brunel_sample_matches_reference(engine, tmp_path):
+    exe = tmp_path / "brunel"
+    libdir = os.path.join(ROOT, "spice2_gb300")
+    subprocess.run(["g++", "-std=c++20", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "spice2_gb300", "examples", "brunel.cpp"), "-L", libdir, "-lspice_gb300",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    rows = json.loads(out)["spikes"]
+    g = np.load(os.path.join(GOLDEN, "brunel_n20000.npz"))
+    counts, idx = g["counts"], g["idx"]
+    assert len(rows) == counts.shape[0]
+    pos = 0
+    for t, row in enumerate(rows):
+        per = []
+        for k in range(3):
+            per.append(idx[pos:pos + counts[t, k]])
+            pos += counts[t, k]
+        P, E, I = per
+        expect = [int(x) for x in I] + [int(x) + 2000 for x in E] + [int(x) + 10000 for x in P]
+        assert row == expect, f"step {t}"
+    assert rows[0][:3] == [10533, 11015, 11209]  # README.md:112
+
+
+@pytest.mark.gpu
+def test_samples_cli_brunel_json(engine, capsys):
+    """python -m spice2_gb300.samples brunel --json prints the reference's README raster."""
+    from spice2_gb300 import samples
+    samples.main(["brunel", "--steps", "5", "--json"])
+    rows = json.loads(capsys.readouterr().out)["spikes"]
+    assert len(rows) == 5 and rows[0][:3] == [10533, 11015, 11209] and rows[1][:3] == [10310, 11115, 11884]
