@@ -103,6 +103,7 @@ enum {
 	                                   2: one warp per spike, 8 sub-rows in flight,
 	                                   3: one thread per spike with 16-byte loads           */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
+	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's
@@ -175,6 +176,32 @@ int spice_launch_count(spice_net* net, int64_t* launches_out);
 int spice_get_stream(spice_net* net, void** stream_out);
 int spice_synchronize(spice_net* net);
 const char* spice_last_error(void);
+
+/* ---- Batched networks (no counterpart in the reference) ----
+ * Many independent nets stepped together: one launch per kernel kind and window covers the
+ * populations and connections of every member, so networks far too small to fill the GPU alone
+ * run at the throughput of one large network.  The members are ordinary nets built with the calls
+ * above (each with its own populations, connections and seed); they must share dt, max_delay,
+ * mode and time, have the same minimum delay and no external_input population.  The batch runs
+ * on the members' own device state: between batch runs every per-net call (spikes, state, csr,
+ * events, spice_run) works on each member as usual, and a member's results are bit-identical to
+ * running it alone.  The window loop is captured in a CUDA graph (SPICE_TUNE_GRAPH_WINDOWS windows
+ * per graph launch, default 8); each window's time-dependent values (time, dt, step seeds) are
+ * advanced on the device, so the graph is replayed unchanged.  The members must stay alive while
+ * the batch exists; tuning knobs 0..4 set on a batch apply to it and to every member. */
+typedef struct spice_batch spice_batch;
+int spice_batch_create(spice_net* const* nets, int nnets, spice_batch** out);
+int spice_batch_destroy(spice_batch* batch);
+/* `steps` steps of every member; returns when they are done. */
+int spice_batch_run(spice_batch* batch, int64_t steps);
+int spice_batch_set_tuning(spice_batch* batch, int knob, int64_t value);
+/* Per-kernel timing (CUDA events; windows launched directly, not through the graph).  Kinds as
+ * spice_kernel_stats, plus 4 = window prologue (dt, step seeds) and jump tables. */
+int spice_batch_set_profiling(spice_batch* batch, int on);
+int spice_batch_kernel_stats(spice_batch* batch, int kind, int64_t* launches_out, double* ms_out);
+/* Kernels launched for this batch so far (graph replays count their kernels). */
+int spice_batch_launch_count(spice_batch* batch, int64_t* launches_out);
+int spice_batch_get_stream(spice_batch* batch, void** stream_out);
 
 #ifdef __cplusplus
 }

@@ -93,6 +93,14 @@ def _load():
         "spice_get_stream": [vp, P(vp)],
         "spice_set_tuning": [vp, i32, i64],
         "spice_synchronize": [vp],
+        "spice_batch_create": [P(vp), i32, P(vp)],
+        "spice_batch_destroy": [vp],
+        "spice_batch_run": [vp, i64],
+        "spice_batch_set_tuning": [vp, i32, i64],
+        "spice_batch_set_profiling": [vp, i32],
+        "spice_batch_kernel_stats": [vp, i32, P(i64), P(f64)],
+        "spice_batch_launch_count": [vp, P(i64)],
+        "spice_batch_get_stream": [vp, P(vp)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -430,6 +438,87 @@ def brunel(N: int, p: float, seed: int = 1337, dt: float = 1e-4, delay: float = 
     return net, (P, E, I)
 
 
+class batch:
+    """Many independent nets stepped together (spice_batch_* in include/spice_gb300.h): one launch
+    per kernel kind and window covers every member, and full windows replay as a CUDA graph.  The
+    members keep working as ordinary nets between runs, and each member's results are identical to
+    running it alone.  No counterpart in the reference."""
+
+    def __init__(self, nets: Sequence[snn]):
+        self._nets = list(nets)
+        arr = (C.c_void_p * max(1, len(self._nets)))(*[n._h for n in self._nets])
+        h = C.c_void_p()
+        _check(lib().spice_batch_create(arr, len(self._nets), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().spice_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def nets(self) -> list:
+        return list(self._nets)
+
+    def run(self, steps: int):
+        _check(lib().spice_batch_run(self._h, int(steps)))
+
+    def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
+                   deliver_parts: int | None = None, deliver_algo: int | None = None,
+                   overlap_sources: bool | None = None, graph_windows: int | None = None):
+        """Launch shape of the batch (and of its members); results are independent of it."""
+        for knob, v in ((0, tile_bytes), (1, deliver_threads), (2, deliver_parts), (3, deliver_algo),
+                        (4, None if overlap_sources is None else int(bool(overlap_sources))), (5, graph_windows)):
+            if v is not None:
+                _check(lib().spice_batch_set_tuning(self._h, knob, int(v)))
+
+    def set_profiling(self, on: bool):
+        _check(lib().spice_batch_set_profiling(self._h, 1 if on else 0))
+
+    def kernel_stats(self, kind: int):
+        n, ms = C.c_int64(), C.c_double()
+        _check(lib().spice_batch_kernel_stats(self._h, kind, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def launch_count(self) -> int:
+        v = C.c_int64()
+        _check(lib().spice_batch_launch_count(self._h, C.byref(v)))
+        return v.value
+
+    def synchronize(self):
+        """spice_batch_run returns when its steps are done; kept for the tuner's interface."""
+
+    def stream_handle(self) -> int:
+        v = C.c_void_p()
+        _check(lib().spice_batch_get_stream(self._h, C.byref(v)))
+        return v.value or 0
+
+    @property
+    def events(self) -> int:
+        return sum(n.events for n in self._nets)
+
+
+def brunel_sweep_sizes(count: int = 256, n_min: int = 5000, n_max: int = 80000, seed: int = 4):
+    """Network sizes of the batched Brunel sweep: `count` sizes drawn log-uniformly from
+    [n_min, n_max] with a seeded numpy generator, rounded to multiples of 10 (so the 5:4:1
+    P/E/I split is exact)."""
+    rng = np.random.default_rng(seed)
+    n = np.exp(rng.uniform(np.log(n_min), np.log(n_max), size=count))
+    return [int(round(x / 10.0)) * 10 for x in n]
+
+
+def brunel_sweep(sizes: Sequence[int], seed0: int = 1000, mode: int = MODE_DETERMINISTIC):
+    """One Brunel net per size with p = 0.1 * min(1, 2e4 / N) (weights scaled by 0.1/p) and seed
+    seed0 + i.  Returns a list of (net, (P, E, I))."""
+    return [brunel(int(N), 0.1 * min(1.0, 20000.0 / N), seed0 + i, mode=mode) for i, N in enumerate(sizes)]
+
+
 __all__ = ["snn", "Population", "poisson", "lif", "lif_cond", "external_input", "fixed_weight", "excitatory",
-           "inhibitory", "fixed_probability", "adj_list", "brunel", "SpiceError", "LogicError", "CudaError",
-           "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib"]
+           "inhibitory", "fixed_probability", "adj_list", "brunel", "batch", "brunel_sweep", "brunel_sweep_sizes",
+           "SpiceError", "LogicError", "CudaError", "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib"]

@@ -67,6 +67,7 @@ struct PopDev {
 	int zero_inputs;     // 1: the input ring is accumulated (mixed delays), consumers clear it;
 	                     // 0: each slot is fully overwritten by one delivery, no clearing needed
 	const u128* chunk_poly;  // POISSON: x^(draw_offset + 32 c) mod P for chunk c
+	int net;             // index of the owning net in a batch (0 outside batches)
 	// EXTERNAL: cyclic train
 	const int32_t* ext_counts;
 	const int64_t* ext_off;
@@ -180,3 +181,9 @@ struct spice_net {
 	int overlap_sources = 1;         // source kernels on their own stream (tunable)
 	int dmin = 1, dmax = 1;          // connection delays in steps
 };
+
+namespace spice_gb300 {
+int set_last_error(int code, std::string const& msg);  // net.cu
+int neuron_block_kind(PopDev const& P);                  // net.cu
+int net_prepare(spice_net* n);                           // net.cu
+}  // namespace spice_gb300

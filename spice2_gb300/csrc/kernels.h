@@ -70,6 +70,7 @@ struct WindowArgs {
 	const PopDev* pops;
 	const float* dts;     // dt of steps t0 .. t0+K-1
 	const u128* tables;   // jump tables of step t0 (then t0+1, ...)
+	int64_t tab_net_stride;  // 0: one net
 	int32_t* counts;      // [K][npop] spikes per step and population (window parity buffer)
 	int list_k0;          // first list slot of this window's parity: lists are [2K][size]
 	int blk_begin[kMaxPops + 1];
@@ -133,5 +134,49 @@ struct RasterArgs {
 	int64_t row0;
 };
 cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a);
+
+// ---- batched networks (step.cu kernels, batch.cu runtime) ----
+// The window a batch's kernels step, advanced on the device by k_batch_prologue.
+struct BatchClock {
+	int64_t t0;          // first step of the current window
+	int parity;          // counts / list half of the current window
+	int k;               // steps in the current window
+	int64_t next_t0;
+	int next_parity;
+	float kahan_c, kahan_sum;  // the nets' shared dt accumulator (identical dt and time)
+};
+
+// Fixed arguments of a batch's kernels.  Populations are numbered net-major; PopDev::net is the
+// net, PopDev::in_begin/in_end index `conns` (all nets' connections in by-target order, src
+// renumbered to the global population index).
+struct BatchArgs {
+	const PopDev* pops;
+	const ConnDev* conns;
+	int npop, nnets;
+	const int* nblk_begin;   // [npop + 1] per-neuron CTAs (k_batch_neurons)
+	const int* nblk_kind;    // [npop] 0 generic, 3 fast LIF
+	int nblk_total;
+	const int* sblk_begin;   // [npop + 1] Poisson CTAs per step (k_batch_sources)
+	int sblk_total;
+	const int* tile_begin;   // [npop + 1] delivery tiles
+	int ntiles_total;
+	int32_t* counts;         // [2][K][npop]
+	float* dts;              // [K] dt of the current window's steps
+	u128* step_seeds;        // [nnets][K]
+	u128* tables;            // [nnets][K][kJumpTable]
+	u128* seed_state;        // [nnets] seed_seq states
+	unsigned long long* const* net_events;  // [nnets] each net's event counter
+	BatchClock* clock;
+	float dt;
+	int K, Hb;
+	int64_t D;
+	int mode, dmin, dmax, parts, algo, smem_bytes, only_fast;
+};
+cudaError_t launch_batch_prologue(cudaStream_t stream, BatchArgs const& b, int k);
+cudaError_t launch_batch_sources(cudaStream_t stream, BatchArgs const& b, int k);
+cudaError_t launch_batch_neurons(cudaStream_t stream, BatchArgs const& b);
+// Sets the delivery kernel's dynamic shared memory limit for b's mode, mapping and tile size.
+cudaError_t configure_batch_deliver(BatchArgs const& b);
+cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k, int threads);
 
 }  // namespace spice_gb300

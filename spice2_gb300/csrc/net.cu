@@ -133,6 +133,15 @@ int harvest(spice_net* n) {
 namespace spice_gb300 {
 // Records the calling thread's last error for spice_last_error() (for other translation units).
 int set_last_error(int code, std::string const& msg) { return fail(code, msg); }
+
+// k_neurons CTA kind of a per-neuron population: 3 for a LIF whose every input group adds to V
+// through a 16-bit counter of word 0 (the fast replay), else 0.
+int neuron_block_kind(PopDev const& P) {
+	bool fast = P.model == LIF && P.W == 1 && P.ngroups <= 2;
+	for (int g = 0; g < P.ngroups && fast; g++)
+		fast = P.group_field[g] == 0 && P.group_bits[g] == 16 && P.group_word[g] == 0 && P.group_shift[g] == 16 * g;
+	return fast ? 3 : 0;
+}
 }  // namespace spice_gb300
 
 // ------------------------------------------------------------------------------------------------
@@ -605,6 +614,7 @@ int prepare(spice_net* n) {
 		d.F        = T.F;
 		d.fslot    = T.field_slot[d.field];
 	}
+	for (auto& p : n->pops) p.d.net = 0;
 	TRY(dalloc(n, &n->d_counts, (size_t)2 * n->K * std::max(np, 1)));
 	TRY(dalloc(n, &n->d_pops, std::max(np, 1), false));
 	TRY(dalloc(n, &n->d_conns, std::max<size_t>(n->conns.size(), 1), false));
@@ -704,12 +714,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					ws.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
 					wa.blk_kind[p] = 2;
 				} else {
-					// LIF with every input group adding to V through a 16-bit counter of word 0
-					bool fast = P.model == LIF && P.W == 1 && P.ngroups <= 2;
-					for (int g = 0; g < P.ngroups && fast; g++)
-						fast = P.group_field[g] == 0 && P.group_bits[g] == 16 && P.group_word[g] == 0 &&
-						       P.group_shift[g] == 16 * g;
-					wa.blk_kind[p] = fast ? 3 : 0;
+					wa.blk_kind[p] = neuron_block_kind(P);
 					ws.blk_kind[p] = wa.blk_kind[p];
 					nb += (int)((P.size + 255) / 256);
 				}
@@ -1108,3 +1113,8 @@ extern "C" int spice_synchronize(spice_net* n) {
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
 	return SPICE_OK;
 }
+
+namespace spice_gb300 {
+// Generates pending adjacency and allocates the device state (batch.cu prepares its members).
+int net_prepare(spice_net* n) { return prepare(n); }
+}  // namespace spice_gb300

@@ -42,11 +42,45 @@ SPICE_HD double canonical_f64_leftopen(uint64_t u) {
 	return (double)((u >> 11) + 1) * (1.0 / 9007199254740992.0);
 }
 
+// ---- MurmurHash3-x64-128 with the reference's fixed seed (random.h:19-139) ----
+namespace mm3 {
+constexpr uint64_t C1 = 0x87c37b91114253d5ULL;
+constexpr uint64_t C2 = 0x4cf5ad432745937fULL;
+constexpr uint64_t H0_LO = 0x2E4016967F18E81ULL, H0_HI = 0x447567949F9AA86ULL;
+
+SPICE_HD uint64_t fmix64(uint64_t k) {  // random.h:19-26
+	k ^= k >> 33;
+	k *= 0xff51afd7ed558ccdULL;
+	k ^= k >> 33;
+	k *= 0xc4ceb9fe1a85ec53ULL;
+	k ^= k >> 33;
+	return k;
+}
+SPICE_HD void mix_block(u128& h, uint64_t k1, uint64_t k2) {
+	k1 *= C1; k1 = rotl64(k1, 31); k1 *= C2; h.lo ^= k1;
+	h.lo = rotl64(h.lo, 27); h.lo += h.hi; h.lo = h.lo * 5 + 0x52dce729;
+	k2 *= C2; k2 = rotl64(k2, 33); k2 *= C1; h.hi ^= k2;
+	h.hi = rotl64(h.hi, 31); h.hi += h.lo; h.hi = h.hi * 5 + 0x38495ab5;
+}
+SPICE_HD void finish(u128& h, uint64_t len) {
+	h.lo ^= len; h.hi ^= len;
+	h.lo += h.hi; h.hi += h.lo;
+	h.lo = fmix64(h.lo); h.hi = fmix64(h.hi);
+	h.lo += h.hi; h.hi += h.lo;
+}
+}  // namespace mm3
+
+// The one-block hash that advances a seed_seq (random.h:108-139); host and device.
+SPICE_HD u128 murmur3_u128(u128 k) {
+	u128 h = {mm3::H0_LO, mm3::H0_HI};
+	mm3::mix_block(h, k.lo, k.hi);
+	mm3::finish(h, 16);
+	return h;
+}
+
 // ---- host-side helpers (rng_host.cpp) ----
 // MurmurHash3-x64-128 of bytes with the reference's fixed seed (random.h:32-107).
 u128 murmur3_bytes(const void* data, uint64_t len);
-// The one-block hash that advances a seed_seq (random.h:108-139).
-u128 murmur3_u128(u128 k);
 // Characteristic polynomial of the xoroshiro128+ transition: x^128 + (hi:lo).
 u128 xoro_charpoly();
 // (a * b) mod P over GF(2); a, b of degree < 128.

@@ -7,37 +7,14 @@
 
 namespace spice_gb300 {
 
-namespace {
-uint64_t fmix64(uint64_t k) {  // random.h:19-26
-	k ^= k >> 33;
-	k *= 0xff51afd7ed558ccdULL;
-	k ^= k >> 33;
-	k *= 0xc4ceb9fe1a85ec53ULL;
-	k ^= k >> 33;
-	return k;
-}
-constexpr uint64_t C1 = 0x87c37b91114253d5ULL;
-constexpr uint64_t C2 = 0x4cf5ad432745937fULL;
-constexpr u128 H0     = {0x2E4016967F18E81ULL, 0x447567949F9AA86ULL};
-
-void mix_block(u128& h, uint64_t k1, uint64_t k2) {
-	k1 *= C1; k1 = rotl64(k1, 31); k1 *= C2; h.lo ^= k1;
-	h.lo = rotl64(h.lo, 27); h.lo += h.hi; h.lo = h.lo * 5 + 0x52dce729;
-	k2 *= C2; k2 = rotl64(k2, 33); k2 *= C1; h.hi ^= k2;
-	h.hi = rotl64(h.hi, 31); h.hi += h.lo; h.hi = h.hi * 5 + 0x38495ab5;
-}
-
-void finish(u128& h, uint64_t len) {
-	h.lo ^= len; h.hi ^= len;
-	h.lo += h.hi; h.hi += h.lo;
-	h.lo = fmix64(h.lo); h.hi = fmix64(h.hi);
-	h.lo += h.hi; h.hi += h.lo;
-}
-}  // namespace
+using mm3::C1;
+using mm3::C2;
+using mm3::finish;
+using mm3::mix_block;
 
 u128 murmur3_bytes(const void* ptr, uint64_t len) {
 	const uint8_t* data = static_cast<const uint8_t*>(ptr);
-	u128 h              = H0;
+	u128 h              = {mm3::H0_LO, mm3::H0_HI};
 	uint64_t const nblocks = len / 16;
 	for (uint64_t i = 0; i < nblocks; i++) {
 		uint64_t k1, k2;
@@ -61,12 +38,6 @@ u128 murmur3_bytes(const void* ptr, uint64_t len) {
 	return h;
 }
 
-u128 murmur3_u128(u128 k) {
-	u128 h = H0;
-	mix_block(h, k.lo, k.hi);
-	finish(h, 16);
-	return h;
-}
 
 namespace {
 // Berlekamp-Massey over GF(2): the shortest LFSR c_1..c_L with b[n] = sum c_i b[n-i].

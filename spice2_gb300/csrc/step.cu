@@ -122,6 +122,29 @@ __device__ __forceinline__ void red_add_f32(float* p, float v) {
 	asm volatile("red.relaxed.gpu.global.add.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
 }
 
+// The per-window values the population bodies read, for a batch (from its device clock).  The
+// bodies are templates over the argument type: plain nets pass their WindowArgs / DeliverArgs
+// (kernel parameters, read from the constant bank), batches these register structs.  tables: the
+// jump tables of step k of net j are tables + (j * tab_net_stride + k).
+struct WinCtx {
+	int K, slot0, hslot0, Hb, npop, list_k0;
+	int64_t D;
+	const float* dts;
+	const u128* tables;
+	int64_t tab_net_stride;
+	int32_t* counts;
+};
+
+
+struct DelCtx {
+	int64_t t0, D, slot_lo;
+	int K, npop, list_k0, parts;
+	const ConnDev* conns;
+	const int32_t* counts;
+	unsigned long long* events;  // the target population's net's event counter
+};
+
+
 // v += w, n times, one IEEE add at a time (the reference's n sequential deliver() calls), with the
 // loop overhead paid once per four adds.
 __device__ __forceinline__ float add_n(float v, float w, uint32_t n) {
@@ -162,8 +185,8 @@ __device__ __forceinline__ void replay_words(PopDev const& P, const uint32_t (&x
 // already, so the input words of up to 16 consecutive slots are loaded together first; the step
 // loop itself is kept rolled and small (instruction-cache friendly).  FAST: every input group adds to
 // V through a 16-bit counter of word 0 (Brunel).
-template <int MODE, bool FAST>
-__device__ void window_neurons(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int b) {
+template <int MODE, bool FAST, class A>
+__device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p, int b) {
 	int const N       = (int)Pg->size;
 	int const i       = b * kThreads + threadIdx.x;
 	bool const valid  = i < N;
@@ -294,12 +317,13 @@ __device__ void window_neurons(WindowArgs const& a, const PopDev* __restrict__ P
 // jump is 16 independent table loads.
 // canonical<float>(u) < thr with canonical = (u >> 40) * 2^-24 is evaluated exactly in integers:
 // for an integer m < 2^24, m < thr * 2^24  <=>  m < ceil(thr * 2^24), and m < c <=> hi32(u) < 256 c.
-__device__ void window_poisson(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int b, int* red) {
+template <class A>
+__device__ void window_poisson(A const& a, const PopDev* __restrict__ Pg, int p, int b, int bps, int* red) {
 	PopDev const P  = *Pg;
-	int const k     = b / a.blk_per_step[p];
-	int const cb    = b % a.blk_per_step[p];
+	int const k     = b / bps;
+	int const cb    = b % bps;
 	int const hslot = (a.hslot0 + k) % a.Hb;
-	const u128* tab = a.tables + (int64_t)k * kJumpTable;
+	const u128* tab = a.tables + ((int64_t)P.net * a.tab_net_stride + k) * kJumpTable;
 	int64_t const c  = (int64_t)cb * kThreads + threadIdx.x;
 	float const thr  = __fmul_rn(P.p0, a.dts[k]);
 	float const cthr = ceilf(thr * 16777216.0f);  // exact: scaling by 2^24
@@ -367,13 +391,14 @@ __device__ void window_poisson(WindowArgs const& a, const PopDev* __restrict__ P
 }
 
 // One step of an external population (samples/external_input.cpp:17-30).
-__device__ void window_external(WindowArgs const& a, const PopDev* __restrict__ Pg, int p, int k) {
+template <class A>
+__device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p, int k, int64_t ext_pos) {
 	PopDev const P  = *Pg;
 	uint32_t* bits  = P.bits + (int64_t)((a.hslot0 + k) % a.Hb) * P.nwords;
 	for (int j = threadIdx.x; j < P.nwords; j += blockDim.x) bits[j] = 0;
 	__syncthreads();
 	if (P.ext_steps <= 0) return;
-	int64_t const pos = (a.ext_pos[p] + k) % P.ext_steps;
+	int64_t const pos = (ext_pos + k) % P.ext_steps;
 	int32_t const n   = P.ext_counts[pos];
 	const int32_t* src = P.ext_idx + P.ext_off[pos];
 	for (int j = threadIdx.x; j < n; j += blockDim.x) {
@@ -406,22 +431,68 @@ __global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ Wi
 	int p       = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb = b - a.blk_begin[p];
-	if (a.blk_kind[p] == 1) window_poisson(a, a.pops + p, p, lb, red);
-	else if (a.blk_kind[p] == 2) window_external(a, a.pops + p, p, lb);
+	if (a.blk_kind[p] == 1) window_poisson(a, a.pops + p, p, lb, a.blk_per_step[p], red);
+	else if (a.blk_kind[p] == 2) window_external(a, a.pops + p, p, lb, a.ext_pos[p]);
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(1024) k_deliver(const __grid_constant__ DeliverArgs a) {
+// Writes a finished shared-memory tile into ring slot sigma mod D: a plain store when this CTA is
+// the slot's only writer, an add when the ring accumulates (mixed delays), reductions when several
+// CTAs share the tile.
+template <int MODE, class A>
+__device__ __forceinline__ void flush_tile(A const& a, PopDev const& P, int tbase, int words, int64_t sigma,
+                                           const uint32_t* tile_sm) {
+	int64_t const slot = sigma % a.D;
+	if (MODE == 0) {
+		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) red_add_u32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				uint32_t const v = tile_sm[i];
+				if (v) dst[i] += v;
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
+		}
+	} else {
+		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
+		const float* sm = reinterpret_cast<const float*>(tile_sm);
+		if (a.parts > 1) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) red_add_f32(dst + i, v);
+			}
+		} else if (P.zero_inputs) {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) {
+				float const v = sm[i];
+				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
+			}
+		} else {
+			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
+		}
+	}
+}
+
+// Block-wide event count of a delivery CTA into the net's counter.
+__device__ __forceinline__ void add_events(unsigned long long* dst, unsigned long long mine, unsigned long long* ev_block) {
+	for (int d = 16; d; d >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, d);
+	if ((threadIdx.x & 31) == 0 && mine) atomicAdd(ev_block, mine);
+	__syncthreads();
+	if (threadIdx.x == 0 && *ev_block) atomicAdd(dst, *ev_block);
+}
+
+// Delivery of one (input slot sigma = slot_lo + si, target tile t of population P) work item:
+// every connection into P whose spikes of the window reach slot sigma adds its events to the
+// shared-memory tile, which is then flushed.  part: this CTA's share when `parts` CTAs split it.
+// Warp-flattened mapping: a warp takes 32 spikes, prefix-sums their sub-row lengths and lanes walk
+// the concatenated sub-rows (8 loads in flight per lane).
+template <int MODE, class A>
+__device__ __forceinline__ void deliver_flat(A const& a, PopDev const& P, int t, int si, int part) {
 	extern __shared__ uint32_t tile_sm[];
 	__shared__ unsigned long long ev_block;
-	int const part = blockIdx.x % a.parts;
-	int const b    = blockIdx.x / a.parts;
-	int const si   = b / a.ntiles_total;
-	int const g    = b - si * a.ntiles_total;
-	int Q        = 0;
-	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
-	PopDev const& P = a.pops[Q];
-	int const t     = g - a.tile_begin[Q];
 	int const T     = P.tile;
 	int const tbase = t * T;
 	int const tn    = (int)min((int64_t)T, P.size - tbase);
@@ -429,8 +500,6 @@ __global__ void __launch_bounds__(1024) k_deliver(const __grid_constant__ Delive
 	int const words = tn * width;
 	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
 	if (threadIdx.x == 0) ev_block = 0;
-	if (blockIdx.x == 0)
-		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
 	__syncthreads();
 	int64_t const sigma = a.slot_lo + si;
 	int const lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
@@ -503,68 +572,23 @@ __global__ void __launch_bounds__(1024) k_deliver(const __grid_constant__ Delive
 			j0 = jn;
 		}
 	}
-	if (lane == 0 && my_events) atomicAdd(&ev_block, my_events);
-	__syncthreads();
-	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+	add_events(a.events, my_events, &ev_block);
 	if (!touched) return;
-	// flush the tile into ring slot sigma mod D
-	int64_t const slot = sigma % a.D;
-	if (MODE == 0) {
-		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
-		if (a.parts > 1) {  // several CTAs share the slot's tile: coalesced reductions
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				uint32_t const v = tile_sm[i];
-				if (v) red_add_u32(dst + i, v);
-			}
-		} else if (P.zero_inputs) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				uint32_t const v = tile_sm[i];
-				if (v) dst[i] += v;
-			}
-		} else {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
-		}
-	} else {
-		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
-		const float* sm = reinterpret_cast<const float*>(tile_sm);
-		if (a.parts > 1) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				float const v = sm[i];
-				if (v != 0.0f) red_add_f32(dst + i, v);
-			}
-		} else if (P.zero_inputs) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				float const v = sm[i];
-				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
-			}
-		} else {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
-		}
-	}
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
-// Thread-per-spike variant of the tiled delivery: each thread walks the sub-row of one spike
-// within the CTA's tile (8 loads in flight), no cross-lane work distribution.
-template <int MODE, bool VEC>
-__global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
+// Thread-per-spike mapping: each thread walks the sub-row of one spike within the CTA's tile
+// (8 loads in flight), no cross-lane work distribution.  VEC: 16-byte loads of the sub-row body.
+template <int MODE, bool VEC, class A>
+__device__ __forceinline__ void deliver_tps(A const& a, PopDev const& P, int t, int si, int part) {
 	extern __shared__ uint32_t tile_sm[];
 	__shared__ unsigned long long ev_block;
-	int const part = blockIdx.x % a.parts;
-	int const b    = blockIdx.x / a.parts;
-	int const si   = b / a.ntiles_total;
-	int const g    = b - si * a.ntiles_total;
-	int Q          = 0;
-	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
-	PopDev const& P = a.pops[Q];
-	int const t     = g - a.tile_begin[Q];
 	int const tbase = t * P.tile;
 	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
 	int const width = MODE == 0 ? P.W : P.F;
 	int const words = tn * width;
 	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
 	if (threadIdx.x == 0) ev_block = 0;
-	if (blockIdx.x == 0)
-		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
 	__syncthreads();
 	int64_t const sigma = a.slot_lo + si;
 	unsigned long long my_events = 0;
@@ -624,61 +648,18 @@ __global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
 			for (int64_t e = body_end; e < e1; e++) add(__ldg(nb + e));
 		}
 	}
-	for (int d = 16; d; d >>= 1) my_events += __shfl_xor_sync(0xffffffffu, my_events, d);
-	if ((threadIdx.x & 31) == 0 && my_events) atomicAdd(&ev_block, my_events);
-	__syncthreads();
-	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+	add_events(a.events, my_events, &ev_block);
 	if (!touched) return;
-	int64_t const slot = sigma % a.D;
-	if (MODE == 0) {
-		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
-		if (a.parts > 1) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				uint32_t const v = tile_sm[i];
-				if (v) red_add_u32(dst + i, v);
-			}
-		} else if (P.zero_inputs) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				uint32_t const v = tile_sm[i];
-				if (v) dst[i] += v;
-			}
-		} else {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
-		}
-	} else {
-		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
-		const float* sm = reinterpret_cast<const float*>(tile_sm);
-		if (a.parts > 1) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				float const v = sm[i];
-				if (v != 0.0f) red_add_f32(dst + i, v);
-			}
-		} else if (P.zero_inputs) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				float const v = sm[i];
-				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
-			}
-		} else {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
-		}
-	}
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
-// Warp-per-spike variant of the tiled delivery: a warp takes 32 spikes, loads their sub-row bounds
-// lane-parallel, then streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced
-// loads, 8 in flight per lane, no cross-lane search).
-template <int MODE>
-__global__ void __launch_bounds__(1024) k_deliver_wps(const __grid_constant__ DeliverArgs a) {
+// Warp-per-spike mapping: a warp takes 32 spikes, loads their sub-row bounds lane-parallel, then
+// streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced loads, 8 in flight per
+// lane, no cross-lane search).
+template <int MODE, class A>
+__device__ __forceinline__ void deliver_wps(A const& a, PopDev const& P, int t, int si, int part) {
 	extern __shared__ uint32_t tile_sm[];
 	__shared__ unsigned long long ev_block;
-	int const part = blockIdx.x % a.parts;
-	int const b    = blockIdx.x / a.parts;
-	int const si   = b / a.ntiles_total;
-	int const g    = b - si * a.ntiles_total;
-	int Q          = 0;
-	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
-	PopDev const& P = a.pops[Q];
-	int const t     = g - a.tile_begin[Q];
 	int const tbase = t * P.tile;
 	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
 	int const width = MODE == 0 ? P.W : P.F;
@@ -744,44 +725,46 @@ __global__ void __launch_bounds__(1024) k_deliver_wps(const __grid_constant__ De
 			}
 		}
 	}
-	for (int d = 16; d; d >>= 1) my_events += __shfl_xor_sync(0xffffffffu, my_events, d);
-	if (lane == 0 && my_events) atomicAdd(&ev_block, my_events);
-	__syncthreads();
-	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+	add_events(a.events, my_events, &ev_block);
 	if (!touched) return;
-	int64_t const slot = sigma % a.D;
-	if (MODE == 0) {
-		uint32_t* dst = P.cnt + (slot * P.size + tbase) * P.W;
-		if (a.parts > 1) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				uint32_t const v = tile_sm[i];
-				if (v) red_add_u32(dst + i, v);
-			}
-		} else if (P.zero_inputs) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				uint32_t const v = tile_sm[i];
-				if (v) dst[i] += v;
-			}
-		} else {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = tile_sm[i];
-		}
-	} else {
-		float* dst      = P.acc + (slot * P.size + tbase) * P.F;
-		const float* sm = reinterpret_cast<const float*>(tile_sm);
-		if (a.parts > 1) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				float const v = sm[i];
-				if (v != 0.0f) red_add_f32(dst + i, v);
-			}
-		} else if (P.zero_inputs) {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) {
-				float const v = sm[i];
-				if (v != 0.0f) dst[i] = __fadd_rn(dst[i], v);
-			}
-		} else {
-			for (int i = threadIdx.x; i < words; i += blockDim.x) dst[i] = sm[i];
-		}
-	}
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
+// Plain-net delivery kernels: block -> (part, slot si, tile g over all target populations).
+struct DeliverItem {
+	int part, si, Q, t;
+};
+__device__ __forceinline__ DeliverItem deliver_item(DeliverArgs const& a) {
+	DeliverItem it;
+	it.part    = blockIdx.x % a.parts;
+	int const b = blockIdx.x / a.parts;
+	it.si      = b / a.ntiles_total;
+	int const g = b - it.si * a.ntiles_total;
+	int Q       = 0;
+	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
+	it.Q = Q;
+	it.t = g - a.tile_begin[Q];
+	if (blockIdx.x == 0)
+		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
+	return it;
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(1024) k_deliver(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_flat<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+template <int MODE, bool VEC>
+__global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_tps<MODE, VEC>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(1024) k_deliver_wps(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_wps<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
 __global__ void k_tile_bounds(const int64_t* __restrict__ off, const int32_t* __restrict__ nb, int64_t rows, int tile,
@@ -961,6 +944,127 @@ __global__ void k_scan_add(int64_t* out, int64_t n, const int64_t* __restrict__ 
 	if (i < n) out[i + 1] += sums[blockIdx.x];
 }
 
+
+// ---------------------------------------------------------------------------------------------
+// Batched networks: the populations and connections of many independent nets (same dt, delay
+// ring, window and time) are concatenated and one launch per kernel kind steps all of them.  The
+// window's time-dependent values live in a device clock that k_batch_prologue advances, so every
+// launch of a window has fixed arguments and a window (or several) can be replayed as a CUDA graph.
+// ---------------------------------------------------------------------------------------------
+
+// Largest p < n with begin[p] <= x (begin ascending; empty segments are skipped).
+__device__ __forceinline__ int find_segment(const int* __restrict__ begin, int n, int x) {
+	int lo = 0, hi = n - 1;
+	while (lo < hi) {
+		int const mid = (lo + hi + 1) >> 1;
+		if (__ldg(begin + mid) <= x) lo = mid;
+		else hi = mid - 1;
+	}
+	return lo;
+}
+
+__device__ __forceinline__ WinCtx batch_win_ctx(BatchArgs const& b, BatchClock const& c) {
+	WinCtx w;
+	w.K              = c.k;
+	w.slot0          = (int)((c.t0 - 1 + b.D) % b.D);
+	w.hslot0         = (int)(c.t0 % b.Hb);
+	w.Hb             = b.Hb;
+	w.npop           = b.npop;
+	w.list_k0        = c.parity * b.K;
+	w.D              = b.D;
+	w.dts            = b.dts;
+	w.tables         = b.tables;
+	w.tab_net_stride = b.K;
+	w.counts         = b.counts + (int64_t)c.parity * b.K * b.npop;
+	return w;
+}
+
+// One CTA: advances the clock to the next window of k steps, computes the window's dt (Kahan, as
+// kahan_next on the host: kahan_sum<float> then the reset at >= 1 s) and every net's step seeds
+// (seed_seq post-increment, one per step), and clears this window's spike counters.
+__global__ void k_batch_prologue(const __grid_constant__ BatchArgs b, int k) {
+	BatchClock* clk    = b.clock;
+	int64_t const t0   = clk->next_t0;
+	int const parity   = clk->next_parity;
+	__syncthreads();
+	if (threadIdx.x == 0) {
+		clk->t0          = t0;
+		clk->parity      = parity;
+		clk->k           = k;
+		clk->next_t0     = t0 + k;
+		clk->next_parity = parity ^ 1;
+		float c = clk->kahan_c, sum = clk->kahan_sum;
+		for (int j = 0; j < k; j++) {
+			float const y = __fsub_rn(b.dt, c);
+			float const t = __fadd_rn(sum, y);
+			c             = __fsub_rn(__fsub_rn(t, sum), y);
+			sum           = t >= 1.0f ? 0.0f : t;
+			b.dts[j]      = y;
+		}
+		clk->kahan_c   = c;
+		clk->kahan_sum = sum;
+	}
+	int32_t* counts = b.counts + (int64_t)parity * b.K * b.npop;
+	for (int i = threadIdx.x; i < b.K * b.npop; i += blockDim.x) counts[i] = 0;
+	for (int n = threadIdx.x; n < b.nnets; n += blockDim.x) {
+		u128 s = b.seed_state[n];
+		for (int j = 0; j < k; j++) {
+			b.step_seeds[(int64_t)n * b.K + j] = s;
+			s = murmur3_u128(s);
+		}
+		b.seed_state[n] = s;
+	}
+}
+
+// Source populations of all nets: grid (Poisson chunk CTAs of one step, steps of the window).
+__global__ void __launch_bounds__(kThreads) k_batch_sources(const __grid_constant__ BatchArgs b) {
+	__shared__ int red[kThreads / 32 + 1];
+	BatchClock const c = *b.clock;
+	int const x   = blockIdx.x;
+	int const p   = find_segment(b.sblk_begin, b.npop, x);
+	int const bps = __ldg(b.sblk_begin + p + 1) - __ldg(b.sblk_begin + p);
+	WinCtx const w = batch_win_ctx(b, c);
+	window_poisson(w, b.pops + p, p, (int)blockIdx.y * bps + (x - __ldg(b.sblk_begin + p)), bps, red);
+}
+
+// Per-neuron populations of all nets, K steps each with the state in registers.
+template <int MODE, bool ONLY_FAST>
+__global__ void __launch_bounds__(kThreads) k_batch_neurons(const __grid_constant__ BatchArgs b) {
+	BatchClock const c = *b.clock;
+	int const x        = blockIdx.x;
+	int const p        = find_segment(b.nblk_begin, b.npop, x);
+	int const lb       = x - __ldg(b.nblk_begin + p);
+	WinCtx const w     = batch_win_ctx(b, c);
+	if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true>(w, b.pops + p, p, lb);
+	else if (!ONLY_FAST) window_neurons<MODE, false>(w, b.pops + p, p, lb);
+}
+
+// Delivery of all nets: grid (target tiles x parts, input slots of the window).
+template <int MODE, int ALGO>
+__global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
+	BatchClock const c = *b.clock;
+	int const part     = blockIdx.x % b.parts;
+	int const g        = blockIdx.x / b.parts;
+	int const Q        = find_segment(b.tile_begin, b.npop, g);
+	PopDev const& P    = b.pops[Q];
+	DelCtx a;
+	a.t0      = c.t0;
+	a.D       = b.D;
+	a.slot_lo = c.t0 + b.dmin - 1;
+	a.K       = c.k;
+	a.npop    = b.npop;
+	a.list_k0 = c.parity * b.K;
+	a.parts   = b.parts;
+	a.conns   = b.conns;
+	a.counts  = b.counts + (int64_t)c.parity * b.K * b.npop;
+	a.events  = b.net_events[P.net];
+	int const t = g - __ldg(b.tile_begin + Q);
+	if (ALGO == 0) deliver_flat<MODE>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 1) deliver_tps<MODE, false>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 2) deliver_wps<MODE>(a, P, t, (int)blockIdx.y, part);
+	else deliver_tps<MODE, true>(a, P, t, (int)blockIdx.y, part);
+}
+
 }  // namespace
 
 cudaError_t scan_row_lengths(cudaStream_t stream, const int32_t* lens, int64_t n, int64_t* offsets) {
@@ -1079,6 +1183,64 @@ cudaError_t launch_apply_pending(cudaStream_t stream, const PopDev*, int, const 
 
 cudaError_t launch_extract(cudaStream_t stream, const uint32_t* bits, int nwords, int32_t* out, int64_t* n_out) {
 	k_extract<<<1, 1024, 0, stream>>>(bits, nwords, out, n_out);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_batch_prologue(cudaStream_t stream, BatchArgs const& b, int k) {
+	k_batch_prologue<<<1, 256, 0, stream>>>(b, k);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_batch_sources(cudaStream_t stream, BatchArgs const& b, int k) {
+	if (b.sblk_total <= 0 || k <= 0) return cudaSuccess;
+	k_batch_sources<<<dim3((unsigned)b.sblk_total, (unsigned)k), kThreads, 0, stream>>>(b);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_batch_neurons(cudaStream_t stream, BatchArgs const& b) {
+	if (b.nblk_total <= 0) return cudaSuccess;
+	if (b.mode == 0) {
+		if (b.only_fast) k_batch_neurons<0, true><<<b.nblk_total, kThreads, 0, stream>>>(b);
+		else k_batch_neurons<0, false><<<b.nblk_total, kThreads, 0, stream>>>(b);
+	} else {
+		if (b.only_fast) k_batch_neurons<1, true><<<b.nblk_total, kThreads, 0, stream>>>(b);
+		else k_batch_neurons<1, false><<<b.nblk_total, kThreads, 0, stream>>>(b);
+	}
+	return cudaGetLastError();
+}
+
+namespace {
+void const* batch_deliver_fn(BatchArgs const& b) {
+	int const m = (b.mode == 0 ? 0 : 1) + 2 * b.algo;
+	void const* fns[8] = {(void const*)k_batch_deliver<0, 0>, (void const*)k_batch_deliver<1, 0>,
+	                      (void const*)k_batch_deliver<0, 1>, (void const*)k_batch_deliver<1, 1>,
+	                      (void const*)k_batch_deliver<0, 2>, (void const*)k_batch_deliver<1, 2>,
+	                      (void const*)k_batch_deliver<0, 3>, (void const*)k_batch_deliver<1, 3>};
+	return fns[m & 7];
+}
+}  // namespace
+
+cudaError_t configure_batch_deliver(BatchArgs const& b) {
+	return cudaFuncSetAttribute(batch_deliver_fn(b), cudaFuncAttributeMaxDynamicSharedMemorySize, b.smem_bytes);
+}
+
+cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k, int threads) {
+	int const nslots = k + b.dmax - b.dmin;
+	if (b.ntiles_total <= 0 || nslots <= 0) return cudaSuccess;
+	cudaFuncAttributes fa;
+	if (cudaFuncGetAttributes(&fa, batch_deliver_fn(b)) == cudaSuccess && threads > fa.maxThreadsPerBlock)
+		threads = fa.maxThreadsPerBlock / 32 * 32;  // the launch shape never changes results
+	dim3 const grid((unsigned)(b.ntiles_total * b.parts), (unsigned)nslots);
+	switch ((b.mode == 0 ? 0 : 1) + 2 * b.algo) {
+		case 0: k_batch_deliver<0, 0><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 1: k_batch_deliver<1, 0><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 2: k_batch_deliver<0, 1><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 3: k_batch_deliver<1, 1><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 4: k_batch_deliver<0, 2><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 5: k_batch_deliver<1, 2><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 6: k_batch_deliver<0, 3><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 7: k_batch_deliver<1, 3><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+	}
 	return cudaGetLastError();
 }
 
