@@ -18,6 +18,9 @@ Printed JSON (one line, rank 0):
   cpu_baseline the CPU restatement of the reference step loop (oracle/oracle_bench, the same
                algorithm as the reference's single-core path) timed on this host's cores
   atomic_mode  value with the fast atomic delivery mode (order-dependent float rounding)
+  batched      the batched sweep (256 Brunel networks, N log-uniform in [5e3, 8e4], 1000 steps):
+               events/s as one batch and as the plain path network after network, their ratio,
+               and whether both gave bit-identical final states
 
 --impl reference runs the reference's CPU implementation of the path on the host cores (the
 reference binary when it was built on this host, else its CPU restatement) and prints the same
@@ -83,9 +86,12 @@ def _sum_over_ranks(x: float, ws: int) -> float:
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+    """nvidia-smi sampling (every 20 ms) of SM clocks and throttle reasons.  The sampler is started
+    during the warm-up (nvidia-smi needs a moment to start); mark() brackets the timed region and
+    summary() keeps the samples taken inside it (or, for a region shorter than the sampling period,
+    the sample right after its start)."""
 
-    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+    Q = ("timestamp,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
@@ -93,18 +99,30 @@ class ClockSampler:
         self.gpu = gpu_index
         self.proc = None
         self.out = os.path.join("/tmp", f"spice_clocks_{os.getpid()}.csv")
+        self.t0 = self.t1 = None
 
     def __enter__(self):
+        if self.proc is not None:
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                          "--format=csv,noheader,nounits", "-lms", "20"],
                                          stdout=open(self.out, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
         return self
 
+    def mark(self, which: str):
+        import datetime
+        now = datetime.datetime.now()
+        if which == "start":
+            self.t0 = now
+        else:
+            self.t1 = now
+
     def __exit__(self, *a):
         if self.proc:
+            time.sleep(0.05)
             self.proc.terminate()
             try:
                 self.proc.wait(timeout=5)
@@ -112,19 +130,31 @@ class ClockSampler:
                 self.proc.kill()
 
     def summary(self):
+        import datetime
         try:
-            rows = [r.split(",") for r in open(self.out).read().strip().splitlines() if r.strip()]
+            rows = [[c.strip() for c in r.split(",")] for r in open(self.out).read().strip().splitlines() if r.strip()]
         except Exception:
             rows = []
+        stamped = []
+        for r in rows:
+            try:
+                stamped.append((datetime.datetime.strptime(r[0], "%Y/%m/%d %H:%M:%S.%f"), r))
+            except Exception:
+                continue
+        inside = [r for t, r in stamped if self.t0 and self.t1 and self.t0 <= t <= self.t1]
+        if not inside and self.t0:
+            after = [r for t, r in stamped if t >= self.t0]
+            inside = after[:1]
+        rows = inside
         if not rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
-        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in rows if r[2].strip().replace(".", "").isdigit()]
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         reasons = set()
         for r in rows:
-            for j, n in enumerate(names):
-                if len(r) > 5 + j and r[5 + j].strip() == "Active":
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() in ("active", "1"):
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": sorted(reasons), "samples": len(rows)}
@@ -150,6 +180,72 @@ def cpu_baseline(threads: int | None = None, steps: int = 200, warmup: int = 50,
     d = json.loads(out.strip().splitlines()[-1])
     d["kind"] = "port"
     return d
+
+
+def batched_sweep(n_nets: int, steps: int, warm: int = 60):
+    """The batched Brunel sweep: n_nets networks with N log-uniform in [5e3, 8e4] (seeded), p = 0.1 *
+    min(1, 2e4/N), seeds 1000 + i, delay 15 steps, deterministic mode.  Two identical sets are built:
+    one steps every network on its own, one after the other (the plain path), the other as one batch
+    (shared launches per window, CUDA graph replay, launch shape from the autotuner).  Both run the
+    same simulated steps; the timed stretch is `steps` steps after warm-up and tuning, and the final
+    states of both sets must be bit-identical."""
+    import gc
+    import numpy as np
+    import torch
+    import spice2_gb300 as sp
+    from spice2_gb300.autotune import autotune
+    sizes = sp.brunel_sweep_sizes(n_nets)
+    t0 = time.perf_counter()
+    A = sp.brunel_sweep(sizes, seed0=1000)
+    B = sp.brunel_sweep(sizes, seed0=1000)
+    for n, _ in A + B:
+        n.csr(0)  # generate the adjacency (construction, not timed)
+    syn = sum(n.synapses(c) for n, _ in A for c in range(6))
+    batch = sp.batch([n for n, _ in B])
+    build_s = time.perf_counter() - t0
+    batch.run(warm)
+    tuned = autotune(batch, steps=150, warm=15)["best"]
+    advanced = batch.nets[0].time
+    for n, _ in A:  # bring the plain set to the same step (untimed)
+        n.run(advanced)
+        n.synchronize()
+    # plain path, network after network
+    e0 = sum(n.events for n, _ in A)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for n, _ in A:
+        n.run(steps)
+        n.synchronize()
+    plain_s = time.perf_counter() - t
+    plain_events = sum(n.events for n, _ in A) - e0
+    # batched
+    e0 = batch.events
+    l0 = batch.launch_count()
+    stream = torch.cuda.ExternalStream(batch.stream_handle())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    a.record(stream)
+    batch.run(steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    batch_s = time.perf_counter() - t
+    batch_dev_ms = a.elapsed_time(b)
+    batch_events = batch.events - e0
+    launches = batch.launch_count() - l0
+    same = all(np.array_equal(na.get_state(pa[k], sp.FIELD_V).view(np.uint32), nb.get_state(pb[k], sp.FIELD_V).view(np.uint32))
+               for (na, pa), (nb, pb) in zip(A, B) for k in (1, 2))
+    same = same and plain_events == batch_events
+    out = {"metric": "synaptic_events_per_s", "unit": "events/s", "nets": n_nets, "N_min": min(sizes),
+           "N_max": max(sizes), "synapses": syn, "sim_steps": steps,
+           "value": batch_events / batch_s, "device_value": batch_events / (batch_dev_ms / 1e3),
+           "plain_sequential_value": plain_events / plain_s, "speedup_vs_plain": (batch_events / batch_s) / (plain_events / plain_s),
+           "batch_ms": batch_s * 1e3, "plain_ms": plain_s * 1e3, "events": batch_events, "gpu_launches": launches,
+           "graph_windows": 8, "delivery_shape": tuned, "bit_identical_to_plain": bool(same),
+           "build_seconds": build_s, "timing": "host wall clock around run() with the device synchronised on both sides"}
+    del A, B, batch
+    gc.collect()
+    return out
 
 
 def reference_arm(args):
@@ -189,6 +285,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-nets", type=int, default=256,
+                    help="networks of the batched Brunel sweep (0 skips it)")
+    ap.add_argument("--batched-steps", type=int, default=1000)
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -214,6 +313,7 @@ def main():
     from spice2_gb300.autotune import autotune
     tuned = autotune(net, steps=300, warm=30)["best"]
 
+    clk = ClockSampler(lrank).__enter__()  # sampling starts during the warm-up (nvidia-smi start-up)
     for _ in range(args.warmup):
         net.run(STEPS_PER_RUN)
     net.synchronize()
@@ -224,12 +324,14 @@ def main():
     _barrier(ws)
     torch.cuda.synchronize()
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(lrank) as clk:
+    with clk:
+        clk.mark("start")
         start.record(stream)
         for _ in range(args.steps):
             net.run(STEPS_PER_RUN)
         end.record(stream)
         torch.cuda.synchronize()
+        clk.mark("end")
     _barrier(ws)
     ms = start.elapsed_time(end)
     events = net.events - ev0
@@ -303,6 +405,15 @@ def main():
     if DELIVER_DRAM_BYTES_PER_EVENT is not None:
         traffic = DELIVER_DRAM_BYTES_PER_EVENT * ev_per_launch
 
+    batched = None
+    import gc
+    gc.collect()  # the N=5e5 nets (populations and nets reference each other)
+    if args.batched_nets > 0:
+        try:
+            batched = batched_sweep(args.batched_nets, args.batched_steps)
+        except Exception as e:  # reported, never a reason to lose the headline line
+            batched = {"error": str(e)}
+
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         try:
@@ -336,6 +447,7 @@ def main():
                      "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3},
         "cpu_baseline": cpu,
         "atomic_mode": atomic,
+        "batched": batched,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

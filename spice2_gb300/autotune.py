@@ -18,10 +18,11 @@ import json
 import sys
 
 DEFAULT_CANDIDATES = [
-    # (tile bytes, threads per CTA, parts per (slot, tile), work mapping)
-    (12 * 1024, 256, 1, 1), (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1),
-    (48 * 1024, 1024, 1, 1), (96 * 1024, 1024, 1, 1), (24 * 1024, 256, 2, 1), (24 * 1024, 256, 1, 0),
-    (48 * 1024, 512, 1, 3),
+    # (tile bytes, threads per CTA, parts per (slot, tile), work mapping: 0 warp-flattened,
+    #  1 thread per spike, 2 warp per spike, 3 thread per spike with 16-byte loads)
+    (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
+    (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
+    (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
 ]
 
 
