@@ -21,6 +21,8 @@ Printed JSON (one line, rank 0):
   batched      the batched sweep (256 Brunel networks, N log-uniform in [5e3, 8e4], 1000 steps):
                events/s as one batch and as the plain path network after network, their ratio,
                and whether both gave bit-identical final states
+  adjoint      the differentiable recurrent LIF layer (batch 64, 700 -> 1024, 200 steps): forward and
+               adjoint-backward times, their ratio, and plain PyTorch autograd on dense weights
 
 --impl reference runs the reference's CPU implementation of the path on the host cores (the
 reference binary when it was built on this host, else its CPU restatement) and prints the same
@@ -248,6 +250,75 @@ def batched_sweep(n_nets: int, steps: int, warm: int = 60):
     return out
 
 
+def adjoint_bench(reps: int = 10):
+    """The differentiable recurrent LIF layer (batch 64, 700 Poisson inputs -> 1024 LIF, p = 0.2 / 0.1,
+    dt = 1e-3, 200 steps, surrogate slope 25, checkpoint every 20, MSE on the first 128 counts):
+    CUDA-event times of the forward kernel and of the adjoint backward (which recomputes every
+    20-step segment from its checkpoint), and the same loss and gradients through plain PyTorch
+    autograd on dense masked float32 matrices (the surrogate spike as a custom function) for
+    comparison."""
+    import torch
+    from spice2_gb300.lif import RecurrentLIF, count_loss, count_targets, poisson_input, time_step
+    torch.backends.cuda.matmul.allow_tf32 = False
+    out = time_step(64, 200, reps=reps)
+    layer = RecurrentLIF()
+    _, x = poisson_input(64, 200, 700, seed=2, return_dense=True)
+    target = count_targets(64)
+    dev = "cuda"
+
+    def dense(csr, w, ns, nd):
+        off, nb = (torch.as_tensor(a, device=dev) for a in csr)
+        rows = torch.repeat_interleave(torch.arange(ns, device=dev), off[1:] - off[:-1])
+        W = torch.zeros(ns, nd, device=dev)
+        W[rows, nb.long()] = w.detach()
+        return W.requires_grad_(True)
+
+    class Spike(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, xm):
+            ctx.save_for_backward(xm)
+            return (xm > 0).float()
+
+        @staticmethod
+        def backward(ctx, g):
+            (xm,) = ctx.saved_tensors
+            return g / (1.0 + 25.0 * xm.abs()) ** 2
+
+    xf = x.float()
+
+    def plain():
+        Win, Wrec = dense(layer.in_csr, layer.w_in, 700, 1024), dense(layer.rec_csr, layer.w_rec, 1024, 1024)
+        th = layer.theta.detach().clone().requires_grad_(True)
+        be = layer.beta.detach().clone().requires_grad_(True)
+        v = torch.zeros(64, 1024, device=dev)
+        s = torch.zeros(64, 1024, device=dev)
+        c = torch.zeros(64, 1024, device=dev)
+        for t in range(200):
+            u = be * v + xf[:, t] @ Win + s @ Wrec
+            s = Spike.apply(u - th)
+            v = u - th * s
+            c = c + s
+        count_loss(c, target).backward()
+
+    for _ in range(3):
+        plain()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    ts = []
+    for _ in range(5):
+        torch.cuda.synchronize()
+        ev[0].record()
+        plain()
+        ev[1].record()
+        torch.cuda.synchronize()
+        ts.append(ev[0].elapsed_time(ev[1]))
+    ts.sort()
+    out["plain_pytorch_fwd_bwd_ms"] = ts[len(ts) // 2]
+    out["speedup_vs_plain"] = out["plain_pytorch_fwd_bwd_ms"] / (out["forward_ms"] + out["backward_ms"])
+    out["config"] = "batch 64, 700 -> 1024 LIF, p 0.2 / 0.1, 200 steps, checkpoint every 20, slope 25"
+    out["plain"] = "PyTorch autograd, dense masked float32 weights (TF32 off), surrogate spike function"
+    return out
+
+
 def reference_arm(args):
     ws, rank, _ = _dist()
     if rank != 0:
@@ -414,6 +485,12 @@ def main():
         except Exception as e:  # reported, never a reason to lose the headline line
             batched = {"error": str(e)}
 
+    adjoint = None
+    try:
+        adjoint = adjoint_bench()
+    except Exception as e:
+        adjoint = {"error": str(e)}
+
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         try:
@@ -448,6 +525,7 @@ def main():
         "cpu_baseline": cpu,
         "atomic_mode": atomic,
         "batched": batched,
+        "adjoint": adjoint,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

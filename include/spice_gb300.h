@@ -203,6 +203,36 @@ int spice_batch_kernel_stats(spice_batch* batch, int kind, int64_t* launches_out
 int spice_batch_launch_count(spice_batch* batch, int64_t* launches_out);
 int spice_batch_get_stream(spice_batch* batch, void** stream_out);
 
+/* ---- Differentiable recurrent LIF layer (no counterpart in the reference) ----
+ * n_in inputs x_t in {0,1} and n_rec LIF neurons, delay 1 step, t = 1..T:
+ *   u_t = beta .* v_{t-1} + W_in^T x_{t-1} + W_rec^T s_{t-1},  s_t = H(u_t - theta),
+ *   v_t = u_t - theta .* s_t (reset by subtraction),  counts = sum_t s_t.
+ * Weights are per synapse in the CSR order of the connectivity (by source); theta and beta are per
+ * neuron.  The backward is the adjoint recursion backwards in time with the fast-sigmoid surrogate
+ * 1 / (1 + slope |u - theta|)^2 in place of H'.  relaxed = 1 replaces H by the smooth
+ * g(x) = (1 + slope x / (1 + slope |x|)) / 2 in the forward and uses its exact derivative (for
+ * finite-difference checks).  One CTA per sample keeps the layer in shared memory.
+ * All arrays except the CSR of spice_lif_layer_create are device pointers; stream is a
+ * cudaStream_t (NULL: default stream).  Layouts: x_bits [batch][steps][ceil(n_in/32)] (bit k of word
+ * k/32 = input k), counts and grad_counts [batch][n_rec], spikes [batch][steps][n_rec] (s_t at t-1),
+ * v_ckpt [batch][ceil(steps/checkpoint_every) + 1][n_rec].  The forward stores spikes and v every
+ * checkpoint_every steps; the backward recomputes each segment from its checkpoint.  Gradients are
+ * summed over the batch (a fixed order: bit-reproducible). */
+typedef struct spice_lif_layer spice_lif_layer;
+int spice_lif_layer_create(int n_in, int n_rec, const int64_t* in_off, const int32_t* in_nb,
+                           const int64_t* rec_off, const int32_t* rec_nb, spice_lif_layer** out);
+int spice_lif_layer_destroy(spice_lif_layer* layer);
+int spice_lif_layer_synapses(spice_lif_layer* layer, int64_t* in_syn_out, int64_t* rec_syn_out);
+int spice_lif_forward(spice_lif_layer* layer, int batch, int steps, int checkpoint_every, int relaxed,
+                      float slope, const uint32_t* x_bits, const float* w_in, const float* w_rec,
+                      const float* theta, const float* beta, float* counts, float* spikes, float* v_ckpt,
+                      void* stream);
+int spice_lif_backward(spice_lif_layer* layer, int batch, int steps, int checkpoint_every, int relaxed,
+                       float slope, const uint32_t* x_bits, const float* w_in, const float* w_rec,
+                       const float* theta, const float* beta, const float* spikes, const float* v_ckpt,
+                       const float* grad_counts, float* grad_w_in, float* grad_w_rec, float* grad_theta,
+                       float* grad_beta, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -101,6 +101,11 @@ def _load():
         "spice_batch_kernel_stats": [vp, i32, P(i64), P(f64)],
         "spice_batch_launch_count": [vp, P(i64)],
         "spice_batch_get_stream": [vp, P(vp)],
+        "spice_lif_layer_create": [i32, i32, vp, vp, vp, vp, P(vp)],
+        "spice_lif_layer_destroy": [vp],
+        "spice_lif_layer_synapses": [vp, P(i64), P(i64)],
+        "spice_lif_forward": [vp, i32, i32, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp, vp, vp],
+        "spice_lif_backward": [vp, i32, i32, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
