@@ -258,7 +258,7 @@ def adjoint_bench(reps: int = 10):
     autograd on dense masked float32 matrices (the surrogate spike as a custom function) for
     comparison."""
     import torch
-    from spice2_gb300.lif import RecurrentLIF, count_loss, count_targets, poisson_input, time_step
+    from spice2_gb300.lif_layer import RecurrentLIF, count_loss, count_targets, poisson_input, time_step
     torch.backends.cuda.matmul.allow_tf32 = False
     out = time_step(64, 200, reps=reps)
     layer = RecurrentLIF()
@@ -317,6 +317,55 @@ def adjoint_bench(reps: int = 10):
     out["config"] = "batch 64, 700 -> 1024 LIF, p 0.2 / 0.1, 200 steps, checkpoint every 20, slope 25"
     out["plain"] = "PyTorch autograd, dense masked float32 weights (TF32 off), surrogate spike function"
     return out
+
+
+def plastic_bench(N: int = 100000, steps: int = 5000):
+    """The plastic E/I network: N conductance-LIF neurons (80 % E, 20 % I; tau_E 5 ms, tau_I 10 ms,
+    the neuron of samples/vogels.cpp), fixed_probability(0.02), delay 1 step, E weights 0.03 and
+    I weights 0.3 (0.3 nS and 3 nS over the 10 nS leak), I->E synapses iSTDP (tau 20 ms, rho0 5 Hz,
+    eta 1e-3) with lazy event-driven updates, atomic mode, dt 1e-4, `steps` steps after 200 warm-up
+    steps.  Reported: synaptic events/s and simulated seconds per wall second (CUDA events on the
+    net's stream), firing rates and the I->E weight drift."""
+    import numpy as np
+    import torch
+    import spice2_gb300 as sp
+    t0 = time.perf_counter()
+    net = sp.snn(1e-4, 1e-4, [1])
+    net.set_mode(sp.MODE_ATOMIC)
+    E = net.add_population(sp.lif_cond(), N * 8 // 10)
+    I = net.add_population(sp.lif_cond(), N * 2 // 10)
+    net.connect(E, E, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
+    net.connect(E, I, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
+    c = net.connect(I, E, sp.fixed_probability(0.02), 1e-4, sp.istdp(0.3, eta=1e-3, rho0=5.0, tau=0.02))
+    net.connect(I, I, sp.fixed_probability(0.02), 1e-4, sp.inhibitory(0.3))
+    net.csr(0)
+    syn = sum(net.synapses(k) for k in range(4))
+    build_s = time.perf_counter() - t0
+    net.run(200)
+    net.synchronize()
+    W0 = net.synapse_state(c, 0).astype(np.float64)
+    stream = torch.cuda.ExternalStream(net.stream_handle())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0, l0 = net.events, net.launch_count()
+    torch.cuda.synchronize()
+    a.record(stream)
+    net.run(steps)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    ev = net.events - e0
+    launches = net.launch_count() - l0
+    W = net.synapse_state(c, 0).astype(np.float64)
+    raster = net.run_record(1000)  # rates over the next 0.1 s (not timed)
+    rE = sum(len(r[0]) for r in raster) / (N * 0.8) / 0.1
+    rI = sum(len(r[1]) for r in raster) / (N * 0.2) / 0.1
+    net.close()
+    return {"metric": "synaptic_events_per_s", "unit": "events/s", "value": ev / (ms / 1e3), "N": N,
+            "synapses": syn, "sim_steps": steps, "ms": ms, "sim_seconds_per_wall_second": steps * 1e-4 / (ms / 1e3),
+            "events": ev, "gpu_launches": launches, "rate_E_hz": rE, "rate_I_hz": rI,
+            "istdp_weight_mean_start": float(W0.mean()), "istdp_weight_mean_end": float(W.mean()),
+            "istdp_weight_std_end": float(W.std()), "build_seconds": build_s, "mode": "atomic",
+            "config": "plastic E/I: conductance LIF, p 0.02, delay 1 step, iSTDP on I->E"}
 
 
 def reference_arm(args):
@@ -490,6 +539,11 @@ def main():
         adjoint = adjoint_bench()
     except Exception as e:
         adjoint = {"error": str(e)}
+    plastic = None
+    try:
+        plastic = plastic_bench()
+    except Exception as e:
+        plastic = {"error": str(e)}
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -526,6 +580,7 @@ def main():
         "atomic_mode": atomic,
         "batched": batched,
         "adjoint": adjoint,
+        "plastic": plastic,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

@@ -50,6 +50,21 @@ enum {
 	/* fixed_weight (samples/brunel.cpp:67-70): deliver adds params[0] (weight) to state field
 	 * params[1] of the target (0 = V, 1 = Gex, 2 = Gin; default 0). */
 	SPICE_SYNAPSE_FIXED_WEIGHT = 0,
+	/* Plastic synapses (the reference's PlasticSynapse concept, concepts.h:86-92, driven by
+	 * synapse_population.h:82-140): per-synapse state brought up to date lazily -- at each
+	 * delivery of its source's spike and every 64 steps -- from the target's 64-step post-spike
+	 * history.  A net with plastic connections steps in windows of one step.
+	 * ISTDP: inhibitory symmetric STDP (Vogels et al. 2011; no model of this kind ships with the
+	 * reference).  params {w0, field, eta, rho0 (Hz), tau (s)}: W starts at w0; a pre spike does
+	 * W = max(0, W + eta (x_post - 2 rho0 tau)), a post spike W += eta x_pre; traces add 1 per
+	 * spike and decay by x -= x dt/tau per step (skip(n): x *= (1 - dt/tau)^n, in double).
+	 * Delivery adds W to the target field; the sum over a step's events is order-dependent, so
+	 * ISTDP needs SPICE_MODE_ATOMIC.
+	 * COUNT: the counting model of the reference's tests (test/detail/synapse_population.cpp:
+	 * 84-94): update() adds 1, skip(n) adds n; params {scale, field}: delivery adds scale * count
+	 * (scale 0: delivers nothing, allowed in either mode). */
+	SPICE_SYNAPSE_ISTDP = 1,
+	SPICE_SYNAPSE_COUNT = 2,
 };
 
 /* Delivery modes. */
@@ -139,6 +154,11 @@ int spice_events(spice_net* net, uint64_t* events_out);
 /* csr<T> of a connection -- spice/include/spice/detail/csr.h:69-99: offsets (src+1 int64) and
  * neighbors (synapses int32), copied to host buffers. */
 int spice_conn_size(spice_net* net, int conn, int64_t* src_out, int64_t* synapses_out);
+/* Per-synapse state of a plastic connection, in CSR order, as stored: a synapse holds its state
+ * as of its last catch-up (its source's last delivery or the last multiple of 64 steps), exactly
+ * like the reference's synapse_population.  field 0 = W (COUNT: the count), 1 = x_pre,
+ * 2 = x_post; out holds synapses floats. */
+int spice_get_synapse_state(spice_net* net, int conn, int field, float* out);
 int spice_get_csr(spice_net* net, int conn, int64_t* offsets_out, int32_t* neighbors_out);
 
 /* fixed_probability(p) adjacency of one projection (the generator behind

@@ -23,6 +23,7 @@ REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
 REF_SOURCES = os.environ.get("SPICE_REFERENCE_DIR", "/root/reference")
 
 POISSON, LIF, LIF_COND, EXTERNAL = 0, 1, 2, 3
+SYN_ISTDP, SYN_COUNT = 1, 2  # plastic models of spo_set_plastic
 
 
 def build(with_reference: bool | None = None) -> None:
@@ -109,6 +110,10 @@ def lib():
         L.spo_last_dt.restype = C.c_float
         L.spo_last_dt.argtypes = [C.c_void_p]
         L.spo_last_error.restype = C.c_char_p
+        L.spo_set_plastic.restype = C.c_int
+        L.spo_set_plastic.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float]
+        L.spo_syn_state.restype = C.c_int
+        L.spo_syn_state.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p]
         _lib = L
     return _lib
 
@@ -232,6 +237,15 @@ class Net:
     def set_state(self, pop, field, values):
         v = np.ascontiguousarray(values, dtype=np.int32 if field == 3 else np.float32)
         self._chk(lib().spo_set_state(self.h, pop, field, v.ctypes.data))
+
+    def set_plastic(self, conn, model, w0=0.0, eta=0.0, rho0=0.0, tau=0.02):
+        """model: SYN_ISTDP or SYN_COUNT (spo_set_plastic)."""
+        self._chk(lib().spo_set_plastic(self.h, conn, model, w0, eta, rho0, tau))
+
+    def syn_state(self, conn, field=0) -> np.ndarray:
+        out = np.zeros(max(1, lib().spo_conn_synapses(self.h, conn)), dtype=np.float32)
+        self._chk(lib().spo_syn_state(self.h, conn, field, out.ctypes.data))
+        return out[:lib().spo_conn_synapses(self.h, conn)]
 
     def csr(self, conn):
         n = lib().spo_conn_synapses(self.h, conn)

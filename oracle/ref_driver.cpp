@@ -19,6 +19,10 @@
 //               pop poisson SIZE RATE | pop lif SIZE
 //               conn SRC DST P DELAY WEIGHT        (fixed_probability + fixed_weight)
 //               adj SRC DST DELAY WEIGHT M s0 d0 s1 d1 ...   (adj_list + fixed_weight)
+//               plastic POP P DELAY SCALE        (POP -> POP fixed_probability + count_syn; the
+//                                                 reference keeps the history of a plastic
+//                                                 connection's source, snn.h:44-45, so source and
+//                                                 target are the same population)
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -61,6 +65,19 @@ struct lif {
 struct fixed_weight {
 	float weight;
 	void deliver(lif::neuron& to) const { to.V += weight; }
+};
+
+// The counting plastic synapse of test/detail/synapse_population.cpp:84-94 (update adds 1, skip
+// adds n), delivering scale * count so the lazy schedule shows in the targets' V.  scale is a power
+// of two: the product is exact and the fast-math build cannot round it differently.
+struct count_syn {
+	float scale;
+	struct synapse {
+		int count = 0;
+	};
+	void deliver(synapse const& s, lif::neuron& to) const { to.V += s.count * scale; }
+	void update(synapse& s, float, bool, bool) const { s.count++; }
+	void skip(synapse& s, float, Int n) const { s.count += n; }
 };
 
 std::vector<float> g_dt;
@@ -188,6 +205,12 @@ static int run_net(int argc, char** argv) {
 				auto* L = net.add_population<lif>(size);
 				pops.push_back({true, size, L, L});
 			}
+		} else if (kw == "plastic") {
+			Int q;
+			double p;
+			float delay, scale;
+			in >> q >> p >> delay >> scale;
+			net.connect<count_syn>(pops[q].L, pops[q].L, fixed_probability(p), delay, {scale});
 		} else if (kw == "conn" || kw == "adj") {
 			Int s, d;
 			in >> s >> d;

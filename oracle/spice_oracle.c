@@ -215,6 +215,9 @@ typedef struct {
 	int64_t hist_len, hist_head;  /* hist_head = slot of age 0 */
 	/* EXTERNAL */
 	int ext_steps, ext_pos; int32_t* ext_counts; int64_t* ext_off; int32_t* ext_idx;
+	/* post-spike history of a plastic connection's target: bit k = spiked k steps ago
+	 * (neuron_population.h:126-132) */
+	uint64_t* post_hist;
 } spo_pop;
 
 typedef struct {
@@ -222,6 +225,12 @@ typedef struct {
 	float weight;
 	int64_t delay;
 	int64_t* off; int32_t* nb; int64_t nsyn;
+	/* plastic synapses (synapse_population.h:27-44, 82-140) */
+	int plastic;            /* 0 fixed weight, SPO_SYN_ISTDP, SPO_SYN_COUNT */
+	float eta, alpha, cdt;  /* iSTDP: learning rate, 2 rho0 tau, dt / tau */
+	double skip_tab[129];   /* pow(1 - dt / tau, n), n = -64 .. 64 */
+	float* sW; float* sA; float* sB;  /* per-synapse state in CSR order */
+	uint64_t* ages;         /* per source: bit 63 = pending pre update, low bits = step + 1 */
 } spo_conn;
 
 struct spo_net {
@@ -254,7 +263,11 @@ void spo_net_destroy(spo_net* n) {
 		free(p->hist); free(p->hist_n); free(p->hist_cap);
 		free(p->ext_counts); free(p->ext_off); free(p->ext_idx);
 	}
-	for (int i = 0; i < n->nconn; i++) { free(n->conns[i].off); free(n->conns[i].nb); }
+	for (int i = 0; i < n->nconn; i++) {
+		spo_conn* c = &n->conns[i];
+		free(c->off); free(c->nb); free(c->sW); free(c->sA); free(c->sB); free(c->ages);
+	}
+	for (int i = 0; i < n->npop; i++) free(n->pops[i].post_hist);
 	free(n);
 }
 
@@ -424,6 +437,96 @@ static inline int spo_lifc_update(float* V, float* Gex, float* Gin, int32_t* T, 
 	return spiked;
 }
 
+/* ---- plastic synapses ----
+ * The iSTDP model (inhibitory symmetric STDP, Vogels et al. 2011) written against the reference's
+ * PlasticSynapse concept (concepts.h:86-92): update() at a step with a pre and/or post spike,
+ * skip(n) over n quiet steps.  Traces decay by x -= x * dt/tau per step, as the sample plastic
+ * model of samples/brunel+.cpp:59-99 does; skip(n) multiplies by pow(1 - dt/tau, n) in double and
+ * rounds once to float (std::pow(float, Int) promotes to double).  The counting model is the
+ * plastic_synapse of test/detail/synapse_population.cpp:84-94: update adds 1, skip adds n. */
+static void syn_update(spo_conn* c, int64_t e, int pre, int post) {
+	if (c->plastic == SPO_SYN_COUNT) {
+		c->sW[e] = c->sW[e] + 1.0f;
+		return;
+	}
+	float W = c->sW[e], xa = c->sA[e], xb = c->sB[e];
+	if (pre) {
+		float const w = W + c->eta * (xb - c->alpha);
+		W             = w > 0.0f ? w : 0.0f;
+	}
+	if (post) W = W + c->eta * xa;
+	xa = xa + (pre ? 1.0f : 0.0f);
+	xb = xb + (post ? 1.0f : 0.0f);
+	xa = xa - xa * c->cdt;
+	xb = xb - xb * c->cdt;
+	c->sW[e] = W; c->sA[e] = xa; c->sB[e] = xb;
+}
+
+static void syn_skip(spo_conn* c, int64_t e, int64_t n) {
+	if (c->plastic == SPO_SYN_COUNT) {
+		c->sW[e] = c->sW[e] + (float)n;
+		return;
+	}
+	double const f = c->skip_tab[n + 64];
+	c->sA[e] = (float)((double)c->sA[e] * f);
+	c->sB[e] = (float)((double)c->sB[e] * f);
+}
+
+static int clz64(uint64_t x) { return __builtin_clzll(x); }
+
+/* synapse_population::_update's per-edge catch-up (synapse_population.h:88-116): replays the
+ * steps since the synapse was last brought up to date -- the pending pre update of the last
+ * delivery, then every post spike in the target's history, with skip() over the quiet steps.
+ * The reference computes ~0 >> prefix with prefix up to 64 (pre set and time == age); x86-64
+ * shifts by prefix mod 64, and that is what is restated here. */
+static void catch_up(spo_conn* c, int64_t e, int64_t time, uint64_t ages, uint64_t hist) {
+	int const pre     = (int)(ages >> 63);
+	int64_t const age = (int64_t)(ages & ~(1ULL << 63));
+	if (!(time >= age)) return;
+	int64_t const prefix = 63 + pre - time + age;
+	uint64_t const mask  = ~0ULL >> (prefix & 63);
+	if (pre) syn_update(c, e, 1, (hist & (1ULL << ((time - age) & 63))) != 0);
+	hist &= mask;
+	int64_t p = prefix;
+	while (hist) {
+		int const lz = clz64(hist);
+		syn_skip(c, e, lz - p);
+		syn_update(c, e, 0, 1);
+		hist ^= 1ULL << (63 - lz);
+		p = lz + 1;
+	}
+	syn_skip(c, e, 64 - p);
+}
+
+int spo_set_plastic(spo_net* n, int conn, int model, float w0, float eta, float rho0, float tau) {
+	if (conn < 0 || conn >= n->nconn) return fail("bad connection");
+	if (model != SPO_SYN_ISTDP && model != SPO_SYN_COUNT) return fail("bad plastic model");
+	spo_conn* c = &n->conns[conn];
+	spo_pop* d  = &n->pops[c->dst];
+	int64_t S = n->pops[c->src].size;
+	c->plastic = model;
+	c->eta     = eta;
+	c->alpha   = 2.0f * rho0 * tau;
+	c->cdt     = n->dt * (1.0f / tau);
+	float const base = 1.0f - c->cdt;
+	for (int k = -64; k <= 64; k++) c->skip_tab[k + 64] = pow((double)base, (double)k);
+	c->sW   = (float*)malloc(sizeof(float) * (size_t)(c->nsyn + 1));
+	c->sA   = (float*)calloc((size_t)(c->nsyn + 1), sizeof(float));
+	c->sB   = (float*)calloc((size_t)(c->nsyn + 1), sizeof(float));
+	c->ages = (uint64_t*)calloc((size_t)(S + 1), sizeof(uint64_t));
+	for (int64_t e = 0; e < c->nsyn; e++) c->sW[e] = model == SPO_SYN_COUNT ? 0.0f : w0;
+	if (!d->post_hist) d->post_hist = (uint64_t*)calloc((size_t)(d->size + 1), sizeof(uint64_t));
+	return 0;
+}
+
+int spo_syn_state(const spo_net* n, int conn, int field, float* out) {
+	if (conn < 0 || conn >= n->nconn || !n->conns[conn].plastic) return fail("not a plastic connection");
+	const spo_conn* c = &n->conns[conn];
+	const float* src  = field == 0 ? c->sW : (field == 1 ? c->sA : c->sB);
+	memcpy(out, src, sizeof(float) * (size_t)c->nsyn);
+	return 0;
+}
+
 void spo_step(spo_net* n) {
 	/* snn::step (snn.cpp:7-28) */
 	float dt   = spo_kahan_step(&n->simtime, n->dt);
@@ -464,7 +567,23 @@ void spo_step(spo_net* n) {
 				}
 				break;
 		}
+		if (p->post_hist) { /* neuron_population.h:126-132 */
+			for (int64_t i = 0; i < p->size; i++) p->post_hist[i] <<= 1;
+			for (int64_t k = 0; k < p->hist_n[slot]; k++) p->post_hist[p->hist[slot][k]] |= 1;
+		}
 	}
+
+	/* every 64 steps all plastic synapses catch up (snn.cpp:17-19, synapse_population.h:70-74) */
+	if (n->time % 64 == 0)
+		for (int ci = 0; ci < n->nconn; ci++) {
+			spo_conn* c = &n->conns[ci];
+			if (!c->plastic) continue;
+			const uint64_t* h = n->pops[c->dst].post_hist;
+			for (int64_t s = 0; s < n->pops[c->src].size; s++) {
+				for (int64_t e = c->off[s]; e < c->off[s + 1]; e++) catch_up(c, e, n->time, c->ages[s], h[c->nb[e]]);
+				c->ages[s] = (uint64_t)(n->time + 1);
+			}
+		}
 
 	/* deliveries in connect order, spikes of age d-1 (snn.cpp:21-25, synapse_population.h:82-140) */
 	for (int ci = 0; ci < n->nconn; ci++) {
@@ -477,7 +596,16 @@ void spo_step(spo_net* n) {
 		float w  = c->weight;
 		for (int64_t k = 0; k < sp->hist_n[slot]; k++) {
 			int32_t s = sp->hist[slot][k];
-			for (int64_t e = c->off[s]; e < c->off[s + 1]; e++) F[c->nb[e]] = F[c->nb[e]] + w;
+			if (c->plastic) {
+				for (int64_t e = c->off[s]; e < c->off[s + 1]; e++) {
+					catch_up(c, e, n->time, c->ages[s], dp->post_hist[c->nb[e]]);
+					if (c->plastic == SPO_SYN_ISTDP) F[c->nb[e]] = F[c->nb[e]] + c->sW[e];
+					else if (w != 0.0f) F[c->nb[e]] = F[c->nb[e]] + c->sW[e] * w;
+				}
+				c->ages[s] = (uint64_t)(n->time + 1) | (1ULL << 63);
+			} else {
+				for (int64_t e = c->off[s]; e < c->off[s + 1]; e++) F[c->nb[e]] = F[c->nb[e]] + w;
+			}
 			n->events += c->off[s + 1] - c->off[s];
 		}
 	}

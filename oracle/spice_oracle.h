@@ -58,6 +58,12 @@ enum {
 	SPO_EXTERNAL = 3, /* per-population update from a cyclic train   (samples/external_input.cpp:17-30) */
 };
 
+/* plastic synapse models (spo_set_plastic) */
+enum {
+	SPO_SYN_ISTDP = 1, /* inhibitory symmetric STDP (Vogels et al. 2011) on pre/post traces */
+	SPO_SYN_COUNT = 2  /* counts update() calls and skipped steps (test/detail/synapse_population.cpp:84-94) */
+};
+
 typedef struct spo_net spo_net;
 
 spo_net* spo_net_create(float dt, float max_delay, const uint32_t* seeds, int nseeds);
@@ -71,6 +77,15 @@ int spo_set_external(spo_net* net, int pop, int nsteps, const int32_t* counts,
  * to state field `field` of the target (0=V, 1=Gex, 2=Gin).  Returns the connection id,
  * or -1 with a message from spo_last_error(). */
 int spo_connect(spo_net* net, int src, int dst, double p, float delay, int field, float weight);
+/* Makes connection `conn` plastic (the reference's synapse_population with a PlasticSynapse model,
+ * synapse_population.h:27-140): per-synapse state, lazy catch-up from the target's post history at
+ * each delivery and every 64 steps.  iSTDP: W starts at w0; pre spike W += eta (x_post - 2 rho0 tau)
+ * (W >= 0), post spike W += eta x_pre; traces decay with tau.  The iSTDP delivery adds the synapse's
+ * W to the connection's target field; the counting model's delivery adds count * (the connection's
+ * weight), nothing for weight 0. */
+int spo_set_plastic(spo_net* net, int conn, int model, float w0, float eta, float rho0, float tau);
+/* Per-synapse state in CSR order: field 0 W (counting model: the count), 1 x_pre, 2 x_post. */
+int spo_syn_state(const spo_net* net, int conn, int field, float* out);
 /* adj_list projection (spice/src/topology.cpp:56-71): n (src, dst) pairs. */
 int spo_connect_adj(spo_net* net, int src, int dst, int64_t n, const int32_t* pairs,
                     float delay, int field, float weight);

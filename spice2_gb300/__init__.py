@@ -31,7 +31,7 @@ LIB_PATH = os.path.join(_HERE, "libspice_gb300.so")
 
 OK, EINVAL, ECUDA, ENOMEM, ESTATE, EOVERFLOW = 0, 1, 2, 3, 4, 5
 NEURON_POISSON, NEURON_LIF, NEURON_LIF_COND, NEURON_EXTERNAL = 0, 1, 2, 3
-SYNAPSE_FIXED_WEIGHT = 0
+SYNAPSE_FIXED_WEIGHT, SYNAPSE_ISTDP, SYNAPSE_COUNT = 0, 1, 2
 MODE_DETERMINISTIC, MODE_ATOMIC = 0, 1
 FIELD_V, FIELD_GEX, FIELD_GIN, FIELD_TREF = 0, 1, 2, 3
 
@@ -86,6 +86,7 @@ def _load():
         "spice_time": [vp, P(i64)],
         "spice_events": [vp, P(C.c_uint64)],
         "spice_conn_size": [vp, i32, P(i64), P(i64)],
+        "spice_get_synapse_state": [vp, i32, i32, vp],
         "spice_get_csr": [vp, i32, vp, vp],
         "spice_set_profiling": [vp, i32],
         "spice_kernel_stats": [vp, i32, P(i64), P(f64)],
@@ -182,6 +183,35 @@ class fixed_weight:
 
     def params(self):
         return [self.weight, float(self.field)]
+
+
+@dataclass(frozen=True)
+class istdp:
+    """Inhibitory symmetric STDP (Vogels et al. 2011) as a plastic synapse with lazy, event-driven
+    updates (the reference's PlasticSynapse concept, synapse_population.h:82-140): W starts at w0;
+    a pre spike does W = max(0, W + eta (x_post - 2 rho0 tau)), a post spike W += eta x_pre; the
+    traces decay with tau.  Delivery adds W to the target field (default Gin).  Needs atomic mode."""
+    w0: float
+    field: int = FIELD_GIN
+    eta: float = 1e-3
+    rho0: float = 5.0
+    tau: float = 0.02
+    model = SYNAPSE_ISTDP
+
+    def params(self):
+        return [self.w0, float(self.field), self.eta, self.rho0, self.tau]
+
+
+@dataclass(frozen=True)
+class count_synapse:
+    """The counting plastic synapse of the reference's tests (test/detail/synapse_population.cpp:
+    84-94): update() adds 1, skip(n) adds n; delivery adds scale * count (scale 0: nothing)."""
+    scale: float = 0.0
+    field: int = FIELD_V
+    model = SYNAPSE_COUNT
+
+    def params(self):
+        return [self.scale, float(self.field)]
 
 
 def excitatory(weight: float) -> fixed_weight:
@@ -294,11 +324,13 @@ class snn:
         out = C.c_int()
         if isinstance(topology, fixed_probability):
             _check(lib().spice_connect_fixed_probability(self._h, source.id, target.id, float(topology.p),
-                                                         delay, SYNAPSE_FIXED_WEIGHT, arr, len(prm), C.byref(out)))
+                                                         delay, getattr(syn, "model", SYNAPSE_FIXED_WEIGHT), arr,
+                                                         len(prm), C.byref(out)))
         elif isinstance(topology, adj_list):
             pairs = np.ascontiguousarray(np.asarray(topology.edges, dtype=np.int32).reshape(-1, 2))
             _check(lib().spice_connect_adj_list(self._h, source.id, target.id, pairs.ctypes.data, len(pairs),
-                                                delay, SYNAPSE_FIXED_WEIGHT, arr, len(prm), C.byref(out)))
+                                                delay, getattr(syn, "model", SYNAPSE_FIXED_WEIGHT), arr, len(prm),
+                                                C.byref(out)))
         else:
             raise TypeError("topology must be fixed_probability or adj_list")
         self._conns.append((source, target, topology, delay, syn))
@@ -394,6 +426,13 @@ class snn:
         src, syn = C.c_int64(), C.c_int64()
         _check(lib().spice_conn_size(self._h, conn, C.byref(src), C.byref(syn)))
         return syn.value
+
+    def synapse_state(self, conn: int, field: int = 0) -> np.ndarray:
+        """Per-synapse state of a plastic connection (CSR order): 0 W / count, 1 x_pre, 2 x_post."""
+        m = self.synapses(conn)
+        out = np.zeros(max(1, m), dtype=np.float32)
+        _check(lib().spice_get_synapse_state(self._h, conn, field, out.ctypes.data))
+        return out[:m]
 
     def csr(self, conn: int):
         src, syn = C.c_int64(), C.c_int64()
@@ -525,5 +564,5 @@ def brunel_sweep(sizes: Sequence[int], seed0: int = 1000, mode: int = MODE_DETER
 
 
 __all__ = ["snn", "Population", "poisson", "lif", "lif_cond", "external_input", "fixed_weight", "excitatory",
-           "inhibitory", "fixed_probability", "adj_list", "brunel", "batch", "brunel_sweep", "brunel_sweep_sizes",
+           "inhibitory", "istdp", "count_synapse", "fixed_probability", "adj_list", "brunel", "batch", "brunel_sweep", "brunel_sweep_sizes",
            "SpiceError", "LogicError", "CudaError", "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib"]

@@ -324,6 +324,8 @@ extern "C" int spice_batch_create(spice_net* const* nets, int nnets, spice_batch
 		if (n->mode != n0->mode) return bfail(SPICE_EINVAL, "batched nets must use the same mode");
 		for (auto const& p : n->pops)
 			if (p.d.model == EXTERNAL) return bfail(SPICE_EINVAL, "batched nets cannot have external_input populations");
+		for (auto const& c : n->conns)
+			if (c.d.plastic) return bfail(SPICE_EINVAL, "batched nets cannot have plastic connections");
 	}
 	int dev_prev = 0;
 	cudaGetDevice(&dev_prev);

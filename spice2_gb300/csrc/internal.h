@@ -68,6 +68,7 @@ struct PopDev {
 	                     // 0: each slot is fully overwritten by one delivery, no clearing needed
 	const u128* chunk_poly;  // POISSON: x^(draw_offset + 32 c) mod P for chunk c
 	int net;             // index of the owning net in a batch (0 outside batches)
+	uint64_t* hist;      // targets of plastic connections: post-spike history, bit k = spiked k steps ago
 	// EXTERNAL: cyclic train
 	const int32_t* ext_counts;
 	const int64_t* ext_off;
@@ -92,6 +93,17 @@ struct ConnDev {
 	uint32_t inc;             // 1 << group_shift
 	int F, fslot;             // atomic: sums per neuron, index of this connection's field
 	const int64_t* bounds;    // [src_size][ntiles of dst + 1]: row positions where each tile starts
+	// plastic synapses (synapse_population.h:27-140); plastic = 0 for fixed_weight
+	int plastic;              // SPICE_SYNAPSE_ISTDP or SPICE_SYNAPSE_COUNT
+	float eta, alpha, cdt;    // iSTDP: learning rate, 2 rho0 tau, dt / tau
+	float* sW;                // per synapse, CSR order: W (counting model: the count)
+	float* sA;                // x_pre
+	float* sB;                // x_post
+	uint64_t* ages;           // per source: bit 63 = pending pre update, low bits = step + 1
+	const uint64_t* dst_hist; // the target population's post-spike history
+	const double* skip_tab;   // pow(1 - dt/tau, n) for n = -64 .. 64
+	int src_nwords;           // source bitmap words
+	const uint32_t* src_bits; // source spike bitmap ring [Hb][src_nwords]
 };
 
 struct Pop {
@@ -106,6 +118,7 @@ struct Conn {
 	ConnDev d;
 	int64_t synapses = 0;
 	bool adj         = false;
+	float w0 = 0, rho0 = 0, tau = 0;  // plastic parameters
 };
 
 struct PendingGen {  // a fixed_probability connection whose adjacency is not generated yet
@@ -180,6 +193,7 @@ struct spice_net {
 	int deliver_algo = 1;            // delivery work mapping (tunable)
 	int overlap_sources = 1;         // source kernels on their own stream (tunable)
 	int dmin = 1, dmax = 1;          // connection delays in steps
+	bool plastic = false;            // any plastic connection (windows of one step)
 };
 
 namespace spice_gb300 {

@@ -58,6 +58,8 @@ cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const i
 // Jump tables of steps t < nsteps: tables[t][g][m] = XOR of T^(8g+q)(seed_t) over the bits q of m.
 cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* tables);
 
+constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
+
 struct WindowArgs {
 	int64_t t0;        // absolute step of the window's first step
 	int K;             // steps in this window
@@ -76,7 +78,8 @@ struct WindowArgs {
 	int blk_begin[kMaxPops + 1];
 	int blk_kind[kMaxPops];      // 0: per-neuron window CTAs, 1: Poisson step CTAs, 2: external,
 	                             // 3: per-neuron CTAs of a LIF whose inputs all add to V (16-bit counts)
-	                             // (k_neurons launches kinds 0 and 3, k_sources kinds 1 and 2)
+	                             // (k_neurons launches kinds 0 and 3, k_sources kinds 1 and 2);
+	                             // + kHistKind: the population keeps a post-spike history
 	int blk_per_step[kMaxPops];  // Poisson / external: CTAs per step
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
 };
@@ -110,6 +113,12 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 // bounds[s][t] = position in row s of the first target >= t * tile (t = 0..ntiles).
 cudaError_t launch_tile_bounds(cudaStream_t stream, const int64_t* off, const int32_t* nb, int64_t rows, int tile,
                                int ntiles, int64_t* bounds);
+
+// Plastic connections: the periodic catch-up of every synapse (every 64 steps), and the delivery
+// of the spikes in bitmap slot hslot into input ring slot `slot` at step `time`.
+cudaError_t launch_plastic_update_all(cudaStream_t stream, ConnDev const& c, int64_t time);
+cudaError_t launch_plastic_deliver(cudaStream_t stream, ConnDev const& c, int64_t time, int hslot, int64_t slot,
+                                   bool deliver, unsigned long long* events);
 
 // Applies the inputs waiting in ring slot (t - 1) to the state and clears them.
 cudaError_t launch_apply_pending(cudaStream_t stream, const PopDev* pops, int npop_dev, const int* stateful,

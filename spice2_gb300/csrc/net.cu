@@ -244,11 +244,27 @@ extern "C" int spice_add_population(spice_net* n, int model, int64_t size, const
 }
 
 namespace {
-int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int np, float* w, int* field) {
-	if (synapse != SPICE_SYNAPSE_FIXED_WEIGHT) return fail(SPICE_EINVAL, "unknown synapse model");
-	if (np < 1 || !params) return fail(SPICE_EINVAL, "fixed_weight needs params {weight[, field]}");
-	*w     = params[0];
-	*field = np > 1 ? (int)params[1] : 0;
+int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int np, Conn& c) {
+	float* w   = &c.d.weight;
+	int* field = &c.d.field;
+	if (synapse == SPICE_SYNAPSE_FIXED_WEIGHT) {
+		if (np < 1 || !params) return fail(SPICE_EINVAL, "fixed_weight needs params {weight[, field]}");
+	} else if (synapse == SPICE_SYNAPSE_ISTDP) {
+		if (np < 5 || !params) return fail(SPICE_EINVAL, "istdp needs params {w0, field, eta, rho0, tau}");
+		if (!(params[4] > 0)) return fail(SPICE_EINVAL, "istdp tau must be > 0");
+		c.w0   = params[0];
+		c.rho0 = params[3];
+		c.tau  = params[4];
+		c.d.eta = params[2];
+	} else if (synapse == SPICE_SYNAPSE_COUNT) {
+		if (np < 1 || !params) return fail(SPICE_EINVAL, "count needs params {scale[, field]}");
+		c.tau = 1.0f;
+	} else {
+		return fail(SPICE_EINVAL, "unknown synapse model");
+	}
+	c.d.plastic = synapse;
+	*w          = params[0];
+	*field      = np > 1 ? (int)params[1] : 0;
 	int const m = n->pops[dst].d.model;
 	if (*field < 0 || *field > 2 || (m == LIF && *field != 0))
 		return fail(SPICE_EINVAL, "the synapse's target field does not exist in the target neuron model");
@@ -278,16 +294,12 @@ extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, d
 	int d = 0;
 	TRY(conn_common(n, src, dst, delay, &d));
 	if (!(0 <= p && p <= 1)) return pre_failed("topology.cpp:79", "0 <= p && p <= 1");
-	float w   = 0;
-	int field = 0;
-	TRY(parse_synapse(n, dst, synapse, params, np, &w, &field));
 	Conn c{};
 	memset(&c.d, 0, sizeof c.d);
+	TRY(parse_synapse(n, dst, synapse, params, np, c));
 	c.d.src = src;
 	c.d.dst = dst;
 	c.d.delay  = d;
-	c.d.weight = w;
-	c.d.field  = field;
 	c.d.src_size = n->pops[src].d.size;
 	c.d.dst_size = n->pops[dst].d.size;
 	n->conns.push_back(c);
@@ -302,9 +314,9 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	int d = 0;
 	TRY(conn_common(n, src, dst, delay, &d));
 	if (npairs < 0 || (npairs > 0 && !pairs)) return fail(SPICE_EINVAL, "bad pairs");
-	float w   = 0;
-	int field = 0;
-	TRY(parse_synapse(n, dst, synapse, params, np, &w, &field));
+	Conn c{};
+	memset(&c.d, 0, sizeof c.d);
+	TRY(parse_synapse(n, dst, synapse, params, np, c));
 	int64_t const S = n->pops[src].d.size, Dn = n->pops[dst].d.size;
 	// adj_list::generate: sort src<<32|dst, stream the edges (topology.cpp:56-71, 12-32)
 	std::vector<uint64_t> e((size_t)npairs);
@@ -324,13 +336,9 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 		nb[i] = (int32_t)(e[i] & 0xffffffffu);
 	}
 	while (s <= S) off[s++] = npairs;
-	Conn c{};
-	memset(&c.d, 0, sizeof c.d);
 	c.d.src = src;
 	c.d.dst = dst;
 	c.d.delay    = d;
-	c.d.weight   = w;
-	c.d.field    = field;
 	c.d.src_size = S;
 	c.d.dst_size = Dn;
 	c.synapses   = npairs;
@@ -459,6 +467,7 @@ int setup_tiles(spice_net* n, bool first) {
 				by_dst.push_back(ci);
 				if (dfirst < 0) dfirst = n->conns[ci].d.delay;
 				mixed |= n->conns[ci].d.delay != dfirst;
+				mixed |= n->conns[ci].d.plastic != 0;  // plastic deliveries add into the ring
 			}
 		d.in_end      = (int)by_dst.size();
 		// slots are overwritten by one delivery CTA unless delays differ or tiles are split
@@ -493,10 +502,21 @@ int prepare(spice_net* n) {
 	int const np = (int)n->pops.size();
 	int64_t const D = n->max_delay;
 	if (D < 1) return pre_failed("neuron_population.h:108", "max_delay >= 1");
+	// plastic connections: per-step catch-up timing, so windows of one step
+	n->plastic = false;
+	for (auto const& c : n->conns) {
+		if (!c.d.plastic) continue;
+		n->plastic = true;
+		bool const delivers = c.d.plastic == SPICE_SYNAPSE_ISTDP || c.d.weight != 0.0f;
+		if (delivers && n->mode != SPICE_MODE_ATOMIC)
+			return fail(SPICE_EINVAL, "plastic synapses that deliver per-synapse weights need SPICE_MODE_ATOMIC "
+			                          "(their per-step sums are order-dependent)");
+	}
 	// window: the minimum delay (every delay is >= 1)
 	int K = kMaxWindow;
 	for (auto const& c : n->conns) K = std::min<int>(K, c.d.delay);
 	if (n->max_window > 0) K = std::min(K, n->max_window);
+	if (n->plastic) K = 1;
 	// the delivery kernel keeps a (step, connection) prefix of K * nconn entries in shared memory
 	if (!n->conns.empty()) K = std::min<int>(K, std::max<int>(1, 4096 / (int)n->conns.size()));
 	n->K  = std::max(K, 1);
@@ -534,7 +554,7 @@ int prepare(spice_net* n) {
 		d.ngroups = 0;
 		for (int ci = 0; ci < (int)n->conns.size(); ci++) {
 			ConnDev& c = n->conns[ci].d;
-			if (c.dst != pi) continue;
+			if (c.dst != pi || c.plastic) continue;
 			int g = last_of_field[c.field];
 			if (g < 0 || memcmp(&d.group_weight[g], &c.weight, sizeof(float)) != 0) {
 				if (d.ngroups >= kMaxGroups)
@@ -594,6 +614,9 @@ int prepare(spice_net* n) {
 		int F = 0;
 		for (int g = 0; g < d.ngroups; g++)
 			if (d.field_slot[d.group_field[g]] < 0) d.field_slot[d.group_field[g]] = F++;
+		for (auto const& cc : n->conns)  // plastic deliveries add into the atomic-mode sums
+			if (cc.d.dst == pi && cc.d.plastic && n->mode == SPICE_MODE_ATOMIC && d.field_slot[cc.d.field] < 0)
+				d.field_slot[cc.d.field] = F++;
 		d.F = std::max(F, 1);
 		if (n->mode == SPICE_MODE_DETERMINISTIC)
 			TRY(dalloc(n, &d.cnt, (size_t)D * d.size * d.W));
@@ -615,6 +638,33 @@ int prepare(spice_net* n) {
 		d.fslot    = T.field_slot[d.field];
 	}
 	for (auto& p : n->pops) p.d.net = 0;
+	// plastic connections: per-synapse state, per-source ages, the targets' post history
+	for (auto& c : n->conns) {
+		ConnDev& d = c.d;
+		if (!d.plastic) continue;
+		PopDev& T = n->pops[d.dst].d;
+		PopDev const& S = n->pops[d.src].d;
+		if (!T.hist) TRY(dalloc(n, &T.hist, (size_t)std::max<int64_t>(T.size, 1)));
+		TRY(dalloc(n, &d.sW, (size_t)std::max<int64_t>(c.synapses, 1), false));
+		TRY(dalloc(n, &d.sA, (size_t)std::max<int64_t>(c.synapses, 1)));
+		TRY(dalloc(n, &d.sB, (size_t)std::max<int64_t>(c.synapses, 1)));
+		TRY(dalloc(n, &d.ages, (size_t)std::max<int64_t>(S.size, 1)));
+		std::vector<float> w0((size_t)std::max<int64_t>(c.synapses, 1), d.plastic == SPICE_SYNAPSE_ISTDP ? c.w0 : 0.0f);
+		CUDA_TRY(cudaMemcpy(d.sW, w0.data(), sizeof(float) * w0.size(), cudaMemcpyHostToDevice));
+		d.alpha = 2.0f * c.rho0 * c.tau;
+		d.cdt   = n->dt * (1.0f / c.tau);
+		std::vector<double> tab(129);
+		float const base = 1.0f - d.cdt;
+		for (int k = -64; k <= 64; k++) tab[k + 64] = pow((double)base, (double)k);
+		double* dt = nullptr;
+		TRY(dalloc(n, &dt, tab.size(), false));
+		CUDA_TRY(cudaMemcpy(dt, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
+		d.skip_tab   = dt;
+		d.src_bits   = S.bits;
+		d.src_nwords = S.nwords;
+	}
+	for (auto& c : n->conns)
+		if (c.d.plastic) c.d.dst_hist = n->pops[c.d.dst].d.hist;
 	TRY(dalloc(n, &n->d_counts, (size_t)2 * n->K * std::max(np, 1)));
 	TRY(dalloc(n, &n->d_pops, std::max(np, 1), false));
 	TRY(dalloc(n, &n->d_conns, std::max<size_t>(n->conns.size(), 1), false));
@@ -714,7 +764,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					ws.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
 					wa.blk_kind[p] = 2;
 				} else {
-					wa.blk_kind[p] = neuron_block_kind(P);
+					wa.blk_kind[p] = neuron_block_kind(P) + (P.hist ? kHistKind : 0);
 					ws.blk_kind[p] = wa.blk_kind[p];
 					nb += (int)((P.size + 255) / 256);
 				}
@@ -736,6 +786,12 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			CUDA_TRY(launch_neurons(n->stream, wa, nb));
 			TRY(ev_end(n, slot));
 			if (nb > 0) n->launches++;
+			if (n->plastic && n->time % 64 == 0)  // snn.cpp:17-19 (windows are one step long)
+				for (auto const& c : n->conns)
+					if (c.d.plastic) {
+						CUDA_TRY(launch_plastic_update_all(n->stream, c.d, n->time));
+						n->launches++;
+					}
 			if (nbs > 0) CUDA_TRY(cudaStreamWaitEvent(n->stream, n->ev_src[q], 0));
 			DeliverArgs da{};
 			da.t0     = n->time;
@@ -767,6 +823,16 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			da.algo           = n->deliver_algo;
 			TRY(ev_begin(n, 1, &slot));
 			CUDA_TRY(launch_deliver(n->stream, da, n->deliver_threads));
+			if (n->plastic)  // spikes of age d - 1 (snn.cpp:21-25), from the source's bitmap ring
+				for (auto const& c : n->conns)
+					if (c.d.plastic && n->time >= c.d.delay - 1) {
+						int const hs = (int)((n->time - c.d.delay + 1) % n->Hb);
+						bool const delivers = n->mode == SPICE_MODE_ATOMIC &&
+						                      (c.d.plastic == SPICE_SYNAPSE_ISTDP || c.d.weight != 0.0f);
+						CUDA_TRY(launch_plastic_deliver(n->stream, c.d, n->time, hs, n->time % n->max_delay, delivers,
+						                                n->d_events));
+						n->launches++;
+					}
 			TRY(ev_end(n, slot));
 			n->launches++;
 			if (record) {
@@ -1013,6 +1079,20 @@ extern "C" int spice_set_profiling(spice_net* n, int on) {
 			CUDA_TRY(cudaEventCreate(&e));
 			n->ev_pool.push_back(e);
 		}
+	return SPICE_OK;
+}
+
+extern "C" int spice_get_synapse_state(spice_net* n, int conn, int field, float* out) {
+	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	if (field < 0 || field > 2) return fail(SPICE_EINVAL, "field must be 0 (W), 1 (x_pre) or 2 (x_post)");
+	if (!n->conns[conn].d.plastic) return fail(SPICE_EINVAL, "not a plastic connection");
+	TRY(prepare(n));
+	ConnDev const& d = n->conns[conn].d;
+	const float* src = field == 0 ? d.sW : (field == 1 ? d.sA : d.sB);
+	int64_t const m  = n->conns[conn].synapses;
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	if (m > 0) CUDA_TRY(cudaMemcpy(out, src, sizeof(float) * m, cudaMemcpyDeviceToHost));
 	return SPICE_OK;
 }
 

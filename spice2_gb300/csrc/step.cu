@@ -17,6 +17,7 @@
 // atomics and replaying the adds one by one in group order with IEEE round-to-nearest
 // (__fadd_rn; the library is built with -fmad=false).  Atomic mode adds float weights with
 // atomics (fast, order-dependent rounding).
+#include "spice_gb300.h"
 #include "internal.h"
 #include "kernels.h"
 
@@ -185,7 +186,7 @@ __device__ __forceinline__ void replay_words(PopDev const& P, const uint32_t (&x
 // already, so the input words of up to 16 consecutive slots are loaded together first; the step
 // loop itself is kept rolled and small (instruction-cache friendly).  FAST: every input group adds to
 // V through a 16-bit counter of word 0 (Brunel).
-template <int MODE, bool FAST, class A>
+template <int MODE, bool FAST, bool HIST, class A>
 __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p, int b) {
 	int const N       = (int)Pg->size;
 	int const i       = b * kThreads + threadIdx.x;
@@ -208,6 +209,8 @@ __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p,
 	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
 	float V = 0, Gex = 0, Gin = 0;
 	int32_t T = 0;
+	uint64_t* const hp = HIST ? Pg->hist : nullptr;
+	uint64_t h         = 0;
 	if (valid) {
 		V = Vp[i];
 		T = Tp[i];
@@ -215,6 +218,7 @@ __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p,
 			Gex = Pg->Gex[i];
 			Gin = Pg->Gin[i];
 		}
+		if (HIST) h = hp[i];
 	}
 	int const D = (int)a.D, Hb = a.Hb;
 	int slot  = a.slot0;   // (t0 - 1) mod D: inputs applied before the update of step t0
@@ -288,6 +292,7 @@ __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p,
 				else
 					spike = lifc_update(V, Gex, Gin, T, dt);
 			}
+			if (HIST) h = (h << 1) | (spike ? 1ull : 0ull);  // neuron_population.h:126-132
 			unsigned const mask = __ballot_sync(0xffffffffu, spike);
 			if (lane == 0 && word < nwords) bits[(int64_t)hslot * nwords + word] = mask;
 			if (mask) {  // one list reservation per warp with spikes
@@ -307,6 +312,7 @@ __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p,
 			Pg->Gex[i] = Gex;
 			Pg->Gin[i] = Gin;
 		}
+		if (HIST) hp[i] = h;
 	}
 }
 
@@ -417,9 +423,14 @@ __global__ void __launch_bounds__(kThreads) k_neurons(const __grid_constant__ Wi
 	int const b = blockIdx.x;
 	int p       = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
-	int const lb = b - a.blk_begin[p];
-	if (a.blk_kind[p] == 3) window_neurons<MODE, true>(a, a.pops + p, p, lb);
-	else if (!ONLY_FAST) window_neurons<MODE, false>(a, a.pops + p, p, lb);
+	int const lb   = b - a.blk_begin[p];
+	int const kind = a.blk_kind[p];
+	if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
+	else if (!ONLY_FAST) {
+		if (kind == 0) window_neurons<MODE, false, false>(a, a.pops + p, p, lb);
+		else if (kind == 3 + kHistKind) window_neurons<MODE, true, true>(a, a.pops + p, p, lb);
+		else window_neurons<MODE, false, true>(a, a.pops + p, p, lb);
+	}
 }
 
 // Populations without inputs (Poisson, external trains): one CTA per (step, chunk).  They depend on
@@ -508,7 +519,7 @@ __device__ __forceinline__ void deliver_flat(A const& a, PopDev const& P, int t,
 	for (int ci = P.in_begin; ci < P.in_end; ci++) {
 		ConnDev const& C = a.conns[ci];
 		int64_t const k  = sigma - (a.t0 + C.delay - 1);
-		if (k < 0 || k >= a.K) continue;
+		if (k < 0 || k >= a.K || C.plastic) continue;
 		touched = true;
 		int const n          = a.counts[k * a.npop + C.src];
 		const int32_t* lst   = C.src_list + (a.list_k0 + k) * C.src_size;
@@ -596,7 +607,7 @@ __device__ __forceinline__ void deliver_tps(A const& a, PopDev const& P, int t, 
 	for (int ci = P.in_begin; ci < P.in_end; ci++) {
 		ConnDev const& C = a.conns[ci];
 		int64_t const k  = sigma - (a.t0 + C.delay - 1);
-		if (k < 0 || k >= a.K) continue;
+		if (k < 0 || k >= a.K || C.plastic) continue;
 		touched = true;
 		int const n        = a.counts[k * a.npop + C.src];
 		const int32_t* lst = C.src_list + (a.list_k0 + k) * C.src_size;
@@ -674,7 +685,7 @@ __device__ __forceinline__ void deliver_wps(A const& a, PopDev const& P, int t, 
 	for (int ci = P.in_begin; ci < P.in_end; ci++) {
 		ConnDev const& C = a.conns[ci];
 		int64_t const k  = sigma - (a.t0 + C.delay - 1);
-		if (k < 0 || k >= a.K) continue;
+		if (k < 0 || k >= a.K || C.plastic) continue;
 		touched = true;
 		int const n        = a.counts[k * a.npop + C.src];
 		const int32_t* lst = C.src_list + (a.list_k0 + k) * C.src_size;
@@ -946,6 +957,120 @@ __global__ void k_scan_add(int64_t* out, int64_t n, const int64_t* __restrict__ 
 
 
 // ---------------------------------------------------------------------------------------------
+// Plastic synapses: the lazy per-synapse catch-up of synapse_population::_update
+// (synapse_population.h:82-140).  A synapse's state is current as of the step recorded in its
+// source's `ages` word; at each delivery of the source's spike and every 64 steps it replays the
+// steps since: the pending pre update of the last delivery (bit 63), then every post spike in
+// the target's 64-step history with skip() over the quiet steps between them.
+// ---------------------------------------------------------------------------------------------
+
+struct SynState {
+	float W, A, B;
+};
+
+// iSTDP (Vogels et al. 2011) and the counting model of the reference's tests.
+__device__ __forceinline__ void syn_update(ConnDev const& C, SynState& s, bool pre, bool post) {
+	if (C.plastic == SPICE_SYNAPSE_COUNT) {
+		s.W = __fadd_rn(s.W, 1.0f);
+		return;
+	}
+	if (pre) {
+		float const w = __fadd_rn(s.W, __fmul_rn(C.eta, __fsub_rn(s.B, C.alpha)));
+		s.W           = w > 0.0f ? w : 0.0f;
+	}
+	if (post) s.W = __fadd_rn(s.W, __fmul_rn(C.eta, s.A));
+	s.A = __fadd_rn(s.A, pre ? 1.0f : 0.0f);
+	s.B = __fadd_rn(s.B, post ? 1.0f : 0.0f);
+	s.A = __fsub_rn(s.A, __fmul_rn(s.A, C.cdt));
+	s.B = __fsub_rn(s.B, __fmul_rn(s.B, C.cdt));
+}
+
+__device__ __forceinline__ void syn_skip(ConnDev const& C, SynState& s, int64_t n) {
+	if (C.plastic == SPICE_SYNAPSE_COUNT) {
+		s.W = __fadd_rn(s.W, (float)n);
+		return;
+	}
+	double const f = __ldg(C.skip_tab + (n + 64));
+	s.A            = __double2float_rn(__dmul_rn((double)s.A, f));
+	s.B            = __double2float_rn(__dmul_rn((double)s.B, f));
+}
+
+// The catch-up of one edge to step `time` (synapse_population.h:88-116).  The reference computes
+// ~0 >> prefix with prefix up to 64 (pre set and time == age); x86-64 shifts by prefix mod 64, and
+// that is what is computed here.
+__device__ __forceinline__ void catch_up(ConnDev const& C, SynState& s, int64_t time, uint64_t ages, uint64_t hist) {
+	int const pre     = (int)(ages >> 63);
+	int64_t const age = (int64_t)(ages & ~(1ull << 63));
+	if (!(time >= age)) return;
+	int64_t const prefix = 63 + pre - time + age;
+	uint64_t const mask  = ~0ull >> (prefix & 63);
+	if (pre) syn_update(C, s, true, (hist & (1ull << ((time - age) & 63))) != 0);
+	hist &= mask;
+	int64_t p = prefix;
+	while (hist) {
+		int const lz = __clzll((long long)hist);
+		syn_skip(C, s, lz - p);
+		syn_update(C, s, false, true);
+		hist ^= 1ull << (63 - lz);
+		p = lz + 1;
+	}
+	syn_skip(C, s, 64 - p);
+}
+
+// Every 64 steps (snn.cpp:17-19): every synapse of the connection catches up; a warp per source.
+__global__ void __launch_bounds__(256) k_plastic_update_all(const __grid_constant__ ConnDev C, int64_t time) {
+	int const lane = threadIdx.x & 31;
+	int64_t const src = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+	if (src >= C.src_size) return;
+	uint64_t const ages = C.ages[src];
+	for (int64_t e = C.off[src] + lane; e < C.off[src + 1]; e += 32) {
+		SynState st{C.sW[e], C.sA[e], C.sB[e]};
+		catch_up(C, st, time, ages, C.dst_hist[C.nb[e]]);
+		C.sW[e] = st.W;
+		C.sA[e] = st.A;
+		C.sB[e] = st.B;
+	}
+	__syncwarp();
+	if (lane == 0) C.ages[src] = (uint64_t)(time + 1);
+}
+
+// Delivery of the spikes of step time - delay + 1 through a plastic connection (synapse_population
+// .h:82-140): a warp per word of the source's spike bitmap, each spiking source's row lane-parallel:
+// catch up, then deliver W into input ring slot `slot` (atomic-mode sums; COUNT with scale 0 and
+// any model in deterministic mode deliver nothing).
+__global__ void __launch_bounds__(256) k_plastic_deliver(const __grid_constant__ ConnDev C, int64_t time, int hslot,
+                                                          int64_t slot, int deliver, unsigned long long* events) {
+	int const lane = threadIdx.x & 31;
+	int const w    = blockIdx.x * 8 + (threadIdx.x >> 5);
+	if (w >= C.src_nwords) return;
+	uint32_t bits = C.src_bits[(int64_t)hslot * C.src_nwords + w];
+	unsigned long long ev = 0;
+	while (bits) {
+		int const r       = __ffs(bits) - 1;
+		bits &= bits - 1;
+		int64_t const src = 32 * (int64_t)w + r;
+		uint64_t const ages = C.ages[src];
+		int64_t const e0 = C.off[src], e1 = C.off[src + 1];
+		ev += (unsigned long long)(e1 - e0);
+		for (int64_t e = e0 + lane; e < e1; e += 32) {
+			SynState st{C.sW[e], C.sA[e], C.sB[e]};
+			int32_t const j = C.nb[e];
+			catch_up(C, st, time, ages, C.dst_hist[j]);
+			C.sW[e] = st.W;
+			C.sA[e] = st.A;
+			C.sB[e] = st.B;
+			if (deliver) {
+				float const v = C.plastic == SPICE_SYNAPSE_COUNT ? __fmul_rn(C.weight, st.W) : st.W;
+				red_add_f32(C.dst_acc + (slot * C.dst_size + j) * C.F + C.fslot, v);
+			}
+		}
+		__syncwarp();
+		if (lane == 0) C.ages[src] = (uint64_t)(time + 1) | (1ull << 63);
+	}
+	if (lane == 0 && ev) atomicAdd(events, ev);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Batched networks: the populations and connections of many independent nets (same dt, delay
 // ring, window and time) are concatenated and one launch per kernel kind steps all of them.  The
 // window's time-dependent values live in a device clock that k_batch_prologue advances, so every
@@ -1035,8 +1160,8 @@ __global__ void __launch_bounds__(kThreads) k_batch_neurons(const __grid_constan
 	int const p        = find_segment(b.nblk_begin, b.npop, x);
 	int const lb       = x - __ldg(b.nblk_begin + p);
 	WinCtx const w     = batch_win_ctx(b, c);
-	if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true>(w, b.pops + p, p, lb);
-	else if (!ONLY_FAST) window_neurons<MODE, false>(w, b.pops + p, p, lb);
+	if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
+	else if (!ONLY_FAST) window_neurons<MODE, false, false>(w, b.pops + p, p, lb);
 }
 
 // Delivery of all nets: grid (target tiles x parts, input slots of the window).
@@ -1112,7 +1237,7 @@ cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t n
 cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks) {
 	if (nblocks <= 0) return cudaSuccess;
 	bool only_fast = true;
-	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0;
+	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
 	if (a.mode == 0) {
 		if (only_fast) k_neurons<0, true><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, false><<<nblocks, kThreads, 0, stream>>>(a);
@@ -1241,6 +1366,20 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 6: k_batch_deliver<0, 3><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 7: k_batch_deliver<1, 3><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_plastic_update_all(cudaStream_t stream, ConnDev const& c, int64_t time) {
+	if (c.src_size <= 0) return cudaSuccess;
+	k_plastic_update_all<<<(unsigned)((c.src_size + 7) / 8), 256, 0, stream>>>(c, time);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_plastic_deliver(cudaStream_t stream, ConnDev const& c, int64_t time, int hslot, int64_t slot,
+                                   bool deliver, unsigned long long* events) {
+	if (c.src_nwords <= 0) return cudaSuccess;
+	k_plastic_deliver<<<(unsigned)((c.src_nwords + 7) / 8), 256, 0, stream>>>(c, time, hslot, slot, deliver ? 1 : 0,
+	                                                                        events);
 	return cudaGetLastError();
 }
 

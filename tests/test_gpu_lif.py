@@ -16,7 +16,7 @@ def _rel(g, ref):
 
 
 def _setup(B, T, seed=1, ck=20):
-    from spice2_gb300.lif import RecurrentLIF, poisson_input
+    from spice2_gb300.lif_layer import RecurrentLIF, poisson_input
     layer = RecurrentLIF(seed=seed, checkpoint_every=ck)
     x_bits, x = poisson_input(B, T, 700, seed=seed + 10, return_dense=True)
     g = torch.Generator(device="cuda").manual_seed(seed + 20)
@@ -113,7 +113,7 @@ def test_checkpointing_is_exact(engine):
 
 def test_full_config_matches_fp64(engine):
     """Batch 64, 700 -> 1024, 200 steps, checkpoint every 20, MSE on the first 128 counts."""
-    from spice2_gb300.lif import count_loss, count_targets
+    from spice2_gb300.lif_layer import count_loss, count_targets
     layer, x_bits, x, _ = _setup(64, 200, seed=11)
     target = count_targets(64)
     layer.zero_grad()
@@ -130,7 +130,7 @@ def test_full_config_matches_fp64(engine):
 
 
 def test_training_lowers_the_loss(engine):
-    from spice2_gb300.lif import count_loss, count_targets
+    from spice2_gb300.lif_layer import count_loss, count_targets
     layer, x_bits, x, _ = _setup(16, 100, seed=13)
     target = count_targets(16, seed=4)
     opt = torch.optim.Adam([layer.w_in, layer.w_rec, layer.theta], lr=3e-3)

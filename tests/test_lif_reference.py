@@ -53,7 +53,7 @@ def test_dense_reference_spiking_forward_resets_by_subtraction():
 
 
 def test_pack_bits_layout():
-    from spice2_gb300.lif import pack_bits
+    from spice2_gb300.lif_layer import pack_bits
     g = torch.Generator().manual_seed(1)
     x = torch.rand(2, 3, 70, generator=g) < 0.5
     w = pack_bits(x).numpy().astype(np.uint32)
