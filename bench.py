@@ -51,7 +51,9 @@ WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
 # runs on a smaller network than the bench so that the ncu replay stays small; the traffic per
 # event does not depend on the network size as long as the rows do not fit in L2).
 DELIVER_DRAM_BYTES_PER_EVENT = (22.117120e6 + 1.792e3) / 4235947
-DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>"}
+DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
+                   4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
+                   7: "k_deliver_groups_occ"}
 
 
 def _dist():
@@ -408,6 +410,8 @@ def main():
     ap.add_argument("--batched-nets", type=int, default=256,
                     help="networks of the batched Brunel sweep (0 skips it)")
     ap.add_argument("--batched-steps", type=int, default=1000)
+    ap.add_argument("--headline-only", action="store_true",
+                    help="skip the batched, adjoint and plastic sections (faster iterations)")
     args = ap.parse_args()
     if args.impl == "reference":
         return reference_arm(args)
@@ -528,22 +532,22 @@ def main():
     batched = None
     import gc
     gc.collect()  # the N=5e5 nets (populations and nets reference each other)
-    if args.batched_nets > 0:
+    if args.batched_nets > 0 and not args.headline_only:
         try:
             batched = batched_sweep(args.batched_nets, args.batched_steps)
         except Exception as e:  # reported, never a reason to lose the headline line
             batched = {"error": str(e)}
 
-    adjoint = None
-    try:
-        adjoint = adjoint_bench()
-    except Exception as e:
-        adjoint = {"error": str(e)}
-    plastic = None
-    try:
-        plastic = plastic_bench()
-    except Exception as e:
-        plastic = {"error": str(e)}
+    adjoint = plastic = None
+    if not args.headline_only:
+        try:
+            adjoint = adjoint_bench()
+        except Exception as e:
+            adjoint = {"error": str(e)}
+        try:
+            plastic = plastic_bench()
+        except Exception as e:
+            plastic = {"error": str(e)}
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:

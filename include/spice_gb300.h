@@ -116,7 +116,10 @@ enum {
 	SPICE_TUNE_DELIVER_PARTS   = 2, /* CTAs sharing one (input slot, tile)                    */
 	SPICE_TUNE_DELIVER_ALGO    = 3, /* 0: warp-flattened sub-rows, 1: one thread per spike,
 	                                   2: one warp per spike, 8 sub-rows in flight,
-	                                   3: one thread per spike with 16-byte loads           */
+	                                   3: one thread per spike with 16-byte loads,
+	                                   4: one thread per spike, software-pipelined,
+	                                   5, 6: 4 or 8 lanes per spike, software-pipelined,
+	                                   7: as 5 with <= 32 registers (4 x 512 threads per SM) */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 };

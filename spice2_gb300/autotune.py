@@ -19,10 +19,17 @@ import sys
 
 DEFAULT_CANDIDATES = [
     # (tile bytes, threads per CTA, parts per (slot, tile), work mapping: 0 warp-flattened,
-    #  1 thread per spike, 2 warp per spike, 3 thread per spike with 16-byte loads)
+    #  1 thread per spike, 2 warp per spike, 3 thread per spike with 16-byte loads,
+    #  4 thread per spike, software-pipelined, 5 / 6 four / eight lanes per spike, 7 as 5 with
+    #  at most 32 registers)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
+    (24 * 1024, 256, 1, 4), (12 * 1024, 128, 1, 4), (12 * 1024, 256, 1, 4), (6 * 1024, 128, 1, 4),
+    (24 * 1024, 256, 1, 5), (12 * 1024, 128, 1, 5), (48 * 1024, 256, 1, 5), (24 * 1024, 256, 1, 6),
+    (48 * 1024, 256, 1, 6), (48 * 1024, 512, 1, 6), (96 * 1024, 512, 1, 6), (12 * 1024, 128, 1, 3),
+    (24 * 1024, 512, 1, 7), (26 * 1024, 512, 1, 7), (28 * 1024, 512, 1, 7), (32 * 1024, 512, 1, 7),
+    (16 * 1024, 256, 1, 7), (12 * 1024, 128, 1, 7),
 ]
 
 

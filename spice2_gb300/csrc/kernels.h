@@ -105,7 +105,9 @@ struct DeliverArgs {
 	int tile_begin[kMaxPops + 1];  // prefix over populations of their tile counts
 	int smem_bytes;
 	int parts;               // CTAs sharing one (slot, tile); > 1 flushes with reductions
-	int algo;                // 0: warp-flattened sub-rows, 1: one thread per spike, 2: warp per spike
+	int algo;                // 0: warp-flattened sub-rows, 1: one thread per spike, 2: warp per spike,
+	                         // 3: thread per spike with 16-byte loads, 4: thread per spike, pipelined,
+	                         // 5 / 6: 4 / 8 lanes per spike, pipelined
 	int list_k0;             // first list slot of this window's parity
 };
 // One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.

@@ -316,6 +316,80 @@ __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p,
 	}
 }
 
+// The Brunel LIF window (deterministic mode, every input group adds to V through a 16-bit counter
+// of word 0): the input words of 16 consecutive slots are loaded up front into registers and the
+// 16 step bodies are unrolled, so nothing is indexed dynamically (no local memory); dt comes from
+// shared memory.  Same arithmetic, in the same order, as window_neurons<0, true, false>.
+template <class A>
+__device__ __forceinline__ void window_lif_fast(A const& a, const PopDev* __restrict__ Pg, int p, int b,
+                                                const float* dts_sm) {
+	int const N      = (int)Pg->size;
+	int const i      = b * kThreads + threadIdx.x;
+	bool const valid = i < N;
+	int const lane   = threadIdx.x & 31;
+	int const word   = i >> 5;
+	int const nwords = Pg->nwords;
+	uint32_t* const cnt  = Pg->cnt;
+	bool const zero      = Pg->zero_inputs != 0;
+	float const vthres   = Pg->p0;
+	int32_t const tref   = (int32_t)Pg->p1;
+	float const tminv    = Pg->p2;
+	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
+	float V   = 0;
+	int32_t T = 0;
+	if (valid) {
+		V = Pg->V[i];
+		T = Pg->T[i];
+	}
+	int const D = (int)a.D, Hb = a.Hb, npop = a.npop;
+	int slot  = a.slot0;
+	int hslot = a.hslot0;
+	uint32_t* const bits = Pg->bits;
+	int32_t* const list  = Pg->list;
+	int32_t* const count = a.counts + p;
+	bool const wl = lane == 0 && word < nwords;
+	for (int k0 = 0; k0 < a.K; k0 += 16) {
+		int const nk = min(16, a.K - k0);
+		uint32_t x[16];
+		int sl = slot;
+#pragma unroll
+		for (int u = 0; u < 16; u++) {
+			x[u] = (valid && u < nk) ? cnt[(int64_t)sl * N + i] : 0u;
+			sl   = sl + 1 == D ? 0 : sl + 1;
+		}
+#pragma unroll
+		for (int u = 0; u < 16; u++) {
+			if (u < nk) {
+				int const k    = k0 + u;
+				bool spike     = false;
+				if (valid) {
+					uint32_t const xx = x[u];
+					if (xx) {
+						V = add_n(V, w0, xx & 0xffffu);
+						V = add_n(V, w1, xx >> 16);
+						if (zero) cnt[(int64_t)slot * N + i] = 0;
+					}
+					spike = lif_update(V, T, __fmaf_rn(-dts_sm[k], tminv, 1.0f), vthres, tref);
+				}
+				unsigned const mask = __ballot_sync(0xffffffffu, spike);
+				if (wl) bits[(int64_t)hslot * nwords + word] = mask;
+				if (mask) {
+					int base = 0;
+					if (lane == 0) base = atomicAdd(count + k * npop, __popc(mask));
+					base = __shfl_sync(0xffffffffu, base, 0);
+					if (spike) list[(int64_t)(a.list_k0 + k) * N + base + __popc(mask & lanemask_lt())] = i;
+				}
+				slot  = slot + 1 == D ? 0 : slot + 1;
+				hslot = hslot + 1 == Hb ? 0 : hslot + 1;
+			}
+		}
+	}
+	if (valid) {
+		Pg->V[i] = V;
+		Pg->T[i] = T;
+	}
+}
+
 // One step of a Poisson population (samples/brunel.cpp:27-30): thread c owns neurons
 // [32c, 32c + 32), jumps to draw draw_offset + 32c of the step's stream and draws 32 numbers.
 // The jump XORs the states T^i(s), i < 128, selected by the 128 bits of x^(offset) mod P; the step's
@@ -420,12 +494,16 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 // compiled out (fewer registers).
 template <int MODE, bool ONLY_FAST>
 __global__ void __launch_bounds__(kThreads) k_neurons(const __grid_constant__ WindowArgs a) {
+	__shared__ float dts_sm[kMaxWindow];
+	for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
+	__syncthreads();
 	int const b = blockIdx.x;
 	int p       = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
-	if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
+	if (MODE == 0 && kind == 3) window_lif_fast(a, a.pops + p, p, lb, dts_sm);
+	else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
 		if (kind == 0) window_neurons<MODE, false, false>(a, a.pops + p, p, lb);
 		else if (kind == 3 + kHistKind) window_neurons<MODE, true, true>(a, a.pops + p, p, lb);
@@ -664,6 +742,154 @@ __device__ __forceinline__ void deliver_tps(A const& a, PopDev const& P, int t, 
 	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
+// Software-pipelined thread-per-spike mapping: while a thread walks the sub-row of its current
+// spike (16 target loads in flight), the tile bounds of its next spike and the id of the one after
+// are already on their way, so the list -> bounds -> targets chain is exposed once per thread
+// instead of once per spike.
+template <int MODE, class A>
+__device__ __forceinline__ void deliver_tps_pipe(A const& a, PopDev const& P, int t, int si, int part) {
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
+	if (threadIdx.x == 0) ev_block = 0;
+	__syncthreads();
+	int64_t const sigma = a.slot_lo + si;
+	unsigned long long my_events = 0;
+	bool touched = false;
+	for (int ci = P.in_begin; ci < P.in_end; ci++) {
+		ConnDev const& C = a.conns[ci];
+		int64_t const k  = sigma - (a.t0 + C.delay - 1);
+		if (k < 0 || k >= a.K || C.plastic) continue;
+		touched = true;
+		int const n        = a.counts[k * a.npop + C.src];
+		const int32_t* lst = C.src_list + (a.list_k0 + k) * C.src_size;
+		const int64_t* bnd = C.bounds + t;
+		int const stride   = P.ntiles + 1;
+		const int32_t* nb  = C.nb;
+		int const word     = MODE == 0 ? C.word : C.fslot;
+		uint32_t const inc = C.inc;
+		float const w      = C.weight;
+		int const js       = a.parts * blockDim.x;
+		int j              = part * blockDim.x + threadIdx.x;
+		int s_next         = j + js < n ? __ldg(lst + j + js) : -1;
+		int64_t e0 = 0, e1 = 0;
+		if (j < n) {
+			const int64_t* bb = bnd + (int64_t)__ldg(lst + j) * stride;
+			e0                = __ldg(bb);
+			e1                = __ldg(bb + 1);
+		}
+		while (j < n) {
+			int64_t f0 = 0, f1 = 0;
+			if (s_next >= 0) {
+				const int64_t* bb = bnd + (int64_t)s_next * stride;
+				f0                = __ldg(bb);
+				f1                = __ldg(bb + 1);
+			}
+			int const j2 = j + 2 * js;
+			s_next       = j2 < n ? __ldg(lst + j2) : -1;
+			my_events += (unsigned long long)(e1 - e0);
+			for (int64_t e = e0; e < e1; e += 16) {
+				int32_t d[16];
+#pragma unroll
+				for (int u = 0; u < 16; u++) d[u] = e + u < e1 ? __ldg(nb + e + u) : -1;
+#pragma unroll
+				for (int u = 0; u < 16; u++)
+					if (d[u] >= 0) {
+						int const li = (d[u] - tbase) * width + word;
+						if (MODE == 0) atomicAdd(tile_sm + li, inc);
+						else atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+					}
+			}
+			e0 = f0;
+			e1 = f1;
+			j += js;
+		}
+	}
+	add_events(a.events, my_events, &ev_block);
+	if (!touched) return;
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
+// Lane-group mapping: G consecutive lanes share one spike and walk its sub-row G targets at a time
+// (U loads in flight per lane), so one warp load touches 32/G sub-rows -- about 32/G sectors --
+// instead of 32: the thread-per-spike mapping is bound by L1 sector lookups, one per event.  The
+// next spike's id and bounds are loaded while the current sub-row is processed.
+template <int MODE, int G, class A>
+__device__ __forceinline__ void deliver_groups(A const& a, PopDev const& P, int t, int si, int part) {
+	constexpr int U = 4;
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
+	if (threadIdx.x == 0) ev_block = 0;
+	__syncthreads();
+	int64_t const sigma = a.slot_lo + si;
+	int const gl = threadIdx.x & (G - 1);
+	int const gi = threadIdx.x / G;
+	int const ng = blockDim.x / G;
+	unsigned long long my_events = 0;
+	bool touched = false;
+	for (int ci = P.in_begin; ci < P.in_end; ci++) {
+		ConnDev const& C = a.conns[ci];
+		int64_t const k  = sigma - (a.t0 + C.delay - 1);
+		if (k < 0 || k >= a.K || C.plastic) continue;
+		touched = true;
+		int const n        = a.counts[k * a.npop + C.src];
+		const int32_t* lst = C.src_list + (a.list_k0 + k) * C.src_size;
+		const int64_t* bnd = C.bounds + t;
+		int const stride   = P.ntiles + 1;
+		const int32_t* nb  = C.nb;
+		int const word     = MODE == 0 ? C.word : C.fslot;
+		uint32_t const inc = C.inc;
+		float const w      = C.weight;
+		int const js       = a.parts * ng;
+		int j              = part * ng + gi;
+		int64_t e0 = 0, e1 = 0;
+		if (j < n) {
+			const int64_t* bb = bnd + (int64_t)__ldg(lst + j) * stride;
+			e0                = __ldg(bb);
+			e1                = __ldg(bb + 1);
+		}
+		int s_next = j + js < n ? __ldg(lst + j + js) : -1;
+		while (j < n) {
+			int64_t f0 = 0, f1 = 0;
+			if (s_next >= 0) {
+				const int64_t* bb = bnd + (int64_t)s_next * stride;
+				f0                = __ldg(bb);
+				f1                = __ldg(bb + 1);
+			}
+			int const j2 = j + 2 * js;
+			s_next       = j2 < n ? __ldg(lst + j2) : -1;
+			if (gl == 0) my_events += (unsigned long long)(e1 - e0);
+			for (int64_t e = e0 + gl; e < e1; e += G * U) {
+				int32_t d[U];
+#pragma unroll
+				for (int u = 0; u < U; u++) d[u] = e + u * G < e1 ? __ldg(nb + e + u * G) : -1;
+#pragma unroll
+				for (int u = 0; u < U; u++)
+					if (d[u] >= 0) {
+						int const li = (d[u] - tbase) * width + word;
+						if (MODE == 0) atomicAdd(tile_sm + li, inc);
+						else atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+					}
+			}
+			e0 = f0;
+			e1 = f1;
+			j += js;
+		}
+	}
+	add_events(a.events, my_events, &ev_block);
+	if (!touched) return;
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
 // Warp-per-spike mapping: a warp takes 32 spikes, loads their sub-row bounds lane-parallel, then
 // streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced loads, 8 in flight per
 // lane, no cross-lane search).
@@ -770,6 +996,26 @@ template <int MODE, bool VEC>
 __global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item(a);
 	deliver_tps<MODE, VEC>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+template <int MODE>
+__global__ void k_deliver_pipe(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_tps_pipe<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+template <int MODE, int G>
+__global__ void k_deliver_groups(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_groups<MODE, G>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+// The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
+// resident per SM, for windows whose (slot, tile) items fit one wave at that occupancy.
+template <int MODE>
+__global__ void __launch_bounds__(512, 4) k_deliver_groups_occ(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_groups<MODE, 4>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
 template <int MODE>
@@ -1160,7 +1406,11 @@ __global__ void __launch_bounds__(kThreads) k_batch_neurons(const __grid_constan
 	int const p        = find_segment(b.nblk_begin, b.npop, x);
 	int const lb       = x - __ldg(b.nblk_begin + p);
 	WinCtx const w     = batch_win_ctx(b, c);
-	if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
+	__shared__ float dts_sm[kMaxWindow];
+	for (int k = threadIdx.x; k < w.K; k += blockDim.x) dts_sm[k] = b.dts[k];
+	__syncthreads();
+	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_fast(w, b.pops + p, p, lb, dts_sm);
+	else if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
 	else if (!ONLY_FAST) window_neurons<MODE, false, false>(w, b.pops + p, p, lb);
 }
 
@@ -1187,7 +1437,10 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	if (ALGO == 0) deliver_flat<MODE>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 1) deliver_tps<MODE, false>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 2) deliver_wps<MODE>(a, P, t, (int)blockIdx.y, part);
-	else deliver_tps<MODE, true>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 3) deliver_tps<MODE, true>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 4) deliver_tps_pipe<MODE>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 5 || ALGO == 7) deliver_groups<MODE, 4>(a, P, t, (int)blockIdx.y, part);
+	else deliver_groups<MODE, 8>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -1260,12 +1513,16 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		if (a.counts_next_len > 0) return cudaMemsetAsync(a.counts_next, 0, sizeof(int32_t) * a.counts_next_len, stream);
 		return cudaSuccess;
 	}
-	static int configured[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	static int configured[16] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
 	int const m = (a.mode == 0 ? 0 : 1) + 2 * a.algo;
-	void const* fns[8] = {(void const*)k_deliver<0>,            (void const*)k_deliver<1>,
-	                      (void const*)k_deliver_tps<0, false>, (void const*)k_deliver_tps<1, false>,
-	                      (void const*)k_deliver_wps<0>,        (void const*)k_deliver_wps<1>,
-	                      (void const*)k_deliver_tps<0, true>,  (void const*)k_deliver_tps<1, true>};
+	void const* fns[16] = {(void const*)k_deliver<0>,            (void const*)k_deliver<1>,
+	                       (void const*)k_deliver_tps<0, false>, (void const*)k_deliver_tps<1, false>,
+	                       (void const*)k_deliver_wps<0>,        (void const*)k_deliver_wps<1>,
+	                       (void const*)k_deliver_tps<0, true>,  (void const*)k_deliver_tps<1, true>,
+	                       (void const*)k_deliver_pipe<0>,       (void const*)k_deliver_pipe<1>,
+	                       (void const*)k_deliver_groups<0, 4>,  (void const*)k_deliver_groups<1, 4>,
+	                       (void const*)k_deliver_groups<0, 8>,  (void const*)k_deliver_groups<1, 8>,
+	                       (void const*)k_deliver_groups_occ<0>, (void const*)k_deliver_groups_occ<1>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -1284,6 +1541,14 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		case 5: k_deliver_wps<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 6: k_deliver_tps<0, true><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 7: k_deliver_tps<1, true><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 8: k_deliver_pipe<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 9: k_deliver_pipe<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 10: k_deliver_groups<0, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 11: k_deliver_groups<1, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 12: k_deliver_groups<0, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 13: k_deliver_groups<1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 14: k_deliver_groups_occ<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 15: k_deliver_groups_occ<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 	}
 	return cudaGetLastError();
 }
@@ -1337,11 +1602,15 @@ cudaError_t launch_batch_neurons(cudaStream_t stream, BatchArgs const& b) {
 namespace {
 void const* batch_deliver_fn(BatchArgs const& b) {
 	int const m = (b.mode == 0 ? 0 : 1) + 2 * b.algo;
-	void const* fns[8] = {(void const*)k_batch_deliver<0, 0>, (void const*)k_batch_deliver<1, 0>,
-	                      (void const*)k_batch_deliver<0, 1>, (void const*)k_batch_deliver<1, 1>,
-	                      (void const*)k_batch_deliver<0, 2>, (void const*)k_batch_deliver<1, 2>,
-	                      (void const*)k_batch_deliver<0, 3>, (void const*)k_batch_deliver<1, 3>};
-	return fns[m & 7];
+	void const* fns[16] = {(void const*)k_batch_deliver<0, 0>, (void const*)k_batch_deliver<1, 0>,
+	                       (void const*)k_batch_deliver<0, 1>, (void const*)k_batch_deliver<1, 1>,
+	                       (void const*)k_batch_deliver<0, 2>, (void const*)k_batch_deliver<1, 2>,
+	                       (void const*)k_batch_deliver<0, 3>, (void const*)k_batch_deliver<1, 3>,
+	                       (void const*)k_batch_deliver<0, 4>, (void const*)k_batch_deliver<1, 4>,
+	                       (void const*)k_batch_deliver<0, 5>, (void const*)k_batch_deliver<1, 5>,
+	                       (void const*)k_batch_deliver<0, 6>, (void const*)k_batch_deliver<1, 6>,
+	                       (void const*)k_batch_deliver<0, 7>, (void const*)k_batch_deliver<1, 7>};
+	return fns[m < 16 ? m : 0];
 }
 }  // namespace
 
@@ -1365,6 +1634,14 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 5: k_batch_deliver<1, 2><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 6: k_batch_deliver<0, 3><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 7: k_batch_deliver<1, 3><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 8: k_batch_deliver<0, 4><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 9: k_batch_deliver<1, 4><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 10: k_batch_deliver<0, 5><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 11: k_batch_deliver<1, 5><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 12: k_batch_deliver<0, 6><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 13: k_batch_deliver<1, 6><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 14: k_batch_deliver<0, 7><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 15: k_batch_deliver<1, 7><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
 	return cudaGetLastError();
 }

@@ -44,6 +44,9 @@ def brunel(args):
     import spice2_gb300 as sp
     N, p = args.N, args.p
     net, (P, E, I) = sp.brunel(N, p, args.seed, mode=args.mode)
+    if args.tuning:
+        tb, th, parts, algo = (int(x) for x in args.tuning.split(","))
+        net.set_tuning(tile_bytes=tb, deliver_threads=th, deliver_parts=parts, deliver_algo=algo)
     t = time.perf_counter()
     if args.json:
         raster = net.run_record(args.steps)
@@ -107,6 +110,8 @@ def main(argv=None) -> int:
     b.add_argument("--json", action="store_true")
     b.add_argument("--window-events", action="store_true",
                    help="run window by window and print the synaptic events of each (profiling aid)")
+    b.add_argument("--tuning", default="", metavar="TILE_BYTES,THREADS,PARTS,ALGO",
+                   help="delivery launch shape (results do not depend on it)")
     v = sub.add_parser("vogels")
     v.add_argument("--N", type=int, default=4000)
     v.add_argument("--seed", type=int, default=1337)

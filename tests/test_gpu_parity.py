@@ -308,6 +308,25 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
                 assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
+@pytest.mark.parametrize("algo,tile_bytes,threads,parts", [
+    (0, 24 * 1024, 256, 1), (1, 12 * 1024, 128, 1), (2, 24 * 1024, 256, 1), (3, 48 * 1024, 512, 1),
+    (4, 24 * 1024, 256, 1), (4, 6 * 1024, 128, 2), (4, 96 * 1024, 1024, 1), (2, 4096, 64, 3), (0, 8192, 512, 2),
+    (5, 24 * 1024, 256, 1), (5, 4096, 64, 2), (6, 48 * 1024, 512, 1), (6, 200 * 1024, 1024, 3),
+    (7, 26 * 1024, 512, 1), (7, 8192, 1024, 2),
+])
+def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
+    """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
+    16-byte loads, software-pipelined) gives the reference's raster and V bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    net.set_tuning(tile_bytes=tile_bytes, deliver_threads=threads, deliver_parts=parts, deliver_algo=algo)
+    counts, idx = _raster_flat(net.run_record(steps))
+    assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
 def test_retuning_mid_run_keeps_results(engine):
     """Switching tile size, threads and parts between steps (including between overwritten and
     accumulated input slots) leaves the raster and state bit-exact."""
