@@ -200,6 +200,60 @@ int spice_get_stream(spice_net* net, void** stream_out);
 int spice_synchronize(spice_net* net);
 const char* spice_last_error(void);
 
+/* ---- User-defined neuron models (the reference's Neuron concepts, concepts.h:10-58) ----
+ * The engine keeps the population's state (an array of the user's neuron struct, or nothing for a
+ * stateless model), its spike bitmap ring and lists, and delivers synapses into float members of
+ * the struct registered as fields; the update is user code: a kernel compiled in the user's nvcc
+ * translation unit (include/spice/snn.h instantiates it over the model type) and launched by the
+ * callback below on the engine's stream, once per window, with everything it reads and writes
+ * described by spice_user_window.
+ * Stateful models: per step k of the window, apply the inputs of input-ring slot (slot0 + k) mod D
+ * (deterministic: per-group counts replayed as sequential float adds of group_weight into the
+ * group's field; atomic: the field sums), clear them when zero_inputs, then update; apply_only = 1
+ * (K = 0) asks for the inputs of slot0 to be applied and cleared with no update (state reads).
+ * Stateless models draw from the step's random stream: neuron i's stream position is
+ * draw_offset + i (one draw per neuron and step, as the reference's sequential loop gives a model
+ * that draws once), reached through the step's jump table (tables[k]) and the chunk polynomials
+ * chunk_poly[c] = x^(draw_offset + 32 c) mod P (32 neurons per chunk).
+ * Spikes: bitmap word (hslot0 + k) mod Hb, bit i; and the unordered list of step k,
+ * list[(list_k0 + k) * size ...], reserved with atomicAdd on counts[k * npop + pop]. */
+#define SPICE_USER_ABI_VERSION 1
+typedef struct spice_user_window {
+	int version;
+	int apply_only;
+	int64_t t0;
+	int K, slot0, hslot0, Hb, list_k0, npop, pop, mode;
+	int64_t D;
+	const float* dts;          /* [K] */
+	const void* tables;        /* [K][16][256] 16-byte jump table entries (stateless) */
+	const void* chunk_poly;    /* [nwords] 16-byte polynomials (stateless) */
+	int64_t draw_offset;
+	void* state;               /* [size] user neuron structs (stateful) */
+	int64_t size;
+	int neuron_bytes, nwords;
+	uint32_t* bits;
+	int32_t* list;
+	int32_t* counts;
+	uint32_t* cnt;             /* deterministic input ring [D][size][W] */
+	float* acc;                /* atomic input ring [D][size][F] */
+	int W, F, ngroups, zero_inputs;
+	int group_word[4], group_shift[4], group_bits[4], group_field[4];
+	float group_weight[4];
+	int field_offset[3];       /* byte offset of field f in the neuron struct */
+	int field_slot[3];         /* atomic mode: index of field f among the F sums (-1: none) */
+} spice_user_window;
+typedef int (*spice_user_update_fn)(const spice_user_window* window, void* stream, void* ctx);
+/* stateful: neuron_bytes > 0 and init_neuron = the initial struct (copied to every neuron); the
+ * population consumes a seed like every stateful population (neuron_population.h:56-60). */
+int spice_add_user_population(spice_net* net, int64_t size, int stateful, int neuron_bytes,
+                              const void* init_neuron, spice_user_update_fn fn, void* ctx, int* pop_out);
+/* Registers a float member (byte offset) of a stateful user population as a synapse target field;
+ * returns its field index (0..2; the same offset gives the same index). */
+int spice_user_field(spice_net* net, int pop, int byte_offset, int* field_out);
+/* The whole state array of a stateful user population (size * neuron_bytes bytes). */
+int spice_get_user_state(spice_net* net, int pop, void* host_out);
+int spice_set_user_state(spice_net* net, int pop, const void* host_in);
+
 /* ---- Batched networks (no counterpart in the reference) ----
  * Many independent nets stepped together: one launch per kernel kind and window covers the
  * populations and connections of every member, so networks far too small to fill the GPU alone

@@ -102,6 +102,10 @@ def _load():
         "spice_batch_kernel_stats": [vp, i32, P(i64), P(f64)],
         "spice_batch_launch_count": [vp, P(i64)],
         "spice_batch_get_stream": [vp, P(vp)],
+        "spice_add_user_population": [vp, i64, i32, i32, vp, vp, vp, P(i32)],
+        "spice_user_field": [vp, i32, i32, P(i32)],
+        "spice_get_user_state": [vp, i32, vp],
+        "spice_set_user_state": [vp, i32, vp],
         "spice_lif_layer_create": [i32, i32, vp, vp, vp, vp, P(vp)],
         "spice_lif_layer_destroy": [vp],
         "spice_lif_layer_synapses": [vp, P(i64), P(i64)],

@@ -323,7 +323,8 @@ extern "C" int spice_batch_create(spice_net* const* nets, int nnets, spice_batch
 		if (n->max_delay != n0->max_delay) return bfail(SPICE_EINVAL, "batched nets must have the same max_delay");
 		if (n->mode != n0->mode) return bfail(SPICE_EINVAL, "batched nets must use the same mode");
 		for (auto const& p : n->pops)
-			if (p.d.model == EXTERNAL) return bfail(SPICE_EINVAL, "batched nets cannot have external_input populations");
+			if (p.d.model == EXTERNAL || p.d.model == USER)
+				return bfail(SPICE_EINVAL, "batched nets cannot have external_input or user-defined populations");
 		for (auto const& c : n->conns)
 			if (c.d.plastic) return bfail(SPICE_EINVAL, "batched nets cannot have plastic connections");
 	}

@@ -28,7 +28,7 @@ constexpr int kBasis      = 128; // states per step basis
 constexpr int kJumpTable  = 16 * 256;  // u128 entries of one step's jump table
 constexpr int kPoissonChunk = 32; // consecutive Poisson neurons per thread (one jump each)
 
-enum Model { POISSON = 0, LIF = 1, LIF_COND = 2, EXTERNAL = 3 };
+enum Model { POISSON = 0, LIF = 1, LIF_COND = 2, EXTERNAL = 3, USER = 4 };
 
 struct Group {
 	int field;     // 0 V, 1 Gex, 2 Gin
@@ -69,6 +69,8 @@ struct PopDev {
 	const u128* chunk_poly;  // POISSON: x^(draw_offset + 32 c) mod P for chunk c
 	int net;             // index of the owning net in a batch (0 outside batches)
 	uint64_t* hist;      // targets of plastic connections: post-spike history, bit k = spiked k steps ago
+	void* ustate;        // USER: [size] neuron structs of the user's model
+	int ubytes;          // USER: bytes per neuron struct (0: stateless)
 	// EXTERNAL: cyclic train
 	const int32_t* ext_counts;
 	const int64_t* ext_off;
@@ -112,6 +114,11 @@ struct Pop {
 	std::vector<int32_t> ext_counts_h;
 	std::vector<int64_t> ext_off_h;
 	bool stateful = false;
+	// USER: the update callback and the struct offsets of the fields synapses target
+	void* ufn  = nullptr;  // spice_user_update_fn
+	void* uctx = nullptr;
+	int nfields = 0;
+	int field_offset[3] = {0, 0, 0};
 };
 
 struct Conn {

@@ -243,6 +243,62 @@ extern "C" int spice_add_population(spice_net* n, int model, int64_t size, const
 	return SPICE_OK;
 }
 
+extern "C" int spice_add_user_population(spice_net* n, int64_t size, int stateful, int neuron_bytes,
+                                         const void* init_neuron, spice_user_update_fn fn, void* ctx, int* pop_out) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (n->prepared) return fail(SPICE_ESTATE, "populations must be added before the network first steps");
+	if (!fn) return fail(SPICE_EINVAL, "a user population needs an update function");
+	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
+	if (size >= INT32_MAX) return pre_failed("topology.cpp:51", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
+	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
+	if (stateful && (neuron_bytes <= 0 || neuron_bytes % 4 || !init_neuron))
+		return fail(SPICE_EINVAL, "a stateful user model needs its neuron struct size (a multiple of 4) and initial value");
+	Pop p{};
+	PopDev& d = p.d;
+	memset(&d, 0, sizeof d);
+	d.model  = USER;
+	d.size   = size;
+	d.nwords = (int)((size + 31) / 32);
+	for (int f = 0; f < 3; f++) d.field_slot[f] = -1;
+	p.stateful = stateful != 0;
+	p.ufn      = (void*)fn;
+	p.uctx     = ctx;
+	if (p.stateful) {
+		seed_next(n);  // stateful_neuron_adapter: rng(seed++) (neuron_population.h:56-60)
+		d.ubytes = neuron_bytes;
+		char* st = nullptr;
+		TRY(dalloc(n, &st, (size_t)std::max<int64_t>(size, 1) * neuron_bytes, false));
+		std::vector<char> h((size_t)std::max<int64_t>(size, 1) * neuron_bytes);
+		for (int64_t i = 0; i < std::max<int64_t>(size, 1); i++)
+			memcpy(h.data() + i * neuron_bytes, init_neuron, (size_t)neuron_bytes);
+		CUDA_TRY(cudaMemcpy(st, h.data(), h.size(), cudaMemcpyHostToDevice));
+		d.ustate = st;
+	}
+	n->pops.push_back(std::move(p));
+	n->ext_t_set.push_back(0);
+	if (pop_out) *pop_out = (int)n->pops.size() - 1;
+	return SPICE_OK;
+}
+
+extern "C" int spice_user_field(spice_net* n, int pop, int byte_offset, int* field_out) {
+	if (!n || !field_out) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop < 0 || pop >= (int)n->pops.size() || n->pops[pop].d.model != USER || !n->pops[pop].stateful)
+		return fail(SPICE_EINVAL, "not a stateful user population");
+	Pop& P = n->pops[pop];
+	if (byte_offset < 0 || byte_offset % 4 || byte_offset + 4 > P.d.ubytes)
+		return fail(SPICE_EINVAL, "a field must be a float member of the neuron struct");
+	for (int f = 0; f < P.nfields; f++)
+		if (P.field_offset[f] == byte_offset) {
+			*field_out = f;
+			return SPICE_OK;
+		}
+	if (n->prepared) return fail(SPICE_ESTATE, "fields must be registered before the network first steps");
+	if (P.nfields >= 3) return fail(SPICE_EINVAL, "at most 3 fields of a user neuron can be synapse targets");
+	P.field_offset[P.nfields] = byte_offset;
+	*field_out                = P.nfields++;
+	return SPICE_OK;
+}
+
 namespace {
 int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int np, Conn& c) {
 	float* w   = &c.d.weight;
@@ -266,7 +322,7 @@ int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int n
 	*w          = params[0];
 	*field      = np > 1 ? (int)params[1] : 0;
 	int const m = n->pops[dst].d.model;
-	if (*field < 0 || *field > 2 || (m == LIF && *field != 0))
+	if (m == USER ? (*field < 0 || *field >= n->pops[dst].nfields) : (*field < 0 || *field > 2 || (m == LIF && *field != 0)))
 		return fail(SPICE_EINVAL, "the synapse's target field does not exist in the target neuron model");
 	return SPICE_OK;
 }
@@ -526,14 +582,14 @@ int prepare(spice_net* n) {
 	int64_t draws = 0;
 	for (auto& p : n->pops) {
 		p.d.draw_offset = draws;
-		if (p.d.model == POISSON) draws += p.d.size;
+		if (p.d.model == POISSON || (p.d.model == USER && !p.stateful)) draws += p.d.size;
 	}
 	n->total_draws = draws;
 	for (auto& p : n->pops) {
 		PopDev& d = p.d;
 		TRY(dalloc(n, &d.bits, (size_t)n->Hb * std::max(d.nwords, 1)));
 		TRY(dalloc(n, &d.list, (size_t)2 * n->K * std::max<int64_t>(d.size, 1), false));
-		if (d.model == POISSON && d.nwords > 0) {
+		if ((d.model == POISSON || (d.model == USER && !p.stateful)) && d.nwords > 0) {
 			std::vector<u128> polys(d.nwords);
 			u128 const step = gf2_xpow(kPoissonChunk);
 			polys[0]        = gf2_xpow((uint64_t)d.draw_offset);
@@ -691,7 +747,8 @@ int prepare(spice_net* n) {
 	for (auto& p : n->pops) maxN = std::max(maxN, p.d.size);
 	TRY(dalloc(n, &n->d_tmp, maxN, false));
 	TRY(dalloc(n, &n->d_tmp_n, 1));
-	for (auto& p : n->pops) n->has_sources |= p.d.model == POISSON || p.d.model == EXTERNAL;
+	for (auto& p : n->pops)
+		n->has_sources |= p.d.model == POISSON || p.d.model == EXTERNAL || (p.d.model == USER && !p.stateful);
 	CUDA_TRY(cudaStreamCreateWithFlags(&n->stream_src, cudaStreamNonBlocking));
 	CUDA_TRY(cudaEventCreateWithFlags(&n->ev_tab, cudaEventDisableTiming));
 	for (int q = 0; q < 2; q++) {
@@ -701,6 +758,69 @@ int prepare(spice_net* n) {
 	}
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
 	n->prepared = true;
+	return SPICE_OK;
+}
+
+// The window of a user population, as its update kernel sees it (spice_user_window).
+spice_user_window user_window(spice_net* n, int pi, WindowArgs const& wa, int64_t j, bool apply_only) {
+	Pop const& P    = n->pops[pi];
+	PopDev const& d = P.d;
+	spice_user_window w;
+	memset(&w, 0, sizeof w);
+	w.version    = SPICE_USER_ABI_VERSION;
+	w.apply_only = apply_only ? 1 : 0;
+	w.t0         = wa.t0;
+	w.K          = apply_only ? 0 : wa.K;
+	w.slot0      = wa.slot0;
+	w.hslot0     = wa.hslot0;
+	w.Hb         = wa.Hb;
+	w.list_k0    = wa.list_k0;
+	w.npop       = wa.npop;
+	w.pop        = pi;
+	w.mode       = n->mode;
+	w.D          = wa.D;
+	w.dts        = wa.dts;
+	w.tables     = n->d_tables ? (const void*)(n->d_tables + j * kJumpTable) : nullptr;
+	w.chunk_poly = d.chunk_poly;
+	w.draw_offset = d.draw_offset;
+	w.state      = d.ustate;
+	w.size       = d.size;
+	w.neuron_bytes = d.ubytes;
+	w.nwords     = d.nwords;
+	w.bits       = d.bits;
+	w.list       = d.list;
+	w.counts     = wa.counts;
+	w.cnt        = d.cnt;
+	w.acc        = d.acc;
+	w.W          = d.W;
+	w.F          = d.F;
+	w.ngroups    = d.ngroups;
+	w.zero_inputs = d.zero_inputs;
+	for (int g = 0; g < kMaxGroups; g++) {
+		w.group_word[g]   = d.group_word[g];
+		w.group_shift[g]  = d.group_shift[g];
+		w.group_bits[g]   = d.group_bits[g];
+		w.group_field[g]  = d.group_field[g];
+		w.group_weight[g] = d.group_weight[g];
+	}
+	for (int f = 0; f < 3; f++) {
+		w.field_offset[f] = P.field_offset[f];
+		w.field_slot[f]   = d.field_slot[f];
+	}
+	return w;
+}
+
+// Calls the update callbacks of the stateful (or stateless) user populations on `st`.
+int launch_user_pops(spice_net* n, WindowArgs const& wa, int64_t j, bool stateful, bool apply_only, cudaStream_t st) {
+	for (int pi = 0; pi < (int)n->pops.size(); pi++) {
+		Pop const& P = n->pops[pi];
+		if (P.d.model != USER || P.stateful != stateful || P.d.size == 0) continue;
+		spice_user_window const w = user_window(n, pi, wa, j, apply_only);
+		int const r = reinterpret_cast<spice_user_update_fn>(P.ufn)(&w, (void*)st, P.uctx);
+		if (r != 0) return fail(SPICE_ECUDA, "the update function of user population " + std::to_string(pi) +
+		                                          " failed (" + std::to_string(r) + ")");
+		n->launches++;
+	}
 	return SPICE_OK;
 }
 
@@ -756,6 +876,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					ws.blk_per_step[p] = (P.nwords + 255) / 256;
 					nbs += ws.blk_per_step[p] * k;
 					wa.blk_kind[p] = 1;
+				} else if (P.model == USER) {
+					ws.blk_kind[p] = 0;  // launched by the user's callback
+					wa.blk_kind[p] = 0;
 				} else if (P.model == EXTERNAL) {
 					ws.blk_kind[p]     = 2;
 					ws.blk_per_step[p] = 1;
@@ -773,17 +896,25 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			ws.blk_begin[np] = nbs;
 			int slot = -1;
 			cudaStream_t const ss = n->overlap_sources ? n->stream_src : n->stream;
-			if (nbs > 0) {
+			bool user_src = false, user_st = false;
+			for (auto const& P : n->pops)
+				if (P.d.model == USER) (P.stateful ? user_st : user_src) = true;
+			bool const any_src = nbs > 0 || user_src;
+			if (any_src) {
 				// sources of this window may start once the lists of this parity are free
 				CUDA_TRY(cudaStreamWaitEvent(ss, n->ev_free[q], 0));
 				TRY(ev_begin(n, 3, &slot, ss));
-				CUDA_TRY(launch_sources(ss, ws, nbs));
+				if (nbs > 0) {
+					CUDA_TRY(launch_sources(ss, ws, nbs));
+					n->launches++;
+				}
+				if (user_src) TRY(launch_user_pops(n, wa, j, false, false, ss));
 				TRY(ev_end(n, slot, ss));
 				CUDA_TRY(cudaEventRecord(n->ev_src[q], ss));
-				n->launches++;
 			}
 			TRY(ev_begin(n, 0, &slot));
 			CUDA_TRY(launch_neurons(n->stream, wa, nb));
+			if (user_st) TRY(launch_user_pops(n, wa, j, true, false, n->stream));
 			TRY(ev_end(n, slot));
 			if (nb > 0) n->launches++;
 			if (n->plastic && n->time % 64 == 0)  // snn.cpp:17-19 (windows are one step long)
@@ -792,7 +923,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 						CUDA_TRY(launch_plastic_update_all(n->stream, c.d, n->time));
 						n->launches++;
 					}
-			if (nbs > 0) CUDA_TRY(cudaStreamWaitEvent(n->stream, n->ev_src[q], 0));
+			if (any_src) CUDA_TRY(cudaStreamWaitEvent(n->stream, n->ev_src[q], 0));
 			DeliverArgs da{};
 			da.t0     = n->time;
 			da.K      = k;
@@ -872,13 +1003,27 @@ int flush_pending(spice_net* n) {
 	if (!n->prepared || n->time == 0) return SPICE_OK;
 	std::vector<int> st;
 	std::vector<PopDev> hp;
+	bool user = false;
 	for (int i = 0; i < (int)n->pops.size(); i++) {
 		hp.push_back(n->pops[i].d);
-		if (n->pops[i].stateful) st.push_back(i);
+		if (n->pops[i].stateful && n->pops[i].d.model != USER) st.push_back(i);
+		user |= n->pops[i].stateful && n->pops[i].d.model == USER;
 	}
 	CUDA_TRY(launch_apply_pending(n->stream, n->d_pops, (int)hp.size(), st.data(), (int)st.size(), hp, n->time,
 	                              n->max_delay, n->mode));
 	n->launches += (int64_t)st.size();
+	if (user) {
+		WindowArgs wa{};
+		wa.t0     = n->time;
+		wa.slot0  = (int)((n->time - 1 + n->max_delay) % n->max_delay);
+		wa.hslot0 = (int)(n->time % n->Hb);
+		wa.Hb     = n->Hb;
+		wa.D      = n->max_delay;
+		wa.npop   = (int)n->pops.size();
+		wa.dts    = n->d_dt;
+		wa.counts = n->d_counts;
+		TRY(launch_user_pops(n, wa, 0, true, true, n->stream));
+	}
 	return SPICE_OK;
 }
 
@@ -1007,8 +1152,51 @@ int field_ptr(spice_net* n, int pop, int field, void** p) {
 }
 }  // namespace
 
+namespace {
+// Field f of a stateful user population: a float member at field_offset[f] of every struct.
+int user_field_copy(spice_net* n, int pop, int field, void* host, bool to_host) {
+	Pop const& P = n->pops[pop];
+	if (!P.stateful) return fail(SPICE_EINVAL, "Can only return collections of stateful neurons. (neuron_population.h:143)");
+	if (field < 0 || field >= P.nfields) return fail(SPICE_EINVAL, "the neuron model has no such state field");
+	TRY(flush_pending(n));
+	char* base = static_cast<char*>(P.d.ustate) + P.field_offset[field];
+	if (P.d.size > 0) {
+		if (to_host)
+			CUDA_TRY(cudaMemcpy2DAsync(host, 4, base, P.d.ubytes, 4, P.d.size, cudaMemcpyDeviceToHost, n->stream));
+		else
+			CUDA_TRY(cudaMemcpy2DAsync(base, P.d.ubytes, host, 4, 4, P.d.size, cudaMemcpyHostToDevice, n->stream));
+	}
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}
+}  // namespace
+
+extern "C" int spice_get_user_state(spice_net* n, int pop, void* host_out) {
+	if (!n || !host_out) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop < 0 || pop >= (int)n->pops.size() || n->pops[pop].d.model != USER || !n->pops[pop].stateful)
+		return fail(SPICE_EINVAL, "not a stateful user population");
+	TRY(flush_pending(n));
+	PopDev const& P = n->pops[pop].d;
+	CUDA_TRY(cudaMemcpyAsync(host_out, P.ustate, (size_t)P.size * P.ubytes, cudaMemcpyDeviceToHost, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_user_state(spice_net* n, int pop, const void* host_in) {
+	if (!n || !host_in) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop < 0 || pop >= (int)n->pops.size() || n->pops[pop].d.model != USER || !n->pops[pop].stateful)
+		return fail(SPICE_EINVAL, "not a stateful user population");
+	TRY(flush_pending(n));
+	PopDev const& P = n->pops[pop].d;
+	CUDA_TRY(cudaMemcpyAsync(P.ustate, host_in, (size_t)P.size * P.ubytes, cudaMemcpyHostToDevice, n->stream));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}
+
 extern "C" int spice_get_state(spice_net* n, int pop, int field, void* host_out) {
 	if (!n || !host_out) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop >= 0 && pop < (int)n->pops.size() && n->pops[pop].d.model == USER)
+		return user_field_copy(n, pop, field, host_out, true);
 	void* f = nullptr;
 	TRY(field_ptr(n, pop, field, &f));
 	TRY(flush_pending(n));
@@ -1019,6 +1207,8 @@ extern "C" int spice_get_state(spice_net* n, int pop, int field, void* host_out)
 
 extern "C" int spice_set_state(spice_net* n, int pop, int field, const void* host_in) {
 	if (!n || !host_in) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop >= 0 && pop < (int)n->pops.size() && n->pops[pop].d.model == USER)
+		return user_field_copy(n, pop, field, const_cast<void*>(host_in), false);
 	void* f = nullptr;
 	TRY(field_ptr(n, pop, field, &f));
 	TRY(flush_pending(n));

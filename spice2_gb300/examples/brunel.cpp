@@ -32,17 +32,17 @@ int main(int argc, char** argv) {
 	brunel.connect<fixed_weight>(I, I, fixed_probability(p), delay, {wi});
 
 	std::printf("{\n\t\"name\": \"Brunel\",\n\t\"spikes\": [\n");
-	char const* delim = "\t\t[";
-	for (int i = 0; i < steps; i++) {
+	for (int t = 0; t < steps; t++) {
 		brunel.step();
-		long offset = 0;
-		for (auto const& s : I->spikes(0)) { std::printf("%s%ld", delim, s + offset); delim = ","; }
+		std::printf(t == 0 ? "\t\t[" : ",\n\t\t[");
+		char const* sep = "";
+		long offset     = 0;
+		for (auto s : I->spikes(0)) { std::printf("%s%ld", sep, (long)s + offset); sep = ","; }
 		offset += I->size();
-		for (auto const& s : E->spikes(0)) { std::printf("%s%ld", delim, s + offset); delim = ","; }
+		for (auto s : E->spikes(0)) { std::printf("%s%ld", sep, (long)s + offset); sep = ","; }
 		offset += E->size();
-		for (auto const& s : P->spikes(0)) { std::printf("%s%ld", delim, s + offset); delim = ","; }
+		for (auto s : P->spikes(0)) { std::printf("%s%ld", sep, (long)s + offset); sep = ","; }
 		std::printf("]");
-		delim = ",\n\t\t[";
 	}
 	std::printf("\n\t]\n}\n");
 	return 0;

@@ -72,3 +72,48 @@ def test_samples_cli_brunel_json(engine, capsys):
     samples.main(["brunel", "--steps", "5", "--json"])
     rows = json.loads(capsys.readouterr().out)["spikes"]
     assert len(rows) == 5 and rows[0][:3] == [10533, 11015, 11209] and rows[1][:3] == [10310, 11115, 11884]
+
+
+USER_MODEL_NO_NVCC = r"""
+#include "spice/snn.h"
+using namespace spice;
+struct my_lif {
+	struct neuron { float V = 0; int32_t T = 0; };
+	SPICE_HD bool update(neuron& n, float, auto&) const { return false; }
+};
+int main() { snn net(1e-4f, 1e-4f, {1}); net.add_population<my_lif>(4); }
+"""
+
+
+def test_user_models_need_nvcc(tmp_path):
+    """A user model compiled by a host-only compiler is rejected at compile time with a clear message."""
+    src = tmp_path / "u.cpp"
+    src.write_text(USER_MODEL_NO_NVCC)
+    r = subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode != 0 and "compile this translation unit with nvcc" in r.stderr
+
+
+@pytest.mark.gpu
+def test_user_models_compiled_with_nvcc_match_the_reference(engine, oracle_lib, tmp_path):
+    """samples/brunel.cpp with user-defined Poisson, LIF and synapse structs compiled into GPU kernels
+    by the header: the raster equals the oracle's (the reference's algorithm)."""
+    o = oracle_lib
+    exe = tmp_path / "user_models"
+    libdir = os.path.join(ROOT, "spice2_gb300")
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    subprocess.run([nvcc, "-std=c++20", "-gencode", "arch=compute_103a,code=sm_103a", "-fmad=false",
+                    "-I", os.path.join(ROOT, "include"), os.path.join(ROOT, "spice2_gb300", "examples", "user_models.cu"),
+                    "-L", libdir, "-lspice_gb300", f"-Xlinker=-rpath={libdir}", "-o", str(exe)], check=True)
+    N, p, steps, seed = 4000, 0.05, 200, 1337
+    out = subprocess.run([str(exe), str(N), str(p), str(steps), str(seed)], check=True, capture_output=True, text=True)
+    rows = json.loads(out.stdout)["spikes"]
+    ref, pops = o.brunel(N, p, seed)
+    n_spikes = 0
+    for t, row in enumerate(rows):
+        ref.step()
+        P, E, I = (ref.spikes(k, 0) for k in pops)
+        expect = [int(x) for x in I] + [int(x) + N // 10 for x in E] + [int(x) + N // 2 for x in P]
+        assert sorted(row) == expect, f"step {t}"
+        n_spikes += len(I) + len(E)
+    assert n_spikes > 0
