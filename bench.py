@@ -45,12 +45,10 @@ N_NEURONS, P_CONN, SEED, STEPS_PER_RUN = 500000, 0.002, 1, 2000
 DT = 1e-4
 WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
 # DRAM bytes (read + write) per synaptic event of the delivery kernel: dram__bytes_read.sum +
-# dram__bytes_write.sum of one captured k_deliver_tps launch (Brunel N=2e5, p=0.005, the 16th window,
-# 4,235,947 events; profiles/k_deliver_tps_k_neurons_k_sources_brunel_N2e5_p0.005.md) divided by its
-# events.  The bench's traffic per launch is this figure times the launch's mean events (the capture
-# runs on a smaller network than the bench so that the ncu replay stays small; the traffic per
-# event does not depend on the network size as long as the rows do not fit in L2).
-DELIVER_DRAM_BYTES_PER_EVENT = (22.117120e6 + 1.792e3) / 4235947
+# dram__bytes_write.sum of one k_deliver_groups<0,4> launch on this workload (the 11th window,
+# 11,158,496 events; profiles/k_deliver_groups_brunel_N5e5_p0.002.md) divided by its events.  The
+# bench's traffic per launch is this figure times the launch's mean events.
+DELIVER_DRAM_BYTES_PER_EVENT = (62.261504e6 + 1.521152e6) / 11158496
 DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
                    7: "k_deliver_groups_occ"}
@@ -69,24 +67,24 @@ def _barrier(ws):
         dist.barrier()
 
 
-def _max_over_ranks(x: float, ws: int) -> float:
+def _reduce_over_ranks(x: float, ws: int, op: str) -> float:
+    """x reduced over the ranks of the process group (NCCL on the GPUs, or gloo on the CPU)."""
     if ws == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
     return float(t.item())
+
+
+def _max_over_ranks(x: float, ws: int) -> float:
+    return _reduce_over_ranks(x, ws, "max")
 
 
 def _sum_over_ranks(x: float, ws: int) -> float:
-    if ws == 1:
-        return x
-    import torch
-    import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
-    dist.all_reduce(t, op=dist.ReduceOp.SUM)
-    return float(t.item())
+    return _reduce_over_ranks(x, ws, "sum")
 
 
 class ClockSampler:
