@@ -37,7 +37,7 @@ def _worker(rank, ws, port, out):
 
 def test_replica_reductions_world_size_2():
     port = _free_port()
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_worker, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
@@ -63,7 +63,7 @@ def _ref_worker(rank, ws, port, out):
 
 
 def test_reference_arm_other_ranks_do_no_work():
-    with mp.Manager() as mgr:
+    with mp.get_context("spawn").Manager() as mgr:
         out = mgr.dict()
         mp.spawn(_ref_worker, args=(2, _free_port(), out), nprocs=2, join=True)
         assert dict(out)[1] == 0
