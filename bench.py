@@ -51,7 +51,8 @@ WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
 DELIVER_DRAM_BYTES_PER_EVENT = (62.261504e6 + 1.521152e6) / 11158496
 DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
-                   7: "k_deliver_groups_occ"}
+                   7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
+                   9: "k_deliver_staged<4 in flight>"}
 
 
 def _dist():

@@ -119,7 +119,9 @@ enum {
 	                                   3: one thread per spike with 16-byte loads,
 	                                   4: one thread per spike, software-pipelined,
 	                                   5, 6: 4 or 8 lanes per spike, software-pipelined,
-	                                   7: as 5 with <= 32 registers (4 x 512 threads per SM) */
+	                                   7: as 5 with <= 32 registers (4 x 512 threads per SM),
+	                                   8, 9: 4 lanes per spike, sub-rows staged in shared
+	                                   memory, 2 or 4 sub-rows in flight per lane group      */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 };

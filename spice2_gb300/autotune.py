@@ -21,7 +21,8 @@ DEFAULT_CANDIDATES = [
     # (tile bytes, threads per CTA, parts per (slot, tile), work mapping: 0 warp-flattened,
     #  1 thread per spike, 2 warp per spike, 3 thread per spike with 16-byte loads,
     #  4 thread per spike, software-pipelined, 5 / 6 four / eight lanes per spike, 7 as 5 with
-    #  at most 32 registers)
+    #  at most 32 registers, 8 / 9 four lanes per spike with sub-rows staged in shared memory, two /
+    #  four sub-rows in flight per group)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
@@ -29,7 +30,11 @@ DEFAULT_CANDIDATES = [
     (24 * 1024, 256, 1, 5), (12 * 1024, 128, 1, 5), (48 * 1024, 256, 1, 5), (24 * 1024, 256, 1, 6),
     (48 * 1024, 256, 1, 6), (48 * 1024, 512, 1, 6), (96 * 1024, 512, 1, 6), (12 * 1024, 128, 1, 3),
     (24 * 1024, 512, 1, 7), (26 * 1024, 512, 1, 7), (28 * 1024, 512, 1, 7), (32 * 1024, 512, 1, 7),
-    (16 * 1024, 256, 1, 7), (12 * 1024, 128, 1, 7),
+    (16 * 1024, 256, 1, 7), (12 * 1024, 128, 1, 7), (112 * 1024, 1024, 1, 4), (112 * 1024, 1024, 1, 6),
+    (128 * 1024, 1024, 1, 6), (24 * 1024, 256, 1, 8), (24 * 1024, 512, 1, 8), (12 * 1024, 256, 1, 8),
+    (48 * 1024, 512, 1, 8), (112 * 1024, 1024, 1, 8), (96 * 1024, 1024, 1, 8), (100 * 1024, 1024, 1, 8),
+    (104 * 1024, 1024, 1, 8), (108 * 1024, 1024, 1, 8), (104 * 1024, 1024, 1, 6),
+    (100 * 1024, 1024, 1, 9), (104 * 1024, 1024, 1, 9), (24 * 1024, 256, 1, 9), (48 * 1024, 512, 1, 9),
 ]
 
 

@@ -107,7 +107,9 @@ struct DeliverArgs {
 	int parts;               // CTAs sharing one (slot, tile); > 1 flushes with reductions
 	int algo;                // 0: warp-flattened sub-rows, 1: one thread per spike, 2: warp per spike,
 	                         // 3: thread per spike with 16-byte loads, 4: thread per spike, pipelined,
-	                         // 5 / 6: 4 / 8 lanes per spike, pipelined
+	                         // 5 / 6: 4 / 8 lanes per spike, pipelined, 7: 5 at <= 32 registers,
+	                         // 8 / 9: 4 lanes per spike with sub-row descriptors staged in shared memory,
+	                         // 2 / 4 sub-rows in flight per group
 	int list_k0;             // first list slot of this window's parity
 };
 // One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.

@@ -1324,7 +1324,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->deliver_threads = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_ALGO:
-			if (value < 0 || value > 7) return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. 7");
+			if (value < 0 || value > 9) return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. 9");
 			n->deliver_algo = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:

@@ -312,7 +312,8 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
     (0, 24 * 1024, 256, 1), (1, 12 * 1024, 128, 1), (2, 24 * 1024, 256, 1), (3, 48 * 1024, 512, 1),
     (4, 24 * 1024, 256, 1), (4, 6 * 1024, 128, 2), (4, 96 * 1024, 1024, 1), (2, 4096, 64, 3), (0, 8192, 512, 2),
     (5, 24 * 1024, 256, 1), (5, 4096, 64, 2), (6, 48 * 1024, 512, 1), (6, 200 * 1024, 1024, 3),
-    (7, 26 * 1024, 512, 1), (7, 8192, 1024, 2),
+    (7, 26 * 1024, 512, 1), (7, 8192, 1024, 2), (8, 24 * 1024, 256, 1), (8, 4096, 64, 3),
+    (8, 112 * 1024, 1024, 1), (9, 100 * 1024, 1024, 1), (9, 8192, 128, 2),
 ])
 def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
     """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
