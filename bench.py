@@ -54,7 +54,8 @@ DELIVER_DRAM_BYTES_PER_EVENT = {5: (62.261504e6 + 1.521152e6) / 11158496,
 DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
                    7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
-                   9: "k_deliver_staged<4 in flight>"}
+                   9: "k_deliver_staged<4 in flight>", 10: "k_deliver_staged_vec<2 sub-rows, 4 blocks>",
+                   11: "k_deliver_staged_vec<4 sub-rows, 2 blocks>"}
 
 
 def _dist():

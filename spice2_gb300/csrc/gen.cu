@@ -342,7 +342,8 @@ cudaError_t generate_fixed_probability(cudaStream_t stream, std::vector<GenReque
 		for (size_t j = 0; j < jobs.size(); j++) {
 			GenRequest& r = reqs[job_req[j]];
 			CK(cudaMemcpy(&r.synapses, r.offsets + r.src, sizeof(int64_t), cudaMemcpyDeviceToHost));
-			CK(cudaMalloc(&r.neighbors, sizeof(int32_t) * (r.synapses > 0 ? r.synapses : 1)));
+			// whole 16-byte blocks: delivery reads targets as aligned int4 blocks
+			CK(cudaMalloc(&r.neighbors, sizeof(int32_t) * ((r.synapses + 3) / 4 * 4 + 4)));
 			k_fill<<<(unsigned)((r.src + 255) / 256), 256, 0, stream>>>(gaps[job_req[j]], r.offsets, r.src,
 			                                                            r.neighbors);
 			CK(cudaGetLastError());

@@ -59,6 +59,10 @@ cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const i
 cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* tables);
 
 constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
+// Delivery work mappings (SPICE_TUNE_DELIVER_ALGO 0 .. kDeliverAlgos - 1), one kernel per mapping
+// and mode.
+constexpr int kDeliverAlgos = 12;
+constexpr int kDeliverFns   = 2 * kDeliverAlgos;
 
 struct WindowArgs {
 	int64_t t0;        // absolute step of the window's first step

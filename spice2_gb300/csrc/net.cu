@@ -402,7 +402,7 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	int64_t* doff = nullptr;
 	int32_t* dnb  = nullptr;
 	CUDA_TRY(cudaMalloc(&doff, sizeof(int64_t) * (S + 1)));
-	if (cudaMalloc(&dnb, sizeof(int32_t) * (npairs > 0 ? npairs : 1)) != cudaSuccess) {
+	if (cudaMalloc(&dnb, sizeof(int32_t) * ((npairs + 3) / 4 * 4 + 4)) != cudaSuccess) {  // whole 16-byte blocks
 		cudaFree(doff);
 		return fail(SPICE_ENOMEM, "cudaMalloc failed for adjacency");
 	}
@@ -1324,7 +1324,8 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->deliver_threads = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_ALGO:
-			if (value < 0 || value > 9) return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. 9");
+			if (value < 0 || value >= kDeliverAlgos)
+				return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. " + std::to_string(kDeliverAlgos - 1));
 			n->deliver_algo = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:

@@ -1022,6 +1022,150 @@ __device__ __forceinline__ void deliver_staged(A const& a, PopDev const& P, int 
 	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
+// Staged mapping with whole sub-rows in one round trip: as deliver_staged, but a 4-lane group loads
+// its SF sub-rows as aligned 16-byte blocks of the target array, U blocks per lane (4U*4 targets per
+// sub-row) before the first shared-memory add, so a typical sub-row (<= 64 targets) costs one load
+// latency instead of one per 16 targets.  Only blocks holding at least one target of the sub-row are
+// read (target arrays are 16-byte aligned and padded to whole blocks); the targets of a block outside
+// the sub-row are skipped.  Up to kStageV descriptors per round, so most CTAs stage once.
+constexpr int kStageV = 2048;
+
+template <int MODE, int SF, int U, class A>
+__device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, int t, int si, int part) {
+	constexpr int G = 4;
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	__shared__ int64_t st_e0[kStageV];
+	__shared__ int32_t st_len[kStageV];
+	__shared__ uint8_t st_c[kStageV];
+	__shared__ int c_pre[kConnBatch + 1];
+	__shared__ const int32_t* c_lst[kConnBatch];
+	__shared__ const int64_t* c_bnd[kConnBatch];
+	__shared__ const int4* c_nb[kConnBatch];
+	__shared__ uint32_t c_inc[kConnBatch];
+	__shared__ int c_word[kConnBatch];
+	__shared__ float c_w[kConnBatch];
+	__shared__ int s_nc, s_touched, s_next;
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
+	if (threadIdx.x == 0) {
+		ev_block  = 0;
+		s_touched = 0;
+	}
+	int64_t const sigma = a.slot_lo + si;
+	int const stride    = P.ntiles + 1;
+	int const gl        = threadIdx.x & (G - 1);
+	unsigned long long my_events = 0;
+	for (int cb = P.in_begin; cb < P.in_end; cb += kConnBatch) {
+		__syncthreads();
+		if (threadIdx.x == 0) {
+			int tot = 0, nc = 0;
+			for (int ci = cb; ci < min(cb + kConnBatch, P.in_end); ci++) {
+				ConnDev const& C = a.conns[ci];
+				int64_t const k  = sigma - (a.t0 + C.delay - 1);
+				if (k < 0 || k >= a.K || C.plastic) continue;
+				s_touched    = 1;
+				int const n  = a.counts[k * a.npop + C.src];
+				int const pp = (n + a.parts - 1) / a.parts;
+				int const lo = min(n, part * pp), hi = min(n, lo + pp);
+				c_lst[nc]  = C.src_list + (a.list_k0 + k) * C.src_size + lo;
+				c_bnd[nc]  = C.bounds + t;
+				c_nb[nc]   = reinterpret_cast<const int4*>(C.nb);
+				c_inc[nc]  = C.inc;
+				c_word[nc] = MODE == 0 ? C.word : C.fslot;
+				c_w[nc]    = C.weight;
+				c_pre[nc]  = tot;
+				tot += hi - lo;
+				nc++;
+			}
+			c_pre[nc] = tot;
+			s_nc      = nc;
+		}
+		__syncthreads();
+		int const nc    = s_nc;
+		int const total = c_pre[nc];
+		for (int c0 = 0; c0 < total; c0 += kStageV) {
+			int const m = min(kStageV, total - c0);
+			for (int q = threadIdx.x; q < m; q += blockDim.x) {
+				int const g = c0 + q;
+				int j       = 0;
+				while (j + 1 < nc && c_pre[j + 1] <= g) j++;
+				const int64_t* bb = c_bnd[j] + (int64_t)__ldg(c_lst[j] + (g - c_pre[j])) * stride;
+				int64_t const b0  = __ldg(bb);
+				st_e0[q]          = b0;
+				st_len[q]         = (int32_t)(__ldg(bb + 1) - b0);
+				st_c[q]           = (uint8_t)j;
+			}
+			if (threadIdx.x == 0) s_next = 0;
+			__syncthreads();
+			int const nsets = (m + SF - 1) / SF;
+			while (true) {  // a warp takes 32 / G consecutive sets of SF sub-rows per fetch (warp-uniform exit)
+				int base = 0;
+				if ((threadIdx.x & 31) == 0) base = atomicAdd(&s_next, 32 / G);
+				base = __shfl_sync(0xffffffffu, base, 0);
+				if (base >= nsets) break;
+				int const ps = base + ((threadIdx.x & 31) / G);
+				if (ps >= nsets) continue;
+				int64_t qb[SF];  // first 16-byte block of each sub-row
+				int lo[SF], hi[SF], nbk[SF], cj[SF];
+				int nbmax = 0;
+#pragma unroll
+				for (int f = 0; f < SF; f++) {
+					int const q     = ps * SF + f;
+					int64_t const e = q < m ? st_e0[q] : 0;
+					int const len   = q < m ? st_len[q] : 0;
+					cj[f]           = q < m ? st_c[q] : 0;
+					qb[f]           = e >> 2;
+					lo[f]           = (int)(e & 3);  // targets [lo, hi) of the blocks from qb on
+					hi[f]           = lo[f] + len;
+					nbk[f]          = len > 0 ? (hi[f] + 3) >> 2 : 0;
+					nbmax           = max(nbmax, nbk[f]);
+					if (gl == 0) my_events += (unsigned long long)len;
+				}
+				for (int o = gl; o < nbmax; o += G * U) {
+					int4 v[SF][U];
+#pragma unroll
+					for (int f = 0; f < SF; f++) {
+						const int4* nbf = c_nb[cj[f]] + qb[f];
+#pragma unroll
+						for (int u = 0; u < U; u++) {
+							int const ob = o + u * G;
+							v[f][u]      = ob < nbk[f] ? __ldg(nbf + ob) : make_int4(0, 0, 0, 0);
+						}
+					}
+#pragma unroll
+					for (int f = 0; f < SF; f++) {
+						int const word     = c_word[cj[f]];
+						uint32_t const inc = c_inc[cj[f]];
+						float const w      = c_w[cj[f]];
+#pragma unroll
+						for (int u = 0; u < U; u++) {
+							int const x0 = (o + u * G) * 4;  // index of the block's first target
+							int const d[4] = {v[f][u].x, v[f][u].y, v[f][u].z, v[f][u].w};
+#pragma unroll
+							for (int c = 0; c < 4; c++)
+								if (x0 + c >= lo[f] && x0 + c < hi[f]) {
+									int const li = (d[c] - tbase) * width + word;
+									if (MODE == 0) atomicAdd(tile_sm + li, inc);
+									else atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
+								}
+						}
+					}
+				}
+			}
+			__syncthreads();
+		}
+	}
+	__syncthreads();
+	bool const touched = s_touched != 0;
+	add_events(a.events, my_events, &ev_block);
+	if (!touched) return;
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
 // Warp-per-spike mapping: a warp takes 32 spikes, loads their sub-row bounds lane-parallel, then
 // streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced loads, 8 in flight per
 // lane, no cross-lane search).
@@ -1146,6 +1290,12 @@ template <int MODE, int SF>
 __global__ void k_deliver_staged(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item(a);
 	deliver_staged<MODE, SF>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+template <int MODE, int SF, int U>
+__global__ void __launch_bounds__(SF > 2 ? 768 : 1024, 1) k_deliver_staged_vec(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_staged_vec<MODE, SF, U>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
 // The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
@@ -1580,7 +1730,9 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else if (ALGO == 5 || ALGO == 7) deliver_groups<MODE, 4>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 6) deliver_groups<MODE, 8>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 8) deliver_staged<MODE, 2>(a, P, t, (int)blockIdx.y, part);
-	else deliver_staged<MODE, 4>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 9) deliver_staged<MODE, 4>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 10) deliver_staged_vec<MODE, 2, 4>(a, P, t, (int)blockIdx.y, part);
+	else deliver_staged_vec<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -1653,9 +1805,9 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		if (a.counts_next_len > 0) return cudaMemsetAsync(a.counts_next, 0, sizeof(int32_t) * a.counts_next_len, stream);
 		return cudaSuccess;
 	}
-	static int configured[20] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+	static int configured[kDeliverFns] = {};
 	int const m = (a.mode == 0 ? 0 : 1) + 2 * a.algo;
-	void const* fns[20] = {(void const*)k_deliver<0>,            (void const*)k_deliver<1>,
+	void const* fns[kDeliverFns] = {(void const*)k_deliver<0>,            (void const*)k_deliver<1>,
 	                       (void const*)k_deliver_tps<0, false>, (void const*)k_deliver_tps<1, false>,
 	                       (void const*)k_deliver_wps<0>,        (void const*)k_deliver_wps<1>,
 	                       (void const*)k_deliver_tps<0, true>,  (void const*)k_deliver_tps<1, true>,
@@ -1664,7 +1816,9 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 	                       (void const*)k_deliver_groups<0, 8>,  (void const*)k_deliver_groups<1, 8>,
 	                       (void const*)k_deliver_groups_occ<0>, (void const*)k_deliver_groups_occ<1>,
 	                       (void const*)k_deliver_staged<0, 2>,  (void const*)k_deliver_staged<1, 2>,
-	                       (void const*)k_deliver_staged<0, 4>,  (void const*)k_deliver_staged<1, 4>};
+	                       (void const*)k_deliver_staged<0, 4>,  (void const*)k_deliver_staged<1, 4>,
+	                       (void const*)k_deliver_staged_vec<0, 2, 4>, (void const*)k_deliver_staged_vec<1, 2, 4>,
+	                       (void const*)k_deliver_staged_vec<0, 4, 2>, (void const*)k_deliver_staged_vec<1, 4, 2>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -1695,6 +1849,10 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		case 17: k_deliver_staged<1, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 18: k_deliver_staged<0, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 19: k_deliver_staged<1, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 20: k_deliver_staged_vec<0, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 21: k_deliver_staged_vec<1, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 22: k_deliver_staged_vec<0, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 23: k_deliver_staged_vec<1, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 	}
 	return cudaGetLastError();
 }
@@ -1748,7 +1906,7 @@ cudaError_t launch_batch_neurons(cudaStream_t stream, BatchArgs const& b) {
 namespace {
 void const* batch_deliver_fn(BatchArgs const& b) {
 	int const m = (b.mode == 0 ? 0 : 1) + 2 * b.algo;
-	void const* fns[20] = {(void const*)k_batch_deliver<0, 0>, (void const*)k_batch_deliver<1, 0>,
+	void const* fns[kDeliverFns] = {(void const*)k_batch_deliver<0, 0>, (void const*)k_batch_deliver<1, 0>,
 	                       (void const*)k_batch_deliver<0, 1>, (void const*)k_batch_deliver<1, 1>,
 	                       (void const*)k_batch_deliver<0, 2>, (void const*)k_batch_deliver<1, 2>,
 	                       (void const*)k_batch_deliver<0, 3>, (void const*)k_batch_deliver<1, 3>,
@@ -1757,8 +1915,10 @@ void const* batch_deliver_fn(BatchArgs const& b) {
 	                       (void const*)k_batch_deliver<0, 6>, (void const*)k_batch_deliver<1, 6>,
 	                       (void const*)k_batch_deliver<0, 7>, (void const*)k_batch_deliver<1, 7>,
 	                       (void const*)k_batch_deliver<0, 8>, (void const*)k_batch_deliver<1, 8>,
-	                       (void const*)k_batch_deliver<0, 9>, (void const*)k_batch_deliver<1, 9>};
-	return fns[m < 20 ? m : 0];
+	                       (void const*)k_batch_deliver<0, 9>, (void const*)k_batch_deliver<1, 9>,
+	                       (void const*)k_batch_deliver<0, 10>, (void const*)k_batch_deliver<1, 10>,
+	                       (void const*)k_batch_deliver<0, 11>, (void const*)k_batch_deliver<1, 11>};
+	return fns[m];
 }
 }  // namespace
 
@@ -1794,6 +1954,10 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 17: k_batch_deliver<1, 8><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 18: k_batch_deliver<0, 9><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 19: k_batch_deliver<1, 9><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 20: k_batch_deliver<0, 10><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 21: k_batch_deliver<1, 10><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 22: k_batch_deliver<0, 11><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 23: k_batch_deliver<1, 11><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
 	return cudaGetLastError();
 }

@@ -314,10 +314,13 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
     (5, 24 * 1024, 256, 1), (5, 4096, 64, 2), (6, 48 * 1024, 512, 1), (6, 200 * 1024, 1024, 3),
     (7, 26 * 1024, 512, 1), (7, 8192, 1024, 2), (8, 24 * 1024, 256, 1), (8, 4096, 64, 3),
     (8, 112 * 1024, 1024, 1), (9, 100 * 1024, 1024, 1), (9, 8192, 128, 2),
+    (10, 100 * 1024, 1024, 1), (10, 24 * 1024, 256, 1), (10, 4096, 64, 3), (10, 180 * 1024, 1024, 2),
+    (11, 100 * 1024, 1024, 1), (11, 8192, 128, 2), (11, 48 * 1024, 512, 1),
 ])
 def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
     """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
-    16-byte loads, software-pipelined) gives the reference's raster and V bit for bit."""
+    16-byte loads, software-pipelined, lane groups, staged descriptors, aligned-block sub-rows)
+    gives the reference's raster and V bit for bit."""
     g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
     N, seed, steps = (int(x) for x in g["meta"])
     net, pops = engine.brunel(N, float(g["p"][0]), seed)
