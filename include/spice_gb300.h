@@ -126,6 +126,10 @@ enum {
 	                                   16-byte blocks, 64 or 32 targets per load round trip  */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
+	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input
+	                                   words in registers, 1 rolled steps over words parked in
+	                                   shared memory, 2 as 1 with warp-uniform count replay,
+	                                   3 as 0 with warp-uniform count replay                  */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

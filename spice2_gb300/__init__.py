@@ -348,8 +348,9 @@ class snn:
 
     def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
                    deliver_parts: int | None = None, deliver_algo: int | None = None,
-                   overlap_sources: bool | None = None):
-        """Delivery launch shape (any time between steps); results are independent of it."""
+                   overlap_sources: bool | None = None, neuron_variant: int | None = None):
+        """Delivery launch shape and neuron-update variant (any time between steps); results are
+        independent of them."""
         if tile_bytes is not None:
             _check(lib().spice_set_tuning(self._h, 0, int(tile_bytes)))
         if deliver_threads is not None:
@@ -360,6 +361,8 @@ class snn:
             _check(lib().spice_set_tuning(self._h, 3, int(deliver_algo)))
         if overlap_sources is not None:
             _check(lib().spice_set_tuning(self._h, 4, int(bool(overlap_sources))))
+        if neuron_variant is not None:
+            _check(lib().spice_set_tuning(self._h, 6, int(neuron_variant)))
 
     # stepping
     def step(self):

@@ -63,7 +63,34 @@ def autotune(net, steps: int = 600, warm: int = 60, candidates=None, verbose: bo
                   flush=True)
     best = min(results, key=lambda r: r["deliver_us"])
     net.set_tuning(tile_bytes=best["tile_bytes"], deliver_threads=best["threads"], deliver_parts=best["parts"],
-                   deliver_algo=best["algo"], overlap_sources=True)
+                   deliver_algo=best["algo"])
+    from . import batch
+    if not isinstance(net, batch):  # batches run one neuron-update variant
+        nres = tune_neurons(net, steps=steps, warm=warm, verbose=verbose)
+        best = dict(best, neuron_variant=nres["best"]["variant"], neuron_us=nres["best"]["neuron_us"])
+    net.set_tuning(overlap_sources=True)
+    return {"best": best, "results": results}
+
+
+def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3), verbose: bool = False) -> dict:
+    """Times the neuron-update kernel of `net` for each LIF window variant (identical results);
+    applies and returns the fastest."""
+    results = []
+    for v in variants:
+        net.set_tuning(neuron_variant=v)
+        net.run(warm)
+        net.synchronize()
+        net.set_profiling(True)
+        net.run(steps)
+        net.synchronize()
+        n, ms = net.kernel_stats(0)
+        net.set_profiling(False)
+        us = 1e3 * ms / max(n, 1)
+        results.append({"variant": v, "neuron_us": us})
+        if verbose:
+            print(f"neuron variant {v}:  window {us:8.2f} us", flush=True)
+    best = min(results, key=lambda r: r["neuron_us"])
+    net.set_tuning(neuron_variant=best["variant"])
     return {"best": best, "results": results}
 
 

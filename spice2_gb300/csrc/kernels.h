@@ -79,6 +79,7 @@ struct WindowArgs {
 	int64_t tab_net_stride;  // 0: one net
 	int32_t* counts;      // [K][npop] spikes per step and population (window parity buffer)
 	int list_k0;          // first list slot of this window's parity: lists are [2K][size]
+	int variant;          // LIF window variant (SPICE_TUNE_NEURON_VARIANT)
 	int blk_begin[kMaxPops + 1];
 	int blk_kind[kMaxPops];      // 0: per-neuron window CTAs, 1: Poisson step CTAs, 2: external,
 	                             // 3: per-neuron CTAs of a LIF whose inputs all add to V (16-bit counts)

@@ -865,6 +865,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			wa.tables  = n->d_tables ? n->d_tables + j * kJumpTable : nullptr;
 			wa.counts  = n->d_counts + (size_t)q * n->K * np;
 			wa.list_k0 = q * n->K;
+			wa.variant = n->neuron_variant;
 			WindowArgs ws = wa;  // sources
 			int nb = 0, nbs = 0;
 			for (int p = 0; p < np; p++) {
@@ -1327,6 +1328,10 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			if (value < 0 || value >= kDeliverAlgos)
 				return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. " + std::to_string(kDeliverAlgos - 1));
 			n->deliver_algo = (int)value;
+			return SPICE_OK;
+		case SPICE_TUNE_NEURON_VARIANT:
+			if (value < 0 || value > 3) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 3");
+			n->neuron_variant = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:
 			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "overlap must be 0 or 1");

@@ -316,13 +316,32 @@ __device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p,
 	}
 }
 
+// v += w, n times, one IEEE add at a time, with a trip count common to the warp (its largest n):
+// lanes past their own n keep v (predicated adds), so the loop has no divergent branches.  Every
+// lane of the warp must call it.
+__device__ __forceinline__ float add_n_warp(float v, float w, uint32_t n) {
+	uint32_t const m = __reduce_max_sync(0xffffffffu, n);
+	uint32_t j       = 0;
+	for (; j + 2 <= m; j += 2) {
+		v = j < n ? __fadd_rn(v, w) : v;
+		v = j + 1 < n ? __fadd_rn(v, w) : v;
+	}
+	if (j < m) v = j < n ? __fadd_rn(v, w) : v;
+	return v;
+}
+
 // The Brunel LIF window (deterministic mode, every input group adds to V through a 16-bit counter
-// of word 0): the input words of 16 consecutive slots are loaded up front into registers and the
-// 16 step bodies are unrolled, so nothing is indexed dynamically (no local memory); dt comes from
-// shared memory.  Same arithmetic, in the same order, as window_neurons<0, true, false>.
-template <class A>
+// of word 0): the input words of 16 consecutive slots are loaded up front, then the steps run.
+// Same arithmetic, in the same order, as window_neurons<0, true, false>; dt comes from shared
+// memory.  Variants (SPICE_TUNE_NEURON_VARIANT), identical results:
+//   ROLLED = false: the words stay in registers and the 16 step bodies are unrolled (nothing is
+//     indexed dynamically);
+//   ROLLED = true: the words are parked in shared memory (one column per thread) and the step loop
+//     stays rolled, a body small enough for the instruction cache;
+//   UNIFORM: the count replay runs warp-uniform trip counts (add_n_warp) instead of per-lane loops.
+template <bool ROLLED, bool UNIFORM, class A>
 __device__ __forceinline__ void window_lif_fast(A const& a, const PopDev* __restrict__ Pg, int p, int b,
-                                                const float* dts_sm) {
+                                                const float* dts_sm, uint32_t (*xs_sm)[kThreads]) {
 	int const N      = (int)Pg->size;
 	int const i      = b * kThreads + threadIdx.x;
 	bool const valid = i < N;
@@ -348,40 +367,63 @@ __device__ __forceinline__ void window_lif_fast(A const& a, const PopDev* __rest
 	int32_t* const list  = Pg->list;
 	int32_t* const count = a.counts + p;
 	bool const wl = lane == 0 && word < nwords;
+	auto step = [&](int k, uint32_t xx) {
+		bool spike = false;
+		if (UNIFORM) {
+			uint32_t const n0 = valid ? xx & 0xffffu : 0u, n1 = valid ? xx >> 16 : 0u;
+			V = add_n_warp(V, w0, n0);
+			V = add_n_warp(V, w1, n1);
+			if (valid) {
+				if (zero && xx) cnt[(int64_t)slot * N + i] = 0;
+				spike = lif_update(V, T, __fmaf_rn(-dts_sm[k], tminv, 1.0f), vthres, tref);
+			}
+		} else if (valid) {
+			if (xx) {
+				V = add_n(V, w0, xx & 0xffffu);
+				V = add_n(V, w1, xx >> 16);
+				if (zero) cnt[(int64_t)slot * N + i] = 0;
+			}
+			spike = lif_update(V, T, __fmaf_rn(-dts_sm[k], tminv, 1.0f), vthres, tref);
+		}
+		unsigned const mask = __ballot_sync(0xffffffffu, spike);
+		if (wl) bits[(int64_t)hslot * nwords + word] = mask;
+		if (mask) {
+			int base = 0;
+			if (lane == 0) base = atomicAdd(count + k * npop, __popc(mask));
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if (spike) list[(int64_t)(a.list_k0 + k) * N + base + __popc(mask & lanemask_lt())] = i;
+		}
+		slot  = slot + 1 == D ? 0 : slot + 1;
+		hslot = hslot + 1 == Hb ? 0 : hslot + 1;
+	};
 	for (int k0 = 0; k0 < a.K; k0 += 16) {
 		int const nk = min(16, a.K - k0);
-		uint32_t x[16];
-		int sl = slot;
+		int sl       = slot;
+		if (ROLLED) {  // asynchronous copies into the thread's own shared-memory column
 #pragma unroll
-		for (int u = 0; u < 16; u++) {
-			x[u] = (valid && u < nk) ? cnt[(int64_t)sl * N + i] : 0u;
-			sl   = sl + 1 == D ? 0 : sl + 1;
-		}
-#pragma unroll
-		for (int u = 0; u < 16; u++) {
-			if (u < nk) {
-				int const k    = k0 + u;
-				bool spike     = false;
-				if (valid) {
-					uint32_t const xx = x[u];
-					if (xx) {
-						V = add_n(V, w0, xx & 0xffffu);
-						V = add_n(V, w1, xx >> 16);
-						if (zero) cnt[(int64_t)slot * N + i] = 0;
-					}
-					spike = lif_update(V, T, __fmaf_rn(-dts_sm[k], tminv, 1.0f), vthres, tref);
+			for (int u = 0; u < 16; u++) {
+				if (valid && u < nk) {
+					unsigned const dst = (unsigned)__cvta_generic_to_shared(&xs_sm[u][threadIdx.x]);
+					asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(cnt + (int64_t)sl * N + i)
+					             : "memory");
+				} else {
+					xs_sm[u][threadIdx.x] = 0u;
 				}
-				unsigned const mask = __ballot_sync(0xffffffffu, spike);
-				if (wl) bits[(int64_t)hslot * nwords + word] = mask;
-				if (mask) {
-					int base = 0;
-					if (lane == 0) base = atomicAdd(count + k * npop, __popc(mask));
-					base = __shfl_sync(0xffffffffu, base, 0);
-					if (spike) list[(int64_t)(a.list_k0 + k) * N + base + __popc(mask & lanemask_lt())] = i;
-				}
-				slot  = slot + 1 == D ? 0 : slot + 1;
-				hslot = hslot + 1 == Hb ? 0 : hslot + 1;
+				sl = sl + 1 == D ? 0 : sl + 1;
 			}
+			asm volatile("cp.async.wait_all;" ::: "memory");
+#pragma unroll 1
+			for (int u = 0; u < nk; u++) step(k0 + u, xs_sm[u][threadIdx.x]);
+		} else {
+			uint32_t x[16];
+#pragma unroll
+			for (int u = 0; u < 16; u++) {
+				x[u] = (valid && u < nk) ? cnt[(int64_t)sl * N + i] : 0u;
+				sl   = sl + 1 == D ? 0 : sl + 1;
+			}
+#pragma unroll
+			for (int u = 0; u < 16; u++)
+				if (u < nk) step(k0 + u, x[u]);
 		}
 	}
 	if (valid) {
@@ -491,10 +533,13 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 
 // Per-neuron populations: one thread per neuron, K steps with the state in registers.
 // ONLY_FAST: every population of the launch takes the FAST path, so the generic input replay is
-// compiled out (fewer registers).
-template <int MODE, bool ONLY_FAST>
-__global__ void __launch_bounds__(kThreads) k_neurons(const __grid_constant__ WindowArgs a) {
+// compiled out (fewer registers).  VAR: the LIF window variant (window_lif_fast), one kernel each so
+// that each keeps its own register count.
+template <int MODE, bool ONLY_FAST, int VAR>
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const __grid_constant__ WindowArgs a) {
+	constexpr bool ROLLED = VAR == 1 || VAR == 2;
 	__shared__ float dts_sm[kMaxWindow];
+	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
 	for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
 	__syncthreads();
 	int const b = blockIdx.x;
@@ -502,7 +547,7 @@ __global__ void __launch_bounds__(kThreads) k_neurons(const __grid_constant__ Wi
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
-	if (MODE == 0 && kind == 3) window_lif_fast(a, a.pops + p, p, lb, dts_sm);
+	if (MODE == 0 && kind == 3) window_lif_fast<ROLLED, VAR >= 2>(a, a.pops + p, p, lb, dts_sm, xs_sm);
 	else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
 		if (kind == 0) window_neurons<MODE, false, false>(a, a.pops + p, p, lb);
@@ -1697,7 +1742,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_neurons(const __grid_constan
 	__shared__ float dts_sm[kMaxWindow];
 	for (int k = threadIdx.x; k < w.K; k += blockDim.x) dts_sm[k] = b.dts[k];
 	__syncthreads();
-	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_fast(w, b.pops + p, p, lb, dts_sm);
+	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_fast<false, false>(w, b.pops + p, p, lb, dts_sm, nullptr);
 	else if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
 	else if (!ONLY_FAST) window_neurons<MODE, false, false>(w, b.pops + p, p, lb);
 }
@@ -1784,11 +1829,14 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
 	if (a.mode == 0) {
-		if (only_fast) k_neurons<0, true><<<nblocks, kThreads, 0, stream>>>(a);
-		else k_neurons<0, false><<<nblocks, kThreads, 0, stream>>>(a);
+		if (!only_fast) k_neurons<0, false, 0><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 1) k_neurons<0, true, 1><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 2) k_neurons<0, true, 2><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 3) k_neurons<0, true, 3><<<nblocks, kThreads, 0, stream>>>(a);
+		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
-		if (only_fast) k_neurons<1, true><<<nblocks, kThreads, 0, stream>>>(a);
-		else k_neurons<1, false><<<nblocks, kThreads, 0, stream>>>(a);
+		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
+		else k_neurons<1, false, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	}
 	return cudaGetLastError();
 }

@@ -331,6 +331,20 @@ def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threa
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3])
+def test_neuron_variants_match_reference(engine, variant):
+    """Every LIF window variant of the neuron update (unrolled or rolled steps, per-lane or
+    warp-uniform count replay) gives the reference's raster and V bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    net.set_tuning(neuron_variant=variant)
+    counts, idx = _raster_flat(net.run_record(steps))
+    assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
 def test_retuning_mid_run_keeps_results(engine):
     """Switching tile size, threads and parts between steps (including between overwritten and
     accumulated input slots) leaves the raster and state bit-exact."""
