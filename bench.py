@@ -55,7 +55,8 @@ DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
                    7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
                    9: "k_deliver_staged<4 in flight>", 10: "k_deliver_staged_vec<2 sub-rows, 4 blocks>",
-                   11: "k_deliver_staged_vec<4 sub-rows, 2 blocks>"}
+                   11: "k_deliver_staged_vec<4 sub-rows, 2 blocks>", 12: "k_deliver_staged_vec<1 sub-row, 8 blocks>",
+                   13: "k_deliver_staged_vec<2 sub-rows, 6 blocks>"}
 
 
 def _dist():

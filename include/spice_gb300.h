@@ -122,8 +122,9 @@ enum {
 	                                   7: as 5 with <= 32 registers (4 x 512 threads per SM),
 	                                   8, 9: 4 lanes per spike, sub-rows staged in shared
 	                                   memory, 2 or 4 sub-rows in flight per lane group,
-	                                   10, 11: as 8, 9 with each sub-row read as aligned
-	                                   16-byte blocks, 64 or 32 targets per load round trip  */
+	                                   10 .. 13: staged sub-rows read as aligned 16-byte
+	                                   blocks; per lane group and load round trip 2 x 64,
+	                                   4 x 32, 1 x 128 or 2 x 96 targets                     */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input

@@ -22,8 +22,8 @@ DEFAULT_CANDIDATES = [
     #  1 thread per spike, 2 warp per spike, 3 thread per spike with 16-byte loads,
     #  4 thread per spike, software-pipelined, 5 / 6 four / eight lanes per spike, 7 as 5 with
     #  at most 32 registers, 8 / 9 four lanes per spike with sub-rows staged in shared memory, two /
-    #  four sub-rows in flight per group, 10 / 11 as 8 / 9 with sub-rows read as aligned 16-byte
-    #  blocks, 64 / 32 targets per round trip)
+    #  four sub-rows in flight per group, 10 / 11 / 12 / 13 as 8 / 9 with sub-rows read as aligned
+    #  16-byte blocks: 2 x 64, 4 x 32, 1 x 128 and 2 x 96 targets per group and round trip)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
@@ -39,6 +39,8 @@ DEFAULT_CANDIDATES = [
     (24 * 1024, 256, 1, 10), (48 * 1024, 512, 1, 10), (80 * 1024, 1024, 1, 10), (96 * 1024, 1024, 1, 10),
     (100 * 1024, 1024, 1, 10), (112 * 1024, 1024, 1, 10), (128 * 1024, 1024, 1, 10), (160 * 1024, 1024, 1, 10),
     (24 * 1024, 256, 1, 11), (48 * 1024, 512, 1, 11), (100 * 1024, 768, 1, 11), (112 * 1024, 768, 1, 11),
+    (100 * 1024, 1024, 1, 12), (112 * 1024, 1024, 1, 12), (128 * 1024, 1024, 1, 12), (160 * 1024, 1024, 1, 12),
+    (48 * 1024, 512, 1, 12), (100 * 1024, 768, 1, 13), (128 * 1024, 768, 1, 13), (160 * 1024, 768, 1, 13),
 ]
 
 

@@ -1103,6 +1103,8 @@ __device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, 
 	int64_t const sigma = a.slot_lo + si;
 	int const stride    = P.ntiles + 1;
 	int const gl        = threadIdx.x & (G - 1);
+	uint32_t const tile_addr = (uint32_t)__cvta_generic_to_shared(tile_sm);
+	uint32_t const mul       = 4u * (uint32_t)width;
 	unsigned long long my_events = 0;
 	for (int cb = P.in_begin; cb < P.in_end; cb += kConnBatch) {
 		__syncthreads();
@@ -1183,20 +1185,25 @@ __device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, 
 					}
 #pragma unroll
 					for (int f = 0; f < SF; f++) {
-						int const word     = c_word[cj[f]];
-						uint32_t const inc = c_inc[cj[f]];
-						float const w      = c_w[cj[f]];
+						// shared-memory byte address of target d: abase + d * mul (32-bit wrap-around)
+						uint32_t const abase = tile_addr + 4u * (uint32_t)(c_word[cj[f]] - tbase * width);
+						uint32_t const inc   = c_inc[cj[f]];
+						float const w        = c_w[cj[f]];
 #pragma unroll
 						for (int u = 0; u < U; u++) {
-							int const x0 = (o + u * G) * 4;  // index of the block's first target
-							int const d[4] = {v[f][u].x, v[f][u].y, v[f][u].z, v[f][u].w};
+							int const ob = o + u * G;
+							if (ob < nbk[f]) {  // the block holds targets [cl, ch) of the sub-row (cl <= 3, ch >= 1)
+								int const cl    = lo[f] - 4 * ob, ch = hi[f] - 4 * ob;
+								unsigned const m = (0xFu << max(cl, 0)) & (0xFu >> max(4 - ch, 0));
+								int const d[4]   = {v[f][u].x, v[f][u].y, v[f][u].z, v[f][u].w};
 #pragma unroll
-							for (int c = 0; c < 4; c++)
-								if (x0 + c >= lo[f] && x0 + c < hi[f]) {
-									int const li = (d[c] - tbase) * width + word;
-									if (MODE == 0) atomicAdd(tile_sm + li, inc);
-									else atomicAdd(reinterpret_cast<float*>(tile_sm) + li, w);
-								}
+								for (int c = 0; c < 4; c++)
+									if (m & (1u << c)) {
+										uint32_t const addr = abase + (uint32_t)d[c] * mul;
+										if (MODE == 0) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(inc) : "memory");
+										else asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(addr), "f"(w) : "memory");
+									}
+							}
 						}
 					}
 				}
@@ -1338,7 +1345,7 @@ __global__ void k_deliver_staged(const __grid_constant__ DeliverArgs a) {
 }
 
 template <int MODE, int SF, int U>
-__global__ void __launch_bounds__(SF > 2 ? 768 : 1024, 1) k_deliver_staged_vec(const __grid_constant__ DeliverArgs a) {
+__global__ void __launch_bounds__(SF > 2 || SF * U > 8 ? 768 : 1024, 1) k_deliver_staged_vec(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item(a);
 	deliver_staged_vec<MODE, SF, U>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
@@ -1777,7 +1784,9 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else if (ALGO == 8) deliver_staged<MODE, 2>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 9) deliver_staged<MODE, 4>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 10) deliver_staged_vec<MODE, 2, 4>(a, P, t, (int)blockIdx.y, part);
-	else deliver_staged_vec<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 11) deliver_staged_vec<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 12) deliver_staged_vec<MODE, 1, 8>(a, P, t, (int)blockIdx.y, part);
+	else deliver_staged_vec<MODE, 2, 6>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -1866,7 +1875,9 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 	                       (void const*)k_deliver_staged<0, 2>,  (void const*)k_deliver_staged<1, 2>,
 	                       (void const*)k_deliver_staged<0, 4>,  (void const*)k_deliver_staged<1, 4>,
 	                       (void const*)k_deliver_staged_vec<0, 2, 4>, (void const*)k_deliver_staged_vec<1, 2, 4>,
-	                       (void const*)k_deliver_staged_vec<0, 4, 2>, (void const*)k_deliver_staged_vec<1, 4, 2>};
+	                       (void const*)k_deliver_staged_vec<0, 4, 2>, (void const*)k_deliver_staged_vec<1, 4, 2>,
+	                       (void const*)k_deliver_staged_vec<0, 1, 8>, (void const*)k_deliver_staged_vec<1, 1, 8>,
+	                       (void const*)k_deliver_staged_vec<0, 2, 6>, (void const*)k_deliver_staged_vec<1, 2, 6>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -1901,6 +1912,10 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		case 21: k_deliver_staged_vec<1, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 22: k_deliver_staged_vec<0, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 23: k_deliver_staged_vec<1, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 24: k_deliver_staged_vec<0, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 25: k_deliver_staged_vec<1, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 26: k_deliver_staged_vec<0, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 27: k_deliver_staged_vec<1, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 	}
 	return cudaGetLastError();
 }
@@ -1965,7 +1980,9 @@ void const* batch_deliver_fn(BatchArgs const& b) {
 	                       (void const*)k_batch_deliver<0, 8>, (void const*)k_batch_deliver<1, 8>,
 	                       (void const*)k_batch_deliver<0, 9>, (void const*)k_batch_deliver<1, 9>,
 	                       (void const*)k_batch_deliver<0, 10>, (void const*)k_batch_deliver<1, 10>,
-	                       (void const*)k_batch_deliver<0, 11>, (void const*)k_batch_deliver<1, 11>};
+	                       (void const*)k_batch_deliver<0, 11>, (void const*)k_batch_deliver<1, 11>,
+	                       (void const*)k_batch_deliver<0, 12>, (void const*)k_batch_deliver<1, 12>,
+	                       (void const*)k_batch_deliver<0, 13>, (void const*)k_batch_deliver<1, 13>};
 	return fns[m];
 }
 }  // namespace
@@ -2006,6 +2023,10 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 21: k_batch_deliver<1, 10><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 22: k_batch_deliver<0, 11><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 23: k_batch_deliver<1, 11><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 24: k_batch_deliver<0, 12><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 25: k_batch_deliver<1, 12><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 26: k_batch_deliver<0, 13><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 27: k_batch_deliver<1, 13><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
 	return cudaGetLastError();
 }

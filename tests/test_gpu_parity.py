@@ -316,6 +316,8 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
     (8, 112 * 1024, 1024, 1), (9, 100 * 1024, 1024, 1), (9, 8192, 128, 2),
     (10, 100 * 1024, 1024, 1), (10, 24 * 1024, 256, 1), (10, 4096, 64, 3), (10, 180 * 1024, 1024, 2),
     (11, 100 * 1024, 1024, 1), (11, 8192, 128, 2), (11, 48 * 1024, 512, 1),
+    (12, 100 * 1024, 1024, 1), (12, 4096, 64, 3), (12, 24 * 1024, 256, 2),
+    (13, 100 * 1024, 768, 1), (13, 8192, 128, 2),
 ])
 def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
     """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
