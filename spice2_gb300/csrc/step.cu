@@ -1087,50 +1087,85 @@ __device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, 
 	__shared__ const int32_t* c_lst[kConnBatch];
 	__shared__ const int64_t* c_bnd[kConnBatch];
 	__shared__ const int4* c_nb[kConnBatch];
+	__shared__ uint32_t c_abase[kConnBatch];
 	__shared__ uint32_t c_inc[kConnBatch];
-	__shared__ int c_word[kConnBatch];
 	__shared__ float c_w[kConnBatch];
 	__shared__ int s_nc, s_touched, s_next;
 	int const tbase = t * P.tile;
 	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
 	int const width = MODE == 0 ? P.W : P.F;
 	int const words = tn * width;
-	for (int i = threadIdx.x; i < words; i += blockDim.x) tile_sm[i] = 0;
-	if (threadIdx.x == 0) {
-		ev_block  = 0;
-		s_touched = 0;
-	}
+	int const lane  = threadIdx.x & 31;
 	int64_t const sigma = a.slot_lo + si;
 	int const stride    = P.ntiles + 1;
 	int const gl        = threadIdx.x & (G - 1);
 	uint32_t const tile_addr = (uint32_t)__cvta_generic_to_shared(tile_sm);
 	uint32_t const mul       = 4u * (uint32_t)width;
+	if (threadIdx.x == 0) {
+		ev_block  = 0;
+		s_touched = 0;
+	}
+	bool zeroed = false;
 	unsigned long long my_events = 0;
 	for (int cb = P.in_begin; cb < P.in_end; cb += kConnBatch) {
 		__syncthreads();
-		if (threadIdx.x == 0) {
-			int tot = 0, nc = 0;
-			for (int ci = cb; ci < min(cb + kConnBatch, P.in_end); ci++) {
+		if (threadIdx.x < 32) {
+			// warp 0: one lane per connection of the batch -- the connections' fields and spike
+			// counts are loaded in parallel; a warp scan places their spikes in the stage
+			int const ci = cb + lane;
+			int n = 0;
+			bool reach = false;
+			const int32_t* lst = nullptr;
+			const int4* nbp    = nullptr;
+			const int64_t* bnp = nullptr;
+			uint32_t ab = 0, ic = 0;
+			float wt    = 0.0f;
+			if (lane < kConnBatch && ci < P.in_end) {
 				ConnDev const& C = a.conns[ci];
 				int64_t const k  = sigma - (a.t0 + C.delay - 1);
-				if (k < 0 || k >= a.K || C.plastic) continue;
-				s_touched    = 1;
-				int const n  = a.counts[k * a.npop + C.src];
-				int const pp = (n + a.parts - 1) / a.parts;
-				int const lo = min(n, part * pp), hi = min(n, lo + pp);
-				c_lst[nc]  = C.src_list + (a.list_k0 + k) * C.src_size + lo;
-				c_bnd[nc]  = C.bounds + t;
-				c_nb[nc]   = reinterpret_cast<const int4*>(C.nb);
-				c_inc[nc]  = C.inc;
-				c_word[nc] = MODE == 0 ? C.word : C.fslot;
-				c_w[nc]    = C.weight;
-				c_pre[nc]  = tot;
-				tot += hi - lo;
-				nc++;
+				if (k >= 0 && k < a.K && !C.plastic) {
+					int const cnt = a.counts[k * a.npop + C.src];
+					int const pp  = (cnt + a.parts - 1) / a.parts;
+					int const lo  = min(cnt, part * pp);
+					reach         = true;
+					n             = min(cnt, lo + pp) - lo;
+					lst           = C.src_list + (a.list_k0 + k) * C.src_size + lo;
+					nbp           = reinterpret_cast<const int4*>(C.nb);
+					bnp           = C.bounds + t;
+					ab            = tile_addr + 4u * (uint32_t)((MODE == 0 ? C.word : C.fslot) - tbase * width);
+					ic            = C.inc;
+					wt            = C.weight;
+				}
 			}
-			c_pre[nc] = tot;
-			s_nc      = nc;
+			unsigned const rm = __ballot_sync(0xffffffffu, reach);
+			int incl          = n;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				int const o = __shfl_up_sync(0xffffffffu, incl, d);
+				if (lane >= d) incl += o;
+			}
+			int const tot = __shfl_sync(0xffffffffu, incl, 31);
+			if (reach) {  // the reaching connections, compacted to slots 0 .. nc-1 in batch order
+				int const j = __popc(rm & lanemask_lt());
+				c_pre[j]    = incl - n;
+				c_lst[j]    = lst;
+				c_nb[j]     = nbp;
+				c_bnd[j]    = bnp;
+				c_abase[j]  = ab;
+				c_inc[j]    = ic;
+				c_w[j]      = wt;
+				s_touched   = 1;
+			}
+			if (lane == 0) {
+				s_nc            = __popc(rm);
+				c_pre[__popc(rm)] = tot;
+			}
+			if (blockDim.x == 32 && !zeroed)
+				for (int i = lane; i < words; i += 32) tile_sm[i] = 0;
+		} else if (!zeroed) {  // the other warps clear the tile meanwhile
+			for (int i = threadIdx.x - 32; i < words; i += blockDim.x - 32) tile_sm[i] = 0;
 		}
+		zeroed = true;
 		__syncthreads();
 		int const nc    = s_nc;
 		int const total = c_pre[nc];
@@ -1151,59 +1186,58 @@ __device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, 
 			int const nsets = (m + SF - 1) / SF;
 			while (true) {  // a warp takes 32 / G consecutive sets of SF sub-rows per fetch (warp-uniform exit)
 				int base = 0;
-				if ((threadIdx.x & 31) == 0) base = atomicAdd(&s_next, 32 / G);
+				if (lane == 0) base = atomicAdd(&s_next, 32 / G);
 				base = __shfl_sync(0xffffffffu, base, 0);
 				if (base >= nsets) break;
-				int const ps = base + ((threadIdx.x & 31) / G);
-				if (ps >= nsets) continue;
-				int64_t qb[SF];  // first 16-byte block of each sub-row
+				int const ps = base + lane / G;  // lanes past the last set take empty sub-rows
+				const int4* nbf[SF];
 				int lo[SF], hi[SF], nbk[SF], cj[SF];
-				int nbmax = 0;
+				int nbw = 0;
 #pragma unroll
 				for (int f = 0; f < SF; f++) {
 					int const q     = ps * SF + f;
-					int64_t const e = q < m ? st_e0[q] : 0;
-					int const len   = q < m ? st_len[q] : 0;
-					cj[f]           = q < m ? st_c[q] : 0;
-					qb[f]           = e >> 2;
-					lo[f]           = (int)(e & 3);  // targets [lo, hi) of the blocks from qb on
+					bool const ok   = ps < nsets && q < m;
+					int64_t const e = ok ? st_e0[q] : 0;
+					int const len   = ok ? st_len[q] : 0;
+					cj[f]           = ok ? st_c[q] : 0;
+					lo[f]           = (int)(e & 3);  // targets [lo, hi) of the 16-byte blocks from e / 4 on
 					hi[f]           = lo[f] + len;
-					nbk[f]          = len > 0 ? (hi[f] + 3) >> 2 : 0;
-					nbmax           = max(nbmax, nbk[f]);
+					nbk[f]          = (hi[f] + 3) >> 2;
+					if (len == 0) nbk[f] = 0;
+					nbf[f]          = c_nb[cj[f]] + (e >> 2);
+					nbw             = max(nbw, nbk[f]);
 					if (gl == 0) my_events += (unsigned long long)len;
 				}
-				for (int o = gl; o < nbmax; o += G * U) {
+				nbw = __reduce_max_sync(0xffffffffu, nbw);  // the warp's longest sub-row, in blocks
+				for (int o = 0; o < nbw; o += G * U) {
 					int4 v[SF][U];
 #pragma unroll
-					for (int f = 0; f < SF; f++) {
-						const int4* nbf = c_nb[cj[f]] + qb[f];
+					for (int f = 0; f < SF; f++)
 #pragma unroll
 						for (int u = 0; u < U; u++) {
-							int const ob = o + u * G;
-							v[f][u]      = ob < nbk[f] ? __ldg(nbf + ob) : make_int4(0, 0, 0, 0);
+							int const ob = o + u * G + gl;
+							if (ob < nbk[f]) v[f][u] = __ldg(nbf[f] + ob);
 						}
-					}
 #pragma unroll
 					for (int f = 0; f < SF; f++) {
-						// shared-memory byte address of target d: abase + d * mul (32-bit wrap-around)
-						uint32_t const abase = tile_addr + 4u * (uint32_t)(c_word[cj[f]] - tbase * width);
+						uint32_t const abase = c_abase[cj[f]];
 						uint32_t const inc   = c_inc[cj[f]];
 						float const w        = c_w[cj[f]];
 #pragma unroll
 						for (int u = 0; u < U; u++) {
-							int const ob = o + u * G;
-							if (ob < nbk[f]) {  // the block holds targets [cl, ch) of the sub-row (cl <= 3, ch >= 1)
-								int const cl    = lo[f] - 4 * ob, ch = hi[f] - 4 * ob;
-								unsigned const m = (0xFu << max(cl, 0)) & (0xFu >> max(4 - ch, 0));
-								int const d[4]   = {v[f][u].x, v[f][u].y, v[f][u].z, v[f][u].w};
+							if (o + u * G >= nbw) break;  // warp-uniform
+							int const ob = o + u * G + gl;
+							// targets [cl, ch) of this block belong to the sub-row; none when ob >= nbk
+							int const cl     = lo[f] - 4 * ob, ch = hi[f] - 4 * ob;
+							unsigned const m = (0xFu << max(cl, 0)) & (0xFu >> min(max(4 - ch, 0), 4));
+							int const d[4]   = {v[f][u].x, v[f][u].y, v[f][u].z, v[f][u].w};
 #pragma unroll
-								for (int c = 0; c < 4; c++)
-									if (m & (1u << c)) {
-										uint32_t const addr = abase + (uint32_t)d[c] * mul;
-										if (MODE == 0) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(inc) : "memory");
-										else asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(addr), "f"(w) : "memory");
-									}
-							}
+							for (int c = 0; c < 4; c++)
+								if (m & (1u << c)) {
+									uint32_t const addr = abase + (uint32_t)d[c] * mul;
+									if (MODE == 0) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(inc) : "memory");
+									else asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(addr), "f"(w) : "memory");
+								}
 						}
 					}
 				}
