@@ -130,7 +130,9 @@ enum {
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input
 	                                   words in registers, 1 rolled steps over words parked in
 	                                   shared memory, 2 as 1 with warp-uniform count replay,
-	                                   3 as 0 with warp-uniform count replay                  */
+	                                   3 as 0 with warp-uniform count replay, 4 as 1 with
+	                                   branch-free replay and the spike output (bitmap words,
+	                                   list entries) written once per window                 */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

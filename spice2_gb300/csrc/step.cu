@@ -432,6 +432,98 @@ __device__ __forceinline__ void window_lif_fast(A const& a, const PopDev* __rest
 	}
 }
 
+// v += w, n times, one IEEE add at a time, without branches: the adds of the 4-, 2- and 1-blocks of
+// n's low bits are computed and kept by selects (all adds are the same operation, so their grouping
+// does not change the result); counts of 8 or more, rare, loop first.
+__device__ __forceinline__ float add_n_sel(float v, float w, uint32_t n) {
+	for (; n >= 8; n -= 8)
+		v = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, w), w), w), w), w), w), w), w);
+	float const v4 = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, w), w), w), w);
+	v              = (n & 4u) ? v4 : v;
+	float const v2 = __fadd_rn(__fadd_rn(v, w), w);
+	v              = (n & 2u) ? v2 : v;
+	float const v1 = __fadd_rn(v, w);
+	return (n & 1u) ? v1 : v;
+}
+
+// The Brunel LIF window with the spike output deferred to the end of the window (variant 4): the
+// step loop is rolled over input words staged in shared memory, replays counts without branches and
+// only parks each step's warp ballot in shared memory; after the last step the warp writes its
+// bitmap words (one lane per step) and reserves list entries for the steps that had spikes.  Same
+// arithmetic and the same outputs as window_lif_fast (list order within a step is arbitrary in
+// both: reservations are atomic).
+template <class A>
+__device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __restrict__ Pg, int p, int b,
+                                                    const float* dts_sm, uint32_t (*xs_sm)[kThreads],
+                                                    uint32_t (*masks_sm)[16]) {
+	int const N      = (int)Pg->size;
+	int const i      = b * kThreads + threadIdx.x;
+	bool const valid = i < N;
+	int const lane   = threadIdx.x & 31;
+	int const warp   = threadIdx.x >> 5;
+	int const word   = i >> 5;
+	uint32_t* const cnt  = Pg->cnt;
+	bool const zero      = Pg->zero_inputs != 0;
+	float const vthres   = Pg->p0;
+	int32_t const tref   = (int32_t)Pg->p1;
+	float const tminv    = Pg->p2;
+	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
+	float V   = 0;
+	int32_t T = 0;
+	if (valid) {
+		V = Pg->V[i];
+		T = Pg->T[i];
+	}
+	int const D = (int)a.D, Hb = a.Hb;
+	for (int k0 = 0; k0 < a.K; k0 += 16) {
+		int const nk    = min(16, a.K - k0);
+		int const slot0 = (int)((a.slot0 + k0) % D);
+		int sl          = slot0;
+#pragma unroll
+		for (int u = 0; u < 16; u++) {  // asynchronous copies into the thread's own shared-memory column
+			if (valid && u < nk) {
+				unsigned const dst = (unsigned)__cvta_generic_to_shared(&xs_sm[u][threadIdx.x]);
+				asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(cnt + (int64_t)sl * N + i) : "memory");
+			} else {
+				xs_sm[u][threadIdx.x] = 0u;
+			}
+			sl = sl + 1 == D ? 0 : sl + 1;
+		}
+		asm volatile("cp.async.wait_all;" ::: "memory");
+		uint32_t sbits = 0;  // this lane's spikes of the 16 steps
+#pragma unroll 1
+		for (int u = 0; u < nk; u++) {
+			uint32_t const x = xs_sm[u][threadIdx.x];
+			V = add_n_sel(V, w0, x & 0xffffu);
+			V = add_n_sel(V, w1, x >> 16);
+			if (zero && x) cnt[(int64_t)((slot0 + u) % D) * N + i] = 0;
+			bool const spike = lif_update(V, T, __fmaf_rn(-dts_sm[k0 + u], tminv, 1.0f), vthres, tref) && valid;
+			sbits |= (uint32_t)spike << u;
+			unsigned const mask = __ballot_sync(0xffffffffu, spike);
+			if (lane == 0) masks_sm[warp][u] = mask;
+		}
+		__syncwarp();
+		if (lane < nk && word < Pg->nwords)
+			Pg->bits[(int64_t)((a.hslot0 + k0 + lane) % Hb) * Pg->nwords + word] = masks_sm[warp][lane];
+		unsigned const any = __ballot_sync(0xffffffffu, sbits != 0);
+		if (any) {  // list reservations, one per step with spikes
+			for (int u = 0; u < nk; u++) {
+				unsigned const mask = masks_sm[warp][u];
+				if (!mask) continue;
+				int base = 0;
+				if (lane == 0) base = atomicAdd(a.counts + (k0 + u) * a.npop + p, __popc(mask));
+				base = __shfl_sync(0xffffffffu, base, 0);
+				if ((sbits >> u) & 1u) Pg->list[(int64_t)(a.list_k0 + k0 + u) * N + base + __popc(mask & lanemask_lt())] = i;
+			}
+		}
+		__syncwarp();
+	}
+	if (valid) {
+		Pg->V[i] = V;
+		Pg->T[i] = T;
+	}
+}
+
 // One step of a Poisson population (samples/brunel.cpp:27-30): thread c owns neurons
 // [32c, 32c + 32), jumps to draw draw_offset + 32c of the step's stream and draws 32 numbers.
 // The jump XORs the states T^i(s), i < 128, selected by the 128 bits of x^(offset) mod P; the step's
@@ -537,9 +629,10 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 // that each keeps its own register count.
 template <int MODE, bool ONLY_FAST, int VAR>
 __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const __grid_constant__ WindowArgs a) {
-	constexpr bool ROLLED = VAR == 1 || VAR == 2;
+	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR == 4;
 	__shared__ float dts_sm[kMaxWindow];
 	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
+	__shared__ uint32_t masks_sm[VAR == 4 ? kThreads / 32 : 1][16];
 	for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
 	__syncthreads();
 	int const b = blockIdx.x;
@@ -547,7 +640,10 @@ __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const _
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
-	if (MODE == 0 && kind == 3) window_lif_fast<ROLLED, VAR >= 2>(a, a.pops + p, p, lb, dts_sm, xs_sm);
+	if (MODE == 0 && kind == 3) {
+		if (VAR == 4) window_lif_deferred(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
+	}
 	else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
 		if (kind == 0) window_neurons<MODE, false, false>(a, a.pops + p, p, lb);
@@ -1876,6 +1972,7 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 		else if (a.variant == 1) k_neurons<0, true, 1><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 2) k_neurons<0, true, 2><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 3) k_neurons<0, true, 3><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 4) k_neurons<0, true, 4><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
 		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
