@@ -124,7 +124,9 @@ enum {
 	                                   memory, 2 or 4 sub-rows in flight per lane group,
 	                                   10 .. 13: staged sub-rows read as aligned 16-byte
 	                                   blocks; per lane group and load round trip 2 x 64,
-	                                   4 x 32, 1 x 128 or 2 x 96 targets                     */
+	                                   4 x 32, 1 x 128 or 2 x 96 targets,
+	                                   14: as 12 with each sub-row's block pointer and
+	                                   target range precomputed while staging                */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input

@@ -23,7 +23,8 @@ DEFAULT_CANDIDATES = [
     #  4 thread per spike, software-pipelined, 5 / 6 four / eight lanes per spike, 7 as 5 with
     #  at most 32 registers, 8 / 9 four lanes per spike with sub-rows staged in shared memory, two /
     #  four sub-rows in flight per group, 10 / 11 / 12 / 13 as 8 / 9 with sub-rows read as aligned
-    #  16-byte blocks: 2 x 64, 4 x 32, 1 x 128 and 2 x 96 targets per group and round trip)
+    #  16-byte blocks: 2 x 64, 4 x 32, 1 x 128 and 2 x 96 targets per group and round trip, 14 as 12
+    #  with per-sub-row pointers and target ranges precomputed while staging)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
@@ -41,6 +42,8 @@ DEFAULT_CANDIDATES = [
     (24 * 1024, 256, 1, 11), (48 * 1024, 512, 1, 11), (100 * 1024, 768, 1, 11), (112 * 1024, 768, 1, 11),
     (100 * 1024, 1024, 1, 12), (112 * 1024, 1024, 1, 12), (128 * 1024, 1024, 1, 12), (160 * 1024, 1024, 1, 12),
     (48 * 1024, 512, 1, 12), (100 * 1024, 768, 1, 13), (128 * 1024, 768, 1, 13), (160 * 1024, 768, 1, 13),
+    (100 * 1024, 1024, 1, 14), (112 * 1024, 1024, 1, 14), (128 * 1024, 1024, 1, 14), (160 * 1024, 1024, 1, 14),
+    (48 * 1024, 512, 1, 14), (24 * 1024, 256, 1, 14),
 ]
 
 

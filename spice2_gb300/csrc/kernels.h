@@ -61,7 +61,7 @@ cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t n
 constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
 // Delivery work mappings (SPICE_TUNE_DELIVER_ALGO 0 .. kDeliverAlgos - 1), one kernel per mapping
 // and mode.
-constexpr int kDeliverAlgos = 14;
+constexpr int kDeliverAlgos = 15;
 constexpr int kDeliverFns   = 2 * kDeliverAlgos;
 
 struct WindowArgs {

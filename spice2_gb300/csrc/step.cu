@@ -187,7 +187,7 @@ __device__ __forceinline__ void replay_words(PopDev const& P, const uint32_t (&x
 // loop itself is kept rolled and small (instruction-cache friendly).  FAST: every input group adds to
 // V through a 16-bit counter of word 0 (Brunel).
 template <int MODE, bool FAST, bool HIST, class A>
-__device__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p, int b) {
+__device__ __forceinline__ void window_neurons(A const& a, const PopDev* __restrict__ Pg, int p, int b) {
 	int const N       = (int)Pg->size;
 	int const i       = b * kThreads + threadIdx.x;
 	bool const valid  = i < N;
@@ -1348,6 +1348,180 @@ __device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, 
 	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
+// Stores a finished tile like flush_tile; when the ring slot is overwritten by this CTA alone and
+// both ends are 16-byte aligned, in 16-byte vectors.
+template <int MODE, class A>
+__device__ __forceinline__ void flush_tile_vec(A const& a, PopDev const& P, int tbase, int words, int64_t sigma,
+                                               const uint32_t* tile_sm) {
+	int64_t const slot = sigma % a.D;
+	uint32_t* dst      = MODE == 0 ? P.cnt + (slot * P.size + tbase) * P.W
+	                               : reinterpret_cast<uint32_t*>(P.acc + (slot * P.size + tbase) * P.F);
+	if (a.parts == 1 && !P.zero_inputs && (words & 3) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+		uint4* d4       = reinterpret_cast<uint4*>(dst);
+		const uint4* s4 = reinterpret_cast<const uint4*>(tile_sm);
+		for (int i = threadIdx.x; i < (words >> 2); i += blockDim.x) d4[i] = s4[i];
+		return;
+	}
+	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
+// Row mapping (algo 14): as deliver_staged_vec with one sub-row per 4-lane group and 8 blocks per
+// lane, with everything a group needs per sub-row precomputed while staging -- the pointer to its
+// first 16-byte block, its target range within the blocks, and the connection's shared-memory base
+// and increment -- so the fetch loop is a few shared loads, 8 loads at immediate offsets from one
+// pointer, and per target one compare, one multiply-add and one shared-memory reduction.
+constexpr int kStageR = 2048;
+
+template <int MODE, class A>
+__device__ __forceinline__ void deliver_rows(A const& a, PopDev const& P, int t, int si, int part) {
+	constexpr int G = 4, U = 8;
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	__shared__ const int4* st_ptr[kStageR];
+	__shared__ uint32_t st_lohi[kStageR];  // lo (2 bits) | hi << 2: targets [lo, hi) of the blocks from st_ptr
+	__shared__ uint2 st_ai[kStageR];       // shared-memory base of the connection's word, increment (or weight bits)
+	__shared__ int c_pre[kConnBatch + 1];
+	__shared__ const int32_t* c_lst[kConnBatch];
+	__shared__ const int64_t* c_bnd[kConnBatch];
+	__shared__ const int4* c_nb[kConnBatch];
+	__shared__ uint2 c_ai[kConnBatch];
+	__shared__ int s_nc, s_touched, s_next;
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	int const lane  = threadIdx.x & 31;
+	int64_t const sigma = a.slot_lo + si;
+	int const stride    = P.ntiles + 1;
+	int const gl        = threadIdx.x & (G - 1);
+	uint32_t const tile_addr = (uint32_t)__cvta_generic_to_shared(tile_sm);
+	uint32_t const mul       = 4u * (uint32_t)width;
+	if (threadIdx.x == 0) {
+		ev_block  = 0;
+		s_touched = 0;
+	}
+	bool zeroed = false;
+	unsigned long long my_events = 0;
+	for (int cb = P.in_begin; cb < P.in_end; cb += kConnBatch) {
+		__syncthreads();
+		if (threadIdx.x < 32) {  // warp 0: one lane per connection of the batch
+			int const ci = cb + lane;
+			int n = 0;
+			bool reach = false;
+			const int32_t* lst = nullptr;
+			const int4* nbp    = nullptr;
+			const int64_t* bnp = nullptr;
+			uint2 ai           = make_uint2(0u, 0u);
+			if (lane < kConnBatch && ci < P.in_end) {
+				ConnDev const& C = a.conns[ci];
+				int64_t const k  = sigma - (a.t0 + C.delay - 1);
+				if (k >= 0 && k < a.K && !C.plastic) {
+					int const cnt = a.counts[k * a.npop + C.src];
+					int const pp  = (cnt + a.parts - 1) / a.parts;
+					int const lo  = min(cnt, part * pp);
+					reach         = true;
+					n             = min(cnt, lo + pp) - lo;
+					lst           = C.src_list + (a.list_k0 + k) * C.src_size + lo;
+					nbp           = reinterpret_cast<const int4*>(C.nb);
+					bnp           = C.bounds + t;
+					ai.x          = tile_addr + 4u * (uint32_t)((MODE == 0 ? C.word : C.fslot) - tbase * width);
+					ai.y          = MODE == 0 ? C.inc : __float_as_uint(C.weight);
+				}
+			}
+			unsigned const rm = __ballot_sync(0xffffffffu, reach);
+			int incl          = n;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				int const o = __shfl_up_sync(0xffffffffu, incl, d);
+				if (lane >= d) incl += o;
+			}
+			int const tot = __shfl_sync(0xffffffffu, incl, 31);
+			if (reach) {
+				int const j = __popc(rm & lanemask_lt());
+				c_pre[j]    = incl - n;
+				c_lst[j]    = lst;
+				c_nb[j]     = nbp;
+				c_bnd[j]    = bnp;
+				c_ai[j]     = ai;
+				s_touched   = 1;
+			}
+			if (lane == 0) {
+				s_nc              = __popc(rm);
+				c_pre[__popc(rm)] = tot;
+			}
+			if (blockDim.x == 32 && !zeroed)
+				for (int i = lane; i < words; i += 32) tile_sm[i] = 0;
+		} else if (!zeroed) {  // the other warps clear the tile meanwhile (16-byte stores, then the rest)
+			uint4* t4 = reinterpret_cast<uint4*>(tile_sm);
+			for (int i = threadIdx.x - 32; i < (words >> 2); i += blockDim.x - 32) t4[i] = make_uint4(0u, 0u, 0u, 0u);
+			for (int i = (words & ~3) + threadIdx.x - 32; i < words; i += blockDim.x - 32) tile_sm[i] = 0;
+		}
+		zeroed = true;
+		__syncthreads();
+		int const nc    = s_nc;
+		int const total = c_pre[nc];
+		for (int c0 = 0; c0 < total; c0 += kStageR) {
+			int const m = min(kStageR, total - c0);
+			for (int q = threadIdx.x; q < m; q += blockDim.x) {
+				int const g = c0 + q;
+				int j       = 0;
+				while (j + 1 < nc && c_pre[j + 1] <= g) j++;
+				const int64_t* bb = c_bnd[j] + (int64_t)__ldg(c_lst[j] + (g - c_pre[j])) * stride;
+				int64_t const b0  = __ldg(bb);
+				int const len     = (int)(__ldg(bb + 1) - b0);
+				st_ptr[q]         = c_nb[j] + (b0 >> 2);
+				st_lohi[q]        = (uint32_t)(b0 & 3) | ((uint32_t)((int)(b0 & 3) + len) << 2);
+				st_ai[q]          = c_ai[j];
+			}
+			if (threadIdx.x == 0) s_next = 0;
+			__syncthreads();
+			while (true) {  // a warp takes 8 consecutive sub-rows per fetch, one per 4-lane group
+				int base = 0;
+				if (lane == 0) base = atomicAdd(&s_next, 32 / G);
+				base = __shfl_sync(0xffffffffu, base, 0);
+				if (base >= m) break;
+				int const q      = base + lane / G;
+				bool const ok    = q < m;
+				const int4* p    = ok ? st_ptr[q] : nullptr;
+				uint32_t const lh = ok ? st_lohi[q] : 0u;
+				uint2 const ai   = ok ? st_ai[q] : make_uint2(0u, 0u);
+				int const lo     = (int)(lh & 3u), hi = (int)(lh >> 2);
+				int const nb     = hi > lo ? (hi + 3) >> 2 : 0;  // 16-byte blocks of the sub-row
+				if (gl == 0) my_events += (unsigned long long)(hi - lo);
+				int const nbw = __reduce_max_sync(0xffffffffu, nb);
+				for (int o = 0; o < nbw; o += G * U) {
+					const int4* pb = p + (o + gl);
+					int const lim  = nb - (o + gl);       // this lane's block u exists iff 4u < lim
+					int const hr   = hi - 4 * (o + gl);   // target 16u + c of this lane is in the sub-row iff < hr
+					int const lr   = lo - 4 * (o + gl);   // ... and, in block u = 0, iff c >= lr
+					int4 v[U];
+#pragma unroll
+					for (int u = 0; u < U; u++)
+						if (4 * u < lim) v[u] = __ldg(pb + 4 * u);
+#pragma unroll
+					for (int u = 0; u < U; u++) {
+						if (o + 4 * u >= nbw) break;  // warp-uniform
+						int const d[4] = {v[u].x, v[u].y, v[u].z, v[u].w};
+#pragma unroll
+						for (int c = 0; c < 4; c++)
+							if (16 * u + c < hr && (u > 0 || c >= lr)) {
+								uint32_t const addr = ai.x + (uint32_t)d[c] * mul;
+								if (MODE == 0) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(ai.y) : "memory");
+								else asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(addr), "f"(__uint_as_float(ai.y)) : "memory");
+							}
+					}
+				}
+			}
+			__syncthreads();
+		}
+	}
+	__syncthreads();
+	bool const touched = s_touched != 0;
+	add_events(a.events, my_events, &ev_block);
+	if (!touched) return;
+	flush_tile_vec<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
 // Warp-per-spike mapping: a warp takes 32 spikes, loads their sub-row bounds lane-parallel, then
 // streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced loads, 8 in flight per
 // lane, no cross-lane search).
@@ -1478,6 +1652,12 @@ template <int MODE, int SF, int U>
 __global__ void __launch_bounds__(SF > 2 || SF * U > 8 ? 768 : 1024, 1) k_deliver_staged_vec(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item(a);
 	deliver_staged_vec<MODE, SF, U>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(1024, 1) k_deliver_rows(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_rows<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
 // The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
@@ -1870,17 +2050,19 @@ __global__ void __launch_bounds__(kThreads) k_batch_sources(const __grid_constan
 
 // Per-neuron populations of all nets, K steps each with the state in registers.
 template <int MODE, bool ONLY_FAST>
-__global__ void __launch_bounds__(kThreads) k_batch_neurons(const __grid_constant__ BatchArgs b) {
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_batch_neurons(const __grid_constant__ BatchArgs b) {
 	BatchClock const c = *b.clock;
 	int const x        = blockIdx.x;
 	int const p        = find_segment(b.nblk_begin, b.npop, x);
 	int const lb       = x - __ldg(b.nblk_begin + p);
 	WinCtx const w     = batch_win_ctx(b, c);
 	__shared__ float dts_sm[kMaxWindow];
+	__shared__ uint32_t xs_sm[MODE == 0 ? 16 : 1][kThreads];
+	__shared__ uint32_t masks_sm[MODE == 0 ? kThreads / 32 : 1][16];
 	for (int k = threadIdx.x; k < w.K; k += blockDim.x) dts_sm[k] = b.dts[k];
 	__syncthreads();
-	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_fast<false, false>(w, b.pops + p, p, lb, dts_sm, nullptr);
-	else if (__ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
+	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_deferred(w, b.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+	else if (MODE != 0 && __ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
 	else if (!ONLY_FAST) window_neurons<MODE, false, false>(w, b.pops + p, p, lb);
 }
 
@@ -1916,7 +2098,8 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else if (ALGO == 10) deliver_staged_vec<MODE, 2, 4>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 11) deliver_staged_vec<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 12) deliver_staged_vec<MODE, 1, 8>(a, P, t, (int)blockIdx.y, part);
-	else deliver_staged_vec<MODE, 2, 6>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 13) deliver_staged_vec<MODE, 2, 6>(a, P, t, (int)blockIdx.y, part);
+	else deliver_rows<MODE>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -2008,7 +2191,8 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 	                       (void const*)k_deliver_staged_vec<0, 2, 4>, (void const*)k_deliver_staged_vec<1, 2, 4>,
 	                       (void const*)k_deliver_staged_vec<0, 4, 2>, (void const*)k_deliver_staged_vec<1, 4, 2>,
 	                       (void const*)k_deliver_staged_vec<0, 1, 8>, (void const*)k_deliver_staged_vec<1, 1, 8>,
-	                       (void const*)k_deliver_staged_vec<0, 2, 6>, (void const*)k_deliver_staged_vec<1, 2, 6>};
+	                       (void const*)k_deliver_staged_vec<0, 2, 6>, (void const*)k_deliver_staged_vec<1, 2, 6>,
+	                       (void const*)k_deliver_rows<0>,             (void const*)k_deliver_rows<1>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -2047,6 +2231,8 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		case 25: k_deliver_staged_vec<1, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 26: k_deliver_staged_vec<0, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 27: k_deliver_staged_vec<1, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 28: k_deliver_rows<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 29: k_deliver_rows<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 	}
 	return cudaGetLastError();
 }
@@ -2113,7 +2299,8 @@ void const* batch_deliver_fn(BatchArgs const& b) {
 	                       (void const*)k_batch_deliver<0, 10>, (void const*)k_batch_deliver<1, 10>,
 	                       (void const*)k_batch_deliver<0, 11>, (void const*)k_batch_deliver<1, 11>,
 	                       (void const*)k_batch_deliver<0, 12>, (void const*)k_batch_deliver<1, 12>,
-	                       (void const*)k_batch_deliver<0, 13>, (void const*)k_batch_deliver<1, 13>};
+	                       (void const*)k_batch_deliver<0, 13>, (void const*)k_batch_deliver<1, 13>,
+	                       (void const*)k_batch_deliver<0, 14>, (void const*)k_batch_deliver<1, 14>};
 	return fns[m];
 }
 }  // namespace
@@ -2158,6 +2345,8 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 25: k_batch_deliver<1, 12><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 26: k_batch_deliver<0, 13><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 27: k_batch_deliver<1, 13><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 28: k_batch_deliver<0, 14><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 29: k_batch_deliver<1, 14><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
 	return cudaGetLastError();
 }

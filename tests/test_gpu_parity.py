@@ -318,6 +318,7 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
     (11, 100 * 1024, 1024, 1), (11, 8192, 128, 2), (11, 48 * 1024, 512, 1),
     (12, 100 * 1024, 1024, 1), (12, 4096, 64, 3), (12, 24 * 1024, 256, 2),
     (13, 100 * 1024, 768, 1), (13, 8192, 128, 2),
+    (14, 100 * 1024, 1024, 1), (14, 4096, 64, 3), (14, 24 * 1024, 256, 2), (14, 4096, 32, 1), (14, 12 * 1024, 32, 2),
 ])
 def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
     """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
