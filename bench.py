@@ -56,7 +56,9 @@ DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k
                    7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
                    9: "k_deliver_staged<4 in flight>", 10: "k_deliver_staged_vec<2 sub-rows, 4 blocks>",
                    11: "k_deliver_staged_vec<4 sub-rows, 2 blocks>", 12: "k_deliver_staged_vec<1 sub-row, 8 blocks>",
-                   13: "k_deliver_staged_vec<2 sub-rows, 6 blocks>", 14: "k_deliver_rows"}
+                   13: "k_deliver_staged_vec<2 sub-rows, 6 blocks>", 14: "k_deliver_rows",
+                   15: "k_deliver_rows16<1 sub-row>", 16: "k_deliver_rows16<4 sub-rows>",
+                   17: "k_deliver_rows16<2 sub-rows>"}
 
 
 def _dist():

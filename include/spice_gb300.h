@@ -126,7 +126,10 @@ enum {
 	                                   blocks; per lane group and load round trip 2 x 64,
 	                                   4 x 32, 1 x 128 or 2 x 96 targets,
 	                                   14: as 12 with each sub-row's block pointer and
-	                                   target range precomputed while staging                */
+	                                   target range precomputed while staging, 15 .. 17: as
+	                                   14 reading a 16-bit tile-local copy of the targets
+	                                   (2 bytes per synapse, rebuilt with the tiles); per lane
+	                                   group and round trip 1 x 256, 4 x 64, 2 x 128 targets  */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input

@@ -24,7 +24,9 @@ DEFAULT_CANDIDATES = [
     #  at most 32 registers, 8 / 9 four lanes per spike with sub-rows staged in shared memory, two /
     #  four sub-rows in flight per group, 10 / 11 / 12 / 13 as 8 / 9 with sub-rows read as aligned
     #  16-byte blocks: 2 x 64, 4 x 32, 1 x 128 and 2 x 96 targets per group and round trip, 14 as 12
-    #  with per-sub-row pointers and target ranges precomputed while staging)
+    #  with per-sub-row pointers and target ranges precomputed while staging, 15 / 16 / 17 as 14
+    #  reading a 16-bit tile-local copy of the targets, 1 x 256, 4 x 64 and 2 x 128 targets per
+    #  group and round trip)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
@@ -44,6 +46,10 @@ DEFAULT_CANDIDATES = [
     (48 * 1024, 512, 1, 12), (100 * 1024, 768, 1, 13), (128 * 1024, 768, 1, 13), (160 * 1024, 768, 1, 13),
     (100 * 1024, 1024, 1, 14), (112 * 1024, 1024, 1, 14), (128 * 1024, 1024, 1, 14), (160 * 1024, 1024, 1, 14),
     (48 * 1024, 512, 1, 14), (24 * 1024, 256, 1, 14),
+    (100 * 1024, 1024, 1, 15), (112 * 1024, 1024, 1, 15), (128 * 1024, 1024, 1, 15), (160 * 1024, 1024, 1, 15),
+    (180 * 1024, 1024, 1, 15), (48 * 1024, 512, 1, 15), (24 * 1024, 256, 1, 15), (80 * 1024, 1024, 1, 15),
+    (100 * 1024, 768, 1, 16), (112 * 1024, 768, 1, 16), (128 * 1024, 768, 1, 16), (100 * 1024, 512, 1, 16),
+    (100 * 1024, 768, 1, 17), (112 * 1024, 768, 1, 17), (128 * 1024, 768, 1, 17), (48 * 1024, 512, 1, 16),
 ]
 
 

@@ -444,6 +444,7 @@ extern "C" int spice_batch_set_tuning(spice_batch* b, int knob, int64_t value) {
 			for (spice_net* n : b->nets) B_TRY(spice_set_tuning(n, knob, value));
 			b->args.algo = (int)value;
 			drop_graph(b);
+			if (!b->allocs.empty() && compact_algo((int)value)) B_TRY(build(b));  // members' compact targets
 			if (!b->allocs.empty()) B_CUDA_TRY(configure_batch_deliver(b->args));
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:

@@ -95,6 +95,8 @@ struct ConnDev {
 	uint32_t inc;             // 1 << group_shift
 	int F, fslot;             // atomic: sums per neuron, index of this connection's field
 	const int64_t* bounds;    // [src_size][ntiles of dst + 1]: row positions where each tile starts
+	const uint16_t* nb16;     // targets as indices within their tile (nb mod tile), CSR order; built
+	                          // for the compact-target delivery mapping only, else null
 	// plastic synapses (synapse_population.h:27-140); plastic = 0 for fixed_weight
 	int plastic;              // SPICE_SYNAPSE_ISTDP or SPICE_SYNAPSE_COUNT
 	float eta, alpha, cdt;    // iSTDP: learning rate, 2 rho0 tau, dt / tau
@@ -124,6 +126,8 @@ struct Pop {
 struct Conn {
 	ConnDev d;
 	int64_t synapses = 0;
+	uint16_t* nb16    = nullptr;  // owned storage of d.nb16
+	int nb16_tile     = 0;        // tile size d.nb16 was built for
 	bool adj         = false;
 	float w0 = 0, rho0 = 0, tau = 0;  // plastic parameters
 };

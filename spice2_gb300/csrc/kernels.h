@@ -61,7 +61,9 @@ cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t n
 constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
 // Delivery work mappings (SPICE_TUNE_DELIVER_ALGO 0 .. kDeliverAlgos - 1), one kernel per mapping
 // and mode.
-constexpr int kDeliverAlgos = 15;
+constexpr int kDeliverAlgos = 18;
+// the mappings that read ConnDev::nb16
+__host__ __device__ constexpr bool compact_algo(int algo) { return algo >= 15 && algo <= 17; }
 constexpr int kDeliverFns   = 2 * kDeliverAlgos;
 
 struct WindowArgs {
@@ -120,6 +122,7 @@ struct DeliverArgs {
 // One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.
 cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int threads);
 // bounds[s][t] = position in row s of the first target >= t * tile (t = 0..ntiles).
+cudaError_t launch_compact_targets(cudaStream_t stream, const int32_t* nb, int64_t synapses, int tile, uint16_t* nb16);
 cudaError_t launch_tile_bounds(cudaStream_t stream, const int64_t* off, const int32_t* nb, int64_t rows, int tile,
                                int ntiles, int64_t* bounds);
 

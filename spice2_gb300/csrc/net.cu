@@ -182,6 +182,7 @@ extern "C" int spice_net_destroy(spice_net* n) {
 	for (auto& c : n->conns) {
 		cudaFree((void*)c.d.off);
 		cudaFree((void*)c.d.nb);
+		if (c.nb16) cudaFree(c.nb16);
 	}
 	if (n->h_dt) cudaFreeHost(n->h_dt);
 	if (n->h_seeds) cudaFreeHost(n->h_seeds);
@@ -547,6 +548,18 @@ int setup_tiles(spice_net* n, bool first) {
 		CUDA_TRY(launch_tile_bounds(n->stream, d.off, d.nb, d.src_size, T.tile, T.ntiles, bnd));
 		n->launches++;
 		d.bounds = bnd;
+		// the compact-target mapping reads targets as 16-bit indices within their tile
+		if (compact_algo(n->deliver_algo) && !d.plastic && c.synapses > 0 && c.nb16_tile != T.tile) {
+			if (!c.nb16) {  // whole 16-byte blocks plus one, as the target array
+				size_t const bytes = sizeof(uint16_t) * (size_t)((c.synapses + 7) / 8 * 8 + 8);
+				if (cudaMalloc((void**)&c.nb16, bytes) != cudaSuccess)
+					return fail(SPICE_ENOMEM, "cudaMalloc failed for the compact targets (" + std::to_string(bytes) + " bytes)");
+			}
+			CUDA_TRY(launch_compact_targets(n->stream, d.nb, c.synapses, T.tile, c.nb16));
+			n->launches++;
+			c.nb16_tile = T.tile;
+		}
+		d.nb16 = c.nb16_tile == T.tile ? c.nb16 : nullptr;
 	}
 	n->by_dst = by_dst;
 	return SPICE_OK;
@@ -1328,6 +1341,16 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			if (value < 0 || value >= kDeliverAlgos)
 				return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. " + std::to_string(kDeliverAlgos - 1));
 			n->deliver_algo = (int)value;
+			if (n->prepared && compact_algo((int)value)) {  // build the compact targets for the current tiles
+				TRY(setup_tiles(n, false));
+				std::vector<PopDev> hp;
+				for (auto& p : n->pops) hp.push_back(p.d);
+				CUDA_TRY(cudaMemcpy(n->d_pops, hp.data(), sizeof(PopDev) * hp.size(), cudaMemcpyHostToDevice));
+				std::vector<ConnDev> hb;
+				for (int ci : n->by_dst) hb.push_back(n->conns[ci].d);
+				if (!hb.empty())
+					CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
+			}
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
 			if (value < 0 || value > 4) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 4");

@@ -1522,6 +1522,178 @@ __device__ __forceinline__ void deliver_rows(A const& a, PopDev const& P, int t,
 	flush_tile_vec<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
+// Compact-target row mapping (algos 15 .. 17): deliver_rows reading the 16-bit tile-local copy of
+// the targets (ConnDev::nb16), so a sub-row costs half the bytes: one 16-byte block holds 8 targets,
+// a group of 4 lanes takes SF sub-rows per fetch and covers 32 U targets of each per load round trip
+// (all SF sub-rows' loads in flight together), and a target's shared-memory address is the
+// connection's base plus index times the words per neuron.
+template <int MODE, int SF, int U, class A>
+__device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int t, int si, int part) {
+	constexpr int G = 4;
+	extern __shared__ uint32_t tile_sm[];
+	__shared__ unsigned long long ev_block;
+	__shared__ const int4* st_ptr[kStageR];
+	__shared__ uint32_t st_lohi[kStageR];  // lo (3 bits) | hi << 3: targets [lo, hi) of the blocks from st_ptr
+	__shared__ uint2 st_ai[kStageR];       // shared-memory address of the connection's word of index 0, increment
+	__shared__ int c_pre[kConnBatch + 1];
+	__shared__ const int32_t* c_lst[kConnBatch];
+	__shared__ const int64_t* c_bnd[kConnBatch];
+	__shared__ const int4* c_nb[kConnBatch];
+	__shared__ uint2 c_ai[kConnBatch];
+	__shared__ int s_nc, s_touched, s_next;
+	int const tbase = t * P.tile;
+	int const tn    = (int)min((int64_t)P.tile, P.size - tbase);
+	int const width = MODE == 0 ? P.W : P.F;
+	int const words = tn * width;
+	int const lane  = threadIdx.x & 31;
+	int64_t const sigma = a.slot_lo + si;
+	int const stride    = P.ntiles + 1;
+	int const gl        = threadIdx.x & (G - 1);
+	uint32_t const tile_addr = (uint32_t)__cvta_generic_to_shared(tile_sm);
+	uint32_t const mul       = 4u * (uint32_t)width;
+	if (threadIdx.x == 0) {
+		ev_block  = 0;
+		s_touched = 0;
+	}
+	bool zeroed = false;
+	unsigned long long my_events = 0;
+	for (int cb = P.in_begin; cb < P.in_end; cb += kConnBatch) {
+		__syncthreads();
+		if (threadIdx.x < 32) {  // warp 0: one lane per connection of the batch
+			int const ci = cb + lane;
+			int n = 0;
+			bool reach = false;
+			const int32_t* lst = nullptr;
+			const int4* nbp    = nullptr;
+			const int64_t* bnp = nullptr;
+			uint2 ai           = make_uint2(0u, 0u);
+			if (lane < kConnBatch && ci < P.in_end) {
+				ConnDev const& C = a.conns[ci];
+				int64_t const k  = sigma - (a.t0 + C.delay - 1);
+				if (k >= 0 && k < a.K && !C.plastic) {
+					int const cnt = a.counts[k * a.npop + C.src];
+					int const pp  = (cnt + a.parts - 1) / a.parts;
+					int const lo  = min(cnt, part * pp);
+					reach         = true;
+					n             = min(cnt, lo + pp) - lo;
+					lst           = C.src_list + (a.list_k0 + k) * C.src_size + lo;
+					nbp           = reinterpret_cast<const int4*>(C.nb16);
+					bnp           = C.bounds + t;
+					ai.x          = tile_addr + 4u * (uint32_t)(MODE == 0 ? C.word : C.fslot);
+					ai.y          = MODE == 0 ? C.inc : __float_as_uint(C.weight);
+				}
+			}
+			unsigned const rm = __ballot_sync(0xffffffffu, reach);
+			int incl          = n;
+#pragma unroll
+			for (int d = 1; d < 32; d <<= 1) {
+				int const o = __shfl_up_sync(0xffffffffu, incl, d);
+				if (lane >= d) incl += o;
+			}
+			int const tot = __shfl_sync(0xffffffffu, incl, 31);
+			if (reach) {
+				int const j = __popc(rm & lanemask_lt());
+				c_pre[j]    = incl - n;
+				c_lst[j]    = lst;
+				c_nb[j]     = nbp;
+				c_bnd[j]    = bnp;
+				c_ai[j]     = ai;
+				s_touched   = 1;
+			}
+			if (lane == 0) {
+				s_nc              = __popc(rm);
+				c_pre[__popc(rm)] = tot;
+			}
+			if (blockDim.x == 32 && !zeroed)
+				for (int i = lane; i < words; i += 32) tile_sm[i] = 0;
+		} else if (!zeroed) {
+			uint4* t4 = reinterpret_cast<uint4*>(tile_sm);
+			for (int i = threadIdx.x - 32; i < (words >> 2); i += blockDim.x - 32) t4[i] = make_uint4(0u, 0u, 0u, 0u);
+			for (int i = (words & ~3) + threadIdx.x - 32; i < words; i += blockDim.x - 32) tile_sm[i] = 0;
+		}
+		zeroed = true;
+		__syncthreads();
+		int const nc    = s_nc;
+		int const total = c_pre[nc];
+		for (int c0 = 0; c0 < total; c0 += kStageR) {
+			int const m = min(kStageR, total - c0);
+			for (int q = threadIdx.x; q < m; q += blockDim.x) {
+				int const g = c0 + q;
+				int j       = 0;
+				while (j + 1 < nc && c_pre[j + 1] <= g) j++;
+				const int64_t* bb = c_bnd[j] + (int64_t)__ldg(c_lst[j] + (g - c_pre[j])) * stride;
+				int64_t const b0  = __ldg(bb);
+				int const len     = (int)(__ldg(bb + 1) - b0);
+				st_ptr[q]         = c_nb[j] + (b0 >> 3);
+				st_lohi[q]        = (uint32_t)(b0 & 7) | ((uint32_t)((int)(b0 & 7) + len) << 3);
+				st_ai[q]          = c_ai[j];
+			}
+			if (threadIdx.x == 0) s_next = 0;
+			__syncthreads();
+			while (true) {  // a warp takes 8 SF consecutive sub-rows per fetch, SF per 4-lane group
+				int base = 0;
+				if (lane == 0) base = atomicAdd(&s_next, 32 / G * SF);
+				base = __shfl_sync(0xffffffffu, base, 0);
+				if (base >= m) break;
+				const int4* p[SF];
+				uint2 ai[SF];
+				int lo[SF], hi[SF], nb[SF];
+				int nbw = 0;
+#pragma unroll
+				for (int f = 0; f < SF; f++) {
+					int const q       = base + (lane / G) * SF + f;
+					bool const ok     = q < m;
+					p[f]              = ok ? st_ptr[q] : nullptr;
+					uint32_t const lh = ok ? st_lohi[q] : 0u;
+					ai[f]             = ok ? st_ai[q] : make_uint2(0u, 0u);
+					lo[f]             = (int)(lh & 7u);
+					hi[f]             = (int)(lh >> 3);
+					nb[f]             = hi[f] > lo[f] ? (hi[f] + 7) >> 3 : 0;  // 16-byte blocks of the sub-row
+					nbw               = max(nbw, nb[f]);
+					if (gl == 0) my_events += (unsigned long long)(hi[f] - lo[f]);
+				}
+				nbw = __reduce_max_sync(0xffffffffu, nbw);
+				for (int o = 0; o < nbw; o += G * U) {
+					int4 v[SF][U];
+#pragma unroll
+					for (int f = 0; f < SF; f++) {
+						const int4* pb = p[f] + (o + gl);
+						int const lim  = nb[f] - (o + gl);  // this lane's block u exists iff 4u < lim
+#pragma unroll
+						for (int u = 0; u < U; u++)
+							if (4 * u < lim) v[f][u] = __ldg(pb + 4 * u);
+					}
+#pragma unroll
+					for (int f = 0; f < SF; f++) {
+						int const hr = hi[f] - 8 * (o + gl);  // target 32u + c of this lane is in the sub-row iff < hr
+						int const lr = lo[f] - 8 * (o + gl);  // ... and, in block u = 0, iff c >= lr
+#pragma unroll
+						for (int u = 0; u < U; u++) {
+							if (o + 4 * u >= nbw) break;  // warp-uniform
+							uint32_t const x[4] = {(uint32_t)v[f][u].x, (uint32_t)v[f][u].y, (uint32_t)v[f][u].z,
+							                       (uint32_t)v[f][u].w};
+#pragma unroll
+							for (int c = 0; c < 8; c++)
+								if (32 * u + c < hr && (u > 0 || c >= lr)) {
+									uint32_t const d    = (c & 1) ? x[c >> 1] >> 16 : x[c >> 1] & 0xffffu;
+									uint32_t const addr = ai[f].x + d * mul;
+									if (MODE == 0) asm volatile("red.shared.add.u32 [%0], %1;" ::"r"(addr), "r"(ai[f].y) : "memory");
+									else asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(addr), "f"(__uint_as_float(ai[f].y)) : "memory");
+								}
+						}
+					}
+				}
+			}
+			__syncthreads();
+		}
+	}
+	__syncthreads();
+	bool const touched = s_touched != 0;
+	add_events(a.events, my_events, &ev_block);
+	if (!touched) return;
+	flush_tile_vec<MODE>(a, P, tbase, words, sigma, tile_sm);
+}
+
 // Warp-per-spike mapping: a warp takes 32 spikes, loads their sub-row bounds lane-parallel, then
 // streams 8 sub-rows at a time with lanes spanning each sub-row (coalesced loads, 8 in flight per
 // lane, no cross-lane search).
@@ -1660,6 +1832,12 @@ __global__ void __launch_bounds__(1024, 1) k_deliver_rows(const __grid_constant_
 	deliver_rows<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
+template <int MODE, int SF, int U>
+__global__ void __launch_bounds__(SF > 1 ? 768 : 1024, 1) k_deliver_rows16(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item(a);
+	deliver_rows16<MODE, SF, U>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
 // The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
 // resident per SM, for windows whose (slot, tile) items fit one wave at that occupancy.
 template <int MODE>
@@ -1672,6 +1850,12 @@ template <int MODE>
 __global__ void __launch_bounds__(1024) k_deliver_wps(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item(a);
 	deliver_wps<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+}
+
+// Targets as indices within their delivery tile (tile <= 65536 neurons), in CSR order.
+__global__ void k_compact_targets(const int32_t* __restrict__ nb, int64_t synapses, int tile, uint16_t* __restrict__ nb16) {
+	for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < synapses; e += (int64_t)gridDim.x * blockDim.x)
+		nb16[e] = (uint16_t)(nb[e] % tile);
 }
 
 __global__ void k_tile_bounds(const int64_t* __restrict__ off, const int32_t* __restrict__ nb, int64_t rows, int tile,
@@ -2099,7 +2283,10 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else if (ALGO == 11) deliver_staged_vec<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 12) deliver_staged_vec<MODE, 1, 8>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 13) deliver_staged_vec<MODE, 2, 6>(a, P, t, (int)blockIdx.y, part);
-	else deliver_rows<MODE>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 14) deliver_rows<MODE>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 15) deliver_rows16<MODE, 1, 8>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 16) deliver_rows16<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
+	else deliver_rows16<MODE, 2, 4>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -2192,7 +2379,10 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 	                       (void const*)k_deliver_staged_vec<0, 4, 2>, (void const*)k_deliver_staged_vec<1, 4, 2>,
 	                       (void const*)k_deliver_staged_vec<0, 1, 8>, (void const*)k_deliver_staged_vec<1, 1, 8>,
 	                       (void const*)k_deliver_staged_vec<0, 2, 6>, (void const*)k_deliver_staged_vec<1, 2, 6>,
-	                       (void const*)k_deliver_rows<0>,             (void const*)k_deliver_rows<1>};
+	                       (void const*)k_deliver_rows<0>,             (void const*)k_deliver_rows<1>,
+	                       (void const*)k_deliver_rows16<0, 1, 8>,     (void const*)k_deliver_rows16<1, 1, 8>,
+	                       (void const*)k_deliver_rows16<0, 4, 2>,     (void const*)k_deliver_rows16<1, 4, 2>,
+	                       (void const*)k_deliver_rows16<0, 2, 4>,     (void const*)k_deliver_rows16<1, 2, 4>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -2233,7 +2423,19 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		case 27: k_deliver_staged_vec<1, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 28: k_deliver_rows<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 		case 29: k_deliver_rows<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 30: k_deliver_rows16<0, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 31: k_deliver_rows16<1, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 32: k_deliver_rows16<0, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 33: k_deliver_rows16<1, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 34: k_deliver_rows16<0, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
+		case 35: k_deliver_rows16<1, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
 	}
+	return cudaGetLastError();
+}
+
+cudaError_t launch_compact_targets(cudaStream_t stream, const int32_t* nb, int64_t synapses, int tile, uint16_t* nb16) {
+	if (synapses <= 0) return cudaSuccess;
+	k_compact_targets<<<1216, 256, 0, stream>>>(nb, synapses, tile, nb16);
 	return cudaGetLastError();
 }
 
@@ -2300,7 +2502,10 @@ void const* batch_deliver_fn(BatchArgs const& b) {
 	                       (void const*)k_batch_deliver<0, 11>, (void const*)k_batch_deliver<1, 11>,
 	                       (void const*)k_batch_deliver<0, 12>, (void const*)k_batch_deliver<1, 12>,
 	                       (void const*)k_batch_deliver<0, 13>, (void const*)k_batch_deliver<1, 13>,
-	                       (void const*)k_batch_deliver<0, 14>, (void const*)k_batch_deliver<1, 14>};
+	                       (void const*)k_batch_deliver<0, 14>, (void const*)k_batch_deliver<1, 14>,
+	                       (void const*)k_batch_deliver<0, 15>, (void const*)k_batch_deliver<1, 15>,
+	                       (void const*)k_batch_deliver<0, 16>, (void const*)k_batch_deliver<1, 16>,
+	                       (void const*)k_batch_deliver<0, 17>, (void const*)k_batch_deliver<1, 17>};
 	return fns[m];
 }
 }  // namespace
@@ -2347,6 +2552,12 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 27: k_batch_deliver<1, 13><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 28: k_batch_deliver<0, 14><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 29: k_batch_deliver<1, 14><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 30: k_batch_deliver<0, 15><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 31: k_batch_deliver<1, 15><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 32: k_batch_deliver<0, 16><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 33: k_batch_deliver<1, 16><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 34: k_batch_deliver<0, 17><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 35: k_batch_deliver<1, 17><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
 	return cudaGetLastError();
 }

@@ -75,6 +75,8 @@ def test_batch_member_matches_oracle(engine, oracle_lib):
     dict(deliver_algo=0), dict(deliver_algo=2), dict(deliver_algo=3, deliver_threads=512), dict(deliver_algo=4),
     dict(deliver_algo=5), dict(deliver_algo=6, tile_bytes=48 * 1024), dict(deliver_algo=8, deliver_parts=2),
     dict(deliver_algo=9, tile_bytes=100 * 1024, deliver_threads=1024),
+    dict(deliver_algo=12, tile_bytes=48 * 1024, deliver_threads=512), dict(deliver_algo=14, deliver_parts=2),
+    dict(deliver_algo=15, tile_bytes=24 * 1024, deliver_threads=256), dict(deliver_algo=15, deliver_parts=3),
     dict(deliver_parts=2), dict(tile_bytes=4096, deliver_threads=128), dict(overlap_sources=False),
     dict(graph_windows=0),
 ])

@@ -319,6 +319,8 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
     (12, 100 * 1024, 1024, 1), (12, 4096, 64, 3), (12, 24 * 1024, 256, 2),
     (13, 100 * 1024, 768, 1), (13, 8192, 128, 2),
     (14, 100 * 1024, 1024, 1), (14, 4096, 64, 3), (14, 24 * 1024, 256, 2), (14, 4096, 32, 1), (14, 12 * 1024, 32, 2),
+    (15, 100 * 1024, 1024, 1), (15, 4096, 64, 3), (15, 24 * 1024, 256, 2), (15, 4096, 32, 1), (15, 160 * 1024, 1024, 1),
+    (16, 100 * 1024, 768, 1), (16, 4096, 64, 3), (16, 8192, 32, 1), (17, 100 * 1024, 768, 1), (17, 12 * 1024, 128, 2),
 ])
 def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
     """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
@@ -343,6 +345,25 @@ def test_neuron_variants_match_reference(engine, variant):
     net, pops = engine.brunel(N, float(g["p"][0]), seed)
     net.set_tuning(neuron_variant=variant)
     counts, idx = _raster_flat(net.run_record(steps))
+    assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
+def test_compact_targets_follow_retiling(engine):
+    """The 16-bit tile-local target copy (mapping 15) is rebuilt whenever the tile size changes, and
+    switching mappings mid-run keeps the raster and state bit-exact."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    shapes = [(24 * 1024, 256, 1, 15), (8 * 1024, 128, 1, 15), (16 * 1024, 256, 2, 12), (96 * 1024, 1024, 1, 15),
+              (4096, 64, 1, 8)]
+    raster = []
+    for i, (tb, th, parts, algo) in enumerate(shapes):
+        net.set_tuning(tile_bytes=tb, deliver_threads=th, deliver_parts=parts, deliver_algo=algo)
+        n = steps // len(shapes) if i < len(shapes) - 1 else steps - len(raster)
+        raster += list(net.run_record(n))
+    counts, idx = _raster_flat(raster)
     assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
     for k in (1, 2):
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
