@@ -948,8 +948,10 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			da.conns  = n->d_conns_by_dst;
 			da.pops   = n->d_pops;
 			da.counts = wa.counts;
-			da.counts_next     = nullptr;
-			da.counts_next_len = 0;
+			// the other parity's counts (its window is fully delivered) are cleared by the delivery
+			// kernel for the window after this one
+			da.counts_next     = n->d_counts + (size_t)(q ^ 1) * n->K * np;
+			da.counts_next_len = n->K * np;
 			da.list_k0         = q * n->K;
 			da.events = n->d_events;
 			da.slot_lo = n->time + n->dmin - 1;
@@ -980,6 +982,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					}
 			TRY(ev_end(n, slot));
 			n->launches++;
+			CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear
 			if (record) {
 				RasterArgs ra{};
 				ra.t0       = n->time;
@@ -997,9 +1000,6 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				TRY(ev_end(n, slot));
 				n->launches++;
 			}
-			// this parity's counts are consumed: clear them for the window after next
-			CUDA_TRY(cudaMemsetAsync(wa.counts, 0, sizeof(int32_t) * n->K * np, n->stream));
-			CUDA_TRY(cudaEventRecord(n->ev_free[q], n->stream));
 			n->parity ^= 1;
 			n->time += k;
 			rows += k;
