@@ -132,6 +132,10 @@ enum {
 	                                   group and round trip 1 x 256, 4 x 64, 2 x 128 targets  */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
+	SPICE_TUNE_LAUNCH          = 7, /* 1 (default): per window, one grid for the neuron update and
+	                                   the source populations, then the delivery, each launched
+	                                   as the programmatic dependent of the previous kernel;
+	                                   0: sources on a second stream joined by events         */
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input
 	                                   words in registers, 1 rolled steps over words parked in
 	                                   shared memory, 2 as 1 with warp-uniform count replay,

@@ -348,7 +348,8 @@ class snn:
 
     def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
                    deliver_parts: int | None = None, deliver_algo: int | None = None,
-                   overlap_sources: bool | None = None, neuron_variant: int | None = None):
+                   overlap_sources: bool | None = None, neuron_variant: int | None = None,
+                   launch_mode: int | None = None):
         """Delivery launch shape and neuron-update variant (any time between steps); results are
         independent of them."""
         if tile_bytes is not None:
@@ -363,6 +364,8 @@ class snn:
             _check(lib().spice_set_tuning(self._h, 4, int(bool(overlap_sources))))
         if neuron_variant is not None:
             _check(lib().spice_set_tuning(self._h, 6, int(neuron_variant)))
+        if launch_mode is not None:
+            _check(lib().spice_set_tuning(self._h, 7, int(launch_mode)))
 
     # stepping
     def step(self):

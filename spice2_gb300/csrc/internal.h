@@ -204,6 +204,7 @@ struct spice_net {
 	int deliver_algo = 1;            // delivery work mapping (tunable)
 	int overlap_sources = 1;         // source kernels on their own stream (tunable)
 	int neuron_variant  = 0;         // LIF window variant of the neuron update (tunable)
+	int launch_mode     = 1;         // 1: neurons and sources in one grid, programmatic dependent launches
 	int dmin = 1, dmax = 1;          // connection delays in steps
 	bool plastic = false;            // any plastic connection (windows of one step)
 };

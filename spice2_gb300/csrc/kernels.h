@@ -91,6 +91,10 @@ struct WindowArgs {
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
 };
 cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks);
+// The neuron blocks of `a` and the source blocks of `s` in one grid; pdl: launched as the
+// programmatic dependent of the stream's previous kernel.
+cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks, WindowArgs const& s, int nsrc_blocks,
+                          bool pdl);
 cudaError_t launch_sources(cudaStream_t stream, WindowArgs const& a, int nblocks);
 
 struct DeliverArgs {
@@ -107,6 +111,7 @@ struct DeliverArgs {
 	int counts_next_len;
 	unsigned long long* events;
 	int64_t slot_lo;         // first input slot the window's spikes reach: t0 + dmin - 1
+	int pdl;                 // launched as the programmatic dependent of the stream's previous kernel
 	int nslots;              // K + dmax - dmin
 	int ntiles_total;
 	int tile_begin[kMaxPops + 1];  // prefix over populations of their tile counts

@@ -914,7 +914,15 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			for (auto const& P : n->pops)
 				if (P.d.model == USER) (P.stateful ? user_st : user_src) = true;
 			bool const any_src = nbs > 0 || user_src;
-			if (any_src) {
+			// one stream, one grid for neurons and sources, each launch the programmatic dependent
+			// of the previous one (its CTAs wait on the device instead of being launched after it)
+			bool const fused = n->launch_mode == 1 && !user_src && !user_st && !n->plastic;
+			if (fused) {
+				TRY(ev_begin(n, 0, &slot));
+				CUDA_TRY(launch_window(n->stream, wa, nb, ws, nbs, true));
+				TRY(ev_end(n, slot));
+				if (nb + nbs > 0) n->launches++;
+			} else if (any_src) {
 				// sources of this window may start once the lists of this parity are free
 				CUDA_TRY(cudaStreamWaitEvent(ss, n->ev_free[q], 0));
 				TRY(ev_begin(n, 3, &slot, ss));
@@ -926,18 +934,20 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				TRY(ev_end(n, slot, ss));
 				CUDA_TRY(cudaEventRecord(n->ev_src[q], ss));
 			}
-			TRY(ev_begin(n, 0, &slot));
-			CUDA_TRY(launch_neurons(n->stream, wa, nb));
-			if (user_st) TRY(launch_user_pops(n, wa, j, true, false, n->stream));
-			TRY(ev_end(n, slot));
-			if (nb > 0) n->launches++;
+			if (!fused) {
+				TRY(ev_begin(n, 0, &slot));
+				CUDA_TRY(launch_neurons(n->stream, wa, nb));
+				if (user_st) TRY(launch_user_pops(n, wa, j, true, false, n->stream));
+				TRY(ev_end(n, slot));
+				if (nb > 0) n->launches++;
+			}
 			if (n->plastic && n->time % 64 == 0)  // snn.cpp:17-19 (windows are one step long)
 				for (auto const& c : n->conns)
 					if (c.d.plastic) {
 						CUDA_TRY(launch_plastic_update_all(n->stream, c.d, n->time));
 						n->launches++;
 					}
-			if (any_src) CUDA_TRY(cudaStreamWaitEvent(n->stream, n->ev_src[q], 0));
+			if (any_src && !fused) CUDA_TRY(cudaStreamWaitEvent(n->stream, n->ev_src[q], 0));
 			DeliverArgs da{};
 			da.t0     = n->time;
 			da.K      = k;
@@ -968,6 +978,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			da.smem_bytes     = std::max(smem, 4);
 			da.parts          = n->deliver_parts;
 			da.algo           = n->deliver_algo;
+			da.pdl            = fused ? 1 : 0;
 			TRY(ev_begin(n, 1, &slot));
 			CUDA_TRY(launch_deliver(n->stream, da, n->deliver_threads));
 			if (n->plastic)  // spikes of age d - 1 (snn.cpp:21-25), from the source's bitmap ring
@@ -982,7 +993,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					}
 			TRY(ev_end(n, slot));
 			n->launches++;
-			CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear
+			if (!fused) CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear
 			if (record) {
 				RasterArgs ra{};
 				ra.t0       = n->time;
@@ -1351,6 +1362,15 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 				if (!hb.empty())
 					CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
 			}
+			return SPICE_OK;
+		case SPICE_TUNE_LAUNCH:
+			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "launch mode must be 0 or 1");
+			if (n->prepared && n->launch_mode != (int)value) {  // the streams hand over at a quiet point
+				CUDA_TRY(cudaStreamSynchronize(n->stream));
+				if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
+				for (int q = 0; q < 2; q++) CUDA_TRY(cudaEventRecord(n->ev_free[q], n->stream));
+			}
+			n->launch_mode = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
 			if (value < 0 || value > 4) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 4");

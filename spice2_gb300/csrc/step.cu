@@ -623,28 +623,23 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 	if (threadIdx.x == 0) a.counts[k * a.npop + p] = n;
 }
 
-// Per-neuron populations: one thread per neuron, K steps with the state in registers.
-// ONLY_FAST: every population of the launch takes the FAST path, so the generic input replay is
-// compiled out (fewer registers).  VAR: the LIF window variant (window_lif_fast), one kernel each so
-// that each keeps its own register count.
+// One CTA of the neuron update (block b of the window's neuron blocks).
 template <int MODE, bool ONLY_FAST, int VAR>
-__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const __grid_constant__ WindowArgs a) {
+__device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR == 4;
 	__shared__ float dts_sm[kMaxWindow];
 	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
 	__shared__ uint32_t masks_sm[VAR == 4 ? kThreads / 32 : 1][16];
 	for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
 	__syncthreads();
-	int const b = blockIdx.x;
-	int p       = 0;
+	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
 	if (MODE == 0 && kind == 3) {
 		if (VAR == 4) window_lif_deferred(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
-	}
-	else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
+	} else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
 		if (kind == 0) window_neurons<MODE, false, false>(a, a.pops + p, p, lb);
 		else if (kind == 3 + kHistKind) window_neurons<MODE, true, true>(a, a.pops + p, p, lb);
@@ -652,17 +647,47 @@ __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const _
 	}
 }
 
+// Per-neuron populations: one thread per neuron, K steps with the state in registers.
+// ONLY_FAST: every population of the launch takes the FAST path, so the generic input replay is
+// compiled out (fewer registers).  VAR: the LIF window variant (window_lif_fast), one kernel each so
+// that each keeps its own register count.
+template <int MODE, bool ONLY_FAST, int VAR>
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const __grid_constant__ WindowArgs a) {
+	neurons_block<MODE, ONLY_FAST, VAR>(a, (int)blockIdx.x);
+}
+
 // Populations without inputs (Poisson, external trains): one CTA per (step, chunk).  They depend on
 // nothing but the step's random stream, so they run on a second stream, overlapped with the
 // neuron update and the delivery of the previous window.
-__global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ WindowArgs a) {
+__device__ __forceinline__ void sources_block(WindowArgs const& a, int b) {
 	__shared__ int red[kThreads / 32 + 1];
-	int const b = blockIdx.x;
-	int p       = 0;
+	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb = b - a.blk_begin[p];
 	if (a.blk_kind[p] == 1) window_poisson(a, a.pops + p, p, lb, a.blk_per_step[p], red);
 	else if (a.blk_kind[p] == 2) window_external(a, a.pops + p, p, lb, a.ext_pos[p]);
+}
+
+__global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ WindowArgs a) {
+	sources_block(a, (int)blockIdx.x);
+}
+
+// Programmatic dependent launch (sm_90+): griddep_wait() returns once the preceding kernel of the
+// stream has completed and its writes are visible (at once when there is no programmatic edge);
+// griddep_launch() lets the following kernel's CTAs be scheduled while this one still runs.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// One window's neuron update and source populations in one grid: blocks [0, nb) are neuron blocks
+// of `a`, the rest source blocks of `s`.  Launched as the programmatic dependent of the previous
+// delivery, so its CTAs are resident, waiting, when that delivery ends.
+template <int MODE, bool ONLY_FAST, int VAR>
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_window(const __grid_constant__ WindowArgs a,
+                                                                       const __grid_constant__ WindowArgs s, int nb) {
+	griddep_wait();
+	griddep_launch();
+	if ((int)blockIdx.x < nb) neurons_block<MODE, ONLY_FAST, VAR>(a, (int)blockIdx.x);
+	else sources_block(s, (int)blockIdx.x - nb);
 }
 
 // Writes a finished shared-memory tile into ring slot sigma mod D: a plain store when this CTA is
@@ -1776,6 +1801,8 @@ struct DeliverItem {
 	int part, si, Q, t;
 };
 __device__ __forceinline__ DeliverItem deliver_item(DeliverArgs const& a) {
+	griddep_wait();
+	griddep_launch();
 	DeliverItem it;
 	it.part    = blockIdx.x % a.parts;
 	int const b = blockIdx.x / a.parts;
@@ -2351,6 +2378,37 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 	return cudaGetLastError();
 }
 
+cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks, WindowArgs const& s, int nsrc_blocks,
+                          bool pdl) {
+	if (nblocks + nsrc_blocks <= 0) return cudaSuccess;
+	bool only_fast = true;
+	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
+	void const* fn = nullptr;
+	if (a.mode == 0) {
+		if (!only_fast) fn = (void const*)k_window<0, false, 0>;
+		else if (a.variant == 1) fn = (void const*)k_window<0, true, 1>;
+		else if (a.variant == 2) fn = (void const*)k_window<0, true, 2>;
+		else if (a.variant == 3) fn = (void const*)k_window<0, true, 3>;
+		else if (a.variant == 4) fn = (void const*)k_window<0, true, 4>;
+		else fn = (void const*)k_window<0, true, 0>;
+	} else {
+		fn = only_fast ? (void const*)k_window<1, true, 0> : (void const*)k_window<1, false, 0>;
+	}
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks));
+	cfg.blockDim         = dim3((unsigned)kThreads);
+	cfg.dynamicSmemBytes = 0;
+	cfg.stream           = stream;
+	cudaLaunchAttribute at[1];
+	at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
+	cfg.attrs    = at;
+	cfg.numAttrs = 1;
+	int nb       = nblocks;
+	void* args[] = {const_cast<WindowArgs*>(&a), const_cast<WindowArgs*>(&s), &nb};
+	return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
 cudaError_t launch_sources(cudaStream_t stream, WindowArgs const& a, int nblocks) {
 	if (nblocks <= 0) return cudaSuccess;
 	k_sources<<<nblocks, kThreads, 0, stream>>>(a);
@@ -2392,44 +2450,19 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 		if (e != cudaSuccess) return e;
 		configured[m] = a.smem_bytes;
 	}
-	switch (m) {
-		case 0: k_deliver<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 1: k_deliver<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 2: k_deliver_tps<0, false><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 3: k_deliver_tps<1, false><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 4: k_deliver_wps<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 5: k_deliver_wps<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 6: k_deliver_tps<0, true><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 7: k_deliver_tps<1, true><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 8: k_deliver_pipe<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 9: k_deliver_pipe<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 10: k_deliver_groups<0, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 11: k_deliver_groups<1, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 12: k_deliver_groups<0, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 13: k_deliver_groups<1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 14: k_deliver_groups_occ<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 15: k_deliver_groups_occ<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 16: k_deliver_staged<0, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 17: k_deliver_staged<1, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 18: k_deliver_staged<0, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 19: k_deliver_staged<1, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 20: k_deliver_staged_vec<0, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 21: k_deliver_staged_vec<1, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 22: k_deliver_staged_vec<0, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 23: k_deliver_staged_vec<1, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 24: k_deliver_staged_vec<0, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 25: k_deliver_staged_vec<1, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 26: k_deliver_staged_vec<0, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 27: k_deliver_staged_vec<1, 2, 6><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 28: k_deliver_rows<0><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 29: k_deliver_rows<1><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 30: k_deliver_rows16<0, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 31: k_deliver_rows16<1, 1, 8><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 32: k_deliver_rows16<0, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 33: k_deliver_rows16<1, 4, 2><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 34: k_deliver_rows16<0, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-		case 35: k_deliver_rows16<1, 2, 4><<<(unsigned)nblocks, threads, a.smem_bytes, stream>>>(a); break;
-	}
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim          = dim3((unsigned)nblocks);
+	cfg.blockDim         = dim3((unsigned)threads);
+	cfg.dynamicSmemBytes = (size_t)a.smem_bytes;
+	cfg.stream           = stream;
+	cudaLaunchAttribute at[1];
+	at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = a.pdl ? 1 : 0;
+	cfg.attrs    = at;
+	cfg.numAttrs = 1;
+	void* args[] = {const_cast<DeliverArgs*>(&a)};
+	cudaError_t const e = cudaLaunchKernelExC(&cfg, fn, args);
+	if (e != cudaSuccess) return e;
 	return cudaGetLastError();
 }
 

@@ -350,6 +350,23 @@ def test_neuron_variants_match_reference(engine, variant):
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_launch_modes_match_reference(engine, mode):
+    """Sources on their own stream (0) or fused with the neuron update into programmatic dependent
+    launches (1), switched mid-run: the reference's raster and V bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    net.set_tuning(launch_mode=mode)
+    r1 = list(net.run_record(steps // 2))
+    net.set_tuning(launch_mode=1 - mode)
+    r2 = list(net.run_record(steps - steps // 2))
+    counts, idx = _raster_flat(r1 + r2)
+    assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
 def test_compact_targets_follow_retiling(engine):
     """The 16-bit tile-local target copy (mapping 15) is rebuilt whenever the tile size changes, and
     switching mappings mid-run keeps the raster and state bit-exact."""
