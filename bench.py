@@ -45,12 +45,18 @@ N_NEURONS, P_CONN, SEED, STEPS_PER_RUN = 500000, 0.002, 1, 2000
 DT = 1e-4
 WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
 # DRAM bytes (read + write) per synaptic event of the delivery kernels measured on this workload:
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch (the 11th window, 11,158,496 events;
-# profiles/k_deliver_groups_brunel_N5e5_p0.002.md, profiles/k_deliver_staged_brunel_N5e5_p0.002.md)
-# divided by its events, keyed by delivery mapping.  The bench's traffic per launch is this figure
+# dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch
+# (profiles/k_deliver_groups_brunel_N5e5_p0.002.md, profiles/k_deliver_staged_brunel_N5e5_p0.002.md,
+# profiles/k_deliver_rows16_k_window_brunel_N5e5_p0.002.md) divided by its events, keyed by delivery
+# mapping.  The bench's traffic per launch is this figure
 # times the launch's mean events (None for a mapping without a capture).
 DELIVER_DRAM_BYTES_PER_EVENT = {5: (62.261504e6 + 1.521152e6) / 11158496,
-                                8: (56.677376e6 + 0.970496e6) / 11158496}
+                                8: (56.677376e6 + 0.970496e6) / 11158496,
+                                # mappings 15-17 read the same 16-bit target copy; measured on 17
+                                # (window 91, 10,415,589 events)
+                                15: (32.342528e6 + 0.064e6) / 10415589,
+                                16: (32.342528e6 + 0.064e6) / 10415589,
+                                17: (32.342528e6 + 0.064e6) / 10415589}
 DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
                    7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
