@@ -26,7 +26,7 @@ DEFAULT_CANDIDATES = [
     #  16-byte blocks: 2 x 64, 4 x 32, 1 x 128 and 2 x 96 targets per group and round trip, 14 as 12
     #  with per-sub-row pointers and target ranges precomputed while staging, 15 / 16 / 17 as 14
     #  reading a 16-bit tile-local copy of the targets, 1 x 256, 4 x 64 and 2 x 128 targets per
-    #  group and round trip)
+    #  group and round trip, 18 / 19 as 15 / 17 storing the finished tile by TMA bulk copies)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
@@ -50,6 +50,8 @@ DEFAULT_CANDIDATES = [
     (180 * 1024, 1024, 1, 15), (48 * 1024, 512, 1, 15), (24 * 1024, 256, 1, 15), (80 * 1024, 1024, 1, 15),
     (100 * 1024, 768, 1, 16), (112 * 1024, 768, 1, 16), (128 * 1024, 768, 1, 16), (100 * 1024, 512, 1, 16),
     (100 * 1024, 768, 1, 17), (112 * 1024, 768, 1, 17), (128 * 1024, 768, 1, 17), (48 * 1024, 512, 1, 16),
+    (100 * 1024, 1024, 1, 18), (112 * 1024, 1024, 1, 18), (128 * 1024, 1024, 1, 18), (100 * 1024, 768, 1, 19),
+    (112 * 1024, 768, 1, 19), (128 * 1024, 768, 1, 19),
 ]
 
 

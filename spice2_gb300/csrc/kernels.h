@@ -61,9 +61,9 @@ cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t n
 constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
 // Delivery work mappings (SPICE_TUNE_DELIVER_ALGO 0 .. kDeliverAlgos - 1), one kernel per mapping
 // and mode.
-constexpr int kDeliverAlgos = 18;
+constexpr int kDeliverAlgos = 20;
 // the mappings that read ConnDev::nb16
-__host__ __device__ constexpr bool compact_algo(int algo) { return algo >= 15 && algo <= 17; }
+__host__ __device__ constexpr bool compact_algo(int algo) { return algo >= 15 && algo <= 19; }
 constexpr int kDeliverFns   = 2 * kDeliverAlgos;
 
 struct WindowArgs {

@@ -1374,14 +1374,37 @@ __device__ __forceinline__ void deliver_staged_vec(A const& a, PopDev const& P, 
 }
 
 // Stores a finished tile like flush_tile; when the ring slot is overwritten by this CTA alone and
-// both ends are 16-byte aligned, in 16-byte vectors.
-template <int MODE, class A>
+// both ends are 16-byte aligned, in 16-byte vectors (TMA: as bulk asynchronous copies).
+template <int MODE, bool TMA, class A>
 __device__ __forceinline__ void flush_tile_vec(A const& a, PopDev const& P, int tbase, int words, int64_t sigma,
                                                const uint32_t* tile_sm) {
 	int64_t const slot = sigma % a.D;
 	uint32_t* dst      = MODE == 0 ? P.cnt + (slot * P.size + tbase) * P.W
 	                               : reinterpret_cast<uint32_t*>(P.acc + (slot * P.size + tbase) * P.F);
 	if (a.parts == 1 && !P.zero_inputs && (words & 3) == 0 && (reinterpret_cast<uintptr_t>(dst) & 15) == 0) {
+		if (TMA) {
+			// bulk copies by the tensor-memory-access unit: the first lane of up to 8 warps each copies
+			// a 16-byte-aligned share, after a proxy fence that orders the CTA's shared-memory adds
+			// (generic proxy) before the copies' reads (async proxy); each issuer waits for its writes
+			int const nw     = min(8, (int)(blockDim.x >> 5));
+			int const w      = threadIdx.x >> 5;
+			int const blocks = words >> 2;  // 16-byte blocks of the tile
+			int const per    = (blocks + nw - 1) / nw;
+			if ((threadIdx.x & 31) == 0 && w < nw) {
+				int const b0 = w * per, b1 = min(blocks, b0 + per);
+				if (b0 < b1) {
+					asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+					for (int c = b0; c < b1; c += 1024) {  // copies of at most 16 KiB
+						uint32_t const src = (uint32_t)__cvta_generic_to_shared(tile_sm + 4 * c);
+						asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;"
+						             ::"l"(dst + 4 * c), "r"(src), "r"((uint32_t)(min(b1, c + 1024) - c) * 16u) : "memory");
+					}
+					asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+					asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+				}
+			}
+			return;
+		}
 		uint4* d4       = reinterpret_cast<uint4*>(dst);
 		const uint4* s4 = reinterpret_cast<const uint4*>(tile_sm);
 		for (int i = threadIdx.x; i < (words >> 2); i += blockDim.x) d4[i] = s4[i];
@@ -1544,7 +1567,7 @@ __device__ __forceinline__ void deliver_rows(A const& a, PopDev const& P, int t,
 	bool const touched = s_touched != 0;
 	add_events(a.events, my_events, &ev_block);
 	if (!touched) return;
-	flush_tile_vec<MODE>(a, P, tbase, words, sigma, tile_sm);
+	flush_tile_vec<MODE, false>(a, P, tbase, words, sigma, tile_sm);
 }
 
 // Compact-target row mapping (algos 15 .. 17): deliver_rows reading the 16-bit tile-local copy of
@@ -1552,7 +1575,7 @@ __device__ __forceinline__ void deliver_rows(A const& a, PopDev const& P, int t,
 // a group of 4 lanes takes SF sub-rows per fetch and covers 32 U targets of each per load round trip
 // (all SF sub-rows' loads in flight together), and a target's shared-memory address is the
 // connection's base plus index times the words per neuron.
-template <int MODE, int SF, int U, class A>
+template <int MODE, int SF, int U, bool TMA, class A>
 __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int t, int si, int part) {
 	constexpr int G = 4;
 	extern __shared__ uint32_t tile_sm[];
@@ -1716,7 +1739,7 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 	bool const touched = s_touched != 0;
 	add_events(a.events, my_events, &ev_block);
 	if (!touched) return;
-	flush_tile_vec<MODE>(a, P, tbase, words, sigma, tile_sm);
+	flush_tile_vec<MODE, TMA>(a, P, tbase, words, sigma, tile_sm);
 }
 
 // Warp-per-spike mapping: a warp takes 32 spikes, loads their sub-row bounds lane-parallel, then
@@ -1859,10 +1882,10 @@ __global__ void __launch_bounds__(1024, 1) k_deliver_rows(const __grid_constant_
 	deliver_rows<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
-template <int MODE, int SF, int U>
+template <int MODE, int SF, int U, bool TMA>
 __global__ void __launch_bounds__(SF > 1 ? 768 : 1024, 1) k_deliver_rows16(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item(a);
-	deliver_rows16<MODE, SF, U>(a, a.pops[it.Q], it.t, it.si, it.part);
+	deliver_rows16<MODE, SF, U, TMA>(a, a.pops[it.Q], it.t, it.si, it.part);
 }
 
 // The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
@@ -2311,9 +2334,11 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else if (ALGO == 12) deliver_staged_vec<MODE, 1, 8>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 13) deliver_staged_vec<MODE, 2, 6>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 14) deliver_rows<MODE>(a, P, t, (int)blockIdx.y, part);
-	else if (ALGO == 15) deliver_rows16<MODE, 1, 8>(a, P, t, (int)blockIdx.y, part);
-	else if (ALGO == 16) deliver_rows16<MODE, 4, 2>(a, P, t, (int)blockIdx.y, part);
-	else deliver_rows16<MODE, 2, 4>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 15) deliver_rows16<MODE, 1, 8, false>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 16) deliver_rows16<MODE, 4, 2, false>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 17) deliver_rows16<MODE, 2, 4, false>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 18) deliver_rows16<MODE, 1, 8, true>(a, P, t, (int)blockIdx.y, part);
+	else deliver_rows16<MODE, 2, 4, true>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -2438,9 +2463,11 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 	                       (void const*)k_deliver_staged_vec<0, 1, 8>, (void const*)k_deliver_staged_vec<1, 1, 8>,
 	                       (void const*)k_deliver_staged_vec<0, 2, 6>, (void const*)k_deliver_staged_vec<1, 2, 6>,
 	                       (void const*)k_deliver_rows<0>,             (void const*)k_deliver_rows<1>,
-	                       (void const*)k_deliver_rows16<0, 1, 8>,     (void const*)k_deliver_rows16<1, 1, 8>,
-	                       (void const*)k_deliver_rows16<0, 4, 2>,     (void const*)k_deliver_rows16<1, 4, 2>,
-	                       (void const*)k_deliver_rows16<0, 2, 4>,     (void const*)k_deliver_rows16<1, 2, 4>};
+	                       (void const*)k_deliver_rows16<0, 1, 8, false>, (void const*)k_deliver_rows16<1, 1, 8, false>,
+	                       (void const*)k_deliver_rows16<0, 4, 2, false>, (void const*)k_deliver_rows16<1, 4, 2, false>,
+	                       (void const*)k_deliver_rows16<0, 2, 4, false>, (void const*)k_deliver_rows16<1, 2, 4, false>,
+	                       (void const*)k_deliver_rows16<0, 1, 8, true>,  (void const*)k_deliver_rows16<1, 1, 8, true>,
+	                       (void const*)k_deliver_rows16<0, 2, 4, true>,  (void const*)k_deliver_rows16<1, 2, 4, true>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -2538,7 +2565,9 @@ void const* batch_deliver_fn(BatchArgs const& b) {
 	                       (void const*)k_batch_deliver<0, 14>, (void const*)k_batch_deliver<1, 14>,
 	                       (void const*)k_batch_deliver<0, 15>, (void const*)k_batch_deliver<1, 15>,
 	                       (void const*)k_batch_deliver<0, 16>, (void const*)k_batch_deliver<1, 16>,
-	                       (void const*)k_batch_deliver<0, 17>, (void const*)k_batch_deliver<1, 17>};
+	                       (void const*)k_batch_deliver<0, 17>, (void const*)k_batch_deliver<1, 17>,
+	                       (void const*)k_batch_deliver<0, 18>, (void const*)k_batch_deliver<1, 18>,
+	                       (void const*)k_batch_deliver<0, 19>, (void const*)k_batch_deliver<1, 19>};
 	return fns[m];
 }
 }  // namespace
@@ -2591,6 +2620,10 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 33: k_batch_deliver<1, 16><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 34: k_batch_deliver<0, 17><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 35: k_batch_deliver<1, 17><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 36: k_batch_deliver<0, 18><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 37: k_batch_deliver<1, 18><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 38: k_batch_deliver<0, 19><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 39: k_batch_deliver<1, 19><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
 	return cudaGetLastError();
 }
