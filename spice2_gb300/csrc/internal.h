@@ -160,6 +160,8 @@ struct spice_net {
 	cudaEvent_t ev_src[2] = {nullptr, nullptr};   // sources of a parity done
 	cudaEvent_t ev_free[2] = {nullptr, nullptr};  // lists/counts of a parity consumed and cleared
 	cudaEvent_t ev_tab = nullptr;        // dt and jump tables of the current chunk written
+	cudaEvent_t ev_chunk[2] = {nullptr, nullptr};  // the last chunk stepped from buffer b has ended
+	int chunk_buf = 0;                   // buffer of the next chunk
 	bool has_sources = false;
 	std::vector<spice_gb300::Pop> pops;
 	std::vector<spice_gb300::Conn> conns;
@@ -169,9 +171,9 @@ struct spice_net {
 	// device-wide buffers
 	unsigned long long* d_events = nullptr;
 	int32_t* d_counts  = nullptr;  // [2][K][npop] spikes per window step and population, per parity
-	float* d_dt        = nullptr;  // [run capacity]
-	spice_gb300::u128* d_seeds = nullptr;  // [run capacity]
-	spice_gb300::u128* d_tables = nullptr;  // [run capacity][16][256] jump tables
+	float* d_dt        = nullptr;  // [2][run capacity]
+	spice_gb300::u128* d_seeds = nullptr;  // [2][run capacity]
+	spice_gb300::u128* d_tables = nullptr;  // [2][run capacity][16][256] jump tables
 	int64_t run_cap    = 0;
 	spice_gb300::PopDev* d_pops   = nullptr;
 	spice_gb300::ConnDev* d_conns = nullptr;
@@ -179,10 +181,13 @@ struct spice_net {
 	float* h_dt        = nullptr;
 	spice_gb300::u128* h_seeds = nullptr;
 	// raster extraction
-	int32_t* d_raster  = nullptr;
-	int64_t raster_cap = 0;
-	int64_t* d_raster_tab = nullptr;  // [steps][npop][2] (offset, count)
-	unsigned long long* d_raster_cursor = nullptr;
+	// spice_run_record: the raster and the per-step spike counts are written by the GPU straight into
+	// mapped pinned host memory (grown on demand), in (step, population) order
+	int32_t* h_raster    = nullptr;  // [raster_cap]
+	int64_t raster_cap   = 0;
+	int64_t* h_rcounts   = nullptr;  // [rcounts_cap]
+	int64_t rcounts_cap  = 0;
+	int64_t* d_raster_base = nullptr;  // [2] raster position of the current / next window
 	int32_t* d_tmp     = nullptr;  // spikes(age) extraction
 	int64_t* d_tmp_n   = nullptr;
 	// profiling

@@ -147,17 +147,22 @@ cudaError_t launch_extract(cudaStream_t stream, const uint32_t* bits, int nwords
 
 // Raster of a window: for k < K and population p, the ascending spikes of step t0 + k are
 // written at an offset taken from *cursor; tab[(row0 + k) * npop + p] = {offset, count}.
+// Raster of one window in (step, population) order: the spikes of step k of population p start at
+// the window's base plus the spike counts of the window's earlier (step, population) pairs.
 struct RasterArgs {
 	int64_t t0;
 	int K;
 	int Hb;
 	int npop;
 	const PopDev* pops;
-	int32_t* out;
+	const int32_t* counts;  // the window's spike counts [K][npop]
+	int64_t* base;          // [2]: raster position of this window (base[parity]) and of the next
+	int parity;
+	int32_t* out;           // raster, capacity entries (mapped host memory)
 	int64_t capacity;
-	unsigned long long* cursor;
-	int64_t* tab;
-	int64_t row0;
+	int64_t* step_counts;   // [rows][npop] spike counts (mapped host memory)
+	int64_t row0;           // row of the window's first step
+	int pdl;                // launched as the programmatic dependent of the stream's previous kernel
 };
 cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a);
 

@@ -10,6 +10,8 @@
 #include <string.h>
 
 #include <algorithm>
+#include <cstring>
+#include <thread>
 #include <cstdio>
 #include <string>
 #include <vector>
@@ -47,6 +49,25 @@ int pre_failed(const char* file_line, const char* cond) {
 	} while (0)
 
 constexpr int64_t kRunCap = 1024;  // steps of dt / seed / jump tables prepared per chunk
+
+// memcpy of a large host buffer, split over a few threads (host memory bandwidth is per core).
+void parallel_copy(void* dst, const void* src, size_t bytes) {
+	constexpr size_t kChunk = size_t(4) << 20;
+	int const nt = (int)std::min<size_t>(8, (bytes + kChunk - 1) / kChunk);
+	if (nt <= 1) {
+		std::memcpy(dst, src, bytes);
+		return;
+	}
+	size_t const per = (bytes / nt + 63) & ~size_t(63);
+	std::vector<std::thread> th;
+	for (int i = 1; i < nt; i++) {
+		size_t const o = per * i;
+		if (o >= bytes) break;
+		th.emplace_back([=] { std::memcpy((char*)dst + o, (const char*)src + o, std::min(per, bytes - o)); });
+	}
+	std::memcpy(dst, src, std::min(per, bytes));
+	for (auto& x : th) x.join();
+}
 
 template <class T>
 int dalloc(spice_net* n, T** p, size_t count, bool zero = true) {
@@ -185,6 +206,8 @@ extern "C" int spice_net_destroy(spice_net* n) {
 		if (c.nb16) cudaFree(c.nb16);
 	}
 	if (n->h_dt) cudaFreeHost(n->h_dt);
+	if (n->h_raster) cudaFreeHost(n->h_raster);
+	if (n->h_rcounts) cudaFreeHost(n->h_rcounts);
 	if (n->h_seeds) cudaFreeHost(n->h_seeds);
 	for (auto e : n->ev_pool) cudaEventDestroy(e);
 	if (n->stream_src) {
@@ -192,6 +215,8 @@ extern "C" int spice_net_destroy(spice_net* n) {
 		cudaStreamDestroy(n->stream_src);
 	}
 	if (n->ev_tab) cudaEventDestroy(n->ev_tab);
+	for (int b = 0; b < 2; b++)
+		if (n->ev_chunk[b]) cudaEventDestroy(n->ev_chunk[b]);
 	for (int q = 0; q < 2; q++) {
 		if (n->ev_src[q]) cudaEventDestroy(n->ev_src[q]);
 		if (n->ev_free[q]) cudaEventDestroy(n->ev_free[q]);
@@ -751,11 +776,16 @@ int prepare(spice_net* n) {
 			CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
 	}
 	n->run_cap = kRunCap;
-	TRY(dalloc(n, &n->d_dt, kRunCap, false));
-	TRY(dalloc(n, &n->d_seeds, kRunCap, false));
-	if (n->total_draws > 0) TRY(dalloc(n, &n->d_tables, (size_t)kRunCap * kJumpTable, false));
-	CUDA_TRY(cudaMallocHost(&n->h_dt, sizeof(float) * kRunCap));
-	CUDA_TRY(cudaMallocHost(&n->h_seeds, sizeof(u128) * kRunCap));
+	// two chunk buffers: the host prepares one chunk while the GPU still steps the previous one
+	TRY(dalloc(n, &n->d_dt, 2 * kRunCap, false));
+	TRY(dalloc(n, &n->d_seeds, 2 * kRunCap, false));
+	if (n->total_draws > 0) TRY(dalloc(n, &n->d_tables, (size_t)2 * kRunCap * kJumpTable, false));
+	CUDA_TRY(cudaMallocHost(&n->h_dt, sizeof(float) * 2 * kRunCap));
+	CUDA_TRY(cudaMallocHost(&n->h_seeds, sizeof(u128) * 2 * kRunCap));
+	for (int b = 0; b < 2; b++) {
+		CUDA_TRY(cudaEventCreateWithFlags(&n->ev_chunk[b], cudaEventDisableTiming));
+		CUDA_TRY(cudaEventRecord(n->ev_chunk[b], n->stream));
+	}
 	int64_t maxN = 1;
 	for (auto& p : n->pops) maxN = std::max(maxN, p.d.size);
 	TRY(dalloc(n, &n->d_tmp, maxN, false));
@@ -793,7 +823,7 @@ spice_user_window user_window(spice_net* n, int pi, WindowArgs const& wa, int64_
 	w.mode       = n->mode;
 	w.D          = wa.D;
 	w.dts        = wa.dts;
-	w.tables     = n->d_tables ? (const void*)(n->d_tables + j * kJumpTable) : nullptr;
+	w.tables     = (const void*)wa.tables;
 	w.chunk_poly = d.chunk_poly;
 	w.draw_offset = d.draw_offset;
 	w.state      = d.ustate;
@@ -841,20 +871,28 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 	TRY(prepare(n));
 	int const np   = (int)n->pops.size();
 	int64_t rows   = 0;
+	int64_t rec_windows = 0;  // recorded windows: parity of the raster base
 	while (steps > 0) {
 		int64_t const chunk = std::min<int64_t>(steps, n->run_cap);
-		// the pinned staging and the device dt / seed / jump-table arrays are about to be rewritten:
-		// nothing of the previous chunk may still read them, on either stream
-		CUDA_TRY(cudaStreamSynchronize(n->stream));
-		CUDA_TRY(cudaStreamSynchronize(n->stream_src));
+		// chunk buffer cb (pinned staging, device dt / seeds / jump tables) was last used by the chunk
+		// before the previous one: wait for that chunk only (its end is recorded on the main stream,
+		// which joins the source stream before every delivery)
+		int const cb = n->chunk_buf;
+		n->chunk_buf ^= 1;
+		CUDA_TRY(cudaEventSynchronize(n->ev_chunk[cb]));
+		float* const h_dt          = n->h_dt + (size_t)cb * kRunCap;
+		u128* const h_seeds        = n->h_seeds + (size_t)cb * kRunCap;
+		float* const d_dt          = n->d_dt + (size_t)cb * kRunCap;
+		u128* const d_seeds        = n->d_seeds + (size_t)cb * kRunCap;
+		u128* const d_tables       = n->d_tables ? n->d_tables + (size_t)cb * kRunCap * kJumpTable : nullptr;
 		for (int64_t j = 0; j < chunk; j++) {
-			n->h_dt[j]    = kahan_next(n);
-			n->h_seeds[j] = seed_next(n);  // xoroshiro64_128p rng(_seed++) (snn.cpp:12)
+			h_dt[j]    = kahan_next(n);
+			h_seeds[j] = seed_next(n);  // xoroshiro64_128p rng(_seed++) (snn.cpp:12)
 		}
-		CUDA_TRY(cudaMemcpyAsync(n->d_dt, n->h_dt, sizeof(float) * chunk, cudaMemcpyHostToDevice, n->stream));
+		CUDA_TRY(cudaMemcpyAsync(d_dt, h_dt, sizeof(float) * chunk, cudaMemcpyHostToDevice, n->stream));
 		if (n->total_draws > 0) {
-			CUDA_TRY(cudaMemcpyAsync(n->d_seeds, n->h_seeds, sizeof(u128) * chunk, cudaMemcpyHostToDevice, n->stream));
-			CUDA_TRY(launch_jump_tables(n->stream, n->d_seeds, chunk, n->d_tables));
+			CUDA_TRY(cudaMemcpyAsync(d_seeds, h_seeds, sizeof(u128) * chunk, cudaMemcpyHostToDevice, n->stream));
+			CUDA_TRY(launch_jump_tables(n->stream, d_seeds, chunk, d_tables));
 			n->launches++;
 		}
 		// the source kernels of this chunk read dt and the jump tables written above
@@ -874,8 +912,8 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			wa.npop    = np;
 			wa.mode    = n->mode;
 			wa.pops    = n->d_pops;
-			wa.dts     = n->d_dt + j;
-			wa.tables  = n->d_tables ? n->d_tables + j * kJumpTable : nullptr;
+			wa.dts     = d_dt + j;
+			wa.tables  = d_tables ? d_tables + j * kJumpTable : nullptr;
 			wa.counts  = n->d_counts + (size_t)q * n->K * np;
 			wa.list_k0 = q * n->K;
 			wa.variant = n->neuron_variant;
@@ -996,16 +1034,19 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			if (!fused) CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear
 			if (record) {
 				RasterArgs ra{};
-				ra.t0       = n->time;
-				ra.K        = k;
-				ra.Hb       = n->Hb;
-				ra.npop     = np;
-				ra.pops     = n->d_pops;
-				ra.out      = n->d_raster;
-				ra.capacity = n->raster_cap;
-				ra.cursor   = n->d_raster_cursor;
-				ra.tab      = n->d_raster_tab;
-				ra.row0     = rows;
+				ra.t0          = n->time;
+				ra.K           = k;
+				ra.Hb          = n->Hb;
+				ra.npop        = np;
+				ra.pops        = n->d_pops;
+				ra.counts      = wa.counts;
+				ra.base        = n->d_raster_base;
+				ra.parity      = (int)(rec_windows++ & 1);
+				ra.out         = n->h_raster;
+				ra.capacity    = n->raster_cap;
+				ra.step_counts = n->h_rcounts;
+				ra.row0        = rows;
+				ra.pdl         = fused ? 1 : 0;
 				TRY(ev_begin(n, 2, &slot));
 				CUDA_TRY(launch_raster(n->stream, ra));
 				TRY(ev_end(n, slot));
@@ -1016,6 +1057,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			rows += k;
 			j += k;
 		}
+		CUDA_TRY(cudaEventRecord(n->ev_chunk[cb], n->stream));
 		steps -= chunk;
 	}
 	if (rows_done_out) *rows_done_out = rows;
@@ -1075,50 +1117,40 @@ extern "C" int spice_run_record(spice_net* n, int64_t steps, int64_t* counts_out
 	if (steps < 0 || capacity < 0) return fail(SPICE_EINVAL, "steps and capacity must be >= 0");
 	TRY(prepare(n));
 	int const np = (int)n->pops.size();
-	// device raster buffers (grown on demand)
-	if (n->raster_cap < capacity || !n->d_raster) {
-		if (n->d_raster) {
-			CUDA_TRY(cudaStreamSynchronize(n->stream));
-			cudaFree(n->d_raster);
-			n->allocations.erase(std::find(n->allocations.begin(), n->allocations.end(), (void*)n->d_raster));
-		}
-		TRY(dalloc(n, &n->d_raster, std::max<int64_t>(capacity, 1), false));
-		n->raster_cap = std::max<int64_t>(capacity, 1);
-	}
-	static thread_local std::vector<int64_t> tab;
-	if (n->d_raster_tab) {
+	// mapped pinned raster buffers (grown on demand; the GPU writes them directly)
+	int64_t const need_counts = std::max<int64_t>(steps * np, 1);
+	if (n->raster_cap < std::max<int64_t>(capacity, 1) || n->rcounts_cap < need_counts) {
 		CUDA_TRY(cudaStreamSynchronize(n->stream));
-		cudaFree(n->d_raster_tab);
-		n->allocations.erase(std::find(n->allocations.begin(), n->allocations.end(), (void*)n->d_raster_tab));
-		n->d_raster_tab = nullptr;
+		if (n->raster_cap < std::max<int64_t>(capacity, 1)) {
+			if (n->h_raster) cudaFreeHost(n->h_raster);
+			n->h_raster   = nullptr;
+			n->raster_cap = 0;
+			CUDA_TRY(cudaHostAlloc((void**)&n->h_raster, sizeof(int32_t) * std::max<int64_t>(capacity, 1), cudaHostAllocMapped));
+			n->raster_cap = std::max<int64_t>(capacity, 1);
+		}
+		if (n->rcounts_cap < need_counts) {
+			if (n->h_rcounts) cudaFreeHost(n->h_rcounts);
+			n->h_rcounts   = nullptr;
+			n->rcounts_cap = 0;
+			CUDA_TRY(cudaHostAlloc((void**)&n->h_rcounts, sizeof(int64_t) * need_counts, cudaHostAllocMapped));
+			n->rcounts_cap = need_counts;
+		}
 	}
-	TRY(dalloc(n, &n->d_raster_tab, (size_t)std::max<int64_t>(steps, 1) * std::max(np, 1) * 2));
-	if (!n->d_raster_cursor) TRY(dalloc(n, &n->d_raster_cursor, 1));
-	CUDA_TRY(cudaMemsetAsync(n->d_raster_cursor, 0, sizeof(unsigned long long), n->stream));
+	if (!n->d_raster_base) TRY(dalloc(n, &n->d_raster_base, 2));
+	CUDA_TRY(cudaMemsetAsync(n->d_raster_base, 0, sizeof(int64_t) * 2, n->stream));
 	int64_t rows = 0;
 	TRY(run_steps(n, steps, true, &rows));
-	unsigned long long total = 0;
-	CUDA_TRY(cudaMemcpyAsync(&total, n->d_raster_cursor, sizeof(total), cudaMemcpyDeviceToHost, n->stream));
-	tab.resize((size_t)steps * np * 2);
-	if (steps * np > 0)
-		CUDA_TRY(cudaMemcpyAsync(tab.data(), n->d_raster_tab, sizeof(int64_t) * tab.size(), cudaMemcpyDeviceToHost,
-		                         n->stream));
+	int64_t base[2] = {0, 0};
+	CUDA_TRY(cudaMemcpyAsync(base, n->d_raster_base, sizeof(base), cudaMemcpyDeviceToHost, n->stream));
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
-	if (total_out) *total_out = (int64_t)total;
-	if ((int64_t)total > capacity)
+	// the raster ends where the window after the last recorded one would start
+	int64_t const total = std::max(base[0], base[1]);
+	if (total_out) *total_out = total;
+	if (total > capacity)
 		return fail(SPICE_EOVERFLOW, "raster needs " + std::to_string(total) + " entries, capacity is " +
 		                                 std::to_string(capacity));
-	static thread_local std::vector<int32_t> flat;
-	flat.resize(total);
-	if (total) CUDA_TRY(cudaMemcpy(flat.data(), n->d_raster, sizeof(int32_t) * total, cudaMemcpyDeviceToHost));
-	int64_t pos = 0;
-	for (int64_t t = 0; t < steps; t++)
-		for (int p = 0; p < np; p++) {
-			int64_t const o = tab[(t * np + p) * 2], c = tab[(t * np + p) * 2 + 1];
-			if (counts_out) counts_out[t * np + p] = c;
-			if (spikes_out && c) memcpy(spikes_out + pos, flat.data() + o, sizeof(int32_t) * c);
-			pos += c;
-		}
+	if (counts_out && steps * np > 0) std::memcpy(counts_out, n->h_rcounts, sizeof(int64_t) * steps * np);
+	if (spikes_out && total > 0) parallel_copy(spikes_out, n->h_raster, sizeof(int32_t) * (size_t)total);
 	return SPICE_OK;
 }
 

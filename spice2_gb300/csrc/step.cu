@@ -2024,21 +2024,25 @@ __global__ void k_extract(const uint32_t* bits, int nwords, int32_t* out, int64_
 }
 
 __global__ void k_raster(const __grid_constant__ RasterArgs a) {
-	__shared__ int64_t total;
-	__shared__ unsigned long long off;
+	griddep_wait();
+	griddep_launch();
+	__shared__ int64_t off;
 	int const k = blockIdx.x / a.npop, p = blockIdx.x % a.npop;
-	PopDev const& P      = a.pops[p];
-	const uint32_t* bits = P.bits + ((a.t0 + k) % a.Hb) * P.nwords;
-	int64_t c            = 0;
-	for (int w = threadIdx.x; w < P.nwords; w += blockDim.x) c += __popc(bits[w]);
-	(void)block_exclusive_scan(c, &total);
+	PopDev const& P = a.pops[p];
 	if (threadIdx.x == 0) {
-		off = atomicAdd(a.cursor, (unsigned long long)total);
-		a.tab[((a.row0 + k) * a.npop + p) * 2 + 0] = (int64_t)off;
-		a.tab[((a.row0 + k) * a.npop + p) * 2 + 1] = total;
+		int64_t o = a.base[a.parity];
+		for (int j = 0; j < k * a.npop + p; j++) o += a.counts[j];
+		off = o;
+		a.step_counts[(a.row0 + k) * a.npop + p] = a.counts[k * a.npop + p];
+		if (blockIdx.x == 0) {  // where the next window's raster starts
+			int64_t tot = 0;
+			for (int j = 0; j < a.K * a.npop; j++) tot += a.counts[j];
+			a.base[a.parity ^ 1] = a.base[a.parity] + tot;
+		}
 	}
 	__syncthreads();
-	(void)extract_bits(bits, P.nwords, a.out, (int64_t)off, a.capacity);
+	const uint32_t* bits = P.bits + ((a.t0 + k) % a.Hb) * P.nwords;
+	(void)extract_bits(bits, P.nwords, a.out, off, a.capacity);
 }
 
 __global__ void k_count_targets(const int32_t* __restrict__ nb, int64_t n, uint32_t* __restrict__ indeg) {
@@ -2643,9 +2647,18 @@ cudaError_t launch_plastic_deliver(cudaStream_t stream, ConnDev const& c, int64_
 }
 
 cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a) {
-	if (a.K <= 0 || a.npop <= 0) return cudaSuccess;
-	k_raster<<<a.K * a.npop, 1024, 0, stream>>>(a);
-	return cudaGetLastError();
+	if (a.K * a.npop <= 0) return cudaSuccess;
+	cudaLaunchConfig_t cfg = {};
+	cfg.gridDim  = dim3((unsigned)(a.K * a.npop));
+	cfg.blockDim = dim3(1024u);
+	cfg.stream   = stream;
+	cudaLaunchAttribute at[1];
+	at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+	at[0].val.programmaticStreamSerializationAllowed = a.pdl ? 1 : 0;
+	cfg.attrs    = at;
+	cfg.numAttrs = 1;
+	void* args[] = {const_cast<RasterArgs*>(&a)};
+	return cudaLaunchKernelExC(&cfg, (void const*)k_raster, args);
 }
 
 }  // namespace spice_gb300
