@@ -91,10 +91,11 @@ struct WindowArgs {
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
 };
 cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks);
-// The neuron blocks of `a` and the source blocks of `s` in one grid; pdl: launched as the
-// programmatic dependent of the stream's previous kernel.
+struct RasterArgs;
+// The neuron blocks of `a`, the source blocks of `s` and (r not null) the raster blocks of `*r` in one
+// grid; pdl: launched as the programmatic dependent of the stream's previous kernel.
 cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks, WindowArgs const& s, int nsrc_blocks,
-                          bool pdl);
+                          RasterArgs const* r, bool pdl);
 cudaError_t launch_sources(cudaStream_t stream, WindowArgs const& a, int nblocks);
 
 struct DeliverArgs {

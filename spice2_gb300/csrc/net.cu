@@ -872,6 +872,10 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 	int const np   = (int)n->pops.size();
 	int64_t rows   = 0;
 	int64_t rec_windows = 0;  // recorded windows: parity of the raster base
+	// fused launches extract a window's raster in the next window's grid; the last one is pending
+	bool raster_pending = false;
+	RasterArgs pending{};
+	int slot_last = -1;
 	while (steps > 0) {
 		int64_t const chunk = std::min<int64_t>(steps, n->run_cap);
 		// chunk buffer cb (pinned staging, device dt / seeds / jump tables) was last used by the chunk
@@ -957,9 +961,10 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			bool const fused = n->launch_mode == 1 && !user_src && !user_st && !n->plastic;
 			if (fused) {
 				TRY(ev_begin(n, 0, &slot));
-				CUDA_TRY(launch_window(n->stream, wa, nb, ws, nbs, true));
+				CUDA_TRY(launch_window(n->stream, wa, nb, ws, nbs, raster_pending ? &pending : nullptr, true));
 				TRY(ev_end(n, slot));
-				if (nb + nbs > 0) n->launches++;
+				if (nb + nbs > 0 || raster_pending) n->launches++;
+				raster_pending = false;
 			} else if (any_src) {
 				// sources of this window may start once the lists of this parity are free
 				CUDA_TRY(cudaStreamWaitEvent(ss, n->ev_free[q], 0));
@@ -1047,18 +1052,30 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				ra.step_counts = n->h_rcounts;
 				ra.row0        = rows;
 				ra.pdl         = fused ? 1 : 0;
-				TRY(ev_begin(n, 2, &slot));
-				CUDA_TRY(launch_raster(n->stream, ra));
-				TRY(ev_end(n, slot));
-				n->launches++;
+				if (fused) {  // extracted by the next window's grid, or after the last window
+					pending        = ra;
+					raster_pending = true;
+				} else {
+					TRY(ev_begin(n, 2, &slot));
+					CUDA_TRY(launch_raster(n->stream, ra));
+					TRY(ev_end(n, slot));
+					n->launches++;
+				}
 			}
 			n->parity ^= 1;
 			n->time += k;
 			rows += k;
 			j += k;
 		}
-		CUDA_TRY(cudaEventRecord(n->ev_chunk[cb], n->stream));
 		steps -= chunk;
+		if (raster_pending && steps == 0) {  // the last window's raster
+			TRY(ev_begin(n, 2, &slot_last));
+			CUDA_TRY(launch_raster(n->stream, pending));
+			TRY(ev_end(n, slot_last));
+			n->launches++;
+			raster_pending = false;
+		}
+		CUDA_TRY(cudaEventRecord(n->ev_chunk[cb], n->stream));
 	}
 	if (rows_done_out) *rows_done_out = rows;
 	return SPICE_OK;

@@ -678,16 +678,23 @@ __global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ Wi
 __device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
-// One window's neuron update and source populations in one grid: blocks [0, nb) are neuron blocks
-// of `a`, the rest source blocks of `s`.  Launched as the programmatic dependent of the previous
-// delivery, so its CTAs are resident, waiting, when that delivery ends.
+// One window's neuron update and source populations in one grid: first (when recording) the
+// raster blocks of the previous window `r`, whose bitmaps and counts are final, then nb neuron
+// blocks of `a`, then the source blocks of `s`.  Launched as the programmatic dependent
+// of the previous delivery, so its CTAs are resident, waiting, when that delivery ends.
+__device__ void raster_block(RasterArgs const& a, int b);
+
 template <int MODE, bool ONLY_FAST, int VAR>
 __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_window(const __grid_constant__ WindowArgs a,
-                                                                       const __grid_constant__ WindowArgs s, int nb) {
+                                                                       const __grid_constant__ WindowArgs s, int nb,
+                                                                       int nsb, const __grid_constant__ RasterArgs r) {
 	griddep_wait();
 	griddep_launch();
-	if ((int)blockIdx.x < nb) neurons_block<MODE, ONLY_FAST, VAR>(a, (int)blockIdx.x);
-	else sources_block(s, (int)blockIdx.x - nb);
+	int const nrb = r.K * r.npop;  // raster blocks first: they start with the first wave
+	int const b   = (int)blockIdx.x;
+	if (b < nrb) raster_block(r, b);  // the previous window's raster
+	else if (b < nrb + nb) neurons_block<MODE, ONLY_FAST, VAR>(a, b - nrb);
+	else sources_block(s, b - nrb - nb);
 }
 
 // Writes a finished shared-memory tile into ring slot sigma mod D: a plain store when this CTA is
@@ -2023,26 +2030,62 @@ __global__ void k_extract(const uint32_t* bits, int nwords, int32_t* out, int64_
 	if (threadIdx.x == 0) *n_out = n;
 }
 
-__global__ void k_raster(const __grid_constant__ RasterArgs a) {
-	griddep_wait();
-	griddep_launch();
+// One (step, population) pair of a window's raster (block b of the window's K npop raster blocks).
+__device__ void raster_block(RasterArgs const& a, int b) {
 	__shared__ int64_t off;
-	int const k = blockIdx.x / a.npop, p = blockIdx.x % a.npop;
+	int const k = b / a.npop, p = b % a.npop;
 	PopDev const& P = a.pops[p];
 	if (threadIdx.x == 0) {
 		int64_t o = a.base[a.parity];
 		for (int j = 0; j < k * a.npop + p; j++) o += a.counts[j];
 		off = o;
 		a.step_counts[(a.row0 + k) * a.npop + p] = a.counts[k * a.npop + p];
-		if (blockIdx.x == 0) {  // where the next window's raster starts
+		if (b == 0) {  // where the next window's raster starts
 			int64_t tot = 0;
 			for (int j = 0; j < a.K * a.npop; j++) tot += a.counts[j];
 			a.base[a.parity ^ 1] = a.base[a.parity] + tot;
 		}
 	}
-	__syncthreads();
+	// each warp extracts a contiguous range of bitmap words: counts first, one block-wide prefix over
+	// the warps, then warp-level scans only
+	__shared__ int64_t warp_cnt[32];
 	const uint32_t* bits = P.bits + ((a.t0 + k) % a.Hb) * P.nwords;
-	(void)extract_bits(bits, P.nwords, a.out, off, a.capacity);
+	int const lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	int const per  = (P.nwords + nw - 1) / nw;
+	int const w0 = min(P.nwords, w * per), w1 = min(P.nwords, w0 + per);
+	int c = 0;
+	for (int i = w0 + lane; i < w1; i += 32) c += __popc(bits[i]);
+	for (int d = 16; d; d >>= 1) c += __shfl_xor_sync(0xffffffffu, c, d);
+	if (lane == 0) warp_cnt[w] = c;
+	__syncthreads();
+	int64_t pos = off;
+	for (int j = 0; j < w; j++) pos += warp_cnt[j];
+	for (int i0 = w0; i0 < w1; i0 += 32) {
+		int const i      = i0 + lane;
+		uint32_t const m = i < w1 ? bits[i] : 0u;
+		int const pc     = __popc(m);
+		int incl         = pc;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			int const o = __shfl_up_sync(0xffffffffu, incl, d);
+			if (lane >= d) incl += o;
+		}
+		int64_t p2 = pos + incl - pc;
+		uint32_t mm = m;
+		while (mm) {
+			int const r = __ffs(mm) - 1;
+			mm &= mm - 1;
+			if (p2 < a.capacity) a.out[p2] = 32 * i + r;
+			p2++;
+		}
+		pos += __shfl_sync(0xffffffffu, incl, 31);
+	}
+}
+
+__global__ void k_raster(const __grid_constant__ RasterArgs a) {
+	griddep_wait();
+	griddep_launch();
+	raster_block(a, (int)blockIdx.x);
 }
 
 __global__ void k_count_targets(const int32_t* __restrict__ nb, int64_t n, uint32_t* __restrict__ indeg) {
@@ -2408,8 +2451,9 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 }
 
 cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks, WindowArgs const& s, int nsrc_blocks,
-                          bool pdl) {
-	if (nblocks + nsrc_blocks <= 0) return cudaSuccess;
+                          RasterArgs const* r, bool pdl) {
+	int const nrb = r ? r->K * r->npop : 0;
+	if (nblocks + nsrc_blocks + nrb <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
 	void const* fn = nullptr;
@@ -2424,7 +2468,7 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 		fn = only_fast ? (void const*)k_window<1, true, 0> : (void const*)k_window<1, false, 0>;
 	}
 	cudaLaunchConfig_t cfg = {};
-	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks));
+	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks + nrb));
 	cfg.blockDim         = dim3((unsigned)kThreads);
 	cfg.dynamicSmemBytes = 0;
 	cfg.stream           = stream;
@@ -2433,8 +2477,10 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
 	cfg.attrs    = at;
 	cfg.numAttrs = 1;
-	int nb       = nblocks;
-	void* args[] = {const_cast<WindowArgs*>(&a), const_cast<WindowArgs*>(&s), &nb};
+	int nb = nblocks, nsb = nsrc_blocks;
+	RasterArgs rr{};
+	if (r) rr = *r;
+	void* args[] = {const_cast<WindowArgs*>(&a), const_cast<WindowArgs*>(&s), &nb, &nsb, &rr};
 	return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
