@@ -143,7 +143,8 @@ enum {
 	                                   shared memory, 2 as 1 with warp-uniform count replay,
 	                                   3 as 0 with warp-uniform count replay, 4 as 1 with
 	                                   branch-free replay and the spike output (bitmap words,
-	                                   list entries) written once per window                 */
+	                                   list entries) written once per window, 5 as 4 with
+	                                   predicated instead of selected adds                    */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

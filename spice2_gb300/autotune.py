@@ -52,6 +52,9 @@ DEFAULT_CANDIDATES = [
     (100 * 1024, 768, 1, 17), (112 * 1024, 768, 1, 17), (128 * 1024, 768, 1, 17), (48 * 1024, 512, 1, 16),
     (100 * 1024, 1024, 1, 18), (112 * 1024, 1024, 1, 18), (128 * 1024, 1024, 1, 18), (100 * 1024, 768, 1, 19),
     (112 * 1024, 768, 1, 19), (128 * 1024, 768, 1, 19),
+    # two CTAs per SM: 50 KiB tiles make 300 (slot, tile) items at Brunel N=5e5, one wave
+    (50 * 1024, 512, 1, 15), (50 * 1024, 512, 1, 17), (50 * 1024, 512, 1, 18), (50 * 1024, 512, 1, 19),
+    (50 * 1024, 384, 1, 17), (56 * 1024, 512, 1, 15), (64 * 1024, 512, 1, 15),
 ]
 
 
@@ -85,7 +88,7 @@ def autotune(net, steps: int = 600, warm: int = 60, candidates=None, verbose: bo
     return {"best": best, "results": results}
 
 
-def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4), verbose: bool = False) -> dict:
+def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4, 5), verbose: bool = False) -> dict:
     """Times the neuron-update kernel of `net` for each LIF window variant (identical results);
     applies and returns the fastest."""
     results = []

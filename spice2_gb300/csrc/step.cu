@@ -446,13 +446,24 @@ __device__ __forceinline__ float add_n_sel(float v, float w, uint32_t n) {
 	return (n & 1u) ? v1 : v;
 }
 
+// As add_n_sel with the 4-, 2- and 1-blocks as predicated adds (one compare per block, the adds on
+// the floating-point pipe) instead of computed-and-selected ones.
+__device__ __forceinline__ float add_n_pred(float v, float w, uint32_t n) {
+	for (; n >= 8; n -= 8)
+		v = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, w), w), w), w), w), w), w), w);
+	if (n & 4u) v = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(v, w), w), w), w);
+	if (n & 2u) v = __fadd_rn(__fadd_rn(v, w), w);
+	if (n & 1u) v = __fadd_rn(v, w);
+	return v;
+}
+
 // The Brunel LIF window with the spike output deferred to the end of the window (variant 4): the
 // step loop is rolled over input words staged in shared memory, replays counts without branches and
 // only parks each step's warp ballot in shared memory; after the last step the warp writes its
 // bitmap words (one lane per step) and reserves list entries for the steps that had spikes.  Same
 // arithmetic and the same outputs as window_lif_fast (list order within a step is arbitrary in
 // both: reservations are atomic).
-template <class A>
+template <bool PRED, class A>
 __device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __restrict__ Pg, int p, int b,
                                                     const float* dts_sm, uint32_t (*xs_sm)[kThreads],
                                                     uint32_t (*masks_sm)[16]) {
@@ -494,8 +505,8 @@ __device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __
 #pragma unroll 1
 		for (int u = 0; u < nk; u++) {
 			uint32_t const x = xs_sm[u][threadIdx.x];
-			V = add_n_sel(V, w0, x & 0xffffu);
-			V = add_n_sel(V, w1, x >> 16);
+			V = PRED ? add_n_pred(V, w0, x & 0xffffu) : add_n_sel(V, w0, x & 0xffffu);
+			V = PRED ? add_n_pred(V, w1, x >> 16) : add_n_sel(V, w1, x >> 16);
 			if (zero && x) cnt[(int64_t)((slot0 + u) % D) * N + i] = 0;
 			bool const spike = lif_update(V, T, __fmaf_rn(-dts_sm[k0 + u], tminv, 1.0f), vthres, tref) && valid;
 			sbits |= (uint32_t)spike << u;
@@ -626,10 +637,10 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 // One CTA of the neuron update (block b of the window's neuron blocks).
 template <int MODE, bool ONLY_FAST, int VAR>
 __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
-	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR == 4;
+	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;
 	__shared__ float dts_sm[kMaxWindow];
 	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
-	__shared__ uint32_t masks_sm[VAR == 4 ? kThreads / 32 : 1][16];
+	__shared__ uint32_t masks_sm[VAR >= 4 ? kThreads / 32 : 1][16];
 	for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
 	__syncthreads();
 	int p = 0;
@@ -637,7 +648,8 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
 	if (MODE == 0 && kind == 3) {
-		if (VAR == 4) window_lif_deferred(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		if (VAR == 4) window_lif_deferred<false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else if (VAR == 5) window_lif_deferred<true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
 	} else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
@@ -684,15 +696,15 @@ __device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.
 // of the previous delivery, so its CTAs are resident, waiting, when that delivery ends.
 __device__ void raster_block(RasterArgs const& a, int b);
 
-template <int MODE, bool ONLY_FAST, int VAR>
+template <int MODE, bool ONLY_FAST, int VAR, bool REC>
 __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_window(const __grid_constant__ WindowArgs a,
                                                                        const __grid_constant__ WindowArgs s, int nb,
                                                                        int nsb, const __grid_constant__ RasterArgs r) {
 	griddep_wait();
 	griddep_launch();
-	int const nrb = r.K * r.npop;  // raster blocks first: they start with the first wave
+	int const nrb = REC ? r.K * r.npop : 0;  // raster blocks first: they start with the first wave
 	int const b   = (int)blockIdx.x;
-	if (b < nrb) raster_block(r, b);  // the previous window's raster
+	if (REC && b < nrb) raster_block(r, b);  // the previous window's raster
 	else if (b < nrb + nb) neurons_block<MODE, ONLY_FAST, VAR>(a, b - nrb);
 	else sources_block(s, b - nrb - nb);
 }
@@ -2342,7 +2354,7 @@ __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_batch_neurons(c
 	__shared__ uint32_t masks_sm[MODE == 0 ? kThreads / 32 : 1][16];
 	for (int k = threadIdx.x; k < w.K; k += blockDim.x) dts_sm[k] = b.dts[k];
 	__syncthreads();
-	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_deferred(w, b.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_deferred<false>(w, b.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 	else if (MODE != 0 && __ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
 	else if (!ONLY_FAST) window_neurons<MODE, false, false>(w, b.pops + p, p, lb);
 }
@@ -2442,6 +2454,7 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 		else if (a.variant == 2) k_neurons<0, true, 2><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 3) k_neurons<0, true, 3><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 4) k_neurons<0, true, 4><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 5) k_neurons<0, true, 5><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
 		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
@@ -2456,17 +2469,19 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	if (nblocks + nsrc_blocks + nrb <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
+	void const* fns[2][8] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
+	                          (void const*)k_window<0, true, 1, false>, (void const*)k_window<0, true, 2, false>,
+	                          (void const*)k_window<0, true, 3, false>, (void const*)k_window<0, true, 4, false>,
+	                          (void const*)k_window<0, true, 5, false>, (void const*)k_window<1, true, 0, false>},
+	                         {(void const*)k_window<0, false, 0, true>, (void const*)k_window<0, true, 0, true>,
+	                          (void const*)k_window<0, true, 1, true>, (void const*)k_window<0, true, 2, true>,
+	                          (void const*)k_window<0, true, 3, true>, (void const*)k_window<0, true, 4, true>,
+	                          (void const*)k_window<0, true, 5, true>, (void const*)k_window<1, true, 0, true>}};
+	void const* fk_atomic_generic[2] = {(void const*)k_window<1, false, 0, false>, (void const*)k_window<1, false, 0, true>};
+	int const rec = nrb > 0 ? 1 : 0;
 	void const* fn = nullptr;
-	if (a.mode == 0) {
-		if (!only_fast) fn = (void const*)k_window<0, false, 0>;
-		else if (a.variant == 1) fn = (void const*)k_window<0, true, 1>;
-		else if (a.variant == 2) fn = (void const*)k_window<0, true, 2>;
-		else if (a.variant == 3) fn = (void const*)k_window<0, true, 3>;
-		else if (a.variant == 4) fn = (void const*)k_window<0, true, 4>;
-		else fn = (void const*)k_window<0, true, 0>;
-	} else {
-		fn = only_fast ? (void const*)k_window<1, true, 0> : (void const*)k_window<1, false, 0>;
-	}
+	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 5 ? a.variant : 0)];
+	else fn = only_fast ? fns[rec][7] : fk_atomic_generic[rec];
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks + nrb));
 	cfg.blockDim         = dim3((unsigned)kThreads);
