@@ -144,7 +144,9 @@ enum {
 	                                   3 as 0 with warp-uniform count replay, 4 as 1 with
 	                                   branch-free replay and the spike output (bitmap words,
 	                                   list entries) written once per window, 5 as 4 with
-	                                   predicated instead of selected adds                    */
+	                                   predicated instead of selected adds, 6 as 4 with the
+	                                   count bits tested on the packed input word and the
+	                                   leak factors computed once per CTA                     */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

@@ -88,7 +88,7 @@ def autotune(net, steps: int = 600, warm: int = 60, candidates=None, verbose: bo
     return {"best": best, "results": results}
 
 
-def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4, 5), verbose: bool = False) -> dict:
+def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4, 5, 6), verbose: bool = False) -> dict:
     """Times the neuron-update kernel of `net` for each LIF window variant (identical results);
     applies and returns the fastest."""
     results = []

@@ -1422,7 +1422,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->launch_mode = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
-			if (value < 0 || value > 5) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 5");
+			if (value < 0 || value > 6) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 6");
 			n->neuron_variant = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:

@@ -463,7 +463,7 @@ __device__ __forceinline__ float add_n_pred(float v, float w, uint32_t n) {
 // bitmap words (one lane per step) and reserves list entries for the steps that had spikes.  Same
 // arithmetic and the same outputs as window_lif_fast (list order within a step is arbitrary in
 // both: reservations are atomic).
-template <bool PRED, class A>
+template <bool PRED, bool LEAN, class A>
 __device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __restrict__ Pg, int p, int b,
                                                     const float* dts_sm, uint32_t (*xs_sm)[kThreads],
                                                     uint32_t (*masks_sm)[16]) {
@@ -505,10 +505,33 @@ __device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __
 #pragma unroll 1
 		for (int u = 0; u < nk; u++) {
 			uint32_t const x = xs_sm[u][threadIdx.x];
-			V = PRED ? add_n_pred(V, w0, x & 0xffffu) : add_n_sel(V, w0, x & 0xffffu);
-			V = PRED ? add_n_pred(V, w1, x >> 16) : add_n_sel(V, w1, x >> 16);
+			if (LEAN) {
+				// both counts below 8 (the common case): the adds of the counts' 4-, 2- and 1-bits,
+				// tested on the packed word; otherwise the general replay
+				if ((x & 0xfff8fff8u) == 0) {
+					float v4 = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V, w0), w0), w0), w0);
+					V        = (x & 4u) ? v4 : V;
+					float v2 = __fadd_rn(__fadd_rn(V, w0), w0);
+					V        = (x & 2u) ? v2 : V;
+					float v1 = __fadd_rn(V, w0);
+					V        = (x & 1u) ? v1 : V;
+					v4       = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V, w1), w1), w1), w1);
+					V        = (x & 0x40000u) ? v4 : V;
+					v2       = __fadd_rn(__fadd_rn(V, w1), w1);
+					V        = (x & 0x20000u) ? v2 : V;
+					v1       = __fadd_rn(V, w1);
+					V        = (x & 0x10000u) ? v1 : V;
+				} else {
+					V = add_n_sel(V, w0, x & 0xffffu);
+					V = add_n_sel(V, w1, x >> 16);
+				}
+			} else {
+				V = PRED ? add_n_pred(V, w0, x & 0xffffu) : add_n_sel(V, w0, x & 0xffffu);
+				V = PRED ? add_n_pred(V, w1, x >> 16) : add_n_sel(V, w1, x >> 16);
+			}
 			if (zero && x) cnt[(int64_t)((slot0 + u) % D) * N + i] = 0;
-			bool const spike = lif_update(V, T, __fmaf_rn(-dts_sm[k0 + u], tminv, 1.0f), vthres, tref) && valid;
+			float const om   = LEAN ? dts_sm[k0 + u] : __fmaf_rn(-dts_sm[k0 + u], tminv, 1.0f);
+			bool const spike = lif_update(V, T, om, vthres, tref) && valid;
 			sbits |= (uint32_t)spike << u;
 			unsigned const mask = __ballot_sync(0xffffffffu, spike);
 			if (lane == 0) masks_sm[warp][u] = mask;
@@ -637,19 +660,25 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 // One CTA of the neuron update (block b of the window's neuron blocks).
 template <int MODE, bool ONLY_FAST, int VAR>
 __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
-	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;
+	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;  // 4 .. 6: deferred spike output
 	__shared__ float dts_sm[kMaxWindow];
 	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
 	__shared__ uint32_t masks_sm[VAR >= 4 ? kThreads / 32 : 1][16];
-	for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
-	__syncthreads();
 	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
+	if (VAR == 6 && MODE == 0 && kind == 3) {  // the LIF leak factors of the window's steps
+		float const tminv = a.pops[p].p2;
+		for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = __fmaf_rn(-a.dts[k], tminv, 1.0f);
+	} else {
+		for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
+	}
+	__syncthreads();
 	if (MODE == 0 && kind == 3) {
-		if (VAR == 4) window_lif_deferred<false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
-		else if (VAR == 5) window_lif_deferred<true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		if (VAR == 4) window_lif_deferred<false, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else if (VAR == 5) window_lif_deferred<true, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else if (VAR == 6) window_lif_deferred<false, true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
 	} else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
@@ -2354,7 +2383,7 @@ __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_batch_neurons(c
 	__shared__ uint32_t masks_sm[MODE == 0 ? kThreads / 32 : 1][16];
 	for (int k = threadIdx.x; k < w.K; k += blockDim.x) dts_sm[k] = b.dts[k];
 	__syncthreads();
-	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_deferred<false>(w, b.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+	if (MODE == 0 && __ldg(b.nblk_kind + p) == 3) window_lif_deferred<false, false>(w, b.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 	else if (MODE != 0 && __ldg(b.nblk_kind + p) == 3) window_neurons<MODE, true, false>(w, b.pops + p, p, lb);
 	else if (!ONLY_FAST) window_neurons<MODE, false, false>(w, b.pops + p, p, lb);
 }
@@ -2455,6 +2484,7 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 		else if (a.variant == 3) k_neurons<0, true, 3><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 4) k_neurons<0, true, 4><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 5) k_neurons<0, true, 5><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 6) k_neurons<0, true, 6><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
 		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
@@ -2469,19 +2499,21 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	if (nblocks + nsrc_blocks + nrb <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
-	void const* fns[2][8] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
+	void const* fns[2][9] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
 	                          (void const*)k_window<0, true, 1, false>, (void const*)k_window<0, true, 2, false>,
 	                          (void const*)k_window<0, true, 3, false>, (void const*)k_window<0, true, 4, false>,
-	                          (void const*)k_window<0, true, 5, false>, (void const*)k_window<1, true, 0, false>},
+	                          (void const*)k_window<0, true, 5, false>, (void const*)k_window<0, true, 6, false>,
+	                          (void const*)k_window<1, true, 0, false>},
 	                         {(void const*)k_window<0, false, 0, true>, (void const*)k_window<0, true, 0, true>,
 	                          (void const*)k_window<0, true, 1, true>, (void const*)k_window<0, true, 2, true>,
 	                          (void const*)k_window<0, true, 3, true>, (void const*)k_window<0, true, 4, true>,
-	                          (void const*)k_window<0, true, 5, true>, (void const*)k_window<1, true, 0, true>}};
+	                          (void const*)k_window<0, true, 5, true>, (void const*)k_window<0, true, 6, true>,
+	                          (void const*)k_window<1, true, 0, true>}};
 	void const* fk_atomic_generic[2] = {(void const*)k_window<1, false, 0, false>, (void const*)k_window<1, false, 0, true>};
 	int const rec = nrb > 0 ? 1 : 0;
 	void const* fn = nullptr;
-	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 5 ? a.variant : 0)];
-	else fn = only_fast ? fns[rec][7] : fk_atomic_generic[rec];
+	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 6 ? a.variant : 0)];
+	else fn = only_fast ? fns[rec][8] : fk_atomic_generic[rec];
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks + nrb));
 	cfg.blockDim         = dim3((unsigned)kThreads);

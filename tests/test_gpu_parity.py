@@ -337,7 +337,7 @@ def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threa
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 def test_neuron_variants_match_reference(engine, variant):
     """Every LIF window variant of the neuron update (unrolled or rolled steps, per-lane or
     warp-uniform count replay) gives the reference's raster and V bit for bit."""
