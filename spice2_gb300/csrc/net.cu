@@ -961,7 +961,8 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			bool const fused = n->launch_mode == 1 && !user_src && !user_st && !n->plastic;
 			if (fused) {
 				TRY(ev_begin(n, 0, &slot));
-				CUDA_TRY(launch_window(n->stream, wa, nb, ws, nbs, raster_pending ? &pending : nullptr, true));
+				// the first window of a chunk follows the chunk's host-to-device copies: a plain launch
+				CUDA_TRY(launch_window(n->stream, wa, nb, ws, nbs, raster_pending ? &pending : nullptr, j > 0));
 				TRY(ev_end(n, slot));
 				if (nb + nbs > 0 || raster_pending) n->launches++;
 				raster_pending = false;

@@ -27,6 +27,12 @@ namespace {
 
 constexpr int kThreads = 256;
 
+// Programmatic dependent launch (sm_90+): griddep_wait() returns once the preceding kernel of the
+// stream has completed and its writes are visible (at once when there is no programmatic edge);
+// griddep_launch() lets the following kernel's CTAs be scheduled while this one still runs.
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
 __device__ __forceinline__ unsigned lanemask_lt() {
 	unsigned m;
 	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
@@ -481,10 +487,11 @@ __device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __
 	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
 	float V   = 0;
 	int32_t T = 0;
-	if (valid) {
+	if (valid) {  // written two launches back: loaded before waiting for the previous launch
 		V = Pg->V[i];
 		T = Pg->T[i];
 	}
+	griddep_wait();  // the input ring, counts and lists are the previous launches' output
 	int const D = (int)a.D, Hb = a.Hb;
 	for (int k0 = 0; k0 < a.K; k0 += 16) {
 		int const nk    = min(16, a.K - k0);
@@ -675,12 +682,19 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 		for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = a.dts[k];
 	}
 	__syncthreads();
+	// window_lif_deferred waits for the previous launch after loading the state; the others first
 	if (MODE == 0 && kind == 3) {
 		if (VAR == 4) window_lif_deferred<false, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else if (VAR == 5) window_lif_deferred<true, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else if (VAR == 6) window_lif_deferred<false, true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
-		else window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
-	} else if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
+		else {
+			griddep_wait();
+			window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
+		}
+		return;
+	}
+	griddep_wait();
+	if (kind == 3) window_neurons<MODE, true, false>(a, a.pops + p, p, lb);
 	else if (!ONLY_FAST) {
 		if (kind == 0) window_neurons<MODE, false, false>(a, a.pops + p, p, lb);
 		else if (kind == 3 + kHistKind) window_neurons<MODE, true, true>(a, a.pops + p, p, lb);
@@ -702,6 +716,7 @@ __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const _
 // neuron update and the delivery of the previous window.
 __device__ __forceinline__ void sources_block(WindowArgs const& a, int b) {
 	__shared__ int red[kThreads / 32 + 1];
+	griddep_wait();  // this parity's counts were cleared by the previous delivery
 	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb = b - a.blk_begin[p];
@@ -713,11 +728,6 @@ __global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ Wi
 	sources_block(a, (int)blockIdx.x);
 }
 
-// Programmatic dependent launch (sm_90+): griddep_wait() returns once the preceding kernel of the
-// stream has completed and its writes are visible (at once when there is no programmatic edge);
-// griddep_launch() lets the following kernel's CTAs be scheduled while this one still runs.
-__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
-__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
 
 // One window's neuron update and source populations in one grid: first (when recording) the
 // raster blocks of the previous window `r`, whose bitmaps and counts are final, then nb neuron
@@ -729,7 +739,8 @@ template <int MODE, bool ONLY_FAST, int VAR, bool REC>
 __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_window(const __grid_constant__ WindowArgs a,
                                                                        const __grid_constant__ WindowArgs s, int nb,
                                                                        int nsb, const __grid_constant__ RasterArgs r) {
-	griddep_wait();
+	// each block kind waits for the previous launch where it first reads that launch's output; the
+	// raster blocks read only final data (the previous window's bitmaps and counts)
 	griddep_launch();
 	int const nrb = REC ? r.K * r.npop : 0;  // raster blocks first: they start with the first wave
 	int const b   = (int)blockIdx.x;
@@ -1663,21 +1674,31 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 			const int4* nbp    = nullptr;
 			const int64_t* bnp = nullptr;
 			uint2 ai           = make_uint2(0u, 0u);
-			if (lane < kConnBatch && ci < P.in_end) {
+			int64_t k = -1;
+			int src = 0;
+			if (lane < kConnBatch && ci < P.in_end) {  // the connection's fixed fields
 				ConnDev const& C = a.conns[ci];
-				int64_t const k  = sigma - (a.t0 + C.delay - 1);
+				k = sigma - (a.t0 + C.delay - 1);
 				if (k >= 0 && k < a.K && !C.plastic) {
-					int const cnt = a.counts[k * a.npop + C.src];
-					int const pp  = (cnt + a.parts - 1) / a.parts;
-					int const lo  = min(cnt, part * pp);
-					reach         = true;
-					n             = min(cnt, lo + pp) - lo;
-					lst           = C.src_list + (a.list_k0 + k) * C.src_size + lo;
-					nbp           = reinterpret_cast<const int4*>(C.nb16);
-					bnp           = C.bounds + t;
-					ai.x          = tile_addr + 4u * (uint32_t)(MODE == 0 ? C.word : C.fslot);
-					ai.y          = MODE == 0 ? C.inc : __float_as_uint(C.weight);
+					reach = true;
+					src   = C.src;
+					lst   = C.src_list + (a.list_k0 + k) * C.src_size;
+					nbp   = reinterpret_cast<const int4*>(C.nb16);
+					bnp   = C.bounds + t;
+					ai.x  = tile_addr + 4u * (uint32_t)(MODE == 0 ? C.word : C.fslot);
+					ai.y  = MODE == 0 ? C.inc : __float_as_uint(C.weight);
 				}
+			}
+			if (cb == P.in_begin) {  // spike counts and lists: the previous launch's output
+				griddep_wait();
+				griddep_launch();
+			}
+			if (reach) {
+				int const cnt = a.counts[k * a.npop + src];
+				int const pp  = (cnt + a.parts - 1) / a.parts;
+				int const lo  = min(cnt, part * pp);
+				n             = min(cnt, lo + pp) - lo;
+				lst += lo;
 			}
 			unsigned const rm = __ballot_sync(0xffffffffu, reach);
 			int incl          = n;
@@ -1706,6 +1727,8 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 			uint4* t4 = reinterpret_cast<uint4*>(tile_sm);
 			for (int i = threadIdx.x - 32; i < (words >> 2); i += blockDim.x - 32) t4[i] = make_uint4(0u, 0u, 0u, 0u);
 			for (int i = (words & ~3) + threadIdx.x - 32; i < words; i += blockDim.x - 32) tile_sm[i] = 0;
+			griddep_wait();
+			griddep_launch();
 		}
 		zeroed = true;
 		__syncthreads();
@@ -1784,6 +1807,8 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 		}
 	}
 	__syncthreads();
+	griddep_wait();  // (no-op when done above) the ring slot is read by the previous launch
+	griddep_launch();
 	bool const touched = s_touched != 0;
 	add_events(a.events, my_events, &ev_block);
 	if (!touched) return;
@@ -1871,9 +1896,23 @@ __device__ __forceinline__ void deliver_wps(A const& a, PopDev const& P, int t, 
 struct DeliverItem {
 	int part, si, Q, t;
 };
+// The spike counts of the other parity (fully delivered) are cleared for the window after next.
+__device__ __forceinline__ void clear_counts_next(DeliverArgs const& a) {
+	if (blockIdx.x == 0)
+		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
+}
+
+// The work item of a plain delivery CTA.  WAIT: wait for the previous launch (and clear the other
+// parity's counts) first; otherwise the caller waits, releases the dependents and clears the counts
+// once its independent prologue is done.
+// The dependents are released only after the wait: the next window's grid reads the neuron state
+// of this window's neuron update (complete once this launch has waited for it) before it waits.
+template <bool WAIT = true>
 __device__ __forceinline__ DeliverItem deliver_item(DeliverArgs const& a) {
-	griddep_wait();
-	griddep_launch();
+	if (WAIT) {
+		griddep_wait();
+		griddep_launch();
+	}
 	DeliverItem it;
 	it.part    = blockIdx.x % a.parts;
 	int const b = blockIdx.x / a.parts;
@@ -1883,8 +1922,7 @@ __device__ __forceinline__ DeliverItem deliver_item(DeliverArgs const& a) {
 	while (Q + 1 < a.npop && g >= a.tile_begin[Q + 1]) Q++;
 	it.Q = Q;
 	it.t = g - a.tile_begin[Q];
-	if (blockIdx.x == 0)
-		for (int j = threadIdx.x; j < a.counts_next_len; j += blockDim.x) a.counts_next[j] = 0;
+	if (WAIT) clear_counts_next(a);
 	return it;
 }
 
@@ -1932,8 +1970,9 @@ __global__ void __launch_bounds__(1024, 1) k_deliver_rows(const __grid_constant_
 
 template <int MODE, int SF, int U, bool TMA>
 __global__ void __launch_bounds__(SF > 1 ? 768 : 1024, 1) k_deliver_rows16(const __grid_constant__ DeliverArgs a) {
-	DeliverItem const it = deliver_item(a);
+	DeliverItem const it = deliver_item<false>(a);  // deliver_rows16 waits after its prologue
 	deliver_rows16<MODE, SF, U, TMA>(a, a.pops[it.Q], it.t, it.si, it.part);
+	clear_counts_next(a);
 }
 
 // The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
