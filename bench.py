@@ -340,8 +340,9 @@ def plastic_bench(N: int = 100000, steps: int = 5000):
     the neuron of samples/vogels.cpp), fixed_probability(0.02), delay 1 step, E weights 0.03 and
     I weights 0.3 (0.3 nS and 3 nS over the 10 nS leak), I->E synapses iSTDP (tau 20 ms, rho0 5 Hz,
     eta 1e-3) with lazy event-driven updates, atomic mode, dt 1e-4, `steps` steps after 200 warm-up
-    steps.  Reported: synaptic events/s and simulated seconds per wall second (CUDA events on the
-    net's stream), firing rates and the I->E weight drift."""
+    steps and the delivery autotuner's (~7,700 steps of the network's own dynamics).  Reported:
+    synaptic events/s and simulated seconds per wall second (CUDA events on the net's stream),
+    firing rates and the I->E weight drift."""
     import numpy as np
     import torch
     import spice2_gb300 as sp
@@ -358,6 +359,8 @@ def plastic_bench(N: int = 100000, steps: int = 5000):
     syn = sum(net.synapses(k) for k in range(4))
     build_s = time.perf_counter() - t0
     net.run(200)
+    from spice2_gb300.autotune import autotune
+    tuned = autotune(net, steps=100, warm=10)["best"]  # delivery shape of the non-plastic projections
     net.synchronize()
     W0 = net.synapse_state(c, 0).astype(np.float64)
     stream = torch.cuda.ExternalStream(net.stream_handle())
@@ -381,6 +384,7 @@ def plastic_bench(N: int = 100000, steps: int = 5000):
             "events": ev, "gpu_launches": launches, "rate_E_hz": rE, "rate_I_hz": rI,
             "istdp_weight_mean_start": float(W0.mean()), "istdp_weight_mean_end": float(W.mean()),
             "istdp_weight_std_end": float(W.std()), "build_seconds": build_s, "mode": "atomic",
+            "delivery_shape": tuned,
             "config": "plastic E/I: conductance LIF, p 0.02, delay 1 step, iSTDP on I->E"}
 
 

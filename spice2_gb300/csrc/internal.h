@@ -104,6 +104,8 @@ struct ConnDev {
 	float* sA;                // x_pre
 	float* sB;                // x_post
 	uint64_t* ages;           // per source: bit 63 = pending pre update, low bits = step + 1
+	uint32_t* chunks_done;    // per source: row chunks of the current plastic delivery finished
+	int64_t max_row;          // longest row (synapses of one source)
 	const uint64_t* dst_hist; // the target population's post-spike history
 	const double* skip_tab;   // pow(1 - dt/tau, n) for n = -64 .. 64
 	int src_nwords;           // source bitmap words

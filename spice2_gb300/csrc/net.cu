@@ -743,6 +743,13 @@ int prepare(spice_net* n) {
 		TRY(dalloc(n, &d.sA, (size_t)std::max<int64_t>(c.synapses, 1)));
 		TRY(dalloc(n, &d.sB, (size_t)std::max<int64_t>(c.synapses, 1)));
 		TRY(dalloc(n, &d.ages, (size_t)std::max<int64_t>(S.size, 1)));
+		TRY(dalloc(n, &d.chunks_done, (size_t)std::max<int64_t>(S.size, 1)));
+		{  // the longest row sizes the plastic delivery's grid
+			std::vector<int64_t> off((size_t)S.size + 1);
+			CUDA_TRY(cudaMemcpy(off.data(), d.off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost));
+			d.max_row = 0;
+			for (int64_t r = 0; r < S.size; r++) d.max_row = std::max(d.max_row, off[r + 1] - off[r]);
+		}
 		std::vector<float> w0((size_t)std::max<int64_t>(c.synapses, 1), d.plastic == SPICE_SYNAPSE_ISTDP ? c.w0 : 0.0f);
 		CUDA_TRY(cudaMemcpy(d.sW, w0.data(), sizeof(float) * w0.size(), cudaMemcpyHostToDevice));
 		d.alpha = 2.0f * c.rho0 * c.tau;
@@ -958,7 +965,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			bool const any_src = nbs > 0 || user_src;
 			// one stream, one grid for neurons and sources, each launch the programmatic dependent
 			// of the previous one (its CTAs wait on the device instead of being launched after it)
-			bool const fused = n->launch_mode == 1 && !user_src && !user_st && !n->plastic;
+			// (plastic kernels stay plain launches between them: a plain kernel releases its dependents
+			// when it completes)
+			bool const fused = n->launch_mode == 1 && !user_src && !user_st;
 			if (fused) {
 				TRY(ev_begin(n, 0, &slot));
 				// the first window of a chunk follows the chunk's host-to-device copies: a plain launch

@@ -2292,24 +2292,30 @@ __global__ void __launch_bounds__(256) k_plastic_update_all(const __grid_constan
 }
 
 // Delivery of the spikes of step time - delay + 1 through a plastic connection (synapse_population
-// .h:82-140): a warp per word of the source's spike bitmap, each spiking source's row lane-parallel:
-// catch up, then deliver W into input ring slot `slot` (atomic-mode sums; COUNT with scale 0 and
-// any model in deterministic mode deliver nothing).
-__global__ void __launch_bounds__(256) k_plastic_deliver(const __grid_constant__ ConnDev C, int64_t time, int hslot,
-                                                          int64_t slot, int deliver, unsigned long long* events) {
-	int const lane = threadIdx.x & 31;
-	int const w    = blockIdx.x * 8 + (threadIdx.x >> 5);
-	if (w >= C.src_nwords) return;
+// .h:82-140): CTA (w, c) takes chunk c (kPlasticChunk synapses, a thread each) of the row of every
+// spiking source of bitmap word w: catch up, then deliver W into input ring slot `slot` (atomic-mode
+// sums; COUNT with scale 0 and any model in deterministic mode deliver nothing).  Every chunk of a
+// row catches up from the source's `ages` word as it was at launch; the row's last chunk to finish
+// (a per-source counter) writes the new value.
+constexpr int kPlasticChunk = 256;
+
+__global__ void __launch_bounds__(kPlasticChunk) k_plastic_deliver(const __grid_constant__ ConnDev C, int64_t time,
+                                                                   int hslot, int64_t slot, int deliver,
+                                                                   unsigned long long* events) {
+	int const w = blockIdx.x;
 	uint32_t bits = C.src_bits[(int64_t)hslot * C.src_nwords + w];
 	unsigned long long ev = 0;
 	while (bits) {
 		int const r       = __ffs(bits) - 1;
 		bits &= bits - 1;
 		int64_t const src = 32 * (int64_t)w + r;
-		uint64_t const ages = C.ages[src];
 		int64_t const e0 = C.off[src], e1 = C.off[src + 1];
-		ev += (unsigned long long)(e1 - e0);
-		for (int64_t e = e0 + lane; e < e1; e += 32) {
+		int64_t const nchunks = (e1 - e0 + kPlasticChunk - 1) / kPlasticChunk;
+		if (blockIdx.y == 0 && threadIdx.x == 0) ev += (unsigned long long)(e1 - e0);
+		for (int64_t c = blockIdx.y; c < nchunks; c += gridDim.y) {
+		uint64_t const ages = C.ages[src];
+		int64_t const e = e0 + c * kPlasticChunk + threadIdx.x;
+		if (e < e1) {
 			SynState st{C.sW[e], C.sA[e], C.sB[e]};
 			int32_t const j = C.nb[e];
 			catch_up(C, st, time, ages, C.dst_hist[j]);
@@ -2321,10 +2327,18 @@ __global__ void __launch_bounds__(256) k_plastic_deliver(const __grid_constant__
 				red_add_f32(C.dst_acc + (slot * C.dst_size + j) * C.F + C.fslot, v);
 			}
 		}
-		__syncwarp();
-		if (lane == 0) C.ages[src] = (uint64_t)(time + 1) | (1ull << 63);
+		__syncthreads();  // every thread of this chunk has read `ages`
+		if (threadIdx.x == 0) {
+			__threadfence();
+			if (atomicAdd(C.chunks_done + src, 1u) == (uint32_t)(nchunks - 1)) {  // the row's last chunk
+				C.ages[src]        = (uint64_t)(time + 1) | (1ull << 63);
+				C.chunks_done[src] = 0;
+			}
+		}
+		__syncthreads();
+		}
 	}
-	if (lane == 0 && ev) atomicAdd(events, ev);
+	if (threadIdx.x == 0 && ev) atomicAdd(events, ev);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -2772,9 +2786,10 @@ cudaError_t launch_plastic_update_all(cudaStream_t stream, ConnDev const& c, int
 
 cudaError_t launch_plastic_deliver(cudaStream_t stream, ConnDev const& c, int64_t time, int hslot, int64_t slot,
                                    bool deliver, unsigned long long* events) {
-	if (c.src_nwords <= 0) return cudaSuccess;
-	k_plastic_deliver<<<(unsigned)((c.src_nwords + 7) / 8), 256, 0, stream>>>(c, time, hslot, slot, deliver ? 1 : 0,
-	                                                                        events);
+	if (c.src_nwords <= 0 || c.max_row <= 0) return cudaSuccess;
+	dim3 const grid((unsigned)c.src_nwords,
+	                (unsigned)std::min<int64_t>(65535, (c.max_row + kPlasticChunk - 1) / kPlasticChunk));
+	k_plastic_deliver<<<grid, kPlasticChunk, 0, stream>>>(c, time, hslot, slot, deliver ? 1 : 0, events);
 	return cudaGetLastError();
 }
 
