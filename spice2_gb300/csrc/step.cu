@@ -738,7 +738,7 @@ __device__ void raster_block(RasterArgs const& a, int b);
 template <int MODE, bool ONLY_FAST, int VAR, bool REC>
 __global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_window(const __grid_constant__ WindowArgs a,
                                                                        const __grid_constant__ WindowArgs s, int nb,
-                                                                       int nsb, const __grid_constant__ RasterArgs r) {
+                                                                       const __grid_constant__ RasterArgs r) {
 	// each block kind waits for the previous launch where it first reads that launch's output; the
 	// raster blocks read only final data (the previous window's bitmaps and counts)
 	griddep_launch();
@@ -2577,10 +2577,10 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	at[0].val.programmaticStreamSerializationAllowed = pdl ? 1 : 0;
 	cfg.attrs    = at;
 	cfg.numAttrs = 1;
-	int nb = nblocks, nsb = nsrc_blocks;
+	int nb = nblocks;
 	RasterArgs rr{};
 	if (r) rr = *r;
-	void* args[] = {const_cast<WindowArgs*>(&a), const_cast<WindowArgs*>(&s), &nb, &nsb, &rr};
+	void* args[] = {const_cast<WindowArgs*>(&a), const_cast<WindowArgs*>(&s), &nb, &rr};
 	return cudaLaunchKernelExC(&cfg, fn, args);
 }
 

@@ -47,3 +47,53 @@ def test_precondition_messages_without_a_device(engine):
     import pytest
     with pytest.raises(engine.LogicError, match="at least 1 seed"):
         engine.snn(1e-4, 15e-4, [])
+
+
+def _enum(name_prefix):
+    src = open(os.path.join(ROOT, "include", "spice_gb300.h")).read()
+    return {m.group(1): int(m.group(2)) for m in re.finditer(r"\b(" + name_prefix + r"[A-Z0-9_]*)\s*=\s*(\d+)", src)}
+
+
+def _kernels_header_int(name):
+    src = open(os.path.join(ROOT, "spice2_gb300", "csrc", "kernels.h")).read()
+    return int(re.search(r"constexpr int " + name + r"\s*=\s*(\d+);", src).group(1))
+
+
+def test_tuning_knobs_reach_the_python_mirror(engine, monkeypatch):
+    """Every SPICE_TUNE_* knob of the header is set by snn.set_tuning or batch.set_tuning."""
+    knobs = _enum("SPICE_TUNE_")
+    seen = []
+
+    class _L:
+        def spice_set_tuning(self, h, knob, value):
+            seen.append(knob)
+            return 0
+
+        def spice_batch_set_tuning(self, h, knob, value):
+            seen.append(knob)
+            return 0
+
+    monkeypatch.setattr(engine, "lib", lambda: _L())
+    net = engine.snn.__new__(engine.snn)
+    net._h = None
+    net.set_tuning(tile_bytes=4096, deliver_threads=64, deliver_parts=1, deliver_algo=1, overlap_sources=True,
+                   neuron_variant=0, launch_mode=1)
+    b = engine.batch.__new__(engine.batch)
+    b._h = None
+    b.set_tuning(graph_windows=2)
+    assert sorted(set(seen)) == sorted(knobs.values()), (knobs, seen)
+
+
+def test_autotune_candidates_are_valid_launch_shapes():
+    """Every candidate of the autotuner is a shape spice_set_tuning accepts, and bench.py names the
+    kernel of every delivery mapping."""
+    import sys
+    sys.path.insert(0, ROOT)
+    from spice2_gb300.autotune import DEFAULT_CANDIDATES
+    import bench
+    n_algos = _kernels_header_int("kDeliverAlgos")
+    for tb, th, parts, algo in DEFAULT_CANDIDATES:
+        assert 1024 <= tb <= 220 * 1024 and 32 <= th <= 1024 and th % 32 == 0 and 1 <= parts <= 64
+        assert 0 <= algo < n_algos
+    assert sorted(bench.DELIVER_KERNELS) == list(range(n_algos))
+    assert set(bench.DELIVER_DRAM_BYTES_PER_EVENT) <= set(range(n_algos))
