@@ -335,6 +335,14 @@ int spice_lif_backward(spice_lif_layer* layer, int batch, int steps, int checkpo
                        const float* grad_counts, float* grad_w_in, float* grad_w_rec, float* grad_theta,
                        float* grad_beta, void* stream);
 
+/* Self-test (no reference counterpart): the plastic synapses' trace decay computes
+ * (float)((double)x * f) -- the reference's skip() -- in integer arithmetic; this compares it with
+ * the GPU's double multiply for `count` random pairs (finite x >= 0 including subnormals, f in
+ * [2^-4, 2^5)).  mismatches: pairs whose results differ in any bit; first_a / first_f (either may
+ * be NULL): the first such pair. */
+int spice_selftest_skip_rounding(int64_t count, uint64_t seed, int64_t* mismatches, uint32_t* first_a,
+                                 double* first_f);
+
 #ifdef __cplusplus
 }
 #endif

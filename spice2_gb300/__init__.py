@@ -111,6 +111,7 @@ def _load():
         "spice_lif_layer_synapses": [vp, P(i64), P(i64)],
         "spice_lif_forward": [vp, i32, i32, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp, vp, vp],
         "spice_lif_backward": [vp, i32, i32, i32, i32, f32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
+        "spice_selftest_skip_rounding": [i64, C.c_uint64, P(i64), P(u32), P(f64)],
     }
     for name, args in sig.items():
         fn = getattr(L, name)
@@ -573,6 +574,15 @@ def brunel_sweep(sizes: Sequence[int], seed0: int = 1000, mode: int = MODE_DETER
     return [brunel(int(N), 0.1 * min(1.0, 20000.0 / N), seed0 + i, mode=mode) for i, N in enumerate(sizes)]
 
 
+def selftest_skip_rounding(count: int = 1 << 26, seed: int = 1):
+    """Runs the device self-test of the plastic trace decay's rounding (integer arithmetic against
+    the double multiply) on `count` random pairs; returns (mismatches, first_a_bits, first_f)."""
+    m, a, f = C.c_int64(), C.c_uint32(), C.c_double()
+    _check(lib().spice_selftest_skip_rounding(int(count), int(seed), C.byref(m), C.byref(a), C.byref(f)))
+    return m.value, a.value, f.value
+
+
 __all__ = ["snn", "Population", "poisson", "lif", "lif_cond", "external_input", "fixed_weight", "excitatory",
            "inhibitory", "istdp", "count_synapse", "fixed_probability", "adj_list", "brunel", "batch", "brunel_sweep", "brunel_sweep_sizes",
-           "SpiceError", "LogicError", "CudaError", "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib"]
+           "SpiceError", "LogicError", "CudaError", "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib",
+           "selftest_skip_rounding"]

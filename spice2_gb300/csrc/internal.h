@@ -108,6 +108,7 @@ struct ConnDev {
 	int64_t max_row;          // longest row (synapses of one source)
 	const uint64_t* dst_hist; // the target population's post-spike history
 	const double* skip_tab;   // pow(1 - dt/tau, n) for n = -64 .. 64
+	const uint64_t* skip_pk;  // the same factors packed for mul_f32_f64_rn (significand | exponent << 53)
 	int src_nwords;           // source bitmap words
 	const uint32_t* src_bits; // source spike bitmap ring [Hb][src_nwords]
 };

@@ -135,6 +135,8 @@ cudaError_t launch_tile_bounds(cudaStream_t stream, const int64_t* off, const in
 // Plastic connections: the periodic catch-up of every synapse (every 64 steps), and the delivery
 // of the spikes in bitmap slot hslot into input ring slot `slot` at step `time`.
 cudaError_t launch_plastic_update_all(cudaStream_t stream, ConnDev const& c, int64_t time);
+cudaError_t launch_selftest_mulround(cudaStream_t stream, int64_t count, uint64_t seed, unsigned long long* mismatches,
+                                     unsigned long long* first);
 cudaError_t launch_plastic_deliver(cudaStream_t stream, ConnDev const& c, int64_t time, int hslot, int64_t slot,
                                    bool deliver, unsigned long long* events);
 

@@ -18,6 +18,7 @@
 
 #include "spice_gb300.h"
 #include "internal.h"
+#include "mulround.h"
 #include "kernels.h"
 
 using namespace spice_gb300;
@@ -761,6 +762,12 @@ int prepare(spice_net* n) {
 		TRY(dalloc(n, &dt, tab.size(), false));
 		CUDA_TRY(cudaMemcpy(dt, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice));
 		d.skip_tab   = dt;
+		std::vector<uint64_t> pk(tab.size());
+		for (size_t q = 0; q < tab.size(); q++) pk[q] = pack_f64(tab[q]);
+		uint64_t* dpk = nullptr;
+		TRY(dalloc(n, &dpk, pk.size(), false));
+		CUDA_TRY(cudaMemcpy(dpk, pk.data(), sizeof(uint64_t) * pk.size(), cudaMemcpyHostToDevice));
+		d.skip_pk = dpk;
 		d.src_bits   = S.bits;
 		d.src_nwords = S.nwords;
 	}
@@ -1489,6 +1496,23 @@ extern "C" int spice_get_stream(spice_net* n, void** out) {
 extern "C" int spice_synchronize(spice_net* n) {
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	return SPICE_OK;
+}
+
+extern "C" int spice_selftest_skip_rounding(int64_t count, uint64_t seed, int64_t* mismatches,
+                                            uint32_t* first_a, double* first_f) {
+	if (count < 0 || !mismatches) return fail(SPICE_EINVAL, "count must be >= 0 and mismatches not NULL");
+	unsigned long long* d = nullptr;
+	CUDA_TRY(cudaMalloc(&d, sizeof(unsigned long long) * 3));
+	cudaError_t e = cudaMemset(d, 0, sizeof(unsigned long long) * 3);
+	if (e == cudaSuccess) e = launch_selftest_mulround(nullptr, count, seed, d, d + 1);
+	unsigned long long h[3] = {0, 0, 0};
+	if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+	cudaFree(d);
+	if (e != cudaSuccess) return fail(SPICE_ECUDA, cudaGetErrorString(e));
+	*mismatches = (int64_t)h[0];
+	if (first_a) *first_a = (uint32_t)h[1];
+	if (first_f) memcpy(first_f, &h[2], sizeof(double));
 	return SPICE_OK;
 }
 

@@ -20,6 +20,7 @@
 #include "spice_gb300.h"
 #include "internal.h"
 #include "kernels.h"
+#include "mulround.h"
 
 namespace spice_gb300 {
 
@@ -2242,14 +2243,17 @@ __device__ __forceinline__ void syn_update(ConnDev const& C, SynState& s, bool p
 	s.B = __fsub_rn(s.B, __fmul_rn(s.B, C.cdt));
 }
 
+// skip(n): the traces decay by (1 - dt/tau)^n, a double, each trace rounded back to float
+// (synapse_population.h:118-139); mul_f32_f64_rn gives the bits of that double multiply without
+// the FP64 pipe (the traces are never negative).
 __device__ __forceinline__ void syn_skip(ConnDev const& C, SynState& s, int64_t n) {
 	if (C.plastic == SPICE_SYNAPSE_COUNT) {
 		s.W = __fadd_rn(s.W, (float)n);
 		return;
 	}
-	double const f = __ldg(C.skip_tab + (n + 64));
-	s.A            = __double2float_rn(__dmul_rn((double)s.A, f));
-	s.B            = __double2float_rn(__dmul_rn((double)s.B, f));
+	uint64_t const f = __ldg(C.skip_pk + (n + 64));
+	s.A              = mul_f32_f64_rn(s.A, f);
+	s.B              = mul_f32_f64_rn(s.B, f);
 }
 
 // The catch-up of one edge to step `time` (synapse_population.h:88-116).  The reference computes
@@ -2775,6 +2779,48 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 38: k_batch_deliver<0, 19><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 39: k_batch_deliver<1, 19><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 	}
+	return cudaGetLastError();
+}
+
+namespace {
+// Self-test of mul_f32_f64_rn against the double multiply: random finite a >= 0 (every exponent,
+// subnormals included) and random f in [2^-4, 2^5) (products overflowing float included).
+__global__ void k_selftest_mulround(int64_t count, uint64_t seed, unsigned long long* mismatches,
+                                    unsigned long long* first) {
+	for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x) {
+		uint64_t x = seed ^ (0x9e3779b97f4a7c15ull * (uint64_t)(i + 1));
+		x ^= x >> 31;
+		x *= 0xbf58476d1ce4e5b9ull;
+		x ^= x >> 29;
+		x *= 0x94d049bb133111ebull;
+		x ^= x >> 32;
+		uint32_t ab = (uint32_t)x & 0x7fffffffu;
+		if ((ab >> 23) == 0xffu) ab &= 0x7f7fffffu;  // finite
+		if ((i & 7) == 0) ab &= 0x007fffffu;      // every eighth a subnormal
+		uint64_t y = x * 0xd1342543de82ef95ull + 1;
+		y ^= y >> 33;
+		int const ex  = (int)(y % 9) - 4;
+		double const f = ldexp(1.0 + (double)(y >> 12) * 0x1p-52, ex);
+		float const a  = __uint_as_float(ab);
+		float const r1 = __double2float_rn(__dmul_rn((double)a, f));
+		// pack f on the device as pack_f64 does on the host
+		uint64_t const fb = (uint64_t)__double_as_longlong(f);
+		int const e       = (int)((fb >> 52) & 0x7ff) - 1023;  // f = 1.m 2^e
+		uint64_t const pk = ((fb & ((1ull << 52) - 1)) | (1ull << 52)) | ((uint64_t)(e - 52 + 1100) << 53);
+		float const r2    = mul_f32_f64_rn(a, pk);
+		if (__float_as_uint(r1) != __float_as_uint(r2)) {
+			if (atomicAdd(mismatches, 1ull) == 0) {
+				first[0] = ab;
+				first[1] = fb;
+			}
+		}
+	}
+}
+}  // namespace
+
+cudaError_t launch_selftest_mulround(cudaStream_t stream, int64_t count, uint64_t seed, unsigned long long* mismatches,
+                                     unsigned long long* first) {
+	k_selftest_mulround<<<1216, 256, 0, stream>>>(count, seed, mismatches, first);
 	return cudaGetLastError();
 }
 

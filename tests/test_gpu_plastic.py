@@ -123,3 +123,10 @@ def test_plastic_ei_network_statistics(engine, oracle_lib):
         assert abs(gE - oE) < 0.15 * oE and abs(gI - oI) < 0.15 * oI, (seed, gE, oE, gI, oI)
         assert abs(gdW.std() - odW.std()) < 0.25 * odW.std(), (seed, gdW.std(), odW.std())
         assert gE > 1.0 and gI > 1.0
+
+
+def test_trace_decay_rounding_matches_double_multiply(engine):
+    """The traces' skip() decay, (float)((double)x * f), is computed in integer arithmetic: equal in
+    every bit to the GPU's double multiply on 2^27 random pairs (subnormal x, overflowing products)."""
+    m, a, f = engine.selftest_skip_rounding(1 << 27, 12345)
+    assert m == 0, f"{m} mismatches, first x bits {a:#010x}, f {f!r}"
