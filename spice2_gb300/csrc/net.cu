@@ -61,12 +61,19 @@ void parallel_copy(void* dst, const void* src, size_t bytes) {
 	}
 	size_t const per = (bytes / nt + 63) & ~size_t(63);
 	std::vector<std::thread> th;
+	size_t done = per;  // [0, per) is copied by this thread; parts no thread could be started for too
 	for (int i = 1; i < nt; i++) {
 		size_t const o = per * i;
 		if (o >= bytes) break;
-		th.emplace_back([=] { std::memcpy((char*)dst + o, (const char*)src + o, std::min(per, bytes - o)); });
+		try {
+			th.emplace_back([=] { std::memcpy((char*)dst + o, (const char*)src + o, std::min(per, bytes - o)); });
+			done = std::min(bytes, o + per);
+		} catch (...) {
+			break;
+		}
 	}
 	std::memcpy(dst, src, std::min(per, bytes));
+	if (done < bytes) std::memcpy((char*)dst + done, (const char*)src + done, bytes - done);
 	for (auto& x : th) x.join();
 }
 
