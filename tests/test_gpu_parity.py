@@ -191,6 +191,25 @@ def test_long_run_across_chunks_matches_oracle(engine, oracle_lib):
         assert np.array_equal(net.get_state(pops[k], sp.FIELD_TREF), ref.state(rpops[k], 3))
 
 
+def test_large_recorded_raster_equals_piecewise_recording(engine):
+    """A 2000-step recording at N=5e5 (an 11.7 MB raster, copied to the caller's buffer by several
+    host threads) equals the same network recorded in 200-step pieces, entry for entry."""
+    sp = engine
+    a, _ = sp.brunel(500000, 0.002, 3)
+    b, _ = sp.brunel(500000, 0.002, 3)
+    whole = a.run_record(2000)
+    pieces = []
+    for _ in range(10):
+        pieces += list(b.run_record(200))
+    assert len(whole) == len(pieces) == 2000
+    n = 0
+    for t, (r1, r2) in enumerate(zip(whole, pieces)):
+        for k in range(3):
+            assert np.array_equal(np.asarray(r1[k]), np.asarray(r2[k])), (t, k)
+            n += len(r1[k])
+    assert n * 4 > (8 << 20)  # large enough for the threaded copy
+
+
 # ---- the reference's own known-answer tests, restated ----------------------------------------------
 def test_external_input_sample(engine):
     """samples/external_input.cpp: a per-population update replays a cyclic spike train."""
