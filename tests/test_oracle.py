@@ -215,13 +215,16 @@ def test_jump_ahead_equals_stepping(oracle_lib, n):
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
                                                     "ref_driver")), reason="reference driver not built here")
-def test_oracle_vs_live_reference(oracle_lib):
-    """The restatement against the reference binary on a fresh configuration."""
+@pytest.mark.parametrize("N,p,seed,steps", [(3000, 0.07, 99, 400), (12000, 0.02, 7, 250), (800, 0.3, 2024, 600),
+                                           (20000, 0.005, 31337, 150)])
+def test_oracle_vs_live_reference(oracle_lib, N, p, seed, steps):
+    """The restatement against the reference binary on fresh configurations (sizes, densities and
+    seeds the fixtures do not hold): every step's raster and dt, and the final LIF state."""
     o = oracle_lib
-    res = o.run_reference_net(o.brunel_spec(3000, 0.07, 99, 400))
+    res = o.run_reference_net(o.brunel_spec(N, p, seed, steps))
     st, _, _ = o.reference_states(res, [1, 2])
-    net, pops = o.brunel(3000, 0.07, 99)
-    for t in range(400):
+    net, pops = o.brunel(N, p, seed)
+    for t in range(steps):
         net.step()
         for k in range(3):
             assert np.array_equal(net.spikes(pops[k], 0), res["raster"][t][k])
