@@ -73,6 +73,21 @@ def test_csr_small_cases(oracle_lib):
             assert o.fp_max_degree(d, p) == int(g["md_" + key][0]), key
 
 
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+@pytest.mark.parametrize("src,dst,p,seed", [(1, 1, 1.0, 5), (257, 1000, 0.013, 77), (4000, 300, 0.5, 9),
+                                            (3, 70000, 0.0007, 123), (1000, 1000, 0.999, 42), (50, 20, 0.0, 1)])
+def test_csr_vs_live_reference(oracle_lib, src, dst, p, seed):
+    """fixed_probability adjacency of the restatement against the reference binary on shapes the
+    fixtures do not hold (single synapse, near-empty and near-full rows, very sparse wide rows)."""
+    o = oracle_lib
+    md, off_r, nb_r = o.run_reference_gen(src, dst, p, seed)
+    off, nb, _ = o.fp_generate(src, dst, p, o.seed_from_list([seed]))
+    assert np.array_equal(off, off_r) and np.array_equal(nb, nb_r)
+    if src:
+        assert o.fp_max_degree(dst, p) == md
+
+
 def test_csr_checksums_n20000(oracle_lib):
     o = oracle_lib
     cs = json.load(open(os.path.join(GOLDEN, "brunel_csr_checksums.json")))["N=20000,p=0.1"]["1337"]
