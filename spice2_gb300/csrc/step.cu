@@ -3,20 +3,26 @@
 // A spike emitted at step t through a connection of delay d is delivered at the end of step
 // t + d - 1 and first seen by the update of step t + d (snn.cpp:21-25).  So with K <= min delay,
 // the K updates of a window [t0, t0 + K) only read inputs caused by spikes older than t0, and a
-// window is two launches:
-//   k_window  -- every neuron runs its K updates with its state in registers.  Before the update
-//                of step t it applies the inputs that the reference delivers at the end of step
-//                t - 1 (ring slot (t - 1) mod D).  Spikes go to a bitmap (one ballot word per
-//                warp: the ascending order of neuron_population::spikes) and to an unordered
-//                list per step (warp-aggregated atomics) for delivery.
-//   k_deliver -- work-queue delivery, one warp per (spike, connection): the warp streams the CSR
-//                row (int32 targets) and adds into ring slot (t + d - 1) mod D.
+// window is two launches on one stream, each the programmatic dependent of the previous one:
+//   k_window  -- every neuron runs its K updates with its state in registers (window_lif_* and
+//                window_neurons).  Before the update of step t it applies the inputs that the
+//                reference delivers at the end of step t - 1 (ring slot (t - 1) mod D).  Spikes go
+//                to a bitmap (one ballot word per warp: the ascending order of
+//                neuron_population::spikes) and to an unordered list per step for delivery.  The
+//                same grid runs the source populations (Poisson, external trains) and, when
+//                recording, the previous window's raster.
+//   delivery  -- one CTA per (input slot, target tile): the spikes of every connection into the
+//                tile's population that reach the slot add into a shared-memory tile of
+//                counters, which is then stored to the ring slot.  Twenty work mappings
+//                (k_deliver*, SPICE_TUNE_DELIVER_ALGO) with identical results.
 // Deterministic mode: fixed_weight synapses add one constant per connection, so the reference's
 // sequential order (connections in connect order, sources ascending) is reproduced exactly by
 // counting events per (target, group of consecutive connections with equal weight) with integer
 // atomics and replaying the adds one by one in group order with IEEE round-to-nearest
 // (__fadd_rn; the library is built with -fmad=false).  Atomic mode adds float weights with
 // atomics (fast, order-dependent rounding).
+// Also here: the plastic synapses' catch-up and delivery (k_plastic_*), the batched-network
+// kernels (k_batch_*), tile bounds, scans and the raster.
 #include "spice_gb300.h"
 #include "internal.h"
 #include "kernels.h"
