@@ -64,11 +64,13 @@ def _plastic_brunel_oracle(N, p, seed, pp, pdelay):
     return net, (P, E, I), c
 
 
-@pytest.mark.parametrize("pdelay", [1e-4, 15e-4])
-def test_oracle_plastic_matches_reference_binary(pdelay):
+@pytest.mark.parametrize("pdelay,N,p,seed,steps", [(1e-4, 4000, 0.05, 7, 400), (15e-4, 4000, 0.05, 7, 400),
+                                                  (5e-4, 2500, 0.08, 99, 500), (3e-4, 6000, 0.03, 2024, 300)])
+def test_oracle_plastic_matches_reference_binary(pdelay, N, p, seed, steps):
+    """The plastic restatement (counting model on E->E, lazy catch-up every 64 steps and at each
+    delivery) against the reference binary: rasters, LIF state and the schedule's counts."""
     if not o.have_reference():
         pytest.skip("reference driver not built on this host")
-    N, p, seed, steps = 4000, 0.05, 7, 400
     res = o.run_reference_net(_plastic_brunel_spec(N, p, seed, steps, 0.05, pdelay))
     net, pops, c = _plastic_brunel_oracle(N, p, seed, 0.05, pdelay)
     for t in range(steps):
