@@ -12,9 +12,10 @@ Printed JSON (one line, rank 0):
   value        events/s with the network resident in HBM (CUDA events on the net's stream)
   e2e          the same through the public C ABI call spice_run_record with host buffers: per
                step the dt/seed inputs go host->device and the spike raster comes back
-  roofline     the delivery kernel (dominant): algorithmic bytes (4 B int32 target per event; a
-               fixed_weight synapse has one weight per projection, no per-synapse weight) per
-               launch / its mean CUDA-event duration, against MEASURED_PEAKS.json hbm_gbs
+  roofline     the delivery kernel (dominant): algorithmic bytes per launch (8 B per synaptic
+               event: int32 target + fp32 weight) / its mean CUDA-event duration, against
+               MEASURED_PEAKS.json hbm_gbs; frac_at_4_bytes is the same against the 4-byte target
+               alone (a fixed_weight synapse has one weight per projection)
   cpu_baseline the CPU restatement of the reference step loop (oracle/oracle_bench, the same
                algorithm as the reference's single-core path) timed on this host's cores
   atomic_mode  value with the fast atomic delivery mode (order-dependent float rounding)
@@ -186,15 +187,18 @@ def _peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(threads: int | None = None, steps: int = 200, warmup: int = 50, n_neurons: int = N_NEURONS):
+def cpu_baseline(threads: int | None = None, steps: int = 200, warmup: int = 50, n_neurons: int = N_NEURONS,
+                 samples: int = 1, seed: int = SEED):
     """Times the CPU restatement of the reference step loop (oracle/oracle_bench) on the host cores.
-    Each thread runs an independent replica (seeds 1..threads); returns the aggregate."""
+    Every thread runs a replica of the benchmark's network (the same seed): `warmup` untimed steps,
+    then `samples` consecutive timed samples of `steps` steps; returns the aggregate, per-core and
+    per-sample events/s."""
     from oracle import oracle as o
     if not os.path.exists(o.BENCH_PATH):
         o.build(with_reference=False)
     threads = threads or max(1, min(8, (os.cpu_count() or 1)))
-    out = subprocess.run([o.BENCH_PATH, str(n_neurons), repr(P_CONN), str(steps), str(SEED), str(threads),
-                          str(warmup)], check=True, capture_output=True, text=True).stdout
+    out = subprocess.run([o.BENCH_PATH, str(n_neurons), repr(P_CONN), str(steps), str(seed), str(threads),
+                          str(warmup), str(samples), "1"], check=True, capture_output=True, text=True).stdout
     d = json.loads(out.strip().splitlines()[-1])
     d["kind"] = "port"
     return d
@@ -389,30 +393,36 @@ def plastic_bench(N: int = 100000, steps: int = 5000):
 
 
 def reference_arm(args):
+    """The reference's CPU implementation of the path (its C restatement: the reference binary is
+    built for x86-64 with -march=haswell and its sources are not on the GPU host) on the host cores,
+    timing the stretch the GPU arm times: replicas of the seed-1 network, warm-up to the first
+    timed step of the GPU arm (warmup x 2000 steps), then one bounded sample of 100 steps per bench
+    step."""
     ws, rank, _ = _dist()
     if rank != 0:
         return 0
-    from oracle import oracle as o
-    threads = max(1, os.cpu_count() or 1)
-    # bounded sample per bench step: 100 simulation steps of the same workload on every core
+    threads = max(1, min(16, os.cpu_count() or 1))
     per_step = 100
-    vals = []
-    kind = "port"
-    build_s = None
-    for i in range(args.warmup + args.steps):
-        d = cpu_baseline(threads=min(threads, 16), steps=per_step, warmup=10 if i == 0 else 10)
-        build_s = d["build_seconds"]
-        if i >= args.warmup:
-            vals.append(d["events_per_s"])
-    value = statistics.median(vals)
+    start = args.warmup * STEPS_PER_RUN
+    d = cpu_baseline(threads=threads, steps=per_step, warmup=start, samples=args.steps)
+    vals = d["sample_events_per_s"]
+    value = d["events_per_s"]
     line = {"metric": "synaptic_events_per_s", "value": value, "unit": "events/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "N": N_NEURONS, "p": P_CONN, "sample_steps_per_bench_step": per_step,
-                       "replicas": "one independent network per host thread (seeds 1..threads)"},
-            "cpu_baseline": {"value": value, "unit": "events/s", "cores": min(threads, 16), "kind": kind,
-                             "sample": f"{per_step} simulation steps of N=5e5 Brunel per thread after 10 warm-up "
-                                       f"steps; network build {build_s:.1f} s not timed"},
+            "ms_per_step": d["ms_per_step"] * per_step,
+            "config": {"workload": WORKLOAD, "N": N_NEURONS, "p": P_CONN, "seed": SEED, "delay_steps": 15,
+                       "mode": "deterministic", "sim_steps_per_bench_step": per_step,
+                       "first_timed_step": start,
+                       "replicas": f"{threads} host threads, each a replica of the seed-{SEED} network"},
+            "per_core_value": d["events_per_s_per_core"],
+            "sample_values": vals,
+            "cpu_baseline": {"value": value, "unit": "events/s", "cores": threads, "kind": d["kind"],
+                             "per_core": d["events_per_s_per_core"],
+                             "sample": f"{args.steps} samples of {per_step} simulation steps of the seed-{SEED} "
+                                       f"N=5e5 Brunel network per thread, starting at step {start} (the GPU "
+                                       f"arm's first timed step); network build {d['build_seconds']:.1f} s and "
+                                       f"warm-up not timed"},
             "e2e": {"value": value, "unit": "events/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
@@ -443,6 +453,15 @@ def main():
     import spice2_gb300 as sp
 
     seed = SEED + rank  # replicas: independent networks
+    from spice2_gb300.autotune import autotune, apply_shape
+    # launch shape of the delivery kernel and neuron update, measured on a copy of the network (the
+    # tuning advances the simulation); results do not depend on it
+    tnet, _ = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_DETERMINISTIC)
+    tuned = autotune(tnet, steps=300, warm=30)["best"]
+    tnet.close()
+    del tnet
+    # the benchmarked network: built fresh, so the timed stretch is steps
+    # [warmup * 2000, (warmup + steps) * 2000) of the seed's simulation
     t0 = time.perf_counter()
     net, pops = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_DETERMINISTIC)
     net.csr(0)
@@ -450,10 +469,7 @@ def main():
     build_s = time.perf_counter() - t0
     synapses = sum(net.synapses(c) for c in range(6))
     stream = torch.cuda.ExternalStream(net.stream_handle())
-
-    # launch shape of the delivery kernel, measured on this network (results do not depend on it)
-    from spice2_gb300.autotune import autotune
-    tuned = autotune(net, steps=300, warm=30)["best"]
+    apply_shape(net, tuned)
 
     clk = ClockSampler(lrank).__enter__()  # sampling starts during the warm-up (nvidia-smi start-up)
     for _ in range(args.warmup):
@@ -525,7 +541,7 @@ def main():
     if rank == 0:
         del net
         net2, _ = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_ATOMIC)
-        autotune(net2, steps=300, warm=30)
+        autotune(net2, steps=300, warm=30)  # atomic mode has its own fastest shape
         for _ in range(args.warmup):
             net2.run(STEPS_PER_RUN)
         net2.synchronize()
@@ -583,10 +599,13 @@ def main():
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
         try:
-            d = cpu_baseline(steps=200, warmup=20)
+            start = args.warmup * STEPS_PER_RUN
+            d = cpu_baseline(steps=200, warmup=start)
             cpu = {"value": d["events_per_s"], "unit": "events/s", "cores": d["threads"], "kind": d["kind"],
-                   "sample": f"{d['steps']} steps of N=5e5 Brunel per thread ({d['threads']} independent replicas, "
-                             f"seeds 1..{d['threads']}) after 20 warm-up steps; build {d['build_seconds']:.1f} s untimed"}
+                   "per_core": d["events_per_s_per_core"],
+                   "sample": f"{d['steps']} steps of the seed-{SEED} N=5e5 Brunel network per thread "
+                             f"({d['threads']} replicas) from step {start}, the first step of the GPU timed "
+                             f"stretch; build {d['build_seconds']:.1f} s and warm-up untimed"}
         except Exception as e:  # the baseline is reported, never a reason to fail the bench
             cpu = {"value": None, "unit": "events/s", "cores": 0, "kind": "port", "sample": f"failed: {e}"}
 
@@ -597,6 +616,7 @@ def main():
         "config": {"workload": WORKLOAD, "N": N_NEURONS, "p": P_CONN, "synapses": synapses,
                    "sim_steps_per_bench_step": STEPS_PER_RUN, "dt": DT,
                    "delay_steps": 15, "mode": "deterministic", "seed": SEED,
+                   "first_timed_step": args.warmup * STEPS_PER_RUN,
                    "parallelism": f"replicas{ws}" if ws > 1 else "single",
                    "delivery_shape": tuned,
                    "l2": "inputs larger than L2 (1 GB of CSR targets; a window reads ~42 MB of random rows)"},

@@ -190,21 +190,22 @@ int spice_get_synapse_state(spice_net* net, int conn, int field, float* out);
 int spice_get_csr(spice_net* net, int conn, int64_t* offsets_out, int32_t* neighbors_out);
 
 /* fixed_probability(p) adjacency of one projection (the generator behind
- * spice_connect_fixed_probability) for callers that cannot allocate device memory: code recording a
- * stream capture, real-time loops whose memory is fixed up front, and hosts that own every device
- * buffer themselves (a framework's caching allocator, a cgo or JNI runtime handing out an arena).
- * No counterpart in the reference.  It allocates nothing: every intermediate buffer lives in one
- * static device array of about 4.3 MiB inside this library, held by every GPU that loads the library
- * until the process exits.  The caller passes device buffers: offsets (src_count + 1 int64) and
- * neighbors (neighbors_capacity int32); the seed is the 128-bit util::seed_seq value
- * (seed_lo, seed_hi) of the projection, and the result equals the reference's
- * fixed_probability::generate (spice/src/topology.cpp:78-112) for that seed.
+ * spice_connect_fixed_probability) for callers that cannot allocate device memory: real-time loops
+ * whose device memory is fixed up front (an allocation may block or fail mid-run), and hosts that
+ * own every device buffer themselves (a framework's caching allocator, a cgo or JNI runtime handing
+ * out an arena).  No counterpart in the reference.  It allocates nothing: every intermediate buffer
+ * lives in one static device array of about 4.3 MiB inside this library, held by every GPU that
+ * loads the library until the process exits.  The caller passes device buffers: offsets
+ * (src_count + 1 int64) and neighbors (neighbors_capacity int32); the seed is the 128-bit
+ * util::seed_seq value (seed_lo, seed_hi) of the projection.  The result equals the adjacency
+ * spice_connect_fixed_probability generates for a projection with that seed.
  * Limits: src_count <= 65536 and src_count * (max_degree + 1) <= 262144 draws (max_degree =
  * floor(dst*p + 3 sqrt(dst*p*(1-p)))); larger requests fail with SPICE_EINVAL.  A neighbors buffer
  * that is too small fails with SPICE_EOVERFLOW and *synapses_out = the size needed.
- * The first call on each device looks up the scratch array's device address; make that first call
- * before any stream capture.  Every call uses the same scratch, so calls whose GPU work overlaps
- * (on different streams or threads) race: serialise them.  The call synchronises `stream` (a
+ * The first call on a device (and the first after its context was reset) looks up the scratch
+ * array's device address; make that first call before any stream capture.  Every call uses the
+ * same scratch, which keeps the previous call's contents, so calls whose GPU work overlaps (on
+ * different streams or threads) race: serialise them.  The call synchronises `stream` (a
  * cudaStream_t, NULL for the default stream) once, to read the synapse count. */
 int spice_fixed_probability_noalloc(int64_t src_count, int64_t dst_count, double p, uint64_t seed_lo,
                                     uint64_t seed_hi, int64_t* offsets, int32_t* neighbors,

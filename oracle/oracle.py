@@ -20,19 +20,25 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libspice_oracle.so")
 BENCH_PATH = os.path.join(HERE, "_build", "oracle_bench")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
-REF_SOURCES = os.environ.get("SPICE_REFERENCE_DIR", "/root/reference")
+# directory of the reference's sources (only needed to build the reference driver)
+REF_SOURCES = os.environ.get("SPICE_REFERENCE_DIR")
 
 POISSON, LIF, LIF_COND, EXTERNAL = 0, 1, 2, 3
 SYN_ISTDP, SYN_COUNT = 1, 2  # plastic models of spo_set_plastic
 
 
-def build(with_reference: bool | None = None) -> None:
-    """Compiles the restatement (and the reference driver when its sources are present)."""
+def build(with_reference: bool | None = None, reference_dir: str | None = None) -> None:
+    """Compiles the restatement, and the reference driver when the reference's sources are given
+    (reference_dir, else the SPICE_REFERENCE_DIR environment variable) and present."""
     subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    ref = reference_dir or REF_SOURCES
     if with_reference is None:
-        with_reference = os.path.isdir(os.path.join(REF_SOURCES, "spice", "src"))
+        with_reference = bool(ref) and os.path.isdir(os.path.join(ref, "spice", "src"))
     if with_reference:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SOURCES}"], check=True)
+        if not ref:
+            raise RuntimeError("the reference driver needs the reference's source directory "
+                               "(reference_dir or SPICE_REFERENCE_DIR)")
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)
 
 
 class _U128(C.Structure):
@@ -265,6 +271,37 @@ def brunel(N: int, p: float, seed: int, dt=1e-4, delay=15e-4):
     return net, (P, E, I)
 
 
+def vogels_weights(N: int) -> tuple[float, float]:
+    """samples/vogels.cpp:72-75: float(6.4e6 / (N * N)) and float(8.16e7 / (N * N)) (double, then float)."""
+    return float(np.float32(6.4e6 / (N * N))), float(np.float32(8.16e7 / (N * N)))
+
+
+def vogels(N: int, seed: int = 1337, p: float = 0.02, dt=1e-4, delay=8e-4, we=None, wi=None):
+    """samples/vogels.cpp:62-86 (E = 0.8 N, I = 0.2 N conductance LIF; E->E, E->I excitatory,
+    I->E, I->I inhibitory, fixed_probability(p)).  Returns (net, (E, I))."""
+    dwe, dwi = vogels_weights(N)
+    we = dwe if we is None else we
+    wi = dwi if wi is None else wi
+    net = Net(dt, delay, [seed])
+    E = net.add_population(LIF_COND, N * 8 // 10)
+    I = net.add_population(LIF_COND, N * 2 // 10)
+    for s, d, w, fl in ((E, E, we, 1), (E, I, we, 1), (I, E, wi, 2), (I, I, wi, 2)):
+        net.connect(s, d, p, delay, w, fl)
+    return net, (E, I)
+
+
+def vogels_spec(N: int, seed: int, steps: int, p: float = 0.02, dt=1e-4, delay=8e-4, we=None,
+                wi=None) -> list[str]:
+    """The same network as a ref_driver spec."""
+    dwe, dwi = vogels_weights(N)
+    we = dwe if we is None else we
+    wi = dwi if wi is None else wi
+    lines = [f"{dt!r} {delay!r} {seed} {steps} 0", f"pop lif_cond {N * 8 // 10}", f"pop lif_cond {N * 2 // 10}"]
+    for s, d, w, fl in ((0, 0, we, 1), (0, 1, we, 1), (1, 0, wi, 2), (1, 1, wi, 2)):
+        lines.append(f"conn {s} {d} {p!r} {delay!r} {w!r} {fl}")
+    return lines
+
+
 def brunel_weights(N: int, p: float) -> tuple[float, float]:
     """float((2/N)(0.1/p)) and float((-10/N)(0.1/p)), computed in double then rounded."""
     return float(np.float32((2.0 / N) * (0.1 / p))), float(np.float32((-10.0 / N) * (0.1 / p)))
@@ -311,18 +348,45 @@ def read_reference_net(buf: bytes):
     return {"sizes": sizes, "steps": steps, "dt": dts, "raster": raster, "_rest": buf[pos:]}
 
 
-def reference_states(res, lif_pops):
-    """Splits the trailing (V, T) pairs of the LIF populations out of a reference result."""
+def reference_states(res, lif_pops, cond_pops=()):
+    """Splits the trailing neuron states out of a reference result, populations in add order:
+    (V, T) for each LIF population in lif_pops, (V, Gex, Gin, T) for each conductance LIF in
+    cond_pops (the ref_driver writes them in population order)."""
     rest = res["_rest"]
     pos = 0
     out = {}
-    for k in lif_pops:
+    for k in sorted(set(lif_pops) | set(cond_pops)):
         n = res["sizes"][k]
-        rec = np.frombuffer(rest, dtype=np.dtype([("V", "<f4"), ("T", "<i4")]), count=n, offset=pos)
-        out[k] = (rec["V"].copy(), rec["T"].copy())
-        pos += 8 * n
+        if k in cond_pops:
+            dt = np.dtype([("V", "<f4"), ("Gex", "<f4"), ("Gin", "<f4"), ("T", "<i4")])
+            rec = np.frombuffer(rest, dtype=dt, count=n, offset=pos)
+            out[k] = (rec["V"].copy(), rec["Gex"].copy(), rec["Gin"].copy(), rec["T"].copy())
+            pos += 16 * n
+        else:
+            rec = np.frombuffer(rest, dtype=np.dtype([("V", "<f4"), ("T", "<i4")]), count=n, offset=pos)
+            out[k] = (rec["V"].copy(), rec["T"].copy())
+            pos += 8 * n
     build_s, step_s = struct.unpack_from("<dd", rest, pos)
     return out, build_s, step_s
+
+
+def run_reference_brunel_ck(N: int, p: float, seed: int, steps: int, block: int):
+    """Runs Brunel on oracle/_ref/ref_driver (brunel_ck): returns (counts[steps][3] int32,
+    blocks[nblocks][3] uint64 = raster checksum of each block of `block` steps and the E / I state
+    checksums at its end)."""
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "ck.bin")
+        subprocess.run([REF_DRIVER, "brunel_ck", str(N), repr(p), str(seed), str(steps), str(block), out], check=True)
+        buf = open(out, "rb").read()
+    counts, blocks, pos, t = [], [], 0, 0
+    while t < steps:
+        n = min(block, steps - t)
+        counts.append(np.frombuffer(buf, dtype=np.int32, count=3 * n, offset=pos).reshape(n, 3))
+        pos += 12 * n
+        blocks.append(np.frombuffer(buf, dtype=np.uint64, count=3, offset=pos))
+        pos += 24
+        t += n
+    return np.concatenate(counts).copy(), np.array(blocks, dtype=np.uint64)
 
 
 def run_reference_gen(src: int, dst: int, p: float, seed: int):

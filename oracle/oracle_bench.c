@@ -2,10 +2,12 @@
  * oracle_bench.c -- times the CPU restatement of snn::step on the Brunel network
  * (TEST INFRASTRUCTURE ONLY: bench.py's cpu_baseline / --impl reference leg runs it).
  *
- * usage: oracle_bench N P STEPS SEED0 THREADS [WARMUP]
- *   Builds THREADS independent Brunel networks (seeds SEED0, SEED0+1, ...; the same model as
- *   samples/brunel.cpp:75-116 with weights scaled by 0.1/P), one per thread, runs WARMUP
- *   untimed steps, then times STEPS steps of all networks in parallel.  Prints one JSON line.
+ * usage: oracle_bench N P STEPS SEED0 THREADS [WARMUP [SAMPLES [SAME_SEED]]]
+ *   Builds THREADS Brunel networks (the model of samples/brunel.cpp:75-116 with weights scaled by
+ *   0.1/P), one per thread, with seeds SEED0, SEED0+1, ... or, with SAME_SEED = 1, all with SEED0
+ *   (replicas of one simulation), runs WARMUP untimed steps, then times SAMPLES consecutive samples
+ *   of STEPS steps of all networks in parallel (default 1).  Prints one JSON line: the aggregate
+ *   events/s over all samples, per core, and per sample.
  */
 #define _POSIX_C_SOURCE 200809L
 #include <math.h>
@@ -16,11 +18,14 @@
 
 #include "spice_oracle.h"
 
+#define MAX_SAMPLES 1024
+
 typedef struct {
 	long long N, steps, warmup;
+	int samples;
 	double p;
 	unsigned seed;
-	long long events, spikes;
+	long long events[MAX_SAMPLES];
 	double build_s;
 	spo_net* net;
 	pthread_barrier_t* bar;
@@ -58,11 +63,13 @@ static void* worker(void* arg) {
 	j->net      = brunel(j->N, j->p, j->seed);
 	j->build_s  = now() - t0;
 	spo_run(j->net, j->warmup);
-	long long e0 = spo_events(j->net);
-	pthread_barrier_wait(j->bar);
-	spo_run(j->net, j->steps);
-	j->events = spo_events(j->net) - e0;
-	pthread_barrier_wait(j->bar);
+	for (int k = 0; k < j->samples; k++) {
+		long long e0 = spo_events(j->net);
+		pthread_barrier_wait(j->bar);
+		spo_run(j->net, j->steps);
+		j->events[k] = spo_events(j->net) - e0;
+		pthread_barrier_wait(j->bar);
+	}
 	return NULL;
 }
 
@@ -77,31 +84,52 @@ int main(int argc, char** argv) {
 	unsigned seed0  = (unsigned)atoll(argv[4]);
 	int T           = atoi(argv[5]);
 	long long warm  = argc > 6 ? atoll(argv[6]) : 0;
+	int samples     = argc > 7 ? atoi(argv[7]) : 1;
+	int same_seed   = argc > 8 ? atoi(argv[8]) : 0;
 	if (T < 1) T = 1;
+	if (samples < 1) samples = 1;
+	if (samples > MAX_SAMPLES) samples = MAX_SAMPLES;
 	pthread_barrier_t bar;
 	pthread_barrier_init(&bar, NULL, (unsigned)T + 1);
 	job* jobs      = (job*)calloc((size_t)T, sizeof(job));
 	pthread_t* th  = (pthread_t*)calloc((size_t)T, sizeof(pthread_t));
 	for (int i = 0; i < T; i++) {
-		jobs[i] = (job){N, steps, warm, p, seed0 + (unsigned)i, 0, 0, 0, NULL, &bar};
+		jobs[i].N = N;
+		jobs[i].steps = steps;
+		jobs[i].warmup = warm;
+		jobs[i].samples = samples;
+		jobs[i].p = p;
+		jobs[i].seed = same_seed ? seed0 : seed0 + (unsigned)i;
+		jobs[i].bar = &bar;
 		pthread_create(&th[i], NULL, worker, &jobs[i]);
 	}
-	pthread_barrier_wait(&bar);
-	double t0 = now();
-	pthread_barrier_wait(&bar);
-	double t1 = now();
+	double* dts = (double*)calloc((size_t)samples, sizeof(double));
+	for (int k = 0; k < samples; k++) {
+		pthread_barrier_wait(&bar);
+		double t0 = now();
+		pthread_barrier_wait(&bar);
+		dts[k] = now() - t0;
+	}
 	long long ev = 0;
-	double build = 0;
+	double build = 0, dt = 0;
+	for (int i = 0; i < T; i++) pthread_join(th[i], NULL);
 	for (int i = 0; i < T; i++) {
-		pthread_join(th[i], NULL);
-		ev += jobs[i].events;
+		for (int k = 0; k < samples; k++) ev += jobs[i].events[k];
 		build = build > jobs[i].build_s ? build : jobs[i].build_s;
 		spo_net_destroy(jobs[i].net);
 	}
-	double dt = t1 - t0;
+	for (int k = 0; k < samples; k++) dt += dts[k];
 	printf("{\"events\": %lld, \"step_seconds\": %.6f, \"build_seconds\": %.6f, \"threads\": %d, "
-	       "\"steps\": %lld, \"N\": %lld, \"p\": %g, \"events_per_s\": %.6g, \"ms_per_step\": %.6f}\n",
-	       ev, dt, build, T, steps, N, p, ev / dt, 1e3 * dt / (double)steps);
+	       "\"steps\": %lld, \"samples\": %d, \"warmup\": %lld, \"same_seed\": %d, \"N\": %lld, \"p\": %g, "
+	       "\"events_per_s\": %.6g, \"events_per_s_per_core\": %.6g, \"ms_per_step\": %.6f, \"sample_events_per_s\": [",
+	       ev, dt, build, T, steps, samples, warm, same_seed, N, p, ev / dt, ev / dt / T, 1e3 * dt / (double)(steps * samples));
+	for (int k = 0; k < samples; k++) {
+		long long e = 0;
+		for (int i = 0; i < T; i++) e += jobs[i].events[k];
+		printf("%s%.6g", k ? ", " : "", e / dts[k]);
+	}
+	printf("]}\n");
+	free(dts);
 	free(jobs);
 	free(th);
 	return 0;

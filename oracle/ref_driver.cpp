@@ -14,10 +14,18 @@
 //   ref_driver bcsr N P SEED     checksums of the six Brunel CSRs, seeded as snn seeds them:
 //                                seed_seq{SEED}, one seed per stateful population (E, I), then
 //                                one per connection (snn.h:21-48, neuron_population.h:56-60)
+//   ref_driver brunel_ck N P SEED STEPS BLOCK OUT
+//                                runs the Brunel network (samples/brunel.cpp with weights x 0.1/P)
+//                                for STEPS steps and writes, per step, the spike count of P, E, I
+//                                (int32 x 3) and, per block of BLOCK steps, the raster checksum of
+//                                the block and the E and I state checksums at its end (uint64 x 3);
+//                                the checksums are oracle.raster_checksum / state_checksum
 //
 // SPEC (text):  dt max_delay seed steps dump_csr
-//               pop poisson SIZE RATE | pop lif SIZE
-//               conn SRC DST P DELAY WEIGHT        (fixed_probability + fixed_weight)
+//               pop poisson SIZE RATE | pop lif SIZE | pop lif_cond SIZE
+//               conn SRC DST P DELAY WEIGHT        (fixed_probability + fixed_weight into a lif)
+//               conn SRC DST P DELAY WEIGHT FIELD  (into a lif_cond: FIELD 1 excitatory (Gex),
+//                                                   2 inhibitory (Gin), samples/vogels.cpp:48-60)
 //               adj SRC DST DELAY WEIGHT M s0 d0 s1 d1 ...   (adj_list + fixed_weight)
 //               plastic POP P DELAY SCALE        (POP -> POP fixed_probability + count_syn; the
 //                                                 reference keeps the history of a plastic
@@ -62,9 +70,58 @@ struct lif {
 	}
 };
 
+// The conductance-based LIF of samples/vogels.cpp:10-46, as written there.
+struct lif_cond {
+	struct neuron {
+		float V     = -0.06;
+		float Gex   = 0;
+		float Gin   = 0;
+		Int32 Twait = 0;
+	};
+
+	bool update(neuron& n, float const dt, auto&) const {
+		Int32 const Tref    = 50;          // dt
+		float const Vrest   = -0.06;       // v
+		float const Vthres  = -0.05;       // v
+		float const TmemInv = 1.0f / 0.02; // s
+		float const Eex     = 0.0;         // v
+		float const Ein     = -0.08;       // v
+		float const Ibg     = 0.02;        // v
+
+		float const TexInv = 1.0f / 0.005; // s
+		float const TinInv = 1.0f / 0.01;  // s
+
+		bool spiked = false;
+		if (--n.Twait <= 0) {
+			if (n.V > Vthres) {
+				n.V     = Vrest;
+				n.Twait = Tref;
+				spiked  = true;
+			} else
+				n.V += ((Vrest - n.V) + n.Gex * (Eex - n.V) + n.Gin * (Ein - n.V) + Ibg) *
+				       (dt * TmemInv);
+		}
+
+		n.Gex -= n.Gex * (dt * TexInv);
+		n.Gin -= n.Gin * (dt * TinInv);
+
+		return spiked;
+	}
+};
+
 struct fixed_weight {
 	float weight;
 	void deliver(lif::neuron& to) const { to.V += weight; }
+};
+
+// samples/vogels.cpp:48-60
+struct excitatory {
+	float weight;
+	void deliver(lif_cond::neuron& to) const { to.Gex += weight; }
+};
+struct inhibitory {
+	float weight;
+	void deliver(lif_cond::neuron& to) const { to.Gin += weight; }
 };
 
 // The counting plastic synapse of test/detail/synapse_population.cpp:84-94 (update adds 1, skip
@@ -144,6 +201,70 @@ static int run_bcsr(int argc, char** argv) {
 	return 0;
 }
 
+// Order-sensitive checksums of a raster block and of a LIF population's state (the same functions
+// as oracle.raster_checksum / oracle.state_checksum in oracle/oracle.py).
+struct raster_ck {
+	UInt a = 0, b = 0, j = 0, i = 0;
+	void add_count(Int n) { b += (UInt(n) + 7) * ((i++ * 0xD1B54A32D192ED03ull) | 1); }
+	void add_spike(Int32 x) { a += (UInt(Int(x)) + 1) * ((j++ * 0x9E3779B97F4A7C15ull) | 1); }
+	UInt value() const { return a ^ b; }
+};
+
+static UInt state_ck(std::span<lif::neuron const> ns) {
+	UInt h1 = 0, h2 = 0, i = 0;
+	for (auto const& n : ns) {
+		UInt32 v;
+		memcpy(&v, &n.V, 4);
+		h1 += (UInt(v) + 3) * ((i * 0x9E3779B97F4A7C15ull) | 1);
+		h2 += (UInt(UInt32(Int32(n.Twait))) + 5) * ((i * 0xD1B54A32D192ED03ull) | 1);
+		i++;
+	}
+	return h1 ^ h2;
+}
+
+static int run_brunel_ck(int argc, char** argv) {
+	if (argc < 8) return 2;
+	Int const N = atoll(argv[2]);
+	double const p = atof(argv[3]);
+	unsigned const seed = (unsigned)atoll(argv[4]);
+	Int const steps = atoll(argv[5]), block = atoll(argv[6]);
+	if (block < 1) return 2;
+	float const dt = 1e-4f, delay = 15e-4f;
+	snn net(dt, delay, {seed});
+	auto* P = net.add_population<poisson>(N / 2, {20.0f});
+	auto* E = net.add_population<lif>(N * 4 / 10);
+	auto* I = net.add_population<lif>(N / 10);
+	float const we = (float)((2.0 / N) * (0.1 / p)), wi = (float)((-10.0 / N) * (0.1 / p));
+	net.connect<fixed_weight>(P, E, fixed_probability(p), delay, {we});
+	net.connect<fixed_weight>(P, I, fixed_probability(p), delay, {we});
+	net.connect<fixed_weight>(E, E, fixed_probability(p), delay, {we});
+	net.connect<fixed_weight>(E, I, fixed_probability(p), delay, {we});
+	net.connect<fixed_weight>(I, E, fixed_probability(p), delay, {wi});
+	net.connect<fixed_weight>(I, I, fixed_probability(p), delay, {wi});
+	FILE* f = fopen(argv[7], "wb");
+	if (!f) return 2;
+	detail::NeuronPopulation* pops[3] = {P, E, I};
+	raster_ck ck;
+	for (Int t = 0; t < steps; t++) {
+		net.step();
+		for (auto* q : pops) {
+			auto sp = q->spikes(0);
+			put(f, (Int32)sp.size());
+			ck.add_count((Int)sp.size());
+		}
+		for (auto* q : pops)
+			for (Int32 x : q->spikes(0)) ck.add_spike(x);
+		if ((t + 1) % block == 0 || t + 1 == steps) {
+			put(f, ck.value());
+			put(f, state_ck(E->get_neurons()));
+			put(f, state_ck(I->get_neurons()));
+			ck = raster_ck{};
+		}
+	}
+	fclose(f);
+	return 0;
+}
+
 static int run_rng(int argc, char** argv) {
 	if (argc < 5) return 2;
 	unsigned seed = (unsigned)atoll(argv[2]);
@@ -173,11 +294,21 @@ static int run_rng(int argc, char** argv) {
 }
 
 struct pop_rec {
-	bool is_lif;
+	int kind;  // 0 poisson, 1 lif, 2 lif_cond
 	Int size;
 	detail::NeuronPopulation* base;
 	detail::neuron_population<lif>* L;
+	detail::neuron_population<lif_cond>* C;
+	bool is_lif() const { return kind == 1; }
 };
+
+// net.connect<Syn>(pops[s], to, topo, delay, {w}) with the source population's own type.
+template <class Syn, class To, class Topo>
+static void connect_from(snn& net, pop_rec const& s, To* to, Topo&& topo, float delay, float w) {
+	if (s.kind == 1) net.connect<Syn>(s.L, to, topo, delay, {w});
+	else if (s.kind == 2) net.connect<Syn>(s.C, to, topo, delay, {w});
+	else net.connect<Syn>(static_cast<detail::neuron_population<poisson>*>(s.base), to, topo, delay, {w});
+}
 
 static int run_net(int argc, char** argv) {
 	if (argc < 4) return 2;
@@ -200,10 +331,13 @@ static int run_net(int argc, char** argv) {
 				float rate;
 				in >> rate;
 				auto* P = net.add_population<poisson>(size, {rate});
-				pops.push_back({false, size, P, nullptr});
+				pops.push_back({0, size, P, nullptr, nullptr});
+			} else if (kind == "lif_cond") {
+				auto* C = net.add_population<lif_cond>(size);
+				pops.push_back({2, size, C, nullptr, C});
 			} else {
 				auto* L = net.add_population<lif>(size);
-				pops.push_back({true, size, L, L});
+				pops.push_back({1, size, L, L, nullptr});
 			}
 		} else if (kw == "plastic") {
 			Int q;
@@ -218,27 +352,27 @@ static int run_net(int argc, char** argv) {
 			if (kw == "conn") in >> p;
 			float delay, w;
 			in >> delay >> w;
-			auto* L = pops[d].L;
-			if (kw == "conn") {
-				if (pops[s].is_lif)
-					net.connect<fixed_weight>(pops[s].L, L, fixed_probability(p), delay, {w});
-				else
-					net.connect<fixed_weight>(static_cast<detail::neuron_population<poisson>*>(pops[s].base), L,
-					                             fixed_probability(p), delay, {w});
-			} else {
+			int field = 0;
+			if (pops[d].kind == 2) in >> field;
+			adj_list adj;
+			if (kw == "adj") {
 				Int m;
 				in >> m;
-				adj_list adj;
 				for (Int i = 0; i < m; i++) {
 					Int a, b;
 					in >> a >> b;
 					adj.connect(a, b);
 				}
-				if (pops[s].is_lif)
-					net.connect<fixed_weight>(pops[s].L, L, adj, delay, {w});
-				else
-					net.connect<fixed_weight>(static_cast<detail::neuron_population<poisson>*>(pops[s].base), L, adj,
-					                             delay, {w});
+			}
+			if (pops[d].kind == 1) {
+				if (kw == "conn") connect_from<fixed_weight>(net, pops[s], pops[d].L, fixed_probability(p), delay, w);
+				else connect_from<fixed_weight>(net, pops[s], pops[d].L, adj, delay, w);
+			} else if (field == 1) {
+				if (kw == "conn") connect_from<excitatory>(net, pops[s], pops[d].C, fixed_probability(p), delay, w);
+				else connect_from<excitatory>(net, pops[s], pops[d].C, adj, delay, w);
+			} else {
+				if (kw == "conn") connect_from<inhibitory>(net, pops[s], pops[d].C, fixed_probability(p), delay, w);
+				else connect_from<inhibitory>(net, pops[s], pops[d].C, adj, delay, w);
 			}
 		}
 	}
@@ -265,9 +399,16 @@ static int run_net(int argc, char** argv) {
 			fwrite(raster[t][k].data(), sizeof(Int32), raster[t][k].size(), f);
 		}
 	for (auto& p : pops)
-		if (p.is_lif)
+		if (p.kind == 1)
 			for (auto& n : p.L->get_neurons()) {
 				put(f, n.V);
+				put(f, (Int32)n.Twait);
+			}
+		else if (p.kind == 2)
+			for (auto& n : p.C->get_neurons()) {
+				put(f, n.V);
+				put(f, n.Gex);
+				put(f, n.Gin);
 				put(f, (Int32)n.Twait);
 			}
 	put(f, std::chrono::duration<double>(t1 - t0).count());
@@ -284,6 +425,7 @@ int main(int argc, char** argv) {
 		if (!strcmp(argv[1], "gen")) return run_gen(argc, argv);
 		if (!strcmp(argv[1], "rng")) return run_rng(argc, argv);
 		if (!strcmp(argv[1], "bcsr")) return run_bcsr(argc, argv);
+		if (!strcmp(argv[1], "brunel_ck")) return run_brunel_ck(argc, argv);
 	} catch (std::exception const& e) {
 		fprintf(stderr, "%s\n", e.what());
 		return 3;

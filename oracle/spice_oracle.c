@@ -416,24 +416,34 @@ static inline int spo_lif_update(float* V, int32_t* T, float dt, float om, float
 	return 0;
 }
 
-/* Conductance LIF (samples/vogels.cpp:10-46), restated with strict float arithmetic in the
- * order written in the sample. */
+/* Conductance LIF (samples/vogels.cpp:10-46) as the reference's -ffast-math -march=haswell build
+ * executes it.  GCC 13 folds Vrest + Ibg into one constant (-0.06f + 0.02f = -0.04f), drops
+ * Eex = 0, contracts the two products around it into fused multiply-adds and turns the
+ * conductance decay G -= G * (dt * Inv) into G * fma(-dt, Inv, 1), like the Brunel leak:
+ *   V   = fma(dt * TmemInv, (-0.04f - V) + fma(-Gex, V, Gin * (Ein - V)), V)
+ *   Gex = Gex * fma(-dt, TexInv, 1),  Gin = Gin * fma(-dt, TinInv, 1)
+ * (the conductances of the V update are the values before their decay, as in the source order).
+ * Pinned to the reference binary's states over whole runs (tests/test_oracle.py). */
 static inline int spo_lifc_update(float* V, float* Gex, float* Gin, int32_t* T, float dt) {
 	const int32_t Tref  = 50;
 	const float Vrest   = -0.06f, Vthres = -0.05f, TmemInv = 1.0f / 0.02f;
-	const float Eex = 0.0f, Ein = -0.08f, Ibg = 0.02f;
+	const float Ein = -0.08f, VrestIbg = -0.06f + 0.02f;
 	const float TexInv = 1.0f / 0.005f, TinInv = 1.0f / 0.01f;
 	int spiked = 0;
+	float const gex = *Gex, gin = *Gin;
 	if (--(*T) <= 0) {
 		if (*V > Vthres) {
 			*V = Vrest; *T = Tref; spiked = 1;
 		} else {
-			float v = *V;
-			*V = v + ((Vrest - v) + *Gex * (Eex - v) + *Gin * (Ein - v) + Ibg) * (dt * TmemInv);
+			float const v = *V;
+			float const a = gin * (Ein - v);
+			float const b = fmaf(-gex, v, a);
+			float const c = (VrestIbg - v) + b;
+			*V = fmaf(dt * TmemInv, c, v);
 		}
 	}
-	*Gex = *Gex - *Gex * (dt * TexInv);
-	*Gin = *Gin - *Gin * (dt * TinInv);
+	*Gex = gex * fmaf(-dt, TexInv, 1.0f);
+	*Gin = gin * fmaf(-dt, TinInv, 1.0f);
 	return spiked;
 }
 

@@ -88,6 +88,15 @@ def autotune(net, steps: int = 600, warm: int = 60, candidates=None, verbose: bo
     return {"best": best, "results": results}
 
 
+def apply_shape(net, best: dict) -> None:
+    """Applies a shape returned by autotune() (delivery shape and, when present, the neuron-update
+    variant) to another network of the same structure."""
+    net.set_tuning(tile_bytes=best["tile_bytes"], deliver_threads=best["threads"], deliver_parts=best["parts"],
+                   deliver_algo=best["algo"])
+    if "neuron_variant" in best:
+        net.set_tuning(neuron_variant=best["neuron_variant"])
+
+
 def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4, 5, 6), verbose: bool = False) -> dict:
     """Times the neuron-update kernel of `net` for each LIF window variant (identical results);
     applies and returns the fastest."""

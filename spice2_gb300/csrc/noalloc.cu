@@ -1,13 +1,17 @@
 // noalloc.cu -- fixed_probability generation for callers that cannot allocate device memory.
 //
-// Some hosts of this library must not call cudaMalloc: code running inside a stream capture or a
-// CUDA graph being built, real-time loops whose memory is fixed up front, and runtimes that hand
-// the library a fixed arena of buffers (a framework's caching allocator, a JNI/cgo host that owns
-// every device allocation).  spice_fixed_probability_noalloc gives them the GPU generator of
-// fixed_probability adjacency with every intermediate buffer (exponential gaps, their fixed-point
-// prefix, row lengths, scan sums, jump polynomials) placed in one file-scope static device array
-// of fixed size.  The caller passes only the output buffers.
+// Some hosts of this library must not call cudaMalloc: real-time loops whose device memory is
+// fixed up front (an allocation can block and can fail at any time), and runtimes that hand the
+// library a fixed arena of buffers because they own every device allocation themselves (a
+// framework's caching allocator, a JNI/cgo host with its own pool).  spice_fixed_probability_noalloc
+// gives them the GPU generator of fixed_probability adjacency with every intermediate buffer
+// (exponential gaps, their fixed-point prefix, row lengths, scan sums, jump polynomials) placed in
+// one file-scope static device array of fixed size.  The caller passes only the output buffers.
+// The call synchronises its stream once (it reads the synapse count back to the host before the
+// adjacency is filled).
 #include <stdint.h>
+
+#include <cuda.h>
 
 #include <mutex>
 #include <string>
@@ -47,22 +51,45 @@ static __device__ __align__(256) unsigned char g_gen_scratch[kScratchBytes];
 
 constexpr int kMaxDevices = 256;
 std::mutex g_setup_mutex;
-void* g_scratch_ptr[kMaxDevices] = {};
+void* g_scratch_ptr[kMaxDevices]  = {};
+CUcontext g_scratch_ctx[kMaxDevices] = {};  // the context the address was looked up in
+
+// cuCtxGetCurrent, reached through the runtime (the library does not link the driver API).
+using ctx_get_fn = CUresult (*)(CUcontext*);
+ctx_get_fn ctx_get_current() {
+	static ctx_get_fn fn = [] {
+		void* f = nullptr;
+		cudaDriverEntryPointQueryResult q;
+		if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+		    q != cudaDriverEntryPointSuccess)
+			f = nullptr;
+		return reinterpret_cast<ctx_get_fn>(f);
+	}();
+	return fn;
+}
 
 // Host code cannot use &g_gen_scratch (that is a host-side stand-in, not a device address): the
-// device address is looked up once per device, with that device current.
+// device address is looked up with the device current, the first time a device is used and again
+// whenever the calling thread's current context is not the one of the last lookup (after a
+// cudaDeviceReset the old address belongs to a destroyed context; the lookup itself creates the new
+// primary context).
 int scratch_address(void** out) {
 	int dev = 0;
 	cudaError_t e = cudaGetDevice(&dev);
 	if (e != cudaSuccess) return set_last_error(SPICE_ECUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
 	if (dev < 0 || dev >= kMaxDevices) return set_last_error(SPICE_EINVAL, "device ordinal out of range");
+	ctx_get_fn const get = ctx_get_current();
+	CUcontext ctx = nullptr;
+	if (get && get(&ctx) != CUDA_SUCCESS) ctx = nullptr;
 	std::lock_guard<std::mutex> lock(g_setup_mutex);
-	if (!g_scratch_ptr[dev]) {
+	if (!g_scratch_ptr[dev] || !ctx || ctx != g_scratch_ctx[dev]) {
 		void* p = nullptr;
 		e       = cudaGetSymbolAddress(&p, g_gen_scratch);
 		if (e != cudaSuccess || !p)
 			return set_last_error(SPICE_ECUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+		if (get && get(&ctx) != CUDA_SUCCESS) ctx = nullptr;
 		g_scratch_ptr[dev] = p;
+		g_scratch_ctx[dev] = ctx;
 	}
 	*out = g_scratch_ptr[dev];
 	return SPICE_OK;
@@ -76,9 +103,10 @@ extern "C" int spice_fixed_probability_noalloc(int64_t src_count, int64_t dst_co
 	if (synapses_out) *synapses_out = 0;
 	if (!offsets || (!neighbors && neighbors_capacity > 0) || !synapses_out)
 		return set_last_error(SPICE_EINVAL, "offsets, neighbors and synapses_out must not be NULL");
-	if (!(0 <= p && p <= 1)) return set_last_error(SPICE_EINVAL, "Assertion failed (topology.cpp:79): 0 <= p && p <= 1");
+	if (!(0 <= p && p <= 1))
+		return set_last_error(SPICE_EINVAL, "spice_fixed_probability_noalloc: p must be in [0, 1]");
 	if (src_count < 0 || dst_count < 0 || src_count >= INT32_MAX || dst_count >= INT32_MAX)
-		return set_last_error(SPICE_EINVAL, "Assertion failed (topology.cpp:51): 0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
+		return set_last_error(SPICE_EINVAL, "spice_fixed_probability_noalloc: src_count and dst_count must be in [0, 2^31 - 1)");
 	if (src_count > kMaxSrc)
 		return set_last_error(SPICE_EINVAL, "spice_fixed_probability_noalloc: src_count " + std::to_string(src_count) +
 		                                         " exceeds the static scratch limit of " + std::to_string(kMaxSrc) + " rows");

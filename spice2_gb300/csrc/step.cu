@@ -61,11 +61,15 @@ __device__ __forceinline__ bool lif_update(float& V, int32_t& T, float om, float
 	return false;
 }
 
-// Conductance LIF (samples/vogels.cpp:10-46), strict float arithmetic in source order.
+// Conductance LIF (samples/vogels.cpp:10-46) as the reference's -ffast-math -march=haswell build
+// computes it: Vrest + Ibg folded into -0.04f, Eex = 0 dropped, the products contracted into fused
+// multiply-adds, and the conductance decay G -= G * (dt * Inv) turned into G * fma(-dt, Inv, 1):
+//   V = fma(dt * TmemInv, (-0.04f - V) + fma(-Gex, V, Gin * (Ein - V)), V)
+// with the conductances of before their decay.
 __device__ __forceinline__ bool lifc_update(float& V, float& Gex, float& Gin, int32_t& T, float dt) {
 	const int32_t Tref = 50;
 	const float Vrest = -0.06f, Vthres = -0.05f, TmemInv = 50.0f;
-	const float Eex = 0.0f, Ein = -0.08f, Ibg = 0.02f, TexInv = 200.0f, TinInv = 100.0f;
+	const float Ein = -0.08f, VrestIbg = -0.04f, TexInv = 200.0f, TinInv = 100.0f;
 	bool spiked = false;
 	T           = T - 1;
 	if (T <= 0) {
@@ -74,15 +78,14 @@ __device__ __forceinline__ bool lifc_update(float& V, float& Gex, float& Gin, in
 			T      = Tref;
 			spiked = true;
 		} else {
-			float const a = __fsub_rn(Vrest, V);
-			float const b = __fmul_rn(Gex, __fsub_rn(Eex, V));
-			float const c = __fmul_rn(Gin, __fsub_rn(Ein, V));
-			float const s = __fadd_rn(__fadd_rn(__fadd_rn(a, b), c), Ibg);
-			V             = __fadd_rn(V, __fmul_rn(s, __fmul_rn(dt, TmemInv)));
+			float const a = __fmul_rn(Gin, __fsub_rn(Ein, V));
+			float const b = __fmaf_rn(-Gex, V, a);
+			float const c = __fadd_rn(__fsub_rn(VrestIbg, V), b);
+			V             = __fmaf_rn(__fmul_rn(dt, TmemInv), c, V);
 		}
 	}
-	Gex = __fsub_rn(Gex, __fmul_rn(Gex, __fmul_rn(dt, TexInv)));
-	Gin = __fsub_rn(Gin, __fmul_rn(Gin, __fmul_rn(dt, TinInv)));
+	Gex = __fmul_rn(Gex, __fmaf_rn(-dt, TexInv, 1.0f));
+	Gin = __fmul_rn(Gin, __fmaf_rn(-dt, TinInv, 1.0f));
 	return spiked;
 }
 

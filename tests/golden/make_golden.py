@@ -12,8 +12,17 @@ headers) compiled by oracle/Makefile with the reference's Release flags -- and s
   brunel_n5000.npz           N=5e3 p=0.05 seed 7, 500 steps: raster and final V/Tref
   mixed_net.npz              mixed delays (2..7), adj_list edges, three input groups: raster/state
   brunel_n500000_s1.json     N=5e5 p=0.002 seed 1, 300 steps: per-step spike counts and checksums
+  brunel_n500000_long.npz    N=5e5 p=0.002: seed 1 over 50,000 steps (the benchmark's warm-up and
+                             timed stretch) and seeds 2..10 over 2,000 steps: per-step spike counts
+                             of P, E, I and, per block, the raster checksum and E / I state checksums
+  vogels_n4000.npz           samples/vogels.cpp as published (N=4000, delay 8 dt, seed 1337), 1000
+                             steps: raster (E, I) and final V / Gex / Gin / Tref
+  vogels_c3_n10000.npz       the plastic E/I network's neurons and static weights without plasticity
+                             (N=1e4 conductance LIF, p=0.02, E 0.03 / I 0.3, delay 1 step, seed 7),
+                             1000 steps: raster and final state
 
-usage: python tests/golden/make_golden.py   (needs the reference sources; run from the repo root)
+usage: python tests/golden/make_golden.py [GROUP ...]   (needs the reference sources; run from the
+       repo root; groups: base, vogels, brunel_long; default: all)
 """
 from __future__ import annotations
 
@@ -54,9 +63,46 @@ def mixed_spec(steps: int):
     return lines, pairs
 
 
-def main():
+BRUNEL_LONG_SEED1_STEPS, BRUNEL_LONG_BLOCK = 50000, 2000
+BRUNEL_SEEDS_STEPS, BRUNEL_SEEDS_BLOCK = 2000, 500
+
+
+def vogels_fixtures():
+    for name, N, seed, steps, kw in (("vogels_n4000", 4000, 1337, 1000, {}),
+                                     ("vogels_c3_n10000", 10000, 7, 1000, {"we": 0.03, "wi": 0.3, "delay": 1e-4})):
+        res = O.run_reference_net(O.vogels_spec(N, seed, steps, **kw))
+        st, _, _ = O.reference_states(res, [], [0, 1])
+        counts, idx = raster_arrays(res)
+        arrs = {"counts": counts, "idx": idx, "meta": np.array([N, seed, steps])}
+        for k in (0, 1):
+            for j, f in enumerate(("V", "Gex", "Gin", "T")):
+                arrs[f"{f}{k}"] = st[k][j]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
+
+
+def brunel_long_fixtures():
+    arrs = {}
+    jobs = [(1, BRUNEL_LONG_SEED1_STEPS, BRUNEL_LONG_BLOCK)] + [(sd, BRUNEL_SEEDS_STEPS, BRUNEL_SEEDS_BLOCK)
+                                                              for sd in range(2, 11)]
+    for sd, steps, block in jobs:
+        counts, blocks = O.run_reference_brunel_ck(500000, 0.002, sd, steps, block)
+        arrs[f"counts_s{sd}"] = counts
+        arrs[f"blocks_s{sd}"] = blocks
+        arrs[f"meta_s{sd}"] = np.array([steps, block])
+        print("seed", sd, "steps", steps, "spikes", int(counts.sum()), flush=True)
+    np.savez_compressed(os.path.join(HERE, "brunel_n500000_long.npz"), **arrs)
+
+
+def main(groups=("base", "vogels", "brunel_long")):
     if not O.have_reference():
-        O.build(with_reference=True)
+        O.build(with_reference=True, reference_dir=os.environ.get("SPICE_REFERENCE_DIR", "/root/reference"))
+    if "vogels" in groups:
+        vogels_fixtures()
+    if "brunel_long" in groups:
+        brunel_long_fixtures()
+    if "base" not in groups:
+        print("golden fixtures written to", HERE)
+        return
     # rng
     rng = {}
     for seed in (1, 7, 1337):
@@ -113,4 +159,4 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]) or ("base", "vogels", "brunel_long"))

@@ -153,6 +153,62 @@ def test_mixed_network(oracle_lib):
         assert np.array_equal(net.state(pops[k], 3), g[f"T{k}"])
 
 
+@pytest.mark.parametrize("name,delay,weights", [("vogels_n4000.npz", 8e-4, None),
+                                                ("vogels_c3_n10000.npz", 1e-4, (0.03, 0.3))])
+def test_vogels_raster_and_state(oracle_lib, name, delay, weights):
+    """The conductance LIF of samples/vogels.cpp as the reference's -ffast-math build computes it:
+    raster and final V / Gex / Gin / Tref equal the reference binary's bit for bit."""
+    o = oracle_lib
+    g = _golden(name)
+    N, seed, steps = (int(x) for x in g["meta"])
+    we, wi = weights if weights else (None, None)
+    net, pops = o.vogels(N, seed, delay=delay, we=we, wi=wi)
+    _raster_matches(net, pops, g["counts"], g["idx"])
+    for k in (0, 1):
+        for f, fld in (("V", 0), ("Gex", 1), ("Gin", 2)):
+            assert np.array_equal(net.state(pops[k], fld).view(np.uint32), g[f"{f}{k}"].view(np.uint32)), (k, f)
+        assert np.array_equal(net.state(pops[k], 3), g[f"T{k}"])
+
+
+def test_vogels_compiled_form_is_not_source_order():
+    """The pin is not vacuous: evaluated in source order without contraction, the conductance update
+    differs from the reference's compiled form in a fraction of the states the fixtures cover."""
+    f32, f64 = np.float32, np.float64
+    rng = np.random.default_rng(0)
+    V = rng.uniform(-0.08, -0.05, 200000).astype(f32)
+    Gex = rng.uniform(0, 2, V.size).astype(f32)
+    Gin = rng.uniform(0, 5, V.size).astype(f32)
+    dt = f32(1.00000005e-4)
+    strict = V + ((f32(-0.06) - V) + Gex * (f32(0) - V) + Gin * (f32(-0.08) - V) + f32(0.02)) * (dt * f32(50))
+    a = Gin * (f32(-0.08) - V)
+    b = (-(Gex.astype(f64)) * V.astype(f64) + a.astype(f64)).astype(f32)  # product exact in double
+    c = (f32(-0.04) - V) + b
+    compiled = (f64(dt * f32(50)) * c.astype(f64) + V.astype(f64)).astype(f32)
+    assert 0.001 < np.mean(compiled != strict) < 0.1
+
+
+def test_large_brunel_seed_block_vs_reference(oracle_lib):
+    """N=5e5, p=0.002, seed 2: the first 500-step block (per-step counts, raster and state checksums)
+    equals the reference's."""
+    o = oracle_lib
+    g = _golden("brunel_n500000_long.npz")
+    steps, block = 500, int(g["meta_s2"][1])
+    assert block == steps
+    net, pops = o.brunel(500000, 0.002, 2)
+    counts, idx = [], []
+    for _ in range(steps):
+        net.step()
+        row = [net.spikes(pk, 0) for pk in pops]
+        counts.append([len(x) for x in row])
+        idx += row
+    counts = np.array(counts, dtype=np.int32)
+    assert np.array_equal(counts, g["counts_s2"][:steps])
+    ref = tuple(int(x) for x in g["blocks_s2"][0])
+    got = (o.raster_checksum(counts, np.concatenate(idx)), o.state_checksum(net.state(pops[1], 0), net.state(pops[1], 3)),
+           o.state_checksum(net.state(pops[2], 0), net.state(pops[2], 3)))
+    assert got == ref
+
+
 def test_oracle_errors(oracle_lib):
     o = oracle_lib
     net = o.Net(1e-4, 15e-4, [1])

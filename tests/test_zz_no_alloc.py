@@ -1,8 +1,8 @@
 """The allocation-free generator entry point, checked against the regular one.
 
-Callers that cannot allocate device memory (stream capture in progress, fixed-arena runtimes,
-hosts that own all device buffers) use spice_fixed_probability_noalloc, whose scratch is a static
-device array inside the library.  Its adjacency must equal the one spice_connect_fixed_probability
+Callers that cannot allocate device memory (real-time loops whose device memory is fixed up front,
+hosts that own every device buffer themselves) use spice_fixed_probability_noalloc, whose scratch
+is a static device array inside the library.  Its adjacency must equal the one spice_connect_fixed_probability
 generates for the same projection seed, on consecutive calls (the scratch keeps the previous call's
 contents).  This file is collected last so a failure here comes after every other test ran.
 """
