@@ -19,6 +19,10 @@ Printed JSON (one line, rank 0):
   cpu_baseline the CPU restatement of the reference step loop (oracle/oracle_bench, the same
                algorithm as the reference's single-core path) timed on this host's cores
   atomic_mode  value with the fast atomic delivery mode (order-dependent float rounding)
+  pull_mode    the deterministic pull path (every population gathers its inputs over the CSC
+               adjacency, as per-synapse weights need) on the same network: events/s, synapses
+               scanned/s, the pull kernels' roofline (4 B source index per synapse scanned), and
+               whether its states equal the push path's bit for bit
   batched      the batched sweep (256 Brunel networks, N log-uniform in [5e3, 8e4], 1000 steps):
                events/s as one batch and as the plain path network after network, their ratio,
                and whether both gave bit-identical final states
@@ -392,6 +396,67 @@ def plastic_bench(N: int = 100000, steps: int = 5000):
             "config": "plastic E/I: conductance LIF, p 0.02, delay 1 step, iSTDP on I->E"}
 
 
+def pull_bench(steps: int, warmup: int, peak: float):
+    """The pull path on the benchmark's network (SPICE_TUNE_PULL: every population gathers its inputs
+    from the CSC columns of its connections, in the reference's order).  One pull per window scans
+    every synapse once (its 4-byte source index; the synapses of a hit add their weight).  Timed like
+    the headline; the final states are compared with the push path's after the same steps."""
+    import numpy as np
+    import torch
+    import spice2_gb300 as sp
+    net, pops = sp.brunel(N_NEURONS, P_CONN, SEED, mode=sp.MODE_DETERMINISTIC)
+    net.set_tuning(pull=True)
+    t0 = time.perf_counter()
+    net.run(1)
+    net.synchronize()
+    build_s = time.perf_counter() - t0
+    synapses = sum(net.synapses(c) for c in range(6))
+    for _ in range(warmup):
+        net.run(STEPS_PER_RUN)
+    net.synchronize()
+    stream = torch.cuda.ExternalStream(net.stream_handle())
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0 = net.events
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(steps):
+        net.run(STEPS_PER_RUN)
+    b.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    events = net.events - e0
+    net.set_profiling(True)
+    for _ in range(steps):
+        net.run(STEPS_PER_RUN)
+    net.synchronize()
+    n_pull, ms_pull = net.kernel_stats(4)
+    n_win, ms_win = net.kernel_stats(0)
+    net.set_profiling(False)
+    total = 1 + (warmup + 2 * steps) * STEPS_PER_RUN
+    push, ppops = sp.brunel(N_NEURONS, P_CONN, SEED, mode=sp.MODE_DETERMINISTIC)
+    push.run(total)
+    same = all(np.array_equal(net.get_state(pops[k], sp.FIELD_V).view(np.uint32),
+                              push.get_state(ppops[k], sp.FIELD_V).view(np.uint32)) for k in (1, 2))
+    same = same and net.events == push.events
+    windows = n_pull
+    t_pull = ms_pull / max(n_pull, 1) / 1e3
+    achieved = 4 * synapses / t_pull / 1e9 if t_pull > 0 else None
+    out = {"metric": "synaptic_events_per_s", "unit": "events/s", "value": events / (ms / 1e3),
+           # every window's pull scans every synapse once; the profiled run repeats the timed steps,
+           # so it has as many windows
+           "synapses_scanned_per_s": synapses * windows / (ms / 1e3),
+           "ms_per_step": ms / steps, "sim_seconds_per_wall_second": STEPS_PER_RUN * steps * DT / (ms / 1e3),
+           "pull_launches": n_pull, "pull_mean_us": t_pull * 1e6, "neuron_mean_us": ms_win / max(n_win, 1) * 1e3,
+           "roofline": {"bound": "hbm", "kernel": "k_pull_masks + k_pull", "bytes_per_synapse": 4,
+                        "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": (achieved / peak) if achieved else None},
+           "bit_identical_to_push": bool(same), "build_seconds": build_s,
+           "config": "Large Brunel N=5e5 p=0.002 seed 1, every population pulled (SPICE_TUNE_PULL), deterministic"}
+    net.close()
+    push.close()
+    return out
+
+
 def reference_arm(args):
     """The reference's CPU implementation of the path (its C restatement: the reference binary is
     built for x86-64 with -march=haswell and its sources are not on the GPU host) on the host cores,
@@ -576,6 +641,13 @@ def main():
     if tuned["algo"] in DELIVER_DRAM_BYTES_PER_EVENT:
         traffic = DELIVER_DRAM_BYTES_PER_EVENT[tuned["algo"]] * ev_per_launch
 
+    pull = None
+    if rank == 0:
+        try:
+            pull = pull_bench(args.steps, args.warmup, peak)
+        except Exception as e:  # reported, never a reason to lose the headline line
+            pull = {"error": str(e)}
+
     batched = None
     import gc
     gc.collect()  # the N=5e5 nets (populations and nets reference each other)
@@ -636,6 +708,7 @@ def main():
                      "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3},
         "cpu_baseline": cpu,
         "atomic_mode": atomic,
+        "pull_mode": pull,
         "batched": batched,
         "adjoint": adjoint,
         "plastic": plastic,

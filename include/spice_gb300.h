@@ -65,6 +65,14 @@ enum {
 	 * (scale 0: delivers nothing, allowed in either mode). */
 	SPICE_SYNAPSE_ISTDP = 1,
 	SPICE_SYNAPSE_COUNT = 2,
+	/* WEIGHTED: a stateful synapse whose weight is drawn per synapse when the connection is built
+	 * -- the reference's StatefulSynapse + PerSynapseInit concepts (concepts.h:60-104): the
+	 * synapse_population ctor seeds the adjacency with seed++, then walks the CSR in order with
+	 * one more stream rng(seed++), calling init(syn, src, dst, rng) (synapse_population.h:30-41).
+	 * Here init draws once: w = params[0] * canonical<float>(rng); params {wmax, field}.  Delivery
+	 * adds w to the target field.  Every population receiving weighted synapses is delivered by
+	 * the pull path (see SPICE_TUNE_PULL), bit-exact with the reference in either mode. */
+	SPICE_SYNAPSE_WEIGHTED = 3,
 };
 
 /* Delivery modes. */
@@ -138,6 +146,21 @@ enum {
 	                                   the source populations, then the delivery, each launched
 	                                   as the programmatic dependent of the previous kernel;
 	                                   0: sources on a second stream joined by events         */
+	SPICE_TUNE_SOURCE_STEPS    = 9, /* consecutive steps each Poisson source CTA draws; 0 (default):
+	                                   the fewest that keep the window's grid within one wave of
+	                                   resident CTAs                                          */
+	SPICE_TUNE_PULL            = 8, /* 1: deliver into every stateful built-in population with
+	                                   inputs by the pull path, set before the network first
+	                                   steps.  The pull path gathers each target's inputs from
+	                                   the CSC adjacency of its connections in connect order and
+	                                   ascending source order -- the reference's order of
+	                                   additions -- and adds them one IEEE addition at a time:
+	                                   bit-exact for any per-synapse weights.  It is always used
+	                                   for populations with WEIGHTED inputs and, in deterministic
+	                                   mode, for populations with more than four distinct input
+	                                   weights (the push path replays per-weight event counts).
+	                                   Nets with pulled populations step in windows of at most
+	                                   16 steps and need max_delay <= 64 steps             */
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input
 	                                   words in registers, 1 rolled steps over words parked in
 	                                   shared memory, 2 as 1 with warp-uniform count replay,
@@ -185,9 +208,14 @@ int spice_conn_size(spice_net* net, int conn, int64_t* src_out, int64_t* synapse
 /* Per-synapse state of a plastic connection, in CSR order, as stored: a synapse holds its state
  * as of its last catch-up (its source's last delivery or the last multiple of 64 steps), exactly
  * like the reference's synapse_population.  field 0 = W (COUNT: the count), 1 = x_pre,
- * 2 = x_post; out holds synapses floats. */
+ * 2 = x_post; out holds synapses floats.  For a WEIGHTED connection field 0 is the weight. */
 int spice_get_synapse_state(spice_net* net, int conn, int field, float* out);
 int spice_get_csr(spice_net* net, int conn, int64_t* offsets_out, int32_t* neighbors_out);
+/* The CSC (transposed) adjacency of a connection, as the pull path uses it: col_offsets_out
+ * (dst_size + 1 int64) and sources_out (synapses int32, ascending within each target's column;
+ * entry j of column d is the j-th synapse into d in the reference's delivery order).  Built on the
+ * GPU from the CSR on first use.  No counterpart in the reference (csr.h holds only the CSR). */
+int spice_get_csc(spice_net* net, int conn, int64_t* col_offsets_out, int32_t* sources_out);
 
 /* fixed_probability(p) adjacency of one projection (the generator behind
  * spice_connect_fixed_probability) for callers that cannot allocate device memory: real-time loops

@@ -91,6 +91,10 @@ def lib():
         L.spo_set_external.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_void_p]
         L.spo_connect.restype = C.c_int
         L.spo_connect.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_float, C.c_int, C.c_float]
+        L.spo_connect_weighted.restype = C.c_int
+        L.spo_connect_weighted.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_double, C.c_float, C.c_int, C.c_float]
+        L.spo_syn_weights.restype = C.c_int
+        L.spo_syn_weights.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.spo_connect_adj.restype = C.c_int
         L.spo_connect_adj.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int64, C.c_void_p, C.c_float,
                                       C.c_int, C.c_float]
@@ -206,6 +210,23 @@ class Net:
     def connect(self, src, dst, p, delay, weight, field=0):
         return self._chk(lib().spo_connect(self.h, src, dst, p, delay, field, weight))
 
+    def connect_weighted(self, src, dst, p, delay, wmax, field=0):
+        """fixed_probability with per-synapse weights wmax * canonical<float> (PerSynapseInit)."""
+        return self._chk(lib().spo_connect_weighted(self.h, src, dst, p, delay, field, wmax))
+
+    def syn_weights(self, conn) -> np.ndarray:
+        m = lib().spo_conn_synapses(self.h, conn)
+        out = np.zeros(max(1, m), dtype=np.float32)
+        self._chk(lib().spo_syn_weights(self.h, conn, out.ctypes.data))
+        return out[:m]
+
+    def csr_arrays(self, conn, src_size):
+        m = lib().spo_conn_synapses(self.h, conn)
+        off = np.zeros(src_size + 1, dtype=np.int64)
+        nb = np.zeros(max(1, m), dtype=np.int32)
+        self._chk(lib().spo_conn_csr(self.h, conn, off.ctypes.data, nb.ctypes.data))
+        return off, nb[:m]
+
     def connect_adj(self, src, dst, pairs, delay, weight, field=0):
         pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
         return self._chk(lib().spo_connect_adj(self.h, src, dst, len(pr), pr.ctypes.data, delay, field, weight))
@@ -299,6 +320,51 @@ def vogels_spec(N: int, seed: int, steps: int, p: float = 0.02, dt=1e-4, delay=8
     lines = [f"{dt!r} {delay!r} {seed} {steps} 0", f"pop lif_cond {N * 8 // 10}", f"pop lif_cond {N * 2 // 10}"]
     for s, d, w, fl in ((0, 0, we, 1), (0, 1, we, 1), (1, 0, wi, 2), (1, 1, wi, 2)):
         lines.append(f"conn {s} {d} {p!r} {delay!r} {w!r} {fl}")
+    return lines
+
+
+# A network with per-synapse weights (the weighted synapse: PerSynapseInit, w = wmax * canonical
+# <float>) into LIF and conductance-LIF targets, mixed with fixed weights and mixed delays; and a
+# population with six distinct fixed input weights.  (kind, src, dst, p, delay, weight / wmax,
+# field); kind "w" weighted, "f" fixed_weight.
+WEIGHTED_NET = {
+    "dt": 1e-4, "max_delay": 12e-4, "seed": 2718,
+    "pops": [("poisson", 3000, 40.0), ("lif", 2000), ("lif", 500), ("lif_cond", 1000), ("lif", 800)],
+    "conns": [("w", 0, 1, 0.05, 5e-4, 0.01, 0), ("f", 1, 1, 0.05, 7e-4, 0.002, 0),
+              ("w", 2, 1, 0.1, 4e-4, -0.02, 0), ("f", 0, 2, 0.02, 3e-4, 0.004, 0),
+              ("w", 1, 2, 0.05, 6e-4, 0.006, 0), ("f", 2, 2, 0.02, 9e-4, -0.004, 0),
+              ("w", 1, 3, 0.02, 4e-4, 0.8, 1), ("w", 2, 3, 0.05, 5e-4, 0.2, 2), ("f", 0, 3, 0.02, 8e-4, 0.03, 1),
+              ("f", 0, 4, 0.01, 3e-4, 0.011, 0), ("f", 1, 4, 0.01, 4e-4, 0.0035, 0),
+              ("f", 2, 4, 0.02, 5e-4, -0.007, 0), ("f", 0, 4, 0.01, 6e-4, 0.009, 0),
+              ("f", 1, 4, 0.02, 3e-4, 0.0021, 0), ("f", 2, 4, 0.01, 12e-4, -0.0105, 0)],
+}
+
+
+def _f32(x):
+    return float(np.float32(x))
+
+
+def weighted_net(spec=WEIGHTED_NET):
+    """WEIGHTED_NET on the oracle: returns (net, pops, conns)."""
+    net = Net(spec["dt"], spec["max_delay"], [spec["seed"]])
+    kinds = {"poisson": POISSON, "lif": LIF, "lif_cond": LIF_COND}
+    pops = [net.add_population(kinds[p[0]], p[1], p[2:]) for p in spec["pops"]]
+    conns = []
+    for kind, s, d, p, delay, w, fl in spec["conns"]:
+        if kind == "w":
+            conns.append(net.connect_weighted(pops[s], pops[d], p, delay, _f32(w), fl))
+        else:
+            conns.append(net.connect(pops[s], pops[d], p, delay, _f32(w), fl))
+    return net, pops, conns
+
+
+def weighted_net_spec(steps: int, spec=WEIGHTED_NET) -> list[str]:
+    lines = [f"{spec['dt']!r} {spec['max_delay']!r} {spec['seed']} {steps} 0"]
+    for p in spec["pops"]:
+        lines.append(f"pop poisson {p[1]} {p[2]!r}" if p[0] == "poisson" else f"pop {p[0]} {p[1]}")
+    for kind, s, d, p, delay, w, fl in spec["conns"]:
+        cond = spec["pops"][d][0] == "lif_cond"
+        lines.append(f"{'wconn' if kind == 'w' else 'conn'} {s} {d} {p!r} {delay!r} {_f32(w)!r}" + (f" {fl}" if cond else ""))
     return lines
 
 

@@ -27,6 +27,9 @@
 //               conn SRC DST P DELAY WEIGHT FIELD  (into a lif_cond: FIELD 1 excitatory (Gex),
 //                                                   2 inhibitory (Gin), samples/vogels.cpp:48-60)
 //               adj SRC DST DELAY WEIGHT M s0 d0 s1 d1 ...   (adj_list + fixed_weight)
+//               wconn SRC DST P DELAY WMAX [FIELD] (fixed_probability + weighted: a per-synapse
+//                                                   weight wmax * canonical<float> drawn at
+//                                                   construction; FIELD as for conn)
 //               plastic POP P DELAY SCALE        (POP -> POP fixed_probability + count_syn; the
 //                                                 reference keeps the history of a plastic
 //                                                 connection's source, snn.h:44-45, so source and
@@ -122,6 +125,35 @@ struct excitatory {
 struct inhibitory {
 	float weight;
 	void deliver(lif_cond::neuron& to) const { to.Gin += weight; }
+};
+
+// A stateful synapse whose weight is drawn per synapse when the connection is built (the
+// reference's PerSynapseInit concept, synapse_population.h:34-41: one xoroshiro128+ stream seeded
+// after the adjacency's, walked in CSR order): w = wmax * canonical<float>.  A single multiply by a
+// value whose scaling is a power of two, so the fast-math build cannot round it differently.
+struct weighted {
+	float wmax;
+	struct synapse {
+		float w = 0;
+	};
+	void init(synapse& s, Int, Int, auto& rng) const { s.w = wmax * util::generate_canonical<float>(rng); }
+	void deliver(synapse const& s, lif::neuron& to) const { to.V += s.w; }
+};
+struct weighted_ex {
+	float wmax;
+	struct synapse {
+		float w = 0;
+	};
+	void init(synapse& s, Int, Int, auto& rng) const { s.w = wmax * util::generate_canonical<float>(rng); }
+	void deliver(synapse const& s, lif_cond::neuron& to) const { to.Gex += s.w; }
+};
+struct weighted_in {
+	float wmax;
+	struct synapse {
+		float w = 0;
+	};
+	void init(synapse& s, Int, Int, auto& rng) const { s.w = wmax * util::generate_canonical<float>(rng); }
+	void deliver(synapse const& s, lif_cond::neuron& to) const { to.Gin += s.w; }
 };
 
 // The counting plastic synapse of test/detail/synapse_population.cpp:84-94 (update adds 1, skip
@@ -345,6 +377,16 @@ static int run_net(int argc, char** argv) {
 			float delay, scale;
 			in >> q >> p >> delay >> scale;
 			net.connect<count_syn>(pops[q].L, pops[q].L, fixed_probability(p), delay, {scale});
+		} else if (kw == "wconn") {
+			Int s, d;
+			double p;
+			float delay, w;
+			in >> s >> d >> p >> delay >> w;
+			int field = 0;
+			if (pops[d].kind == 2) in >> field;
+			if (pops[d].kind == 1) connect_from<weighted>(net, pops[s], pops[d].L, fixed_probability(p), delay, w);
+			else if (field == 1) connect_from<weighted_ex>(net, pops[s], pops[d].C, fixed_probability(p), delay, w);
+			else connect_from<weighted_in>(net, pops[s], pops[d].C, fixed_probability(p), delay, w);
 		} else if (kw == "conn" || kw == "adj") {
 			Int s, d;
 			in >> s >> d;

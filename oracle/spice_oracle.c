@@ -231,6 +231,7 @@ typedef struct {
 	double skip_tab[129];   /* pow(1 - dt / tau, n), n = -64 .. 64 */
 	float* sW; float* sA; float* sB;  /* per-synapse state in CSR order */
 	uint64_t* ages;         /* per source: bit 63 = pending pre update, low bits = step + 1 */
+	float* wts;             /* weighted synapses: per-synapse weight in CSR order, else NULL */
 } spo_conn;
 
 struct spo_net {
@@ -265,7 +266,7 @@ void spo_net_destroy(spo_net* n) {
 	}
 	for (int i = 0; i < n->nconn; i++) {
 		spo_conn* c = &n->conns[i];
-		free(c->off); free(c->nb); free(c->sW); free(c->sA); free(c->sB); free(c->ages);
+		free(c->off); free(c->nb); free(c->sW); free(c->sA); free(c->sB); free(c->ages); free(c->wts);
 	}
 	for (int i = 0; i < n->npop; i++) free(n->pops[i].post_hist);
 	free(n);
@@ -351,6 +352,28 @@ int spo_connect(spo_net* n, int src, int dst, double p, float delay, int field, 
 	spo_u128 sd = spo_seed_next(&n->seed);
 	c->nsyn = spo_fp_generate(S, D, p, sd, c->off, c->nb, NULL);
 	return n->nconn++;
+}
+
+/* A fixed_probability connection whose synapses carry their own weight, drawn when the connection
+ * is built: the synapse_population ctor seeds the adjacency with seed++ and then, for a
+ * PerSynapseInit synapse, walks the CSR in order with one more stream, rng(seed++), calling
+ * init(syn, src, dst, rng) per synapse (synapse_population.h:30-41).  The weighted synapse's init
+ * draws once: w = wmax * canonical<float>(rng) (random.h:236-247). */
+int spo_connect_weighted(spo_net* n, int src, int dst, double p, float delay, int field, float wmax) {
+	int const ci = spo_connect(n, src, dst, p, delay, field, 0.0f);
+	if (ci < 0) return ci;
+	spo_conn* c      = &n->conns[ci];
+	spo_u128 const s = spo_seed_next(&n->seed);
+	uint64_t rng[2]  = {s.lo, s.hi};
+	c->wts = (float*)malloc(sizeof(float) * (size_t)(c->nsyn + 1));
+	for (int64_t e = 0; e < c->nsyn; e++) c->wts[e] = wmax * spo_canonical_f32(spo_xoroshiro128p_next(rng));
+	return ci;
+}
+
+int spo_syn_weights(const spo_net* n, int conn, float* out) {
+	if (conn < 0 || conn >= n->nconn || !n->conns[conn].wts) return fail("not a weighted connection");
+	memcpy(out, n->conns[conn].wts, sizeof(float) * (size_t)n->conns[conn].nsyn);
+	return 0;
 }
 
 static int cmp_u64(const void* a, const void* b) {
@@ -613,6 +636,8 @@ void spo_step(spo_net* n) {
 					else if (w != 0.0f) F[c->nb[e]] = F[c->nb[e]] + c->sW[e] * w;
 				}
 				c->ages[s] = (uint64_t)(n->time + 1) | (1ULL << 63);
+			} else if (c->wts) {
+				for (int64_t e = c->off[s]; e < c->off[s + 1]; e++) F[c->nb[e]] = F[c->nb[e]] + c->wts[e];
 			} else {
 				for (int64_t e = c->off[s]; e < c->off[s + 1]; e++) F[c->nb[e]] = F[c->nb[e]] + w;
 			}

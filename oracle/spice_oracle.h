@@ -77,6 +77,10 @@ int spo_set_external(spo_net* net, int pop, int nsteps, const int32_t* counts,
  * to state field `field` of the target (0=V, 1=Gex, 2=Gin).  Returns the connection id,
  * or -1 with a message from spo_last_error(). */
 int spo_connect(spo_net* net, int src, int dst, double p, float delay, int field, float weight);
+/* fixed_probability with a per-synapse weight wmax * canonical<float>, drawn from the
+ * PerSynapseInit stream (one seed after the adjacency's) in CSR order. */
+int spo_connect_weighted(spo_net* net, int src, int dst, double p, float delay, int field, float wmax);
+int spo_syn_weights(const spo_net* net, int conn, float* out);
 /* Makes connection `conn` plastic (the reference's synapse_population with a PlasticSynapse model,
  * synapse_population.h:27-140): per-synapse state, lazy catch-up from the target's post history at
  * each delivery and every 64 steps.  iSTDP: W starts at w0; pre spike W += eta (x_post - 2 rho0 tau)

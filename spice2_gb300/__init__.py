@@ -31,7 +31,7 @@ LIB_PATH = os.path.join(_HERE, "libspice_gb300.so")
 
 OK, EINVAL, ECUDA, ENOMEM, ESTATE, EOVERFLOW = 0, 1, 2, 3, 4, 5
 NEURON_POISSON, NEURON_LIF, NEURON_LIF_COND, NEURON_EXTERNAL = 0, 1, 2, 3
-SYNAPSE_FIXED_WEIGHT, SYNAPSE_ISTDP, SYNAPSE_COUNT = 0, 1, 2
+SYNAPSE_FIXED_WEIGHT, SYNAPSE_ISTDP, SYNAPSE_COUNT, SYNAPSE_WEIGHTED = 0, 1, 2, 3
 MODE_DETERMINISTIC, MODE_ATOMIC = 0, 1
 FIELD_V, FIELD_GEX, FIELD_GIN, FIELD_TREF = 0, 1, 2, 3
 
@@ -88,6 +88,7 @@ def _load():
         "spice_conn_size": [vp, i32, P(i64), P(i64)],
         "spice_get_synapse_state": [vp, i32, i32, vp],
         "spice_get_csr": [vp, i32, vp, vp],
+        "spice_get_csc": [vp, i32, vp, vp],
         "spice_set_profiling": [vp, i32],
         "spice_kernel_stats": [vp, i32, P(i64), P(f64)],
         "spice_launch_count": [vp, P(i64)],
@@ -217,6 +218,21 @@ class count_synapse:
 
     def params(self):
         return [self.scale, float(self.field)]
+
+
+@dataclass(frozen=True)
+class weighted:
+    """A synapse with its own weight, drawn when the connection is built: the reference's
+    StatefulSynapse + PerSynapseInit concepts (concepts.h:60-104; the synapse_population ctor walks
+    the CSR in order with the stream seeded after the adjacency's, synapse_population.h:30-41), here
+    w = wmax * canonical<float>(rng).  Delivery adds w to the target field.  Populations receiving
+    weighted synapses are delivered by the deterministic pull path."""
+    wmax: float
+    field: int = FIELD_V
+    model = SYNAPSE_WEIGHTED
+
+    def params(self):
+        return [self.wmax, float(self.field)]
 
 
 def excitatory(weight: float) -> fixed_weight:
@@ -350,9 +366,14 @@ class snn:
     def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
                    deliver_parts: int | None = None, deliver_algo: int | None = None,
                    overlap_sources: bool | None = None, neuron_variant: int | None = None,
-                   launch_mode: int | None = None):
+                   launch_mode: int | None = None, pull: bool | None = None, source_steps: int | None = None):
         """Delivery launch shape and neuron-update variant (any time between steps); results are
-        independent of them."""
+        independent of them.  pull (before the network first steps): deliver every stateful
+        population by the pull path over the CSC adjacency (SPICE_TUNE_PULL)."""
+        if pull is not None:
+            _check(lib().spice_set_tuning(self._h, 8, int(bool(pull))))
+        if source_steps is not None:  # steps per Poisson source CTA (0: automatic, one-wave grid)
+            _check(lib().spice_set_tuning(self._h, 9, int(source_steps)))
         if tile_bytes is not None:
             _check(lib().spice_set_tuning(self._h, 0, int(tile_bytes)))
         if deliver_threads is not None:
@@ -452,6 +473,21 @@ class snn:
         nb = np.zeros(max(1, syn.value), dtype=np.int32)
         _check(lib().spice_get_csr(self._h, conn, off.ctypes.data, nb.ctypes.data))
         return off, nb[:syn.value]
+
+    def csc(self, conn: int):
+        """The transposed adjacency: column starts (dst_size + 1) and the sources of each target's
+        synapses, ascending within a column."""
+        src, syn = C.c_int64(), C.c_int64()
+        _check(lib().spice_conn_size(self._h, conn, C.byref(src), C.byref(syn)))
+        dst = self._conns[conn][1].size()
+        off = np.zeros(dst + 1, dtype=np.int64)
+        nb = np.zeros(max(1, syn.value), dtype=np.int32)
+        _check(lib().spice_get_csc(self._h, conn, off.ctypes.data, nb.ctypes.data))
+        return off, nb[:syn.value]
+
+    def synapse_weights(self, conn: int) -> np.ndarray:
+        """Per-synapse weights of a weighted connection, CSR order."""
+        return self.synapse_state(conn, 0)
 
     # profiling
     def set_profiling(self, on: bool):
@@ -582,7 +618,7 @@ def selftest_skip_rounding(count: int = 1 << 26, seed: int = 1):
     return m.value, a.value, f.value
 
 
-__all__ = ["snn", "Population", "poisson", "lif", "lif_cond", "external_input", "fixed_weight", "excitatory",
+__all__ = ["snn", "Population", "poisson", "lif", "lif_cond", "external_input", "fixed_weight", "weighted", "excitatory",
            "inhibitory", "istdp", "count_synapse", "fixed_probability", "adj_list", "brunel", "batch", "brunel_sweep", "brunel_sweep_sizes",
            "SpiceError", "LogicError", "CudaError", "MODE_DETERMINISTIC", "MODE_ATOMIC", "lib",
            "selftest_skip_rounding"]

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libspice_gb300.so")
 
-SOURCES = ["rng_host.cpp", "gen.cu", "step.cu", "net.cu", "noalloc.cu", "batch.cu", "adjoint.cu"]
+SOURCES = ["rng_host.cpp", "gen.cu", "step.cu", "net.cu", "noalloc.cu", "batch.cu", "adjoint.cu", "pull.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -325,13 +325,19 @@ extern "C" int spice_batch_create(spice_net* const* nets, int nnets, spice_batch
 		for (auto const& p : n->pops)
 			if (p.d.model == EXTERNAL || p.d.model == USER)
 				return bfail(SPICE_EINVAL, "batched nets cannot have external_input or user-defined populations");
-		for (auto const& c : n->conns)
+		for (auto const& c : n->conns) {
 			if (c.d.plastic) return bfail(SPICE_EINVAL, "batched nets cannot have plastic connections");
+			if (c.weighted) return bfail(SPICE_EINVAL, "batched nets cannot have weighted (per-synapse weight) connections");
+		}
+		if (n->pull_all) return bfail(SPICE_EINVAL, "batched nets cannot use the pull path");
 	}
 	int dev_prev = 0;
 	cudaGetDevice(&dev_prev);
 	if (dev_prev != n0->device) B_CUDA_TRY(cudaSetDevice(n0->device));
 	for (int i = 0; i < nnets; i++) B_TRY(net_prepare(nets[i]));
+	for (int i = 0; i < nnets; i++)
+		if (nets[i]->any_pull)
+			return bfail(SPICE_EINVAL, "batched nets cannot have pulled populations (more than 4 distinct input weights)");
 	for (int i = 0; i < nnets; i++)
 		if (nets[i]->K != n0->K || nets[i]->Hb != n0->Hb)
 			return bfail(SPICE_EINVAL, "batched nets must have the same minimum delay (window length)");

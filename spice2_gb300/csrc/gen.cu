@@ -441,4 +441,58 @@ cudaError_t generate_fixed_probability_into(cudaStream_t stream, int64_t src, in
 
 size_t gen_row_job_bytes() { return sizeof(RowJob); }
 
+namespace {
+// w[e] = wmax * canonical<float>(draw e) for e < n: the PerSynapseInit stream of a weighted
+// synapse (synapse_population.h:34-41), one draw per synapse in CSR order; thread j of super-chunk
+// m jumps to draw 65536 m + 256 j like k_gaps.
+__global__ void __launch_bounds__(kGenThreads) k_init_weights(const u128* __restrict__ superstates,
+                                                              const u128* __restrict__ subpolys, float wmax, int64_t n,
+                                                              float* __restrict__ w) {
+	__shared__ u128 basis[kBasis];
+	int64_t const m = blockIdx.x;
+	if (threadIdx.x == 0) {
+		uint64_t s0 = superstates[m].lo, s1 = superstates[m].hi;
+		for (int i = 0; i < kBasis; i++) {
+			basis[i] = {s0, s1};
+			xoro_next(s0, s1);
+		}
+	}
+	__syncthreads();
+	int64_t const first = m * kSuper + (int64_t)threadIdx.x * kSubDraws;
+	if (first >= n) return;
+	uint64_t s0, s1;
+	basis_xor(basis, subpolys[threadIdx.x], s0, s1);
+	int64_t const cnt = min((int64_t)kSubDraws, n - first);
+	for (int r = 0; r < cnt; r++) w[first + r] = __fmul_rn(wmax, canonical_f32(xoro_next(s0, s1)));
+}
+}  // namespace
+
+cudaError_t init_synapse_weights(cudaStream_t stream, u128 seed, int64_t n, float wmax, float* w) {
+	if (n <= 0) return cudaSuccess;
+	int64_t const nsuper = (n + kSuper - 1) / kSuper;
+	std::vector<u128> polys(nsuper), sub(kGenThreads);
+	u128 const stride = gf2_xpow(kSuper), step = gf2_xpow(kSubDraws);
+	polys[0] = {1, 0};
+	for (int64_t m = 1; m < nsuper; m++) polys[m] = gf2_mulmod(polys[m - 1], stride);
+	sub[0] = {1, 0};
+	for (int j = 1; j < kGenThreads; j++) sub[j] = gf2_mulmod(sub[j - 1], step);
+	u128 *d_polys = nullptr, *d_sub = nullptr, *d_states = nullptr;
+	cudaError_t e = cudaMalloc(&d_polys, sizeof(u128) * nsuper);
+	if (e == cudaSuccess) e = cudaMalloc(&d_sub, sizeof(u128) * kGenThreads);
+	if (e == cudaSuccess) e = cudaMalloc(&d_states, sizeof(u128) * nsuper);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(d_polys, polys.data(), sizeof(u128) * nsuper, cudaMemcpyHostToDevice, stream);
+	if (e == cudaSuccess) e = cudaMemcpyAsync(d_sub, sub.data(), sizeof(u128) * kGenThreads, cudaMemcpyHostToDevice, stream);
+	if (e == cudaSuccess) {
+		k_superstates<<<(unsigned)std::min<int64_t>((nsuper + 255) / 256, 1024), 256, 0, stream>>>(seed, d_polys, nsuper,
+		                                                                                     d_states);
+		k_init_weights<<<(unsigned)nsuper, kGenThreads, 0, stream>>>(d_states, d_sub, wmax, n, w);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(stream);  // the host vectors go out of scope
+	cudaFree(d_polys);
+	cudaFree(d_sub);
+	cudaFree(d_states);
+	return e;
+}
+
 }  // namespace spice_gb300

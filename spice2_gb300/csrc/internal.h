@@ -6,7 +6,14 @@
 //                  spike list ring     list[K][N] int32 (unordered, consumed by delivery);
 //                  input ring          deterministic: cnt[D][N][W] u32 packed per-group counts
 //                                      atomic:        acc[D][N][F] f32 per-field sums.
-//   connection c:  CSR offsets i64[src+1], neighbors i32[synapses].
+//   connection c:  CSR offsets i64[src+1], neighbors i32[synapses]; weighted synapses also
+//                  weights f32[synapses] (CSR order); connections into a pulled population also
+//                  the CSC: column starts i64[dst+1], sources i32[synapses] (ascending per
+//                  column), weighted ones their weights f32[synapses] in CSC order.
+//   pulled population p (inputs gathered per target in the reference's order, pull.cu):
+//                  region starts i64[N+1] (prefix of the in-degree over its connections),
+//                  active synapses A u64[in-synapses], step-grouped weights G f32[in-synapses],
+//                  bin offsets koff i32[N][K*F+1].
 //   per run:       dt[t] (Kahan-compensated), per-step xoroshiro state basis T^i(s_t), i < 128.
 #pragma once
 
@@ -27,6 +34,7 @@ constexpr int kMaxWindow  = 64;  // steps fused into one neuron-update launch
 constexpr int kBasis      = 128; // states per step basis
 constexpr int kJumpTable  = 16 * 256;  // u128 entries of one step's jump table
 constexpr int kPoissonChunk = 32; // consecutive Poisson neurons per thread (one jump each)
+constexpr int kPullMaxWindow = 16; // steps fused into one window in a net with pulled populations
 
 enum Model { POISSON = 0, LIF = 1, LIF_COND = 2, EXTERNAL = 3, USER = 4 };
 
@@ -76,6 +84,17 @@ struct PopDev {
 	const int64_t* ext_off;
 	const int32_t* ext_idx;
 	int ext_steps;
+	// pulled population: every input is gathered per target, in connect order and ascending source
+	// order, by the pull kernel over the CSC (pull.cu), instead of the push delivery's input ring
+	int pull;                  // 1: pulled
+	int pull_F;                // state fields receiving inputs (bins per step)
+	int pull_field[3];         // field of bin f
+	int pull_nbins;            // K * pull_F: bin (k, f) = k * pull_F + f
+	const int64_t* pull_base;  // [size + 1] region of neuron i in pull_A / pull_G
+	uint64_t* pull_A;          // active synapses: weight bits | (step mask | f << 16) << 32, CSC order
+	float* pull_G;             // the active synapses' weights grouped by bin
+	int32_t* pull_koff;        // [size][nbins + 1] bin starts in the region; [i][0] = -1: not grouped,
+	                           // [i][1] = number of active synapses (the neuron walks pull_A)
 };
 
 struct ConnDev {
@@ -111,6 +130,29 @@ struct ConnDev {
 	const uint64_t* skip_pk;  // the same factors packed for mul_f32_f64_rn (significand | exponent << 53)
 	int src_nwords;           // source bitmap words
 	const uint32_t* src_bits; // source spike bitmap ring [Hb][src_nwords]
+	// weighted synapses (a per-synapse weight drawn at construction) and pulled targets
+	const float* wts;         // weighted: per-synapse weight, CSR order (else null)
+	const int64_t* csc_off;   // [dst_size + 1] column starts (pulled targets)
+	const int32_t* csc_src;   // [synapses] source of each entry, ascending within a column
+	const float* csc_w;       // weighted: weights in CSC order
+	const uint32_t* pull_orb; // [src_nwords] bit s: source s spiked in one of the pulled steps
+	const uint32_t* pull_wm;  // [src_size] bit k: source s spiked at (first pulled step + k - delay)
+};
+
+// Window masks of one (source population, delay) pair of pulled connections (pull.cu).
+struct PullSet {
+	int src, delay, nwords;
+	int64_t size;
+	const uint32_t* bits;  // the source's bitmap ring [Hb][nwords]
+	uint32_t* orb;         // [nwords]
+	uint32_t* wm;          // [size]
+};
+
+// A pulled connection whose spikes' events are counted (row lengths from its CSR).
+struct PullEvJob {
+	int nwords;
+	const uint32_t* bits;
+	const int64_t* off;
 };
 
 struct Pop {
@@ -129,6 +171,9 @@ struct Pop {
 struct Conn {
 	ConnDev d;
 	int64_t synapses = 0;
+	bool weighted    = false;     // per-synapse weights (d.wts)
+	float wmax       = 0;
+	u128 wseed       = {0, 0};    // the PerSynapseInit stream's seed
 	uint16_t* nb16    = nullptr;  // owned storage of d.nb16
 	int nb16_tile     = 0;        // tile size d.nb16 was built for
 	bool adj         = false;
@@ -198,7 +243,7 @@ struct spice_net {
 	std::vector<cudaEvent_t> ev_pool;
 	std::vector<std::pair<int, int>> ev_pending;  // (kind, event index of the start)
 	size_t ev_used = 0;
-	spice_gb300::KernelStat stats[4];
+	spice_gb300::KernelStat stats[5];
 	int64_t launches = 0;
 	std::vector<void*> allocations;
 	std::vector<spice_gb300::PendingGen> gen_pending;
@@ -213,8 +258,21 @@ struct spice_net {
 	int overlap_sources = 1;         // source kernels on their own stream (tunable)
 	int neuron_variant  = 0;         // LIF window variant of the neuron update (tunable)
 	int launch_mode     = 1;         // 1: neurons and sources in one grid, programmatic dependent launches
+	int src_steps       = 0;         // steps per Poisson CTA (0: the fewest that fit the grid in one wave)
+	int sm_count        = 1;
 	int dmin = 1, dmax = 1;          // connection delays in steps
 	bool plastic = false;            // any plastic connection (windows of one step)
+	// pull delivery (pull.cu)
+	bool pull_all = false;           // every stateful built-in population with inputs is pulled
+	bool any_pull = false;
+	std::vector<spice_gb300::PullSet> pull_sets;
+	std::vector<spice_gb300::PullEvJob> pull_ev;
+	spice_gb300::PullSet* d_pull_sets = nullptr;
+	spice_gb300::PullEvJob* d_pull_ev = nullptr;
+	std::vector<int> pull_pops;      // pulled populations
+	int* d_pull_pops     = nullptr;  // [npull]
+	int* d_pull_blk      = nullptr;  // [npull + 1] prefix of their pull CTAs
+	int pull_blocks      = 0;
 };
 
 namespace spice_gb300 {

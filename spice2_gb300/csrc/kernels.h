@@ -40,6 +40,44 @@ struct GenScratch {
 	int64_t max_draws, max_src, max_super;
 };
 size_t gen_row_job_bytes();
+// w[e] = wmax * canonical<float>(draw e of the stream seeded by `seed`), e < n: the per-synapse
+// weights of a weighted connection in CSR order (synapse_population.h:34-41).  Synchronises.
+cudaError_t init_synapse_weights(cudaStream_t stream, u128 seed, int64_t n, float wmax, float* w);
+
+// ---- pull.cu ----
+// CSC of a CSR (rows sources, ndst targets): col_off[ndst + 1], col_src[synapses] ascending per
+// column (CSR order among duplicates), col_w[synapses] = wts in CSC order when wts is not null.
+// Allocates and frees its own scratch; synchronises.
+cudaError_t build_csc(cudaStream_t stream, const int64_t* off, const int32_t* nb, const float* wts, int64_t rows,
+                      int64_t ndst, int64_t synapses, int64_t* col_off, int32_t* col_src, float* col_w);
+// base[i] = sum over nconn column-start arrays (a device array of device pointers) of [i], i <= n.
+cudaError_t pull_region_bases(cudaStream_t stream, const int64_t* const* col_offs, int nconn, int64_t n, int64_t* base);
+
+// One window's pull: masks of every (source, delay) set, events of the window that just ended, then
+// the active lists and bins of every pulled population.
+struct PullArgs {
+	int64_t t;               // first pulled step (the next window's first step)
+	int K;                   // steps pulled (the net's window length, <= kPullMaxWindow)
+	int Hb;                  // bitmap ring length
+	int nsets;
+	const PullSet* sets;     // [nsets]
+	int nev;
+	const PullEvJob* ev;     // [nev] one per pulled connection
+	int64_t t_emit0;         // the window that just ended (its spikes' events are counted)
+	int k_emit;
+	unsigned long long* events;
+	int npull;
+	const int* pull_pops;    // [npull] pulled population ids
+	const int* pull_blk;     // [npull + 1] prefix of their k_pull CTAs
+	int pull_blocks;
+	const PopDev* pops;
+	const ConnDev* conns;    // by-target order (PopDev::in_begin / in_end)
+};
+cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<PullSet> const& sets,
+                        std::vector<PullEvJob> const& ev);
+int pull_blocks_for(int64_t size);  // k_pull CTAs of a population of `size` neurons
+// Applies the bins of the first pulled step to the state and empties them (state reads).
+cudaError_t launch_pull_apply_first(cudaStream_t stream, PopDev const& P);
 cudaError_t generate_fixed_probability_into(cudaStream_t stream, int64_t src, int64_t dst, double p, u128 seed,
                                             GenScratch const& sc, int64_t* offsets, int32_t* neighbors,
                                             int64_t capacity, int64_t* synapses);
@@ -88,6 +126,7 @@ struct WindowArgs {
 	                             // (k_neurons launches kinds 0 and 3, k_sources kinds 1 and 2);
 	                             // + kHistKind: the population keeps a post-spike history
 	int blk_per_step[kMaxPops];  // Poisson / external: CTAs per step
+	int src_steps;               // Poisson: consecutive steps each source CTA draws (>= 1)
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
 };
 cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks);

@@ -166,7 +166,7 @@ int set_last_error(int code, std::string const& msg) { return fail(code, msg); }
 // k_neurons CTA kind of a per-neuron population: 3 for a LIF whose every input group adds to V
 // through a 16-bit counter of word 0 (the fast replay), else 0.
 int neuron_block_kind(PopDev const& P) {
-	bool fast = P.model == LIF && P.W == 1 && P.ngroups <= 2;
+	bool fast = P.model == LIF && P.W == 1 && P.ngroups <= 2 && !P.pull;
 	for (int g = 0; g < P.ngroups && fast; g++)
 		fast = P.group_field[g] == 0 && P.group_bits[g] == 16 && P.group_word[g] == 0 && P.group_shift[g] == 16 * g;
 	return fast ? 3 : 0;
@@ -349,11 +349,17 @@ int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int n
 	} else if (synapse == SPICE_SYNAPSE_COUNT) {
 		if (np < 1 || !params) return fail(SPICE_EINVAL, "count needs params {scale[, field]}");
 		c.tau = 1.0f;
+	} else if (synapse == SPICE_SYNAPSE_WEIGHTED) {
+		if (np < 1 || !params) return fail(SPICE_EINVAL, "weighted needs params {wmax[, field]}");
+		if (n->pops[dst].d.model == USER)
+			return fail(SPICE_EINVAL, "weighted synapses into user-defined populations are not supported");
+		c.weighted = true;
+		c.wmax     = params[0];
 	} else {
 		return fail(SPICE_EINVAL, "unknown synapse model");
 	}
-	c.d.plastic = synapse;
-	*w          = params[0];
+	c.d.plastic = synapse == SPICE_SYNAPSE_WEIGHTED ? 0 : synapse;
+	*w          = c.weighted ? 0.0f : params[0];
 	*field      = np > 1 ? (int)params[1] : 0;
 	int const m = n->pops[dst].d.model;
 	if (m == USER ? (*field < 0 || *field >= n->pops[dst].nfields) : (*field < 0 || *field > 2 || (m == LIF && *field != 0)))
@@ -395,6 +401,8 @@ extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, d
 	n->conns.push_back(c);
 	// synapse_population ctor: _graph(c, seed++) (synapse_population.h:30-31)
 	n->gen_pending.push_back({(int)n->conns.size() - 1, seed_next(n), p});
+	// PerSynapseInit: rng(seed++) after the adjacency's (synapse_population.h:34-41)
+	if (c.weighted) n->conns.back().wseed = seed_next(n);
 	if (conn_out) *conn_out = (int)n->conns.size() - 1;
 	return SPICE_OK;
 }
@@ -448,6 +456,7 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	c.d.nb  = dnb;
 	n->conns.push_back(c);
 	seed_next(n);  // the synapse_population ctor consumes a seed for every topology
+	if (c.weighted) n->conns.back().wseed = seed_next(n);  // PerSynapseInit (synapse_population.h:34-41)
 	if (conn_out) *conn_out = (int)n->conns.size() - 1;
 	return SPICE_OK;
 }
@@ -534,6 +543,38 @@ int generate_pending(spice_net* n) {
 	return SPICE_OK;
 }
 
+// The per-synapse weights of weighted connections (their adjacency generated), drawn from each
+// connection's PerSynapseInit stream in CSR order.
+int init_weights(spice_net* n) {
+	for (auto& c : n->conns) {
+		if (!c.weighted || c.d.wts) continue;
+		float* w = nullptr;
+		TRY(dalloc(n, &w, (size_t)std::max<int64_t>(c.synapses, 1), false));
+		CUDA_TRY(init_synapse_weights(n->stream, c.wseed, c.synapses, c.wmax, w));
+		n->launches += 2;
+		c.d.wts = w;
+	}
+	return SPICE_OK;
+}
+
+// The CSC of connection ci (built once).
+int ensure_csc(spice_net* n, int ci) {
+	Conn& c = n->conns[ci];
+	if (c.d.csc_off) return SPICE_OK;
+	int64_t* off = nullptr;
+	int32_t* src = nullptr;
+	float* w     = nullptr;
+	TRY(dalloc(n, &off, (size_t)c.d.dst_size + 1, false));
+	TRY(dalloc(n, &src, (size_t)std::max<int64_t>(c.synapses, 1), false));
+	if (c.d.wts) TRY(dalloc(n, &w, (size_t)std::max<int64_t>(c.synapses, 1), false));
+	CUDA_TRY(build_csc(n->stream, c.d.off, c.d.nb, c.d.wts, c.d.src_size, c.d.dst_size, c.synapses, off, src, w));
+	n->launches += 5;
+	c.d.csc_off = off;
+	c.d.csc_src = src;
+	c.d.csc_w   = w;
+	return SPICE_OK;
+}
+
 // Tile sizes of the delivery kernel, the by-target connection order and the per-row positions
 // where each tile starts.  Called at preparation and again when the launch shape is re-tuned.
 int setup_tiles(spice_net* n, bool first) {
@@ -566,12 +607,13 @@ int setup_tiles(spice_net* n, bool first) {
 		int tile        = n->tile_bytes / (4 * std::max(width, 1));
 		tile            = std::max(32, tile / 32 * 32);
 		d.tile          = tile;
-		d.ntiles        = (d.in_end > d.in_begin && d.size > 0) ? (int)((d.size + tile - 1) / tile) : 0;
+		d.ntiles        = (d.in_end > d.in_begin && d.size > 0 && !d.pull) ? (int)((d.size + tile - 1) / tile) : 0;
 	}
 	for (auto& c : n->conns) {
 		ConnDev& d      = c.d;
 		PopDev const& T = n->pops[d.dst].d;
 		int64_t* bnd    = nullptr;
+		if (T.pull) continue;  // gathered by the pull kernel over the CSC: no tiles
 		if (!first && d.bounds) {
 			CUDA_TRY(cudaStreamSynchronize(n->stream));
 			cudaFree((void*)d.bounds);
@@ -598,9 +640,86 @@ int setup_tiles(spice_net* n, bool first) {
 	return SPICE_OK;
 }
 
+// Pulled populations: the CSC of their incoming connections, region starts, active-list, grouped
+// and bin-offset buffers; one window-mask set per (source population, delay); event jobs.
+int setup_pull(spice_net* n) {
+	int const np = (int)n->pops.size();
+	n->pull_pops.clear();
+	n->pull_sets.clear();
+	n->pull_ev.clear();
+	std::vector<int> blk(1, 0);
+	for (int pi = 0; pi < np; pi++) {
+		PopDev& d = n->pops[pi].d;
+		if (!d.pull) continue;
+		std::vector<const int64_t*> offs;
+		d.pull_F = 0;
+		for (int b = d.in_begin; b < d.in_end; b++) {
+			int const ci = n->by_dst[b];
+			TRY(ensure_csc(n, ci));
+			Conn& c = n->conns[ci];
+			offs.push_back(c.d.csc_off);
+			bool seen = false;
+			for (int f = 0; f < d.pull_F; f++) seen |= d.pull_field[f] == c.d.field;
+			if (!seen) d.pull_field[d.pull_F++] = c.d.field;
+			// the window masks of (source, delay)
+			int set = -1;
+			for (int q = 0; q < (int)n->pull_sets.size(); q++)
+				if (n->pull_sets[q].src == c.d.src && n->pull_sets[q].delay == c.d.delay) set = q;
+			if (set < 0) {
+				PopDev const& S = n->pops[c.d.src].d;
+				PullSet ps{};
+				ps.src    = c.d.src;
+				ps.delay  = c.d.delay;
+				ps.nwords = S.nwords;
+				ps.size   = S.size;
+				ps.bits   = S.bits;
+				TRY(dalloc(n, &ps.orb, (size_t)std::max(S.nwords, 1)));
+				TRY(dalloc(n, &ps.wm, (size_t)std::max<int64_t>(S.size, 1)));
+				set = (int)n->pull_sets.size();
+				n->pull_sets.push_back(ps);
+			}
+			c.d.pull_orb = n->pull_sets[set].orb;
+			c.d.pull_wm  = n->pull_sets[set].wm;
+			n->pull_ev.push_back({n->pops[c.d.src].d.nwords, n->pops[c.d.src].d.bits, c.d.off});
+		}
+		for (int f = d.pull_F; f < 3; f++) d.pull_field[f] = 0;
+		d.pull_nbins = n->K * d.pull_F;
+		const int64_t** d_offs = nullptr;
+		TRY(dalloc(n, &d_offs, offs.size(), false));
+		CUDA_TRY(cudaMemcpy(d_offs, offs.data(), sizeof(void*) * offs.size(), cudaMemcpyHostToDevice));
+		int64_t* base = nullptr;
+		TRY(dalloc(n, &base, (size_t)d.size + 1, false));
+		CUDA_TRY(pull_region_bases(n->stream, d_offs, (int)offs.size(), d.size, base));
+		n->launches++;
+		int64_t total = 0;
+		CUDA_TRY(cudaMemcpyAsync(&total, base + d.size, sizeof(int64_t), cudaMemcpyDeviceToHost, n->stream));
+		CUDA_TRY(cudaStreamSynchronize(n->stream));
+		d.pull_base = base;
+		TRY(dalloc(n, &d.pull_A, (size_t)std::max<int64_t>(total, 1), false));
+		TRY(dalloc(n, &d.pull_G, (size_t)std::max<int64_t>(total, 1), false));
+		TRY(dalloc(n, &d.pull_koff, (size_t)std::max<int64_t>(d.size, 1) * (d.pull_nbins + 1)));  // zero: no inputs yet
+		n->pull_pops.push_back(pi);
+		blk.push_back(blk.back() + pull_blocks_for(d.size));
+	}
+	n->pull_blocks = blk.back();
+	TRY(dalloc(n, &n->d_pull_pops, std::max<size_t>(n->pull_pops.size(), 1), false));
+	TRY(dalloc(n, &n->d_pull_blk, blk.size(), false));
+	TRY(dalloc(n, &n->d_pull_sets, std::max<size_t>(n->pull_sets.size(), 1), false));
+	TRY(dalloc(n, &n->d_pull_ev, std::max<size_t>(n->pull_ev.size(), 1), false));
+	if (!n->pull_pops.empty())
+		CUDA_TRY(cudaMemcpy(n->d_pull_pops, n->pull_pops.data(), sizeof(int) * n->pull_pops.size(), cudaMemcpyHostToDevice));
+	CUDA_TRY(cudaMemcpy(n->d_pull_blk, blk.data(), sizeof(int) * blk.size(), cudaMemcpyHostToDevice));
+	if (!n->pull_sets.empty())
+		CUDA_TRY(cudaMemcpy(n->d_pull_sets, n->pull_sets.data(), sizeof(PullSet) * n->pull_sets.size(), cudaMemcpyHostToDevice));
+	if (!n->pull_ev.empty())
+		CUDA_TRY(cudaMemcpy(n->d_pull_ev, n->pull_ev.data(), sizeof(PullEvJob) * n->pull_ev.size(), cudaMemcpyHostToDevice));
+	return SPICE_OK;
+}
+
 int prepare(spice_net* n) {
 	if (n->prepared) return SPICE_OK;
 	TRY(generate_pending(n));
+	TRY(init_weights(n));
 	int const np = (int)n->pops.size();
 	int64_t const D = n->max_delay;
 	if (D < 1) return pre_failed("neuron_population.h:108", "max_delay >= 1");
@@ -614,6 +733,37 @@ int prepare(spice_net* n) {
 			return fail(SPICE_EINVAL, "plastic synapses that deliver per-synapse weights need SPICE_MODE_ATOMIC "
 			                          "(their per-step sums are order-dependent)");
 	}
+	// pulled populations: inputs with per-synapse weights, the pull knob, or (deterministic mode)
+	// more distinct input weights than the count replay keeps apart
+	n->any_pull = false;
+	for (int pi = 0; pi < np; pi++) {
+		Pop& P = n->pops[pi];
+		P.d.pull = 0;
+		bool has_in = false, weighted_in = false, plastic_in = false;
+		int groups = 0, last_of_field[3] = {-1, -1, -1};
+		std::vector<float> gw;
+		for (auto const& c : n->conns) {
+			if (c.d.dst != pi) continue;
+			has_in = true;
+			weighted_in |= c.weighted;
+			plastic_in |= c.d.plastic != 0;
+			if (c.d.plastic || c.weighted) continue;
+			int const g = last_of_field[c.d.field];
+			if (g < 0 || memcmp(&gw[g], &c.d.weight, sizeof(float)) != 0) {
+				gw.push_back(c.d.weight);
+				last_of_field[c.d.field] = groups++;
+			}
+		}
+		if (!P.stateful || P.d.model == USER || !has_in) continue;
+		bool const pull = weighted_in || n->pull_all || (n->mode == SPICE_MODE_DETERMINISTIC && groups > kMaxGroups);
+		if (!pull) continue;
+		if (plastic_in)
+			return fail(SPICE_EINVAL, "population " + std::to_string(pi) +
+			                              ": plastic synapses into a population whose inputs are pulled (weighted synapses, "
+			                              "more than 4 distinct weights, or the pull knob) are not supported");
+		P.d.pull    = 1;
+		n->any_pull = true;
+	}
 	// window: the minimum delay (every delay is >= 1)
 	int K = kMaxWindow;
 	for (auto const& c : n->conns) K = std::min<int>(K, c.d.delay);
@@ -621,9 +771,11 @@ int prepare(spice_net* n) {
 	if (n->plastic) K = 1;
 	// the delivery kernel keeps a (step, connection) prefix of K * nconn entries in shared memory
 	if (!n->conns.empty()) K = std::min<int>(K, std::max<int>(1, 4096 / (int)n->conns.size()));
+	if (n->any_pull) K = std::min(K, kPullMaxWindow);  // step masks of 16 bits
 	n->K  = std::max(K, 1);
-	// bitmaps: the last D steps for spikes(age), and two windows in flight (sources run ahead)
-	n->Hb = (int)std::max<int64_t>(D, 2 * n->K) + 1;
+	// bitmaps: the last D steps for spikes(age), and two windows in flight (sources run ahead);
+	// the pull reads the D steps before the next window while sources may already write it
+	n->Hb = (int)std::max<int64_t>(D, 2 * n->K) + 1 + (n->any_pull ? n->K : 0);
 	// draw offsets in the step's shared stream (populations in add order, snn.cpp:14-15)
 	int64_t draws = 0;
 	for (auto& p : n->pops) {
@@ -652,11 +804,16 @@ int prepare(spice_net* n) {
 	for (int pi = 0; pi < np; pi++) {
 		PopDev& d = n->pops[pi].d;
 		if (!n->pops[pi].stateful) continue;
+		if (d.pull) {  // inputs are gathered by the pull kernel: no input ring
+			d.ngroups = 0;
+			d.W = d.F = 1;
+			continue;
+		}
 		int last_of_field[3] = {-1, -1, -1};
 		d.ngroups = 0;
 		for (int ci = 0; ci < (int)n->conns.size(); ci++) {
 			ConnDev& c = n->conns[ci].d;
-			if (c.dst != pi || c.plastic) continue;
+			if (c.dst != pi || c.plastic || n->conns[ci].weighted) continue;
 			int g = last_of_field[c.field];
 			if (g < 0 || memcmp(&d.group_weight[g], &c.weight, sizeof(float)) != 0) {
 				if (d.ngroups >= kMaxGroups)
@@ -780,6 +937,7 @@ int prepare(spice_net* n) {
 	}
 	for (auto& c : n->conns)
 		if (c.d.plastic) c.d.dst_hist = n->pops[c.d.dst].d.hist;
+	if (n->any_pull) TRY(setup_pull(n));
 	TRY(dalloc(n, &n->d_counts, (size_t)2 * n->K * std::max(np, 1)));
 	TRY(dalloc(n, &n->d_pops, std::max(np, 1), false));
 	TRY(dalloc(n, &n->d_conns, std::max<size_t>(n->conns.size(), 1), false));
@@ -797,6 +955,7 @@ int prepare(spice_net* n) {
 			CUDA_TRY(cudaMemcpy(n->d_conns_by_dst, hb.data(), sizeof(ConnDev) * hb.size(), cudaMemcpyHostToDevice));
 	}
 	n->run_cap = kRunCap;
+	CUDA_TRY(cudaDeviceGetAttribute(&n->sm_count, cudaDevAttrMultiProcessorCount, n->device));
 	// two chunk buffers: the host prepares one chunk while the GPU still steps the previous one
 	TRY(dalloc(n, &n->d_dt, 2 * kRunCap, false));
 	TRY(dalloc(n, &n->d_seeds, 2 * kRunCap, false));
@@ -951,7 +1110,6 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				if (P.model == POISSON) {
 					ws.blk_kind[p]     = 1;
 					ws.blk_per_step[p] = (P.nwords + 255) / 256;
-					nbs += ws.blk_per_step[p] * k;
 					wa.blk_kind[p] = 1;
 				} else if (P.model == USER) {
 					ws.blk_kind[p] = 0;  // launched by the user's callback
@@ -968,6 +1126,27 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					ws.blk_kind[p] = wa.blk_kind[p];
 					nb += (int)((P.size + 255) / 256);
 				}
+			}
+			// Poisson CTAs: src_steps consecutive steps each -- by default the fewest that keep the
+			// window's grid (neuron, source and raster CTAs) within one wave of resident CTAs
+			int poisson_bps = 0;
+			for (int p = 0; p < np; p++)
+				if (n->pops[p].d.model == POISSON) poisson_bps += ws.blk_per_step[p];
+			int S = n->src_steps > 0 ? std::min(n->src_steps, k) : 1;
+			if (n->src_steps == 0 && poisson_bps > 0) {
+				int const wave = n->sm_count * 8 - (record ? k * np : 0);
+				while (S < k && nb + nbs + poisson_bps * ((k + S - 1) / S) > wave) S++;
+			}
+			ws.src_steps = S;
+			{  // source block ranges with the chosen steps per CTA
+				int acc = 0;
+				for (int p = 0; p < np; p++) {
+					PopDev const& P = n->pops[p].d;
+					ws.blk_begin[p] = acc;
+					if (P.model == POISSON) acc += ws.blk_per_step[p] * ((k + S - 1) / S);
+					else if (P.model == EXTERNAL) acc += k;
+				}
+				nbs = acc;
 			}
 			wa.blk_begin[np] = nb;
 			ws.blk_begin[np] = nbs;
@@ -1060,6 +1239,29 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					}
 			TRY(ev_end(n, slot));
 			n->launches++;
+			if (n->any_pull) {  // the pulled populations' inputs of the next window, steps [time + k, time + k + K)
+				PullArgs pa{};
+				pa.t           = n->time + k;
+				pa.K           = n->K;
+				pa.Hb          = n->Hb;
+				pa.nsets       = (int)n->pull_sets.size();
+				pa.sets        = n->d_pull_sets;
+				pa.nev         = (int)n->pull_ev.size();
+				pa.ev          = n->d_pull_ev;
+				pa.t_emit0     = n->time;
+				pa.k_emit      = k;
+				pa.events      = n->d_events;
+				pa.npull       = (int)n->pull_pops.size();
+				pa.pull_pops   = n->d_pull_pops;
+				pa.pull_blk    = n->d_pull_blk;
+				pa.pull_blocks = n->pull_blocks;
+				pa.pops        = n->d_pops;
+				pa.conns       = n->d_conns_by_dst;
+				TRY(ev_begin(n, 4, &slot));
+				CUDA_TRY(launch_pull(n->stream, pa, n->pull_sets, n->pull_ev));
+				TRY(ev_end(n, slot));
+				n->launches += 2;
+			}
 			if (!fused) CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear
 			if (record) {
 				RasterArgs ra{};
@@ -1114,8 +1316,12 @@ int flush_pending(spice_net* n) {
 	bool user = false;
 	for (int i = 0; i < (int)n->pops.size(); i++) {
 		hp.push_back(n->pops[i].d);
-		if (n->pops[i].stateful && n->pops[i].d.model != USER) st.push_back(i);
+		if (n->pops[i].stateful && n->pops[i].d.model != USER && !n->pops[i].d.pull) st.push_back(i);
 		user |= n->pops[i].stateful && n->pops[i].d.model == USER;
+	}
+	for (int i : n->pull_pops) {  // the pulled inputs of the next step
+		CUDA_TRY(launch_pull_apply_first(n->stream, n->pops[i].d));
+		n->launches++;
 	}
 	CUDA_TRY(launch_apply_pending(n->stream, n->d_pops, (int)hp.size(), st.data(), (int)st.size(), hp, n->time,
 	                              n->max_delay, n->mode));
@@ -1356,6 +1562,18 @@ extern "C" int spice_get_csr(spice_net* n, int conn, int64_t* off, int32_t* nb) 
 	return SPICE_OK;
 }
 
+extern "C" int spice_get_csc(spice_net* n, int conn, int64_t* col_off, int32_t* src) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	TRY(generate_pending(n));
+	TRY(init_weights(n));
+	TRY(ensure_csc(n, conn));
+	Conn const& c = n->conns[conn];
+	if (col_off) CUDA_TRY(cudaMemcpy(col_off, c.d.csc_off, sizeof(int64_t) * (c.d.dst_size + 1), cudaMemcpyDeviceToHost));
+	if (src && c.synapses) CUDA_TRY(cudaMemcpy(src, c.d.csc_src, sizeof(int32_t) * c.synapses, cudaMemcpyDeviceToHost));
+	return SPICE_OK;
+}
+
 extern "C" int spice_set_profiling(spice_net* n, int on) {
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
 	TRY(harvest(n));
@@ -1374,10 +1592,11 @@ extern "C" int spice_get_synapse_state(spice_net* n, int conn, int field, float*
 	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
 	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
 	if (field < 0 || field > 2) return fail(SPICE_EINVAL, "field must be 0 (W), 1 (x_pre) or 2 (x_post)");
-	if (!n->conns[conn].d.plastic) return fail(SPICE_EINVAL, "not a plastic connection");
+	if (!n->conns[conn].d.plastic && !(n->conns[conn].weighted && field == 0))
+		return fail(SPICE_EINVAL, "not a plastic connection (a weighted connection has field 0, its weights)");
 	TRY(prepare(n));
 	ConnDev const& d = n->conns[conn].d;
-	const float* src = field == 0 ? d.sW : (field == 1 ? d.sA : d.sB);
+	const float* src = n->conns[conn].weighted ? d.wts : (field == 0 ? d.sW : (field == 1 ? d.sA : d.sB));
 	int64_t const m  = n->conns[conn].synapses;
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
 	if (m > 0) CUDA_TRY(cudaMemcpy(out, src, sizeof(float) * m, cudaMemcpyDeviceToHost));
@@ -1386,7 +1605,7 @@ extern "C" int spice_get_synapse_state(spice_net* n, int conn, int field, float*
 
 extern "C" int spice_kernel_stats(spice_net* n, int kind, int64_t* launches, double* ms) {
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
-	if (kind < 0 || kind > 3) return fail(SPICE_EINVAL, "unknown kernel kind");
+	if (kind < 0 || kind > 4) return fail(SPICE_EINVAL, "unknown kernel kind");
 	TRY(harvest(n));
 	if (launches) *launches = n->stats[kind].launches;
 	if (ms) *ms = n->stats[kind].ms;
@@ -1444,6 +1663,16 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 				for (int q = 0; q < 2; q++) CUDA_TRY(cudaEventRecord(n->ev_free[q], n->stream));
 			}
 			n->launch_mode = (int)value;
+			return SPICE_OK;
+		case SPICE_TUNE_SOURCE_STEPS:
+			if (value < 0 || value > kMaxWindow) return fail(SPICE_EINVAL, "source steps must be in [0, 64]");
+			n->src_steps = (int)value;
+			return SPICE_OK;
+		case SPICE_TUNE_PULL:
+			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "pull must be 0 or 1");
+			if (n->prepared && n->pull_all != (value != 0))
+				return fail(SPICE_ESTATE, "the delivery path of a population is fixed once the network steps");
+			n->pull_all = value != 0;
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
 			if (value < 0 || value > 6) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 6");

@@ -1,0 +1,402 @@
+// pull.cu -- deterministic delivery of per-synapse weights: the pull path over CSC adjacency.
+//
+// The reference delivers a step's spikes connection by connection in connect order, and within a
+// connection source by source in ascending order, each synapse adding its weight to its target
+// (synapse_population.h:118-133, snn.cpp:21-25).  For fixed_weight synapses the engine replays
+// per-target event counts (step.cu); a synapse that carries its own weight (the reference's
+// StatefulSynapse / PerSynapseInit concepts, concepts.h:60-104, synapse_population.h:34-41) needs
+// the weights themselves, in that order.  A population with such inputs is "pulled": per window,
+// every target gathers its own inputs from the columns of the CSC adjacency of its incoming
+// connections -- connect order, then ascending source, which is exactly the reference's order of
+// additions into that target -- and the neuron update adds them one IEEE addition at a time.
+//
+// Per window [t, t + K) (K <= min delay, so every input comes from spikes older than t):
+//   k_pull_masks -- for each (source population, delay d) of a pulled connection, from the
+//                   source's spike bitmap ring: orb (one bit per source: spiked at a step
+//                   t + k - d, k < K) and wm (per such source, bit k set when it spiked at
+//                   t + k - d).  The same launch counts the synaptic events of the window that
+//                   just ended for the pulled connections (row lengths of their spikes).
+//   k_pull       -- one warp per target neuron: scans the target's CSC column of each incoming
+//                   connection (coalesced source indices), keeps the synapses whose source bit is
+//                   set in orb (a few percent at biological rates) as an ordered active list
+//                   (weight, step mask, field), then groups the list by bin (step k, field f) with
+//                   a stable counting sort into the target's region of G, and writes the bin
+//                   starts koff.  A region holds as many entries as the target has synapses, so
+//                   grouping always fits unless one synapse reaches the target at several steps
+//                   of the window and the bins overflow; then koff[i][0] = -1 and the neuron
+//                   update walks the active list step by step instead.  Both orders are exact.
+// The neuron update of the window (window_neurons, step.cu) then adds, before step t + k, the
+// weights of bins (k, f) to field f in G order.
+//
+// CSC construction (build_csc): source rows are cut into nblk consecutive blocks; cnt[b][d] counts
+// block b's entries with target d; an exclusive prefix over b per target gives each block's start
+// within each column; then each block writes its rows in order (a barrier between rows), so the
+// entries of every column are in ascending source order without a sort.  Duplicate (source,
+// target) pairs of an adj_list row keep their CSR order.
+#include <stdint.h>
+
+#include <algorithm>
+#include <vector>
+
+#include "internal.h"
+#include "kernels.h"
+
+namespace spice_gb300 {
+
+namespace {
+
+constexpr int kPullThreads = 256;
+constexpr int kPullWarps   = kPullThreads / 32;
+constexpr int kMaxBins     = kPullMaxWindow * 3;
+
+__device__ __forceinline__ unsigned lanemask_lt_pull() {
+	unsigned m;
+	asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+	return m;
+}
+
+// ---- CSC construction ----
+
+__global__ void k_csc_count(const int64_t* __restrict__ off, const int32_t* __restrict__ nb, int64_t rows,
+                            int64_t rows_per_blk, int64_t ndst, uint32_t* __restrict__ cnt) {
+	int64_t const b  = blockIdx.y;
+	int64_t const r0 = b * rows_per_blk, r1 = min(rows, r0 + rows_per_blk);
+	if (r0 >= r1) return;
+	int64_t const e0 = off[r0], e1 = off[r1];
+	uint32_t* c      = cnt + b * ndst;
+	for (int64_t e = e0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < e1; e += (int64_t)gridDim.x * blockDim.x)
+		atomicAdd(c + nb[e], 1u);
+}
+
+// Per target d: cnt[b][d] becomes the exclusive prefix over blocks, indeg[d] the column length.
+__global__ void k_csc_colscan(uint32_t* __restrict__ cnt, int64_t nblk, int64_t ndst, int32_t* __restrict__ indeg) {
+	for (int64_t d = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; d < ndst; d += (int64_t)gridDim.x * blockDim.x) {
+		uint32_t run = 0;
+		for (int64_t b = 0; b < nblk; b++) {
+			uint32_t const c = cnt[b * ndst + d];
+			cnt[b * ndst + d] = run;
+			run += c;
+		}
+		indeg[d] = (int32_t)run;
+	}
+}
+
+// Block b writes its rows in order; the entries of one row are written in parallel.
+__global__ void k_csc_fill(const int64_t* __restrict__ off, const int32_t* __restrict__ nb, const float* __restrict__ w,
+                           int64_t rows, int64_t rows_per_blk, int64_t ndst, uint32_t* __restrict__ cnt,
+                           const int64_t* __restrict__ col_off, int32_t* __restrict__ col_src,
+                           float* __restrict__ col_w) {
+	int64_t const b  = blockIdx.x;
+	int64_t const r0 = b * rows_per_blk, r1 = min(rows, r0 + rows_per_blk);
+	uint32_t* c      = cnt + b * ndst;
+	for (int64_t r = r0; r < r1; r++) {
+		int64_t const e0 = off[r], e1 = off[r + 1];
+		for (int64_t base = e0; base < e1; base += blockDim.x) {
+			int64_t const e = base + threadIdx.x;
+			bool last       = false;
+			int32_t d       = 0;
+			uint32_t rank   = 0;
+			if (e < e1) {
+				d = nb[e];
+				while (e - (int64_t)rank - 1 >= e0 && nb[e - rank - 1] == d) rank++;  // earlier duplicates
+				int64_t const pos = col_off[d] + c[d] + rank;
+				col_src[pos]      = (int32_t)r;
+				if (w) col_w[pos] = w[e];
+				last = e + 1 == e1 || nb[e + 1] != d;
+			}
+			__syncthreads();
+			if (last) c[d] += rank + 1;
+			__syncthreads();
+		}
+	}
+}
+
+// base[i] = sum over the pulled connections of their column starts: the prefix of the total
+// in-degree, i <= n.
+__global__ void k_pull_base(const int64_t* const* __restrict__ col_offs, int nconn, int64_t n, int64_t* __restrict__ base) {
+	for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i <= n; i += (int64_t)gridDim.x * blockDim.x) {
+		int64_t s = 0;
+		for (int c = 0; c < nconn; c++) s += col_offs[c][i];
+		base[i] = s;
+	}
+}
+
+// ---- per window ----
+
+__device__ __forceinline__ int64_t ring_step(int64_t step, int Hb) { return ((step % Hb) + Hb) % Hb; }
+
+// Blocks: first the mask sets (one thread per source bitmap word), then the event jobs.
+__global__ void __launch_bounds__(kPullThreads) k_pull_masks(const __grid_constant__ PullArgs a) {
+	int b = (int)blockIdx.x;
+	for (int s = 0; s < a.nsets; s++) {
+		PullSet const S = a.sets[s];
+		int const nb    = (S.nwords + kPullThreads - 1) / kPullThreads;
+		if (b < nb) {
+			int const w = b * kPullThreads + threadIdx.x;
+			if (w >= S.nwords) return;
+			uint32_t x[kPullMaxWindow];
+			uint32_t any = 0;
+#pragma unroll
+			for (int k = 0; k < kPullMaxWindow; k++) {
+				int64_t const step = a.t + k - S.delay;
+				x[k]               = (k < a.K && step >= 0) ? S.bits[ring_step(step, a.Hb) * S.nwords + w] : 0u;
+				any |= x[k];
+			}
+			S.orb[w] = any;
+			uint32_t rest = any;
+			while (rest) {
+				int const bit = __ffs(rest) - 1;
+				rest &= rest - 1;
+				uint32_t m = 0;
+#pragma unroll
+				for (int k = 0; k < kPullMaxWindow; k++) m |= ((x[k] >> bit) & 1u) << k;
+				S.wm[32 * (int64_t)w + bit] = m;
+			}
+			return;
+		}
+		b -= nb;
+	}
+	// events of the pulled connections' spikes of the window that just ended
+	__shared__ unsigned long long ev_sm;
+	if (threadIdx.x == 0) ev_sm = 0;
+	__syncthreads();
+	for (int j = 0; j < a.nev; j++) {
+		PullEvJob const J = a.ev[j];
+		int const nb      = (J.nwords + kPullThreads - 1) / kPullThreads;
+		if (b < nb) {
+			int const w = b * kPullThreads + threadIdx.x;
+			unsigned long long ev = 0;
+			if (w < J.nwords)
+				for (int k = 0; k < a.k_emit; k++) {
+					uint32_t x = J.bits[ring_step(a.t_emit0 + k, a.Hb) * J.nwords + w];
+					while (x) {
+						int64_t const s = 32 * (int64_t)w + __ffs(x) - 1;
+						x &= x - 1;
+						ev += (unsigned long long)(J.off[s + 1] - J.off[s]);
+					}
+				}
+			for (int o = 16; o > 0; o >>= 1) ev += __shfl_down_sync(0xffffffffu, ev, o);
+			if ((threadIdx.x & 31) == 0 && ev) atomicAdd(&ev_sm, ev);
+			__syncthreads();
+			if (threadIdx.x == 0 && ev_sm) atomicAdd(a.events, ev_sm);
+			return;
+		}
+		b -= nb;
+	}
+}
+
+// One chunk of up to 32 active entries (one per lane; m = step mask, f = field bin) against the
+// bins (k, f) = k * F + f.  PLACE = false: adds each bin's entry count to cnt.  PLACE = true:
+// writes each entry's weight to G at run[bin] + its rank among the chunk's earlier lanes of that
+// bin, then advances run.  Lanes of one bin are handled in lane order within each step k, and steps
+// in ascending order, so the entries of every bin keep the active list's order.  With at most one
+// step bit per lane (the common case) one pass covers every bin.
+template <bool PLACE>
+__device__ __forceinline__ void bin_pass(uint32_t m, int f, int F, int nbins, int lane, int* cnt, int* run, float* G,
+                                         uint32_t wbits) {
+	unsigned const lt = lanemask_lt_pull();
+	if (__all_sync(0xffffffffu, __popc(m) <= 1)) {
+		int const bn        = m ? (__ffs(m) - 1) * F + f : nbins;  // lanes without a bit: the spare bin
+		unsigned const same = __match_any_sync(0xffffffffu, bn);
+		if (m) {
+			if (PLACE) G[run[bn] + __popc(same & lt)] = __uint_as_float(wbits);
+			__syncwarp(same);
+			if ((same & lt) == 0) (PLACE ? run : cnt)[bn] += __popc(same);
+		}
+		__syncwarp();
+		return;
+	}
+	uint32_t all = __reduce_or_sync(0xffffffffu, m);
+	while (all) {
+		int const k = __ffs(all) - 1;
+		all &= all - 1;
+		bool const has      = (m >> k) & 1u;
+		int const bn        = has ? k * F + f : nbins;
+		unsigned const same = __match_any_sync(0xffffffffu, bn);
+		if (has) {
+			if (PLACE) G[run[bn] + __popc(same & lt)] = __uint_as_float(wbits);
+			__syncwarp(same);
+			if ((same & lt) == 0) (PLACE ? run : cnt)[bn] += __popc(same);
+		}
+		__syncwarp();
+	}
+}
+
+// One warp per target neuron of the pulled populations.
+__global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ PullArgs a) {
+	__shared__ int bin_cnt[kPullWarps][kMaxBins + 1];
+	__shared__ int bin_run[kPullWarps][kMaxBins + 1];
+	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	int const blk  = (int)blockIdx.x;
+	int q          = 0;
+	while (q + 1 < a.npull && blk >= a.pull_blk[q + 1]) q++;
+	int const pi     = a.pull_pops[q];
+	PopDev const& P  = a.pops[pi];
+	int64_t const i  = (int64_t)(blk - a.pull_blk[q]) * kPullWarps + wid;
+	if (i >= P.size) return;
+	int const F = P.pull_F, nbins = a.K * F;
+	int64_t const base = P.pull_base[i];
+	int64_t const cap  = P.pull_base[i + 1] - base;
+	uint64_t* A        = P.pull_A + base;
+	// 1. the active synapses, in connect order and ascending source order
+	int64_t nA = 0;
+	for (int c = P.in_begin; c < P.in_end; c++) {
+		ConnDev const& C = a.conns[c];
+		int f            = 0;
+		while (f + 1 < F && P.pull_field[f] != C.field) f++;
+		int64_t const e0 = C.csc_off[i], e1 = C.csc_off[i + 1];
+		uint32_t const fw = __float_as_uint(C.weight);
+		for (int64_t eb = e0; eb < e1; eb += 32) {
+			int64_t const e = eb + lane;
+			bool act        = false;
+			uint32_t m = 0, wb = 0;
+			if (e < e1) {
+				int32_t const s = __ldg(C.csc_src + e);
+				act             = (__ldg(C.pull_orb + (s >> 5)) >> (s & 31)) & 1u;
+				if (act) {
+					m  = __ldg(C.pull_wm + s) & ((1u << a.K) - 1u);
+					wb = C.csc_w ? __float_as_uint(__ldg(C.csc_w + e)) : fw;
+					act = m != 0;
+				}
+			}
+			unsigned const bal = __ballot_sync(0xffffffffu, act);
+			if (act) A[nA + __popc(bal & lanemask_lt_pull())] = (uint64_t)wb | ((uint64_t)(m | ((uint32_t)f << 16)) << 32);
+			nA += __popc(bal);
+		}
+	}
+	__syncwarp();
+	int32_t* ko = P.pull_koff + i * (int64_t)(P.pull_nbins + 1);
+	// 2. entries per bin (an entry with several step bits lands in several bins)
+	for (int bn = lane; bn <= nbins; bn += 32) bin_cnt[wid][bn] = 0;
+	__syncwarp();
+	for (int64_t c0 = 0; c0 < nA; c0 += 32) {
+		int64_t const e = c0 + lane;
+		uint32_t const mf = e < nA ? (uint32_t)(A[e] >> 32) : 0u;
+		bin_pass<false>(mf & 0xffffu, (int)(mf >> 16), F, nbins, lane, bin_cnt[wid], bin_run[wid], nullptr, 0u);
+	}
+	__syncwarp();
+	// exclusive prefix over the bins
+	int64_t total = 0;
+	for (int b0 = 0; b0 < nbins; b0 += 32) {
+		int const bn = b0 + lane;
+		int const v  = bn < nbins ? bin_cnt[wid][bn] : 0;
+		int incl     = v;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			int const o = __shfl_up_sync(0xffffffffu, incl, d);
+			if (lane >= d) incl += o;
+		}
+		if (bn < nbins) bin_run[wid][bn] = (int)total + incl - v;
+		total += __shfl_sync(0xffffffffu, incl, 31);
+	}
+	__syncwarp();
+	if (total > cap) {  // several spikes of one source in the window overflow the region: walk A
+		if (lane == 0) {
+			ko[0] = -1;
+			ko[1] = (int32_t)nA;
+		}
+		return;
+	}
+	for (int bn = lane; bn < nbins; bn += 32) ko[bn] = bin_run[wid][bn];
+	if (lane == 0) ko[nbins] = (int32_t)total;
+	__syncwarp();
+	// 3. stable placement: chunks in order, and within a chunk lanes in order per bin
+	float* G = P.pull_G + base;
+	for (int64_t c0 = 0; c0 < nA; c0 += 32) {
+		int64_t const e = c0 + lane;
+		uint64_t const v = e < nA ? A[e] : 0ull;
+		uint32_t const mf = (uint32_t)(v >> 32);
+		bin_pass<true>(mf & 0xffffu, (int)(mf >> 16), F, nbins, lane, bin_cnt[wid], bin_run[wid], G, (uint32_t)v);
+	}
+}
+
+// The inputs of the first pulled step (bins k = 0), applied now and removed from the bins: state
+// reads between steps see the reference's state after step(), which has delivered them already.
+__global__ void k_pull_apply_first(PopDev P) {
+	int64_t const i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	if (i >= P.size) return;
+	int32_t* ko        = P.pull_koff + i * (int64_t)(P.pull_nbins + 1);
+	int64_t const base = P.pull_base[i];
+	float v[3]         = {P.V[i], P.Gex ? P.Gex[i] : 0.0f, P.Gin ? P.Gin[i] : 0.0f};
+	if (ko[0] >= 0) {
+		for (int f = 0; f < P.pull_F; f++) {
+			float x = v[P.pull_field[f]];
+			for (int32_t e = ko[f]; e < ko[f + 1]; e++) x = __fadd_rn(x, P.pull_G[base + e]);
+			v[P.pull_field[f]] = x;
+		}
+		for (int f = 0; f < P.pull_F; f++) ko[f] = ko[P.pull_F];  // bins (0, f) are now empty
+	} else {
+		int32_t const nA = ko[1];
+		for (int32_t e = 0; e < nA; e++) {
+			uint64_t const a = P.pull_A[base + e];
+			uint32_t const mf = (uint32_t)(a >> 32);
+			if (mf & 1u) {
+				int const fi = P.pull_field[mf >> 16];
+				v[fi]        = __fadd_rn(v[fi], __uint_as_float((uint32_t)a));
+				P.pull_A[base + e] = a & ~(1ull << 32);
+			}
+		}
+	}
+	P.V[i] = v[0];
+	if (P.Gex) P.Gex[i] = v[1];
+	if (P.Gin) P.Gin[i] = v[2];
+}
+
+}  // namespace
+
+cudaError_t build_csc(cudaStream_t stream, const int64_t* off, const int32_t* nb, const float* wts, int64_t rows,
+                      int64_t ndst, int64_t synapses, int64_t* col_off, int32_t* col_src, float* col_w) {
+	cudaError_t e = cudaMemsetAsync(col_off, 0, sizeof(int64_t) * (ndst + 1), stream);
+	if (e != cudaSuccess || synapses == 0 || rows == 0 || ndst == 0) return e;
+	// blocks of rows: at most 1024, and the count array at most 2^25 entries
+	int64_t nblk = std::max<int64_t>(1, std::min<int64_t>(1024, (int64_t(1) << 25) / std::max<int64_t>(ndst, 1)));
+	nblk         = std::min(nblk, rows);
+	int64_t const rows_per_blk = (rows + nblk - 1) / nblk;
+	nblk                       = (rows + rows_per_blk - 1) / rows_per_blk;
+	uint32_t* cnt  = nullptr;
+	int32_t* indeg = nullptr;
+	e = cudaMalloc(&cnt, sizeof(uint32_t) * nblk * ndst);
+	if (e == cudaSuccess) e = cudaMalloc(&indeg, sizeof(int32_t) * ndst);
+	if (e == cudaSuccess) e = cudaMemsetAsync(cnt, 0, sizeof(uint32_t) * nblk * ndst, stream);
+	if (e == cudaSuccess) {
+		dim3 const g((unsigned)std::max<int64_t>(1, std::min<int64_t>(256, synapses / nblk / 1024 + 1)), (unsigned)nblk);
+		k_csc_count<<<g, 256, 0, stream>>>(off, nb, rows, rows_per_blk, ndst, cnt);
+		k_csc_colscan<<<(unsigned)std::min<int64_t>((ndst + 255) / 256, 4096), 256, 0, stream>>>(cnt, nblk, ndst, indeg);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = scan_row_lengths(stream, indeg, ndst, col_off);
+	if (e == cudaSuccess) {
+		k_csc_fill<<<(unsigned)nblk, 256, 0, stream>>>(off, nb, wts, rows, rows_per_blk, ndst, cnt, col_off, col_src, col_w);
+		e = cudaGetLastError();
+	}
+	if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
+	cudaFree(cnt);
+	cudaFree(indeg);
+	return e;
+}
+
+cudaError_t pull_region_bases(cudaStream_t stream, const int64_t* const* col_offs, int nconn, int64_t n, int64_t* base) {
+	k_pull_base<<<(unsigned)std::min<int64_t>((n + 256) / 256, 4096), 256, 0, stream>>>(col_offs, nconn, n, base);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<PullSet> const& sets,
+                        std::vector<PullEvJob> const& ev) {
+	int64_t nb = 0;
+	for (auto const& s : sets) nb += (s.nwords + kPullThreads - 1) / kPullThreads;
+	if (a.k_emit > 0)
+		for (auto const& j : ev) nb += (j.nwords + kPullThreads - 1) / kPullThreads;
+	if (nb > 0) k_pull_masks<<<(unsigned)nb, kPullThreads, 0, stream>>>(a);
+	if (a.pull_blocks > 0) k_pull<<<(unsigned)a.pull_blocks, kPullThreads, 0, stream>>>(a);
+	return cudaGetLastError();
+}
+
+int pull_blocks_for(int64_t size) { return (int)((size + kPullWarps - 1) / kPullWarps); }
+
+cudaError_t launch_pull_apply_first(cudaStream_t stream, PopDev const& P) {
+	if (P.size <= 0) return cudaSuccess;
+	k_pull_apply_first<<<(unsigned)((P.size + 255) / 256), 256, 0, stream>>>(P);
+	return cudaGetLastError();
+}
+
+}  // namespace spice_gb300

@@ -240,7 +240,18 @@ __device__ __forceinline__ void window_neurons(A const& a, const PopDev* __restr
 	int slot  = a.slot0;   // (t0 - 1) mod D: inputs applied before the update of step t0
 	int hslot = a.hslot0;  // t0 mod Hb
 	int32_t* const count = a.counts + p;
-	bool const word_in = MODE == 0 && W == 1;
+	// pulled population (pull.cu): the inputs of step k are the weights of bins (k, f), in order
+	bool const pulled  = Pg->pull != 0;
+	int const pF       = Pg->pull_F;
+	const int32_t* ko  = nullptr;
+	int64_t pbase      = 0;
+	int32_t ko0        = 0;
+	if (pulled && valid) {
+		ko    = Pg->pull_koff + (int64_t)i * (Pg->pull_nbins + 1);
+		pbase = Pg->pull_base[i];
+		ko0   = ko[0];
+	}
+	bool const word_in = MODE == 0 && W == 1 && !pulled;
 	for (int k0 = 0; k0 < a.K; k0 += 16) {
 		int const nk = min(16, a.K - k0);
 		uint32_t xs[16];
@@ -258,7 +269,32 @@ __device__ __forceinline__ void window_neurons(A const& a, const PopDev* __restr
 			float const dt = a.dts[k];
 			bool spike     = false;
 			if (valid) {
-				if (word_in) {
+				if (pulled) {
+					if (ko0 >= 0) {
+						for (int f = 0; f < pF; f++) {
+							int const fi = Pg->pull_field[f];
+							float v      = fi == 0 ? V : (fi == 1 ? Gex : Gin);
+							int32_t const e1 = ko[k * pF + f + 1];
+							for (int32_t e = ko[k * pF + f]; e < e1; e++) v = __fadd_rn(v, Pg->pull_G[pbase + e]);
+							if (fi == 0) V = v;
+							else if (fi == 1) Gex = v;
+							else Gin = v;
+						}
+					} else {  // not grouped: the active synapses with step bit k, in order
+						int32_t const nA = ko[1];
+						for (int32_t e = 0; e < nA; e++) {
+							uint64_t const av = Pg->pull_A[pbase + e];
+							uint32_t const mf = (uint32_t)(av >> 32);
+							if ((mf >> k) & 1u) {
+								int const fi  = Pg->pull_field[mf >> 16];
+								float const w = __uint_as_float((uint32_t)av);
+								if (fi == 0) V = __fadd_rn(V, w);
+								else if (fi == 1) Gex = __fadd_rn(Gex, w);
+								else Gin = __fadd_rn(Gin, w);
+							}
+						}
+					}
+				} else if (word_in) {
 					uint32_t const x = xs[u];
 					if (x) {
 						if (FAST) {
@@ -730,7 +766,16 @@ __device__ __forceinline__ void sources_block(WindowArgs const& a, int b) {
 	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb = b - a.blk_begin[p];
-	if (a.blk_kind[p] == 1) window_poisson(a, a.pops + p, p, lb, a.blk_per_step[p], red);
+	if (a.blk_kind[p] == 1) {
+		// the chunk's steps [k0, k0 + src_steps): src_steps > 1 keeps the window's grid within one wave
+		int const bps = a.blk_per_step[p];
+		int const S   = a.src_steps > 0 ? a.src_steps : 1;
+		int const k0  = (lb / bps) * S, cb = lb % bps;
+		for (int k = k0; k < min(a.K, k0 + S); k++) {
+			if (k > k0) __syncthreads();  // red[] of the previous step is read
+			window_poisson(a, a.pops + p, p, k * bps + cb, bps, red);
+		}
+	}
 	else if (a.blk_kind[p] == 2) window_external(a, a.pops + p, p, lb, a.ext_pos[p]);
 }
 

@@ -48,6 +48,8 @@ def brunel(args):
         tb, th, parts, algo = (int(x) for x in args.tuning.split(","))
         net.set_tuning(tile_bytes=tb, deliver_threads=th, deliver_parts=parts, deliver_algo=algo)
     net.set_tuning(neuron_variant=args.neuron_variant)
+    if args.pull:
+        net.set_tuning(pull=True)
     t = time.perf_counter()
     if args.json:
         raster = net.run_record(args.steps)
@@ -114,6 +116,7 @@ def main(argv=None) -> int:
     b.add_argument("--tuning", default="", metavar="TILE_BYTES,THREADS,PARTS,ALGO",
                    help="delivery launch shape (results do not depend on it)")
     b.add_argument("--neuron-variant", type=int, default=0, help="LIF window variant (results do not depend on it)")
+    b.add_argument("--pull", action="store_true", help="deliver every population by the pull path over the CSC")
     v = sub.add_parser("vogels")
     v.add_argument("--N", type=int, default=4000)
     v.add_argument("--seed", type=int, default=1337)

@@ -17,12 +17,15 @@ headers) compiled by oracle/Makefile with the reference's Release flags -- and s
                              of P, E, I and, per block, the raster checksum and E / I state checksums
   vogels_n4000.npz           samples/vogels.cpp as published (N=4000, delay 8 dt, seed 1337), 1000
                              steps: raster (E, I) and final V / Gex / Gin / Tref
+  weighted_net.npz           oracle.WEIGHTED_NET (per-synapse weights drawn by PerSynapseInit into LIF
+                             and conductance targets, fixed weights, delays 3..12, a population with
+                             six distinct input weights), 600 steps: raster and final states
   vogels_c3_n10000.npz       the plastic E/I network's neurons and static weights without plasticity
                              (N=1e4 conductance LIF, p=0.02, E 0.03 / I 0.3, delay 1 step, seed 7),
                              1000 steps: raster and final state
 
 usage: python tests/golden/make_golden.py [GROUP ...]   (needs the reference sources; run from the
-       repo root; groups: base, vogels, brunel_long; default: all)
+       repo root; groups: base, vogels, weighted, brunel_long; default: all)
 """
 from __future__ import annotations
 
@@ -80,6 +83,21 @@ def vogels_fixtures():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **arrs)
 
 
+def weighted_fixtures(steps: int = 600):
+    res = O.run_reference_net(O.weighted_net_spec(steps))
+    kinds = [p[0] for p in O.WEIGHTED_NET["pops"]]
+    lif = [k for k, x in enumerate(kinds) if x == "lif"]
+    cond = [k for k, x in enumerate(kinds) if x == "lif_cond"]
+    st, _, _ = O.reference_states(res, lif, cond)
+    counts, idx = raster_arrays(res)
+    arrs = {"counts": counts, "idx": idx, "steps": np.array([steps])}
+    for k in lif:
+        arrs[f"V{k}"], arrs[f"T{k}"] = st[k]
+    for k in cond:
+        arrs[f"V{k}"], arrs[f"Gex{k}"], arrs[f"Gin{k}"], arrs[f"T{k}"] = st[k]
+    np.savez_compressed(os.path.join(HERE, "weighted_net.npz"), **arrs)
+
+
 def brunel_long_fixtures():
     arrs = {}
     jobs = [(1, BRUNEL_LONG_SEED1_STEPS, BRUNEL_LONG_BLOCK)] + [(sd, BRUNEL_SEEDS_STEPS, BRUNEL_SEEDS_BLOCK)
@@ -93,11 +111,13 @@ def brunel_long_fixtures():
     np.savez_compressed(os.path.join(HERE, "brunel_n500000_long.npz"), **arrs)
 
 
-def main(groups=("base", "vogels", "brunel_long")):
+def main(groups=("base", "vogels", "weighted", "brunel_long")):
     if not O.have_reference():
         O.build(with_reference=True, reference_dir=os.environ.get("SPICE_REFERENCE_DIR", "/root/reference"))
     if "vogels" in groups:
         vogels_fixtures()
+    if "weighted" in groups:
+        weighted_fixtures()
     if "brunel_long" in groups:
         brunel_long_fixtures()
     if "base" not in groups:
@@ -159,4 +179,4 @@ def main(groups=("base", "vogels", "brunel_long")):
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("base", "vogels", "brunel_long"))
+    main(tuple(sys.argv[1:]) or ("base", "vogels", "weighted", "brunel_long"))

@@ -454,3 +454,26 @@ def test_retuning_mid_run_keeps_results(engine):
     assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
     for k in (1, 2):
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
+@pytest.mark.parametrize("steps_per_cta", [0, 1, 3, 7, 15])
+def test_results_independent_of_source_steps(engine, oracle_lib, steps_per_cta):
+    """Poisson source CTAs drawing several consecutive steps each (0: chosen so the window's grid is
+    one wave) give the reference's raster and state bit for bit, recorded and step by step."""
+    sp, o = engine, oracle_lib
+    N, p, seed = 30000, 0.02, 4
+    net, pops = sp.brunel(N, p, seed)
+    net.set_tuning(source_steps=steps_per_cta)
+    ref, rpops = o.brunel(N, p, seed)
+    raster = net.run_record(200)
+    for t, row in enumerate(raster):
+        ref.step()
+        for k in range(3):
+            assert np.array_equal(np.asarray(row[k]), ref.spikes(rpops[k], 0)), (t, k)
+    for _ in range(7):
+        net.step()
+        ref.step()
+    for k in range(3):
+        assert np.array_equal(net.spikes(pops[k], 0), ref.spikes(rpops[k], 0))
+    for k in (1, 2):
+        assert np.array_equal(net.get_state(pops[k], sp.FIELD_V).view(np.uint32), ref.state(rpops[k], 0).view(np.uint32))

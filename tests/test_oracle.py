@@ -209,6 +209,38 @@ def test_large_brunel_seed_block_vs_reference(oracle_lib):
     assert got == ref
 
 
+def test_weighted_net_raster_and_state(oracle_lib):
+    """Per-synapse weights drawn by the PerSynapseInit stream (oracle.WEIGHTED_NET: weighted synapses
+    into LIF and conductance targets, fixed weights, delays 3..12 steps, six distinct weights into
+    one population): raster and final states equal the reference binary's bit for bit."""
+    o = oracle_lib
+    g = _golden("weighted_net.npz")
+    net, pops, _ = o.weighted_net()
+    _raster_matches(net, pops, g["counts"], g["idx"])
+    for k, (kind, *_rest) in enumerate(o.WEIGHTED_NET["pops"]):
+        if kind == "lif":
+            assert np.array_equal(net.state(pops[k], 0).view(np.uint32), g[f"V{k}"].view(np.uint32)), k
+            assert np.array_equal(net.state(pops[k], 3), g[f"T{k}"]), k
+        elif kind == "lif_cond":
+            for f, fld in (("V", 0), ("Gex", 1), ("Gin", 2)):
+                assert np.array_equal(net.state(pops[k], fld).view(np.uint32), g[f"{f}{k}"].view(np.uint32)), (k, f)
+            assert np.array_equal(net.state(pops[k], 3), g[f"T{k}"]), k
+
+
+def test_weighted_weights_are_the_init_stream(oracle_lib):
+    """The weights are wmax * canonical<float> of consecutive draws of the stream seeded one seed
+    after the adjacency's, in CSR order (synapse_population.h:30-41)."""
+    o = oracle_lib
+    net = o.Net(1e-4, 1e-4, [99])
+    S = net.add_population(o.POISSON, 300, (20.0,))
+    D = net.add_population(o.LIF, 200)
+    c = net.connect_weighted(S, D, 0.1, 1e-4, 0.25)
+    chain = o.seed_chain([99], 3)  # 0: the LIF population, 1: the adjacency, 2: the weights
+    draws = o.xoroshiro_draws(tuple(int(x) for x in chain[2]), len(net.syn_weights(c)))
+    canon = np.array([o.lib().spo_canonical_f32(int(u)) for u in draws], dtype=np.float32)
+    assert np.array_equal(net.syn_weights(c).view(np.uint32), (np.float32(0.25) * canon).view(np.uint32))
+
+
 def test_oracle_errors(oracle_lib):
     o = oracle_lib
     net = o.Net(1e-4, 15e-4, [1])
