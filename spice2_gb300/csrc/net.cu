@@ -815,7 +815,10 @@ int prepare(spice_net* n) {
 			ConnDev& c = n->conns[ci].d;
 			if (c.dst != pi || c.plastic || n->conns[ci].weighted) continue;
 			int g = last_of_field[c.field];
-			if (g < 0 || memcmp(&d.group_weight[g], &c.weight, sizeof(float)) != 0) {
+			// deterministic mode replays counts per weight; atomic mode sums weights per field
+			bool const new_group = g < 0 || (n->mode == SPICE_MODE_DETERMINISTIC &&
+			                                 memcmp(&d.group_weight[g], &c.weight, sizeof(float)) != 0);
+			if (new_group) {
 				if (d.ngroups >= kMaxGroups)
 					return fail(SPICE_EINVAL, "too many distinct input weights into one population (max 4)");
 				g                 = d.ngroups++;
