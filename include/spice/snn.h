@@ -1,27 +1,48 @@
 // spice/snn.h -- the reference's C++20 user API (spice/include/spice/snn.h:16-75) on the GB300
-// engine.  A program written against spice2's snn for the sample models compiles against this
-// header unchanged in its calls: snn(dt, max_delay, {seed}), add_population<Model>(size, model),
-// connect<Synapse>(from, to, fixed_probability(p) | adj_list, delay, {params}), step(), and the
-// population handle's spikes(age) / get_neurons().  Everything runs on the GPU through the C ABI of
-// spice_gb300.h; violated preconditions throw std::logic_error with the reference's message
+// engine.  A program written against spice2's snn compiles against this header unchanged in its
+// calls: snn(dt, max_delay, {seed}), add_population<Model>(size, model), connect<Synapse>(from, to,
+// fixed_probability(p) | adj_list, delay, {params}), step(), and the population handle's
+// spikes(age) / get_neurons().  Everything runs on the GPU through the C ABI of spice_gb300.h;
+// violated preconditions throw std::logic_error with the reference's message
 // (spice/src/util/assert.cpp:8-15).
 //
-// The models of the reference's samples are built into the engine: poisson (samples/brunel.cpp:
-// 23-31), lif (brunel.cpp:39-62), lif_cond (samples/vogels.cpp:10-46), external_input
-// (samples/external_input.cpp:17-30); synapses fixed_weight (brunel.cpp:67-70), excitatory /
-// inhibitory (vogels.cpp:48-60).  Any other model type is a user model (the reference's Neuron
-// concepts, concepts.h:10-58): compiled with nvcc, this header instantiates GPU kernels over it --
-// a stateful model's `SPICE_HD bool update(neuron&, float dt, auto& rng) const` (no random stream:
-// draws return 0), a stateless model's `SPICE_HD bool update(float dt, auto& rng) const` drawing once
-// per neuron and step from the reference's stream -- and the engine launches them each window.
-// Synapses into a user neuron add their `weight` to the float member named by their
-// `static constexpr auto field`.
+// Models.  The reference ships no models: its samples define them.  spice::models holds the
+// samples' models built into the engine -- poisson (samples/brunel.cpp:23-31), lif (brunel.cpp:
+// 39-62), lif_cond (samples/vogels.cpp:10-46), external_input (samples/external_input.cpp:17-30);
+// synapses fixed_weight (brunel.cpp:67-70), excitatory / inhibitory (vogels.cpp:48-60) and weighted
+// (a per-synapse weight drawn at construction) -- computed the way the reference's -ffast-math
+// build computes them, so their results are bit-exact.  Any other type is a user model (the
+// reference's concepts, concepts.h:10-104), compiled with nvcc into GPU kernels by this header:
+//   neurons  stateless `SPICE_HD bool update(float dt, auto& rng) const` (one draw per neuron and
+//            step from the step's stream, the reference's order); stateful `SPICE_HD bool
+//            update(neuron&, float dt, auto& rng) const` with a nested `neuron` struct of 4-byte
+//            members.  A stateful model that declares `static constexpr int draws_per_update = n`
+//            draws n numbers per neuron and step from the step's stream in the reference's order
+//            (populations in add order, neurons ascending); without it its draws come from an
+//            independent stream per (population, neuron, step) (statistically uniform, not the
+//            reference's sequence).  init(neuron&, Int id, rng) / init(span<neuron>, rng) run on
+//            the host at add_population with the population's own stream (neuron_population.h:
+//            56-67), exactly as the reference runs them.
+//   synapses stateless `SPICE_HD void deliver(Dst::neuron&) const` or stateful (a nested `synapse`
+//            struct) `SPICE_HD void deliver(synapse const&, Dst::neuron&) const` that add a
+//            constant, or a float member of the synapse, to one float member of the target neuron
+//            -- found by calling deliver() on probe values at connect time (a synapse may also name
+//            the member with `static constexpr auto field = &Dst::neuron::member` and carry it in
+//            `weight`).  A stateful synapse with init(synapse&, Int src, Int dst, rng) runs it on
+//            the host over the CSR in order with the connection's PerSynapseInit stream
+//            (synapse_population.h:30-41); its weights are then delivered by the engine's pull path
+//            (bit-exact order).  deliver() that reads the source neuron (DeliverFromTo) and plastic
+//            synapses written as user code are refused at compile time.
+// Arithmetic: user models compile under nvcc (-fmad=false recommended), not under the reference's
+// GCC -ffast-math, so a user model reproduces the reference bit for bit only where both compilers
+// evaluate its expressions the same way; the built-in models always do.
 #pragma once
 
 #include <cstdint>
 #include <cstring>
 #include <initializer_list>
 #include <memory>
+#include <span>
 #include <stdexcept>
 #include <string>
 #include <type_traits>
@@ -31,11 +52,21 @@
 
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
-// Marks a user model's update() / deliver() for the GPU.
+// Marks a user model's update() / deliver() / init() for the GPU (and the host).
 #define SPICE_HD __host__ __device__
 #else
 #define SPICE_HD
 #endif
+
+// The reference's integer names (spice/include/spice/util/stdint.h:5-12), which its models use.
+using Int8   = std::int8_t;
+using Int16  = std::int16_t;
+using Int32  = std::int32_t;
+using Int    = std::int64_t;
+using UInt8  = std::uint8_t;
+using UInt16 = std::uint16_t;
+using UInt32 = std::uint32_t;
+using UInt   = std::uint64_t;
 
 namespace spice {
 
@@ -55,6 +86,18 @@ struct seed_seq {
 	seed_seq(std::initializer_list<uint32_t> il) : seeds(il) {}
 };
 
+// xoroshiro64_128p (random.h:222-234): the engine's streams, on the host (init()) and the GPU.
+struct xoroshiro64_128p {
+	uint64_t s0 = 0, s1 = 0;
+	SPICE_HD uint64_t operator()() {
+		uint64_t const r = s0 + s1;
+		uint64_t const t = s0 ^ s1;
+		s0 = ((s0 << 24) | (s0 >> 40)) ^ t ^ (t << 16);
+		s1 = (t << 37) | (t >> 27);
+		return r;
+	}
+};
+
 // generate_canonical<Real, LeftOpen>(rng) (random.h:236-247) for user models: float from the top
 // 24 bits, double from the top 53 bits (left-open: ((u >> 11) + 1) / 2^53).
 template <class Real, bool LeftOpen = false, class Rng>
@@ -68,7 +111,8 @@ SPICE_HD Real generate_canonical(Rng& rng) {
 }
 }  // namespace util
 
-// ---- models ----
+// ---- the samples' models, built into the engine ----
+namespace models {
 struct poisson {
 	float rate = 20;  // Hz
 	static constexpr int model = SPICE_NEURON_POISSON;
@@ -99,16 +143,28 @@ struct external_input {
 };
 struct fixed_weight {
 	float weight;
+	static constexpr int kind = SPICE_SYNAPSE_FIXED_WEIGHT;
 	std::vector<float> params() const { return {weight, float(SPICE_FIELD_V)}; }
 };
 struct excitatory {
 	float weight;
+	static constexpr int kind = SPICE_SYNAPSE_FIXED_WEIGHT;
 	std::vector<float> params() const { return {weight, float(SPICE_FIELD_GEX)}; }
 };
 struct inhibitory {
 	float weight;
+	static constexpr int kind = SPICE_SYNAPSE_FIXED_WEIGHT;
 	std::vector<float> params() const { return {weight, float(SPICE_FIELD_GIN)}; }
 };
+// A per-synapse weight wmax * canonical<float> drawn at construction (PerSynapseInit), delivered
+// into `field` by the pull path.
+struct weighted {
+	float wmax;
+	int field = SPICE_FIELD_V;
+	static constexpr int kind = SPICE_SYNAPSE_WEIGHTED;
+	std::vector<float> params() const { return {wmax, float(field)}; }
+};
+}  // namespace models
 
 // ---- topologies (spice/include/spice/topology.h:37-58) ----
 class fixed_probability {
@@ -135,54 +191,189 @@ private:
 
 namespace detail {
 template <class T>
-inline constexpr bool is_builtin_model = std::is_same_v<T, poisson> || std::is_same_v<T, lif> ||
-                                         std::is_same_v<T, lif_cond> || std::is_same_v<T, external_input>;
-template <class T, class = void>
-struct has_neuron : std::false_type {};
+inline constexpr bool is_builtin_model =
+    std::is_same_v<T, models::poisson> || std::is_same_v<T, models::lif> || std::is_same_v<T, models::lif_cond> ||
+    std::is_same_v<T, models::external_input>;
 template <class T>
-struct has_neuron<T, std::void_t<typename T::neuron>> : std::true_type {};
-template <class T, class = void>
-struct has_field : std::false_type {};
+inline constexpr bool is_builtin_synapse = std::is_same_v<T, models::fixed_weight> ||
+                                           std::is_same_v<T, models::excitatory> ||
+                                           std::is_same_v<T, models::inhibitory> || std::is_same_v<T, models::weighted>;
 template <class T>
-struct has_field<T, std::void_t<decltype(T::field)>> : std::true_type {};
+concept has_neuron = requires { typename T::neuron; };
+template <class T>
+concept has_synapse = requires { typename T::synapse; };
+template <class T>
+concept has_field = requires { T::field; };
+template <class T>
+concept declares_draws = requires { T::draws_per_update; };
+// the reference's concepts (concepts.h:22-30, 86-104), with this header's stream type
+template <class T>
+concept per_neuron_init = has_neuron<T> && requires(T const t, typename T::neuron& n, Int id, util::xoroshiro64_128p& rng) {
+	t.init(n, id, rng);
+};
+template <class T>
+concept per_population_init = has_neuron<T> && requires(T t, std::span<typename T::neuron> s, util::xoroshiro64_128p& rng) {
+	t.init(s, rng);
+};
+template <class S>
+concept per_synapse_init = has_synapse<S> && requires(S const t, typename S::synapse& syn, Int a, Int b,
+                                                      util::xoroshiro64_128p& rng) { t.init(syn, a, b, rng); };
+template <class S>
+concept plastic_synapse = has_synapse<S> && requires(S const t, typename S::synapse& syn, float dt, bool pre, bool post, Int n) {
+	t.update(syn, dt, pre, post);
+	t.skip(syn, dt, n);
+};
+template <class S, class N>
+concept deliver_to_stateless = requires(S const t, N& n) { t.deliver(n); };
+template <class S, class N>
+concept deliver_to_stateful = has_synapse<S> && requires(S const t, typename S::synapse const& syn, N& n) { t.deliver(syn, n); };
 template <class>
 inline constexpr bool always_false = false;
 
-#if defined(__CUDACC__)
-// xoroshiro128+ (random.h:222-234) positioned in the step's stream.
-struct device_rng {
-	uint64_t s0, s1;
-	__device__ uint64_t operator()() {
-		uint64_t const r = s0 + s1;
-		uint64_t const t = s0 ^ s1;
-		s0 = ((s0 << 24) | (s0 >> 40)) ^ t ^ (t << 16);
-		s1 = (t << 37) | (t >> 27);
-		return r;
-	}
-};
-// Stateful user models get no random stream (the reference's sequential stream has no parallel
-// position for a model that draws a data-dependent number of times); draws return 0.
-struct no_rng {
-	__device__ uint64_t operator()() const { return 0; }
-};
+// The neuron struct of a target model (built-in or user).
+template <class M>
+using neuron_t = typename M::neuron;
 
-// One window of a stateful user population: per neuron, per step, the inputs of the step's slot
-// (the engine's per-group counts replayed as sequential float adds into the group's field, or the
-// atomic-mode field sums), then the user's update(); spikes to the bitmap and the step's list.
+// A built-in target's field index for a byte offset into its neuron struct (lif: V; lif_cond: V, Gex,
+// Gin), or -1.
+template <class M>
+int builtin_field(int offset) {
+	if constexpr (std::is_same_v<M, models::lif>) return offset == 0 ? SPICE_FIELD_V : -1;
+	else if constexpr (std::is_same_v<M, models::lif_cond>)
+		return offset == 0 ? SPICE_FIELD_V : offset == 4 ? SPICE_FIELD_GEX : offset == 8 ? SPICE_FIELD_GIN : -1;
+	else return -1;
+}
+
+// What deliver() does to a target neuron, found by calling it on probe values: it must add a constant
+// (stateless) or one float member of the synapse (stateful; member index `syn_word`) to one float
+// member of the neuron (byte offset `dst_offset`).  Returns false otherwise.
+struct deliver_probe {
+	int dst_offset = -1;
+	int syn_word   = -1;
+	float constant = 0;
+};
+template <class N>
+float word_of(N const& n, int w) {
+	float f;
+	std::memcpy(&f, reinterpret_cast<char const*>(&n) + 4 * w, 4);
+	return f;
+}
+template <class N>
+void set_word(N& n, int w, float f) {
+	std::memcpy(reinterpret_cast<char*>(&n) + 4 * w, &f, 4);
+}
+template <class S, class N, class Deliver>
+bool probe_additive(Deliver&& deliver, deliver_probe& out, float syn_value_of_word, bool stateful) {
+	static_assert(sizeof(N) % 4 == 0, "a target neuron must be a struct of 4-byte members");
+	constexpr int words = (int)(sizeof(N) / 4);
+	N n{};
+	std::memset(static_cast<void*>(&n), 0, sizeof n);
+	deliver(n);
+	int changed = -1;
+	for (int w = 0; w < words; w++)
+		if (word_of(n, w) != 0.0f) {
+			if (changed >= 0) return false;
+			changed = w;
+		}
+	if (changed < 0) return false;
+	float const c = word_of(n, changed);
+	(void)syn_value_of_word;
+	(void)stateful;
+	float const xs[4] = {0.5f, -1.25f, 3.0e-3f, 1000.0f};
+	for (float x : xs) {  // the same member, now from x: x + c, one IEEE addition
+		N m{};
+		std::memset(static_cast<void*>(&m), 0, sizeof m);
+		set_word(m, changed, x);
+		deliver(m);
+		volatile float expect = x;
+		expect                = expect + c;
+		if (word_of(m, changed) != expect) return false;
+		for (int w = 0; w < words; w++)
+			if (w != changed && word_of(m, w) != 0.0f) return false;
+	}
+	out.dst_offset = 4 * changed;
+	out.constant   = c;
+	return true;
+}
+
+#if defined(__CUDACC__)
+// xoroshiro128+ positioned in the step's stream.
+using device_rng = util::xoroshiro64_128p;
+
+// The counter-based stream of a stateful model without declared draws: xoroshiro128+ seeded by
+// SplitMix64-mixing the step's seed with the population and neuron index.
+SPICE_HD inline uint64_t splitmix64(uint64_t x) {
+	x += 0x9E3779B97F4A7C15ull;
+	x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+	x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+	return x ^ (x >> 31);
+}
+__device__ inline device_rng counter_stream(const uint64_t* step_seed, int pop, int64_t i) {
+	uint64_t const a = splitmix64(step_seed[0] ^ splitmix64((uint64_t)i * 2 + 1));
+	uint64_t const b = splitmix64(step_seed[1] ^ splitmix64(((uint64_t)pop << 40) ^ (uint64_t)i));
+	return device_rng{a, b | 1ull};  // never the all-zero state
+}
+
+// The stream position of `draws`-per-neuron model neuron i in step k: the chunk's jump (16 table
+// lookups), then (i mod 32) * draws draws.
+__device__ inline device_rng jumped_stream(spice_user_window const& w, int k, int64_t i) {
+	const uint64_t* tab  = static_cast<const uint64_t*>(w.tables) + (int64_t)k * 16 * 256 * 2;
+	const uint64_t* poly = static_cast<const uint64_t*>(w.chunk_poly) + 2 * (i >> 5);
+	uint64_t const plo = poly[0], phi = poly[1];
+	device_rng rng{0, 0};
+	for (int g = 0; g < 16; g++) {
+		uint64_t const byte = ((g < 8 ? plo : phi) >> (8 * (g & 7))) & 255;
+		rng.s0 ^= tab[2 * (g * 256 + byte)];
+		rng.s1 ^= tab[2 * (g * 256 + byte) + 1];
+	}
+	for (int64_t r = (i & 31) * w.draws; r > 0; r--) rng();
+	return rng;
+}
+
+// One window of a stateful user population: per neuron, per step, the inputs of the step (the
+// engine's per-group counts replayed as sequential float adds, the atomic-mode sums, or the pulled
+// per-synapse weights in the reference's order), then the user's update(); spikes to the bitmap
+// and the step's list.
 template <class Neur>
 __global__ void __launch_bounds__(256) user_update_kernel(const spice_user_window w, const Neur neur) {
-	using N            = typename Neur::neuron;
-	int64_t const i    = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-	bool const valid   = i < w.size;
-	int const lane     = threadIdx.x & 31;
-	N* const st        = static_cast<N*>(w.state);
+	using N          = typename Neur::neuron;
+	int64_t const i  = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	bool const valid = i < w.size;
+	int const lane   = threadIdx.x & 31;
+	N* const st      = static_cast<N*>(w.state);
 	N n{};
 	if (valid) n = st[i];
 	auto field = [&](int f) -> float& {
 		return *reinterpret_cast<float*>(reinterpret_cast<char*>(&n) + w.field_offset[f]);
 	};
-	auto apply = [&](int64_t slot) {
-		if (w.mode == SPICE_MODE_DETERMINISTIC) {
+	auto apply_pulled = [&](int k) {
+		int32_t* const ko  = w.pull_koff + i * (int64_t)(w.pull_nbins + 1);
+		int64_t const base = w.pull_base[i];
+		if (ko[0] >= 0) {
+			for (int f = 0; f < w.pull_F; f++) {
+				float& x = field(w.pull_field[f]);
+				float v  = x;
+				for (int32_t e = ko[k * w.pull_F + f]; e < ko[k * w.pull_F + f + 1]; e++) v = __fadd_rn(v, w.pull_G[base + e]);
+				x = v;
+			}
+			if (w.apply_only)
+				for (int f = 0; f < w.pull_F; f++) ko[f] = ko[w.pull_F];
+		} else {
+			for (int32_t e = 0; e < ko[1]; e++) {
+				uint64_t const a  = w.pull_A[base + e];
+				uint32_t const mf = (uint32_t)(a >> 32);
+				if ((mf >> k) & 1u) {
+					float& x = field(w.pull_field[mf >> 16]);
+					x        = __fadd_rn(x, __uint_as_float((uint32_t)a));
+					if (w.apply_only) w.pull_A[base + e] = a & ~(1ull << 32);
+				}
+			}
+		}
+	};
+	auto apply = [&](int64_t slot, int k) {
+		if (w.pull) {
+			apply_pulled(k);
+		} else if (w.mode == SPICE_MODE_DETERMINISTIC) {
 			uint32_t* const wp = w.cnt + (slot * w.size + i) * w.W;
 			uint32_t x[4] = {0, 0, 0, 0};
 			for (int j = 0; j < w.W && j < 4; j++) x[j] = wp[j];
@@ -212,18 +403,19 @@ __global__ void __launch_bounds__(256) user_update_kernel(const spice_user_windo
 	};
 	if (w.apply_only) {
 		if (valid) {
-			apply(w.slot0);
+			apply(w.slot0, 0);
 			st[i] = n;
 		}
 		return;
 	}
 	int slot = w.slot0, hslot = w.hslot0;
-	no_rng rng;
 	for (int k = 0; k < w.K; k++) {
 		bool spike = false;
 		if (valid) {
-			apply(slot);
-			spike = neur.update(n, w.dts[k], rng);
+			apply(slot, k);
+			const uint64_t* seed = static_cast<const uint64_t*>(w.step_seeds) + 2 * k;
+			device_rng rng       = w.draws > 0 ? jumped_stream(w, k, i) : counter_stream(seed, w.pop, i);
+			spike                = neur.update(n, w.dts[k], rng);
 		}
 		unsigned const mask = __ballot_sync(0xffffffffu, spike);
 		int64_t const word  = i >> 5;
@@ -285,7 +477,7 @@ template <class Neur>
 int user_launch(const spice_user_window* w, void* stream, void* ctx) {
 	Neur const& neur  = *static_cast<const Neur*>(ctx);
 	cudaStream_t const st = static_cast<cudaStream_t>(stream);
-	if constexpr (has_neuron<Neur>::value) {
+	if constexpr (has_neuron<Neur>) {
 		unsigned const blocks = (unsigned)((w->size + 255) / 256);
 		user_update_kernel<Neur><<<blocks, 256, 0, st>>>(*w, neur);
 	} else {
@@ -317,7 +509,7 @@ public:
 		return out;
 	}
 	// neuron_population::get_neurons() (neuron_population.h:139-145), copied from the device.
-	// Only for models with per-neuron state (lif, lif_cond).
+	// Only for models with per-neuron state.
 	template <class M = Neur>
 	std::vector<typename M::neuron> get_neurons() const {
 		std::vector<typename M::neuron> out((size_t)size());
@@ -365,13 +557,27 @@ public:
 			static_assert(std::is_trivially_copyable_v<Neur>, "a user model must be trivially copyable");
 			auto model = std::make_shared<Neur>(neur);
 			int id     = -1;
-			if constexpr (detail::has_neuron<Neur>::value) {
+			if constexpr (detail::has_neuron<Neur>) {
 				using N = typename Neur::neuron;
 				static_assert(std::is_trivially_copyable_v<N> && sizeof(N) % 4 == 0,
 				              "a user neuron must be a trivially copyable struct of 4-byte members");
 				N const init{};
 				detail::check(spice_add_user_population(_net, size, 1, (int)sizeof(N), &init, &detail::user_launch<Neur>,
 				                                        model.get(), &id));
+				if constexpr (detail::declares_draws<Neur>) detail::check(spice_user_draws(_net, id, (int)Neur::draws_per_update));
+				if constexpr (detail::per_neuron_init<Neur> || detail::per_population_init<Neur>) {
+					// stateful_neuron_adapter's init with the population's own stream (neuron_population.h:56-67)
+					util::xoroshiro64_128p rng;
+					detail::check(spice_population_seed(_net, id, &rng.s0, &rng.s1));
+					std::vector<N> ns((size_t)size);
+					if constexpr (detail::per_neuron_init<Neur>) {
+						Int i = 0;
+						for (auto& x : ns) neur.init(x, i++, rng);
+					} else {
+						neur.init(std::span<N>(ns), rng);
+					}
+					detail::check(spice_set_user_state(_net, id, ns.data()));
+				}
 			} else {
 				detail::check(spice_add_user_population(_net, size, 0, 0, nullptr, &detail::user_launch<Neur>, model.get(), &id));
 			}
@@ -403,19 +609,21 @@ public:
 	template <class Syn, class SrcNeur, class DstNeur>
 	void connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target,
 	             fixed_probability const& c, float delay, Syn syn = {}) {
-		auto const prm = params_of(syn, target);
-		int id         = -1;
-		detail::check(spice_connect_fixed_probability(_net, source->id(), target->id(), c.p(), delay,
-		                                              SPICE_SYNAPSE_FIXED_WEIGHT, prm.data(), (int)prm.size(), &id));
+		plan const pl = plan_of<Syn, DstNeur>(syn, target);
+		int id        = -1;
+		detail::check(spice_connect_fixed_probability(_net, source->id(), target->id(), c.p(), delay, pl.kind,
+		                                              pl.params.data(), (int)pl.params.size(), &id));
+		finish<Syn>(syn, id, pl);
 	}
 
 	template <class Syn, class SrcNeur, class DstNeur>
 	void connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target, adj_list const& c,
 	             float delay, Syn syn = {}) {
-		auto const prm = params_of(syn, target);
-		int id         = -1;
+		plan const pl = plan_of<Syn, DstNeur>(syn, target);
+		int id        = -1;
 		detail::check(spice_connect_adj_list(_net, source->id(), target->id(), c.pairs().data(), c.size(), delay,
-		                                     SPICE_SYNAPSE_FIXED_WEIGHT, prm.data(), (int)prm.size(), &id));
+		                                     pl.kind, pl.params.data(), (int)pl.params.size(), &id));
+		finish<Syn>(syn, id, pl);
 	}
 
 	void step() { detail::check(spice_step(_net)); }  // snn.cpp:7-28
@@ -424,21 +632,124 @@ public:
 	spice_net* handle() { return _net; }
 
 private:
-	// Synapse parameters {weight, field}.  Into a user neuron, a synapse adds its `weight` to the
-	// float member it names with `static constexpr auto field = &Model::neuron::member;` (the
-	// member its deliver() adds to); the member is registered as a target field of the population.
-	template <class Syn, class DstNeur>
-	std::vector<float> params_of(Syn const& syn, neuron_population<DstNeur>* target) {
+	// How a synapse type reaches the engine: kind + params, and for a stateful synapse with
+	// PerSynapseInit the float member of its struct whose per-synapse values are the weights.
+	struct plan {
+		int kind = SPICE_SYNAPSE_FIXED_WEIGHT;
+		std::vector<float> params;
+		int weight_word = -1;  // host weights: word of the synapse struct delivered
+	};
+
+	template <class DstNeur>
+	int field_index(neuron_population<DstNeur>* target, int offset) {
 		if constexpr (detail::is_builtin_model<DstNeur>) {
-			return syn.params();
+			int const f = detail::builtin_field<DstNeur>(offset);
+			if (f < 0) throw std::logic_error("the synapse's deliver() targets no float state field of the neuron model");
+			return f;
 		} else {
-			static_assert(detail::has_field<Syn>::value,
-			              "a synapse into a user neuron declares `static constexpr auto field = &Model::neuron::member;`");
-			typename DstNeur::neuron probe{};
-			int const off = (int)(reinterpret_cast<char const*>(&(probe.*Syn::field)) - reinterpret_cast<char const*>(&probe));
-			int fi        = -1;
-			detail::check(spice_user_field(_net, target->id(), off, &fi));
-			return {syn.weight, float(fi)};
+			int fi = -1;
+			detail::check(spice_user_field(_net, target->id(), offset, &fi));
+			return fi;
+		}
+	}
+
+	template <class Syn, class DstNeur>
+	plan plan_of(Syn const& syn, neuron_population<DstNeur>* target) {
+		plan pl;
+		if constexpr (detail::is_builtin_synapse<Syn>) {
+			pl.kind   = Syn::kind;
+			pl.params = syn.params();
+			return pl;
+		} else {
+			using N = detail::neuron_t<DstNeur>;
+			static_assert(!detail::plastic_synapse<Syn>,
+			              "plastic user synapses (update()/skip()) are not supported by this engine: its plastic "
+			              "synapses are the built-in iSTDP and counting models (spice_gb300.h)");
+			if constexpr (detail::has_field<Syn>) {  // the member named by the synapse, its `weight`
+				N probe{};
+				int const off = (int)(reinterpret_cast<char const*>(&(probe.*Syn::field)) - reinterpret_cast<char const*>(&probe));
+				pl.params     = {syn.weight, float(field_index(target, off))};
+				return pl;
+			} else if constexpr (detail::deliver_to_stateless<Syn, N>) {
+				detail::deliver_probe pr;
+				if (!detail::probe_additive<Syn, N>([&](N& n) { syn.deliver(n); }, pr, 0.0f, false))
+					throw std::logic_error("a synapse's deliver() must add one constant to one float member of the target neuron");
+				pl.params = {pr.constant, float(field_index(target, pr.dst_offset))};
+				return pl;
+			} else if constexpr (detail::deliver_to_stateful<Syn, N>) {
+				using S = typename Syn::synapse;
+				static_assert(std::is_trivially_copyable_v<S> && sizeof(S) % 4 == 0,
+				              "a synapse struct must be trivially copyable, of 4-byte members");
+				constexpr int words = (int)(sizeof(S) / 4);
+				// which member of the synapse struct is delivered: probe each word alone
+				int wsel = -1;
+				detail::deliver_probe pr;
+				for (int wd = 0; wd < words && wsel < 0; wd++) {
+					S s{};
+					std::memset(static_cast<void*>(&s), 0, sizeof s);
+					detail::set_word(s, wd, 0.375f);
+					detail::deliver_probe p1;
+					if (detail::probe_additive<Syn, N>([&](N& n) { syn.deliver(s, n); }, p1, 0.375f, true) && p1.constant == 0.375f) {
+						S s2{};
+						std::memset(static_cast<void*>(&s2), 0, sizeof s2);
+						detail::set_word(s2, wd, -2.5f);
+						detail::deliver_probe p2;
+						if (detail::probe_additive<Syn, N>([&](N& n) { syn.deliver(s2, n); }, p2, -2.5f, true) &&
+						    p2.constant == -2.5f && p2.dst_offset == p1.dst_offset) {
+							wsel = wd;
+							pr   = p1;
+						}
+					}
+				}
+				if (wsel < 0)
+					throw std::logic_error("a stateful synapse's deliver() must add one float member of the synapse to one "
+					                       "float member of the target neuron");
+				int const f = field_index(target, pr.dst_offset);
+				if constexpr (detail::per_synapse_init<Syn>) {
+					pl.kind        = SPICE_SYNAPSE_WEIGHTED;
+					pl.params      = {0.0f, float(f), 1.0f};  // host weights, the init seed consumed
+					pl.weight_word = wsel;
+				} else {  // every synapse starts as synapse{}: one weight for the whole connection
+					S const s0{};
+					pl.params = {detail::word_of(s0, wsel), float(f)};
+				}
+				return pl;
+			} else {
+				static_assert(detail::always_false<Syn>,
+				              "deliver() that reads the source neuron (DeliverFromTo) is not supported: the engine "
+				              "delivers a window of spikes at once, when the source neurons have moved on");
+				return pl;
+			}
+		}
+	}
+
+	// A stateful synapse with PerSynapseInit: its init() over the CSR in order, on the host, with the
+	// connection's init stream (synapse_population.h:34-41), and the delivered member as the weights.
+	template <class Syn>
+	void finish(Syn const& syn, int id, plan const& pl) {
+		if constexpr (detail::per_synapse_init<Syn>) {
+			if (pl.weight_word < 0) return;
+			using S = typename Syn::synapse;
+			int64_t src = 0, nsyn = 0;
+			detail::check(spice_conn_size(_net, id, &src, &nsyn));
+			std::vector<int64_t> off((size_t)src + 1);
+			std::vector<int32_t> nb((size_t)std::max<int64_t>(nsyn, 1));
+			detail::check(spice_get_csr(_net, id, off.data(), nb.data()));
+			uint64_t seeds[4];
+			detail::check(spice_connection_seeds(_net, id, seeds));
+			util::xoroshiro64_128p rng{seeds[2], seeds[3]};
+			std::vector<float> w((size_t)std::max<int64_t>(nsyn, 1));
+			for (int64_t s = 0; s < src; s++)
+				for (int64_t e = off[s]; e < off[s + 1]; e++) {
+					S x{};
+					syn.init(x, s, nb[e], rng);
+					w[e] = detail::word_of(x, pl.weight_word);
+				}
+			detail::check(spice_set_synapse_weights(_net, id, w.data()));
+		} else {
+			(void)syn;
+			(void)id;
+			(void)pl;
 		}
 	}
 

@@ -69,9 +69,13 @@ enum {
 	 * -- the reference's StatefulSynapse + PerSynapseInit concepts (concepts.h:60-104): the
 	 * synapse_population ctor seeds the adjacency with seed++, then walks the CSR in order with
 	 * one more stream rng(seed++), calling init(syn, src, dst, rng) (synapse_population.h:30-41).
-	 * Here init draws once: w = params[0] * canonical<float>(rng); params {wmax, field}.  Delivery
-	 * adds w to the target field.  Every population receiving weighted synapses is delivered by
-	 * the pull path (see SPICE_TUNE_PULL), bit-exact with the reference in either mode. */
+	 * Here init draws once: w = params[0] * canonical<float>(rng); params {wmax, field[, source]}.
+	 * source 0 (default): that init; 1: the weights are the host's (spice_set_synapse_weights,
+	 * e.g. a user synapse's own init() run on the host with the seed of spice_connection_seeds),
+	 * the connection still consumes the init seed; 2: host weights, no init seed (a stateful
+	 * synapse without PerSynapseInit).  Delivery adds w to the target field.  Every population
+	 * receiving weighted synapses is delivered by the pull path (see SPICE_TUNE_PULL), bit-exact
+	 * with the reference in either mode. */
 	SPICE_SYNAPSE_WEIGHTED = 3,
 };
 
@@ -270,8 +274,20 @@ const char* spice_last_error(void);
  * that draws once), reached through the step's jump table (tables[k]) and the chunk polynomials
  * chunk_poly[c] = x^(draw_offset + 32 c) mod P (32 neurons per chunk).
  * Spikes: bitmap word (hslot0 + k) mod Hb, bit i; and the unordered list of step k,
- * list[(list_k0 + k) * size ...], reserved with atomicAdd on counts[k * npop + pop]. */
-#define SPICE_USER_ABI_VERSION 1
+ * list[(list_k0 + k) * size ...], reserved with atomicAdd on counts[k * npop + pop].
+ * Version 2 adds the per-step seeds, declared draws of stateful models and pulled inputs:
+ * a stateful model whose update draws a fixed number of times per neuron (spice_user_draws) takes
+ * its draws from the step's stream at position draw_offset + i * draws for neuron i -- the
+ * reference's order, populations in add order and neurons ascending (snn.cpp:12-15,
+ * neuron_population.h:72-77) -- reached through tables[k], chunk_poly[i / 32] = x^(draw_offset +
+ * 32 (i / 32) draws) mod P and (i mod 32) * draws further draws.  A population receiving
+ * per-synapse weights is pulled (pull = 1): before step k, for each bin f < pull_F, the weights
+ * pull_G[pull_base[i] + e], e in [koff[k * pull_F + f], koff[k * pull_F + f + 1]) with koff =
+ * pull_koff + i * (pull_nbins + 1), add in order to field pull_field[f]; when koff[0] < 0 the first
+ * koff[1] entries of pull_A (weight bits | (step mask | bin << 16) << 32) with bit k set add instead.
+ * apply_only on a pulled population applies the bins of step 0 and empties them (koff[f] =
+ * koff[pull_F] for f < pull_F; or clears bit 0 of the masks). */
+#define SPICE_USER_ABI_VERSION 2
 typedef struct spice_user_window {
 	int version;
 	int apply_only;
@@ -295,6 +311,15 @@ typedef struct spice_user_window {
 	float group_weight[4];
 	int field_offset[3];       /* byte offset of field f in the neuron struct */
 	int field_slot[3];         /* atomic mode: index of field f among the F sums (-1: none) */
+	/* version >= 2 */
+	const void* step_seeds;    /* [K] 16-byte seed_seq values seeding the window's step streams */
+	int draws;                 /* stateful: draws per neuron and update (spice_user_draws), else 0 */
+	int pull, pull_F, pull_nbins;
+	int pull_field[3];
+	const int64_t* pull_base;
+	uint64_t* pull_A;
+	const float* pull_G;
+	int32_t* pull_koff;
 } spice_user_window;
 typedef int (*spice_user_update_fn)(const spice_user_window* window, void* stream, void* ctx);
 /* stateful: neuron_bytes > 0 and init_neuron = the initial struct (copied to every neuron); the
@@ -307,6 +332,23 @@ int spice_user_field(spice_net* net, int pop, int byte_offset, int* field_out);
 /* The whole state array of a stateful user population (size * neuron_bytes bytes). */
 int spice_get_user_state(spice_net* net, int pop, void* host_out);
 int spice_set_user_state(spice_net* net, int pop, const void* host_in);
+/* Declares that the update of stateful user population `pop` draws exactly `draws` random numbers
+ * per neuron and step from the step's shared stream (the reference hands every stateful neuron
+ * that stream, snn.cpp:12-15); the engine then positions each neuron in the reference's order.
+ * Without it a stateful user model draws from an independent stream per (population, neuron,
+ * step), seeded by mixing the step's seed with the neuron index: statistically uniform and
+ * independent, not the reference's sequence.  Before the network first steps.  No counterpart in
+ * the reference. */
+int spice_user_draws(spice_net* net, int pop, int draws);
+/* The seed_seq value a stateful population consumed when it was added: the seed of the stream its
+ * init() draws from (stateful_neuron_adapter: rng(seed++), neuron_population.h:56-67). */
+int spice_population_seed(spice_net* net, int pop, uint64_t* lo_out, uint64_t* hi_out);
+/* The seeds a connection consumed: [0, 1] the adjacency's (_graph(c, seed++)), [2, 3] the
+ * PerSynapseInit stream's (rng(seed++), synapse_population.h:30-41) or 0 when it has none. */
+int spice_connection_seeds(spice_net* net, int conn, uint64_t* seeds_out);
+/* Per-synapse weights of a WEIGHTED connection created with params[2] = 1 or 2 (host weights), in
+ * CSR order (spice_get_csr), before the network first steps. */
+int spice_set_synapse_weights(spice_net* net, int conn, const float* weights);
 
 /* ---- Batched networks (no counterpart in the reference) ----
  * Many independent nets stepped together: one launch per kernel kind and window covers the

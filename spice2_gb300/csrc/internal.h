@@ -166,6 +166,8 @@ struct Pop {
 	void* uctx = nullptr;
 	int nfields = 0;
 	int field_offset[3] = {0, 0, 0};
+	int udraws = 0;        // USER stateful: declared draws per neuron and update (0: counter-based stream)
+	u128 seed = {0, 0};    // stateful: the seed its init stream would use (seed_seq value consumed at add)
 };
 
 struct Conn {
@@ -173,6 +175,8 @@ struct Conn {
 	int64_t synapses = 0;
 	bool weighted    = false;     // per-synapse weights (d.wts)
 	float wmax       = 0;
+	int wsource      = 0;         // weighted: 0 drawn by the engine, 1 / 2 set by the host (2: no init seed)
+	u128 gseed       = {0, 0};    // the adjacency's seed
 	u128 wseed       = {0, 0};    // the PerSynapseInit stream's seed
 	uint16_t* nb16    = nullptr;  // owned storage of d.nb16
 	int nb16_tile     = 0;        // tile size d.nb16 was built for
@@ -211,6 +215,7 @@ struct spice_net {
 	cudaEvent_t ev_chunk[2] = {nullptr, nullptr};  // the last chunk stepped from buffer b has ended
 	int chunk_buf = 0;                   // buffer of the next chunk
 	bool has_sources = false;
+	bool user_seeds  = false;            // stateful user populations read the step seeds
 	std::vector<spice_gb300::Pop> pops;
 	std::vector<spice_gb300::Conn> conns;
 	int K  = 1;          // window length used by run

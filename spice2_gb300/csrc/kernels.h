@@ -116,6 +116,7 @@ struct WindowArgs {
 	const PopDev* pops;
 	const float* dts;     // dt of steps t0 .. t0+K-1
 	const u128* tables;   // jump tables of step t0 (then t0+1, ...)
+	const u128* seeds;    // seed_seq values of steps t0 .. t0+K-1 (the step streams' seeds)
 	int64_t tab_net_stride;  // 0: one net
 	int32_t* counts;      // [K][npop] spikes per step and population (window parity buffer)
 	int list_k0;          // first list slot of this window's parity: lists are [2K][size]

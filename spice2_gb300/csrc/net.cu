@@ -260,7 +260,7 @@ extern "C" int spice_add_population(spice_net* n, int model, int64_t size, const
 	}
 	p.stateful = stateful_model(model);
 	if (p.stateful) {
-		seed_next(n);  // stateful_neuron_adapter: rng(seed++) (neuron_population.h:56-60)
+		p.seed = seed_next(n);  // stateful_neuron_adapter: rng(seed++) (neuron_population.h:56-60)
 		TRY(dalloc(n, &d.V, size));
 		TRY(dalloc(n, &d.T, size));
 		if (model == LIF_COND) {
@@ -298,7 +298,7 @@ extern "C" int spice_add_user_population(spice_net* n, int64_t size, int statefu
 	p.ufn      = (void*)fn;
 	p.uctx     = ctx;
 	if (p.stateful) {
-		seed_next(n);  // stateful_neuron_adapter: rng(seed++) (neuron_population.h:56-60)
+		p.seed   = seed_next(n);  // stateful_neuron_adapter: rng(seed++) (neuron_population.h:56-60)
 		d.ubytes = neuron_bytes;
 		char* st = nullptr;
 		TRY(dalloc(n, &st, (size_t)std::max<int64_t>(size, 1) * neuron_bytes, false));
@@ -350,11 +350,11 @@ int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int n
 		if (np < 1 || !params) return fail(SPICE_EINVAL, "count needs params {scale[, field]}");
 		c.tau = 1.0f;
 	} else if (synapse == SPICE_SYNAPSE_WEIGHTED) {
-		if (np < 1 || !params) return fail(SPICE_EINVAL, "weighted needs params {wmax[, field]}");
-		if (n->pops[dst].d.model == USER)
-			return fail(SPICE_EINVAL, "weighted synapses into user-defined populations are not supported");
+		if (np < 1 || !params) return fail(SPICE_EINVAL, "weighted needs params {wmax[, field[, source]]}");
 		c.weighted = true;
 		c.wmax     = params[0];
+		c.wsource  = np > 2 ? (int)params[2] : 0;
+		if (c.wsource < 0 || c.wsource > 2) return fail(SPICE_EINVAL, "weighted source must be 0, 1 or 2");
 	} else {
 		return fail(SPICE_EINVAL, "unknown synapse model");
 	}
@@ -400,9 +400,10 @@ extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, d
 	c.d.dst_size = n->pops[dst].d.size;
 	n->conns.push_back(c);
 	// synapse_population ctor: _graph(c, seed++) (synapse_population.h:30-31)
-	n->gen_pending.push_back({(int)n->conns.size() - 1, seed_next(n), p});
+	n->conns.back().gseed = seed_next(n);
+	n->gen_pending.push_back({(int)n->conns.size() - 1, n->conns.back().gseed, p});
 	// PerSynapseInit: rng(seed++) after the adjacency's (synapse_population.h:34-41)
-	if (c.weighted) n->conns.back().wseed = seed_next(n);
+	if (c.weighted && c.wsource != 2) n->conns.back().wseed = seed_next(n);
 	if (conn_out) *conn_out = (int)n->conns.size() - 1;
 	return SPICE_OK;
 }
@@ -455,8 +456,8 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	c.d.off = doff;
 	c.d.nb  = dnb;
 	n->conns.push_back(c);
-	seed_next(n);  // the synapse_population ctor consumes a seed for every topology
-	if (c.weighted) n->conns.back().wseed = seed_next(n);  // PerSynapseInit (synapse_population.h:34-41)
+	n->conns.back().gseed = seed_next(n);  // the synapse_population ctor consumes a seed for every topology
+	if (c.weighted && c.wsource != 2) n->conns.back().wseed = seed_next(n);  // PerSynapseInit (synapse_population.h:34-41)
 	if (conn_out) *conn_out = (int)n->conns.size() - 1;
 	return SPICE_OK;
 }
@@ -546,8 +547,12 @@ int generate_pending(spice_net* n) {
 // The per-synapse weights of weighted connections (their adjacency generated), drawn from each
 // connection's PerSynapseInit stream in CSR order.
 int init_weights(spice_net* n) {
-	for (auto& c : n->conns) {
+	for (size_t ci = 0; ci < n->conns.size(); ci++) {
+		Conn& c = n->conns[ci];
 		if (!c.weighted || c.d.wts) continue;
+		if (c.wsource != 0)
+			return fail(SPICE_ESTATE, "connection " + std::to_string(ci) +
+			                              ": its per-synapse weights come from the host (spice_set_synapse_weights) and were not set");
 		float* w = nullptr;
 		TRY(dalloc(n, &w, (size_t)std::max<int64_t>(c.synapses, 1), false));
 		CUDA_TRY(init_synapse_weights(n->stream, c.wseed, c.synapses, c.wmax, w));
@@ -754,8 +759,9 @@ int prepare(spice_net* n) {
 				last_of_field[c.d.field] = groups++;
 			}
 		}
-		if (!P.stateful || P.d.model == USER || !has_in) continue;
-		bool const pull = weighted_in || n->pull_all || (n->mode == SPICE_MODE_DETERMINISTIC && groups > kMaxGroups);
+		if (!P.stateful || !has_in) continue;
+		bool const pull = weighted_in || (P.d.model != USER && n->pull_all) ||
+		                  (P.d.model != USER && n->mode == SPICE_MODE_DETERMINISTIC && groups > kMaxGroups);
 		if (!pull) continue;
 		if (plastic_in)
 			return fail(SPICE_EINVAL, "population " + std::to_string(pi) +
@@ -781,15 +787,17 @@ int prepare(spice_net* n) {
 	for (auto& p : n->pops) {
 		p.d.draw_offset = draws;
 		if (p.d.model == POISSON || (p.d.model == USER && !p.stateful)) draws += p.d.size;
+		if (p.d.model == USER && p.stateful) draws += p.d.size * p.udraws;  // declared draws per update
 	}
 	n->total_draws = draws;
 	for (auto& p : n->pops) {
 		PopDev& d = p.d;
 		TRY(dalloc(n, &d.bits, (size_t)n->Hb * std::max(d.nwords, 1)));
 		TRY(dalloc(n, &d.list, (size_t)2 * n->K * std::max<int64_t>(d.size, 1), false));
-		if ((d.model == POISSON || (d.model == USER && !p.stateful)) && d.nwords > 0) {
+		bool const drawing_user = d.model == USER && p.stateful && p.udraws > 0;
+		if ((d.model == POISSON || (d.model == USER && !p.stateful) || drawing_user) && d.nwords > 0) {
 			std::vector<u128> polys(d.nwords);
-			u128 const step = gf2_xpow(kPoissonChunk);
+			u128 const step = gf2_xpow((uint64_t)kPoissonChunk * (drawing_user ? p.udraws : 1));
 			polys[0]        = gf2_xpow((uint64_t)d.draw_offset);
 			for (int c = 1; c < d.nwords; c++) polys[c] = gf2_mulmod(polys[c - 1], step);
 			u128* dp = nullptr;
@@ -973,8 +981,10 @@ int prepare(spice_net* n) {
 	for (auto& p : n->pops) maxN = std::max(maxN, p.d.size);
 	TRY(dalloc(n, &n->d_tmp, maxN, false));
 	TRY(dalloc(n, &n->d_tmp_n, 1));
-	for (auto& p : n->pops)
+	for (auto& p : n->pops) {
 		n->has_sources |= p.d.model == POISSON || p.d.model == EXTERNAL || (p.d.model == USER && !p.stateful);
+		n->user_seeds |= p.d.model == USER && p.stateful;  // their counter-based streams read the step seeds
+	}
 	CUDA_TRY(cudaStreamCreateWithFlags(&n->stream_src, cudaStreamNonBlocking));
 	CUDA_TRY(cudaEventCreateWithFlags(&n->ev_tab, cudaEventDisableTiming));
 	for (int q = 0; q < 2; q++) {
@@ -1033,6 +1043,16 @@ spice_user_window user_window(spice_net* n, int pi, WindowArgs const& wa, int64_
 		w.field_offset[f] = P.field_offset[f];
 		w.field_slot[f]   = d.field_slot[f];
 	}
+	w.step_seeds = wa.seeds;
+	w.draws      = P.stateful ? P.udraws : 0;
+	w.pull       = d.pull;
+	w.pull_F     = d.pull_F;
+	w.pull_nbins = d.pull_nbins;
+	for (int f = 0; f < 3; f++) w.pull_field[f] = d.pull_field[f];
+	w.pull_base = d.pull_base;
+	w.pull_A    = d.pull_A;
+	w.pull_G    = d.pull_G;
+	w.pull_koff = d.pull_koff;
 	return w;
 }
 
@@ -1077,8 +1097,10 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			h_seeds[j] = seed_next(n);  // xoroshiro64_128p rng(_seed++) (snn.cpp:12)
 		}
 		CUDA_TRY(cudaMemcpyAsync(d_dt, h_dt, sizeof(float) * chunk, cudaMemcpyHostToDevice, n->stream));
-		if (n->total_draws > 0) {
+		if (n->total_draws > 0 || n->user_seeds) {
 			CUDA_TRY(cudaMemcpyAsync(d_seeds, h_seeds, sizeof(u128) * chunk, cudaMemcpyHostToDevice, n->stream));
+		}
+		if (n->total_draws > 0) {
 			CUDA_TRY(launch_jump_tables(n->stream, d_seeds, chunk, d_tables));
 			n->launches++;
 		}
@@ -1101,6 +1123,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			wa.pops    = n->d_pops;
 			wa.dts     = d_dt + j;
 			wa.tables  = d_tables ? d_tables + j * kJumpTable : nullptr;
+			wa.seeds   = d_seeds + j;
 			wa.counts  = n->d_counts + (size_t)q * n->K * np;
 			wa.list_k0 = q * n->K;
 			wa.variant = n->neuron_variant;
@@ -1322,7 +1345,8 @@ int flush_pending(spice_net* n) {
 		if (n->pops[i].stateful && n->pops[i].d.model != USER && !n->pops[i].d.pull) st.push_back(i);
 		user |= n->pops[i].stateful && n->pops[i].d.model == USER;
 	}
-	for (int i : n->pull_pops) {  // the pulled inputs of the next step
+	for (int i : n->pull_pops) {  // the pulled inputs of the next step (user models: their callback)
+		if (n->pops[i].d.model == USER) continue;
 		CUDA_TRY(launch_pull_apply_first(n->stream, n->pops[i].d));
 		n->launches++;
 	}
@@ -1752,6 +1776,52 @@ extern "C" int spice_selftest_skip_rounding(int64_t count, uint64_t seed, int64_
 	*mismatches = (int64_t)h[0];
 	if (first_a) *first_a = (uint32_t)h[1];
 	if (first_f) memcpy(first_f, &h[2], sizeof(double));
+	return SPICE_OK;
+}
+
+extern "C" int spice_user_draws(spice_net* n, int pop, int draws) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (pop < 0 || pop >= (int)n->pops.size() || n->pops[pop].d.model != USER || !n->pops[pop].stateful)
+		return fail(SPICE_EINVAL, "not a stateful user population");
+	if (draws < 0 || draws > 1024) return fail(SPICE_EINVAL, "draws per update must be in [0, 1024]");
+	if (n->prepared) return fail(SPICE_ESTATE, "draws must be declared before the network first steps");
+	n->pops[pop].udraws = draws;
+	return SPICE_OK;
+}
+
+extern "C" int spice_population_seed(spice_net* n, int pop, uint64_t* lo, uint64_t* hi) {
+	if (!n || !lo || !hi) return fail(SPICE_EINVAL, "NULL argument");
+	if (pop < 0 || pop >= (int)n->pops.size()) return fail(SPICE_EINVAL, "population id out of range");
+	if (!n->pops[pop].stateful) return fail(SPICE_EINVAL, "a stateless population consumes no seed");
+	*lo = n->pops[pop].seed.lo;
+	*hi = n->pops[pop].seed.hi;
+	return SPICE_OK;
+}
+
+extern "C" int spice_connection_seeds(spice_net* n, int conn, uint64_t* out) {
+	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	Conn const& c = n->conns[conn];
+	out[0] = c.gseed.lo;
+	out[1] = c.gseed.hi;
+	out[2] = c.wseed.lo;
+	out[3] = c.wseed.hi;
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_synapse_weights(spice_net* n, int conn, const float* w) {
+	if (!n || !w) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	Conn& c = n->conns[conn];
+	if (!c.weighted || c.wsource == 0) return fail(SPICE_EINVAL, "not a weighted connection with host weights");
+	if (n->prepared) return fail(SPICE_ESTATE, "weights must be set before the network first steps");
+	TRY(generate_pending(n));
+	if (!c.d.wts) {
+		float* d = nullptr;
+		TRY(dalloc(n, &d, (size_t)std::max<int64_t>(c.synapses, 1), false));
+		c.d.wts = d;
+	}
+	if (c.synapses > 0) CUDA_TRY(cudaMemcpy((void*)c.d.wts, w, sizeof(float) * c.synapses, cudaMemcpyHostToDevice));
 	return SPICE_OK;
 }
 

@@ -8,6 +8,7 @@
 #include "spice/snn.h"
 
 using namespace spice;
+using namespace spice::models;  // the samples' models, built into the engine
 
 int main(int argc, char** argv) {
 	int const N        = argc > 1 ? atoi(argv[1]) : 20000;

@@ -13,6 +13,7 @@ from conftest import GOLDEN, ROOT
 HEADER_USE = r"""
 #include "spice/snn.h"
 using namespace spice;
+using namespace spice::models;
 int main() {
 	snn net(1e-4f, 8e-4f, {1337});
 	auto P = net.add_population<poisson>(10);

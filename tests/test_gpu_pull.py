@@ -179,7 +179,7 @@ def test_pull_ungrouped_bins(engine, oracle_lib):
             "conns": [("w", 0, 1, 0.2, 16e-4, 1e-4, 0), ("f", 1, 1, 0.1, 16e-4, 0.001, 0)]}
     net, pops, _ = _weighted_net(sp, o, spec=spec)
     ref, rpops, _ = o.weighted_net(spec)
-    raster = net.run_record(200)
+    raster = net.run_record(200, capacity=200 * 700)
     for t, row in enumerate(raster):
         ref.step()
         for k in range(2):
