@@ -31,13 +31,19 @@
 //            `weight`).  A stateful synapse with init(synapse&, Int src, Int dst, rng) runs it on
 //            the host over the CSR in order with the connection's PerSynapseInit stream
 //            (synapse_population.h:30-41); its weights are then delivered by the engine's pull path
-//            (bit-exact order).  deliver() that reads the source neuron (DeliverFromTo) and plastic
-//            synapses written as user code are refused at compile time.
+//            (bit-exact order).  A plastic synapse (update(synapse&, dt, pre, post) and
+//            skip(synapse&, dt, Int n), concepts.h:86-92) runs the reference's lazy catch-up
+//            (synapse_population.h:88-139) in kernels instantiated here over its type; its deliver()
+//            adds one float member of the synapse to the target (connecting one switches the net to
+//            atomic mode: per-step sums of per-synapse weights depend on the order).  deliver() that reads the source neuron
+//            (DeliverFromTo) is refused at compile time.
 // Arithmetic: user models compile under nvcc (-fmad=false recommended), not under the reference's
 // GCC -ffast-math, so a user model reproduces the reference bit for bit only where both compilers
 // evaluate its expressions the same way; the built-in models always do.
 #pragma once
 
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <initializer_list>
@@ -49,6 +55,12 @@
 #include <vector>
 
 #include "spice_gb300.h"
+
+// The reference's checks (spice/include/spice/util/assert.h): a failed condition throws
+// std::logic_error("Assertion failed (file:line): cond") (spice/src/util/assert.cpp:8-15).
+#define SPICE_ASSERT(cond) ((cond) ? (void)0 : ::spice::detail::assert_failed(__FILE__, __LINE__, #cond))
+#define SPICE_PRE(cond) SPICE_ASSERT(cond)
+#define SPICE_INV(cond) SPICE_ASSERT(cond)
 
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
@@ -71,6 +83,9 @@ using UInt   = std::uint64_t;
 namespace spice {
 
 namespace detail {
+[[noreturn]] inline void assert_failed(char const* file, int line, char const* cond) {
+	throw std::logic_error(std::string("Assertion failed (") + file + ":" + std::to_string(line) + "): " + cond);
+}
 inline void check(int rc) {
 	if (rc == SPICE_OK) return;
 	std::string const msg = spice_last_error();
@@ -97,6 +112,25 @@ struct xoroshiro64_128p {
 		return r;
 	}
 };
+
+// range(n) / range(first, last): the integers of [first, last) to iterate over (util/range.h).
+struct int_range {
+	struct iterator {
+		Int i;
+		constexpr Int operator*() const { return i; }
+		constexpr iterator& operator++() {
+			++i;
+			return *this;
+		}
+		constexpr bool operator!=(iterator const& o) const { return i != o.i; }
+	};
+	Int first, last;
+	constexpr iterator begin() const { return {first}; }
+	constexpr iterator end() const { return {last}; }
+	constexpr Int size() const { return last - first; }
+};
+constexpr int_range range(Int first, Int last) { return {first, last > first ? last : first}; }
+constexpr int_range range(Int n) { return range(0, n); }
 
 // generate_canonical<Real, LeftOpen>(rng) (random.h:236-247) for user models: float from the top
 // 24 bits, double from the top 53 bits (left-open: ((u >> 11) + 1) / 2^53).
@@ -253,9 +287,9 @@ struct deliver_probe {
 	float constant = 0;
 };
 template <class N>
-float word_of(N const& n, int w) {
+SPICE_HD float word_of(N const& n, int w) {
 	float f;
-	std::memcpy(&f, reinterpret_cast<char const*>(&n) + 4 * w, 4);
+	memcpy(&f, reinterpret_cast<char const*>(&n) + 4 * w, 4);
 	return f;
 }
 template <class N>
@@ -409,6 +443,7 @@ __global__ void __launch_bounds__(256) user_update_kernel(const spice_user_windo
 		return;
 	}
 	int slot = w.slot0, hslot = w.hslot0;
+	uint64_t h = (valid && w.hist) ? w.hist[i] : 0ull;
 	for (int k = 0; k < w.K; k++) {
 		bool spike = false;
 		if (valid) {
@@ -417,6 +452,7 @@ __global__ void __launch_bounds__(256) user_update_kernel(const spice_user_windo
 			device_rng rng       = w.draws > 0 ? jumped_stream(w, k, i) : counter_stream(seed, w.pop, i);
 			spike                = neur.update(n, w.dts[k], rng);
 		}
+		h = (h << 1) | (spike ? 1ull : 0ull);  // a plastic synapses' target keeps 64 steps (neuron_population.h:126-132)
 		unsigned const mask = __ballot_sync(0xffffffffu, spike);
 		int64_t const word  = i >> 5;
 		if (lane == 0 && word < w.nwords) w.bits[(int64_t)hslot * w.nwords + word] = mask;
@@ -430,7 +466,10 @@ __global__ void __launch_bounds__(256) user_update_kernel(const spice_user_windo
 		slot  = slot + 1 == (int)w.D ? 0 : slot + 1;
 		hslot = hslot + 1 == w.Hb ? 0 : hslot + 1;
 	}
-	if (valid) st[i] = n;
+	if (valid) {
+		st[i] = n;
+		if (w.hist) w.hist[i] = h;
+	}
 }
 
 // One step (blockIdx.y) of a stateless user population: thread c owns neurons [32c, 32c + 32),
@@ -473,6 +512,103 @@ __global__ void __launch_bounds__(256) user_source_kernel(const spice_user_windo
 	for (unsigned m = mask; m; m &= m - 1) *out++ = (int32_t)(32 * c + (__ffs(m) - 1));
 }
 
+// The catch-up of one plastic synapse to step `time` (synapse_population.h:88-116): the pending pre
+// update of its source's last delivery, then every post spike of the target's 64-step history, with
+// skip() over the quiet steps.  ~0 >> prefix with prefix up to 64 is computed as x86-64 does
+// (shift mod 64).
+template <class Syn, class S>
+__device__ void user_catch_up(Syn const& syn, S& s, float dt, int64_t time, uint64_t ages, uint64_t hist) {
+	int const pre     = (int)(ages >> 63);
+	int64_t const age = (int64_t)(ages & ~(1ull << 63));
+	if (!(time >= age)) return;
+	int64_t const prefix = 63 + pre - time + age;
+	uint64_t const mask  = ~0ull >> (prefix & 63);
+	if (pre) syn.update(s, dt, true, (hist & (1ull << ((time - age) & 63))) != 0);
+	hist &= mask;
+	int64_t p = prefix;
+	while (hist) {
+		int const lz = __clzll((long long)hist);
+		syn.skip(s, dt, (Int)(lz - p));
+		syn.update(s, dt, false, true);
+		hist ^= 1ull << (63 - lz);
+		p = lz + 1;
+	}
+	syn.skip(s, dt, (Int)(64 - p));
+}
+
+// Every 64 steps: every synapse catches up, a warp per source, then the source's age is time + 1.
+template <class Syn>
+__global__ void __launch_bounds__(256) user_plastic_update_all(const spice_user_plastic_call c, const Syn syn) {
+	using S = typename Syn::synapse;
+	int const lane    = threadIdx.x & 31;
+	int64_t const src = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
+	if (src >= c.src_size) return;
+	S* const st         = static_cast<S*>(c.state);
+	uint64_t const ages = c.ages[src];
+	for (int64_t e = c.off[src] + lane; e < c.off[src + 1]; e += 32) {
+		S x = st[e];
+		user_catch_up(syn, x, c.dt, c.time, ages, c.dst_hist[c.nb[e]]);
+		st[e] = x;
+	}
+	__syncwarp();
+	if (lane == 0) c.ages[src] = (uint64_t)(c.time + 1);
+}
+
+// Delivery of a step's spikes: CTA (w, y) takes 256-synapse chunks y, y + gridDim.y, ... of the row of
+// every spiking source of bitmap word w: catch up, add the weight member into the input ring; the
+// row's last chunk to finish sets the source's age (time + 1, pending pre update).
+template <class Syn>
+__global__ void __launch_bounds__(256) user_plastic_deliver(const spice_user_plastic_call c, const Syn syn) {
+	using S = typename Syn::synapse;
+	S* const st   = static_cast<S*>(c.state);
+	int const w   = blockIdx.x;
+	uint32_t bits = c.src_bits[(int64_t)c.hslot * c.src_nwords + w];
+	unsigned long long ev = 0;
+	while (bits) {
+		int const r = __ffs(bits) - 1;
+		bits &= bits - 1;
+		int64_t const src     = 32 * (int64_t)w + r;
+		int64_t const e0      = c.off[src], e1 = c.off[src + 1];
+		int64_t const nchunks = (e1 - e0 + 255) / 256;
+		if (blockIdx.y == 0 && threadIdx.x == 0) ev += (unsigned long long)(e1 - e0);
+		for (int64_t ch = blockIdx.y; ch < nchunks; ch += gridDim.y) {
+			uint64_t const ages = c.ages[src];
+			int64_t const e     = e0 + ch * 256 + threadIdx.x;
+			if (e < e1) {
+				S x             = st[e];
+				int32_t const j = c.nb[e];
+				user_catch_up(syn, x, c.dt, c.time, ages, c.dst_hist[j]);
+				st[e] = x;
+				if (c.deliver)
+					atomicAdd(c.dst_acc + (c.slot * c.dst_size + j) * c.F + c.fslot, word_of(x, c.weight_word));
+			}
+			__syncthreads();  // every thread of this chunk has read the source's age
+			if (threadIdx.x == 0) {
+				__threadfence();
+				if (atomicAdd(c.chunks_done + src, 1u) == (uint32_t)(nchunks - 1)) {
+					c.ages[src]        = (uint64_t)(c.time + 1) | (1ull << 63);
+					c.chunks_done[src] = 0;
+				}
+			}
+			__syncthreads();
+		}
+	}
+	if (threadIdx.x == 0 && ev) atomicAdd(c.events, ev);
+}
+
+template <class Syn>
+int user_plastic_launch(const spice_user_plastic_call* c, void* stream, void* ctx) {
+	Syn const& syn         = *static_cast<const Syn*>(ctx);
+	cudaStream_t const st  = static_cast<cudaStream_t>(stream);
+	if (c->what == 0) {
+		if (c->src_size > 0) user_plastic_update_all<Syn><<<(unsigned)((c->src_size + 7) / 8), 256, 0, st>>>(*c, syn);
+	} else if (c->src_nwords > 0) {
+		dim3 const grid((unsigned)c->src_nwords, (unsigned)(c->max_row > 0 ? (c->max_row + 255) / 256 < 65535 ? (c->max_row + 255) / 256 : 65535 : 1));
+		user_plastic_deliver<Syn><<<grid, 256, 0, st>>>(*c, syn);
+	}
+	return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
 template <class Neur>
 int user_launch(const spice_user_window* w, void* stream, void* ctx) {
 	Neur const& neur  = *static_cast<const Neur*>(ctx);
@@ -488,6 +624,41 @@ int user_launch(const spice_user_window* w, void* stream, void* ctx) {
 }
 #endif
 }  // namespace detail
+
+// CheckNeuron<T>() / CheckSynapse<T>() (concepts.h:163-228): compile-time checks of a model's
+// methods, true when they pass (static_assert with an explanation otherwise).
+namespace detail {
+struct any_arg {  // converts to any argument type (unevaluated)
+	template <class U>
+	operator U&() const;
+};
+template <class T>
+concept any_update = requires(T const t, any_arg a) { t.update(a, a); } || requires(T const t, any_arg a) { t.update(a, a, a); };
+template <class T>
+concept any_deliver = requires(T const t, any_arg a) { t.deliver(a); } || requires(T const t, any_arg a) { t.deliver(a, a); } ||
+                      requires(T const t, any_arg a) { t.deliver(a, a, a); };
+template <class T>
+concept any_syn_update = requires(T const t, any_arg a) { t.update(a, a, a, a); };
+template <class T>
+concept any_syn_skip = requires(T const t, any_arg a) { t.skip(a, a, a); };
+}  // namespace detail
+
+template <class T>
+constexpr bool CheckNeuron() {
+	static_assert(std::is_default_constructible_v<T>, "a neuron model must be default-constructible");
+	static_assert(detail::any_update<T>, "a neuron model defines update(dt, rng) or update(neuron&, dt, rng)");
+	return true;
+}
+
+template <class T>
+constexpr bool CheckSynapse() {
+	static_assert(std::is_default_constructible_v<T>, "a synapse model must be default-constructible");
+	static_assert(detail::any_deliver<T>, "a synapse model defines deliver()");
+	static_assert(detail::any_syn_update<T> == detail::any_syn_skip<T>,
+	              "a plastic synapse defines both update(synapse&, dt, pre, post) and skip(synapse&, dt, n)");
+	static_assert(!detail::any_syn_update<T> || detail::has_synapse<T>, "a plastic synapse needs a nested `synapse` struct");
+	return true;
+}
 
 class snn;
 
@@ -606,27 +777,42 @@ public:
 		}
 	}
 
+	// Returns the connection's id (the reference returns nothing; callers may ignore it).
 	template <class Syn, class SrcNeur, class DstNeur>
-	void connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target,
-	             fixed_probability const& c, float delay, Syn syn = {}) {
+	int connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target,
+	            fixed_probability const& c, float delay, Syn syn = {}) {
 		plan const pl = plan_of<Syn, DstNeur>(syn, target);
 		int id        = -1;
 		detail::check(spice_connect_fixed_probability(_net, source->id(), target->id(), c.p(), delay, pl.kind,
 		                                              pl.params.data(), (int)pl.params.size(), &id));
 		finish<Syn>(syn, id, pl);
+		return id;
 	}
 
 	template <class Syn, class SrcNeur, class DstNeur>
-	void connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target, adj_list const& c,
-	             float delay, Syn syn = {}) {
+	int connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target, adj_list const& c,
+	            float delay, Syn syn = {}) {
 		plan const pl = plan_of<Syn, DstNeur>(syn, target);
 		int id        = -1;
 		detail::check(spice_connect_adj_list(_net, source->id(), target->id(), c.pairs().data(), c.size(), delay,
 		                                     pl.kind, pl.params.data(), (int)pl.params.size(), &id));
 		finish<Syn>(syn, id, pl);
+		return id;
 	}
 
 	void step() { detail::check(spice_step(_net)); }  // snn.cpp:7-28
+	// The per-synapse state of a plastic user connection, CSR order: each synapse as of its last
+	// catch-up (its source's last delivery or the last multiple of 64 steps), as the reference's
+	// synapse_population holds it.
+	template <class Syn>
+	std::vector<typename Syn::synapse> get_synapses(int conn) {
+		int64_t src = 0, n = 0;
+		detail::check(spice_conn_size(_net, conn, &src, &n));
+		std::vector<typename Syn::synapse> out((size_t)std::max<int64_t>(n, 1));
+		detail::check(spice_get_user_synapse_state(_net, conn, out.data()));
+		out.resize((size_t)n);
+		return out;
+	}
 	void run(int64_t steps) { detail::check(spice_run(_net, steps)); }
 	void set_mode(int mode) { detail::check(spice_set_mode(_net, mode)); }
 	spice_net* handle() { return _net; }
@@ -662,9 +848,6 @@ private:
 			return pl;
 		} else {
 			using N = detail::neuron_t<DstNeur>;
-			static_assert(!detail::plastic_synapse<Syn>,
-			              "plastic user synapses (update()/skip()) are not supported by this engine: its plastic "
-			              "synapses are the built-in iSTDP and counting models (spice_gb300.h)");
 			if constexpr (detail::has_field<Syn>) {  // the member named by the synapse, its `weight`
 				N probe{};
 				int const off = (int)(reinterpret_cast<char const*>(&(probe.*Syn::field)) - reinterpret_cast<char const*>(&probe));
@@ -705,7 +888,11 @@ private:
 					throw std::logic_error("a stateful synapse's deliver() must add one float member of the synapse to one "
 					                       "float member of the target neuron");
 				int const f = field_index(target, pr.dst_offset);
-				if constexpr (detail::per_synapse_init<Syn>) {
+				if constexpr (detail::plastic_synapse<Syn>) {
+					pl.kind        = SPICE_SYNAPSE_USER_PLASTIC;
+					pl.params      = {float(f), float(sizeof(S)), float(wsel), detail::per_synapse_init<Syn> ? 1.0f : 0.0f};
+					pl.weight_word = wsel;
+				} else if constexpr (detail::per_synapse_init<Syn>) {
 					pl.kind        = SPICE_SYNAPSE_WEIGHTED;
 					pl.params      = {0.0f, float(f), 1.0f};  // host weights, the init seed consumed
 					pl.weight_word = wsel;
@@ -727,7 +914,34 @@ private:
 	// connection's init stream (synapse_population.h:34-41), and the delivered member as the weights.
 	template <class Syn>
 	void finish(Syn const& syn, int id, plan const& pl) {
-		if constexpr (detail::per_synapse_init<Syn>) {
+		if constexpr (detail::plastic_synapse<Syn>) {
+#if defined(__CUDACC__)
+			using S = typename Syn::synapse;
+			static_assert(std::is_trivially_copyable_v<Syn>, "a user synapse model must be trivially copyable");
+			auto model = std::make_shared<Syn>(syn);
+			S const init{};
+			detail::check(spice_user_plastic(_net, id, &detail::user_plastic_launch<Syn>, model.get(), &init));
+			// per-synapse weights that change over time have no fixed summation order: atomic mode
+			detail::check(spice_set_mode(_net, SPICE_MODE_ATOMIC));
+			_models.push_back(model);
+			if constexpr (detail::per_synapse_init<Syn>) {  // the synapses' init() on the host, CSR order
+				int64_t src = 0, nsyn = 0;
+				detail::check(spice_conn_size(_net, id, &src, &nsyn));
+				std::vector<int64_t> off((size_t)src + 1);
+				std::vector<int32_t> nb((size_t)std::max<int64_t>(nsyn, 1));
+				detail::check(spice_get_csr(_net, id, off.data(), nb.data()));
+				uint64_t seeds[4];
+				detail::check(spice_connection_seeds(_net, id, seeds));
+				util::xoroshiro64_128p rng{seeds[2], seeds[3]};
+				std::vector<S> st((size_t)std::max<int64_t>(nsyn, 1));
+				for (int64_t s = 0; s < src; s++)
+					for (int64_t e = off[s]; e < off[s + 1]; e++) syn.init(st[e], s, nb[e], rng);
+				detail::check(spice_set_user_synapse_state(_net, id, st.data()));
+			}
+#else
+			static_assert(detail::always_false<Syn>, "plastic user synapses run as GPU kernels: compile with nvcc");
+#endif
+		} else if constexpr (detail::per_synapse_init<Syn>) {
 			if (pl.weight_word < 0) return;
 			using S = typename Syn::synapse;
 			int64_t src = 0, nsyn = 0;

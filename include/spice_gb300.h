@@ -77,6 +77,15 @@ enum {
 	 * receiving weighted synapses is delivered by the pull path (see SPICE_TUNE_PULL), bit-exact
 	 * with the reference in either mode. */
 	SPICE_SYNAPSE_WEIGHTED = 3,
+	/* USER_PLASTIC: a plastic synapse written as user code (the reference's PlasticSynapse
+	 * concept, concepts.h:86-92): per-synapse state is an array of synapse_bytes-byte structs in
+	 * CSR order, brought up to date lazily like the built-in plastic synapses; its update()/skip()
+	 * run in kernels of the user's translation unit (include/spice/snn.h) that the engine calls
+	 * through spice_user_plastic.  params {field, synapse_bytes, weight_word[, init]}: delivery adds
+	 * the float at 4-byte word weight_word of a synapse's state to the target field (atomic mode);
+	 * init = 1 when the synapse has a PerSynapseInit init() (the connection then consumes that
+	 * stream's seed, synapse_population.h:34-41, and the host sets the initial state). */
+	SPICE_SYNAPSE_USER_PLASTIC = 4,
 };
 
 /* Delivery modes. */
@@ -150,9 +159,9 @@ enum {
 	                                   the source populations, then the delivery, each launched
 	                                   as the programmatic dependent of the previous kernel;
 	                                   0: sources on a second stream joined by events         */
-	SPICE_TUNE_SOURCE_STEPS    = 9, /* consecutive steps each Poisson source CTA draws; 0 (default):
-	                                   the fewest that keep the window's grid within one wave of
-	                                   resident CTAs                                          */
+	SPICE_TUNE_SOURCE_STEPS    = 9, /* consecutive steps each Poisson source CTA draws (default 1);
+	                                   0: the fewest that keep the window's grid within one wave
+	                                   of resident CTAs                                       */
 	SPICE_TUNE_PULL            = 8, /* 1: deliver into every stateful built-in population with
 	                                   inputs by the pull path, set before the network first
 	                                   steps.  The pull path gathers each target's inputs from
@@ -320,6 +329,8 @@ typedef struct spice_user_window {
 	uint64_t* pull_A;
 	const float* pull_G;
 	int32_t* pull_koff;
+	uint64_t* hist;            /* target of plastic synapses: per neuron, bit j = spiked j steps ago;
+	                              shift in every step's spike bit (neuron_population.h:126-132) */
 } spice_user_window;
 typedef int (*spice_user_update_fn)(const spice_user_window* window, void* stream, void* ctx);
 /* stateful: neuron_bytes > 0 and init_neuron = the initial struct (copied to every neuron); the
@@ -349,6 +360,50 @@ int spice_connection_seeds(spice_net* net, int conn, uint64_t* seeds_out);
 /* Per-synapse weights of a WEIGHTED connection created with params[2] = 1 or 2 (host weights), in
  * CSR order (spice_get_csr), before the network first steps. */
 int spice_set_synapse_weights(spice_net* net, int conn, const float* weights);
+
+/* ---- User plastic synapses (SPICE_SYNAPSE_USER_PLASTIC) ----
+ * The engine keeps the per-synapse state, the per-source ages (bit 63: pending pre update, low
+ * bits: step + 1) and the target's 64-step spike history, and calls `fn` on its stream:
+ *   what = 0 every 64 steps (snn.cpp:17-19): every synapse catches up to `time`, then each
+ *            source's age becomes time + 1 (synapse_population.h:68-72);
+ *   what = 1 each step (snn.cpp:21-25): the spiking sources of bitmap slot `hslot` catch up their
+ *            synapses to `time`, deliver (when `deliver`) the state's word weight_word into
+ *            dst_acc[(slot * dst_size + target) * F + fslot], add their row lengths to *events and
+ *            set their age to (time + 1) | bit 63.
+ * The catch-up of one synapse is synapse_population.h:88-116.  chunks_done (per source, zero) is
+ * scratch for kernels that split a row over several CTAs. */
+#define SPICE_USER_PLASTIC_ABI_VERSION 1
+typedef struct spice_user_plastic_call {
+	int version, what;
+	int64_t time;
+	float dt;
+	int hslot;
+	int64_t slot;
+	int deliver;
+	int64_t src_size, dst_size;
+	const int64_t* off;
+	const int32_t* nb;
+	void* state;
+	int synapse_bytes, weight_word;
+	uint64_t* ages;
+	uint32_t* chunks_done;
+	int64_t max_row;
+	const uint64_t* dst_hist;
+	const uint32_t* src_bits;
+	int src_nwords;
+	float* dst_acc;
+	int F, fslot;
+	unsigned long long* events;
+} spice_user_plastic_call;
+typedef int (*spice_user_plastic_fn)(const spice_user_plastic_call* call, void* stream, void* ctx);
+/* Registers the kernels of USER_PLASTIC connection `conn` and the initial state of every synapse
+ * (synapse_bytes bytes), before the network first steps. */
+int spice_user_plastic(spice_net* net, int conn, spice_user_plastic_fn fn, void* ctx, const void* init_synapse);
+/* The whole per-synapse state array of a USER_PLASTIC connection, CSR order: set before the network
+ * first steps (a PerSynapseInit run on the host), read at any time (each synapse as of its last
+ * catch-up, like the reference's synapse_population). */
+int spice_set_user_synapse_state(spice_net* net, int conn, const void* host_in);
+int spice_get_user_synapse_state(spice_net* net, int conn, void* host_out);
 
 /* ---- Batched networks (no counterpart in the reference) ----
  * Many independent nets stepped together: one launch per kernel kind and window covers the

@@ -368,6 +368,15 @@ def weighted_net_spec(steps: int, spec=WEIGHTED_NET) -> list[str]:
     return lines
 
 
+def brunel_plus_spec(seed: int, steps: int, N: int = 20000) -> list[str]:
+    """samples/brunel+.cpp (Brunel at p = 0.1 with the STDP synapse on E->E) as a ref_driver spec."""
+    d = 15e-4
+    we, wi = float(np.float32(2.0 / N)), float(np.float32(-10.0 / N))
+    return [f"{1e-4!r} {d!r} {seed} {steps} 0", f"pop poisson {N // 2} 20", f"pop lif {N * 4 // 10}",
+            f"pop lif {N // 10}", f"conn 0 1 0.1 {d!r} {we!r}", f"conn 0 2 0.1 {d!r} {we!r}", f"stdp 1 0.1 {d!r}",
+            f"conn 1 2 0.1 {d!r} {we!r}", f"conn 2 1 0.1 {d!r} {wi!r}", f"conn 2 2 0.1 {d!r} {wi!r}"]
+
+
 def brunel_weights(N: int, p: float) -> tuple[float, float]:
     """float((2/N)(0.1/p)) and float((-10/N)(0.1/p)), computed in double then rounded."""
     return float(np.float32((2.0 / N) * (0.1 / p))), float(np.float32((-10.0 / N) * (0.1 / p)))

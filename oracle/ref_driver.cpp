@@ -30,11 +30,15 @@
 //               wconn SRC DST P DELAY WMAX [FIELD] (fixed_probability + weighted: a per-synapse
 //                                                   weight wmax * canonical<float> drawn at
 //                                                   construction; FIELD as for conn)
+//               stdp POP P DELAY                 (POP -> POP fixed_probability + the STDP synapse of
+//                                                 samples/brunel+.cpp:58-99)
 //               plastic POP P DELAY SCALE        (POP -> POP fixed_probability + count_syn; the
 //                                                 reference keeps the history of a plastic
 //                                                 connection's source, snn.h:44-45, so source and
 //                                                 target are the same population)
+#include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -167,6 +171,32 @@ struct count_syn {
 	void deliver(synapse const& s, lif::neuron& to) const { to.V += s.count * scale; }
 	void update(synapse& s, float, bool, bool) const { s.count++; }
 	void skip(synapse& s, float, Int n) const { s.count += n; }
+};
+
+// The plastic synapse of samples/brunel+.cpp:58-99 (weight W, pre / post traces Zpre / Zpost).
+struct stdp_syn {
+	struct synapse {
+		float W     = 1e-4;
+		float Zpre  = 0;
+		float Zpost = 0;
+	};
+	void deliver(synapse const& syn, lif::neuron& to) const { to.V += syn.W; }
+	void update(synapse& syn, float const dt, bool const pre, bool const post) const {
+		float const TstdpInv = 1.0f / 0.02f;
+		float const dtInv    = 1.0f / dt;
+		syn.W = std::clamp(syn.W - pre * 0.0202f * syn.W * std::exp(-syn.Zpost * dtInv) +
+		                       post * 0.01f * (1.0f - syn.W) * std::exp(-syn.Zpre * dtInv),
+		                   0.0f, 0.0003f);
+		syn.Zpre += pre;
+		syn.Zpost += post;
+		syn.Zpre -= syn.Zpre * dt * TstdpInv;
+		syn.Zpost -= syn.Zpost * dt * TstdpInv;
+	}
+	void skip(synapse& syn, float const dt, Int const n) const {
+		float const TstdpInv = 1.0f / 0.02f;
+		syn.Zpre *= std::pow(1 - dt * TstdpInv, n);
+		syn.Zpost *= std::pow(1 - dt * TstdpInv, n);
+	}
 };
 
 std::vector<float> g_dt;
@@ -371,6 +401,12 @@ static int run_net(int argc, char** argv) {
 				auto* L = net.add_population<lif>(size);
 				pops.push_back({1, size, L, L, nullptr});
 			}
+		} else if (kw == "stdp") {
+			Int q;
+			double p;
+			float delay;
+			in >> q >> p >> delay;
+			net.connect<stdp_syn>(pops[q].L, pops[q].L, fixed_probability(p), delay);
 		} else if (kw == "plastic") {
 			Int q;
 			double p;

@@ -372,7 +372,7 @@ class snn:
         population by the pull path over the CSC adjacency (SPICE_TUNE_PULL)."""
         if pull is not None:
             _check(lib().spice_set_tuning(self._h, 8, int(bool(pull))))
-        if source_steps is not None:  # steps per Poisson source CTA (0: automatic, one-wave grid)
+        if source_steps is not None:  # steps per Poisson source CTA (default 1; 0: one-wave grid)
             _check(lib().spice_set_tuning(self._h, 9, int(source_steps)))
         if tile_bytes is not None:
             _check(lib().spice_set_tuning(self._h, 0, int(tile_bytes)))

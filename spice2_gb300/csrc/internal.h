@@ -176,6 +176,15 @@ struct Conn {
 	bool weighted    = false;     // per-synapse weights (d.wts)
 	float wmax       = 0;
 	int wsource      = 0;         // weighted: 0 drawn by the engine, 1 / 2 set by the host (2: no init seed)
+	// USER_PLASTIC: the user's per-synapse structs and kernels
+	void* ustate     = nullptr;   // [synapses * ubytes], CSR order
+	int ubytes       = 0;
+	int weight_word  = 0;
+	bool init_seed   = false;     // USER_PLASTIC with PerSynapseInit: consumes the init stream's seed
+	void* ufn        = nullptr;   // spice_user_plastic_fn
+	void* uctx       = nullptr;
+	std::vector<char> uinit;      // the initial synapse struct
+	std::vector<char> uhost;      // whole-array initial state set by the host (PerSynapseInit)
 	u128 gseed       = {0, 0};    // the adjacency's seed
 	u128 wseed       = {0, 0};    // the PerSynapseInit stream's seed
 	uint16_t* nb16    = nullptr;  // owned storage of d.nb16
@@ -263,7 +272,7 @@ struct spice_net {
 	int overlap_sources = 1;         // source kernels on their own stream (tunable)
 	int neuron_variant  = 0;         // LIF window variant of the neuron update (tunable)
 	int launch_mode     = 1;         // 1: neurons and sources in one grid, programmatic dependent launches
-	int src_steps       = 0;         // steps per Poisson CTA (0: the fewest that fit the grid in one wave)
+	int src_steps       = 1;         // steps per Poisson CTA (0: the fewest that fit the grid in one wave)
 	int sm_count        = 1;
 	int dmin = 1, dmax = 1;          // connection delays in steps
 	bool plastic = false;            // any plastic connection (windows of one step)

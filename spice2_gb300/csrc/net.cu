@@ -349,6 +349,21 @@ int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int n
 	} else if (synapse == SPICE_SYNAPSE_COUNT) {
 		if (np < 1 || !params) return fail(SPICE_EINVAL, "count needs params {scale[, field]}");
 		c.tau = 1.0f;
+	} else if (synapse == SPICE_SYNAPSE_USER_PLASTIC) {
+		if (np < 3 || !params) return fail(SPICE_EINVAL, "user plastic synapses need params {field, synapse_bytes, weight_word}");
+		c.ubytes      = (int)params[1];
+		c.weight_word = (int)params[2];
+		c.init_seed   = np > 3 && params[3] != 0.0f;  // PerSynapseInit: the ctor's rng(seed++)
+		if (c.ubytes <= 0 || c.ubytes % 4 || c.weight_word < 0 || 4 * c.weight_word + 4 > c.ubytes)
+			return fail(SPICE_EINVAL, "a user synapse struct is a multiple of 4 bytes and holds its weight word");
+		c.d.plastic = synapse;
+		c.d.weight  = 0.0f;
+		c.d.field   = (int)params[0];
+		c.tau       = 1.0f;
+		int const m = n->pops[dst].d.model;
+		if (m == USER ? (c.d.field < 0 || c.d.field >= n->pops[dst].nfields) : (c.d.field < 0 || c.d.field > 2 || (m == LIF && c.d.field != 0)))
+			return fail(SPICE_EINVAL, "the synapse's target field does not exist in the target neuron model");
+		return SPICE_OK;
 	} else if (synapse == SPICE_SYNAPSE_WEIGHTED) {
 		if (np < 1 || !params) return fail(SPICE_EINVAL, "weighted needs params {wmax[, field[, source]]}");
 		c.weighted = true;
@@ -403,7 +418,7 @@ extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, d
 	n->conns.back().gseed = seed_next(n);
 	n->gen_pending.push_back({(int)n->conns.size() - 1, n->conns.back().gseed, p});
 	// PerSynapseInit: rng(seed++) after the adjacency's (synapse_population.h:34-41)
-	if (c.weighted && c.wsource != 2) n->conns.back().wseed = seed_next(n);
+	if ((c.weighted && c.wsource != 2) || c.init_seed) n->conns.back().wseed = seed_next(n);
 	if (conn_out) *conn_out = (int)n->conns.size() - 1;
 	return SPICE_OK;
 }
@@ -457,7 +472,7 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	c.d.nb  = dnb;
 	n->conns.push_back(c);
 	n->conns.back().gseed = seed_next(n);  // the synapse_population ctor consumes a seed for every topology
-	if (c.weighted && c.wsource != 2) n->conns.back().wseed = seed_next(n);  // PerSynapseInit (synapse_population.h:34-41)
+	if ((c.weighted && c.wsource != 2) || c.init_seed) n->conns.back().wseed = seed_next(n);  // PerSynapseInit (synapse_population.h:34-41)
 	if (conn_out) *conn_out = (int)n->conns.size() - 1;
 	return SPICE_OK;
 }
@@ -733,7 +748,10 @@ int prepare(spice_net* n) {
 	for (auto const& c : n->conns) {
 		if (!c.d.plastic) continue;
 		n->plastic = true;
-		bool const delivers = c.d.plastic == SPICE_SYNAPSE_ISTDP || c.d.weight != 0.0f;
+		bool const delivers = c.d.plastic == SPICE_SYNAPSE_ISTDP || c.d.plastic == SPICE_SYNAPSE_USER_PLASTIC ||
+		                      c.d.weight != 0.0f;
+		if (c.d.plastic == SPICE_SYNAPSE_USER_PLASTIC && !c.ufn)
+			return fail(SPICE_ESTATE, "a user plastic connection needs its kernels (spice_user_plastic) before the network steps");
 		if (delivers && n->mode != SPICE_MODE_ATOMIC)
 			return fail(SPICE_EINVAL, "plastic synapses that deliver per-synapse weights need SPICE_MODE_ATOMIC "
 			                          "(their per-step sums are order-dependent)");
@@ -915,9 +933,24 @@ int prepare(spice_net* n) {
 		PopDev& T = n->pops[d.dst].d;
 		PopDev const& S = n->pops[d.src].d;
 		if (!T.hist) TRY(dalloc(n, &T.hist, (size_t)std::max<int64_t>(T.size, 1)));
-		TRY(dalloc(n, &d.sW, (size_t)std::max<int64_t>(c.synapses, 1), false));
-		TRY(dalloc(n, &d.sA, (size_t)std::max<int64_t>(c.synapses, 1)));
-		TRY(dalloc(n, &d.sB, (size_t)std::max<int64_t>(c.synapses, 1)));
+		if (d.plastic == SPICE_SYNAPSE_USER_PLASTIC) {  // the user's structs, initial value or host state
+			char* st = nullptr;
+			size_t const bytes = (size_t)std::max<int64_t>(c.synapses, 1) * c.ubytes;
+			TRY(dalloc(n, &st, bytes, false));
+			if (!c.uhost.empty()) {
+				CUDA_TRY(cudaMemcpy(st, c.uhost.data(), c.uhost.size(), cudaMemcpyHostToDevice));
+				c.uhost.clear();
+			} else {
+				std::vector<char> h(bytes);
+				for (size_t q = 0; q + c.ubytes <= bytes; q += c.ubytes) memcpy(h.data() + q, c.uinit.data(), c.ubytes);
+				CUDA_TRY(cudaMemcpy(st, h.data(), bytes, cudaMemcpyHostToDevice));
+			}
+			c.ustate = st;
+		} else {
+			TRY(dalloc(n, &d.sW, (size_t)std::max<int64_t>(c.synapses, 1), false));
+			TRY(dalloc(n, &d.sA, (size_t)std::max<int64_t>(c.synapses, 1)));
+			TRY(dalloc(n, &d.sB, (size_t)std::max<int64_t>(c.synapses, 1)));
+		}
 		TRY(dalloc(n, &d.ages, (size_t)std::max<int64_t>(S.size, 1)));
 		TRY(dalloc(n, &d.chunks_done, (size_t)std::max<int64_t>(S.size, 1)));
 		{  // the longest row sizes the plastic delivery's grid
@@ -926,8 +959,10 @@ int prepare(spice_net* n) {
 			d.max_row = 0;
 			for (int64_t r = 0; r < S.size; r++) d.max_row = std::max(d.max_row, off[r + 1] - off[r]);
 		}
-		std::vector<float> w0((size_t)std::max<int64_t>(c.synapses, 1), d.plastic == SPICE_SYNAPSE_ISTDP ? c.w0 : 0.0f);
-		CUDA_TRY(cudaMemcpy(d.sW, w0.data(), sizeof(float) * w0.size(), cudaMemcpyHostToDevice));
+		if (d.sW) {
+			std::vector<float> w0((size_t)std::max<int64_t>(c.synapses, 1), d.plastic == SPICE_SYNAPSE_ISTDP ? c.w0 : 0.0f);
+			CUDA_TRY(cudaMemcpy(d.sW, w0.data(), sizeof(float) * w0.size(), cudaMemcpyHostToDevice));
+		}
 		d.alpha = 2.0f * c.rho0 * c.tau;
 		d.cdt   = n->dt * (1.0f / c.tau);
 		std::vector<double> tab(129);
@@ -1053,6 +1088,7 @@ spice_user_window user_window(spice_net* n, int pi, WindowArgs const& wa, int64_
 	w.pull_A    = d.pull_A;
 	w.pull_G    = d.pull_G;
 	w.pull_koff = d.pull_koff;
+	w.hist      = d.hist;
 	return w;
 }
 
@@ -1067,6 +1103,40 @@ int launch_user_pops(spice_net* n, WindowArgs const& wa, int64_t j, bool statefu
 		                                          " failed (" + std::to_string(r) + ")");
 		n->launches++;
 	}
+	return SPICE_OK;
+}
+
+// One call of a user plastic connection's kernels (spice_user_plastic_call).
+int call_user_plastic(spice_net* n, Conn const& c, int what, int hslot, int64_t slot, bool deliver) {
+	spice_user_plastic_call u;
+	memset(&u, 0, sizeof u);
+	u.version       = SPICE_USER_PLASTIC_ABI_VERSION;
+	u.what          = what;
+	u.time          = n->time;
+	u.dt            = n->dt;  // synapses see the raw dt (snn.cpp:19, 23)
+	u.hslot         = hslot;
+	u.slot          = slot;
+	u.deliver       = deliver ? 1 : 0;
+	u.src_size      = c.d.src_size;
+	u.dst_size      = c.d.dst_size;
+	u.off           = c.d.off;
+	u.nb            = c.d.nb;
+	u.state         = c.ustate;
+	u.synapse_bytes = c.ubytes;
+	u.weight_word   = c.weight_word;
+	u.ages          = c.d.ages;
+	u.chunks_done   = c.d.chunks_done;
+	u.max_row       = c.d.max_row;
+	u.dst_hist      = c.d.dst_hist;
+	u.src_bits      = c.d.src_bits;
+	u.src_nwords    = c.d.src_nwords;
+	u.dst_acc       = c.d.dst_acc;
+	u.F             = c.d.F;
+	u.fslot         = c.d.fslot;
+	u.events        = n->d_events;
+	int const r     = reinterpret_cast<spice_user_plastic_fn>(c.ufn)(&u, (void*)n->stream, c.uctx);
+	if (r != 0) return fail(SPICE_ECUDA, "the kernels of a user plastic connection failed (" + std::to_string(r) + ")");
+	n->launches++;
 	return SPICE_OK;
 }
 
@@ -1215,7 +1285,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			}
 			if (n->plastic && n->time % 64 == 0)  // snn.cpp:17-19 (windows are one step long)
 				for (auto const& c : n->conns)
-					if (c.d.plastic) {
+					if (c.d.plastic == SPICE_SYNAPSE_USER_PLASTIC) {
+						TRY(call_user_plastic(n, c, 0, 0, 0, false));
+					} else if (c.d.plastic) {
 						CUDA_TRY(launch_plastic_update_all(n->stream, c.d, n->time));
 						n->launches++;
 					}
@@ -1258,10 +1330,15 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 					if (c.d.plastic && n->time >= c.d.delay - 1) {
 						int const hs = (int)((n->time - c.d.delay + 1) % n->Hb);
 						bool const delivers = n->mode == SPICE_MODE_ATOMIC &&
-						                      (c.d.plastic == SPICE_SYNAPSE_ISTDP || c.d.weight != 0.0f);
-						CUDA_TRY(launch_plastic_deliver(n->stream, c.d, n->time, hs, n->time % n->max_delay, delivers,
-						                                n->d_events));
-						n->launches++;
+						                      (c.d.plastic == SPICE_SYNAPSE_ISTDP || c.d.plastic == SPICE_SYNAPSE_USER_PLASTIC ||
+						                       c.d.weight != 0.0f);
+						if (c.d.plastic == SPICE_SYNAPSE_USER_PLASTIC) {
+							TRY(call_user_plastic(n, c, 1, hs, n->time % n->max_delay, delivers));
+						} else {
+							CUDA_TRY(launch_plastic_deliver(n->stream, c.d, n->time, hs, n->time % n->max_delay, delivers,
+							                                n->d_events));
+							n->launches++;
+						}
 					}
 			TRY(ev_end(n, slot));
 			n->launches++;
@@ -1822,6 +1899,40 @@ extern "C" int spice_set_synapse_weights(spice_net* n, int conn, const float* w)
 		c.d.wts = d;
 	}
 	if (c.synapses > 0) CUDA_TRY(cudaMemcpy((void*)c.d.wts, w, sizeof(float) * c.synapses, cudaMemcpyHostToDevice));
+	return SPICE_OK;
+}
+
+extern "C" int spice_user_plastic(spice_net* n, int conn, spice_user_plastic_fn fn, void* ctx, const void* init_syn) {
+	if (!n || !fn || !init_syn) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	Conn& c = n->conns[conn];
+	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC) return fail(SPICE_EINVAL, "not a user plastic connection");
+	if (n->prepared) return fail(SPICE_ESTATE, "user plastic kernels are registered before the network first steps");
+	c.ufn  = (void*)fn;
+	c.uctx = ctx;
+	c.uinit.assign(static_cast<const char*>(init_syn), static_cast<const char*>(init_syn) + c.ubytes);
+	return SPICE_OK;
+}
+
+extern "C" int spice_set_user_synapse_state(spice_net* n, int conn, const void* in) {
+	if (!n || !in) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	Conn& c = n->conns[conn];
+	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC) return fail(SPICE_EINVAL, "not a user plastic connection");
+	if (n->prepared) return fail(SPICE_ESTATE, "the initial synapse state is set before the network first steps");
+	TRY(generate_pending(n));
+	c.uhost.assign(static_cast<const char*>(in), static_cast<const char*>(in) + (size_t)c.synapses * c.ubytes);
+	return SPICE_OK;
+}
+
+extern "C" int spice_get_user_synapse_state(spice_net* n, int conn, void* out) {
+	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	Conn const& c = n->conns[conn];
+	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC) return fail(SPICE_EINVAL, "not a user plastic connection");
+	TRY(prepare(n));
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	if (c.synapses > 0) CUDA_TRY(cudaMemcpy(out, c.ustate, (size_t)c.synapses * c.ubytes, cudaMemcpyDeviceToHost));
 	return SPICE_OK;
 }
 

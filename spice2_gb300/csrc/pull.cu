@@ -48,6 +48,7 @@ namespace {
 constexpr int kPullThreads = 256;
 constexpr int kPullWarps   = kPullThreads / 32;
 constexpr int kMaxBins     = kPullMaxWindow * 3;
+constexpr int kPullUnroll  = 8;  // chunks of 32 column entries loaded together by a warp
 
 __device__ __forceinline__ unsigned lanemask_lt_pull() {
 	unsigned m;
@@ -246,22 +247,33 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 		while (f + 1 < F && P.pull_field[f] != C.field) f++;
 		int64_t const e0 = C.csc_off[i], e1 = C.csc_off[i + 1];
 		uint32_t const fw = __float_as_uint(C.weight);
-		for (int64_t eb = e0; eb < e1; eb += 32) {
-			int64_t const e = eb + lane;
-			bool act        = false;
-			uint32_t m = 0, wb = 0;
-			if (e < e1) {
-				int32_t const s = __ldg(C.csc_src + e);
-				act             = (__ldg(C.pull_orb + (s >> 5)) >> (s & 31)) & 1u;
+		// kPullUnroll coalesced chunks of 32 sources in flight per warp, then their tests and appends
+		// in entry order
+		for (int64_t eb = e0; eb < e1; eb += 32 * kPullUnroll) {
+			int32_t src[kPullUnroll];
+#pragma unroll
+			for (int u = 0; u < kPullUnroll; u++) {
+				int64_t const e = eb + 32 * u + lane;
+				src[u]          = e < e1 ? __ldg(C.csc_src + e) : -1;
+			}
+			uint32_t orw[kPullUnroll];
+#pragma unroll
+			for (int u = 0; u < kPullUnroll; u++) orw[u] = src[u] >= 0 ? __ldg(C.pull_orb + (src[u] >> 5)) : 0u;
+#pragma unroll
+			for (int u = 0; u < kPullUnroll; u++) {
+				if (eb + 32 * u >= e1) break;  // warp-uniform
+				int64_t const e = eb + 32 * u + lane;
+				bool act        = src[u] >= 0 && ((orw[u] >> (src[u] & 31)) & 1u);
+				uint32_t m = 0, wb = 0;
 				if (act) {
-					m  = __ldg(C.pull_wm + s) & ((1u << a.K) - 1u);
-					wb = C.csc_w ? __float_as_uint(__ldg(C.csc_w + e)) : fw;
+					m   = __ldg(C.pull_wm + src[u]) & ((1u << a.K) - 1u);
+					wb  = C.csc_w ? __float_as_uint(__ldg(C.csc_w + e)) : fw;
 					act = m != 0;
 				}
+				unsigned const bal = __ballot_sync(0xffffffffu, act);
+				if (act) A[nA + __popc(bal & lanemask_lt_pull())] = (uint64_t)wb | ((uint64_t)(m | ((uint32_t)f << 16)) << 32);
+				nA += __popc(bal);
 			}
-			unsigned const bal = __ballot_sync(0xffffffffu, act);
-			if (act) A[nA + __popc(bal & lanemask_lt_pull())] = (uint64_t)wb | ((uint64_t)(m | ((uint32_t)f << 16)) << 32);
-			nA += __popc(bal);
 		}
 	}
 	__syncwarp();

@@ -20,12 +20,15 @@ headers) compiled by oracle/Makefile with the reference's Release flags -- and s
   weighted_net.npz           oracle.WEIGHTED_NET (per-synapse weights drawn by PerSynapseInit into LIF
                              and conductance targets, fixed weights, delays 3..12, a population with
                              six distinct input weights), 600 steps: raster and final states
+  brunel_plus.npz            samples/brunel+.cpp (N=2e4, STDP on E->E) for seeds 1..10, 1000 steps each:
+                             per-step spike counts of P, E, I (plasticity with exp(): compared
+                             statistically)
   vogels_c3_n10000.npz       the plastic E/I network's neurons and static weights without plasticity
                              (N=1e4 conductance LIF, p=0.02, E 0.03 / I 0.3, delay 1 step, seed 7),
                              1000 steps: raster and final state
 
 usage: python tests/golden/make_golden.py [GROUP ...]   (needs the reference sources; run from the
-       repo root; groups: base, vogels, weighted, brunel_long; default: all)
+       repo root; groups: base, vogels, weighted, brunel_plus, brunel_long; default: all)
 """
 from __future__ import annotations
 
@@ -98,6 +101,14 @@ def weighted_fixtures(steps: int = 600):
     np.savez_compressed(os.path.join(HERE, "weighted_net.npz"), **arrs)
 
 
+def brunel_plus_fixtures(steps: int = 1000):
+    arrs = {}
+    for sd in range(1, 11):
+        res = O.run_reference_net(O.brunel_plus_spec(sd, steps))
+        arrs[f"counts_s{sd}"] = np.array([[len(x) for x in row] for row in res["raster"]], dtype=np.int32)
+    np.savez_compressed(os.path.join(HERE, "brunel_plus.npz"), **arrs)
+
+
 def brunel_long_fixtures():
     arrs = {}
     jobs = [(1, BRUNEL_LONG_SEED1_STEPS, BRUNEL_LONG_BLOCK)] + [(sd, BRUNEL_SEEDS_STEPS, BRUNEL_SEEDS_BLOCK)
@@ -111,13 +122,15 @@ def brunel_long_fixtures():
     np.savez_compressed(os.path.join(HERE, "brunel_n500000_long.npz"), **arrs)
 
 
-def main(groups=("base", "vogels", "weighted", "brunel_long")):
+def main(groups=("base", "vogels", "weighted", "brunel_plus", "brunel_long")):
     if not O.have_reference():
         O.build(with_reference=True, reference_dir=os.environ.get("SPICE_REFERENCE_DIR", "/root/reference"))
     if "vogels" in groups:
         vogels_fixtures()
     if "weighted" in groups:
         weighted_fixtures()
+    if "brunel_plus" in groups:
+        brunel_plus_fixtures()
     if "brunel_long" in groups:
         brunel_long_fixtures()
     if "base" not in groups:
@@ -179,4 +192,4 @@ def main(groups=("base", "vogels", "weighted", "brunel_long")):
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("base", "vogels", "weighted", "brunel_long"))
+    main(tuple(sys.argv[1:]) or ("base", "vogels", "weighted", "brunel_plus", "brunel_long"))

@@ -118,3 +118,32 @@ def test_user_models_compiled_with_nvcc_match_the_reference(engine, oracle_lib, 
         assert sorted(row) == expect, f"step {t}"
         n_spikes += len(I) + len(E)
     assert n_spikes > 0
+
+
+def _reference_samples_dir():
+    import __graft_entry__ as g
+    d = os.path.join(g.REFERENCE_DIR, "samples")
+    return d if os.path.isdir(d) else None
+
+
+@pytest.mark.skipif(_reference_samples_dir() is None, reason="the reference's sources are not on this machine")
+@pytest.mark.parametrize("sample", ["brunel", "brunel+", "vogels"])
+def test_reference_samples_compile_against_the_header(engine, tmp_path, sample):
+    """The reference's own sample programs, with SPICE_HD added in front of their models' update(),
+    deliver(), skip() and init() and nothing else changed, compile with nvcc against
+    include/spice/snn.h and spice2_gb300/examples/matplot.h (their output stream) and link against
+    the engine: the reference's user API, model concepts and integer names are all there."""
+    import re
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    if not os.path.exists(nvcc):
+        pytest.skip("nvcc not found")
+    src = open(os.path.join(_reference_samples_dir(), sample + ".cpp")).read()
+    annotated = re.sub(r"^(\s*)(bool|void) (update|deliver|skip|init)\(", r"\1SPICE_HD \2 \3(", src, flags=re.M)
+    assert annotated.count("SPICE_HD") >= 2
+    f = tmp_path / (sample.replace("+", "_plus") + ".cu")
+    f.write_text(annotated)
+    libdir = os.path.join(ROOT, "spice2_gb300")
+    subprocess.run([nvcc, "-std=c++20", "--expt-relaxed-constexpr", "-gencode", "arch=compute_103a,code=sm_103a",
+                    "-fmad=false", "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "spice2_gb300", "examples"),
+                    str(f), "-L", libdir, "-lspice_gb300", f"-Xlinker=-rpath={libdir}", "-o", str(tmp_path / "sample")],
+                   check=True)
