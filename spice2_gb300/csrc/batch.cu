@@ -120,10 +120,10 @@ int build(spice_batch* b) {
 			hp.push_back(d);
 			int nb = 0, kind = 0, sb = 0;
 			if (d.model == POISSON) {
-				sb = (d.nwords + 255) / 256;
+				sb = (d.nwords + kNeuronThreads - 1) / kNeuronThreads;
 				b->draws |= d.size > 0;
 			} else {
-				nb   = (int)((d.size + 255) / 256);
+				nb   = (int)((d.size + kNeuronThreads - 1) / kNeuronThreads);
 				kind = neuron_block_kind(d);
 				if (nb > 0) only_fast &= kind == 3;
 			}

@@ -96,6 +96,10 @@ cudaError_t max_indegree(cudaStream_t stream, const int32_t* const* nbs, const i
 // Jump tables of steps t < nsteps: tables[t][g][m] = XOR of T^(8g+q)(seed_t) over the bits q of m.
 cudaError_t launch_jump_tables(cudaStream_t stream, const u128* seeds, int64_t nsteps, u128* tables);
 
+// Threads per CTA of the neuron update and source populations (one neuron, or one 32-neuron Poisson
+// chunk, per thread); smaller CTAs balance the window's grid across the SMs more evenly.
+constexpr int kNeuronThreads = 128;
+constexpr int kNeuronBlocksPerSM = 2048 / kNeuronThreads;  // resident CTAs of the register-lean kernels
 constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
 // Delivery work mappings (SPICE_TUNE_DELIVER_ALGO 0 .. kDeliverAlgos - 1), one kernel per mapping
 // and mode.

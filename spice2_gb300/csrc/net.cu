@@ -1205,7 +1205,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				ws.blk_begin[p] = nbs;
 				if (P.model == POISSON) {
 					ws.blk_kind[p]     = 1;
-					ws.blk_per_step[p] = (P.nwords + 255) / 256;
+					ws.blk_per_step[p] = (P.nwords + kNeuronThreads - 1) / kNeuronThreads;
 					wa.blk_kind[p] = 1;
 				} else if (P.model == USER) {
 					ws.blk_kind[p] = 0;  // launched by the user's callback
@@ -1220,7 +1220,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				} else {
 					wa.blk_kind[p] = neuron_block_kind(P) + (P.hist ? kHistKind : 0);
 					ws.blk_kind[p] = wa.blk_kind[p];
-					nb += (int)((P.size + 255) / 256);
+					nb += (int)((P.size + kNeuronThreads - 1) / kNeuronThreads);
 				}
 			}
 			// Poisson CTAs: src_steps consecutive steps each -- by default the fewest that keep the
@@ -1230,7 +1230,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				if (n->pops[p].d.model == POISSON) poisson_bps += ws.blk_per_step[p];
 			int S = n->src_steps > 0 ? std::min(n->src_steps, k) : 1;
 			if (n->src_steps == 0 && poisson_bps > 0) {
-				int const wave = n->sm_count * 8 - (record ? k * np : 0);
+				int const wave = n->sm_count * kNeuronBlocksPerSM - (record ? k * np : 0);
 				while (S < k && nb + nbs + poisson_bps * ((k + S - 1) / S) > wave) S++;
 			}
 			ws.src_steps = S;

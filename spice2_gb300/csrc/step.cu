@@ -32,7 +32,7 @@ namespace spice_gb300 {
 
 namespace {
 
-constexpr int kThreads = 256;
+constexpr int kThreads = kNeuronThreads;
 
 // Programmatic dependent launch (sm_90+): griddep_wait() returns once the preceding kernel of the
 // stream has completed and its writes are visible (at once when there is no programmatic edge);
@@ -753,7 +753,7 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 // compiled out (fewer registers).  VAR: the LIF window variant (window_lif_fast), one kernel each so
 // that each keeps its own register count.
 template <int MODE, bool ONLY_FAST, int VAR>
-__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_neurons(const __grid_constant__ WindowArgs a) {
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? kNeuronBlocksPerSM : 1) k_neurons(const __grid_constant__ WindowArgs a) {
 	neurons_block<MODE, ONLY_FAST, VAR>(a, (int)blockIdx.x);
 }
 
@@ -791,7 +791,7 @@ __global__ void __launch_bounds__(kThreads) k_sources(const __grid_constant__ Wi
 __device__ void raster_block(RasterArgs const& a, int b);
 
 template <int MODE, bool ONLY_FAST, int VAR, bool REC>
-__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_window(const __grid_constant__ WindowArgs a,
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? kNeuronBlocksPerSM : 1) k_window(const __grid_constant__ WindowArgs a,
                                                                        const __grid_constant__ WindowArgs s, int nb,
                                                                        const __grid_constant__ RasterArgs r) {
 	// each block kind waits for the previous launch where it first reads that launch's output; the
@@ -2483,7 +2483,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_sources(const __grid_constan
 
 // Per-neuron populations of all nets, K steps each with the state in registers.
 template <int MODE, bool ONLY_FAST>
-__global__ void __launch_bounds__(kThreads, ONLY_FAST ? 8 : 1) k_batch_neurons(const __grid_constant__ BatchArgs b) {
+__global__ void __launch_bounds__(kThreads, ONLY_FAST ? kNeuronBlocksPerSM : 1) k_batch_neurons(const __grid_constant__ BatchArgs b) {
 	BatchClock const c = *b.clock;
 	int const x        = blockIdx.x;
 	int const p        = find_segment(b.nblk_begin, b.npop, x);
