@@ -57,13 +57,15 @@ WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
 # times the launch's mean events (None for a mapping without a capture).
 DELIVER_DRAM_BYTES_PER_EVENT = {5: (62.261504e6 + 1.521152e6) / 11158496,
                                 8: (56.677376e6 + 0.970496e6) / 11158496,
-                                # mappings 15-19 read the same 16-bit target copy; measured on 17
+                                # mappings 15-21 read the same 16-bit target copy; measured on 17
                                 # (window 91, 10,415,589 events)
                                 15: (32.342528e6 + 0.064e6) / 10415589,
                                 16: (32.342528e6 + 0.064e6) / 10415589,
                                 17: (32.342528e6 + 0.064e6) / 10415589,
                                 18: (32.342528e6 + 0.064e6) / 10415589,
-                                19: (32.342528e6 + 0.064e6) / 10415589}
+                                19: (32.342528e6 + 0.064e6) / 10415589,
+                                20: (32.342528e6 + 0.064e6) / 10415589,
+                                21: (32.342528e6 + 0.064e6) / 10415589}
 DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
                    7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
@@ -72,7 +74,8 @@ DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k
                    13: "k_deliver_staged_vec<2 sub-rows, 6 blocks>", 14: "k_deliver_rows",
                    15: "k_deliver_rows16<1 sub-row>", 16: "k_deliver_rows16<4 sub-rows>",
                    17: "k_deliver_rows16<2 sub-rows>", 18: "k_deliver_rows16<1 sub-row, TMA store>",
-                   19: "k_deliver_rows16<2 sub-rows, TMA store>"}
+                   19: "k_deliver_rows16<2 sub-rows, TMA store>", 20: "k_deliver_rows16_occ<1 sub-row>",
+                   21: "k_deliver_rows16_occ<2 sub-rows>"}
 
 
 def _dist():

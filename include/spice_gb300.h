@@ -152,7 +152,8 @@ enum {
 	                                   (2 bytes per synapse, rebuilt with the tiles); per lane
 	                                   group and round trip 1 x 256, 4 x 64, 2 x 128 targets,
 	                                   18, 19: as 15, 17 storing the finished tile by TMA bulk
-	                                   copies                                                 */
+	                                   copies, 20, 21: as 15, 17 at two 512-thread CTAs per SM
+	                                   (<= 64 registers, 1024 staged sub-rows)                */
 	SPICE_TUNE_OVERLAP_SOURCES = 4, /* 1: source populations run on a second stream, 0: inline */
 	SPICE_TUNE_GRAPH_WINDOWS   = 5, /* batches only: windows per captured CUDA graph, 0: none */
 	SPICE_TUNE_LAUNCH          = 7, /* 1 (default): per window, one grid for the neuron update and

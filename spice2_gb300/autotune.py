@@ -26,7 +26,8 @@ DEFAULT_CANDIDATES = [
     #  16-byte blocks: 2 x 64, 4 x 32, 1 x 128 and 2 x 96 targets per group and round trip, 14 as 12
     #  with per-sub-row pointers and target ranges precomputed while staging, 15 / 16 / 17 as 14
     #  reading a 16-bit tile-local copy of the targets, 1 x 256, 4 x 64 and 2 x 128 targets per
-    #  group and round trip, 18 / 19 as 15 / 17 storing the finished tile by TMA bulk copies)
+    #  group and round trip, 18 / 19 as 15 / 17 storing the finished tile by TMA bulk copies,
+    #  20 / 21 as 15 / 17 at two 512-thread CTAs per SM)
     (6 * 1024, 128, 1, 1), (12 * 1024, 128, 1, 1), (24 * 1024, 128, 1, 1), (12 * 1024, 256, 1, 1),
     (24 * 1024, 256, 1, 1), (24 * 1024, 512, 1, 1), (48 * 1024, 512, 1, 1), (24 * 1024, 256, 2, 1),
     (24 * 1024, 256, 1, 0), (12 * 1024, 128, 1, 2), (24 * 1024, 256, 1, 2), (48 * 1024, 512, 1, 3),
@@ -55,6 +56,9 @@ DEFAULT_CANDIDATES = [
     # two CTAs per SM: 50 KiB tiles make 300 (slot, tile) items at Brunel N=5e5, one wave
     (50 * 1024, 512, 1, 15), (50 * 1024, 512, 1, 17), (50 * 1024, 512, 1, 18), (50 * 1024, 512, 1, 19),
     (50 * 1024, 384, 1, 17), (56 * 1024, 512, 1, 15), (64 * 1024, 512, 1, 15),
+    # two 512-thread CTAs per SM (at most 64 registers, 1024 staged sub-rows each)
+    (48 * 1024, 512, 1, 20), (64 * 1024, 512, 1, 20), (80 * 1024, 512, 1, 20), (88 * 1024, 512, 1, 20),
+    (48 * 1024, 512, 1, 21), (64 * 1024, 512, 1, 21), (80 * 1024, 512, 1, 21), (88 * 1024, 512, 1, 21),
 ]
 
 

@@ -103,9 +103,9 @@ constexpr int kNeuronBlocksPerSM = 2048 / kNeuronThreads;  // resident CTAs of t
 constexpr int kHistKind = 8;  // blk_kind flag of populations with a post-spike history
 // Delivery work mappings (SPICE_TUNE_DELIVER_ALGO 0 .. kDeliverAlgos - 1), one kernel per mapping
 // and mode.
-constexpr int kDeliverAlgos = 20;
+constexpr int kDeliverAlgos = 22;
 // the mappings that read ConnDev::nb16
-__host__ __device__ constexpr bool compact_algo(int algo) { return algo >= 15 && algo <= 19; }
+__host__ __device__ constexpr bool compact_algo(int algo) { return algo >= 15 && algo <= 21; }
 constexpr int kDeliverFns   = 2 * kDeliverAlgos;
 
 struct WindowArgs {

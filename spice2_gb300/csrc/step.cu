@@ -1689,14 +1689,14 @@ __device__ __forceinline__ void deliver_rows(A const& a, PopDev const& P, int t,
 // a group of 4 lanes takes SF sub-rows per fetch and covers 32 U targets of each per load round trip
 // (all SF sub-rows' loads in flight together), and a target's shared-memory address is the
 // connection's base plus index times the words per neuron.
-template <int MODE, int SF, int U, bool TMA, class A>
+template <int MODE, int SF, int U, bool TMA, int STAGE = kStageR, class A>
 __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int t, int si, int part) {
 	constexpr int G = 4;
 	extern __shared__ uint32_t tile_sm[];
 	__shared__ unsigned long long ev_block;
-	__shared__ const int4* st_ptr[kStageR];
-	__shared__ uint32_t st_lohi[kStageR];  // lo (3 bits) | hi << 3: targets [lo, hi) of the blocks from st_ptr
-	__shared__ uint2 st_ai[kStageR];       // shared-memory address of the connection's word of index 0, increment
+	__shared__ const int4* st_ptr[STAGE];
+	__shared__ uint32_t st_lohi[STAGE];  // lo (3 bits) | hi << 3: targets [lo, hi) of the blocks from st_ptr
+	__shared__ uint2 st_ai[STAGE];       // shared-memory address of the connection's word of index 0, increment
 	__shared__ int c_pre[kConnBatch + 1];
 	__shared__ const int32_t* c_lst[kConnBatch];
 	__shared__ const int64_t* c_bnd[kConnBatch];
@@ -1789,8 +1789,8 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 		__syncthreads();
 		int const nc    = s_nc;
 		int const total = c_pre[nc];
-		for (int c0 = 0; c0 < total; c0 += kStageR) {
-			int const m = min(kStageR, total - c0);
+		for (int c0 = 0; c0 < total; c0 += STAGE) {
+			int const m = min(STAGE, total - c0);
 			for (int q = threadIdx.x; q < m; q += blockDim.x) {
 				int const g = c0 + q;
 				int j       = 0;
@@ -2027,6 +2027,15 @@ template <int MODE, int SF, int U, bool TMA>
 __global__ void __launch_bounds__(SF > 1 ? 768 : 1024, 1) k_deliver_rows16(const __grid_constant__ DeliverArgs a) {
 	DeliverItem const it = deliver_item<false>(a);  // deliver_rows16 waits after its prologue
 	deliver_rows16<MODE, SF, U, TMA>(a, a.pops[it.Q], it.t, it.si, it.part);
+	clear_counts_next(a);
+}
+
+// The compact-target row mapping at two 512-thread CTAs per SM (at most 64 registers, 1024 staged
+// sub-rows): one CTA's staging, barriers and flush overlap the other's reductions.
+template <int MODE, int SF, int U>
+__global__ void __launch_bounds__(512, 2) k_deliver_rows16_occ(const __grid_constant__ DeliverArgs a) {
+	DeliverItem const it = deliver_item<false>(a);
+	deliver_rows16<MODE, SF, U, false, 1024>(a, a.pops[it.Q], it.t, it.si, it.part);
 	clear_counts_next(a);
 }
 
@@ -2537,7 +2546,9 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else if (ALGO == 16) deliver_rows16<MODE, 4, 2, false>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 17) deliver_rows16<MODE, 2, 4, false>(a, P, t, (int)blockIdx.y, part);
 	else if (ALGO == 18) deliver_rows16<MODE, 1, 8, true>(a, P, t, (int)blockIdx.y, part);
-	else deliver_rows16<MODE, 2, 4, true>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 19) deliver_rows16<MODE, 2, 4, true>(a, P, t, (int)blockIdx.y, part);
+	else if (ALGO == 20) deliver_rows16<MODE, 1, 8, false, 1024>(a, P, t, (int)blockIdx.y, part);
+	else deliver_rows16<MODE, 2, 4, false, 1024>(a, P, t, (int)blockIdx.y, part);
 }
 
 }  // namespace
@@ -2675,7 +2686,9 @@ cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int thread
 	                       (void const*)k_deliver_rows16<0, 4, 2, false>, (void const*)k_deliver_rows16<1, 4, 2, false>,
 	                       (void const*)k_deliver_rows16<0, 2, 4, false>, (void const*)k_deliver_rows16<1, 2, 4, false>,
 	                       (void const*)k_deliver_rows16<0, 1, 8, true>,  (void const*)k_deliver_rows16<1, 1, 8, true>,
-	                       (void const*)k_deliver_rows16<0, 2, 4, true>,  (void const*)k_deliver_rows16<1, 2, 4, true>};
+	                       (void const*)k_deliver_rows16<0, 2, 4, true>,  (void const*)k_deliver_rows16<1, 2, 4, true>,
+	                       (void const*)k_deliver_rows16_occ<0, 1, 8>,   (void const*)k_deliver_rows16_occ<1, 1, 8>,
+	                       (void const*)k_deliver_rows16_occ<0, 2, 4>,   (void const*)k_deliver_rows16_occ<1, 2, 4>};
 	void const* fn = fns[m];
 	cudaFuncAttributes fa;
 	if (cudaFuncGetAttributes(&fa, fn) == cudaSuccess && threads > fa.maxThreadsPerBlock)
@@ -2775,7 +2788,9 @@ void const* batch_deliver_fn(BatchArgs const& b) {
 	                       (void const*)k_batch_deliver<0, 16>, (void const*)k_batch_deliver<1, 16>,
 	                       (void const*)k_batch_deliver<0, 17>, (void const*)k_batch_deliver<1, 17>,
 	                       (void const*)k_batch_deliver<0, 18>, (void const*)k_batch_deliver<1, 18>,
-	                       (void const*)k_batch_deliver<0, 19>, (void const*)k_batch_deliver<1, 19>};
+	                       (void const*)k_batch_deliver<0, 19>, (void const*)k_batch_deliver<1, 19>,
+	                       (void const*)k_batch_deliver<0, 20>, (void const*)k_batch_deliver<1, 20>,
+	                       (void const*)k_batch_deliver<0, 21>, (void const*)k_batch_deliver<1, 21>};
 	return fns[m];
 }
 }  // namespace

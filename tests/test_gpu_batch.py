@@ -78,7 +78,8 @@ def test_batch_member_matches_oracle(engine, oracle_lib):
     dict(deliver_algo=12, tile_bytes=48 * 1024, deliver_threads=512), dict(deliver_algo=14, deliver_parts=2),
     dict(deliver_algo=15, tile_bytes=24 * 1024, deliver_threads=256), dict(deliver_algo=15, deliver_parts=3),
     dict(deliver_parts=2), dict(tile_bytes=4096, deliver_threads=128), dict(overlap_sources=False),
-    dict(graph_windows=0),
+    dict(graph_windows=0), dict(deliver_algo=20, tile_bytes=48 * 1024, deliver_threads=512),
+    dict(deliver_algo=21, tile_bytes=24 * 1024, deliver_threads=512),
 ])
 def test_batch_launch_shapes(engine, shape):
     """Every launch shape gives the same bits (results never depend on the shape)."""

@@ -368,6 +368,7 @@ def test_results_independent_of_launch_shape(engine, tile_bytes, threads):
     (15, 100 * 1024, 1024, 1), (15, 4096, 64, 3), (15, 24 * 1024, 256, 2), (15, 4096, 32, 1), (15, 160 * 1024, 1024, 1),
     (16, 100 * 1024, 768, 1), (16, 4096, 64, 3), (16, 8192, 32, 1), (17, 100 * 1024, 768, 1), (17, 12 * 1024, 128, 2),
     (18, 100 * 1024, 1024, 1), (18, 4096, 32, 1), (18, 180 * 1024, 1024, 1), (19, 100 * 1024, 768, 1), (19, 8192, 64, 2),
+    (20, 64 * 1024, 512, 1), (20, 4096, 32, 1), (20, 8192, 128, 2), (21, 88 * 1024, 512, 1), (21, 4096, 64, 3),
 ])
 def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threads, parts):
     """Every work mapping of the delivery kernel (warp-flattened, thread per spike, warp per spike,
