@@ -15,8 +15,8 @@
 // reference's concepts, concepts.h:10-104), compiled with nvcc into GPU kernels by this header:
 //   neurons  stateless `SPICE_HD bool update(float dt, auto& rng) const` (one draw per neuron and
 //            step from the step's stream, the reference's order); stateful `SPICE_HD bool
-//            update(neuron&, float dt, auto& rng) const` with a nested `neuron` struct of 4-byte
-//            members.  A stateful model that declares `static constexpr int draws_per_update = n`
+//            update(neuron&, float dt, auto& rng) const` with a nested trivially copyable `neuron`
+//            struct (the members synapses add to are 4-byte floats).  A stateful model that declares `static constexpr int draws_per_update = n`
 //            draws n numbers per neuron and step from the step's stream in the reference's order
 //            (populations in add order, neurons ascending); without it its draws come from an
 //            independent stream per (population, neuron, step) (statistically uniform, not the
@@ -298,36 +298,44 @@ void set_word(N& n, int w, float f) {
 }
 template <class S, class N, class Deliver>
 bool probe_additive(Deliver&& deliver, deliver_probe& out, float syn_value_of_word, bool stateful) {
-	static_assert(sizeof(N) % 4 == 0, "a target neuron must be a struct of 4-byte members");
-	constexpr int words = (int)(sizeof(N) / 4);
-	N n{};
-	std::memset(static_cast<void*>(&n), 0, sizeof n);
-	deliver(n);
-	int changed = -1;
-	for (int w = 0; w < words; w++)
-		if (word_of(n, w) != 0.0f) {
-			if (changed >= 0) return false;
-			changed = w;
-		}
-	if (changed < 0) return false;
-	float const c = word_of(n, changed);
 	(void)syn_value_of_word;
 	(void)stateful;
-	float const xs[4] = {0.5f, -1.25f, 3.0e-3f, 1000.0f};
-	for (float x : xs) {  // the same member, now from x: x + c, one IEEE addition
-		N m{};
-		std::memset(static_cast<void*>(&m), 0, sizeof m);
-		set_word(m, changed, x);
-		deliver(m);
-		volatile float expect = x;
-		expect                = expect + c;
-		if (word_of(m, changed) != expect) return false;
+	constexpr int words = (int)(sizeof(N) / 4);
+	if constexpr (words == 0) {
+		return false;  // no float member to add to
+	} else {
+		auto same_tail = [](N const& a, N const& b) {  // the bytes after the last whole word
+			return std::memcmp(reinterpret_cast<char const*>(&a) + 4 * words, reinterpret_cast<char const*>(&b) + 4 * words,
+			                   sizeof(N) - 4 * words) == 0;
+		};
+		N zero{};
+		std::memset(static_cast<void*>(&zero), 0, sizeof zero);
+		N n = zero;
+		deliver(n);
+		if (!same_tail(n, zero)) return false;
+		int changed = -1;
 		for (int w = 0; w < words; w++)
-			if (w != changed && word_of(m, w) != 0.0f) return false;
+			if (word_of(n, w) != 0.0f) {
+				if (changed >= 0) return false;
+				changed = w;
+			}
+		if (changed < 0) return false;
+		float const c     = word_of(n, changed);
+		float const xs[4] = {0.5f, -1.25f, 3.0e-3f, 1000.0f};
+		for (float x : xs) {  // the same member, now from x: x + c, one IEEE addition
+			N m = zero;
+			set_word(m, changed, x);
+			deliver(m);
+			volatile float expect = x;
+			expect                = expect + c;
+			if (word_of(m, changed) != expect || !same_tail(m, zero)) return false;
+			for (int w = 0; w < words; w++)
+				if (w != changed && word_of(m, w) != 0.0f) return false;
+		}
+		out.dst_offset = 4 * changed;
+		out.constant   = c;
+		return true;
 	}
-	out.dst_offset = 4 * changed;
-	out.constant   = c;
-	return true;
 }
 
 #if defined(__CUDACC__)
@@ -730,8 +738,7 @@ public:
 			int id     = -1;
 			if constexpr (detail::has_neuron<Neur>) {
 				using N = typename Neur::neuron;
-				static_assert(std::is_trivially_copyable_v<N> && sizeof(N) % 4 == 0,
-				              "a user neuron must be a trivially copyable struct of 4-byte members");
+				static_assert(std::is_trivially_copyable_v<N>, "a user neuron must be a trivially copyable struct");
 				N const init{};
 				detail::check(spice_add_user_population(_net, size, 1, (int)sizeof(N), &init, &detail::user_launch<Neur>,
 				                                        model.get(), &id));

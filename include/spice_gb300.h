@@ -86,6 +86,17 @@ enum {
 	 * init = 1 when the synapse has a PerSynapseInit init() (the connection then consumes that
 	 * stream's seed, synapse_population.h:34-41, and the host sets the initial state). */
 	SPICE_SYNAPSE_USER_PLASTIC = 4,
+	/* USER_DELIVER: a synapse whose deliver() is arbitrary user code on the target neuron (and,
+	 * for the reference's DeliverFromTo concept, concepts.h:70-79, the source neuron): setting a
+	 * flag, taking a minimum, anything but adding one value to one float member.  Targets of such
+	 * synapses (stateful user populations) receive every input at the end of each step directly into
+	 * their neuron structs, connection by connection in connect order (snn.cpp:21-25), through the
+	 * kernels registered with spice_user_deliver; their other inputs (fixed_weight, weighted) are
+	 * added the same way by the engine; nets with them step in windows of one step.  params
+	 * {synapse_bytes (0: stateless), reads_source, init}: reads_source = 1 when deliver() takes the
+	 * source neuron; init = 1 when the synapse has a PerSynapseInit init() (the connection consumes
+	 * that stream's seed, and the host sets the initial state). */
+	SPICE_SYNAPSE_USER_DELIVER = 5,
 };
 
 /* Delivery modes. */
@@ -332,10 +343,12 @@ typedef struct spice_user_window {
 	int32_t* pull_koff;
 	uint64_t* hist;            /* target of plastic synapses: per neuron, bit j = spiked j steps ago;
 	                              shift in every step's spike bit (neuron_population.h:126-132) */
+	int direct;                /* 1: inputs arrive directly in the neuron structs (USER_DELIVER
+	                              targets): nothing to apply */
 } spice_user_window;
 typedef int (*spice_user_update_fn)(const spice_user_window* window, void* stream, void* ctx);
-/* stateful: neuron_bytes > 0 and init_neuron = the initial struct (copied to every neuron); the
- * population consumes a seed like every stateful population (neuron_population.h:56-60). */
+/* stateful: neuron_bytes > 0 (any struct size) and init_neuron = the initial struct (copied to every
+ * neuron); the population consumes a seed like every stateful population (neuron_population.h:56-60). */
 int spice_add_user_population(spice_net* net, int64_t size, int stateful, int neuron_bytes,
                               const void* init_neuron, spice_user_update_fn fn, void* ctx, int* pop_out);
 /* Registers a float member (byte offset) of a stateful user population as a synapse target field;
@@ -397,10 +410,44 @@ typedef struct spice_user_plastic_call {
 	unsigned long long* events;
 } spice_user_plastic_call;
 typedef int (*spice_user_plastic_fn)(const spice_user_plastic_call* call, void* stream, void* ctx);
+/* ---- User deliver() code (SPICE_SYNAPSE_USER_DELIVER) ----
+ * Called at the end of every step `time` >= delay - 1 for the spikes of step time - delay + 1
+ * (bitmap slot `hslot` of the source): every target whose sources spiked applies deliver() for
+ * each such synapse in ascending source order (a target's CSC column, col_pos[e] = the synapse's
+ * CSR index, its state's position) -- or, when deliver() reads source neurons of the target's own
+ * population, the spiking sources in ascending order each deliver along their CSR row
+ * (synapse_population.h:118-133), since a later source may read what an earlier delivery wrote.
+ * Adds the delivered synapses to *events. */
+#define SPICE_USER_DELIVER_ABI_VERSION 1
+typedef struct spice_user_deliver_call {
+	int version;
+	int64_t time;
+	float dt;
+	int hslot;
+	int64_t src_size, dst_size;
+	const int64_t* off;
+	const int32_t* nb;
+	const int64_t* col_off;
+	const int32_t* col_src;
+	const int64_t* col_pos;
+	const uint32_t* src_bits;
+	int src_nwords;
+	const void* src_state;     /* source neuron structs (stateful sources) */
+	void* dst_state;           /* target neuron structs */
+	void* synapse_state;       /* synapse structs, CSR order (stateful synapses), else NULL */
+	int same_population;       /* source population == target population */
+	unsigned long long* events;
+} spice_user_deliver_call;
+typedef int (*spice_user_deliver_fn)(const spice_user_deliver_call* call, void* stream, void* ctx);
+/* Registers the kernels of USER_DELIVER connection `conn` and its synapses' initial state
+ * (synapse_bytes bytes; NULL for stateless synapses), before the network first steps. */
+int spice_user_deliver(spice_net* net, int conn, spice_user_deliver_fn fn, void* ctx, const void* init_synapse);
+
 /* Registers the kernels of USER_PLASTIC connection `conn` and the initial state of every synapse
  * (synapse_bytes bytes), before the network first steps. */
 int spice_user_plastic(spice_net* net, int conn, spice_user_plastic_fn fn, void* ctx, const void* init_synapse);
-/* The whole per-synapse state array of a USER_PLASTIC connection, CSR order: set before the network
+/* The whole per-synapse state array of a USER_PLASTIC (or stateful USER_DELIVER) connection, CSR
+ * order: set before the network
  * first steps (a PerSynapseInit run on the host), read at any time (each synapse as of its last
  * catch-up, like the reference's synapse_population). */
 int spice_set_user_synapse_state(spice_net* net, int conn, const void* host_in);

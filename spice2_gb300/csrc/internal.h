@@ -95,6 +95,7 @@ struct PopDev {
 	float* pull_G;             // the active synapses' weights grouped by bin
 	int32_t* pull_koff;        // [size][nbins + 1] bin starts in the region; [i][0] = -1: not grouped,
 	                           // [i][1] = number of active synapses (the neuron walks pull_A)
+	int direct;                // USER_DELIVER target: inputs applied into the neuron structs at the end of each step
 };
 
 struct ConnDev {
@@ -181,6 +182,9 @@ struct Conn {
 	int ubytes       = 0;
 	int weight_word  = 0;
 	bool init_seed   = false;     // USER_PLASTIC with PerSynapseInit: consumes the init stream's seed
+	bool udeliver    = false;     // USER_DELIVER: deliver() is user code (spice_user_deliver)
+	bool reads_source = false;    // USER_DELIVER: deliver() takes the source neuron
+	int64_t* csc_pos = nullptr;   // CSR index of each CSC entry (USER_DELIVER with synapse state)
 	void* ufn        = nullptr;   // spice_user_plastic_fn
 	void* uctx       = nullptr;
 	std::vector<char> uinit;      // the initial synapse struct
@@ -279,6 +283,7 @@ struct spice_net {
 	// pull delivery (pull.cu)
 	bool pull_all = false;           // every stateful built-in population with inputs is pulled
 	bool any_pull = false;
+	bool any_direct = false;         // populations receiving USER_DELIVER synapses (windows of one step)
 	std::vector<spice_gb300::PullSet> pull_sets;
 	std::vector<spice_gb300::PullEvJob> pull_ev;
 	spice_gb300::PullSet* d_pull_sets = nullptr;

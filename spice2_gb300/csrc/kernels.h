@@ -48,8 +48,15 @@ cudaError_t init_synapse_weights(cudaStream_t stream, u128 seed, int64_t n, floa
 // CSC of a CSR (rows sources, ndst targets): col_off[ndst + 1], col_src[synapses] ascending per
 // column (CSR order among duplicates), col_w[synapses] = wts in CSC order when wts is not null.
 // Allocates and frees its own scratch; synchronises.
+// col_pos (when not null): the CSR index of each CSC entry.
 cudaError_t build_csc(cudaStream_t stream, const int64_t* off, const int32_t* nb, const float* wts, int64_t rows,
-                      int64_t ndst, int64_t synapses, int64_t* col_off, int32_t* col_src, float* col_w);
+                      int64_t ndst, int64_t synapses, int64_t* col_off, int32_t* col_src, float* col_w,
+                      int64_t* col_pos = nullptr);
+// A fixed_weight or weighted connection into a USER_DELIVER target: at the end of step `time`, every
+// target adds, in ascending source order, the weights of its synapses whose source spiked in bitmap
+// slot hslot, to the float at byte offset `field_offset` of its neuron struct.
+cudaError_t launch_direct_add(cudaStream_t stream, ConnDev const& c, int hslot, void* dst_state, int neuron_bytes,
+                              int field_offset, unsigned long long* events);
 // base[i] = sum over nconn column-start arrays (a device array of device pointers) of [i], i <= n.
 cudaError_t pull_region_bases(cudaStream_t stream, const int64_t* const* col_offs, int nconn, int64_t n, int64_t* base);
 

@@ -285,8 +285,8 @@ extern "C" int spice_add_user_population(spice_net* n, int64_t size, int statefu
 	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
 	if (size >= INT32_MAX) return pre_failed("topology.cpp:51", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
 	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
-	if (stateful && (neuron_bytes <= 0 || neuron_bytes % 4 || !init_neuron))
-		return fail(SPICE_EINVAL, "a stateful user model needs its neuron struct size (a multiple of 4) and initial value");
+	if (stateful && (neuron_bytes <= 0 || !init_neuron))
+		return fail(SPICE_EINVAL, "a stateful user model needs its neuron struct size and initial value");
 	Pop p{};
 	PopDev& d = p.d;
 	memset(&d, 0, sizeof d);
@@ -363,6 +363,19 @@ int parse_synapse(spice_net* n, int dst, int synapse, const float* params, int n
 		int const m = n->pops[dst].d.model;
 		if (m == USER ? (c.d.field < 0 || c.d.field >= n->pops[dst].nfields) : (c.d.field < 0 || c.d.field > 2 || (m == LIF && c.d.field != 0)))
 			return fail(SPICE_EINVAL, "the synapse's target field does not exist in the target neuron model");
+		return SPICE_OK;
+	} else if (synapse == SPICE_SYNAPSE_USER_DELIVER) {
+		if (np < 2 || !params) return fail(SPICE_EINVAL, "user deliver synapses need params {synapse_bytes, reads_source[, init]}");
+		if (n->pops[dst].d.model != USER || !n->pops[dst].stateful)
+			return fail(SPICE_EINVAL, "a synapse with its own deliver() code targets a stateful user population");
+		c.ubytes       = (int)params[0];
+		c.reads_source = params[1] != 0.0f;
+		c.init_seed    = np > 2 && params[2] != 0.0f;
+		if (c.ubytes < 0) return fail(SPICE_EINVAL, "synapse struct size must be >= 0");
+		c.d.plastic = 0;
+		c.d.weight  = 0.0f;
+		c.d.field   = 0;
+		c.udeliver  = true;
 		return SPICE_OK;
 	} else if (synapse == SPICE_SYNAPSE_WEIGHTED) {
 		if (np < 1 || !params) return fail(SPICE_EINVAL, "weighted needs params {wmax[, field[, source]]}");
@@ -627,13 +640,13 @@ int setup_tiles(spice_net* n, bool first) {
 		int tile        = n->tile_bytes / (4 * std::max(width, 1));
 		tile            = std::max(32, tile / 32 * 32);
 		d.tile          = tile;
-		d.ntiles        = (d.in_end > d.in_begin && d.size > 0 && !d.pull) ? (int)((d.size + tile - 1) / tile) : 0;
+		d.ntiles        = (d.in_end > d.in_begin && d.size > 0 && !d.pull && !d.direct) ? (int)((d.size + tile - 1) / tile) : 0;
 	}
 	for (auto& c : n->conns) {
 		ConnDev& d      = c.d;
 		PopDev const& T = n->pops[d.dst].d;
 		int64_t* bnd    = nullptr;
-		if (T.pull) continue;  // gathered by the pull kernel over the CSC: no tiles
+		if (T.pull || T.direct) continue;  // gathered over the CSC: no tiles
 		if (!first && d.bounds) {
 			CUDA_TRY(cudaStreamSynchronize(n->stream));
 			cudaFree((void*)d.bounds);
@@ -736,6 +749,86 @@ int setup_pull(spice_net* n) {
 	return SPICE_OK;
 }
 
+// USER_DELIVER targets: the CSC of every incoming connection (with CSR positions for synapse state)
+// and the user synapses' state.
+int setup_direct(spice_net* n) {
+	for (size_t ci = 0; ci < n->conns.size(); ci++) {
+		Conn& c = n->conns[ci];
+		if (!n->pops[c.d.dst].d.direct) continue;
+		if (c.reads_source && (n->pops[c.d.src].d.model != USER || !n->pops[c.d.src].stateful))
+			return fail(SPICE_EINVAL, "a deliver() that reads the source neuron needs a stateful user source population");
+		if (c.udeliver && c.ubytes > 0 && !c.csc_pos) {  // CSR positions: build this connection's CSC with them
+			int64_t* pos = nullptr;
+			TRY(dalloc(n, &pos, (size_t)std::max<int64_t>(c.synapses, 1), false));
+			c.csc_pos = pos;
+			if (c.d.csc_off) return fail(SPICE_ESTATE, "internal: CSC built without positions");
+			int64_t* off = nullptr;
+			int32_t* src = nullptr;
+			TRY(dalloc(n, &off, (size_t)c.d.dst_size + 1, false));
+			TRY(dalloc(n, &src, (size_t)std::max<int64_t>(c.synapses, 1), false));
+			CUDA_TRY(build_csc(n->stream, c.d.off, c.d.nb, nullptr, c.d.src_size, c.d.dst_size, c.synapses, off, src, nullptr, pos));
+			n->launches += 5;
+			c.d.csc_off = off;
+			c.d.csc_src = src;
+		}
+		TRY(ensure_csc(n, (int)ci));
+		if (c.udeliver && c.ubytes > 0 && !c.ustate) {
+			char* st = nullptr;
+			size_t const bytes = (size_t)std::max<int64_t>(c.synapses, 1) * c.ubytes;
+			TRY(dalloc(n, &st, bytes, false));
+			if (!c.uhost.empty()) {
+				CUDA_TRY(cudaMemcpy(st, c.uhost.data(), c.uhost.size(), cudaMemcpyHostToDevice));
+				c.uhost.clear();
+			} else {
+				std::vector<char> h(bytes);
+				for (size_t q = 0; q + c.ubytes <= bytes; q += c.ubytes) memcpy(h.data() + q, c.uinit.data(), c.ubytes);
+				CUDA_TRY(cudaMemcpy(st, h.data(), bytes, cudaMemcpyHostToDevice));
+			}
+			c.ustate = st;
+		}
+	}
+	return SPICE_OK;
+}
+
+// The deliveries into USER_DELIVER targets at the end of step n->time, connection by connection in
+// connect order (snn.cpp:21-25).
+int deliver_direct(spice_net* n) {
+	for (auto const& c : n->conns) {
+		PopDev const& T = n->pops[c.d.dst].d;
+		if (!T.direct || n->time < c.d.delay - 1) continue;
+		int const hs = (int)((n->time - c.d.delay + 1) % n->Hb);
+		if (c.udeliver) {
+			spice_user_deliver_call u;
+			memset(&u, 0, sizeof u);
+			u.version         = SPICE_USER_DELIVER_ABI_VERSION;
+			u.time            = n->time;
+			u.dt              = n->dt;
+			u.hslot           = hs;
+			u.src_size        = c.d.src_size;
+			u.dst_size        = c.d.dst_size;
+			u.off             = c.d.off;
+			u.nb              = c.d.nb;
+			u.col_off         = c.d.csc_off;
+			u.col_src         = c.d.csc_src;
+			u.col_pos         = c.csc_pos;
+			u.src_bits        = c.d.src_bits;
+			u.src_nwords      = c.d.src_nwords;
+			u.src_state       = n->pops[c.d.src].d.ustate;
+			u.dst_state       = T.ustate;
+			u.synapse_state   = c.ustate;
+			u.same_population = c.d.src == c.d.dst;
+			u.events          = n->d_events;
+			int const r = reinterpret_cast<spice_user_deliver_fn>(c.ufn)(&u, (void*)n->stream, c.uctx);
+			if (r != 0) return fail(SPICE_ECUDA, "the deliver() kernels of a user connection failed (" + std::to_string(r) + ")");
+		} else {
+			CUDA_TRY(launch_direct_add(n->stream, c.d, hs, T.ustate, T.ubytes, n->pops[c.d.dst].field_offset[c.d.field],
+			                           n->d_events));
+		}
+		n->launches++;
+	}
+	return SPICE_OK;
+}
+
 int prepare(spice_net* n) {
 	if (n->prepared) return SPICE_OK;
 	TRY(generate_pending(n));
@@ -755,6 +848,26 @@ int prepare(spice_net* n) {
 		if (delivers && n->mode != SPICE_MODE_ATOMIC)
 			return fail(SPICE_EINVAL, "plastic synapses that deliver per-synapse weights need SPICE_MODE_ATOMIC "
 			                          "(their per-step sums are order-dependent)");
+	}
+	// populations receiving user deliver() code get every input directly at the end of each step
+	n->any_direct = false;
+	for (int pi = 0; pi < np; pi++) {
+		n->pops[pi].d.direct = 0;
+		bool udel = false, plastic_in = false;
+		for (auto const& c : n->conns)
+			if (c.d.dst == pi) {
+				udel |= c.udeliver;
+				plastic_in |= c.d.plastic != 0;
+			}
+		if (!udel) continue;
+		if (plastic_in)
+			return fail(SPICE_EINVAL, "population " + std::to_string(pi) +
+			                              ": plastic synapses into a population with user deliver() code are not supported");
+		for (auto const& c : n->conns)
+			if (c.udeliver && !c.ufn)
+				return fail(SPICE_ESTATE, "a user deliver connection needs its kernels (spice_user_deliver) before the network steps");
+		n->pops[pi].d.direct = 1;
+		n->any_direct        = true;
 	}
 	// pulled populations: inputs with per-synapse weights, the pull knob, or (deterministic mode)
 	// more distinct input weights than the count replay keeps apart
@@ -777,7 +890,7 @@ int prepare(spice_net* n) {
 				last_of_field[c.d.field] = groups++;
 			}
 		}
-		if (!P.stateful || !has_in) continue;
+		if (!P.stateful || !has_in || P.d.direct) continue;
 		bool const pull = weighted_in || (P.d.model != USER && n->pull_all) ||
 		                  (P.d.model != USER && n->mode == SPICE_MODE_DETERMINISTIC && groups > kMaxGroups);
 		if (!pull) continue;
@@ -792,7 +905,7 @@ int prepare(spice_net* n) {
 	int K = kMaxWindow;
 	for (auto const& c : n->conns) K = std::min<int>(K, c.d.delay);
 	if (n->max_window > 0) K = std::min(K, n->max_window);
-	if (n->plastic) K = 1;
+	if (n->plastic || n->any_direct) K = 1;  // per-step catch-up, or deliveries at the end of each step
 	// the delivery kernel keeps a (step, connection) prefix of K * nconn entries in shared memory
 	if (!n->conns.empty()) K = std::min<int>(K, std::max<int>(1, 4096 / (int)n->conns.size()));
 	if (n->any_pull) K = std::min(K, kPullMaxWindow);  // step masks of 16 bits
@@ -830,7 +943,7 @@ int prepare(spice_net* n) {
 	for (int pi = 0; pi < np; pi++) {
 		PopDev& d = n->pops[pi].d;
 		if (!n->pops[pi].stateful) continue;
-		if (d.pull) {  // inputs are gathered by the pull kernel: no input ring
+		if (d.pull || d.direct) {  // inputs gathered by the pull kernel, or applied directly: no input ring
 			d.ngroups = 0;
 			d.W = d.F = 1;
 			continue;
@@ -984,6 +1097,11 @@ int prepare(spice_net* n) {
 	for (auto& c : n->conns)
 		if (c.d.plastic) c.d.dst_hist = n->pops[c.d.dst].d.hist;
 	if (n->any_pull) TRY(setup_pull(n));
+	for (size_t ci = 0; ci < n->conns.size(); ci++) {  // every connection: its source's bitmap ring
+		n->conns[ci].d.src_bits   = n->pops[n->conns[ci].d.src].d.bits;
+		n->conns[ci].d.src_nwords = n->pops[n->conns[ci].d.src].d.nwords;
+	}
+	if (n->any_direct) TRY(setup_direct(n));
 	TRY(dalloc(n, &n->d_counts, (size_t)2 * n->K * std::max(np, 1)));
 	TRY(dalloc(n, &n->d_pops, std::max(np, 1), false));
 	TRY(dalloc(n, &n->d_conns, std::max<size_t>(n->conns.size(), 1), false));
@@ -1089,6 +1207,7 @@ spice_user_window user_window(spice_net* n, int pi, WindowArgs const& wa, int64_
 	w.pull_G    = d.pull_G;
 	w.pull_koff = d.pull_koff;
 	w.hist      = d.hist;
+	w.direct    = d.direct;
 	return w;
 }
 
@@ -1365,6 +1484,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				TRY(ev_end(n, slot));
 				n->launches += 2;
 			}
+			if (n->any_direct) TRY(deliver_direct(n));  // windows of one step: the end of step n->time
 			if (!fused) CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear
 			if (record) {
 				RasterArgs ra{};
@@ -1914,11 +2034,25 @@ extern "C" int spice_user_plastic(spice_net* n, int conn, spice_user_plastic_fn 
 	return SPICE_OK;
 }
 
+extern "C" int spice_user_deliver(spice_net* n, int conn, spice_user_deliver_fn fn, void* ctx, const void* init_syn) {
+	if (!n || !fn) return fail(SPICE_EINVAL, "NULL argument");
+	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
+	Conn& c = n->conns[conn];
+	if (!c.udeliver) return fail(SPICE_EINVAL, "not a user deliver connection");
+	if (n->prepared) return fail(SPICE_ESTATE, "user deliver kernels are registered before the network first steps");
+	if (c.ubytes > 0 && !init_syn) return fail(SPICE_EINVAL, "a stateful synapse needs its initial state");
+	c.ufn  = (void*)fn;
+	c.uctx = ctx;
+	if (c.ubytes > 0) c.uinit.assign(static_cast<const char*>(init_syn), static_cast<const char*>(init_syn) + c.ubytes);
+	return SPICE_OK;
+}
+
 extern "C" int spice_set_user_synapse_state(spice_net* n, int conn, const void* in) {
 	if (!n || !in) return fail(SPICE_EINVAL, "NULL argument");
 	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
 	Conn& c = n->conns[conn];
-	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC) return fail(SPICE_EINVAL, "not a user plastic connection");
+	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC && !(c.udeliver && c.ubytes > 0))
+		return fail(SPICE_EINVAL, "not a connection of user synapse structs");
 	if (n->prepared) return fail(SPICE_ESTATE, "the initial synapse state is set before the network first steps");
 	TRY(generate_pending(n));
 	c.uhost.assign(static_cast<const char*>(in), static_cast<const char*>(in) + (size_t)c.synapses * c.ubytes);
@@ -1929,7 +2063,8 @@ extern "C" int spice_get_user_synapse_state(spice_net* n, int conn, void* out) {
 	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
 	if (conn < 0 || conn >= (int)n->conns.size()) return fail(SPICE_EINVAL, "connection id out of range");
 	Conn const& c = n->conns[conn];
-	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC) return fail(SPICE_EINVAL, "not a user plastic connection");
+	if (c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC && !(c.udeliver && c.ubytes > 0))
+		return fail(SPICE_EINVAL, "not a connection of user synapse structs");
 	TRY(prepare(n));
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
 	if (c.synapses > 0) CUDA_TRY(cudaMemcpy(out, c.ustate, (size_t)c.synapses * c.ubytes, cudaMemcpyDeviceToHost));

@@ -86,7 +86,7 @@ __global__ void k_csc_colscan(uint32_t* __restrict__ cnt, int64_t nblk, int64_t 
 __global__ void k_csc_fill(const int64_t* __restrict__ off, const int32_t* __restrict__ nb, const float* __restrict__ w,
                            int64_t rows, int64_t rows_per_blk, int64_t ndst, uint32_t* __restrict__ cnt,
                            const int64_t* __restrict__ col_off, int32_t* __restrict__ col_src,
-                           float* __restrict__ col_w) {
+                           float* __restrict__ col_w, int64_t* __restrict__ col_pos) {
 	int64_t const b  = blockIdx.x;
 	int64_t const r0 = b * rows_per_blk, r1 = min(rows, r0 + rows_per_blk);
 	uint32_t* c      = cnt + b * ndst;
@@ -103,6 +103,7 @@ __global__ void k_csc_fill(const int64_t* __restrict__ off, const int32_t* __res
 				int64_t const pos = col_off[d] + c[d] + rank;
 				col_src[pos]      = (int32_t)r;
 				if (w) col_w[pos] = w[e];
+				if (col_pos) col_pos[pos] = e;
 				last = e + 1 == e1 || nb[e + 1] != d;
 			}
 			__syncthreads();
@@ -354,10 +355,42 @@ __global__ void k_pull_apply_first(PopDev P) {
 	if (P.Gin) P.Gin[i] = v[2];
 }
 
+// A fixed_weight / weighted connection into a USER_DELIVER target, at the end of a step: thread per
+// target, ascending source order along its CSC column.
+__global__ void k_direct_add(const __grid_constant__ ConnDev C, int hslot, char* __restrict__ dst, int nbytes,
+                             int foff, unsigned long long* events) {
+	int64_t const j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	unsigned long long ev = 0;
+	if (j < C.dst_size) {
+		float* const x   = reinterpret_cast<float*>(dst + j * nbytes + foff);
+		float v          = *x;
+		const uint32_t* bits = C.src_bits + (int64_t)hslot * C.src_nwords;
+		for (int64_t e = C.csc_off[j]; e < C.csc_off[j + 1]; e++) {
+			int32_t const s = C.csc_src[e];
+			if ((bits[s >> 5] >> (s & 31)) & 1u) {
+				v = __fadd_rn(v, C.csc_w ? C.csc_w[e] : C.weight);
+				ev++;
+			}
+		}
+		*x = v;
+	}
+	for (int o = 16; o > 0; o >>= 1) ev += __shfl_down_sync(0xffffffffu, ev, o);
+	if ((threadIdx.x & 31) == 0 && ev) atomicAdd(events, ev);
+}
+
 }  // namespace
 
+cudaError_t launch_direct_add(cudaStream_t stream, ConnDev const& c, int hslot, void* dst_state, int neuron_bytes,
+                              int field_offset, unsigned long long* events) {
+	if (c.dst_size <= 0) return cudaSuccess;
+	k_direct_add<<<(unsigned)((c.dst_size + 255) / 256), 256, 0, stream>>>(c, hslot, static_cast<char*>(dst_state),
+	                                                                        neuron_bytes, field_offset, events);
+	return cudaGetLastError();
+}
+
 cudaError_t build_csc(cudaStream_t stream, const int64_t* off, const int32_t* nb, const float* wts, int64_t rows,
-                      int64_t ndst, int64_t synapses, int64_t* col_off, int32_t* col_src, float* col_w) {
+                      int64_t ndst, int64_t synapses, int64_t* col_off, int32_t* col_src, float* col_w,
+                      int64_t* col_pos) {
 	cudaError_t e = cudaMemsetAsync(col_off, 0, sizeof(int64_t) * (ndst + 1), stream);
 	if (e != cudaSuccess || synapses == 0 || rows == 0 || ndst == 0) return e;
 	// blocks of rows: at most 1024, and the count array at most 2^25 entries
@@ -378,7 +411,8 @@ cudaError_t build_csc(cudaStream_t stream, const int64_t* off, const int32_t* nb
 	}
 	if (e == cudaSuccess) e = scan_row_lengths(stream, indeg, ndst, col_off);
 	if (e == cudaSuccess) {
-		k_csc_fill<<<(unsigned)nblk, 256, 0, stream>>>(off, nb, wts, rows, rows_per_blk, ndst, cnt, col_off, col_src, col_w);
+		k_csc_fill<<<(unsigned)nblk, 256, 0, stream>>>(off, nb, wts, rows, rows_per_blk, ndst, cnt, col_off, col_src, col_w,
+		                                               col_pos);
 		e = cudaGetLastError();
 	}
 	if (e == cudaSuccess) e = cudaStreamSynchronize(stream);
