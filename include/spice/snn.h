@@ -16,7 +16,8 @@
 //   neurons  stateless `SPICE_HD bool update(float dt, auto& rng) const` (one draw per neuron and
 //            step from the step's stream, the reference's order); stateful `SPICE_HD bool
 //            update(neuron&, float dt, auto& rng) const` with a nested trivially copyable `neuron`
-//            struct (the members synapses add to are 4-byte floats).  A stateful model that declares `static constexpr int draws_per_update = n`
+//            struct (the members synapses add to are 4-byte floats).  A stateful model that
+//            declares `static constexpr int draws_per_update = n`
 //            draws n numbers per neuron and step from the step's stream in the reference's order
 //            (populations in add order, neurons ascending); without it its draws come from an
 //            independent stream per (population, neuron, step) (statistically uniform, not the
@@ -35,8 +36,12 @@
 //            skip(synapse&, dt, Int n), concepts.h:86-92) runs the reference's lazy catch-up
 //            (synapse_population.h:88-139) in kernels instantiated here over its type; its deliver()
 //            adds one float member of the synapse to the target (connecting one switches the net to
-//            atomic mode: per-step sums of per-synapse weights depend on the order).  deliver() that reads the source neuron
-//            (DeliverFromTo) is refused at compile time.
+//            atomic mode: per-step sums of per-synapse weights depend on the order).  Any other
+//            deliver() -- setting a flag, taking a minimum, or reading the source neuron
+//            (DeliverFromTo, concepts.h:70-79) -- runs as user code into a user-defined target at the
+//            end of each step (windows of one step), connection by connection in connect order, each
+//            target's synapses in ascending source order; a deliver() that reads neurons of its own
+//            target population runs in the reference's exact source-by-source order on one thread.
 // Arithmetic: user models compile under nvcc (-fmad=false recommended), not under the reference's
 // GCC -ffast-math, so a user model reproduces the reference bit for bit only where both compilers
 // evaluate its expressions the same way; the built-in models always do.
@@ -64,7 +69,7 @@
 
 #if defined(__CUDACC__)
 #include <cuda_runtime.h>
-// Marks a user model's update() / deliver() / init() for the GPU (and the host).
+// Marks a user model's update() / deliver() / skip() for the GPU (init() runs on the host).
 #define SPICE_HD __host__ __device__
 #else
 #define SPICE_HD
@@ -261,12 +266,35 @@ template <class S, class N>
 concept deliver_to_stateless = requires(S const t, N& n) { t.deliver(n); };
 template <class S, class N>
 concept deliver_to_stateful = has_synapse<S> && requires(S const t, typename S::synapse const& syn, N& n) { t.deliver(syn, n); };
+// DeliverFromTo (concepts.h:70-79): deliver() also reads the source neuron
+template <class S, class SrcN, class N>
+concept deliver_from_to = requires(S const t, SrcN const& s, N& n) { t.deliver(s, n); } ||
+                          (has_synapse<S> && requires(S const t, typename S::synapse const& syn, SrcN const& s, N& n) {
+	                          t.deliver(syn, s, n);
+                          });
 template <class>
 inline constexpr bool always_false = false;
 
 // The neuron struct of a target model (built-in or user).
 template <class M>
 using neuron_t = typename M::neuron;
+// The neuron struct of a source model, or a placeholder for a stateless source.
+template <class M, bool = has_neuron<M>>
+struct source_neuron {
+	using type = char;
+};
+template <class M>
+struct source_neuron<M, true> {
+	using type = typename M::neuron;
+};
+template <class M>
+using source_neuron_t = typename source_neuron<M>::type;
+// deliver() reads the source neuron: both models stateful, the DeliverFromTo form exists and the
+// DeliverTo form, which the reference prefers (synapse_population.h:118-132), does not
+template <class S, class SrcM, class DstM>
+concept delivers_from = has_neuron<SrcM> && has_neuron<DstM> &&
+                        deliver_from_to<S, typename SrcM::neuron, typename DstM::neuron> &&
+                        !deliver_to_stateless<S, typename DstM::neuron> && !deliver_to_stateful<S, typename DstM::neuron>;
 
 // A built-in target's field index for a byte offset into its neuron struct (lif: V; lif_cond: V, Gex,
 // Gin), or -1.
@@ -413,7 +441,8 @@ __global__ void __launch_bounds__(256) user_update_kernel(const spice_user_windo
 		}
 	};
 	auto apply = [&](int64_t slot, int k) {
-		if (w.pull) {
+		if (w.direct) {  // inputs arrive in the structs at the end of each step
+		} else if (w.pull) {
 			apply_pulled(k);
 		} else if (w.mode == SPICE_MODE_DETERMINISTIC) {
 			uint32_t* const wp = w.cnt + (slot * w.size + i) * w.W;
@@ -617,6 +646,79 @@ int user_plastic_launch(const spice_user_plastic_call* c, void* stream, void* ct
 	return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
+// One synapse's deliver(), in whichever of the reference's forms the synapse defines, the DeliverTo
+// form first (synapse_population.h:118-132).
+template <class Syn, class SrcN, class DstN>
+__device__ __forceinline__ void deliver_one(Syn const& syn, void* sst, int64_t pos, SrcN const* src, DstN& dst) {
+	if constexpr (has_synapse<Syn>) {
+		auto const& x = static_cast<typename Syn::synapse const*>(sst)[pos];
+		if constexpr (requires { syn.deliver(x, dst); }) syn.deliver(x, dst);
+		else syn.deliver(x, *src, dst);
+	} else {
+		if constexpr (requires { syn.deliver(dst); }) syn.deliver(dst);
+		else syn.deliver(*src, dst);
+	}
+}
+
+// User deliver() code, target-parallel: thread j applies, in ascending source order along its CSC
+// column, every synapse whose source spiked in bitmap slot hslot.
+template <class Syn, class SrcNeur, class DstNeur>
+__global__ void __launch_bounds__(256) user_deliver_targets(const spice_user_deliver_call c, const Syn syn) {
+	using SN = source_neuron_t<SrcNeur>;
+	using DN = neuron_t<DstNeur>;
+	int64_t const j = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+	unsigned long long ev = 0;
+	if (j < c.dst_size) {
+		DN d                 = static_cast<DN*>(c.dst_state)[j];
+		const uint32_t* bits = c.src_bits + (int64_t)c.hslot * c.src_nwords;
+		SN const* src        = static_cast<SN const*>(c.src_state);
+		for (int64_t e = c.col_off[j]; e < c.col_off[j + 1]; e++) {
+			int32_t const s = c.col_src[e];
+			if ((bits[s >> 5] >> (s & 31)) & 1u) {
+				deliver_one<Syn>(syn, c.synapse_state, c.col_pos ? c.col_pos[e] : 0, src ? src + s : nullptr, d);
+				ev++;
+			}
+		}
+		static_cast<DN*>(c.dst_state)[j] = d;
+	}
+	for (int o = 16; o > 0; o >>= 1) ev += __shfl_down_sync(0xffffffffu, ev, o);
+	if ((threadIdx.x & 31) == 0 && ev) atomicAdd(c.events, ev);
+}
+
+// User deliver() code that reads neurons of its own target population: the reference's order
+// exactly -- spiking sources ascending, each along its CSR row -- by one thread, so that a later
+// source reads what an earlier delivery wrote (synapse_population.h:118-133).
+template <class Syn, class SrcNeur, class DstNeur>
+__global__ void user_deliver_sequential(const spice_user_deliver_call c, const Syn syn) {
+	using SN = source_neuron_t<SrcNeur>;
+	using DN = neuron_t<DstNeur>;
+	if (blockIdx.x != 0 || threadIdx.x != 0) return;
+	const uint32_t* bits = c.src_bits + (int64_t)c.hslot * c.src_nwords;
+	SN const* src        = static_cast<SN const*>(c.src_state);
+	DN* dst              = static_cast<DN*>(c.dst_state);
+	unsigned long long ev = 0;
+	for (int w = 0; w < c.src_nwords; w++)
+		for (uint32_t x = bits[w]; x; x &= x - 1) {
+			int64_t const s = 32 * (int64_t)w + __ffs(x) - 1;
+			for (int64_t e = c.off[s]; e < c.off[s + 1]; e++) {
+				deliver_one<Syn>(syn, c.synapse_state, e, src + s, dst[c.nb[e]]);
+				ev++;
+			}
+		}
+	if (ev) atomicAdd(c.events, ev);
+}
+
+template <class Syn, class SrcNeur, class DstNeur>
+int user_deliver_launch(const spice_user_deliver_call* c, void* stream, void* ctx) {
+	Syn const& syn        = *static_cast<const Syn*>(ctx);
+	cudaStream_t const st = static_cast<cudaStream_t>(stream);
+	constexpr bool reads  = delivers_from<Syn, SrcNeur, DstNeur>;
+	if (reads && c->same_population) user_deliver_sequential<Syn, SrcNeur, DstNeur><<<1, 1, 0, st>>>(*c, syn);
+	else if (c->dst_size > 0)
+		user_deliver_targets<Syn, SrcNeur, DstNeur><<<(unsigned)((c->dst_size + 255) / 256), 256, 0, st>>>(*c, syn);
+	return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
 template <class Neur>
 int user_launch(const spice_user_window* w, void* stream, void* ctx) {
 	Neur const& neur  = *static_cast<const Neur*>(ctx);
@@ -788,22 +890,22 @@ public:
 	template <class Syn, class SrcNeur, class DstNeur>
 	int connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target,
 	            fixed_probability const& c, float delay, Syn syn = {}) {
-		plan const pl = plan_of<Syn, DstNeur>(syn, target);
+		plan const pl = plan_of<Syn, SrcNeur, DstNeur>(syn, target);
 		int id        = -1;
 		detail::check(spice_connect_fixed_probability(_net, source->id(), target->id(), c.p(), delay, pl.kind,
 		                                              pl.params.data(), (int)pl.params.size(), &id));
-		finish<Syn>(syn, id, pl);
+		finish<Syn, SrcNeur, DstNeur>(syn, id, pl);
 		return id;
 	}
 
 	template <class Syn, class SrcNeur, class DstNeur>
 	int connect(neuron_population<SrcNeur>* source, neuron_population<DstNeur>* target, adj_list const& c,
 	            float delay, Syn syn = {}) {
-		plan const pl = plan_of<Syn, DstNeur>(syn, target);
+		plan const pl = plan_of<Syn, SrcNeur, DstNeur>(syn, target);
 		int id        = -1;
 		detail::check(spice_connect_adj_list(_net, source->id(), target->id(), c.pairs().data(), c.size(), delay,
 		                                     pl.kind, pl.params.data(), (int)pl.params.size(), &id));
-		finish<Syn>(syn, id, pl);
+		finish<Syn, SrcNeur, DstNeur>(syn, id, pl);
 		return id;
 	}
 
@@ -831,6 +933,7 @@ private:
 		int kind = SPICE_SYNAPSE_FIXED_WEIGHT;
 		std::vector<float> params;
 		int weight_word = -1;  // host weights: word of the synapse struct delivered
+		bool user_deliver = false;  // deliver() runs as user code (SPICE_SYNAPSE_USER_DELIVER)
 	};
 
 	template <class DstNeur>
@@ -846,7 +949,7 @@ private:
 		}
 	}
 
-	template <class Syn, class DstNeur>
+	template <class Syn, class SrcNeur, class DstNeur>
 	plan plan_of(Syn const& syn, neuron_population<DstNeur>* target) {
 		plan pl;
 		if constexpr (detail::is_builtin_synapse<Syn>) {
@@ -855,15 +958,33 @@ private:
 			return pl;
 		} else {
 			using N = detail::neuron_t<DstNeur>;
-			if constexpr (detail::has_field<Syn>) {  // the member named by the synapse, its `weight`
+			// deliver() as user code on the target (and source) neuron structs, in the reference's order
+			auto user_code = [&](bool reads_source) {
+				if constexpr (detail::is_builtin_model<DstNeur>) {
+					throw std::logic_error("a synapse whose deliver() is not an addition of one value to one float member "
+					                       "targets user-defined neuron models only");
+				} else {
+					pl.kind = SPICE_SYNAPSE_USER_DELIVER;
+					if constexpr (detail::has_synapse<Syn>)
+						pl.params = {float(sizeof(typename Syn::synapse)), reads_source ? 1.0f : 0.0f,
+						             detail::per_synapse_init<Syn> ? 1.0f : 0.0f};
+					else
+						pl.params = {0.0f, reads_source ? 1.0f : 0.0f, 0.0f};
+					pl.user_deliver = true;
+				}
+				return pl;
+			};
+			if constexpr (!detail::is_builtin_model<SrcNeur> && !detail::is_builtin_model<DstNeur> &&
+			              detail::delivers_from<Syn, SrcNeur, DstNeur>) {
+				return user_code(true);
+			} else if constexpr (detail::has_field<Syn>) {  // the member named by the synapse, its `weight`
 				N probe{};
 				int const off = (int)(reinterpret_cast<char const*>(&(probe.*Syn::field)) - reinterpret_cast<char const*>(&probe));
 				pl.params     = {syn.weight, float(field_index(target, off))};
 				return pl;
 			} else if constexpr (detail::deliver_to_stateless<Syn, N>) {
 				detail::deliver_probe pr;
-				if (!detail::probe_additive<Syn, N>([&](N& n) { syn.deliver(n); }, pr, 0.0f, false))
-					throw std::logic_error("a synapse's deliver() must add one constant to one float member of the target neuron");
+				if (!detail::probe_additive<Syn, N>([&](N& n) { syn.deliver(n); }, pr, 0.0f, false)) return user_code(false);
 				pl.params = {pr.constant, float(field_index(target, pr.dst_offset))};
 				return pl;
 			} else if constexpr (detail::deliver_to_stateful<Syn, N>) {
@@ -891,9 +1012,13 @@ private:
 						}
 					}
 				}
-				if (wsel < 0)
-					throw std::logic_error("a stateful synapse's deliver() must add one float member of the synapse to one "
-					                       "float member of the target neuron");
+				if (wsel < 0) {
+					if constexpr (detail::plastic_synapse<Syn>)
+						throw std::logic_error("a plastic synapse's deliver() must add one float member of the synapse to one "
+						                       "float member of the target neuron");
+					else
+						return user_code(false);
+				}
 				int const f = field_index(target, pr.dst_offset);
 				if constexpr (detail::plastic_synapse<Syn>) {
 					pl.kind        = SPICE_SYNAPSE_USER_PLASTIC;
@@ -910,8 +1035,7 @@ private:
 				return pl;
 			} else {
 				static_assert(detail::always_false<Syn>,
-				              "deliver() that reads the source neuron (DeliverFromTo) is not supported: the engine "
-				              "delivers a window of spikes at once, when the source neurons have moved on");
+				              "the synapse's deliver() does not take the target population's neuron struct");
 				return pl;
 			}
 		}
@@ -919,8 +1043,28 @@ private:
 
 	// A stateful synapse with PerSynapseInit: its init() over the CSR in order, on the host, with the
 	// connection's init stream (synapse_population.h:34-41), and the delivered member as the weights.
-	template <class Syn>
+	template <class Syn, class SrcNeur, class DstNeur>
 	void finish(Syn const& syn, int id, plan const& pl) {
+		if (pl.user_deliver) {
+#if defined(__CUDACC__)
+			if constexpr (!detail::is_builtin_model<DstNeur>) {
+				static_assert(std::is_trivially_copyable_v<Syn>, "a user synapse model must be trivially copyable");
+				auto model = std::make_shared<Syn>(syn);
+				_models.push_back(model);
+				if constexpr (detail::has_synapse<Syn>) {
+					using S = typename Syn::synapse;
+					S const init{};
+					detail::check(spice_user_deliver(_net, id, &detail::user_deliver_launch<Syn, SrcNeur, DstNeur>, model.get(), &init));
+					if constexpr (detail::per_synapse_init<Syn>) host_synapse_init<Syn>(syn, id);
+				} else {
+					detail::check(spice_user_deliver(_net, id, &detail::user_deliver_launch<Syn, SrcNeur, DstNeur>, model.get(), nullptr));
+				}
+			}
+#else
+			throw std::logic_error("synapses with their own deliver() code run as GPU kernels: compile with nvcc");
+#endif
+			return;
+		}
 		if constexpr (detail::plastic_synapse<Syn>) {
 #if defined(__CUDACC__)
 			using S = typename Syn::synapse;
@@ -972,6 +1116,25 @@ private:
 			(void)id;
 			(void)pl;
 		}
+	}
+
+	// A synapse type's init(synapse&, src, dst, rng) over the CSR in order with the connection's
+	// PerSynapseInit stream (synapse_population.h:34-41): the whole state array, to the engine.
+	template <class Syn>
+	void host_synapse_init(Syn const& syn, int id) {
+		using S = typename Syn::synapse;
+		int64_t src = 0, nsyn = 0;
+		detail::check(spice_conn_size(_net, id, &src, &nsyn));
+		std::vector<int64_t> off((size_t)src + 1);
+		std::vector<int32_t> nb((size_t)std::max<int64_t>(nsyn, 1));
+		detail::check(spice_get_csr(_net, id, off.data(), nb.data()));
+		uint64_t seeds[4];
+		detail::check(spice_connection_seeds(_net, id, seeds));
+		util::xoroshiro64_128p rng{seeds[2], seeds[3]};
+		std::vector<S> st((size_t)std::max<int64_t>(nsyn, 1));
+		for (int64_t s = 0; s < src; s++)
+			for (int64_t e = off[s]; e < off[s + 1]; e++) syn.init(st[e], s, nb[e], rng);
+		detail::check(spice_set_user_synapse_state(_net, id, st.data()));
 	}
 
 	spice_net* _net = nullptr;

@@ -127,18 +127,20 @@ def _reference_samples_dir():
 
 
 @pytest.mark.skipif(_reference_samples_dir() is None, reason="the reference's sources are not on this machine")
-@pytest.mark.parametrize("sample", ["brunel", "brunel+", "vogels"])
+@pytest.mark.parametrize("sample", ["brunel", "brunel+", "vogels", "ping_pong", "sssp"])
 def test_reference_samples_compile_against_the_header(engine, tmp_path, sample):
     """The reference's own sample programs, with SPICE_HD added in front of their models' update(),
-    deliver(), skip() and init() and nothing else changed, compile with nvcc against
+    deliver() and skip() and nothing else changed, compile with nvcc against
     include/spice/snn.h and spice2_gb300/examples/matplot.h (their output stream) and link against
-    the engine: the reference's user API, model concepts and integer names are all there."""
+    the engine: the reference's user API, model concepts and integer names are all there.  init()
+    runs on the host in this engine (sssp's reads a host array), so it stays unannotated; ping_pong
+    and sssp deliver through deliver() functors that set flags and take minima."""
     import re
     nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not found")
     src = open(os.path.join(_reference_samples_dir(), sample + ".cpp")).read()
-    annotated = re.sub(r"^(\s*)(bool|void) (update|deliver|skip|init)\(", r"\1SPICE_HD \2 \3(", src, flags=re.M)
+    annotated = re.sub(r"^(\s*)(bool|void) (update|deliver|skip)\(", r"\1SPICE_HD \2 \3(", src, flags=re.M)
     assert annotated.count("SPICE_HD") >= 2
     f = tmp_path / (sample.replace("+", "_plus") + ".cu")
     f.write_text(annotated)
