@@ -464,6 +464,19 @@ def run_reference_brunel_ck(N: int, p: float, seed: int, steps: int, block: int)
     return np.concatenate(counts).copy(), np.array(blocks, dtype=np.uint64)
 
 
+def run_reference_plastic_ei(N: int, seed: int, steps: int, eta: float = 1e-3):
+    """Runs the plastic E/I network on oracle/_ref/ref_driver (plastic_ei): returns (counts[steps][2]
+    int32 spike counts of E and I, isi[2][3] pooled inter-spike interval count / sum / sum of
+    squares in steps, (build seconds, run seconds))."""
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "pe.bin")
+        subprocess.run([REF_DRIVER, "plastic_ei", str(N), str(seed), str(steps), repr(eta), out], check=True)
+        buf = open(out, "rb").read()
+    counts = np.frombuffer(buf, dtype=np.int32, count=2 * steps).reshape(steps, 2).copy()
+    rest = np.frombuffer(buf, dtype=np.float64, offset=8 * steps).copy()
+    return counts, rest[:6].reshape(2, 3), (float(rest[6]), float(rest[7]))
+
+
 def run_reference_gen(src: int, dst: int, p: float, seed: int):
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "g.bin")

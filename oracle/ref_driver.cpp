@@ -20,6 +20,13 @@
 //                                (int32 x 3) and, per block of BLOCK steps, the raster checksum of
 //                                the block and the E and I state checksums at its end (uint64 x 3);
 //                                the checksums are oracle.raster_checksum / state_checksum
+//   ref_driver plastic_ei N SEED STEPS ETA OUT
+//                                the plastic E/I network (conductance LIF, N/5 inhibitory; E->E,
+//                                E->I excitatory 0.03, I->I inhibitory 0.3, I->E the iSTDP synapse
+//                                below from W 0.3, all fixed_probability(0.02), delay 1 step,
+//                                dt 1e-4): per step the spike count of E and I (int32 x 2), then per
+//                                population the pooled inter-spike intervals in steps (count, sum,
+//                                sum of squares: double x 3), then the build and run seconds
 //
 // SPEC (text):  dt max_delay seed steps dump_csr
 //               pop poisson SIZE RATE | pop lif SIZE | pop lif_cond SIZE
@@ -199,6 +206,43 @@ struct stdp_syn {
 	}
 };
 
+// Inhibitory symmetric STDP (Vogels et al. 2011) against the PlasticSynapse concept: at a pre
+// spike W += eta (xpost - 2 rho0 tau), floored at 0; at a post spike W += eta xpre; the traces jump
+// by 1 and decay by x -= x dt / tau per step, skip(n) multiplies them by (1 - dt / tau)^n.
+struct istdp {
+	float eta, alpha, tau_inv;
+	struct synapse {
+		float W = 0.3f;
+		float A = 0;
+		float B = 0;
+	};
+	void deliver(synapse const& s, lif_cond::neuron& to) const { to.Gin += s.W; }
+	void update(synapse& s, float const dt, bool const pre, bool const post) const {
+		if (pre) s.W = std::max(0.0f, s.W + eta * (s.B - alpha));
+		if (post) s.W += eta * s.A;
+		s.A += pre;
+		s.B += post;
+		s.A -= s.A * (dt * tau_inv);
+		s.B -= s.B * (dt * tau_inv);
+	}
+	void skip(synapse& s, float const dt, Int const n) const {
+		s.A *= std::pow(1 - dt * tau_inv, n);
+		s.B *= std::pow(1 - dt * tau_inv, n);
+	}
+};
+
+// A plastic synapse that is never built (p = 0): connecting it from a population makes the
+// reference keep that population's spike history (snn.h:44-45), which the catch-up of a plastic
+// connection INTO the population reads (snn.cpp:17-25 pass c.to->history()).
+struct history_only {
+	struct synapse {
+		float W = 0;
+	};
+	void deliver(synapse const&, lif_cond::neuron&) const {}
+	void update(synapse&, float, bool, bool) const {}
+	void skip(synapse&, float, Int) const {}
+};
+
 std::vector<float> g_dt;
 struct dt_probe {
 	bool update(float dt, auto&) const {
@@ -323,6 +367,53 @@ static int run_brunel_ck(int argc, char** argv) {
 			ck = raster_ck{};
 		}
 	}
+	fclose(f);
+	return 0;
+}
+
+static int run_plastic_ei(int argc, char** argv) {
+	if (argc < 7) return 2;
+	Int const N = atoll(argv[2]);
+	unsigned const seed = (unsigned)atoll(argv[3]);
+	Int const steps = atoll(argv[4]);
+	float const eta = (float)atof(argv[5]);
+	float const dt = 1e-4f;
+	auto t0 = std::chrono::steady_clock::now();
+	snn net(dt, dt, {seed});
+	auto* E = net.add_population<lif_cond>(N * 8 / 10);
+	auto* I = net.add_population<lif_cond>(N * 2 / 10);
+	net.connect<excitatory>(E, E, fixed_probability(0.02), dt, {0.03f});
+	net.connect<excitatory>(E, I, fixed_probability(0.02), dt, {0.03f});
+	net.connect<istdp>(I, E, fixed_probability(0.02), dt, {eta, 2.0f * 5.0f * 0.02f, 1.0f / 0.02f});
+	net.connect<inhibitory>(I, I, fixed_probability(0.02), dt, {0.3f});
+	net.connect<history_only>(E, E, fixed_probability(0.0), dt);
+	auto t1 = std::chrono::steady_clock::now();
+	FILE* f = fopen(argv[6], "wb");
+	if (!f) return 2;
+	detail::NeuronPopulation* pops[2] = {E, I};
+	std::vector<Int> last[2] = {std::vector<Int>(E->size(), -1), std::vector<Int>(I->size(), -1)};
+	double isi[2][3] = {};
+	for (Int t = 0; t < steps; t++) {
+		net.step();
+		for (int k = 0; k < 2; k++) {
+			auto sp = pops[k]->spikes(0);
+			put(f, (Int32)sp.size());
+			for (Int32 x : sp) {
+				if (last[k][x] >= 0) {
+					double const d = double(t - last[k][x]);
+					isi[k][0] += 1;
+					isi[k][1] += d;
+					isi[k][2] += d * d;
+				}
+				last[k][x] = t;
+			}
+		}
+	}
+	auto t2 = std::chrono::steady_clock::now();
+	for (int k = 0; k < 2; k++)
+		for (int j = 0; j < 3; j++) put(f, isi[k][j]);
+	put(f, std::chrono::duration<double>(t1 - t0).count());
+	put(f, std::chrono::duration<double>(t2 - t1).count());
 	fclose(f);
 	return 0;
 }
@@ -504,6 +595,7 @@ int main(int argc, char** argv) {
 		if (!strcmp(argv[1], "rng")) return run_rng(argc, argv);
 		if (!strcmp(argv[1], "bcsr")) return run_bcsr(argc, argv);
 		if (!strcmp(argv[1], "brunel_ck")) return run_brunel_ck(argc, argv);
+		if (!strcmp(argv[1], "plastic_ei")) return run_plastic_ei(argc, argv);
 	} catch (std::exception const& e) {
 		fprintf(stderr, "%s\n", e.what());
 		return 3;

@@ -2847,7 +2847,13 @@ cudaError_t launch_batch_deliver(cudaStream_t stream, BatchArgs const& b, int k,
 		case 37: k_batch_deliver<1, 18><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 38: k_batch_deliver<0, 19><<<grid, threads, b.smem_bytes, stream>>>(b); break;
 		case 39: k_batch_deliver<1, 19><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 40: k_batch_deliver<0, 20><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 41: k_batch_deliver<1, 20><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 42: k_batch_deliver<0, 21><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		case 43: k_batch_deliver<1, 21><<<grid, threads, b.smem_bytes, stream>>>(b); break;
+		default: return cudaErrorInvalidValue;  // a delivery mapping without a batched kernel
 	}
+	static_assert(kDeliverFns == 44, "every delivery mapping has a case above");
 	return cudaGetLastError();
 }
 

@@ -26,9 +26,13 @@ headers) compiled by oracle/Makefile with the reference's Release flags -- and s
   vogels_c3_n10000.npz       the plastic E/I network's neurons and static weights without plasticity
                              (N=1e4 conductance LIF, p=0.02, E 0.03 / I 0.3, delay 1 step, seed 7),
                              1000 steps: raster and final state
+  plastic_ei_n100000.npz     the plastic E/I network (N=1e5 conductance LIF, p=0.02, iSTDP on I->E,
+                             eta 1e-3, delay 1 step) for seeds 1..10, 5000 steps each: per-step spike
+                             counts of E and I and the pooled inter-spike interval sums (compared
+                             statistically: the GPU's atomic-mode sums make the dynamics diverge)
 
 usage: python tests/golden/make_golden.py [GROUP ...]   (needs the reference sources; run from the
-       repo root; groups: base, vogels, weighted, brunel_plus, brunel_long; default: all)
+       repo root; groups: base, vogels, weighted, brunel_plus, brunel_long, plastic_ei; default: all)
 """
 from __future__ import annotations
 
@@ -122,7 +126,20 @@ def brunel_long_fixtures():
     np.savez_compressed(os.path.join(HERE, "brunel_n500000_long.npz"), **arrs)
 
 
-def main(groups=("base", "vogels", "weighted", "brunel_plus", "brunel_long")):
+def plastic_ei_fixtures(N: int = 100000, steps: int = 5000, seeds=range(1, 11), eta: float = 1e-3):
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max(1, min(len(seeds), (os.cpu_count() or 2) - 2))) as ex:
+        res = list(ex.map(lambda sd: O.run_reference_plastic_ei(N, sd, steps, eta), seeds))
+    arrs = {"meta": np.array([N, steps]), "eta": np.array([eta])}
+    for sd, (counts, isi, secs) in zip(seeds, res):
+        arrs[f"counts_s{sd}"] = counts
+        arrs[f"isi_s{sd}"] = isi
+        arrs[f"seconds_s{sd}"] = np.array(secs)
+        print("seed", sd, "spikes", counts.sum(0), "run seconds", round(secs[1], 1), flush=True)
+    np.savez_compressed(os.path.join(HERE, "plastic_ei_n100000.npz"), **arrs)
+
+
+def main(groups=("base", "vogels", "weighted", "brunel_plus", "brunel_long", "plastic_ei")):
     if not O.have_reference():
         O.build(with_reference=True, reference_dir=os.environ.get("SPICE_REFERENCE_DIR", "/root/reference"))
     if "vogels" in groups:
@@ -133,6 +150,8 @@ def main(groups=("base", "vogels", "weighted", "brunel_plus", "brunel_long")):
         brunel_plus_fixtures()
     if "brunel_long" in groups:
         brunel_long_fixtures()
+    if "plastic_ei" in groups:
+        plastic_ei_fixtures()
     if "base" not in groups:
         print("golden fixtures written to", HERE)
         return
@@ -192,4 +211,4 @@ def main(groups=("base", "vogels", "weighted", "brunel_plus", "brunel_long")):
 
 
 if __name__ == "__main__":
-    main(tuple(sys.argv[1:]) or ("base", "vogels", "weighted", "brunel_plus", "brunel_long"))
+    main(tuple(sys.argv[1:]) or ("base", "vogels", "weighted", "brunel_plus", "brunel_long", "plastic_ei"))

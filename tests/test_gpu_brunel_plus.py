@@ -59,9 +59,10 @@ def test_brunel_plus_rates_match_the_reference(gpu_runs):
 
 
 def test_brunel_plus_weights_stay_in_bounds_and_move(gpu_runs):
-    """The rule clamps W to [0, 3e-4]; E->E synapses start at 1e-4 and plasticity moves them."""
+    """The rule clamps W to [0, 0.0003f] (the float nearest 3e-4, a little above it); E->E synapses
+    start at 1e-4 and plasticity moves them."""
     for sd in SEEDS:
         r = gpu_runs[sd]
         assert r["synapses"] > 3_000_000
-        assert 0.0 <= r["W_min"] and r["W_max"] <= 3e-4 + 1e-12
+        assert 0.0 <= r["W_min"] and np.float32(r["W_max"]) <= np.float32(3e-4)
         assert abs(r["W_mean"] - 1e-4) > 1e-7 and r["W_std"] > 0
