@@ -140,20 +140,22 @@ def test_plastic_ei_network_matches_the_reference_over_ten_seeds(engine):
 
 
 def test_istdp_moves_the_excitatory_rate_toward_rho0(engine):
-    """With a learning rate that acts within seconds (eta 0.05), iSTDP lowers the I->E weights while
-    E fires below rho0 = 5 Hz: the E rate rises toward 5 Hz and the weights fall."""
+    """The plastic E/I network at N=1e5 with a learning rate that acts within seconds (eta 0.05):
+    after the opening burst E fires far below rho0 = 5 Hz, so iSTDP depresses the I->E weights
+    and the E rate climbs toward 5 Hz over 4 s of simulated time (the oracle's run of the same
+    network: 0.5 Hz after the burst, 1.6 Hz after 3.5 s, 3.5 Hz after 4 s; weights 0.336 -> 0.305)."""
     sp = engine
-    N = 20000
+    N = 100000
     net, E, I, c = _plastic_ei_c3(sp, N, 3, eta=0.05)
     rates, wmean = [], []
-    for _ in range(8):
-        raster = net.run_record(2500, capacity=2500 * 200 + 4096)
+    for _ in range(16):
+        raster = net.run_record(2500, capacity=2500 * 2000 + 4096)
         rates.append(sum(len(r[0]) for r in raster) / (N * 0.8) / 0.25)
         wmean.append(float(net.synapse_state(c, 0).mean()))
     net.close()
-    assert rates[0] < 4.0, rates
-    assert abs(rates[-1] - 5.0) < 0.5 * abs(rates[0] - 5.0), rates
-    assert wmean[-1] < wmean[0], wmean
+    early, late = np.mean(rates[1:4]), np.mean(rates[-4:])
+    assert early < 1.5 and late > 2 * early, rates
+    assert wmean[-1] < wmean[1] - 0.015, wmean
 
 
 def test_trace_decay_rounding_matches_double_multiply(engine):
