@@ -186,6 +186,17 @@ enum {
 	                                   weights (the push path replays per-weight event counts).
 	                                   Nets with pulled populations step in windows of at most
 	                                   16 steps and need max_delay <= 64 steps             */
+	SPICE_TUNE_PERSISTENT      = 10, /* 1 (default): a network whose windows are one step long
+	                                   (plastic connections, a minimum delay of one step) runs
+	                                   each chunk of up to 1024 steps as one cooperative launch,
+	                                   the phases of a step (neuron update and sources; the
+	                                   periodic plastic catch-up; deliveries and raster)
+	                                   separated by grid-wide barriers (2 .. 32: the same with
+	                                   that many CTAs per SM, default 4); 0: one launch per phase.
+	                                   Taken into account when the network first steps (it sets
+	                                   the input ring up for accumulation); after that it can be
+	                                   switched off and on.  Not used with user models, pulled
+	                                   populations or user deliver() code                      */
 	SPICE_TUNE_NEURON_VARIANT  = 6, /* LIF window of the neuron update: 0 unrolled steps, input
 	                                   words in registers, 1 rolled steps over words parked in
 	                                   shared memory, 2 as 1 with warp-uniform count replay,

@@ -366,12 +366,16 @@ class snn:
     def set_tuning(self, tile_bytes: int | None = None, deliver_threads: int | None = None,
                    deliver_parts: int | None = None, deliver_algo: int | None = None,
                    overlap_sources: bool | None = None, neuron_variant: int | None = None,
-                   launch_mode: int | None = None, pull: bool | None = None, source_steps: int | None = None):
+                   launch_mode: int | None = None, pull: bool | None = None, source_steps: int | None = None,
+                   persistent: bool | None = None):
         """Delivery launch shape and neuron-update variant (any time between steps); results are
         independent of them.  pull (before the network first steps): deliver every stateful
         population by the pull path over the CSC adjacency (SPICE_TUNE_PULL)."""
         if pull is not None:
             _check(lib().spice_set_tuning(self._h, 8, int(bool(pull))))
+        if persistent is not None:  # one cooperative launch per chunk of one-step windows (SPICE_TUNE_PERSISTENT;
+            # an int >= 2: CTAs per SM)
+            _check(lib().spice_set_tuning(self._h, 10, int(persistent)))
         if source_steps is not None:  # steps per Poisson source CTA (default 1; 0: one-wave grid)
             _check(lib().spice_set_tuning(self._h, 9, int(source_steps)))
         if tile_bytes is not None:

@@ -277,6 +277,14 @@ struct spice_net {
 	int neuron_variant  = 0;         // LIF window variant of the neuron update (tunable)
 	int launch_mode     = 1;         // 1: neurons and sources in one grid, programmatic dependent launches
 	int src_steps       = 1;         // steps per Poisson CTA (0: the fewest that fit the grid in one wave)
+	// persistent steps (step.cu k_persist): windows of one step, one cooperative launch per chunk
+	int persist_knob    = 1;         // SPICE_TUNE_PERSISTENT
+	bool persist_ok     = false;     // eligible when prepared (the input ring accumulates)
+	int persist_grid    = 0;         // resident CTAs over all SMs
+	unsigned* d_barrier = nullptr;   // arrival counter of the grid barriers
+	int* d_pstatus      = nullptr;   // nonzero: a barrier wait gave up
+	int* h_pstatus      = nullptr;   // pinned copy, read after the chunk's event
+	std::vector<int64_t> persist_chunks;  // per connection: delivery units per spike
 	int sm_count        = 1;
 	int dmin = 1, dmax = 1;          // connection delays in steps
 	bool plastic = false;            // any plastic connection (windows of one step)

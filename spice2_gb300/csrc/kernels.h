@@ -220,6 +220,39 @@ struct RasterArgs {
 };
 cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a);
 
+// Persistent steps (step.cu): every step of a chunk of a network whose windows are one step long
+// in one cooperative launch, the phases of a step separated by grid-wide barriers.
+constexpr int kPersistThreads = kNeuronThreads;  // the window bodies' CTA size
+constexpr int kPersistChunk   = 256;             // synapses of one delivery work unit (a warp's)
+constexpr int kPersistBlocksPerSM = 4;           // default CTAs per SM (fewer barrier arrivals)
+struct PersistArgs {
+	int64_t t0;             // first step of the launch
+	int nsteps;
+	int parity0;            // counts / list half of step t0
+	int D, Hb, npop, nconn, mode;
+	const PopDev* pops;
+	const ConnDev* conns;   // any order (deliveries of one step commute)
+	const float* dts;       // dt of steps t0 .. t0 + nsteps - 1
+	const u128* tables;     // their jump tables (kJumpTable each; null without Poisson draws)
+	int32_t* counts;        // [2][npop] spikes per step, per parity
+	unsigned long long* events;
+	unsigned* barrier;      // arrival counter, zero at launch
+	int* status;            // set nonzero when a barrier wait gave up (results then invalid)
+	int any_plastic;
+	int nblk;                     // CTA-sized work items of the update phase
+	int blk_begin[kMaxPops + 1];  // per population: first work item
+	int blk_kind[kMaxPops];       // as WindowArgs::blk_kind
+	int blk_per_step[kMaxPops];   // Poisson: items per step
+	int64_t ext_pos[kMaxPops];    // external: train position of step t0
+	int64_t chunks[kMaxConns];    // per connection: delivery units per spike (ceil(max row / kPersistChunk))
+	int record;                   // extract the raster of every step (RasterArgs below, K = 1)
+	int rec_parity0;              // raster base parity of step t0
+	RasterArgs raster;
+};
+// blocks_per_sm: resident CTAs of the persistent kernel per SM (0: query only).
+cudaError_t persist_occupancy(int mode, int* blocks_per_sm);
+cudaError_t launch_persist(cudaStream_t stream, PersistArgs const& a, int grid);
+
 // ---- batched networks (step.cu kernels, batch.cu runtime) ----
 // The window a batch's kernels step, advanced on the device by k_batch_prologue.
 struct BatchClock {

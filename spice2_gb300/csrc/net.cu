@@ -217,6 +217,7 @@ extern "C" int spice_net_destroy(spice_net* n) {
 	if (n->h_raster) cudaFreeHost(n->h_raster);
 	if (n->h_rcounts) cudaFreeHost(n->h_rcounts);
 	if (n->h_seeds) cudaFreeHost(n->h_seeds);
+	if (n->h_pstatus) cudaFreeHost(n->h_pstatus);
 	for (auto e : n->ev_pool) cudaEventDestroy(e);
 	if (n->stream_src) {
 		cudaStreamSynchronize(n->stream_src);
@@ -634,8 +635,9 @@ int setup_tiles(spice_net* n, bool first) {
 				mixed |= n->conns[ci].d.plastic != 0;  // plastic deliveries add into the ring
 			}
 		d.in_end      = (int)by_dst.size();
-		// slots are overwritten by one delivery CTA unless delays differ or tiles are split
-		d.zero_inputs = (mixed || n->deliver_parts > 1) ? 1 : 0;
+		// slots are overwritten by one delivery CTA unless delays differ, tiles are split or the
+		// persistent steps deliver (they add into the ring)
+		d.zero_inputs = (mixed || n->deliver_parts > 1 || n->persist_ok) ? 1 : 0;
 		int const width = n->mode == SPICE_MODE_DETERMINISTIC ? d.W : d.F;
 		int tile        = n->tile_bytes / (4 * std::max(width, 1));
 		tile            = std::max(32, tile / 32 * 32);
@@ -913,6 +915,20 @@ int prepare(spice_net* n) {
 	// bitmaps: the last D steps for spikes(age), and two windows in flight (sources run ahead);
 	// the pull reads the D steps before the next window while sources may already write it
 	n->Hb = (int)std::max<int64_t>(D, 2 * n->K) + 1 + (n->any_pull ? n->K : 0);
+	// persistent steps: windows of one step, built-in models and synapses, pushed deliveries
+	n->persist_ok = n->persist_knob != 0 && n->K == 1 && !n->any_pull && !n->any_direct &&
+	                np <= kMaxPops && n->conns.size() <= (size_t)kMaxConns;
+	for (auto const& p : n->pops) n->persist_ok &= p.d.model != USER;
+	for (auto const& c : n->conns)
+		n->persist_ok &= !c.weighted && !c.udeliver && c.d.plastic != SPICE_SYNAPSE_USER_PLASTIC;
+	if (n->persist_ok) {
+		int coop = 0, sms = 0, per_sm = 0;
+		CUDA_TRY(cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, n->device));
+		CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, n->device));
+		CUDA_TRY(persist_occupancy(n->mode == SPICE_MODE_DETERMINISTIC ? 0 : 1, &per_sm));
+		n->persist_grid = sms * per_sm;  // the most resident CTAs (the knob may ask for fewer per SM)
+		n->persist_ok   = coop != 0 && n->persist_grid > 0;
+	}
 	// draw offsets in the step's shared stream (populations in add order, snn.cpp:14-15)
 	int64_t draws = 0;
 	for (auto& p : n->pops) {
@@ -1120,6 +1136,24 @@ int prepare(spice_net* n) {
 	}
 	n->run_cap = kRunCap;
 	CUDA_TRY(cudaDeviceGetAttribute(&n->sm_count, cudaDevAttrMultiProcessorCount, n->device));
+	if (n->persist_ok) {  // delivery units: a warp and at most kPersistChunk synapses of one row
+		n->persist_chunks.assign(n->conns.size(), 1);
+		for (size_t ci = 0; ci < n->conns.size(); ci++) {
+			ConnDev const& d = n->conns[ci].d;
+			int64_t mr = d.max_row;
+			if (!d.plastic && d.src_size > 0) {
+				std::vector<int64_t> off((size_t)d.src_size + 1);
+				CUDA_TRY(cudaMemcpy(off.data(), d.off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost));
+				mr = 0;
+				for (int64_t r = 0; r < d.src_size; r++) mr = std::max(mr, off[r + 1] - off[r]);
+			}
+			n->persist_chunks[ci] = std::max<int64_t>(1, (mr + kPersistChunk - 1) / kPersistChunk);
+		}
+		TRY(dalloc(n, &n->d_barrier, 1));
+		TRY(dalloc(n, &n->d_pstatus, 1));
+		CUDA_TRY(cudaMallocHost(&n->h_pstatus, sizeof(int)));
+		*n->h_pstatus = 0;
+	}
 	// two chunk buffers: the host prepares one chunk while the GPU still steps the previous one
 	TRY(dalloc(n, &n->d_dt, 2 * kRunCap, false));
 	TRY(dalloc(n, &n->d_seeds, 2 * kRunCap, false));
@@ -1259,6 +1293,82 @@ int call_user_plastic(spice_net* n, Conn const& c, int what, int hslot, int64_t 
 	return SPICE_OK;
 }
 
+// A grid barrier of an earlier persistent launch that gave up waiting leaves its steps incomplete.
+int check_persist(spice_net* n) {
+	if (n->h_pstatus && *(volatile int*)n->h_pstatus != 0)
+		return fail(SPICE_ECUDA, "a grid-wide barrier of the persistent step kernel gave up waiting; the network state "
+		                         "is invalid");
+	return SPICE_OK;
+}
+
+// The steps [time, time + chunk) of a network whose windows are one step long, as one cooperative
+// launch of k_persist (step.cu).
+int run_persist(spice_net* n, int64_t chunk, const float* d_dt, const u128* d_tables, bool record, int64_t rows,
+                int64_t rec_windows) {
+	int const np = (int)n->pops.size();
+	PersistArgs pa{};
+	pa.t0          = n->time;
+	pa.nsteps      = (int)chunk;
+	pa.parity0     = n->parity;
+	pa.D           = (int)n->max_delay;
+	pa.Hb          = n->Hb;
+	pa.npop        = np;
+	pa.nconn       = (int)n->conns.size();
+	pa.mode        = n->mode;
+	pa.pops        = n->d_pops;
+	pa.conns       = n->d_conns;
+	pa.dts         = d_dt;
+	pa.tables      = n->total_draws > 0 ? d_tables : nullptr;
+	pa.counts      = n->d_counts;
+	pa.events      = n->d_events;
+	pa.barrier     = n->d_barrier;
+	pa.status      = n->d_pstatus;
+	pa.any_plastic = n->plastic ? 1 : 0;
+	int nb = 0;
+	for (int p = 0; p < np; p++) {
+		PopDev const& P = n->pops[p].d;
+		pa.blk_begin[p] = nb;
+		if (P.model == POISSON) {
+			pa.blk_kind[p]     = 1;
+			pa.blk_per_step[p] = (P.nwords + kNeuronThreads - 1) / kNeuronThreads;
+			nb += pa.blk_per_step[p];
+		} else if (P.model == EXTERNAL) {
+			pa.blk_kind[p] = 2;
+			int64_t const ns = P.ext_steps;
+			pa.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
+			nb += 1;
+		} else {
+			pa.blk_kind[p] = neuron_block_kind(P) + (P.hist ? kHistKind : 0);
+			nb += (int)((P.size + kNeuronThreads - 1) / kNeuronThreads);
+		}
+	}
+	pa.blk_begin[np] = nb;
+	pa.nblk          = nb;
+	for (size_t ci = 0; ci < n->conns.size(); ci++) pa.chunks[ci] = n->persist_chunks[ci];
+	pa.record = record ? 1 : 0;
+	if (record) {
+		RasterArgs& ra = pa.raster;
+		ra.Hb          = n->Hb;
+		ra.npop        = np;
+		ra.pops        = n->d_pops;
+		ra.base        = n->d_raster_base;
+		ra.out         = n->h_raster;
+		ra.capacity    = n->raster_cap;
+		ra.step_counts = n->h_rcounts;
+		ra.row0        = rows;
+		pa.rec_parity0 = (int)(rec_windows & 1);
+	}
+	CUDA_TRY(cudaMemsetAsync(n->d_barrier, 0, sizeof(unsigned), n->stream));
+	int slot = -1;
+	TRY(ev_begin(n, 0, &slot));
+	int const per_sm = n->persist_knob >= 2 ? n->persist_knob : kPersistBlocksPerSM;
+	CUDA_TRY(launch_persist(n->stream, pa, std::min(n->persist_grid, n->sm_count * per_sm)));
+	TRY(ev_end(n, slot));
+	n->launches++;
+	CUDA_TRY(cudaMemcpyAsync(n->h_pstatus, n->d_pstatus, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
+	return SPICE_OK;
+}
+
 int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) {
 	TRY(prepare(n));
 	int const np   = (int)n->pops.size();
@@ -1276,6 +1386,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 		int const cb = n->chunk_buf;
 		n->chunk_buf ^= 1;
 		CUDA_TRY(cudaEventSynchronize(n->ev_chunk[cb]));
+		TRY(check_persist(n));
 		float* const h_dt          = n->h_dt + (size_t)cb * kRunCap;
 		u128* const h_seeds        = n->h_seeds + (size_t)cb * kRunCap;
 		float* const d_dt          = n->d_dt + (size_t)cb * kRunCap;
@@ -1292,6 +1403,16 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 		if (n->total_draws > 0) {
 			CUDA_TRY(launch_jump_tables(n->stream, d_seeds, chunk, d_tables));
 			n->launches++;
+		}
+		if (n->persist_ok && n->persist_knob) {  // every step of the chunk in one cooperative launch
+			TRY(run_persist(n, chunk, d_dt, d_tables, record, rows, rec_windows));
+			n->parity ^= (int)(chunk & 1);
+			n->time += chunk;
+			rows += chunk;
+			rec_windows += chunk;
+			steps -= chunk;
+			CUDA_TRY(cudaEventRecord(n->ev_chunk[cb], n->stream));
+			continue;
 		}
 		// the source kernels of this chunk read dt and the jump tables written above
 		CUDA_TRY(cudaEventRecord(n->ev_tab, n->stream));
@@ -1898,6 +2019,13 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 				return fail(SPICE_ESTATE, "the delivery path of a population is fixed once the network steps");
 			n->pull_all = value != 0;
 			return SPICE_OK;
+		case SPICE_TUNE_PERSISTENT:
+			if (value < 0 || value > 32) return fail(SPICE_EINVAL, "persistent must be 0 (off), 1 (on) or 2 .. 32 (on, CTAs per SM)");
+			if (n->prepared && value != 0 && !n->persist_ok)
+				return fail(SPICE_ESTATE, "persistent steps are set up when the network first steps (this network "
+				                          "was prepared without them, or is not eligible)");
+			n->persist_knob = (int)value;
+			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
 			if (value < 0 || value > 6) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 6");
 			n->neuron_variant = (int)value;
@@ -1956,7 +2084,7 @@ extern "C" int spice_get_stream(spice_net* n, void** out) {
 extern "C" int spice_synchronize(spice_net* n) {
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
-	return SPICE_OK;
+	return check_persist(n);
 }
 
 extern "C" int spice_selftest_skip_rounding(int64_t count, uint64_t seed, int64_t* mismatches,

@@ -2551,6 +2551,228 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 	else deliver_rows16<MODE, 2, 4, false, 1024>(a, P, t, (int)blockIdx.y, part);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Persistent steps: a network whose windows are one step long (plastic connections, or a minimum
+// delay of one step) pays three to four launches per step in the window design, each mostly
+// launch latency.  Here one cooperative launch runs every step of a chunk; the phases of a step
+// are separated by grid-wide barriers:
+//   A  the neuron update and source populations of step t (the window bodies with K = 1)
+//   B  (t mod 64 == 0, plastic connections) every plastic synapse catches up (snn.cpp:17-19)
+//   C  the deliveries of step t (snn.cpp:21-25) -- each fixed-weight connection's spikes of step t
+//      into ring slot (t + d - 1) mod D, and each plastic connection's spikes of step t - d + 1
+//      (catch-up, then the synapse's weight into slot t mod D), with global reductions, in work
+//      units of a warp and at most kPersistChunk synapses of one row; the raster of step t; the
+//      other parity's spike counts cleared.  A plastic source's `ages` word is written in phase A
+//      of the next step, when every unit of its row has read the old value.
+// Deterministic mode adds integer counts (exact in any order); atomic mode adds floats as the
+// window design does.
+// ---------------------------------------------------------------------------------------------
+constexpr long long kBarrierCycles = 2000000000ll;  // ~1 s at the SM clock, then the wait gives up
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+	unsigned v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+
+// Grid-wide barrier over a monotonic arrival counter (every CTA calls it the same number of times;
+// `target` is this CTA's running count of expected arrivals).  Returns false once any wait has
+// given up: the caller stops.
+__device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned& target, int* status) {
+	__syncthreads();
+	target += gridDim.x;
+	if (threadIdx.x == 0) {
+		__threadfence();
+		atomicAdd(count, 1u);
+		long long const start = clock64();
+		while (ld_acquire(count) < target) {
+			if (clock64() - start > kBarrierCycles || *(volatile int*)status != 0) {
+				atomicExch(status, 1);
+				break;
+			}
+			__nanosleep(32);
+		}
+		__threadfence();
+	}
+	__syncthreads();
+	return *(volatile int*)status == 0;
+}
+
+// The catch-up and weight of one plastic synapse e of connection C at step `time` (the body of
+// k_plastic_deliver for one thread).
+__device__ __forceinline__ void plastic_deliver_one(ConnDev const& C, int64_t e, int64_t time, uint64_t ages,
+                                                    int64_t slot, bool deliver) {
+	SynState st{C.sW[e], C.sA[e], C.sB[e]};
+	int32_t const j = C.nb[e];
+	catch_up(C, st, time, ages, C.dst_hist[j]);
+	C.sW[e] = st.W;
+	C.sA[e] = st.A;
+	C.sB[e] = st.B;
+	if (deliver) {
+		float const v = C.plastic == SPICE_SYNAPSE_COUNT ? __fmul_rn(C.weight, st.W) : st.W;
+		red_add_f32(C.dst_acc + (slot * C.dst_size + j) * C.F + C.fslot, v);
+	}
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_constant__ PersistArgs a) {
+	__shared__ int red[kPersistThreads / 32 + 1];
+	__shared__ int64_t u_begin[kMaxConns + 1];  // phase C: first unit of each connection
+	__shared__ unsigned long long ev_block;
+	int const lane = threadIdx.x & 31;
+	int const wib  = threadIdx.x >> 5;
+	constexpr int WPB = kPersistThreads / 32;
+	int64_t const gwarp  = (int64_t)blockIdx.x * WPB + wib;
+	int64_t const nwarps = (int64_t)gridDim.x * WPB;
+	unsigned target = 0;
+	if (threadIdx.x == 0) ev_block = 0;
+	for (int s = 0; s < a.nsteps; s++) {
+		int64_t const t = a.t0 + s;
+		int const q     = (a.parity0 + s) & 1;
+		WinCtx w;
+		w.K              = 1;
+		w.D              = a.D;
+		w.slot0          = (int)((t - 1 + a.D) % a.D);
+		w.hslot0         = (int)(t % a.Hb);
+		w.Hb             = a.Hb;
+		w.npop           = a.npop;
+		w.list_k0        = q;
+		w.dts            = a.dts + s;
+		w.tables         = a.tables ? a.tables + (int64_t)s * kJumpTable : nullptr;
+		w.tab_net_stride = 0;
+		w.counts         = a.counts + q * a.npop;
+		// ---- A: the update of step t; the ages of the previous step's plastic deliveries ----
+		for (int vb = blockIdx.x; vb < a.nblk; vb += gridDim.x) {
+			int p = 0;
+			while (p + 1 < a.npop && vb >= a.blk_begin[p + 1]) p++;
+			int const lb   = vb - a.blk_begin[p];
+			int const kind = a.blk_kind[p];
+			if (kind == 1) window_poisson(w, a.pops + p, p, lb, a.blk_per_step[p], red);
+			else if (kind == 2) window_external(w, a.pops + p, p, 0, a.ext_pos[p] + s);
+			else if ((kind & 7) == 3) {
+				if (kind & kHistKind) window_neurons<MODE, true, true>(w, a.pops + p, p, lb);
+				else window_neurons<MODE, true, false>(w, a.pops + p, p, lb);
+			} else {
+				if (kind & kHistKind) window_neurons<MODE, false, true>(w, a.pops + p, p, lb);
+				else window_neurons<MODE, false, false>(w, a.pops + p, p, lb);
+			}
+			__syncthreads();  // shared scratch of the bodies is reused by the next item
+		}
+		if (a.any_plastic && t > a.t0) {  // sources delivered at step t - 1: caught up to t
+			for (int c = 0; c < a.nconn; c++) {
+				ConnDev const& C = a.conns[c];
+				if (!C.plastic || t - 1 < C.delay - 1) continue;
+				const uint32_t* bits = C.src_bits + ((t - C.delay) % a.Hb) * C.src_nwords;
+				for (int64_t wd = blockIdx.x * (int64_t)kPersistThreads + threadIdx.x; wd < C.src_nwords;
+				     wd += (int64_t)gridDim.x * kPersistThreads)
+					for (uint32_t m = bits[wd]; m; m &= m - 1)
+						C.ages[32 * wd + __ffs(m) - 1] = (uint64_t)t | (1ull << 63);
+			}
+		}
+		if (!grid_barrier(a.barrier, target, a.status)) return;
+		// ---- B: the periodic catch-up of every plastic synapse, a warp per source ----
+		if (a.any_plastic && t % 64 == 0) {
+			int64_t base = 0;
+			for (int c = 0; c < a.nconn; c++) {
+				ConnDev const& C = a.conns[c];
+				if (!C.plastic) continue;
+				for (int64_t u = gwarp - base; u < C.src_size; u += nwarps) {
+					if (u < 0) continue;
+					uint64_t const ages = C.ages[u];
+					for (int64_t e = C.off[u] + lane; e < C.off[u + 1]; e += 32) {
+						SynState st{C.sW[e], C.sA[e], C.sB[e]};
+						catch_up(C, st, t, ages, C.dst_hist[C.nb[e]]);
+						C.sW[e] = st.W;
+						C.sA[e] = st.A;
+						C.sB[e] = st.B;
+					}
+					__syncwarp();
+					if (lane == 0) C.ages[u] = (uint64_t)(t + 1);
+				}
+				base += C.src_size;
+				base %= nwarps;  // unit u of this connection runs on warp (base + u) mod nwarps
+			}
+			if (!grid_barrier(a.barrier, target, a.status)) return;
+		}
+		// ---- C: deliveries of step t, raster, counts of the other parity ----
+		if (threadIdx.x == 0) {
+			int64_t acc = 0;
+			for (int c = 0; c < a.nconn; c++) {
+				ConnDev const& C = a.conns[c];
+				u_begin[c] = acc;
+				if (C.plastic) {
+					if (t >= C.delay - 1) acc += (int64_t)C.src_nwords * a.chunks[c];
+				} else {
+					acc += (int64_t)a.counts[q * a.npop + C.src] * a.chunks[c];
+				}
+			}
+			u_begin[a.nconn] = acc;
+		}
+		if (blockIdx.x == 0 && threadIdx.x < a.npop) a.counts[(q ^ 1) * a.npop + threadIdx.x] = 0;
+		__syncthreads();
+		if (a.record && blockIdx.x < a.npop) {
+			RasterArgs r = a.raster;
+			r.t0     = t;
+			r.K      = 1;
+			r.counts = a.counts + q * a.npop;
+			r.parity = (a.rec_parity0 + s) & 1;
+			r.row0   = a.raster.row0 + s;
+			raster_block(r, blockIdx.x);
+		}
+		int64_t const total = u_begin[a.nconn];
+		unsigned long long ev = 0;
+		int c = 0;
+		for (int64_t u = gwarp; u < total; u += nwarps) {
+			while (c + 1 < a.nconn && u >= u_begin[c + 1]) c++;
+			while (c > 0 && u < u_begin[c]) c--;
+			ConnDev const& C = a.conns[c];
+			int64_t const r  = u - u_begin[c];
+			int64_t const ch = r % a.chunks[c];
+			if (C.plastic) {  // unit: (bitmap word, chunk) of the spikes of step t - d + 1
+				int64_t const wd = r / a.chunks[c];
+				uint32_t m = C.src_bits[((t - C.delay + 1) % a.Hb) * C.src_nwords + wd];
+				bool const deliver = MODE == 1 && (C.plastic == SPICE_SYNAPSE_ISTDP || C.weight != 0.0f);
+				int64_t const slot = t % a.D;
+				for (; m; m &= m - 1) {
+					int64_t const src = 32 * wd + __ffs(m) - 1;
+					int64_t const e0 = C.off[src] + ch * kPersistChunk, e1 = min(C.off[src + 1], e0 + kPersistChunk);
+					if (ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
+					uint64_t const ages = C.ages[src];
+					for (int64_t e = e0 + lane; e < e1; e += 32) plastic_deliver_one(C, e, t, ages, slot, deliver);
+				}
+			} else {  // unit: (spike, chunk) of step t
+				int32_t const src = C.src_list[(int64_t)q * C.src_size + r / a.chunks[c]];
+				int64_t const e0 = C.off[src] + ch * kPersistChunk, e1 = min(C.off[src + 1], e0 + kPersistChunk);
+				if (ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
+				int64_t const slot = (t + C.delay - 1) % a.D;
+				if (MODE == 0) {
+					uint32_t* const base = C.dst_cnt + slot * C.dst_size * C.W + C.word;
+					for (int64_t e = e0 + lane; e < e1; e += 32) red_add_u32(base + (int64_t)C.nb[e] * C.W, C.inc);
+				} else {
+					float* const base = C.dst_acc + slot * C.dst_size * C.F + C.fslot;
+					for (int64_t e = e0 + lane; e < e1; e += 32) red_add_f32(base + (int64_t)C.nb[e] * C.F, C.weight);
+				}
+			}
+		}
+		if (lane == 0 && ev) atomicAdd(&ev_block, ev);
+		if (!grid_barrier(a.barrier, target, a.status)) return;
+	}
+	// the ages of the last step's plastic deliveries
+	if (a.any_plastic) {
+		int64_t const t = a.t0 + a.nsteps;
+		for (int c = 0; c < a.nconn; c++) {
+			ConnDev const& C = a.conns[c];
+			if (!C.plastic || t - 1 < C.delay - 1) continue;
+			const uint32_t* bits = C.src_bits + ((t - C.delay) % a.Hb) * C.src_nwords;
+			for (int64_t wd = blockIdx.x * (int64_t)kPersistThreads + threadIdx.x; wd < C.src_nwords;
+			     wd += (int64_t)gridDim.x * kPersistThreads)
+				for (uint32_t m = bits[wd]; m; m &= m - 1) C.ages[32 * wd + __ffs(m) - 1] = (uint64_t)t | (1ull << 63);
+		}
+	}
+	__syncthreads();
+	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
+}
+
 }  // namespace
 
 cudaError_t scan_row_lengths(cudaStream_t stream, const int32_t* lens, int64_t n, int64_t* offsets) {
@@ -2912,6 +3134,19 @@ cudaError_t launch_plastic_deliver(cudaStream_t stream, ConnDev const& c, int64_
 	                (unsigned)std::min<int64_t>(65535, (c.max_row + kPlasticChunk - 1) / kPlasticChunk));
 	k_plastic_deliver<<<grid, kPlasticChunk, 0, stream>>>(c, time, hslot, slot, deliver ? 1 : 0, events);
 	return cudaGetLastError();
+}
+
+cudaError_t persist_occupancy(int mode, int* blocks_per_sm) {
+	void const* f = mode == 0 ? (void const*)k_persist<0> : (void const*)k_persist<1>;
+	return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, f, kPersistThreads, 0);
+}
+
+// A cooperative launch: every CTA of the grid is resident at once (the barriers wait on each other).
+cudaError_t launch_persist(cudaStream_t stream, PersistArgs const& a, int grid) {
+	if (a.nsteps <= 0) return cudaSuccess;
+	void const* f = a.mode == 0 ? (void const*)k_persist<0> : (void const*)k_persist<1>;
+	void* args[]  = {const_cast<PersistArgs*>(&a)};
+	return cudaLaunchCooperativeKernel(f, dim3((unsigned)grid), dim3((unsigned)kPersistThreads), args, 0, stream);
 }
 
 cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a) {

@@ -77,7 +77,7 @@ def test_tuning_knobs_reach_the_python_mirror(engine, monkeypatch):
     net = engine.snn.__new__(engine.snn)
     net._h = None
     net.set_tuning(tile_bytes=4096, deliver_threads=64, deliver_parts=1, deliver_algo=1, overlap_sources=True,
-                   neuron_variant=0, launch_mode=1, pull=False, source_steps=0)
+                   neuron_variant=0, launch_mode=1, pull=False, source_steps=0, persistent=1)
     b = engine.batch.__new__(engine.batch)
     b._h = None
     b.set_tuning(graph_windows=2)
