@@ -346,57 +346,105 @@ def adjoint_bench(reps: int = 10):
     return out
 
 
-def plastic_bench(N: int = 100000, steps: int = 5000):
+def plastic_bench(N: int = 100000, steps: int = 5000, peak: float | None = None, cpu_steps: int = 400):
     """The plastic E/I network: N conductance-LIF neurons (80 % E, 20 % I; tau_E 5 ms, tau_I 10 ms,
     the neuron of samples/vogels.cpp), fixed_probability(0.02), delay 1 step, E weights 0.03 and
     I weights 0.3 (0.3 nS and 3 nS over the 10 nS leak), I->E synapses iSTDP (tau 20 ms, rho0 5 Hz,
-    eta 1e-3) with lazy event-driven updates, atomic mode, dt 1e-4, `steps` steps after 200 warm-up
-    steps and the delivery autotuner's (~7,700 steps of the network's own dynamics).  Reported:
-    synaptic events/s and simulated seconds per wall second (CUDA events on the net's stream),
-    firing rates and the I->E weight drift."""
+    eta 1e-3) with lazy event-driven updates, atomic mode, dt 1e-4, `steps` steps after 300 warm-up
+    steps.  Windows are one step long, so the net runs persistent steps (one cooperative launch
+    per 1024 steps, SPICE_TUNE_PERSISTENT); the launch-per-phase path is timed beside it.
+    Reported: synaptic events/s and simulated seconds per wall second (CUDA events on the net's
+    stream), firing rates, the I->E weight drift, the roofline of the persistent kernel and the
+    CPU restatement of the same network timed on the host cores from the first timed step."""
     import numpy as np
     import torch
     import spice2_gb300 as sp
+
+    def build(seed=1):
+        net = sp.snn(1e-4, 1e-4, [seed])
+        net.set_mode(sp.MODE_ATOMIC)
+        E = net.add_population(sp.lif_cond(), N * 8 // 10)
+        I = net.add_population(sp.lif_cond(), N * 2 // 10)
+        net.connect(E, E, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
+        net.connect(E, I, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
+        c = net.connect(I, E, sp.fixed_probability(0.02), 1e-4, sp.istdp(0.3, eta=1e-3, rho0=5.0, tau=0.02))
+        net.connect(I, I, sp.fixed_probability(0.02), 1e-4, sp.inhibitory(0.3))
+        return net, E, I, c
+
+    def timed(net, n):
+        stream = torch.cuda.ExternalStream(net.stream_handle())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, l0 = net.events, net.launch_count()
+        torch.cuda.synchronize()
+        a.record(stream)
+        net.run(n)
+        b.record(stream)
+        torch.cuda.synchronize()
+        return a.elapsed_time(b), net.events - e0, net.launch_count() - l0
+
+    warm = 300
     t0 = time.perf_counter()
-    net = sp.snn(1e-4, 1e-4, [1])
-    net.set_mode(sp.MODE_ATOMIC)
-    E = net.add_population(sp.lif_cond(), N * 8 // 10)
-    I = net.add_population(sp.lif_cond(), N * 2 // 10)
-    net.connect(E, E, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
-    net.connect(E, I, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
-    c = net.connect(I, E, sp.fixed_probability(0.02), 1e-4, sp.istdp(0.3, eta=1e-3, rho0=5.0, tau=0.02))
-    net.connect(I, I, sp.fixed_probability(0.02), 1e-4, sp.inhibitory(0.3))
+    net, E, I, c = build()
     net.csr(0)
     syn = sum(net.synapses(k) for k in range(4))
     build_s = time.perf_counter() - t0
-    net.run(200)
-    from spice2_gb300.autotune import autotune
-    tuned = autotune(net, steps=100, warm=10)["best"]  # delivery shape of the non-plastic projections
+    net.run(warm)
     net.synchronize()
     W0 = net.synapse_state(c, 0).astype(np.float64)
-    stream = torch.cuda.ExternalStream(net.stream_handle())
-    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0, l0 = net.events, net.launch_count()
-    torch.cuda.synchronize()
-    a.record(stream)
-    net.run(steps)
-    b.record(stream)
-    torch.cuda.synchronize()
-    ms = a.elapsed_time(b)
-    ev = net.events - e0
-    launches = net.launch_count() - l0
+    ms, ev, launches = timed(net, steps)
     W = net.synapse_state(c, 0).astype(np.float64)
     raster = net.run_record(1000)  # rates over the next 0.1 s (not timed)
     rE = sum(len(r[0]) for r in raster) / (N * 0.8) / 0.1
     rI = sum(len(r[1]) for r in raster) / (N * 0.2) / 0.1
     net.close()
-    return {"metric": "synaptic_events_per_s", "unit": "events/s", "value": ev / (ms / 1e3), "N": N,
-            "synapses": syn, "sim_steps": steps, "ms": ms, "sim_seconds_per_wall_second": steps * 1e-4 / (ms / 1e3),
-            "events": ev, "gpu_launches": launches, "rate_E_hz": rE, "rate_I_hz": rI,
-            "istdp_weight_mean_start": float(W0.mean()), "istdp_weight_mean_end": float(W.mean()),
-            "istdp_weight_std_end": float(W.std()), "build_seconds": build_s, "mode": "atomic",
-            "delivery_shape": tuned,
-            "config": "plastic E/I: conductance LIF, p 0.02, delay 1 step, iSTDP on I->E"}
+    # the same stretch through one launch per phase
+    net2, *_ = build()
+    net2.set_tuning(persistent=0)
+    net2.run(warm)
+    ms_phase, ev_phase, launches_phase = timed(net2, steps)
+    net2.close()
+    us_step = 1000.0 * ms / steps
+    # algorithmic bytes of a step: the conductance-LIF state read and written (V, Gex, Gin, Tref),
+    # the input ring's two sums read and cleared, 8 B per static event (target, weight), 28 B per
+    # plastic event (target, W / x_pre / x_post read and written) and every 64 steps the catch-up of
+    # every plastic synapse (target 4 B, state 24 B)
+    n_plastic = int(0.02 * (N * 2 // 10) * (N * 8 // 10))  # expected I->E synapses
+    bytes_step = 32 * N + 16 * N + 8 * ev / steps + 28 * n_plastic / 64.0
+    peak = peak or _peaks()[0]
+    achieved = bytes_step / (us_step * 1e-6) / 1e9
+    out = {"metric": "synaptic_events_per_s", "unit": "events/s", "value": ev / (ms / 1e3), "N": N,
+           "synapses": syn, "sim_steps": steps, "warmup_steps": warm, "ms": ms, "us_per_step": us_step,
+           "sim_seconds_per_wall_second": steps * 1e-4 / (ms / 1e3),
+           "events": ev, "gpu_launches": launches, "rate_E_hz": rE, "rate_I_hz": rI,
+           "istdp_weight_mean_start": float(W0.mean()), "istdp_weight_mean_end": float(W.mean()),
+           "istdp_weight_std_end": float(W.std()), "build_seconds": build_s, "mode": "atomic",
+           "path": "persistent steps (k_persist, one cooperative launch per 1024 steps)",
+           "launch_per_phase": {"ms": ms_phase, "us_per_step": 1000.0 * ms_phase / steps, "events": ev_phase,
+                                "gpu_launches": launches_phase,
+                                "sim_seconds_per_wall_second": steps * 1e-4 / (ms_phase / 1e3)},
+           "roofline": {"bound": "hbm", "kernel": "k_persist<1>", "achieved": achieved, "peak": peak,
+                        "unit": "GB/s", "frac": achieved / peak, "bytes_per_step": bytes_step,
+                        "bytes_model": "32 B/neuron state + 16 B/neuron input sums + 8 B/static event + "
+                                       "28 B/plastic synapse every 64 steps (catch-up)"},
+           "config": "plastic E/I: conductance LIF, p 0.02, delay 1 step, iSTDP on I->E"}
+    try:  # the CPU restatement of the same network from the first timed step (same seed)
+        from oracle import oracle as o
+        if not os.path.exists(o.BENCH_PATH):
+            o.build(with_reference=False)
+        threads = max(1, min(8, (os.cpu_count() or 1)))
+        r = subprocess.run([o.BENCH_PATH, str(N), "0.02", str(cpu_steps), "1", str(threads), str(warm), "1", "1",
+                            "plastic_ei"], check=True, capture_output=True, text=True).stdout
+        d = json.loads(r.strip().splitlines()[-1])
+        out["cpu_baseline"] = {
+            "value": d["events_per_s"], "unit": "events/s", "cores": threads, "kind": "port",
+            "per_core": d["events_per_s_per_core"],
+            "sim_seconds_per_wall_second_per_core": cpu_steps * 1e-4 / (d["ms_per_step"] * 1e-3 * cpu_steps),
+            "ms_per_step": d["ms_per_step"],
+            "sample": f"steps {warm}..{warm + cpu_steps} of the seed-1 network per thread ({threads} replicas), "
+                      f"the first {cpu_steps} steps of the GPU timed stretch; build and warm-up untimed"}
+    except Exception as e:  # the oracle could not be built or run here
+        out["cpu_baseline"] = {"error": str(e)}
+    return out
 
 
 def pull_bench(steps: int, warmup: int, peak: float):
@@ -667,7 +715,7 @@ def main():
         except Exception as e:
             adjoint = {"error": str(e)}
         try:
-            plastic = plastic_bench()
+            plastic = plastic_bench(peak=peak)
         except Exception as e:
             plastic = {"error": str(e)}
 

@@ -205,7 +205,10 @@ enum {
 	                                   list entries) written once per window, 5 as 4 with
 	                                   predicated instead of selected adds, 6 as 4 with the
 	                                   count bits tested on the packed input word and the
-	                                   leak factors computed once per CTA                     */
+	                                   leak factors computed once per CTA, 7 as 6 with
+	                                   predicated adds, a warp-uniform test for counts of 8 or
+	                                   more, ballots kept in registers and list entries reserved
+	                                   only for the steps with spikes                         */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

@@ -2,18 +2,22 @@
  * oracle_bench.c -- times the CPU restatement of snn::step on the Brunel network
  * (TEST INFRASTRUCTURE ONLY: bench.py's cpu_baseline / --impl reference leg runs it).
  *
- * usage: oracle_bench N P STEPS SEED0 THREADS [WARMUP [SAMPLES [SAME_SEED]]]
+ * usage: oracle_bench N P STEPS SEED0 THREADS [WARMUP [SAMPLES [SAME_SEED [NET]]]]
  *   Builds THREADS Brunel networks (the model of samples/brunel.cpp:75-116 with weights scaled by
  *   0.1/P), one per thread, with seeds SEED0, SEED0+1, ... or, with SAME_SEED = 1, all with SEED0
  *   (replicas of one simulation), runs WARMUP untimed steps, then times SAMPLES consecutive samples
  *   of STEPS steps of all networks in parallel (default 1).  Prints one JSON line: the aggregate
  *   events/s over all samples, per core, and per sample.
+ *   NET = plastic_ei builds the plastic E/I network instead (N conductance LIF neurons, 80 % E and
+ *   20 % I, fixed_probability(0.02), E weights 0.03, I weights 0.3, iSTDP on I->E with eta 1e-3,
+ *   rho0 5 Hz, tau 20 ms, delay 1 step; P is ignored).
  */
 #define _POSIX_C_SOURCE 200809L
 #include <math.h>
 #include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
+#include <string.h>
 #include <time.h>
 
 #include "spice_oracle.h"
@@ -57,10 +61,27 @@ spo_net* brunel(long long N, double p, unsigned seed) {
 	return n;
 }
 
+/* The plastic E/I network (conductance LIF of samples/vogels.cpp, iSTDP on I->E). */
+spo_net* plastic_ei(long long N, unsigned seed) {
+	float dt   = 1e-4f;
+	uint32_t s = seed;
+	spo_net* n = spo_net_create(dt, dt, &s, 1);
+	int E = spo_add_population(n, SPO_LIF_COND, N * 8 / 10, NULL, 0);
+	int I = spo_add_population(n, SPO_LIF_COND, N * 2 / 10, NULL, 0);
+	spo_connect(n, E, E, 0.02, dt, 1, 0.03f);
+	spo_connect(n, E, I, 0.02, dt, 1, 0.03f);
+	int c = spo_connect(n, I, E, 0.02, dt, 2, 0.3f);
+	spo_set_plastic(n, c, SPO_SYN_ISTDP, 0.3f, 1e-3f, 5.0f, 0.02f);
+	spo_connect(n, I, I, 0.02, dt, 2, 0.3f);
+	return n;
+}
+
+static int g_plastic = 0;
+
 static void* worker(void* arg) {
 	job* j      = (job*)arg;
 	double t0   = now();
-	j->net      = brunel(j->N, j->p, j->seed);
+	j->net      = g_plastic ? plastic_ei(j->N, j->seed) : brunel(j->N, j->p, j->seed);
 	j->build_s  = now() - t0;
 	spo_run(j->net, j->warmup);
 	for (int k = 0; k < j->samples; k++) {
@@ -86,6 +107,7 @@ int main(int argc, char** argv) {
 	long long warm  = argc > 6 ? atoll(argv[6]) : 0;
 	int samples     = argc > 7 ? atoi(argv[7]) : 1;
 	int same_seed   = argc > 8 ? atoi(argv[8]) : 0;
+	g_plastic       = argc > 9 && strcmp(argv[9], "plastic_ei") == 0;
 	if (T < 1) T = 1;
 	if (samples < 1) samples = 1;
 	if (samples > MAX_SAMPLES) samples = MAX_SAMPLES;
@@ -120,9 +142,9 @@ int main(int argc, char** argv) {
 	}
 	for (int k = 0; k < samples; k++) dt += dts[k];
 	printf("{\"events\": %lld, \"step_seconds\": %.6f, \"build_seconds\": %.6f, \"threads\": %d, "
-	       "\"steps\": %lld, \"samples\": %d, \"warmup\": %lld, \"same_seed\": %d, \"N\": %lld, \"p\": %g, "
+	       "\"steps\": %lld, \"samples\": %d, \"warmup\": %lld, \"same_seed\": %d, \"net\": \"%s\", \"N\": %lld, \"p\": %g, "
 	       "\"events_per_s\": %.6g, \"events_per_s_per_core\": %.6g, \"ms_per_step\": %.6f, \"sample_events_per_s\": [",
-	       ev, dt, build, T, steps, samples, warm, same_seed, N, p, ev / dt, ev / dt / T, 1e3 * dt / (double)(steps * samples));
+	       ev, dt, build, T, steps, samples, warm, same_seed, g_plastic ? "plastic_ei" : "brunel", N, p, ev / dt, ev / dt / T, 1e3 * dt / (double)(steps * samples));
 	for (int k = 0; k < samples; k++) {
 		long long e = 0;
 		for (int i = 0; i < T; i++) e += jobs[i].events[k];

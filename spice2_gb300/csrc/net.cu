@@ -2027,7 +2027,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->persist_knob = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
-			if (value < 0 || value > 6) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 6");
+			if (value < 0 || value > 7) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 7");
 			n->neuron_variant = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:

@@ -611,6 +611,88 @@ __device__ __forceinline__ void window_lif_deferred(A const& a, const PopDev* __
 	}
 }
 
+// The Brunel LIF window with fewer instructions per step (variant 7), same arithmetic and outputs
+// as variant 6: the count replay takes its 4-, 2- and 1-blocks as predicated adds and falls back
+// to the general replay by a warp-uniform test (a count of 8 or more anywhere in the warp); each
+// step's warp ballot stays in the register of lane u; list entries are reserved only for the
+// steps in which the warp spiked; the input words are staged by walking a pointer.
+template <class A>
+__device__ __forceinline__ void window_lif_lean(A const& a, const PopDev* __restrict__ Pg, int p, int b,
+                                                const float* dts_sm, uint32_t (*xs_sm)[kThreads]) {
+	int const N      = (int)Pg->size;
+	int const i      = b * kThreads + threadIdx.x;
+	bool const valid = i < N;
+	int const lane   = threadIdx.x & 31;
+	int const word   = i >> 5;
+	uint32_t* const cnt = Pg->cnt;
+	bool const zero     = Pg->zero_inputs != 0;
+	float const vthres  = Pg->p0;
+	int32_t const tref  = (int32_t)Pg->p1;
+	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
+	float V   = 0;
+	int32_t T = 0;
+	if (valid) {  // written two launches back: loaded before waiting for the previous launch
+		V = Pg->V[i];
+		T = Pg->T[i];
+	}
+	griddep_wait();  // the input ring, counts and lists are the previous launches' output
+	int const D = (int)a.D, Hb = a.Hb;
+	for (int k0 = 0; k0 < a.K; k0 += 16) {
+		int const nk    = min(16, a.K - k0);
+		int const slot0 = (int)((a.slot0 + k0) % D);
+		const uint32_t* src = cnt + (int64_t)slot0 * N + i;
+		int const wrap      = D - slot0;  // step u >= wrap reads ring slot u - wrap
+#pragma unroll
+		for (int u = 0; u < 16; u++) {  // asynchronous copies into the thread's own shared-memory column
+			if (u == wrap) src -= (int64_t)D * N;
+			if (valid && u < nk) {
+				unsigned const dst = (unsigned)__cvta_generic_to_shared(&xs_sm[u][threadIdx.x]);
+				asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+			} else {
+				xs_sm[u][threadIdx.x] = 0u;
+			}
+			src += N;
+		}
+		asm volatile("cp.async.wait_all;" ::: "memory");
+		uint32_t sbits = 0;   // this lane's spikes of the 16 steps
+		uint32_t mymask = 0;  // lane u: the warp's ballot of step u
+#pragma unroll 1
+		for (int u = 0; u < nk; u++) {
+			uint32_t const x = xs_sm[u][threadIdx.x];
+			if (__any_sync(0xffffffffu, (x & 0xfff8fff8u) != 0)) {  // a count of 8 or more in the warp
+				V = add_n_sel(V, w0, x & 0xffffu);
+				V = add_n_sel(V, w1, x >> 16);
+			} else {
+				if (x & 4u) V = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V, w0), w0), w0), w0);
+				if (x & 2u) V = __fadd_rn(__fadd_rn(V, w0), w0);
+				if (x & 1u) V = __fadd_rn(V, w0);
+				if (x & 0x40000u) V = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V, w1), w1), w1), w1);
+				if (x & 0x20000u) V = __fadd_rn(__fadd_rn(V, w1), w1);
+				if (x & 0x10000u) V = __fadd_rn(V, w1);
+			}
+			if (zero && x) cnt[(int64_t)((slot0 + u) % D) * N + i] = 0;
+			bool const spike = lif_update(V, T, dts_sm[k0 + u], vthres, tref) && valid;
+			sbits |= (uint32_t)spike << u;
+			unsigned const mask = __ballot_sync(0xffffffffu, spike);
+			mymask              = lane == u ? mask : mymask;
+		}
+		if (lane < nk && word < Pg->nwords) Pg->bits[(int64_t)((a.hslot0 + k0 + lane) % Hb) * Pg->nwords + word] = mymask;
+		// list reservations, one per step in which the warp spiked
+		for (unsigned st = __reduce_or_sync(0xffffffffu, sbits); st; st &= st - 1) {
+			int const u         = __ffs(st) - 1;
+			unsigned const mask = __shfl_sync(0xffffffffu, mymask, u);
+			int base = 0;
+			if (lane == 0) base = atomicAdd(a.counts + (k0 + u) * a.npop + p, __popc(mask));
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if ((sbits >> u) & 1u) Pg->list[(int64_t)(a.list_k0 + k0 + u) * N + base + __popc(mask & lanemask_lt())] = i;
+		}
+	}
+	if (valid) {
+		Pg->V[i] = V;
+		Pg->T[i] = T;
+	}
+}
+
 // One step of a Poisson population (samples/brunel.cpp:27-30): thread c owns neurons
 // [32c, 32c + 32), jumps to draw draw_offset + 32c of the step's stream and draws 32 numbers.
 // The jump XORs the states T^i(s), i < 128, selected by the 128 bits of x^(offset) mod P; the step's
@@ -713,15 +795,15 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 // One CTA of the neuron update (block b of the window's neuron blocks).
 template <int MODE, bool ONLY_FAST, int VAR>
 __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
-	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;  // 4 .. 6: deferred spike output
+	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;  // 4 .. 7: deferred spike output
 	__shared__ float dts_sm[kMaxWindow];
 	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
-	__shared__ uint32_t masks_sm[VAR >= 4 ? kThreads / 32 : 1][16];
+	__shared__ uint32_t masks_sm[VAR >= 4 && VAR <= 6 ? kThreads / 32 : 1][16];
 	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
-	if (VAR == 6 && MODE == 0 && kind == 3) {  // the LIF leak factors of the window's steps
+	if ((VAR == 6 || VAR == 7) && MODE == 0 && kind == 3) {  // the LIF leak factors of the window's steps
 		float const tminv = a.pops[p].p2;
 		for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = __fmaf_rn(-a.dts[k], tminv, 1.0f);
 	} else {
@@ -733,6 +815,7 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 		if (VAR == 4) window_lif_deferred<false, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else if (VAR == 5) window_lif_deferred<true, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else if (VAR == 6) window_lif_deferred<false, true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else if (VAR == 7) window_lif_lean(a, a.pops + p, p, lb, dts_sm, xs_sm);
 		else {
 			griddep_wait();
 			window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
@@ -2829,6 +2912,7 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 		else if (a.variant == 4) k_neurons<0, true, 4><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 5) k_neurons<0, true, 5><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 6) k_neurons<0, true, 6><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 7) k_neurons<0, true, 7><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
 		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
@@ -2843,21 +2927,21 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	if (nblocks + nsrc_blocks + nrb <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
-	void const* fns[2][9] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
-	                          (void const*)k_window<0, true, 1, false>, (void const*)k_window<0, true, 2, false>,
-	                          (void const*)k_window<0, true, 3, false>, (void const*)k_window<0, true, 4, false>,
-	                          (void const*)k_window<0, true, 5, false>, (void const*)k_window<0, true, 6, false>,
-	                          (void const*)k_window<1, true, 0, false>},
-	                         {(void const*)k_window<0, false, 0, true>, (void const*)k_window<0, true, 0, true>,
-	                          (void const*)k_window<0, true, 1, true>, (void const*)k_window<0, true, 2, true>,
-	                          (void const*)k_window<0, true, 3, true>, (void const*)k_window<0, true, 4, true>,
-	                          (void const*)k_window<0, true, 5, true>, (void const*)k_window<0, true, 6, true>,
-	                          (void const*)k_window<1, true, 0, true>}};
+	void const* fns[2][10] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
+	                           (void const*)k_window<0, true, 1, false>, (void const*)k_window<0, true, 2, false>,
+	                           (void const*)k_window<0, true, 3, false>, (void const*)k_window<0, true, 4, false>,
+	                           (void const*)k_window<0, true, 5, false>, (void const*)k_window<0, true, 6, false>,
+	                           (void const*)k_window<0, true, 7, false>, (void const*)k_window<1, true, 0, false>},
+	                          {(void const*)k_window<0, false, 0, true>, (void const*)k_window<0, true, 0, true>,
+	                           (void const*)k_window<0, true, 1, true>, (void const*)k_window<0, true, 2, true>,
+	                           (void const*)k_window<0, true, 3, true>, (void const*)k_window<0, true, 4, true>,
+	                           (void const*)k_window<0, true, 5, true>, (void const*)k_window<0, true, 6, true>,
+	                           (void const*)k_window<0, true, 7, true>, (void const*)k_window<1, true, 0, true>}};
 	void const* fk_atomic_generic[2] = {(void const*)k_window<1, false, 0, false>, (void const*)k_window<1, false, 0, true>};
 	int const rec = nrb > 0 ? 1 : 0;
 	void const* fn = nullptr;
-	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 6 ? a.variant : 0)];
-	else fn = only_fast ? fns[rec][8] : fk_atomic_generic[rec];
+	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 7 ? a.variant : 0)];
+	else fn = only_fast ? fns[rec][9] : fk_atomic_generic[rec];
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks + nrb));
 	cfg.blockDim         = dim3((unsigned)kThreads);

@@ -384,7 +384,7 @@ def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threa
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_neuron_variants_match_reference(engine, variant):
     """Every LIF window variant of the neuron update (unrolled or rolled steps, per-lane or
     warp-uniform count replay) gives the reference's raster and V bit for bit."""
@@ -396,6 +396,29 @@ def test_neuron_variants_match_reference(engine, variant):
     assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
     for k in (1, 2):
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+
+
+@pytest.mark.parametrize("variant", [4, 5, 6, 7])
+def test_neuron_variants_with_large_counts(engine, oracle_lib, variant):
+    """Inputs of ~2.4 events per neuron and step from one group (counts of 8 or more, which take
+    the general replay, in about one warp-step in ten): every variant bit-exact with the oracle."""
+    sp, o = engine, oracle_lib
+    spec = {"dt": 1e-4, "max_delay": 2e-4, "seed": 12,
+            "pops": [("poisson", 4000, 30.0), ("lif", 1000), ("poisson", 3000, 15.0)],
+            "conns": [("f", 0, 1, 0.2, 2e-4, 0.003, 0), ("f", 2, 1, 0.3, 2e-4, -0.0011, 0)]}
+    net = sp.snn(spec["dt"], spec["max_delay"], [spec["seed"]])
+    pops = [net.add_population(sp.poisson(30.0), 4000), net.add_population(sp.lif(), 1000),
+            net.add_population(sp.poisson(15.0), 3000)]
+    for _, s_, d, p, delay, w, _f in spec["conns"]:
+        net.connect(pops[s_], pops[d], sp.fixed_probability(p), delay, sp.fixed_weight(float(np.float32(w))))
+    net.set_tuning(neuron_variant=variant)
+    ref, rpops, _ = o.weighted_net(spec)
+    raster = net.run_record(300)
+    for t in range(300):
+        ref.step()
+        assert np.array_equal(np.asarray(raster[t][1]), ref.spikes(rpops[1], 0)), t
+    assert sum(len(r[1]) for r in raster) > 100
+    assert np.array_equal(net.get_state(pops[1], sp.FIELD_V).view(np.uint32), ref.state(rpops[1], 0).view(np.uint32))
 
 
 @pytest.mark.parametrize("mode", [0, 1])

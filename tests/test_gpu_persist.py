@@ -13,6 +13,9 @@ def _compare_brunel(sp, o, N, p, seed, delay, steps, persistent, record=True):
     net, pops = sp.brunel(N, p, seed, delay=delay)
     net.set_tuning(persistent=persistent)
     ref, rpops = o.brunel(N, p, seed, delay=delay)
+    net.csr(0)  # the adjacency and the first launches of the net, before counting
+    net.run(0)
+    l0 = net.launch_count()
     if record:
         raster = net.run_record(steps)
         for t in range(steps):
@@ -22,29 +25,31 @@ def _compare_brunel(sp, o, N, p, seed, delay, steps, persistent, record=True):
     else:
         net.run(steps)
         ref.run(steps)
-        for k in range(3):
-            for age in range(3):
+        for k in range(3):  # the spike history holds max_delay steps (ages 0 .. D - 1)
+            for age in range(max(1, int(round(delay / 1e-4)))):
                 assert np.array_equal(net.spikes(pops[k], age), ref.spikes(rpops[k], age)), (k, age)
+    launches = net.launch_count() - l0
     for k in (1, 2):
         assert np.array_equal(net.get_state(pops[k], sp.FIELD_V).view(np.uint32), ref.state(rpops[k], 0).view(np.uint32))
         assert np.array_equal(net.get_state(pops[k], sp.FIELD_TREF), ref.state(rpops[k], 3))
-    return net
+    return net, launches
 
 
 @pytest.mark.parametrize("persistent", [1, 0, 2, 8])
 def test_delay_one_brunel_bit_exact(engine, oracle_lib, persistent):
     """Brunel with delay 1 step (windows of one step): raster and V / Tref equal the oracle's,
     persistent (default, 2 and 8 CTAs per SM) or one launch per phase."""
-    net = _compare_brunel(engine, oracle_lib, 6000, 0.05, 17, 1e-4, 400, persistent)
-    stats = net.kernel_stats(0)
+    net, launches = _compare_brunel(engine, oracle_lib, 6000, 0.05, 17, 1e-4, 400, persistent)
     if persistent:
-        assert net.launch_count() < 50  # one launch per chunk, not per step
-    assert stats is not None
+        assert launches <= 4  # jump tables and one cooperative launch per chunk, not launches per step
+    else:
+        assert launches >= 400
 
 
 def test_delay_one_brunel_unrecorded_and_stepwise(engine, oracle_lib):
     sp, o = engine, oracle_lib
     _compare_brunel(sp, o, 4000, 0.05, 3, 1e-4, 1500, 1, record=False)  # two chunks of 1024 steps
+    _compare_brunel(sp, o, 4000, 0.05, 4, 3e-4, 700, 1, record=False)   # delay 3: K = 3, not persistent
     net, pops = sp.brunel(3000, 0.1, 9, delay=1e-4)
     ref, rpops = o.brunel(3000, 0.1, 9, delay=1e-4)
     for t in range(120):
@@ -106,13 +111,15 @@ def test_counting_plastic_schedule_persistent(engine, oracle_lib, pdelay):
     ref, rpops = o.brunel(N, p, seed)
     rc = ref.connect(rpops[1], rpops[1], 0.05, pdelay, 0.0)
     ref.set_plastic(rc, o.SYN_COUNT)
+    net.run(0)
+    l0 = net.launch_count()
     raster = net.run_record(steps)
     for t in range(steps):
         ref.step()
         for k in range(3):
             assert np.array_equal(raster[t][k], ref.spikes(rpops[k], 0)), (t, k)
     assert np.array_equal(net.synapse_state(c, 0), ref.syn_state(rc, 0))
-    assert net.launch_count() < 60
+    assert net.launch_count() - l0 <= 4
 
 
 def test_persistent_knob_errors(engine):
