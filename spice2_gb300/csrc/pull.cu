@@ -242,37 +242,43 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 	uint64_t* A        = P.pull_A + base;
 	// 1. the active synapses, in connect order and ascending source order
 	int64_t nA = 0;
+	uint32_t const kmask = a.K >= 32 ? 0xffffffffu : (1u << a.K) - 1u;
 	for (int c = P.in_begin; c < P.in_end; c++) {
 		ConnDev const& C = a.conns[c];
 		int f            = 0;
 		while (f + 1 < F && P.pull_field[f] != C.field) f++;
-		int64_t const e0 = C.csc_off[i], e1 = C.csc_off[i + 1];
-		uint32_t const fw = __float_as_uint(C.weight);
-		// kPullUnroll coalesced chunks of 32 sources in flight per warp, then their tests and appends
-		// in entry order
-		for (int64_t eb = e0; eb < e1; eb += 32 * kPullUnroll) {
+		int64_t const e0    = C.csc_off[i];
+		int const len       = (int)(C.csc_off[i + 1] - e0);
+		const int32_t* col  = C.csc_src + e0;
+		const uint32_t* orb = C.pull_orb;
+		const uint32_t* wm  = C.pull_wm;
+		const float* cw     = C.csc_w ? C.csc_w + e0 : nullptr;
+		uint32_t const fw   = __float_as_uint(C.weight);
+		uint32_t const fb   = (uint32_t)f << 16;
+		// kPullUnroll coalesced chunks of 32 sources in flight per warp (streamed past L1, which keeps
+		// the window's source bits), then their tests and appends in entry order
+		for (int eb = 0; eb < len; eb += 32 * kPullUnroll) {
 			int32_t src[kPullUnroll];
 #pragma unroll
 			for (int u = 0; u < kPullUnroll; u++) {
-				int64_t const e = eb + 32 * u + lane;
-				src[u]          = e < e1 ? __ldg(C.csc_src + e) : -1;
+				int const e = eb + 32 * u + lane;
+				src[u]      = e < len ? __ldcs(col + e) : -1;
 			}
-			uint32_t orw[kPullUnroll];
+			uint32_t hit[kPullUnroll];
 #pragma unroll
-			for (int u = 0; u < kPullUnroll; u++) orw[u] = src[u] >= 0 ? __ldg(C.pull_orb + (src[u] >> 5)) : 0u;
+			for (int u = 0; u < kPullUnroll; u++) hit[u] = src[u] >= 0 ? (__ldg(orb + (src[u] >> 5)) >> (src[u] & 31)) & 1u : 0u;
 #pragma unroll
 			for (int u = 0; u < kPullUnroll; u++) {
-				if (eb + 32 * u >= e1) break;  // warp-uniform
-				int64_t const e = eb + 32 * u + lane;
-				bool act        = src[u] >= 0 && ((orw[u] >> (src[u] & 31)) & 1u);
+				if (!__any_sync(0xffffffffu, hit[u] != 0)) continue;  // warp-uniform: no source spiked
+				bool act   = hit[u] != 0;
 				uint32_t m = 0, wb = 0;
 				if (act) {
-					m   = __ldg(C.pull_wm + src[u]) & ((1u << a.K) - 1u);
-					wb  = C.csc_w ? __float_as_uint(__ldg(C.csc_w + e)) : fw;
+					m   = __ldg(wm + src[u]) & kmask;
+					wb  = cw ? __float_as_uint(__ldg(cw + eb + 32 * u + lane)) : fw;
 					act = m != 0;
 				}
 				unsigned const bal = __ballot_sync(0xffffffffu, act);
-				if (act) A[nA + __popc(bal & lanemask_lt_pull())] = (uint64_t)wb | ((uint64_t)(m | ((uint32_t)f << 16)) << 32);
+				if (act) A[nA + __popc(bal & lanemask_lt_pull())] = (uint64_t)wb | ((uint64_t)(m | fb) << 32);
 				nA += __popc(bal);
 			}
 		}

@@ -2640,13 +2640,15 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 // launch latency.  Here one cooperative launch runs every step of a chunk; the phases of a step
 // are separated by grid-wide barriers:
 //   A  the neuron update and source populations of step t (the window bodies with K = 1)
-//   B  (t mod 64 == 0, plastic connections) every plastic synapse catches up (snn.cpp:17-19)
 //   C  the deliveries of step t (snn.cpp:21-25) -- each fixed-weight connection's spikes of step t
 //      into ring slot (t + d - 1) mod D, and each plastic connection's spikes of step t - d + 1
 //      (catch-up, then the synapse's weight into slot t mod D), with global reductions, in work
 //      units of a warp and at most kPersistChunk synapses of one row; the raster of step t; the
-//      other parity's spike counts cleared.  A plastic source's `ages` word is written in phase A
-//      of the next step, when every unit of its row has read the old value.
+//      other parity's spike counts cleared.  At t mod 64 == 0 the plastic units cover every row:
+//      the periodic catch-up of every synapse (snn.cpp:17-19) and, for a spiking source, the
+//      delivery right after it -- the reference's order per synapse, with no barrier between.  A
+//      plastic source's `ages` word is written in phase A of the next step, when every unit of its
+//      row has read the old value.
 // Deterministic mode adds integer counts (exact in any order); atomic mode adds floats as the
 // window design does.
 // ---------------------------------------------------------------------------------------------
@@ -2681,19 +2683,63 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned& target, 
 	return *(volatile int*)status == 0;
 }
 
-// The catch-up and weight of one plastic synapse e of connection C at step `time` (the body of
-// k_plastic_deliver for one thread).
-__device__ __forceinline__ void plastic_deliver_one(ConnDev const& C, int64_t e, int64_t time, uint64_t ages,
-                                                    int64_t slot, bool deliver) {
-	SynState st{C.sW[e], C.sA[e], C.sB[e]};
-	int32_t const j = C.nb[e];
-	catch_up(C, st, time, ages, C.dst_hist[j]);
-	C.sW[e] = st.W;
-	C.sA[e] = st.A;
-	C.sB[e] = st.B;
-	if (deliver) {
-		float const v = C.plastic == SPICE_SYNAPSE_COUNT ? __fmul_rn(C.weight, st.W) : st.W;
-		red_add_f32(C.dst_acc + (slot * C.dst_size + j) * C.F + C.fslot, v);
+// The catch-up of synapses [e0, e1) of one plastic row to step `time` and, with `deliver`, their
+// weights into ring slot `slot`: lanes take every 32nd synapse, four at a time with their loads in
+// flight together (the per-synapse body of k_plastic_deliver / k_plastic_update_all).
+__device__ __forceinline__ void plastic_row_chunk(ConnDev const& C, int64_t e0, int64_t e1, int64_t time, uint64_t ages,
+                                                  int64_t slot, bool deliver, int lane) {
+	constexpr int U = 4;
+	for (int64_t eb = e0 + lane; eb < e1; eb += 32 * U) {
+		SynState st[U];
+		int32_t j[U];
+		uint64_t h[U];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			int64_t const e = eb + 32 * u;
+			if (e < e1) {
+				st[u] = SynState{C.sW[e], C.sA[e], C.sB[e]};
+				j[u]  = C.nb[e];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < U; u++)
+			if (eb + 32 * u < e1) h[u] = C.dst_hist[j[u]];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			int64_t const e = eb + 32 * u;
+			if (e >= e1) break;
+			catch_up(C, st[u], time, ages, h[u]);
+			C.sW[e] = st[u].W;
+			C.sA[e] = st[u].A;
+			C.sB[e] = st[u].B;
+			if (deliver) {
+				float const v = C.plastic == SPICE_SYNAPSE_COUNT ? __fmul_rn(C.weight, st[u].W) : st[u].W;
+				red_add_f32(C.dst_acc + (slot * C.dst_size + j[u]) * C.F + C.fslot, v);
+			}
+		}
+	}
+}
+
+// The ages of plastic sources after the deliveries of step t (phase C): every source caught up to
+// t + 1 when t mod 64 == 0, and the sources delivered at t with the pending pre update (bit 63).
+__device__ __forceinline__ void plastic_ages_after(PersistArgs const& a, int64_t t) {
+	bool const full = t % 64 == 0;
+	for (int c = 0; c < a.nconn; c++) {
+		ConnDev const& C = a.conns[c];
+		if (!C.plastic) continue;
+		bool const delivered = t >= C.delay - 1;
+		const uint32_t* bits = C.src_bits + ((t - C.delay + 1 + a.Hb) % a.Hb) * C.src_nwords;
+		for (int64_t wd = blockIdx.x * (int64_t)kPersistThreads + threadIdx.x; wd < C.src_nwords;
+		     wd += (int64_t)gridDim.x * kPersistThreads) {
+			uint32_t const m = delivered ? bits[wd] : 0u;
+			if (full) {
+				int64_t const s0 = 32 * wd, s1 = min(C.src_size, s0 + 32);
+				for (int64_t sidx = s0; sidx < s1; sidx++)
+					C.ages[sidx] = (uint64_t)(t + 1) | ((uint64_t)((m >> (sidx - s0)) & 1u) << 63);
+			} else {
+				for (uint32_t x = m; x; x &= x - 1) C.ages[32 * wd + __ffs(x) - 1] = (uint64_t)(t + 1) | (1ull << 63);
+			}
+		}
 	}
 }
 
@@ -2741,50 +2787,18 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 			}
 			__syncthreads();  // shared scratch of the bodies is reused by the next item
 		}
-		if (a.any_plastic && t > a.t0) {  // sources delivered at step t - 1: caught up to t
-			for (int c = 0; c < a.nconn; c++) {
-				ConnDev const& C = a.conns[c];
-				if (!C.plastic || t - 1 < C.delay - 1) continue;
-				const uint32_t* bits = C.src_bits + ((t - C.delay) % a.Hb) * C.src_nwords;
-				for (int64_t wd = blockIdx.x * (int64_t)kPersistThreads + threadIdx.x; wd < C.src_nwords;
-				     wd += (int64_t)gridDim.x * kPersistThreads)
-					for (uint32_t m = bits[wd]; m; m &= m - 1)
-						C.ages[32 * wd + __ffs(m) - 1] = (uint64_t)t | (1ull << 63);
-			}
-		}
+		if (a.any_plastic && t > a.t0) plastic_ages_after(a, t - 1);  // the deliveries of step t - 1
 		if (!grid_barrier(a.barrier, target, a.status)) return;
-		// ---- B: the periodic catch-up of every plastic synapse, a warp per source ----
-		if (a.any_plastic && t % 64 == 0) {
-			int64_t base = 0;
-			for (int c = 0; c < a.nconn; c++) {
-				ConnDev const& C = a.conns[c];
-				if (!C.plastic) continue;
-				for (int64_t u = gwarp - base; u < C.src_size; u += nwarps) {
-					if (u < 0) continue;
-					uint64_t const ages = C.ages[u];
-					for (int64_t e = C.off[u] + lane; e < C.off[u + 1]; e += 32) {
-						SynState st{C.sW[e], C.sA[e], C.sB[e]};
-						catch_up(C, st, t, ages, C.dst_hist[C.nb[e]]);
-						C.sW[e] = st.W;
-						C.sA[e] = st.A;
-						C.sB[e] = st.B;
-					}
-					__syncwarp();
-					if (lane == 0) C.ages[u] = (uint64_t)(t + 1);
-				}
-				base += C.src_size;
-				base %= nwarps;  // unit u of this connection runs on warp (base + u) mod nwarps
-			}
-			if (!grid_barrier(a.barrier, target, a.status)) return;
-		}
 		// ---- C: deliveries of step t, raster, counts of the other parity ----
+		bool const full = a.any_plastic && t % 64 == 0;  // every plastic row catches up
 		if (threadIdx.x == 0) {
 			int64_t acc = 0;
 			for (int c = 0; c < a.nconn; c++) {
 				ConnDev const& C = a.conns[c];
 				u_begin[c] = acc;
 				if (C.plastic) {
-					if (t >= C.delay - 1) acc += (int64_t)C.src_nwords * a.chunks[c];
+					if (full) acc += C.src_size * a.chunks[c];
+					else if (t >= C.delay - 1) acc += (int64_t)C.src_nwords * a.chunks[c];
 				} else {
 					acc += (int64_t)a.counts[q * a.npop + C.src] * a.chunks[c];
 				}
@@ -2811,17 +2825,25 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 			ConnDev const& C = a.conns[c];
 			int64_t const r  = u - u_begin[c];
 			int64_t const ch = r % a.chunks[c];
-			if (C.plastic) {  // unit: (bitmap word, chunk) of the spikes of step t - d + 1
-				int64_t const wd = r / a.chunks[c];
-				uint32_t m = C.src_bits[((t - C.delay + 1) % a.Hb) * C.src_nwords + wd];
-				bool const deliver = MODE == 1 && (C.plastic == SPICE_SYNAPSE_ISTDP || C.weight != 0.0f);
-				int64_t const slot = t % a.D;
-				for (; m; m &= m - 1) {
-					int64_t const src = 32 * wd + __ffs(m) - 1;
+			if (C.plastic) {
+				bool const delivers  = t >= C.delay - 1;
+				bool const weight_in = MODE == 1 && (C.plastic == SPICE_SYNAPSE_ISTDP || C.weight != 0.0f);
+				int64_t const slot   = t % a.D;
+				const uint32_t* bits = C.src_bits + ((t - C.delay + 1 + a.Hb) % a.Hb) * C.src_nwords;
+				if (full) {  // unit: (source, chunk) of every row: catch-up, then the delivery if it spiked
+					int64_t const src = r / a.chunks[c];
+					bool const spiked = delivers && ((bits[src >> 5] >> (src & 31)) & 1u);
 					int64_t const e0 = C.off[src] + ch * kPersistChunk, e1 = min(C.off[src + 1], e0 + kPersistChunk);
-					if (ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
-					uint64_t const ages = C.ages[src];
-					for (int64_t e = e0 + lane; e < e1; e += 32) plastic_deliver_one(C, e, t, ages, slot, deliver);
+					if (spiked && ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
+					plastic_row_chunk(C, e0, e1, t, C.ages[src], slot, spiked && weight_in, lane);
+				} else {  // unit: (bitmap word, chunk) of the spikes of step t - d + 1
+					int64_t const wd = r / a.chunks[c];
+					for (uint32_t m = bits[wd]; m; m &= m - 1) {
+						int64_t const src = 32 * wd + __ffs(m) - 1;
+						int64_t const e0 = C.off[src] + ch * kPersistChunk, e1 = min(C.off[src + 1], e0 + kPersistChunk);
+						if (ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
+						plastic_row_chunk(C, e0, e1, t, C.ages[src], slot, weight_in, lane);
+					}
 				}
 			} else {  // unit: (spike, chunk) of step t
 				int32_t const src = C.src_list[(int64_t)q * C.src_size + r / a.chunks[c]];
@@ -2840,18 +2862,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 		if (lane == 0 && ev) atomicAdd(&ev_block, ev);
 		if (!grid_barrier(a.barrier, target, a.status)) return;
 	}
-	// the ages of the last step's plastic deliveries
-	if (a.any_plastic) {
-		int64_t const t = a.t0 + a.nsteps;
-		for (int c = 0; c < a.nconn; c++) {
-			ConnDev const& C = a.conns[c];
-			if (!C.plastic || t - 1 < C.delay - 1) continue;
-			const uint32_t* bits = C.src_bits + ((t - C.delay) % a.Hb) * C.src_nwords;
-			for (int64_t wd = blockIdx.x * (int64_t)kPersistThreads + threadIdx.x; wd < C.src_nwords;
-			     wd += (int64_t)gridDim.x * kPersistThreads)
-				for (uint32_t m = bits[wd]; m; m &= m - 1) C.ages[32 * wd + __ffs(m) - 1] = (uint64_t)t | (1ull << 63);
-		}
-	}
+	if (a.any_plastic) plastic_ages_after(a, a.t0 + a.nsteps - 1);  // the deliveries of the last step
 	__syncthreads();
 	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
 }
