@@ -23,9 +23,54 @@ inline uint64_t pack_f64(double f) {
 
 __device__ __forceinline__ int bitlen64(uint64_t x) { return 64 - __clzll((long long)x); }
 
+// The common case -- a normal, the result a normal float -- with 32 x 32 -> 64-bit products: f's
+// significand split into its top 29 and low 24 bits, the exact product P = ma mf (76 or 77 bits) as
+// U 2^24 + Ylo, the double's 53 bits d (U, or U with Ylo's top bit, rounded by the rest), then 24
+// bits of d (rounded by its low 29).  Returns false (leaving *out alone) for the other cases.
+__device__ __forceinline__ bool mul_f32_f64_rn_normal(uint32_t ab, uint64_t packed, float* out) {
+	uint32_t const fa = ab >> 23;
+	if (fa == 0u) return false;  // subnormal a
+	uint32_t const ma = (ab & 0x7fffffu) | 0x800000u;
+	uint64_t const mf = packed & ((1ull << 53) - 1);
+	int const ef      = (int)(packed >> 53) - 1100;
+	uint32_t const fh = (uint32_t)(mf >> 24);        // 29 bits
+	uint32_t const fl = (uint32_t)mf & 0xffffffu;    // 24 bits
+	uint64_t const y  = (uint64_t)ma * fl;           // < 2^48
+	uint64_t const u  = (uint64_t)ma * fh + (y >> 24);  // floor(P / 2^24): 52 or 53 bits
+	uint32_t const ylo = (uint32_t)y & 0xffffffu;
+	uint64_t d;
+	int e;  // the double product = d 2^e, d of 53 bits
+	if (u >> 52) {  // P has 77 bits: d = U rounded by the 24 bits below
+		d = u + ((ylo > 0x800000u || (ylo == 0x800000u && (u & 1))) ? 1 : 0);
+		e = (int)fa - 150 + ef + 24;
+	} else {  // 76 bits: d = U and Ylo's top bit, rounded by the 23 bits below
+		uint64_t const k  = (u << 1) | (ylo >> 23);
+		uint32_t const z  = ylo & 0x7fffffu;
+		d = k + ((z > 0x400000u || (z == 0x400000u && (k & 1))) ? 1 : 0);
+		e = (int)fa - 150 + ef + 23;
+	}
+	if (d >> 53) {  // rounded up to 2^53
+		d >>= 1;
+		e += 1;
+	}
+	// 24 bits of d, rounded by its low 29
+	uint32_t const rem = (uint32_t)d & 0x1fffffffu;
+	uint64_t m         = (d >> 29) + ((rem > 0x10000000u || (rem == 0x10000000u && ((d >> 29) & 1))) ? 1 : 0);
+	int e2             = e + 29 + 23;  // the float's unbiased exponent
+	if (m >> 24) {
+		m >>= 1;
+		e2 += 1;
+	}
+	if (e2 < -126 || e2 > 127) return false;  // subnormal, zero or infinite result
+	*out = __uint_as_float(((uint32_t)(e2 + 127) << 23) | ((uint32_t)m & 0x7fffffu));
+	return true;
+}
+
 __device__ __forceinline__ float mul_f32_f64_rn(float a, uint64_t packed) {
 	uint32_t const ab = __float_as_uint(a);
 	if (ab == 0u) return 0.0f;
+	float fast;
+	if (mul_f32_f64_rn_normal(ab, packed, &fast)) return fast;
 	uint64_t const mf = packed & ((1ull << 53) - 1);
 	int const ef      = (int)(packed >> 53) - 1100;  // f = mf 2^ef
 	uint32_t const fa = ab >> 23;
