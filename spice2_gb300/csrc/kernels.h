@@ -245,6 +245,9 @@ struct PersistArgs {
 	int blk_per_step[kMaxPops];   // Poisson: items per step
 	int64_t ext_pos[kMaxPops];    // external: train position of step t0
 	int64_t chunks[kMaxConns];    // per connection: delivery units per spike (ceil(max row / kPersistChunk))
+	int start_at_c;               // the first step's update (phase A) ran in the previous launch
+	int end_after_a;              // the last step stops after its update (its deliveries follow in the next launch)
+	int external_full;            // the periodic catch-up of every plastic synapse runs as its own kernel
 	int record;                   // extract the raster of every step (RasterArgs below, K = 1)
 	int rec_parity0;              // raster base parity of step t0
 	RasterArgs raster;

@@ -1301,15 +1301,14 @@ int check_persist(spice_net* n) {
 	return SPICE_OK;
 }
 
-// The steps [time, time + chunk) of a network whose windows are one step long, as one cooperative
-// launch of k_persist (step.cu).
+// The steps [time, time + chunk) of a network whose windows are one step long, as cooperative
+// launches of k_persist (step.cu): one per chunk; with plastic connections the launches are split at
+// every step t with t mod 64 == 0, whose catch-up of every plastic synapse (snn.cpp:17-19) runs
+// between its update and its deliveries as its own kernel at full occupancy.
 int run_persist(spice_net* n, int64_t chunk, const float* d_dt, const u128* d_tables, bool record, int64_t rows,
                 int64_t rec_windows) {
 	int const np = (int)n->pops.size();
 	PersistArgs pa{};
-	pa.t0          = n->time;
-	pa.nsteps      = (int)chunk;
-	pa.parity0     = n->parity;
 	pa.D           = (int)n->max_delay;
 	pa.Hb          = n->Hb;
 	pa.npop        = np;
@@ -1317,13 +1316,12 @@ int run_persist(spice_net* n, int64_t chunk, const float* d_dt, const u128* d_ta
 	pa.mode        = n->mode;
 	pa.pops        = n->d_pops;
 	pa.conns       = n->d_conns;
-	pa.dts         = d_dt;
-	pa.tables      = n->total_draws > 0 ? d_tables : nullptr;
 	pa.counts      = n->d_counts;
 	pa.events      = n->d_events;
 	pa.barrier     = n->d_barrier;
 	pa.status      = n->d_pstatus;
 	pa.any_plastic = n->plastic ? 1 : 0;
+	pa.external_full = n->plastic ? 1 : 0;
 	int nb = 0;
 	for (int p = 0; p < np; p++) {
 		PopDev const& P = n->pops[p].d;
@@ -1334,8 +1332,6 @@ int run_persist(spice_net* n, int64_t chunk, const float* d_dt, const u128* d_ta
 			nb += pa.blk_per_step[p];
 		} else if (P.model == EXTERNAL) {
 			pa.blk_kind[p] = 2;
-			int64_t const ns = P.ext_steps;
-			pa.ext_pos[p] = ns > 0 ? ((n->time - n->ext_t_set[p]) % ns + ns) % ns : 0;
 			nb += 1;
 		} else {
 			pa.blk_kind[p] = neuron_block_kind(P) + (P.hist ? kHistKind : 0);
@@ -1355,16 +1351,58 @@ int run_persist(spice_net* n, int64_t chunk, const float* d_dt, const u128* d_ta
 		ra.out         = n->h_raster;
 		ra.capacity    = n->raster_cap;
 		ra.step_counts = n->h_rcounts;
-		ra.row0        = rows;
-		pa.rec_parity0 = (int)(rec_windows & 1);
 	}
-	CUDA_TRY(cudaMemsetAsync(n->d_barrier, 0, sizeof(unsigned), n->stream));
-	int slot = -1;
-	TRY(ev_begin(n, 0, &slot));
 	int const per_sm = n->persist_knob >= 2 ? n->persist_knob : kPersistBlocksPerSM;
-	CUDA_TRY(launch_persist(n->stream, pa, std::min(n->persist_grid, n->sm_count * per_sm)));
-	TRY(ev_end(n, slot));
-	n->launches++;
+	int const grid   = std::min(n->persist_grid, n->sm_count * per_sm);
+	// one launch over steps [s, e) of the chunk: start_at_c -- step s's update ran in the previous
+	// launch; end_after_a -- step e - 1 stops after its update
+	auto launch = [&](int64_t s, int64_t e, bool start_at_c, bool end_after_a) -> int {
+		int64_t const t0 = n->time + s;
+		pa.t0          = t0;
+		pa.nsteps      = (int)(e - s);
+		pa.parity0     = (n->parity + (int)(s & 1)) & 1;
+		pa.dts         = d_dt + s;
+		pa.tables      = n->total_draws > 0 ? d_tables + s * kJumpTable : nullptr;
+		pa.start_at_c  = start_at_c ? 1 : 0;
+		pa.end_after_a = end_after_a ? 1 : 0;
+		pa.rec_parity0 = (int)((rec_windows + s) & 1);
+		pa.raster.row0 = rows + s;
+		for (int p = 0; p < np; p++)
+			if (n->pops[p].d.model == EXTERNAL) {
+				int64_t const ns = n->pops[p].d.ext_steps;
+				pa.ext_pos[p] = ns > 0 ? ((t0 - n->ext_t_set[p]) % ns + ns) % ns : 0;
+			}
+		CUDA_TRY(cudaMemsetAsync(n->d_barrier, 0, sizeof(unsigned), n->stream));
+		int slot = -1;
+		TRY(ev_begin(n, 0, &slot));
+		CUDA_TRY(launch_persist(n->stream, pa, grid));
+		TRY(ev_end(n, slot));
+		n->launches++;
+		return SPICE_OK;
+	};
+	if (!n->plastic) {
+		TRY(launch(0, chunk, false, false));
+	} else {
+		int64_t s       = 0;
+		bool start_at_c = false;
+		while (s < chunk) {
+			// the next step f > s (or s itself, not yet updated) whose catch-up runs as its own kernel
+			int64_t f = s + (start_at_c ? 1 : 0);
+			while (f < chunk && (n->time + f) % 64 != 0) f++;
+			if (f >= chunk) {  // no catch-up in the rest of the chunk
+				TRY(launch(s, chunk, start_at_c, false));
+				break;
+			}
+			TRY(launch(s, f + 1, start_at_c, true));  // ... up to step f's update
+			for (auto const& c : n->conns)
+				if (c.d.plastic) {
+					CUDA_TRY(launch_plastic_update_all(n->stream, c.d, n->time + f));
+					n->launches++;
+				}
+			s          = f;
+			start_at_c = true;
+		}
+	}
 	CUDA_TRY(cudaMemcpyAsync(n->h_pstatus, n->d_pstatus, sizeof(int), cudaMemcpyDeviceToHost, n->stream));
 	return SPICE_OK;
 }

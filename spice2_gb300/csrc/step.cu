@@ -2721,9 +2721,10 @@ __device__ __forceinline__ void plastic_row_chunk(ConnDev const& C, int64_t e0, 
 }
 
 // The ages of plastic sources after the deliveries of step t (phase C): every source caught up to
-// t + 1 when t mod 64 == 0, and the sources delivered at t with the pending pre update (bit 63).
+// t + 1 when t mod 64 == 0 (unless that catch-up ran as its own kernel, which set them), and the
+// sources delivered at t with the pending pre update (bit 63).
 __device__ __forceinline__ void plastic_ages_after(PersistArgs const& a, int64_t t) {
-	bool const full = t % 64 == 0;
+	bool const full = t % 64 == 0 && !a.external_full;
 	for (int c = 0; c < a.nconn; c++) {
 		ConnDev const& C = a.conns[c];
 		if (!C.plastic) continue;
@@ -2770,8 +2771,10 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 		w.tables         = a.tables ? a.tables + (int64_t)s * kJumpTable : nullptr;
 		w.tab_net_stride = 0;
 		w.counts         = a.counts + q * a.npop;
+		bool const do_a  = !(s == 0 && a.start_at_c);
+		bool const do_c  = !(s == a.nsteps - 1 && a.end_after_a);
 		// ---- A: the update of step t; the ages of the previous step's plastic deliveries ----
-		for (int vb = blockIdx.x; vb < a.nblk; vb += gridDim.x) {
+		for (int vb = do_a ? (int)blockIdx.x : a.nblk; vb < a.nblk; vb += gridDim.x) {
 			int p = 0;
 			while (p + 1 < a.npop && vb >= a.blk_begin[p + 1]) p++;
 			int const lb   = vb - a.blk_begin[p];
@@ -2787,10 +2790,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 			}
 			__syncthreads();  // shared scratch of the bodies is reused by the next item
 		}
-		if (a.any_plastic && t > a.t0) plastic_ages_after(a, t - 1);  // the deliveries of step t - 1
-		if (!grid_barrier(a.barrier, target, a.status)) return;
+		if (do_a && a.any_plastic && t > a.t0) plastic_ages_after(a, t - 1);  // the deliveries of step t - 1
+		if (!do_c) break;  // the periodic catch-up kernel and the next launch follow
+		if (do_a && !grid_barrier(a.barrier, target, a.status)) return;
 		// ---- C: deliveries of step t, raster, counts of the other parity ----
-		bool const full = a.any_plastic && t % 64 == 0;  // every plastic row catches up
+		bool const full = a.any_plastic && t % 64 == 0 && !a.external_full;  // every plastic row catches up
 		if (threadIdx.x == 0) {
 			int64_t acc = 0;
 			for (int c = 0; c < a.nconn; c++) {
@@ -2862,7 +2866,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 		if (lane == 0 && ev) atomicAdd(&ev_block, ev);
 		if (!grid_barrier(a.barrier, target, a.status)) return;
 	}
-	if (a.any_plastic) plastic_ages_after(a, a.t0 + a.nsteps - 1);  // the deliveries of the last step
+	if (a.any_plastic && !a.end_after_a) plastic_ages_after(a, a.t0 + a.nsteps - 1);  // the last step's deliveries
 	__syncthreads();
 	if (threadIdx.x == 0 && ev_block) atomicAdd(a.events, ev_block);
 }

@@ -119,7 +119,8 @@ def test_counting_plastic_schedule_persistent(engine, oracle_lib, pdelay):
         for k in range(3):
             assert np.array_equal(raster[t][k], ref.spikes(rpops[k], 0)), (t, k)
     assert np.array_equal(net.synapse_state(c, 0), ref.syn_state(rc, 0))
-    assert net.launch_count() - l0 <= 4
+    # per 64 steps: one cooperative launch and the periodic catch-up kernel between two of them
+    assert net.launch_count() - l0 <= 2 * (steps // 64 + 2)
 
 
 def test_persistent_knob_errors(engine):
