@@ -270,7 +270,7 @@ int spice_get_csc(spice_net* net, int conn, int64_t* col_offsets_out, int32_t* s
  * floor(dst*p + 3 sqrt(dst*p*(1-p)))); larger requests fail with SPICE_EINVAL.  A neighbors buffer
  * that is too small fails with SPICE_EOVERFLOW and *synapses_out = the size needed.
  * The first call on a device (and the first after its context was reset) looks up the scratch
- * array's device address; make that first call before any stream capture.  Every call uses the
+ * array's device address.  Every call uses the
  * same scratch, which keeps the previous call's contents, so calls whose GPU work overlaps (on
  * different streams or threads) race: serialise them.  The call synchronises `stream` (a
  * cudaStream_t, NULL for the default stream) once, to read the synapse count. */
