@@ -208,7 +208,8 @@ enum {
 	                                   leak factors computed once per CTA, 7 as 6 with
 	                                   predicated adds, a warp-uniform test for counts of 8 or
 	                                   more, ballots kept in registers and list entries reserved
-	                                   only for the steps with spikes                         */
+	                                   only for the steps with spikes, 8 as 7 with two neurons
+	                                   per thread                                             */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

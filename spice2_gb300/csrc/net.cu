@@ -1477,6 +1477,13 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			wa.variant = n->neuron_variant;
 			WindowArgs ws = wa;  // sources
 			int nb = 0, nbs = 0;
+			// neurons per neuron-update CTA: 2 per thread with LIF window variant 8, which applies when
+			// every per-neuron population takes the fast LIF path (deterministic mode)
+			bool only_fast = n->mode == SPICE_MODE_DETERMINISTIC;
+			for (auto const& P : n->pops)
+				if (P.d.model != POISSON && P.d.model != EXTERNAL)
+					only_fast &= P.d.model != USER && neuron_block_kind(P.d) == 3 && !P.d.hist;
+			int const lif_per_cta = (only_fast && n->neuron_variant == 8) ? 2 * kNeuronThreads : kNeuronThreads;
 			for (int p = 0; p < np; p++) {
 				PopDev const& P = n->pops[p].d;
 				wa.blk_begin[p] = nb;
@@ -1498,7 +1505,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				} else {
 					wa.blk_kind[p] = neuron_block_kind(P) + (P.hist ? kHistKind : 0);
 					ws.blk_kind[p] = wa.blk_kind[p];
-					nb += (int)((P.size + kNeuronThreads - 1) / kNeuronThreads);
+					nb += (int)((P.size + lif_per_cta - 1) / lif_per_cta);
 				}
 			}
 			// Poisson CTAs: src_steps consecutive steps each -- by default the fewest that keep the
@@ -2065,7 +2072,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->persist_knob = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
-			if (value < 0 || value > 7) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 7");
+			if (value < 0 || value > 8) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 8");
 			n->neuron_variant = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:

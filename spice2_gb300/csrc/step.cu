@@ -693,6 +693,118 @@ __device__ __forceinline__ void window_lif_lean(A const& a, const PopDev* __rest
 	}
 }
 
+// Variant 8: variant 7 with two neurons per thread (neurons b*256 + tid and b*256 + 128 + tid of a
+// 128-thread CTA): the step loop's control, the leak factor and the large-count test are shared by
+// both, and the window's grid has half the neuron CTAs.  Same arithmetic and outputs per neuron.
+template <class A>
+__device__ __forceinline__ void window_lif_lean2(A const& a, const PopDev* __restrict__ Pg, int p, int b,
+                                                 const float* dts_sm, uint32_t (*xs_sm)[2 * kThreads]) {
+	int const N    = (int)Pg->size;
+	int const lane = threadIdx.x & 31;
+	int const i0   = b * 2 * kThreads + threadIdx.x, i1 = i0 + kThreads;
+	bool const v0 = i0 < N, v1 = i1 < N;
+	int const word0 = i0 >> 5, word1 = i1 >> 5;
+	uint32_t* const cnt = Pg->cnt;
+	bool const zero     = Pg->zero_inputs != 0;
+	float const vthres  = Pg->p0;
+	int32_t const tref  = (int32_t)Pg->p1;
+	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
+	float V0 = 0, V1 = 0;
+	int32_t T0 = 0, T1 = 0;
+	if (v0) {  // written two launches back: loaded before waiting for the previous launch
+		V0 = Pg->V[i0];
+		T0 = Pg->T[i0];
+	}
+	if (v1) {
+		V1 = Pg->V[i1];
+		T1 = Pg->T[i1];
+	}
+	griddep_wait();  // the input ring, counts and lists are the previous launches' output
+	int const D = (int)a.D, Hb = a.Hb;
+	for (int k0 = 0; k0 < a.K; k0 += 16) {
+		int const nk    = min(16, a.K - k0);
+		int const slot0 = (int)((a.slot0 + k0) % D);
+		const uint32_t* src = cnt + (int64_t)slot0 * N + i0;
+		int const wrap      = D - slot0;  // step u >= wrap reads ring slot u - wrap
+#pragma unroll
+		for (int u = 0; u < 16; u++) {  // asynchronous copies into the thread's two shared-memory columns
+			if (u == wrap) src -= (int64_t)D * N;
+			unsigned const dst = (unsigned)__cvta_generic_to_shared(&xs_sm[u][threadIdx.x]);
+			if (v0 && u < nk) asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+			else xs_sm[u][threadIdx.x] = 0u;
+			if (v1 && u < nk)
+				asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst + 4u * kThreads), "l"(src + kThreads) : "memory");
+			else xs_sm[u][kThreads + threadIdx.x] = 0u;
+			src += N;
+		}
+		asm volatile("cp.async.wait_all;" ::: "memory");
+		uint32_t sb0 = 0, sb1 = 0;  // this thread's spikes of the 16 steps
+		uint32_t my0 = 0, my1 = 0;  // lane u: the warp's ballots of step u
+#pragma unroll 1
+		for (int u = 0; u < nk; u++) {
+			uint32_t const x0 = xs_sm[u][threadIdx.x], x1 = xs_sm[u][kThreads + threadIdx.x];
+			if (__any_sync(0xffffffffu, ((x0 | x1) & 0xfff8fff8u) != 0)) {  // a count of 8 or more in the warp
+				V0 = add_n_sel(V0, w0, x0 & 0xffffu);
+				V0 = add_n_sel(V0, w1, x0 >> 16);
+				V1 = add_n_sel(V1, w0, x1 & 0xffffu);
+				V1 = add_n_sel(V1, w1, x1 >> 16);
+			} else {
+				if (x0 & 4u) V0 = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V0, w0), w0), w0), w0);
+				if (x1 & 4u) V1 = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V1, w0), w0), w0), w0);
+				if (x0 & 2u) V0 = __fadd_rn(__fadd_rn(V0, w0), w0);
+				if (x1 & 2u) V1 = __fadd_rn(__fadd_rn(V1, w0), w0);
+				if (x0 & 1u) V0 = __fadd_rn(V0, w0);
+				if (x1 & 1u) V1 = __fadd_rn(V1, w0);
+				if (x0 & 0x40000u) V0 = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V0, w1), w1), w1), w1);
+				if (x1 & 0x40000u) V1 = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(V1, w1), w1), w1), w1);
+				if (x0 & 0x20000u) V0 = __fadd_rn(__fadd_rn(V0, w1), w1);
+				if (x1 & 0x20000u) V1 = __fadd_rn(__fadd_rn(V1, w1), w1);
+				if (x0 & 0x10000u) V0 = __fadd_rn(V0, w1);
+				if (x1 & 0x10000u) V1 = __fadd_rn(V1, w1);
+			}
+			if (zero) {
+				int64_t const o = (int64_t)((slot0 + u) % D) * N;
+				if (x0) cnt[o + i0] = 0;
+				if (x1) cnt[o + i1] = 0;
+			}
+			float const om = dts_sm[k0 + u];
+			bool const s0  = lif_update(V0, T0, om, vthres, tref) && v0;
+			bool const s1  = lif_update(V1, T1, om, vthres, tref) && v1;
+			sb0 |= (uint32_t)s0 << u;
+			sb1 |= (uint32_t)s1 << u;
+			unsigned const m0 = __ballot_sync(0xffffffffu, s0);
+			unsigned const m1 = __ballot_sync(0xffffffffu, s1);
+			my0 = lane == u ? m0 : my0;
+			my1 = lane == u ? m1 : my1;
+		}
+		if (lane < nk) {
+			int64_t const row = (int64_t)((a.hslot0 + k0 + lane) % Hb) * Pg->nwords;
+			if (word0 < Pg->nwords) Pg->bits[row + word0] = my0;
+			if (word1 < Pg->nwords) Pg->bits[row + word1] = my1;
+		}
+		// list reservations, one per step in which the warp spiked
+		for (unsigned st = __reduce_or_sync(0xffffffffu, sb0 | sb1); st; st &= st - 1) {
+			int const u    = __ffs(st) - 1;
+			unsigned const mask0 = __shfl_sync(0xffffffffu, my0, u);
+			unsigned const mask1 = __shfl_sync(0xffffffffu, my1, u);
+			int base = 0;
+			if (lane == 0) base = atomicAdd(a.counts + (k0 + u) * a.npop + p, __popc(mask0) + __popc(mask1));
+			base = __shfl_sync(0xffffffffu, base, 0);
+			int32_t* const out = Pg->list + (int64_t)(a.list_k0 + k0 + u) * N + base;
+			if ((sb0 >> u) & 1u) out[__popc(mask0 & lanemask_lt())] = i0;
+			if ((sb1 >> u) & 1u) out[__popc(mask0) + __popc(mask1 & lanemask_lt())] = i1;
+		}
+	}
+	if (v0) {
+		Pg->V[i0] = V0;
+		Pg->T[i0] = T0;
+	}
+	if (v1) {
+		Pg->V[i1] = V1;
+		Pg->T[i1] = T1;
+	}
+}
+
 // One step of a Poisson population (samples/brunel.cpp:27-30): thread c owns neurons
 // [32c, 32c + 32), jumps to draw draw_offset + 32c of the step's stream and draws 32 numbers.
 // The jump XORs the states T^i(s), i < 128, selected by the 128 bits of x^(offset) mod P; the step's
@@ -795,15 +907,15 @@ __device__ void window_external(A const& a, const PopDev* __restrict__ Pg, int p
 // One CTA of the neuron update (block b of the window's neuron blocks).
 template <int MODE, bool ONLY_FAST, int VAR>
 __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
-	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;  // 4 .. 7: deferred spike output
+	constexpr bool ROLLED = VAR == 1 || VAR == 2 || VAR >= 4;  // 4 .. 8: deferred spike output
 	__shared__ float dts_sm[kMaxWindow];
-	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][kThreads];
+	__shared__ uint32_t xs_sm[ROLLED ? 16 : 1][VAR == 8 ? 2 * kThreads : kThreads];
 	__shared__ uint32_t masks_sm[VAR >= 4 && VAR <= 6 ? kThreads / 32 : 1][16];
 	int p = 0;
 	while (p + 1 < a.npop && b >= a.blk_begin[p + 1]) p++;
 	int const lb   = b - a.blk_begin[p];
 	int const kind = a.blk_kind[p];
-	if ((VAR == 6 || VAR == 7) && MODE == 0 && kind == 3) {  // the LIF leak factors of the window's steps
+	if (VAR >= 6 && MODE == 0 && kind == 3) {  // the LIF leak factors of the window's steps
 		float const tminv = a.pops[p].p2;
 		for (int k = threadIdx.x; k < a.K; k += blockDim.x) dts_sm[k] = __fmaf_rn(-a.dts[k], tminv, 1.0f);
 	} else {
@@ -812,10 +924,11 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 	__syncthreads();
 	// window_lif_deferred waits for the previous launch after loading the state; the others first
 	if (MODE == 0 && kind == 3) {
-		if (VAR == 4) window_lif_deferred<false, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
-		else if (VAR == 5) window_lif_deferred<true, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
-		else if (VAR == 6) window_lif_deferred<false, true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
-		else if (VAR == 7) window_lif_lean(a, a.pops + p, p, lb, dts_sm, xs_sm);
+		if constexpr (VAR == 8) window_lif_lean2(a, a.pops + p, p, lb, dts_sm, xs_sm);
+		else if constexpr (VAR == 7) window_lif_lean(a, a.pops + p, p, lb, dts_sm, xs_sm);
+		else if constexpr (VAR == 4) window_lif_deferred<false, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else if constexpr (VAR == 5) window_lif_deferred<true, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
+		else if constexpr (VAR == 6) window_lif_deferred<false, true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else {
 			griddep_wait();
 			window_lif_fast<ROLLED, VAR == 2 || VAR == 3>(a, a.pops + p, p, lb, dts_sm, xs_sm);
@@ -2424,19 +2537,49 @@ __device__ __forceinline__ void catch_up(ConnDev const& C, SynState& s, int64_t 
 	syn_skip(C, s, 64 - p);
 }
 
+// The catch-up of synapses [e0, e1) of one plastic row to step `time` and, with `deliver`, their
+// weights into ring slot `slot`: lanes take every 32nd synapse, four at a time with their loads in
+// flight together (the per-synapse body of k_plastic_deliver / k_plastic_update_all).
+__device__ __forceinline__ void plastic_row_chunk(ConnDev const& C, int64_t e0, int64_t e1, int64_t time, uint64_t ages,
+                                                  int64_t slot, bool deliver, int lane) {
+	constexpr int U = 4;
+	for (int64_t eb = e0 + lane; eb < e1; eb += 32 * U) {
+		SynState st[U];
+		int32_t j[U];
+		uint64_t h[U];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			int64_t const e = eb + 32 * u;
+			if (e < e1) {
+				st[u] = SynState{C.sW[e], C.sA[e], C.sB[e]};
+				j[u]  = C.nb[e];
+			}
+		}
+#pragma unroll
+		for (int u = 0; u < U; u++)
+			if (eb + 32 * u < e1) h[u] = C.dst_hist[j[u]];
+#pragma unroll
+		for (int u = 0; u < U; u++) {
+			int64_t const e = eb + 32 * u;
+			if (e >= e1) break;
+			catch_up(C, st[u], time, ages, h[u]);
+			C.sW[e] = st[u].W;
+			C.sA[e] = st[u].A;
+			C.sB[e] = st[u].B;
+			if (deliver) {
+				float const v = C.plastic == SPICE_SYNAPSE_COUNT ? __fmul_rn(C.weight, st[u].W) : st[u].W;
+				red_add_f32(C.dst_acc + (slot * C.dst_size + j[u]) * C.F + C.fslot, v);
+			}
+		}
+	}
+}
+
 // Every 64 steps (snn.cpp:17-19): every synapse of the connection catches up; a warp per source.
 __global__ void __launch_bounds__(256) k_plastic_update_all(const __grid_constant__ ConnDev C, int64_t time) {
 	int const lane = threadIdx.x & 31;
 	int64_t const src = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
 	if (src >= C.src_size) return;
-	uint64_t const ages = C.ages[src];
-	for (int64_t e = C.off[src] + lane; e < C.off[src + 1]; e += 32) {
-		SynState st{C.sW[e], C.sA[e], C.sB[e]};
-		catch_up(C, st, time, ages, C.dst_hist[C.nb[e]]);
-		C.sW[e] = st.W;
-		C.sA[e] = st.A;
-		C.sB[e] = st.B;
-	}
+	plastic_row_chunk(C, C.off[src], C.off[src + 1], time, C.ages[src], 0, false, lane);
 	__syncwarp();
 	if (lane == 0) C.ages[src] = (uint64_t)(time + 1);
 }
@@ -2683,43 +2826,6 @@ __device__ __forceinline__ bool grid_barrier(unsigned* count, unsigned& target, 
 	return *(volatile int*)status == 0;
 }
 
-// The catch-up of synapses [e0, e1) of one plastic row to step `time` and, with `deliver`, their
-// weights into ring slot `slot`: lanes take every 32nd synapse, four at a time with their loads in
-// flight together (the per-synapse body of k_plastic_deliver / k_plastic_update_all).
-__device__ __forceinline__ void plastic_row_chunk(ConnDev const& C, int64_t e0, int64_t e1, int64_t time, uint64_t ages,
-                                                  int64_t slot, bool deliver, int lane) {
-	constexpr int U = 4;
-	for (int64_t eb = e0 + lane; eb < e1; eb += 32 * U) {
-		SynState st[U];
-		int32_t j[U];
-		uint64_t h[U];
-#pragma unroll
-		for (int u = 0; u < U; u++) {
-			int64_t const e = eb + 32 * u;
-			if (e < e1) {
-				st[u] = SynState{C.sW[e], C.sA[e], C.sB[e]};
-				j[u]  = C.nb[e];
-			}
-		}
-#pragma unroll
-		for (int u = 0; u < U; u++)
-			if (eb + 32 * u < e1) h[u] = C.dst_hist[j[u]];
-#pragma unroll
-		for (int u = 0; u < U; u++) {
-			int64_t const e = eb + 32 * u;
-			if (e >= e1) break;
-			catch_up(C, st[u], time, ages, h[u]);
-			C.sW[e] = st[u].W;
-			C.sA[e] = st[u].A;
-			C.sB[e] = st[u].B;
-			if (deliver) {
-				float const v = C.plastic == SPICE_SYNAPSE_COUNT ? __fmul_rn(C.weight, st[u].W) : st[u].W;
-				red_add_f32(C.dst_acc + (slot * C.dst_size + j[u]) * C.F + C.fslot, v);
-			}
-		}
-	}
-}
-
 // The ages of plastic sources after the deliveries of step t (phase C): every source caught up to
 // t + 1 when t mod 64 == 0 (unless that catch-up ran as its own kernel, which set them), and the
 // sources delivered at t with the pending pre update (bit 63).
@@ -2928,6 +3034,7 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 		else if (a.variant == 5) k_neurons<0, true, 5><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 6) k_neurons<0, true, 6><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 7) k_neurons<0, true, 7><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 8) k_neurons<0, true, 8><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
 		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
@@ -2942,21 +3049,23 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	if (nblocks + nsrc_blocks + nrb <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
-	void const* fns[2][10] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
+	void const* fns[2][11] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
 	                           (void const*)k_window<0, true, 1, false>, (void const*)k_window<0, true, 2, false>,
 	                           (void const*)k_window<0, true, 3, false>, (void const*)k_window<0, true, 4, false>,
 	                           (void const*)k_window<0, true, 5, false>, (void const*)k_window<0, true, 6, false>,
-	                           (void const*)k_window<0, true, 7, false>, (void const*)k_window<1, true, 0, false>},
+	                           (void const*)k_window<0, true, 7, false>, (void const*)k_window<0, true, 8, false>,
+	                           (void const*)k_window<1, true, 0, false>},
 	                          {(void const*)k_window<0, false, 0, true>, (void const*)k_window<0, true, 0, true>,
 	                           (void const*)k_window<0, true, 1, true>, (void const*)k_window<0, true, 2, true>,
 	                           (void const*)k_window<0, true, 3, true>, (void const*)k_window<0, true, 4, true>,
 	                           (void const*)k_window<0, true, 5, true>, (void const*)k_window<0, true, 6, true>,
-	                           (void const*)k_window<0, true, 7, true>, (void const*)k_window<1, true, 0, true>}};
+	                           (void const*)k_window<0, true, 7, true>, (void const*)k_window<0, true, 8, true>,
+	                           (void const*)k_window<1, true, 0, true>}};
 	void const* fk_atomic_generic[2] = {(void const*)k_window<1, false, 0, false>, (void const*)k_window<1, false, 0, true>};
 	int const rec = nrb > 0 ? 1 : 0;
 	void const* fn = nullptr;
-	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 7 ? a.variant : 0)];
-	else fn = only_fast ? fns[rec][9] : fk_atomic_generic[rec];
+	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 8 ? a.variant : 0)];
+	else fn = only_fast ? fns[rec][10] : fk_atomic_generic[rec];
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks + nrb));
 	cfg.blockDim         = dim3((unsigned)kThreads);
