@@ -2579,7 +2579,14 @@ __global__ void __launch_bounds__(256) k_plastic_update_all(const __grid_constan
 	int const lane = threadIdx.x & 31;
 	int64_t const src = (int64_t)blockIdx.x * 8 + (threadIdx.x >> 5);
 	if (src >= C.src_size) return;
-	plastic_row_chunk(C, C.off[src], C.off[src + 1], time, C.ages[src], 0, false, lane);
+	uint64_t const ages = C.ages[src];
+	for (int64_t e = C.off[src] + lane; e < C.off[src + 1]; e += 32) {  // one synapse per lane at a time
+		SynState st{C.sW[e], C.sA[e], C.sB[e]};                           // (more in flight lowered the
+		catch_up(C, st, time, ages, C.dst_hist[C.nb[e]]);                  // occupancy and lost)
+		C.sW[e] = st.W;
+		C.sA[e] = st.A;
+		C.sB[e] = st.B;
+	}
 	__syncwarp();
 	if (lane == 0) C.ages[src] = (uint64_t)(time + 1);
 }
