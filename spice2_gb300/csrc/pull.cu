@@ -224,18 +224,12 @@ __device__ __forceinline__ void bin_pass(uint32_t m, int f, int F, int nbins, in
 	}
 }
 
-// One warp per target neuron of the pulled populations.
-__global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ PullArgs a) {
-	__shared__ int bin_cnt[kPullWarps][kMaxBins + 1];
-	__shared__ int bin_run[kPullWarps][kMaxBins + 1];
-	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-	int const blk  = (int)blockIdx.x;
-	int q          = 0;
-	while (q + 1 < a.npull && blk >= a.pull_blk[q + 1]) q++;
-	int const pi     = a.pull_pops[q];
-	PopDev const& P  = a.pops[pi];
-	int64_t const i  = (int64_t)(blk - a.pull_blk[q]) * kPullWarps + wid;
-	if (i >= P.size) return;
+// The pull of one target neuron i of pulled population pi by one warp.  (A variant with the
+// window's bitmaps in shared memory and CTAs resident on every SM, looping over the targets, ran
+// 2.3x slower: at 16 warps per SM the scan has too few loads in flight.)
+__device__ __forceinline__ void pull_target(PullArgs const& a, int pi, int64_t i, int lane, int* bin_cnt_w,
+                                            int* bin_run_w) {
+	PopDev const& P = a.pops[pi];
 	int const F = P.pull_F, nbins = a.K * F;
 	int64_t const base = P.pull_base[i];
 	int64_t const cap  = P.pull_base[i + 1] - base;
@@ -286,26 +280,26 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 	__syncwarp();
 	int32_t* ko = P.pull_koff + i * (int64_t)(P.pull_nbins + 1);
 	// 2. entries per bin (an entry with several step bits lands in several bins)
-	for (int bn = lane; bn <= nbins; bn += 32) bin_cnt[wid][bn] = 0;
+	for (int bn = lane; bn <= nbins; bn += 32) bin_cnt_w[bn] = 0;
 	__syncwarp();
 	for (int64_t c0 = 0; c0 < nA; c0 += 32) {
 		int64_t const e = c0 + lane;
 		uint32_t const mf = e < nA ? (uint32_t)(A[e] >> 32) : 0u;
-		bin_pass<false>(mf & 0xffffu, (int)(mf >> 16), F, nbins, lane, bin_cnt[wid], bin_run[wid], nullptr, 0u);
+		bin_pass<false>(mf & 0xffffu, (int)(mf >> 16), F, nbins, lane, bin_cnt_w, bin_run_w, nullptr, 0u);
 	}
 	__syncwarp();
 	// exclusive prefix over the bins
 	int64_t total = 0;
 	for (int b0 = 0; b0 < nbins; b0 += 32) {
 		int const bn = b0 + lane;
-		int const v  = bn < nbins ? bin_cnt[wid][bn] : 0;
+		int const v  = bn < nbins ? bin_cnt_w[bn] : 0;
 		int incl     = v;
 #pragma unroll
 		for (int d = 1; d < 32; d <<= 1) {
 			int const o = __shfl_up_sync(0xffffffffu, incl, d);
 			if (lane >= d) incl += o;
 		}
-		if (bn < nbins) bin_run[wid][bn] = (int)total + incl - v;
+		if (bn < nbins) bin_run_w[bn] = (int)total + incl - v;
 		total += __shfl_sync(0xffffffffu, incl, 31);
 	}
 	__syncwarp();
@@ -316,7 +310,7 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 		}
 		return;
 	}
-	for (int bn = lane; bn < nbins; bn += 32) ko[bn] = bin_run[wid][bn];
+	for (int bn = lane; bn < nbins; bn += 32) ko[bn] = bin_run_w[bn];
 	if (lane == 0) ko[nbins] = (int32_t)total;
 	__syncwarp();
 	// 3. stable placement: chunks in order, and within a chunk lanes in order per bin
@@ -325,8 +319,21 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 		int64_t const e = c0 + lane;
 		uint64_t const v = e < nA ? A[e] : 0ull;
 		uint32_t const mf = (uint32_t)(v >> 32);
-		bin_pass<true>(mf & 0xffffu, (int)(mf >> 16), F, nbins, lane, bin_cnt[wid], bin_run[wid], G, (uint32_t)v);
+		bin_pass<true>(mf & 0xffffu, (int)(mf >> 16), F, nbins, lane, bin_cnt_w, bin_run_w, G, (uint32_t)v);
 	}
+}
+
+// One warp per target neuron of the pulled populations.
+__global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ PullArgs a) {
+	__shared__ int bin_cnt[kPullWarps][kMaxBins + 1];
+	__shared__ int bin_run[kPullWarps][kMaxBins + 1];
+	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	int const blk  = (int)blockIdx.x;
+	int q          = 0;
+	while (q + 1 < a.npull && blk >= a.pull_blk[q + 1]) q++;
+	int64_t const i = (int64_t)(blk - a.pull_blk[q]) * kPullWarps + wid;
+	if (i >= a.pops[a.pull_pops[q]].size) return;
+	pull_target(a, a.pull_pops[q], i, lane, bin_cnt[wid], bin_run[wid]);
 }
 
 // The inputs of the first pulled step (bins k = 0), applied now and removed from the bins: state
