@@ -95,6 +95,9 @@ struct PopDev {
 	float* pull_G;             // the active synapses' weights grouped by bin
 	int32_t* pull_koff;        // [size][nbins + 1] bin starts in the region; [i][0] = -1: not grouped,
 	                           // [i][1] = number of active synapses (the neuron walks pull_A)
+	int32_t* pull_fill;        // [size] entries pushed for the target this window (push-and-sort gather)
+	uint64_t* ps_key;          // [size][kPushSortSlots] their sort keys (push-and-sort gather)
+	float* ps_w;               // [size][kPushSortSlots] their weights
 	int direct;                // USER_DELIVER target: inputs applied into the neuron structs at the end of each step
 };
 
@@ -300,6 +303,14 @@ struct spice_net {
 	int* d_pull_pops     = nullptr;  // [npull]
 	int* d_pull_blk      = nullptr;  // [npull + 1] prefix of their pull CTAs
 	int pull_blocks      = 0;
+	// push-and-sort gather of the pulled populations (pull.cu k_ps_*): units (pulled connection,
+	// source bitmap word); falls back to the CSC scan when a row is too long for the sort key
+	bool ps_ok           = false;
+	int ps_nconn         = 0;
+	int* d_ps_conn       = nullptr;  // [ps_nconn] connection (by-target position) of each pulled connection
+	int* d_ps_pop        = nullptr;  // [ps_nconn] its pulled population
+	int64_t* d_ps_begin  = nullptr;  // [ps_nconn + 1] prefix of their source bitmap words
+	int64_t ps_units     = 0;
 };
 
 namespace spice_gb300 {

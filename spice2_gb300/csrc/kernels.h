@@ -79,9 +79,20 @@ struct PullArgs {
 	int pull_blocks;
 	const PopDev* pops;
 	const ConnDev* conns;    // by-target order (PopDev::in_begin / in_end)
+	// push-and-sort gather (ps_units > 0): the active synapses of every pulled connection are pushed
+	// into their targets' regions, then each target sorts its entries into the scan's order
+	int ps_nconn;
+	const int* ps_conn;      // [ps_nconn] by-target position of each pulled connection
+	const int* ps_pop;       // [ps_nconn] its pulled population
+	const int64_t* ps_begin; // [ps_nconn + 1] prefix of the source bitmap words (work units)
+	int64_t ps_units;
 };
 cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<PullSet> const& sets,
                         std::vector<PullEvJob> const& ev);
+// the longest source row the push-and-sort gather's sort key can hold (its CSR offset within the row)
+constexpr int64_t kPushSortMaxRow = 1ll << 19;
+// entries one target can take per window in the push-and-sort gather (more: the scan)
+constexpr int kPushSortSlots = 64;
 int pull_blocks_for(int64_t size);  // k_pull CTAs of a population of `size` neurons
 // Applies the bins of the first pulled step to the state and empties them (state reads).
 cudaError_t launch_pull_apply_first(cudaStream_t stream, PopDev const& P);

@@ -733,10 +733,45 @@ int setup_pull(spice_net* n) {
 		TRY(dalloc(n, &d.pull_A, (size_t)std::max<int64_t>(total, 1), false));
 		TRY(dalloc(n, &d.pull_G, (size_t)std::max<int64_t>(total, 1), false));
 		TRY(dalloc(n, &d.pull_koff, (size_t)std::max<int64_t>(d.size, 1) * (d.pull_nbins + 1)));  // zero: no inputs yet
+		TRY(dalloc(n, &d.pull_fill, (size_t)std::max<int64_t>(d.size, 1)));
 		n->pull_pops.push_back(pi);
 		blk.push_back(blk.back() + pull_blocks_for(d.size));
 	}
 	n->pull_blocks = blk.back();
+	{  // push-and-sort gather: units (pulled connection, source bitmap word); rows must fit the sort key
+		std::vector<int> ps_conn, ps_pop;
+		std::vector<int64_t> ps_begin(1, 0);
+		bool ok = !n->pull_pops.empty();
+		for (int pi : n->pull_pops) {
+			PopDev const& d = n->pops[pi].d;
+			for (int b = d.in_begin; b < d.in_end && ok; b++) {
+				ConnDev const& c = n->conns[n->by_dst[b]].d;
+				std::vector<int64_t> off((size_t)c.src_size + 1);
+				if (c.src_size > 0)
+					CUDA_TRY(cudaMemcpy(off.data(), c.off, sizeof(int64_t) * off.size(), cudaMemcpyDeviceToHost));
+				for (int64_t r = 0; r < c.src_size && ok; r++) ok = off[r + 1] - off[r] < kPushSortMaxRow;
+				ps_conn.push_back(b);
+				ps_pop.push_back(pi);
+				ps_begin.push_back(ps_begin.back() + n->pops[c.src].d.nwords);
+			}
+		}
+		n->ps_ok    = ok;
+		n->ps_nconn = (int)ps_conn.size();
+		n->ps_units = ok ? ps_begin.back() : 0;
+		if (ok) {
+			for (int pi : n->pull_pops) {  // the targets' entry slots
+				PopDev& d = n->pops[pi].d;
+				TRY(dalloc(n, &d.ps_key, (size_t)std::max<int64_t>(d.size, 1) * kPushSortSlots, false));
+				TRY(dalloc(n, &d.ps_w, (size_t)std::max<int64_t>(d.size, 1) * kPushSortSlots, false));
+			}
+			TRY(dalloc(n, &n->d_ps_conn, std::max<size_t>(ps_conn.size(), 1), false));
+			TRY(dalloc(n, &n->d_ps_pop, std::max<size_t>(ps_pop.size(), 1), false));
+			TRY(dalloc(n, &n->d_ps_begin, ps_begin.size(), false));
+			CUDA_TRY(cudaMemcpy(n->d_ps_conn, ps_conn.data(), sizeof(int) * ps_conn.size(), cudaMemcpyHostToDevice));
+			CUDA_TRY(cudaMemcpy(n->d_ps_pop, ps_pop.data(), sizeof(int) * ps_pop.size(), cudaMemcpyHostToDevice));
+			CUDA_TRY(cudaMemcpy(n->d_ps_begin, ps_begin.data(), sizeof(int64_t) * ps_begin.size(), cudaMemcpyHostToDevice));
+		}
+	}
 	TRY(dalloc(n, &n->d_pull_pops, std::max<size_t>(n->pull_pops.size(), 1), false));
 	TRY(dalloc(n, &n->d_pull_blk, blk.size(), false));
 	TRY(dalloc(n, &n->d_pull_sets, std::max<size_t>(n->pull_sets.size(), 1), false));
@@ -1645,10 +1680,15 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				pa.pull_blocks = n->pull_blocks;
 				pa.pops        = n->d_pops;
 				pa.conns       = n->d_conns_by_dst;
+				pa.ps_nconn    = n->ps_nconn;
+				pa.ps_conn     = n->d_ps_conn;
+				pa.ps_pop      = n->d_ps_pop;
+				pa.ps_begin    = n->d_ps_begin;
+				pa.ps_units    = n->ps_units;
 				TRY(ev_begin(n, 4, &slot));
 				CUDA_TRY(launch_pull(n->stream, pa, n->pull_sets, n->pull_ev));
 				TRY(ev_end(n, slot));
-				n->launches += 2;
+				n->launches += n->ps_units > 0 ? 3 : 2;
 			}
 			if (n->any_direct) TRY(deliver_direct(n));  // windows of one step: the end of step n->time
 			if (!fused) CUDA_TRY(cudaEventRecord(n->ev_free[q ^ 1], n->stream));  // the other parity's counts are clear

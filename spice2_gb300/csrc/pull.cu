@@ -336,6 +336,140 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 	pull_target(a, a.pull_pops[q], i, lane, bin_cnt[wid], bin_run[wid]);
 }
 
+// ---- push-and-sort gather ----
+// The scan above reads every synapse of a pulled population once per window.  At biological rates
+// a few percent of them carry a spike, so the default gather pushes only those: every synapse of a
+// source that spiked in the window adds, per step bit, one entry to its target's slots (64 per
+// target, compact, so the scattered writes stay close together) -- the weight and a 64-bit key
+// (bin k * F + f, the connection's rank among the target's inputs, the source, the synapse's
+// offset in its row) -- and each target then orders its entries by key (each entry's rank is the
+// number of smaller keys) into its region.  Key order within a bin is the scan's order (connect order, ascending
+// source, CSR order for duplicates), so both gathers give the same bins bit for bit.  A target with
+// more entries than its slots or its region takes the scan (pull_target) instead.
+
+// One warp per (pulled connection, source bitmap word).
+__global__ void __launch_bounds__(kPullThreads) k_ps_scatter(const __grid_constant__ PullArgs a) {
+	int const lane  = threadIdx.x & 31;
+	int64_t const u = (int64_t)blockIdx.x * kPullWarps + (threadIdx.x >> 5);
+	if (u >= a.ps_units) return;
+	int lo = 0, hi = a.ps_nconn - 1;  // the pulled connection of unit u
+	while (lo < hi) {
+		int const mid = (lo + hi + 1) >> 1;
+		if (a.ps_begin[mid] <= u) lo = mid;
+		else hi = mid - 1;
+	}
+	int const cb     = a.ps_conn[lo];
+	ConnDev const& C = a.conns[cb];
+	PopDev const& P  = a.pops[a.ps_pop[lo]];
+	int64_t const wd = u - a.ps_begin[lo];
+	uint32_t bits    = C.pull_orb[wd];
+	if (!bits) return;
+	int const F = P.pull_F;
+	int f       = 0;
+	while (f + 1 < F && P.pull_field[f] != C.field) f++;
+	uint64_t const crank = (uint64_t)(cb - P.in_begin) << 50;
+	uint32_t const kmask = a.K >= 32 ? 0xffffffffu : (1u << a.K) - 1u;
+	for (; bits; bits &= bits - 1) {
+		int64_t const src = 32 * wd + __ffs(bits) - 1;
+		uint32_t const m  = C.pull_wm[src] & kmask;
+		if (!m) continue;
+		int64_t const e0 = C.off[src], e1 = C.off[src + 1];
+		uint64_t const sk = crank | ((uint64_t)src << 19);
+		int const nk = __popc(m);  // entries per synapse: one per step bit, reserved together
+		constexpr int U = 4;       // synapses per lane with their reservations in flight together
+		for (int64_t eb = e0 + lane; eb < e1; eb += 32 * U) {
+			int32_t j[U];
+			float w[U];
+			int pos[U];
+#pragma unroll
+			for (int u = 0; u < U; u++)
+				if (eb + 32 * u < e1) {
+					j[u] = C.nb[eb + 32 * u];
+					w[u] = C.wts ? C.wts[eb + 32 * u] : C.weight;
+				}
+#pragma unroll
+			for (int u = 0; u < U; u++)
+				if (eb + 32 * u < e1) pos[u] = atomicAdd(P.pull_fill + j[u], nk);
+#pragma unroll
+			for (int u = 0; u < U; u++) {
+				int64_t const e = eb + 32 * u;
+				if (e >= e1) break;
+				int q = pos[u];
+				for (uint32_t mm = m; mm; mm &= mm - 1, q++) {
+					if (q >= kPushSortSlots) break;
+					int64_t const slot = (int64_t)j[u] * kPushSortSlots + q;
+					P.ps_key[slot]     = ((uint64_t)((__ffs(mm) - 1) * F + f) << 58) | sk | (uint64_t)(e - e0);
+					P.ps_w[slot]       = w[u];
+				}
+			}
+		}
+	}
+}
+
+// One warp per target: its pushed entries ordered by key into the bins (weights in G, starts in koff).
+__global__ void __launch_bounds__(kPullThreads) k_ps_sort(const __grid_constant__ PullArgs a) {
+	__shared__ int bin_cnt[kPullWarps][kMaxBins + 1];
+	__shared__ int bin_run[kPullWarps][kMaxBins + 1];
+	__shared__ int rank_bin[kPullWarps][kPushSortSlots];
+	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+	int const blk  = (int)blockIdx.x;
+	int q          = 0;
+	while (q + 1 < a.npull && blk >= a.pull_blk[q + 1]) q++;
+	int const pi    = a.pull_pops[q];
+	PopDev const& P = a.pops[pi];
+	int64_t const i = (int64_t)(blk - a.pull_blk[q]) * kPullWarps + wid;
+	if (i >= P.size) return;
+	int const nbins    = a.K * P.pull_F;
+	int64_t const base = P.pull_base[i];
+	int const cap      = (int)(P.pull_base[i + 1] - base);
+	int const n        = P.pull_fill[i];
+	__syncwarp();
+	if (lane == 0) P.pull_fill[i] = 0;  // for the next window
+	if (n > cap || n > kPushSortSlots) {  // more entries than the region or the slots: the scan
+		pull_target(a, pi, i, lane, bin_cnt[wid], bin_run[wid]);
+		return;
+	}
+	int64_t const sl = i * kPushSortSlots;
+	uint64_t const k0 = lane < n ? P.ps_key[sl + lane] : ~0ull;
+	float const w0    = lane < n ? P.ps_w[sl + lane] : 0.0f;
+	uint64_t const k1 = lane + 32 < n ? P.ps_key[sl + lane + 32] : ~0ull;
+	float const w1    = lane + 32 < n ? P.ps_w[sl + lane + 32] : 0.0f;
+	// rank of each entry = the entries with a smaller key (keys are distinct)
+	int r0 = 0, r1 = 0;
+	int const n0 = min(n, 32);
+	for (int q = 0; q < n0; q++) {
+		uint64_t const kq = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(k0 >> 32), q) << 32) |
+		                    __shfl_sync(0xffffffffu, (uint32_t)k0, q);
+		r0 += kq < k0;
+		r1 += kq < k1;
+	}
+	for (int q = 32; q < n; q++) {
+		uint64_t const kq = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(k1 >> 32), q - 32) << 32) |
+		                    __shfl_sync(0xffffffffu, (uint32_t)k1, q - 32);
+		r0 += kq < k0;
+		r1 += kq < k1;
+	}
+	float* G = P.pull_G + base;
+	int* bins = rank_bin[wid];  // the bin of each rank
+	if (lane < n) {
+		G[r0]     = w0;
+		bins[r0]  = (int)(k0 >> 58);
+	}
+	if (lane + 32 < n) {
+		G[r1]    = w1;
+		bins[r1] = (int)(k1 >> 58);
+	}
+	__syncwarp();
+	// bin starts: koff[b] = the entries in bins below b, each written once
+	int32_t* ko = P.pull_koff + i * (int64_t)(nbins + 1);
+	for (int r = lane; r < n; r += 32) {
+		int const prev = r == 0 ? -1 : bins[r - 1];
+		for (int b = prev + 1; b <= bins[r]; b++) ko[b] = r;
+	}
+	int const last = n == 0 ? -1 : bins[n - 1];
+	for (int b = last + 1 + lane; b <= nbins; b += 32) ko[b] = n;
+}
+
 // The inputs of the first pulled step (bins k = 0), applied now and removed from the bins: state
 // reads between steps see the reference's state after step(), which has delivered them already.
 __global__ void k_pull_apply_first(PopDev P) {
@@ -446,7 +580,13 @@ cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<Pull
 	if (a.k_emit > 0)
 		for (auto const& j : ev) nb += (j.nwords + kPullThreads - 1) / kPullThreads;
 	if (nb > 0) k_pull_masks<<<(unsigned)nb, kPullThreads, 0, stream>>>(a);
-	if (a.pull_blocks > 0) k_pull<<<(unsigned)a.pull_blocks, kPullThreads, 0, stream>>>(a);
+	if (a.pull_blocks <= 0) return cudaGetLastError();
+	if (a.ps_units > 0) {  // push-and-sort
+		k_ps_scatter<<<(unsigned)((a.ps_units + kPullWarps - 1) / kPullWarps), kPullThreads, 0, stream>>>(a);
+		k_ps_sort<<<(unsigned)a.pull_blocks, kPullThreads, 0, stream>>>(a);
+	} else {
+		k_pull<<<(unsigned)a.pull_blocks, kPullThreads, 0, stream>>>(a);
+	}
 	return cudaGetLastError();
 }
 
