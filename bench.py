@@ -448,10 +448,13 @@ def plastic_bench(N: int = 100000, steps: int = 5000, peak: float | None = None,
 
 
 def pull_bench(steps: int, warmup: int, peak: float):
-    """The pull path on the benchmark's network (SPICE_TUNE_PULL: every population gathers its inputs
-    from the CSC columns of its connections, in the reference's order).  One pull per window scans
-    every synapse once (its 4-byte source index; the synapses of a hit add their weight).  Timed like
-    the headline; the final states are compared with the push path's after the same steps."""
+    """The deterministic per-synapse-weight path on the benchmark's network (SPICE_TUNE_PULL: every
+    population gathers its inputs in the reference's order of additions -- connect order, ascending
+    source -- and adds them one IEEE addition at a time).  Per window the active synapses are pushed
+    into per-target slots with their order keys and ranked per target (the CSC scan of every synapse
+    remains the per-target fallback).  Timed like the headline; the final states are compared with
+    the push path's after the same steps.  Roofline: 8 B per delivered event (4-byte target, 4-byte
+    weight) against the gather's launches (k_pull_masks, k_ps_scatter, k_ps_sort)."""
     import numpy as np
     import torch
     import spice2_gb300 as sp
@@ -491,14 +494,15 @@ def pull_bench(steps: int, warmup: int, peak: float):
     same = same and net.events == push.events
     windows = n_pull
     t_pull = ms_pull / max(n_pull, 1) / 1e3
-    achieved = 4 * synapses / t_pull / 1e9 if t_pull > 0 else None
+    # the profiled run repeats the timed steps: its windows deliver the timed run's events
+    ev_window = events / max(windows, 1)
+    achieved = 8 * ev_window / t_pull / 1e9 if t_pull > 0 else None
     out = {"metric": "synaptic_events_per_s", "unit": "events/s", "value": events / (ms / 1e3),
-           # every window's pull scans every synapse once; the profiled run repeats the timed steps,
-           # so it has as many windows
-           "synapses_scanned_per_s": synapses * windows / (ms / 1e3),
+           # the inputs of every synapse are settled once per window (a full scan would read each)
+           "synapses_covered_per_s": synapses * windows / (ms / 1e3),
            "ms_per_step": ms / steps, "sim_seconds_per_wall_second": STEPS_PER_RUN * steps * DT / (ms / 1e3),
            "pull_launches": n_pull, "pull_mean_us": t_pull * 1e6, "neuron_mean_us": ms_win / max(n_win, 1) * 1e3,
-           "roofline": {"bound": "hbm", "kernel": "k_pull_masks + k_pull", "bytes_per_synapse": 4,
+           "roofline": {"bound": "hbm", "kernel": "k_pull_masks + k_ps_scatter + k_ps_sort", "bytes_per_event": 8,
                         "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": (achieved / peak) if achieved else None},
            "bit_identical_to_push": bool(same), "build_seconds": build_s,
