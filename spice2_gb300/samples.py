@@ -3,9 +3,12 @@
   python -m spice2_gb300.samples brunel [--N 20000] [--p 0.1] [--seed 1337] [--steps 300] [--json]
   python -m spice2_gb300.samples vogels [--N 4000] [--steps 1500] [--json]
   python -m spice2_gb300.samples external_input [--json]
+  python -m spice2_gb300.samples plastic_ei [--N 100000] [--seed 1] [--steps 5000] [--persistent 1]
 
 brunel follows samples/brunel.cpp:75-116 (weights scaled by 0.1/p so other p keep the mean input),
-vogels samples/vogels.cpp:62-86, external_input samples/external_input.cpp:39-51.  --json prints the
+vogels samples/vogels.cpp:62-86, external_input samples/external_input.cpp:39-51, plastic_ei the
+plastic E/I network (vogels.cpp's conductance LIF, p 0.02, delay 1 step, iSTDP on I->E, atomic
+mode; no counterpart sample in the reference).  --json prints the
 raster in the format of samples/matplot.cpp:96-134 (populations in the order the sample streams
 them, indices offset by the sizes of the populations before); without it a one-line summary with
 the synaptic events and the device time is printed.
@@ -94,6 +97,25 @@ def vogels(args):
         print(json.dumps({"sample": "vogels", "N": N, "steps": args.steps, "spikes": n, "events": net.events}))
 
 
+def plastic_ei(args):
+    import spice2_gb300 as sp
+    N = args.N
+    net = sp.snn(1e-4, 1e-4, [args.seed])
+    net.set_mode(sp.MODE_ATOMIC)
+    net.set_tuning(persistent=args.persistent)
+    E = net.add_population(sp.lif_cond(), N * 8 // 10)
+    I = net.add_population(sp.lif_cond(), N * 2 // 10)
+    net.connect(E, E, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
+    net.connect(E, I, sp.fixed_probability(0.02), 1e-4, sp.excitatory(0.03))
+    net.connect(I, E, sp.fixed_probability(0.02), 1e-4, sp.istdp(0.3, eta=1e-3, rho0=5.0, tau=0.02))
+    net.connect(I, I, sp.fixed_probability(0.02), 1e-4, sp.inhibitory(0.3))
+    t = time.perf_counter()
+    net.run(args.steps)
+    net.synchronize()
+    dt = time.perf_counter() - t
+    print(json.dumps({"sample": "plastic_ei", "N": N, "steps": args.steps, "events": net.events, "wall_s": dt}))
+
+
 def external_input(args):
     import spice2_gb300 as sp
     trains = ((4, 5, 8), (5,), (7, 8), (5, 7))
@@ -128,8 +150,13 @@ def main(argv=None) -> int:
     v.add_argument("--json", action="store_true")
     x = sub.add_parser("external_input")
     x.add_argument("--json", action="store_true")
+    e = sub.add_parser("plastic_ei")
+    e.add_argument("--N", type=int, default=100000)
+    e.add_argument("--seed", type=int, default=1)
+    e.add_argument("--steps", type=int, default=5000)
+    e.add_argument("--persistent", type=int, default=1, help="SPICE_TUNE_PERSISTENT (0: one launch per phase)")
     args = ap.parse_args(argv)
-    {"brunel": brunel, "vogels": vogels, "external_input": external_input}[args.sample](args)
+    {"brunel": brunel, "vogels": vogels, "external_input": external_input, "plastic_ei": plastic_ei}[args.sample](args)
     return 0
 
 
