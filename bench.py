@@ -346,16 +346,19 @@ def adjoint_bench(reps: int = 10):
     return out
 
 
-def plastic_bench(N: int = 100000, steps: int = 5000, peak: float | None = None, cpu_steps: int = 400):
+def plastic_bench(N: int = 100000, steps: int = 5000, peak: float | None = None, cpu_steps: int = 400,
+                  cpu_from: int = 1250):
     """The plastic E/I network: N conductance-LIF neurons (80 % E, 20 % I; tau_E 5 ms, tau_I 10 ms,
     the neuron of samples/vogels.cpp), fixed_probability(0.02), delay 1 step, E weights 0.03 and
     I weights 0.3 (0.3 nS and 3 nS over the 10 nS leak), I->E synapses iSTDP (tau 20 ms, rho0 5 Hz,
     eta 1e-3) with lazy event-driven updates, atomic mode, dt 1e-4, `steps` steps after 300 warm-up
-    steps.  Windows are one step long, so the net runs persistent steps (one cooperative launch
-    per 1024 steps, SPICE_TUNE_PERSISTENT); the launch-per-phase path is timed beside it.
-    Reported: synaptic events/s and simulated seconds per wall second (CUDA events on the net's
-    stream), firing rates, the I->E weight drift, the roofline of the persistent kernel and the
-    CPU restatement of the same network timed on the host cores from the first timed step."""
+    steps.  Windows are one step long, so the net runs persistent steps (cooperative launches split
+    at every 64th step for the periodic catch-up, SPICE_TUNE_PERSISTENT); the launch-per-phase path
+    is timed beside it.  Reported: synaptic events/s and simulated seconds per wall second (CUDA
+    events on the net's stream), firing rates, the I->E weight drift, the roofline of the persistent
+    kernel, and the CPU restatement of the same network on the host cores over steps [cpu_from,
+    cpu_from + cpu_steps) -- past the opening bursts, where it fires steadily -- with the GPU timed
+    on the same steps of a fresh network (`same_stretch`) for the ratio."""
     import numpy as np
     import torch
     import spice2_gb300 as sp
@@ -418,7 +421,7 @@ def plastic_bench(N: int = 100000, steps: int = 5000, peak: float | None = None,
            "events": ev, "gpu_launches": launches, "rate_E_hz": rE, "rate_I_hz": rI,
            "istdp_weight_mean_start": float(W0.mean()), "istdp_weight_mean_end": float(W.mean()),
            "istdp_weight_std_end": float(W.std()), "build_seconds": build_s, "mode": "atomic",
-           "path": "persistent steps (k_persist, one cooperative launch per 1024 steps)",
+           "path": "persistent steps (k_persist; launches split at every 64th step for k_plastic_update_all)",
            "launch_per_phase": {"ms": ms_phase, "us_per_step": 1000.0 * ms_phase / steps, "events": ev_phase,
                                 "gpu_launches": launches_phase,
                                 "sim_seconds_per_wall_second": steps * 1e-4 / (ms_phase / 1e3)},
@@ -427,21 +430,29 @@ def plastic_bench(N: int = 100000, steps: int = 5000, peak: float | None = None,
                         "bytes_model": "32 B/neuron state + 16 B/neuron input sums + 8 B/static event + "
                                        "28 B/plastic synapse every 64 steps (catch-up)"},
            "config": "plastic E/I: conductance LIF, p 0.02, delay 1 step, iSTDP on I->E"}
-    try:  # the CPU restatement of the same network from the first timed step (same seed)
+    # the GPU on the CPU sample's steps (fresh seed-1 network, persistent steps)
+    net3, *_ = build()
+    net3.run(cpu_from)
+    net3.synchronize()
+    ms3, ev3, _ = timed(net3, cpu_steps)
+    net3.close()
+    out["same_stretch"] = {"steps": [cpu_from, cpu_from + cpu_steps], "value": ev3 / (ms3 / 1e3),
+                           "us_per_step": 1000.0 * ms3 / cpu_steps, "events": ev3}
+    try:  # the CPU restatement of the same network over the same steps (same seed)
         from oracle import oracle as o
         if not os.path.exists(o.BENCH_PATH):
             o.build(with_reference=False)
         threads = max(1, min(8, (os.cpu_count() or 1)))
-        r = subprocess.run([o.BENCH_PATH, str(N), "0.02", str(cpu_steps), "1", str(threads), str(warm), "1", "1",
+        r = subprocess.run([o.BENCH_PATH, str(N), "0.02", str(cpu_steps), "1", str(threads), str(cpu_from), "1", "1",
                             "plastic_ei"], check=True, capture_output=True, text=True).stdout
         d = json.loads(r.strip().splitlines()[-1])
         out["cpu_baseline"] = {
             "value": d["events_per_s"], "unit": "events/s", "cores": threads, "kind": "port",
             "per_core": d["events_per_s_per_core"],
-            "sim_seconds_per_wall_second_per_core": cpu_steps * 1e-4 / (d["ms_per_step"] * 1e-3 * cpu_steps),
+            "sim_seconds_per_wall_second_per_core": 1e-4 / (d["ms_per_step"] * 1e-3),
             "ms_per_step": d["ms_per_step"],
-            "sample": f"steps {warm}..{warm + cpu_steps} of the seed-1 network per thread ({threads} replicas), "
-                      f"the first {cpu_steps} steps of the GPU timed stretch; build and warm-up untimed"}
+            "sample": f"steps {cpu_from}..{cpu_from + cpu_steps} of the seed-1 network per thread ({threads} "
+                      f"replicas; `same_stretch` is the GPU on those steps); build and warm-up untimed"}
     except Exception as e:  # the oracle could not be built or run here
         out["cpu_baseline"] = {"error": str(e)}
     return out
