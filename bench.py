@@ -642,11 +642,11 @@ def main():
     events_all = _sum_over_ranks(float(events), ws)
     value = events_all / (ms_max / 1e3)
 
-    # ---- end to end through the public C ABI with host buffers ----
-    import numpy as np
+    # ---- end to end through the public C ABI with host buffers (pinned: the GPU writes the raster
+    # into them while it steps) ----
     cap = 4_000_000
-    counts = np.zeros((STEPS_PER_RUN, 3), dtype=np.int64)
-    spikes = np.zeros(cap, dtype=np.int32)
+    counts = torch.zeros((STEPS_PER_RUN, 3), dtype=torch.int64, pin_memory=True)
+    spikes = torch.zeros(cap, dtype=torch.int32, pin_memory=True)
     import ctypes as C
     total = C.c_int64()
     L = sp.lib()
@@ -656,7 +656,7 @@ def main():
         e0 = net.events
         torch.cuda.synchronize()
         t = time.perf_counter()
-        rc = L.spice_run_record(net._h, STEPS_PER_RUN, counts.ctypes.data, spikes.ctypes.data, cap, C.byref(total))
+        rc = L.spice_run_record(net._h, STEPS_PER_RUN, counts.data_ptr(), spikes.data_ptr(), cap, C.byref(total))
         t = time.perf_counter() - t
         if rc != 0:
             raise RuntimeError(L.spice_last_error().decode())

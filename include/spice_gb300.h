@@ -222,7 +222,10 @@ int spice_step(spice_net* net);
 int spice_run(spice_net* net, int64_t steps);
 /* spice_run that also records every step's spikes (the raster that samples/matplot.cpp:96-134
  * prints): counts_out[steps][npop] and the ascending spike indices, step-major then population
- * order, into spikes_out (capacity entries).  *total_out = number of spikes recorded. */
+ * order, into spikes_out (capacity entries).  *total_out = number of spikes recorded.  When both
+ * buffers are pinned host memory (cudaHostAlloc, cudaHostRegister, a framework's pinned tensors)
+ * the GPU writes them directly while it steps; other host memory is filled from an internal
+ * pinned buffer when the call returns. */
 int spice_run_record(spice_net* net, int64_t steps, int64_t* counts_out, int32_t* spikes_out,
                      int64_t capacity, int64_t* total_out);
 

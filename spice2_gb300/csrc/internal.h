@@ -257,6 +257,11 @@ struct spice_net {
 	int64_t* h_rcounts   = nullptr;  // [rcounts_cap]
 	int64_t rcounts_cap  = 0;
 	int64_t* d_raster_base = nullptr;  // [2] raster position of the current / next window
+	// the raster's destination during one spice_run_record call: the staging buffers above, or the
+	// caller's own buffers when they are pinned host memory the GPU can write
+	int32_t* rec_out   = nullptr;
+	int64_t rec_cap    = 0;
+	int64_t* rec_counts = nullptr;
 	int32_t* d_tmp     = nullptr;  // spikes(age) extraction
 	int64_t* d_tmp_n   = nullptr;
 	// profiling

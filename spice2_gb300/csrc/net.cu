@@ -1383,9 +1383,9 @@ int run_persist(spice_net* n, int64_t chunk, const float* d_dt, const u128* d_ta
 		ra.npop        = np;
 		ra.pops        = n->d_pops;
 		ra.base        = n->d_raster_base;
-		ra.out         = n->h_raster;
-		ra.capacity    = n->raster_cap;
-		ra.step_counts = n->h_rcounts;
+		ra.out         = n->rec_out;
+		ra.capacity    = n->rec_cap;
+		ra.step_counts = n->rec_counts;
 	}
 	int const per_sm = n->persist_knob >= 2 ? n->persist_knob : kPersistBlocksPerSM;
 	int const grid   = std::min(n->persist_grid, n->sm_count * per_sm);
@@ -1702,9 +1702,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				ra.counts      = wa.counts;
 				ra.base        = n->d_raster_base;
 				ra.parity      = (int)(rec_windows++ & 1);
-				ra.out         = n->h_raster;
-				ra.capacity    = n->raster_cap;
-				ra.step_counts = n->h_rcounts;
+				ra.out         = n->rec_out;
+				ra.capacity    = n->rec_cap;
+				ra.step_counts = n->rec_counts;
 				ra.row0        = rows;
 				ra.pdl         = fused ? 1 : 0;
 				if (fused) {  // extracted by the next window's grid, or after the last window
@@ -1794,9 +1794,22 @@ extern "C" int spice_run_record(spice_net* n, int64_t steps, int64_t* counts_out
 	if (steps < 0 || capacity < 0) return fail(SPICE_EINVAL, "steps and capacity must be >= 0");
 	TRY(prepare(n));
 	int const np = (int)n->pops.size();
-	// mapped pinned raster buffers (grown on demand; the GPU writes them directly)
 	int64_t const need_counts = std::max<int64_t>(steps * np, 1);
-	if (n->raster_cap < std::max<int64_t>(capacity, 1) || n->rcounts_cap < need_counts) {
+	// caller buffers in pinned host memory: the GPU writes the raster into them directly
+	auto device_view = [](void* p) -> void* {
+		if (!p) return nullptr;
+		cudaPointerAttributes at{};
+		if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+			cudaGetLastError();  // pageable memory of an older runtime: clear the error
+			return nullptr;
+		}
+		return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+	};
+	int32_t* const direct_out  = static_cast<int32_t*>(device_view(spikes_out));
+	int64_t* const direct_cnt  = static_cast<int64_t*>(device_view(counts_out));
+	bool const direct          = direct_out && direct_cnt;
+	// otherwise mapped pinned staging buffers (grown on demand), copied to the caller's at the end
+	if (!direct && (n->raster_cap < std::max<int64_t>(capacity, 1) || n->rcounts_cap < need_counts)) {
 		CUDA_TRY(cudaStreamSynchronize(n->stream));
 		if (n->raster_cap < std::max<int64_t>(capacity, 1)) {
 			if (n->h_raster) cudaFreeHost(n->h_raster);
@@ -1815,6 +1828,9 @@ extern "C" int spice_run_record(spice_net* n, int64_t steps, int64_t* counts_out
 	}
 	if (!n->d_raster_base) TRY(dalloc(n, &n->d_raster_base, 2));
 	CUDA_TRY(cudaMemsetAsync(n->d_raster_base, 0, sizeof(int64_t) * 2, n->stream));
+	n->rec_out    = direct ? direct_out : n->h_raster;
+	n->rec_cap    = direct ? capacity : n->raster_cap;
+	n->rec_counts = direct ? direct_cnt : n->h_rcounts;
 	int64_t rows = 0;
 	TRY(run_steps(n, steps, true, &rows));
 	int64_t base[2] = {0, 0};
@@ -1826,6 +1842,7 @@ extern "C" int spice_run_record(spice_net* n, int64_t steps, int64_t* counts_out
 	if (total > capacity)
 		return fail(SPICE_EOVERFLOW, "raster needs " + std::to_string(total) + " entries, capacity is " +
 		                                 std::to_string(capacity));
+	if (direct) return SPICE_OK;  // written in place
 	if (counts_out && steps * np > 0) std::memcpy(counts_out, n->h_rcounts, sizeof(int64_t) * steps * np);
 	if (spikes_out && total > 0) parallel_copy(spikes_out, n->h_raster, sizeof(int32_t) * (size_t)total);
 	return SPICE_OK;

@@ -210,6 +210,39 @@ def test_large_recorded_raster_equals_piecewise_recording(engine):
     assert n * 4 > (8 << 20)  # large enough for the threaded copy
 
 
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_pinned_caller_buffers_written_in_place(engine, persistent):
+    """spice_run_record into pinned host buffers (written by the GPU while it steps) and into
+    pageable ones (filled from the staging buffer): equal counts, spikes and totals; a pinned buffer
+    that is too small reports the same overflow and total as a pageable one."""
+    import ctypes as C
+    import torch
+    sp = engine
+    L = sp.lib()
+    delay = 1e-4 if persistent else 15e-4
+    a, _ = sp.brunel(20000, 0.02, 5, delay=delay)
+    b, _ = sp.brunel(20000, 0.02, 5, delay=delay)
+    a.set_tuning(persistent=persistent)
+    b.set_tuning(persistent=persistent)
+    steps, cap = 300, 400000
+    pc = torch.full((steps, 3), -1, dtype=torch.int64, pin_memory=True)
+    ps = torch.full((cap,), -1, dtype=torch.int32, pin_memory=True)
+    hc = np.full((steps, 3), -1, dtype=np.int64)
+    hs = np.full(cap, -1, dtype=np.int32)
+    ta, tb = C.c_int64(), C.c_int64()
+    for _ in range(2):  # a second call starts from the first's end
+        assert L.spice_run_record(a._h, steps, pc.data_ptr(), ps.data_ptr(), cap, C.byref(ta)) == 0
+        assert L.spice_run_record(b._h, steps, hc.ctypes.data, hs.ctypes.data, cap, C.byref(tb)) == 0
+        assert ta.value == tb.value > 0
+        assert np.array_equal(pc.numpy(), hc)
+        assert np.array_equal(ps.numpy()[:ta.value], hs[:tb.value])
+        assert int(hc.sum()) == ta.value
+    small = ta.value // 2
+    ra = L.spice_run_record(a._h, steps, pc.data_ptr(), ps.data_ptr(), small, C.byref(ta))
+    rb = L.spice_run_record(b._h, steps, hc.ctypes.data, hs.ctypes.data, small, C.byref(tb))
+    assert ra == rb == sp.EOVERFLOW and ta.value == tb.value > small
+
+
 # ---- the reference's own known-answer tests, restated ----------------------------------------------
 def test_external_input_sample(engine):
     """samples/external_input.cpp: a per-population update replays a cyclic spike train."""
