@@ -28,6 +28,12 @@ Printed JSON (one line, rank 0):
                and whether both gave bit-identical final states
   adjoint      the differentiable recurrent LIF layer (batch 64, 700 -> 1024, 200 steps): forward and
                adjoint-backward times, their ratio, and plain PyTorch autograd on dense weights
+  plastic      the plastic E/I network (N=1e5 conductance LIF, iSTDP on I->E, delay 1 step, 5000
+               steps): persistent and launch-per-phase times, roofline, CPU restatement beside it
+  seeds        the headline network at seeds 1..10, each timed over the headline's stretch, with
+               the CPU restatement of the ten networks beside it
+  readme_sample the reference's published sample (Brunel N=2e4, p=0.1, seed 1337, 300 steps) from
+               construction, with the CPU restatement on one thread beside it
 
 --impl reference runs the reference's CPU implementation of the path on the host cores (the
 reference binary when it was built on this host, else its CPU restatement) and prints the same
@@ -523,6 +529,109 @@ def pull_bench(steps: int, warmup: int, peak: float):
     return out
 
 
+def seed_sweep(tuned: dict, warmup: int, steps: int = 2, seeds=range(1, 11), cpu_steps: int = 100):
+    """Large Brunel at seeds 1..10 (the benchmark's seed list): each network built fresh, warm-up
+    to the headline's first timed step (warmup x 2000 steps), then `steps` runs of 2000 steps timed
+    with CUDA events on its stream, in the headline's launch shape.  Beside it the CPU restatement
+    of the same ten networks (one thread per seed) over `cpu_steps` steps from the same step."""
+    import torch
+    import spice2_gb300 as sp
+    from spice2_gb300.autotune import apply_shape
+    per_seed = []
+    for seed in seeds:
+        net, _ = sp.brunel(N_NEURONS, P_CONN, seed, mode=sp.MODE_DETERMINISTIC)
+        apply_shape(net, tuned)
+        for _ in range(warmup):
+            net.run(STEPS_PER_RUN)
+        net.synchronize()
+        stream = torch.cuda.ExternalStream(net.stream_handle())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0 = net.events
+        torch.cuda.synchronize()
+        a.record(stream)
+        for _ in range(steps):
+            net.run(STEPS_PER_RUN)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        per_seed.append({"seed": seed, "value": (net.events - e0) / (ms / 1e3), "ms_per_step": ms / steps,
+                         "events": net.events - e0})
+        net.close()
+        del net
+    vals = [d["value"] for d in per_seed]
+    out = {"metric": "synaptic_events_per_s", "unit": "events/s", "seeds": [d["seed"] for d in per_seed],
+           "values": vals, "mean": statistics.fmean(vals), "min": min(vals), "max": max(vals),
+           "first_timed_step": warmup * STEPS_PER_RUN, "sim_steps_per_seed": steps * STEPS_PER_RUN,
+           "per_seed": per_seed}
+    try:
+        start = warmup * STEPS_PER_RUN
+        d = _oracle_bench([N_NEURONS, P_CONN, cpu_steps, min(seeds), len(seeds), start, 1, 0])
+        out["cpu_baseline"] = {"value": d["events_per_s"], "unit": "events/s", "cores": d["threads"], "kind": "port",
+                               "per_core": d["events_per_s_per_core"],
+                               "sample": f"{cpu_steps} steps of each seed's network from step {start}, one thread "
+                                         f"per seed; build and warm-up untimed"}
+    except Exception as e:  # reported, never a reason to lose the section
+        out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    return out
+
+
+def readme_sample(repeats: int = 10):
+    """The reference's own sample as published (samples/brunel.cpp with its README parameters):
+    Brunel N=2e4, p=0.1, weights 2/N and -10/N, delay 15 steps, seed 1337, 300 steps.  A fresh
+    network per repetition: construction timed on the host (synchronised), the 300 steps with CUDA
+    events on the net's stream after the first call's setup; the best and median repetitions are
+    reported.  Beside it the CPU restatement of the same sample on one thread (the reference is
+    single-threaded), construction and steps timed apart."""
+    import torch
+    import spice2_gb300 as sp
+    N, p, seed, steps = 20000, 0.1, 1337, 300
+    runs = []
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        net, _ = sp.brunel(N, p, seed, mode=sp.MODE_DETERMINISTIC)
+        net.run(0)  # construction: adjacency generation and the first call's setup
+        net.synchronize()
+        build = time.perf_counter() - t0
+        stream = torch.cuda.ExternalStream(net.stream_handle())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        net.run(steps)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(b)
+        runs.append({"build_s": build, "ms": ms, "events": net.events})
+        net.close()
+        del net
+    ms = sorted(r["ms"] for r in runs)
+    events = runs[0]["events"]
+    assert all(r["events"] == events for r in runs)
+    out = {"metric": "synaptic_events_per_s", "unit": "events/s",
+           "config": "Brunel N=2e4 (P 1e4, E 8e3, I 2e3), p=0.1, w 2/N and -10/N, delay 15 steps, seed 1337, "
+                     "300 steps from construction",
+           "events": events, "value": events / (ms[0] / 1e3), "median_value": events / (statistics.median(ms) / 1e3),
+           "ms": ms[0], "sim_seconds_per_wall_second": steps * DT / (ms[0] / 1e3),
+           "build_seconds": statistics.median(r["build_s"] for r in runs), "repeats": repeats}
+    try:
+        d = _oracle_bench([N, p, steps, seed, 1, 0, 1, 0])
+        out["cpu_baseline"] = {"value": d["events_per_s"], "unit": "events/s", "cores": 1, "kind": "port",
+                               "ms": d["step_seconds"] * 1e3, "build_seconds": d["build_seconds"],
+                               "sample": "the 300 steps of the sample on one thread; construction timed apart"}
+        out["speedup_vs_cpu"] = out["value"] / d["events_per_s"]
+    except Exception as e:
+        out["cpu_baseline"] = {"value": None, "sample": f"failed: {e}"}
+    return out
+
+
+def _oracle_bench(argv: list) -> dict:
+    from oracle import oracle as o
+    if not os.path.exists(o.BENCH_PATH):
+        o.build(with_reference=False)
+    out = subprocess.run([o.BENCH_PATH] + [repr(a) if isinstance(a, float) else str(a) for a in argv],
+                         check=True, capture_output=True, text=True).stdout
+    return json.loads(out.strip().splitlines()[-1])
+
+
 def reference_arm(args):
     """The reference's CPU implementation of the path (its C restatement: the reference binary is
     built for x86-64 with -march=haswell and its sources are not on the GPU host) on the host cores,
@@ -733,6 +842,16 @@ def main():
             plastic = plastic_bench(peak=peak)
         except Exception as e:
             plastic = {"error": str(e)}
+    seeds = readme = None
+    if not args.headline_only:
+        try:
+            seeds = seed_sweep(tuned, args.warmup)
+        except Exception as e:
+            seeds = {"error": str(e)}
+        try:
+            readme = readme_sample()
+        except Exception as e:
+            readme = {"error": str(e)}
 
     cpu = None
     if not args.no_cpu_baseline and ws == 1:
@@ -778,6 +897,8 @@ def main():
         "batched": batched,
         "adjoint": adjoint,
         "plastic": plastic,
+        "seeds": seeds,
+        "readme_sample": readme,
         "clocks": clk.summary(),
     }
     print(json.dumps(line))

@@ -1832,7 +1832,14 @@ extern "C" int spice_run_record(spice_net* n, int64_t steps, int64_t* counts_out
 	n->rec_cap    = direct ? capacity : n->raster_cap;
 	n->rec_counts = direct ? direct_cnt : n->h_rcounts;
 	int64_t rows = 0;
-	TRY(run_steps(n, steps, true, &rows));
+	int const rc = run_steps(n, steps, true, &rows);
+	n->rec_out    = nullptr;
+	n->rec_counts = nullptr;
+	if (rc != SPICE_OK) {
+		// kernels launched before the failure may still write the caller's buffers: let them finish
+		if (direct) cudaStreamSynchronize(n->stream);
+		return rc;
+	}
 	int64_t base[2] = {0, 0};
 	CUDA_TRY(cudaMemcpyAsync(base, n->d_raster_base, sizeof(base), cudaMemcpyDeviceToHost, n->stream));
 	CUDA_TRY(cudaStreamSynchronize(n->stream));
