@@ -141,7 +141,11 @@ int spice_set_mode(spice_net* net, int mode);
 
 /* Launch-shape knobs of the delivery kernel (no counterpart in the reference; may be changed at
  * any time between steps): shared memory per target tile in bytes, and threads per delivery CTA.
- * Results do not depend on them; spice2_gb300.autotune picks them per network. */
+ * Results do not depend on them.  Those the caller leaves unset are picked from the network's
+ * sizes when it is prepared (its first step): mapping 17 (1 for tiles above 176 KiB), LIF window
+ * 7, the largest tile of at most 100 KiB that gives the most delivery CTAs per window (input slots
+ * x target tiles) within one wave of one CTA per SM, and 768 / 512 / 256 threads for tiles of at
+ * least 64 KiB / 24 KiB / less.  spice2_gb300.autotune measures them on a network instead. */
 enum {
 	SPICE_TUNE_TILE_BYTES      = 0, /* shared memory per target tile                          */
 	SPICE_TUNE_DELIVER_THREADS = 1, /* threads per delivery CTA                               */

@@ -277,12 +277,16 @@ struct spice_net {
 	int parity = 0;                  // which half of d_counts the next window writes
 	spice_gb300::ConnDev* d_conns_by_dst = nullptr;  // connections grouped by target population
 	std::vector<int> by_dst;         // connection ids in that order
-	int tile_bytes = 24 * 1024;      // shared memory per delivery tile (tunable)
-	int deliver_threads = 256;       // threads per delivery CTA (tunable)
-	int deliver_parts = 1;           // CTAs per (slot, tile) (tunable)
-	int deliver_algo = 1;            // delivery work mapping (tunable)
-	int overlap_sources = 1;         // source kernels on their own stream (tunable)
-	int neuron_variant  = 0;         // LIF window variant of the neuron update (tunable)
+	// launch shape (tunable); the values below stand until the network is prepared, which picks
+	// the tile, threads, mapping and LIF variant for the network's sizes (default_shape in net.cu)
+	// unless the caller set them
+	int tile_bytes = 24 * 1024;      // shared memory per delivery tile
+	int deliver_threads = 256;       // threads per delivery CTA
+	int deliver_parts = 1;           // CTAs per (slot, tile)
+	int deliver_algo = 1;            // delivery work mapping
+	int overlap_sources = 1;         // source kernels on their own stream
+	int neuron_variant  = 0;         // LIF window variant of the neuron update
+	bool tile_set = false, threads_set = false, algo_set = false, variant_set = false;  // set by the caller
 	int launch_mode     = 1;         // 1: neurons and sources in one grid, programmatic dependent launches
 	int src_steps       = 1;         // steps per Poisson CTA (0: the fewest that fit the grid in one wave)
 	// persistent steps (step.cu k_persist): windows of one step, one cooperative launch per chunk

@@ -93,6 +93,9 @@ cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<Pull
 constexpr int64_t kPushSortMaxRow = 1ll << 19;
 // entries one target can take per window in the push-and-sort gather (more: the scan)
 constexpr int kPushSortSlots = 64;
+// Largest tile of the compact-target delivery mappings (15 .. 21): their staged sub-rows take
+// ~41 KB of static shared memory beside the tile, within the 227 KiB of one CTA.
+constexpr int kCompactMaxTileBytes = 176 * 1024;
 int pull_blocks_for(int64_t size);  // k_pull CTAs of a population of `size` neurons
 // Applies the bins of the first pulled step to the state and empties them (state reads).
 cudaError_t launch_pull_apply_first(cudaStream_t stream, PopDev const& P);

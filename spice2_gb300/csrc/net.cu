@@ -609,6 +609,61 @@ int ensure_csc(spice_net* n, int ci) {
 	return SPICE_OK;
 }
 
+// The delivery mapping when the caller set none: the compact-target rows (17), unless the tile
+// leaves too little shared memory for its staged sub-rows (then one thread per spike, 1).
+void default_algo(spice_net* n) {
+	if (!n->algo_set) n->deliver_algo = n->tile_bytes <= kCompactMaxTileBytes ? 17 : 1;
+}
+
+// The launch shape of a network whose caller set none (the values an autotuner run on large and
+// small Brunel networks converges to): the compact-target row mapping with two sub-rows per lane
+// group (17), the lean LIF window (variant 7), and the tile size that gives the most delivery CTAs
+// per window -- input slots times target tiles -- within one wave of one CTA per SM, the largest
+// such tile (fewest sub-rows per spike), at most 100 KiB; threads by tile size.
+void default_shape(spice_net* n) {
+	if (!n->variant_set) n->neuron_variant = 7;
+	default_algo(n);
+	if (n->tile_set && n->threads_set) return;
+	int dmin = (int)n->max_delay, dmax = 1;
+	for (auto const& c : n->conns) {
+		dmin = std::min(dmin, c.d.delay);
+		dmax = std::max(dmax, c.d.delay);
+	}
+	int64_t const nslots = n->conns.empty() ? 0 : (int64_t)n->K + dmax - dmin;
+	std::vector<std::pair<int64_t, int>> targets;  // (size, words per neuron) of tiled populations
+	for (int pi = 0; pi < (int)n->pops.size(); pi++) {
+		PopDev const& d = n->pops[pi].d;
+		bool in = false;
+		for (auto const& c : n->conns) in |= c.d.dst == pi;
+		if (in && d.size > 0 && !d.pull && !d.direct)
+			targets.push_back({d.size, std::max(n->mode == SPICE_MODE_DETERMINISTIC ? d.W : d.F, 1)});
+	}
+	int constexpr kMaxTile = 100 * 1024, kMinTile = 4 * 1024;
+	int tb = kMaxTile;
+	if (!n->tile_set && nslots > 0 && !targets.empty()) {
+		auto ctas = [&](int bytes) {
+			int64_t m = 0;
+			for (auto const& [size, width] : targets) {
+				int64_t const tile = std::max(32, bytes / (4 * width) / 32 * 32);
+				m += (size + tile - 1) / tile;
+			}
+			return nslots * m;
+		};
+		int64_t best = -1;
+		for (int bytes = kMaxTile; bytes >= kMinTile; bytes -= 128) {  // CTAs grow as tiles shrink
+			int64_t const m = ctas(bytes);
+			if (m > n->sm_count) break;
+			if (m > best) {
+				best = m;
+				tb   = bytes;
+			}
+		}
+		n->tile_bytes = tb;
+	}
+	if (!n->threads_set) n->deliver_threads = n->tile_bytes >= 64 * 1024 ? 768 : n->tile_bytes >= 24 * 1024 ? 512 : 256;
+	default_algo(n);
+}
+
 // Tile sizes of the delivery kernel, the by-target connection order and the per-row positions
 // where each tile starts.  Called at preparation and again when the launch shape is re-tuned.
 int setup_tiles(spice_net* n, bool first) {
@@ -1075,6 +1130,8 @@ int prepare(spice_net* n) {
 		else
 			TRY(dalloc(n, &d.acc, (size_t)D * d.size * d.F));
 	}
+	CUDA_TRY(cudaDeviceGetAttribute(&n->sm_count, cudaDevAttrMultiProcessorCount, n->device));
+	default_shape(n);
 	TRY(setup_tiles(n, true));
 	for (auto& c : n->conns) {
 		ConnDev& d      = c.d;
@@ -2077,8 +2134,10 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 	switch (knob) {
 		case SPICE_TUNE_TILE_BYTES:
 			if (value < 1024 || value > 220 * 1024) return fail(SPICE_EINVAL, "tile bytes must be in [1 KiB, 220 KiB]");
+			n->tile_set = true;
 			if (n->tile_bytes == (int)value) return SPICE_OK;
 			n->tile_bytes = (int)value;
+			default_algo(n);  // a tile too large for the default mapping's staging
 			if (n->prepared) {  // re-tile: the input ring layout does not depend on the tile size
 				TRY(setup_tiles(n, false));
 				std::vector<PopDev> hp;
@@ -2093,11 +2152,13 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 		case SPICE_TUNE_DELIVER_THREADS:
 			if (value < 32 || value > 1024 || value % 32) return fail(SPICE_EINVAL, "threads must be a multiple of 32 in [32, 1024]");
 			n->deliver_threads = (int)value;
+			n->threads_set     = true;
 			return SPICE_OK;
 		case SPICE_TUNE_DELIVER_ALGO:
 			if (value < 0 || value >= kDeliverAlgos)
 				return fail(SPICE_EINVAL, "delivery algorithm must be 0 .. " + std::to_string(kDeliverAlgos - 1));
 			n->deliver_algo = (int)value;
+			n->algo_set     = true;
 			if (n->prepared && compact_algo((int)value)) {  // build the compact targets for the current tiles
 				TRY(setup_tiles(n, false));
 				std::vector<PopDev> hp;
@@ -2138,6 +2199,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 		case SPICE_TUNE_NEURON_VARIANT:
 			if (value < 0 || value > 8) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 8");
 			n->neuron_variant = (int)value;
+			n->variant_set    = true;
 			return SPICE_OK;
 		case SPICE_TUNE_OVERLAP_SOURCES:
 			if (value < 0 || value > 1) return fail(SPICE_EINVAL, "overlap must be 0 or 1");

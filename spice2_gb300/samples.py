@@ -50,7 +50,8 @@ def brunel(args):
     if args.tuning:
         tb, th, parts, algo = (int(x) for x in args.tuning.split(","))
         net.set_tuning(tile_bytes=tb, deliver_threads=th, deliver_parts=parts, deliver_algo=algo)
-    net.set_tuning(neuron_variant=args.neuron_variant)
+    if args.neuron_variant is not None:
+        net.set_tuning(neuron_variant=args.neuron_variant)
     if args.launch_mode is not None:  # 0: neuron update and sources as separate launches, one stream
         net.set_tuning(launch_mode=args.launch_mode, overlap_sources=bool(args.launch_mode))
     if args.pull:
@@ -139,7 +140,8 @@ def main(argv=None) -> int:
                    help="run window by window and print the synaptic events of each (profiling aid)")
     b.add_argument("--tuning", default="", metavar="TILE_BYTES,THREADS,PARTS,ALGO",
                    help="delivery launch shape (results do not depend on it)")
-    b.add_argument("--neuron-variant", type=int, default=0, help="LIF window variant (results do not depend on it)")
+    b.add_argument("--neuron-variant", type=int, default=None,
+                   help="LIF window variant (results do not depend on it; default: the one the network's size picks)")
     b.add_argument("--pull", action="store_true", help="deliver every population by the pull path over the CSC")
     b.add_argument("--launch-mode", type=int, default=None,
                    help="1: one grid per window for neurons and sources (default); 0: separate launches")
