@@ -406,11 +406,14 @@ __global__ void __launch_bounds__(kPullThreads) k_ps_scatter(const __grid_consta
 	}
 }
 
-// One warp per target: its pushed entries ordered by key into the bins (weights in G, starts in koff).
+// One warp per target: its pushed entries ordered by key into the bins (weights in G, starts in
+// koff).  A counting sort by bin (the key's top bits) gives the bin starts; each entry's place in
+// its bin is the number of the bin's entries with a smaller key (keys are distinct), found among
+// the bin's few entries parked, grouped by bin, in shared memory.
 __global__ void __launch_bounds__(kPullThreads) k_ps_sort(const __grid_constant__ PullArgs a) {
 	__shared__ int bin_cnt[kPullWarps][kMaxBins + 1];
 	__shared__ int bin_run[kPullWarps][kMaxBins + 1];
-	__shared__ int rank_bin[kPullWarps][kPushSortSlots];
+	__shared__ uint64_t key_s[kPullWarps][kPushSortSlots];
 	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	int const blk  = (int)blockIdx.x;
 	int q          = 0;
@@ -429,45 +432,54 @@ __global__ void __launch_bounds__(kPullThreads) k_ps_sort(const __grid_constant_
 		pull_target(a, pi, i, lane, bin_cnt[wid], bin_run[wid]);
 		return;
 	}
-	int64_t const sl = i * kPushSortSlots;
-	uint64_t const k0 = lane < n ? P.ps_key[sl + lane] : ~0ull;
-	float const w0    = lane < n ? P.ps_w[sl + lane] : 0.0f;
-	uint64_t const k1 = lane + 32 < n ? P.ps_key[sl + lane + 32] : ~0ull;
-	float const w1    = lane + 32 < n ? P.ps_w[sl + lane + 32] : 0.0f;
-	// rank of each entry = the entries with a smaller key (keys are distinct)
-	int r0 = 0, r1 = 0;
-	int const n0 = min(n, 32);
-	for (int q = 0; q < n0; q++) {
-		uint64_t const kq = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(k0 >> 32), q) << 32) |
-		                    __shfl_sync(0xffffffffu, (uint32_t)k0, q);
-		r0 += kq < k0;
-		r1 += kq < k1;
-	}
-	for (int q = 32; q < n; q++) {
-		uint64_t const kq = ((uint64_t)__shfl_sync(0xffffffffu, (uint32_t)(k1 >> 32), q - 32) << 32) |
-		                    __shfl_sync(0xffffffffu, (uint32_t)k1, q - 32);
-		r0 += kq < k0;
-		r1 += kq < k1;
-	}
-	float* G = P.pull_G + base;
-	int* bins = rank_bin[wid];  // the bin of each rank
-	if (lane < n) {
-		G[r0]     = w0;
-		bins[r0]  = (int)(k0 >> 58);
-	}
-	if (lane + 32 < n) {
-		G[r1]    = w1;
-		bins[r1] = (int)(k1 >> 58);
-	}
+	int64_t const sl  = i * kPushSortSlots;
+	bool const v0     = lane < n, v1 = lane + 32 < n;
+	uint64_t const k0 = v0 ? P.ps_key[sl + lane] : 0ull;
+	float const w0    = v0 ? P.ps_w[sl + lane] : 0.0f;
+	uint64_t const k1 = v1 ? P.ps_key[sl + lane + 32] : 0ull;
+	float const w1    = v1 ? P.ps_w[sl + lane + 32] : 0.0f;
+	int const b0 = (int)(k0 >> 58), b1 = (int)(k1 >> 58);
+	int* const cnt = bin_cnt[wid];  // entries per bin
+	int* const st  = bin_run[wid];  // bin starts; st[nbins] = n
+	for (int b = lane; b <= nbins; b += 32) cnt[b] = 0;
 	__syncwarp();
-	// bin starts: koff[b] = the entries in bins below b, each written once
-	int32_t* ko = P.pull_koff + i * (int64_t)(nbins + 1);
-	for (int r = lane; r < n; r += 32) {
-		int const prev = r == 0 ? -1 : bins[r - 1];
-		for (int b = prev + 1; b <= bins[r]; b++) ko[b] = r;
+	int p0 = 0, p1 = 0;  // arrival places within the bin (any order: only to park the keys)
+	if (v0) p0 = atomicAdd(&cnt[b0], 1);
+	if (v1) p1 = atomicAdd(&cnt[b1], 1);
+	__syncwarp();
+	// exclusive scan over the bins (nbins <= 48): lane l holds bins 2l and 2l + 1
+	int const c0 = 2 * lane < nbins ? cnt[2 * lane] : 0;
+	int const c1 = 2 * lane + 1 < nbins ? cnt[2 * lane + 1] : 0;
+	int incl     = c0 + c1;
+#pragma unroll
+	for (int d = 1; d < 32; d <<= 1) {
+		int const o = __shfl_up_sync(0xffffffffu, incl, d);
+		if (lane >= d) incl += o;
 	}
-	int const last = n == 0 ? -1 : bins[n - 1];
-	for (int b = last + 1 + lane; b <= nbins; b += 32) ko[b] = n;
+	int const excl = incl - c0 - c1;
+	if (2 * lane <= nbins) st[2 * lane] = excl;
+	if (2 * lane + 1 <= nbins) st[2 * lane + 1] = excl + c0;
+	__syncwarp();
+	uint64_t* const ks = key_s[wid];
+	if (v0) ks[st[b0] + p0] = k0;
+	if (v1) ks[st[b1] + p1] = k1;
+	__syncwarp();
+	float* G = P.pull_G + base;
+	if (v0) {
+		int const s = st[b0], e = s + cnt[b0];
+		int r = s;
+		for (int j = s; j < e; j++) r += ks[j] < k0;
+		G[r] = w0;
+	}
+	if (v1) {
+		int const s = st[b1], e = s + cnt[b1];
+		int r = s;
+		for (int j = s; j < e; j++) r += ks[j] < k1;
+		G[r] = w1;
+	}
+	// bin starts: koff[b] = the entries in bins below b
+	int32_t* ko = P.pull_koff + i * (int64_t)(nbins + 1);
+	for (int b = lane; b <= nbins; b += 32) ko[b] = st[b];
 }
 
 // The inputs of the first pulled step (bins k = 0), applied now and removed from the bins: state
