@@ -96,8 +96,8 @@ struct PopDev {
 	int32_t* pull_koff;        // [size][nbins + 1] bin starts in the region; [i][0] = -1: not grouped,
 	                           // [i][1] = number of active synapses (the neuron walks pull_A)
 	int32_t* pull_fill;        // [size] entries pushed for the target this window (push-and-sort gather)
-	uint64_t* ps_key;          // [size][kPushSortSlots] their sort keys (push-and-sort gather)
-	float* ps_w;               // [size][kPushSortSlots] their weights
+	uint4* ps_slot;            // [size][kPushSortSlots] their sort keys (x: low, y: high word) and
+	                           // weights (z: bits), one 16-byte store each (push-and-sort gather)
 	int direct;                // USER_DELIVER target: inputs applied into the neuron structs at the end of each step
 };
 

@@ -816,8 +816,7 @@ int setup_pull(spice_net* n) {
 		if (ok) {
 			for (int pi : n->pull_pops) {  // the targets' entry slots
 				PopDev& d = n->pops[pi].d;
-				TRY(dalloc(n, &d.ps_key, (size_t)std::max<int64_t>(d.size, 1) * kPushSortSlots, false));
-				TRY(dalloc(n, &d.ps_w, (size_t)std::max<int64_t>(d.size, 1) * kPushSortSlots, false));
+				TRY(dalloc(n, &d.ps_slot, (size_t)std::max<int64_t>(d.size, 1) * kPushSortSlots, false));
 			}
 			TRY(dalloc(n, &n->d_ps_conn, std::max<size_t>(ps_conn.size(), 1), false));
 			TRY(dalloc(n, &n->d_ps_pop, std::max<size_t>(ps_pop.size(), 1), false));

@@ -347,8 +347,9 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 // source, CSR order for duplicates), so both gathers give the same bins bit for bit.  A target with
 // more entries than its slots or its region takes the scan (pull_target) instead.
 
-// One warp per (pulled connection, source bitmap word).
-__global__ void __launch_bounds__(kPullThreads) k_ps_scatter(const __grid_constant__ PullArgs a) {
+// One warp per (pulled connection, source bitmap word).  Latency-bound (the slot reservations are
+// atomics with a result): at most 40 registers, so that six CTAs share an SM.
+__global__ void __launch_bounds__(kPullThreads, 6) k_ps_scatter(const __grid_constant__ PullArgs a) {
 	int const lane  = threadIdx.x & 31;
 	int64_t const u = (int64_t)blockIdx.x * kPullWarps + (threadIdx.x >> 5);
 	if (u >= a.ps_units) return;
@@ -397,9 +398,9 @@ __global__ void __launch_bounds__(kPullThreads) k_ps_scatter(const __grid_consta
 				int q = pos[u];
 				for (uint32_t mm = m; mm; mm &= mm - 1, q++) {
 					if (q >= kPushSortSlots) break;
-					int64_t const slot = (int64_t)j[u] * kPushSortSlots + q;
-					P.ps_key[slot]     = ((uint64_t)((__ffs(mm) - 1) * F + f) << 58) | sk | (uint64_t)(e - e0);
-					P.ps_w[slot]       = w[u];
+					uint64_t const key = ((uint64_t)((__ffs(mm) - 1) * F + f) << 58) | sk | (uint64_t)(e - e0);
+					P.ps_slot[(int64_t)j[u] * kPushSortSlots + q] =
+					    make_uint4((uint32_t)key, (uint32_t)(key >> 32), __float_as_uint(w[u]), 0u);
 				}
 			}
 		}
@@ -434,10 +435,10 @@ __global__ void __launch_bounds__(kPullThreads) k_ps_sort(const __grid_constant_
 	}
 	int64_t const sl  = i * kPushSortSlots;
 	bool const v0     = lane < n, v1 = lane + 32 < n;
-	uint64_t const k0 = v0 ? P.ps_key[sl + lane] : 0ull;
-	float const w0    = v0 ? P.ps_w[sl + lane] : 0.0f;
-	uint64_t const k1 = v1 ? P.ps_key[sl + lane + 32] : 0ull;
-	float const w1    = v1 ? P.ps_w[sl + lane + 32] : 0.0f;
+	uint4 const e0    = v0 ? P.ps_slot[sl + lane] : make_uint4(0u, 0u, 0u, 0u);
+	uint4 const e1    = v1 ? P.ps_slot[sl + lane + 32] : make_uint4(0u, 0u, 0u, 0u);
+	uint64_t const k0 = ((uint64_t)e0.y << 32) | e0.x, k1 = ((uint64_t)e1.y << 32) | e1.x;
+	float const w0 = __uint_as_float(e0.z), w1 = __uint_as_float(e1.z);
 	int const b0 = (int)(k0 >> 58), b1 = (int)(k1 >> 58);
 	int* const cnt = bin_cnt[wid];  // entries per bin
 	int* const st  = bin_run[wid];  // bin starts; st[nbins] = n
