@@ -143,7 +143,7 @@ int spice_set_mode(spice_net* net, int mode);
  * any time between steps): shared memory per target tile in bytes, and threads per delivery CTA.
  * Results do not depend on them.  Those the caller leaves unset are picked from the network's
  * sizes when it is prepared (its first step): mapping 17 (1 for tiles above 176 KiB), LIF window
- * 7, the largest tile of at most 100 KiB that gives the most delivery CTAs per window (input slots
+ * 9, the largest tile of at most 100 KiB that gives the most delivery CTAs per window (input slots
  * x target tiles) within one wave of one CTA per SM, and 768 / 512 / 256 threads for tiles of at
  * least 64 KiB / 24 KiB / less.  spice2_gb300.autotune measures them on a network instead. */
 enum {
@@ -213,7 +213,8 @@ enum {
 	                                   predicated adds, a warp-uniform test for counts of 8 or
 	                                   more, ballots kept in registers and list entries reserved
 	                                   only for the steps with spikes, 8 as 7 with two neurons
-	                                   per thread                                             */
+	                                   per thread, 9 as 7 with the step's count replay and LIF
+	                                   update as predicated PTX (no branch inside a step)     */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's

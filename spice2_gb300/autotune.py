@@ -101,7 +101,7 @@ def apply_shape(net, best: dict) -> None:
         net.set_tuning(neuron_variant=best["neuron_variant"])
 
 
-def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4, 5, 6, 7, 8), verbose: bool = False) -> dict:
+def tune_neurons(net, steps: int = 300, warm: int = 30, variants=(0, 1, 2, 3, 4, 5, 6, 7, 8, 9), verbose: bool = False) -> dict:
     """Times the neuron-update kernel of `net` for each LIF window variant (identical results);
     applies and returns the fastest."""
     results = []

@@ -617,11 +617,11 @@ void default_algo(spice_net* n) {
 
 // The launch shape of a network whose caller set none (the values an autotuner run on large and
 // small Brunel networks converges to): the compact-target row mapping with two sub-rows per lane
-// group (17), the lean LIF window (variant 7), and the tile size that gives the most delivery CTAs
+// group (17), the predicated LIF window (variant 9), and the tile size that gives the most delivery CTAs
 // per window -- input slots times target tiles -- within one wave of one CTA per SM, the largest
 // such tile (fewest sub-rows per spike), at most 100 KiB; threads by tile size.
 void default_shape(spice_net* n) {
-	if (!n->variant_set) n->neuron_variant = 7;
+	if (!n->variant_set) n->neuron_variant = 9;
 	default_algo(n);
 	if (n->tile_set && n->threads_set) return;
 	int dmin = (int)n->max_delay, dmax = 1;
@@ -2196,7 +2196,7 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 			n->persist_knob = (int)value;
 			return SPICE_OK;
 		case SPICE_TUNE_NEURON_VARIANT:
-			if (value < 0 || value > 8) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 8");
+			if (value < 0 || value > 9) return fail(SPICE_EINVAL, "neuron variant must be 0 .. 9");
 			n->neuron_variant = (int)value;
 			n->variant_set    = true;
 			return SPICE_OK;

@@ -693,6 +693,112 @@ __device__ __forceinline__ void window_lif_lean(A const& a, const PopDev* __rest
 	}
 }
 
+// Variant 9: variant 7 with the common step written as predicated PTX -- the count replay's
+// 4-, 2- and 1-blocks of each group as adds under a predicate set from the packed input word, and
+// the LIF step (lif_update) as compares feeding predicated multiply, reset and refractory load --
+// so that no step contains a branch beyond the warp-uniform test for large counts.  Same IEEE
+// operations in the same order as variant 7.
+template <bool ZERO, class A>
+__device__ __forceinline__ void window_lif_pred(A const& a, const PopDev* __restrict__ Pg, int p, int b,
+                                                const float* dts_sm, uint32_t (*xs_sm)[kThreads]) {
+	int const N      = (int)Pg->size;
+	int const i      = b * kThreads + threadIdx.x;
+	bool const valid = i < N;
+	int const lane   = threadIdx.x & 31;
+	int const word   = i >> 5;
+	uint32_t* const cnt = Pg->cnt;
+	float const vthres  = Pg->p0;
+	int32_t const tref  = (int32_t)Pg->p1;
+	float const w0 = Pg->group_weight[0], w1 = Pg->group_weight[1];
+	float V   = 0;
+	int32_t T = 0;
+	if (valid) {  // written two launches back: loaded before waiting for the previous launch
+		V = Pg->V[i];
+		T = Pg->T[i];
+	}
+	uint32_t const vmask = valid ? 0xffffffffu : 0u;
+	griddep_wait();  // the input ring, counts and lists are the previous launches' output
+	int const D = (int)a.D, Hb = a.Hb;
+	for (int k0 = 0; k0 < a.K; k0 += 16) {
+		int const nk    = min(16, a.K - k0);
+		int const slot0 = (int)((a.slot0 + k0) % D);
+		const uint32_t* src = cnt + (int64_t)slot0 * N + i;
+		int const wrap      = D - slot0;  // step u >= wrap reads ring slot u - wrap
+#pragma unroll
+		for (int u = 0; u < 16; u++) {  // asynchronous copies into the thread's own shared-memory column
+			if (u == wrap) src -= (int64_t)D * N;
+			if (valid && u < nk) {
+				unsigned const dst = (unsigned)__cvta_generic_to_shared(&xs_sm[u][threadIdx.x]);
+				asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+			} else {
+				xs_sm[u][threadIdx.x] = 0u;
+			}
+			src += N;
+		}
+		asm volatile("cp.async.wait_all;" ::: "memory");
+		uint32_t sbits = 0;   // this lane's spikes of the 16 steps
+		uint32_t mymask = 0;  // lane u: the warp's ballot of step u
+		uint32_t bit    = 1;  // 1 << u
+#pragma unroll 1
+		for (int u = 0; u < nk; u++, bit <<= 1) {
+			uint32_t const x = xs_sm[u][threadIdx.x];
+			if (__any_sync(0xffffffffu, (x & 0xfff8fff8u) != 0)) {  // a count of 8 or more in the warp
+				V = add_n_sel(V, w0, x & 0xffffu);
+				V = add_n_sel(V, w1, x >> 16);
+			} else {
+				asm("{\n\t.reg .pred q;\n\t.reg .b32 t;\n\t"
+				    "and.b32 t, %1, 4;\n\tsetp.ne.u32 q, t, 0;\n\t"
+				    "@q add.rn.f32 %0, %0, %2;\n\t@q add.rn.f32 %0, %0, %2;\n\t"
+				    "@q add.rn.f32 %0, %0, %2;\n\t@q add.rn.f32 %0, %0, %2;\n\t"
+				    "and.b32 t, %1, 2;\n\tsetp.ne.u32 q, t, 0;\n\t"
+				    "@q add.rn.f32 %0, %0, %2;\n\t@q add.rn.f32 %0, %0, %2;\n\t"
+				    "and.b32 t, %1, 1;\n\tsetp.ne.u32 q, t, 0;\n\t"
+				    "@q add.rn.f32 %0, %0, %2;\n\t"
+				    "and.b32 t, %1, 262144;\n\tsetp.ne.u32 q, t, 0;\n\t"
+				    "@q add.rn.f32 %0, %0, %3;\n\t@q add.rn.f32 %0, %0, %3;\n\t"
+				    "@q add.rn.f32 %0, %0, %3;\n\t@q add.rn.f32 %0, %0, %3;\n\t"
+				    "and.b32 t, %1, 131072;\n\tsetp.ne.u32 q, t, 0;\n\t"
+				    "@q add.rn.f32 %0, %0, %3;\n\t@q add.rn.f32 %0, %0, %3;\n\t"
+				    "and.b32 t, %1, 65536;\n\tsetp.ne.u32 q, t, 0;\n\t"
+				    "@q add.rn.f32 %0, %0, %3;\n\t}"
+				    : "+f"(V)
+				    : "r"(x), "f"(w0), "f"(w1));
+			}
+			if (ZERO && x) cnt[(int64_t)((slot0 + u) % D) * N + i] = 0;
+			// lif_update: T -= 1; when T <= 0, either spike (V > Vthres: V = 0, T = Tref) or leak
+			uint32_t spike;  // bit if the neuron spiked (and exists), else 0
+			asm("{\n\t.reg .pred pr, ps, pl;\n\t"
+			    "sub.s32 %1, %1, 1;\n\t"
+			    "setp.le.s32 pr, %1, 0;\n\t"
+			    "setp.gt.and.f32 ps, %0, %4, pr;\n\t"
+			    "and.pred pl, pr, !ps;\n\t"
+			    "@pl mul.rn.f32 %0, %0, %3;\n\t"
+			    "@ps mov.f32 %0, 0f00000000;\n\t"
+			    "@ps mov.b32 %1, %5;\n\t"
+			    "selp.u32 %2, %6, 0, ps;\n\t}"
+			    : "+f"(V), "+r"(T), "=r"(spike)
+			    : "f"(dts_sm[k0 + u]), "f"(vthres), "r"(tref), "r"(vmask & bit));
+			sbits |= spike;
+			unsigned const mask = __ballot_sync(0xffffffffu, spike != 0);
+			mymask              = lane == u ? mask : mymask;
+		}
+		if (lane < nk && word < Pg->nwords) Pg->bits[(int64_t)((a.hslot0 + k0 + lane) % Hb) * Pg->nwords + word] = mymask;
+		// list reservations, one per step in which the warp spiked
+		for (unsigned st = __reduce_or_sync(0xffffffffu, sbits); st; st &= st - 1) {
+			int const u         = __ffs(st) - 1;
+			unsigned const mask = __shfl_sync(0xffffffffu, mymask, u);
+			int base = 0;
+			if (lane == 0) base = atomicAdd(a.counts + (k0 + u) * a.npop + p, __popc(mask));
+			base = __shfl_sync(0xffffffffu, base, 0);
+			if ((sbits >> u) & 1u) Pg->list[(int64_t)(a.list_k0 + k0 + u) * N + base + __popc(mask & lanemask_lt())] = i;
+		}
+	}
+	if (valid) {
+		Pg->V[i] = V;
+		Pg->T[i] = T;
+	}
+}
+
 // Variant 8: variant 7 with two neurons per thread (neurons b*256 + tid and b*256 + 128 + tid of a
 // 128-thread CTA): the step loop's control, the leak factor and the large-count test are shared by
 // both, and the window's grid has half the neuron CTAs.  Same arithmetic and outputs per neuron.
@@ -926,6 +1032,10 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 	if (MODE == 0 && kind == 3) {
 		if constexpr (VAR == 8) window_lif_lean2(a, a.pops + p, p, lb, dts_sm, xs_sm);
 		else if constexpr (VAR == 7) window_lif_lean(a, a.pops + p, p, lb, dts_sm, xs_sm);
+		else if constexpr (VAR == 9) {
+			if (a.pops[p].zero_inputs) window_lif_pred<true>(a, a.pops + p, p, lb, dts_sm, xs_sm);
+			else window_lif_pred<false>(a, a.pops + p, p, lb, dts_sm, xs_sm);
+		}
 		else if constexpr (VAR == 4) window_lif_deferred<false, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else if constexpr (VAR == 5) window_lif_deferred<true, false>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
 		else if constexpr (VAR == 6) window_lif_deferred<false, true>(a, a.pops + p, p, lb, dts_sm, xs_sm, masks_sm);
@@ -3042,6 +3152,7 @@ cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks
 		else if (a.variant == 6) k_neurons<0, true, 6><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 7) k_neurons<0, true, 7><<<nblocks, kThreads, 0, stream>>>(a);
 		else if (a.variant == 8) k_neurons<0, true, 8><<<nblocks, kThreads, 0, stream>>>(a);
+		else if (a.variant == 9) k_neurons<0, true, 9><<<nblocks, kThreads, 0, stream>>>(a);
 		else k_neurons<0, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
 	} else {
 		if (only_fast) k_neurons<1, true, 0><<<nblocks, kThreads, 0, stream>>>(a);
@@ -3056,23 +3167,23 @@ cudaError_t launch_window(cudaStream_t stream, WindowArgs const& a, int nblocks,
 	if (nblocks + nsrc_blocks + nrb <= 0) return cudaSuccess;
 	bool only_fast = true;
 	for (int p = 0; p < a.npop; p++) only_fast &= a.blk_kind[p] != 0 && a.blk_kind[p] < kHistKind;
-	void const* fns[2][11] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
+	void const* fns[2][12] = {{(void const*)k_window<0, false, 0, false>, (void const*)k_window<0, true, 0, false>,
 	                           (void const*)k_window<0, true, 1, false>, (void const*)k_window<0, true, 2, false>,
 	                           (void const*)k_window<0, true, 3, false>, (void const*)k_window<0, true, 4, false>,
 	                           (void const*)k_window<0, true, 5, false>, (void const*)k_window<0, true, 6, false>,
 	                           (void const*)k_window<0, true, 7, false>, (void const*)k_window<0, true, 8, false>,
-	                           (void const*)k_window<1, true, 0, false>},
+	                           (void const*)k_window<0, true, 9, false>, (void const*)k_window<1, true, 0, false>},
 	                          {(void const*)k_window<0, false, 0, true>, (void const*)k_window<0, true, 0, true>,
 	                           (void const*)k_window<0, true, 1, true>, (void const*)k_window<0, true, 2, true>,
 	                           (void const*)k_window<0, true, 3, true>, (void const*)k_window<0, true, 4, true>,
 	                           (void const*)k_window<0, true, 5, true>, (void const*)k_window<0, true, 6, true>,
 	                           (void const*)k_window<0, true, 7, true>, (void const*)k_window<0, true, 8, true>,
-	                           (void const*)k_window<1, true, 0, true>}};
+	                           (void const*)k_window<0, true, 9, true>, (void const*)k_window<1, true, 0, true>}};
 	void const* fk_atomic_generic[2] = {(void const*)k_window<1, false, 0, false>, (void const*)k_window<1, false, 0, true>};
 	int const rec = nrb > 0 ? 1 : 0;
 	void const* fn = nullptr;
-	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 8 ? a.variant : 0)];
-	else fn = only_fast ? fns[rec][10] : fk_atomic_generic[rec];
+	if (a.mode == 0) fn = !only_fast ? fns[rec][0] : fns[rec][1 + (a.variant >= 0 && a.variant <= 9 ? a.variant : 0)];
+	else fn = only_fast ? fns[rec][11] : fk_atomic_generic[rec];
 	cudaLaunchConfig_t cfg = {};
 	cfg.gridDim          = dim3((unsigned)(nblocks + nsrc_blocks + nrb));
 	cfg.blockDim         = dim3((unsigned)kThreads);

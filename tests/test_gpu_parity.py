@@ -417,7 +417,7 @@ def test_results_independent_of_delivery_mapping(engine, algo, tile_bytes, threa
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7, 8, 9])
 def test_neuron_variants_match_reference(engine, variant):
     """Every LIF window variant of the neuron update (unrolled or rolled steps, per-lane or
     warp-uniform count replay) gives the reference's raster and V bit for bit."""
@@ -431,7 +431,7 @@ def test_neuron_variants_match_reference(engine, variant):
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
 
 
-@pytest.mark.parametrize("variant", [4, 5, 6, 7, 8])
+@pytest.mark.parametrize("variant", [4, 5, 6, 7, 8, 9])
 def test_neuron_variants_with_large_counts(engine, oracle_lib, variant):
     """Inputs of ~2.4 events per neuron and step from one group (counts of 8 or more, which take
     the general replay, in about one warp-step in ten): every variant bit-exact with the oracle."""
