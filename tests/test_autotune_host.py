@@ -49,7 +49,7 @@ def test_autotune_applies_the_fastest_shape_and_variant():
         seen_overlap.append(overlap)
         return {cands[0]: 30.0, cands[1]: 12.0, cands[2]: 20.0}[shape]
 
-    net = FakeNet(deliver_us, lambda v: {0: 9.0, 1: 8.0, 2: 7.0, 3: 9.5, 4: 6.5, 5: 6.9, 6: 6.6, 7: 6.7, 8: 6.8}[v])
+    net = FakeNet(deliver_us, lambda v: {0: 9.0, 1: 8.0, 2: 7.0, 3: 9.5, 4: 6.5, 5: 6.9, 6: 6.6, 7: 6.7, 8: 6.8, 9: 6.55}[v])
     rep = at.autotune(net, steps=5, warm=1, candidates=cands)
     best = rep["best"]
     assert (best["tile_bytes"], best["threads"], best["parts"], best["algo"]) == cands[1]
