@@ -238,6 +238,7 @@ cudaError_t launch_raster(cudaStream_t stream, RasterArgs const& a);
 // in one cooperative launch, the phases of a step separated by grid-wide barriers.
 constexpr int kPersistThreads = kNeuronThreads;  // the window bodies' CTA size
 constexpr int kPersistChunk   = 256;             // synapses of one delivery work unit (a warp's)
+constexpr int kPersistPlasticChunk = 64;         // ... of a plastic row (each synapse catches up first)
 constexpr int kPersistBlocksPerSM = 4;           // default CTAs per SM (fewer barrier arrivals)
 struct PersistArgs {
 	int64_t t0;             // first step of the launch
@@ -258,7 +259,7 @@ struct PersistArgs {
 	int blk_kind[kMaxPops];       // as WindowArgs::blk_kind
 	int blk_per_step[kMaxPops];   // Poisson: items per step
 	int64_t ext_pos[kMaxPops];    // external: train position of step t0
-	int64_t chunks[kMaxConns];    // per connection: delivery units per spike (ceil(max row / kPersistChunk))
+	int64_t chunks[kMaxConns];    // per connection: delivery units per spike (ceil(max row / chunk length))
 	int start_at_c;               // the first step's update (phase A) ran in the previous launch
 	int end_after_a;              // the last step stops after its update (its deliveries follow in the next launch)
 	int external_full;            // the periodic catch-up of every plastic synapse runs as its own kernel

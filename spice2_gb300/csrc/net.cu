@@ -1227,7 +1227,8 @@ int prepare(spice_net* n) {
 	}
 	n->run_cap = kRunCap;
 	CUDA_TRY(cudaDeviceGetAttribute(&n->sm_count, cudaDevAttrMultiProcessorCount, n->device));
-	if (n->persist_ok) {  // delivery units: a warp and at most kPersistChunk synapses of one row
+	if (n->persist_ok) {  // delivery units: a warp and at most kPersistChunk (plastic: kPersistPlasticChunk)
+		                  // synapses of one row
 		n->persist_chunks.assign(n->conns.size(), 1);
 		for (size_t ci = 0; ci < n->conns.size(); ci++) {
 			ConnDev const& d = n->conns[ci].d;
@@ -1238,7 +1239,8 @@ int prepare(spice_net* n) {
 				mr = 0;
 				for (int64_t r = 0; r < d.src_size; r++) mr = std::max(mr, off[r + 1] - off[r]);
 			}
-			n->persist_chunks[ci] = std::max<int64_t>(1, (mr + kPersistChunk - 1) / kPersistChunk);
+			int64_t const len     = d.plastic ? kPersistPlasticChunk : kPersistChunk;
+			n->persist_chunks[ci] = std::max<int64_t>(1, (mr + len - 1) / len);
 		}
 		TRY(dalloc(n, &n->d_barrier, 1));
 		TRY(dalloc(n, &n->d_pstatus, 1));

@@ -2902,8 +2902,9 @@ __global__ void k_batch_deliver(const __grid_constant__ BatchArgs b) {
 //   A  the neuron update and source populations of step t (the window bodies with K = 1)
 //   C  the deliveries of step t (snn.cpp:21-25) -- each fixed-weight connection's spikes of step t
 //      into ring slot (t + d - 1) mod D, and each plastic connection's spikes of step t - d + 1
-//      (catch-up, then the synapse's weight into slot t mod D), with global reductions, in work
-//      units of a warp and at most kPersistChunk synapses of one row; the raster of step t; the
+//      (catch-up, then the synapse's weight into slot t mod D; with delay 1 from the step's spike
+//      list, else from the bitmap), with global reductions, in work units of a warp and at most
+//      kPersistChunk (plastic: kPersistPlasticChunk) synapses of one row; the raster of step t; the
 //      other parity's spike counts cleared.  At t mod 64 == 0 the plastic units cover every row:
 //      the periodic catch-up of every synapse (snn.cpp:17-19) and, for a spiking source, the
 //      delivery right after it -- the reference's order per synapse, with no barrier between.  A
@@ -3025,6 +3026,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 				u_begin[c] = acc;
 				if (C.plastic) {
 					if (full) acc += C.src_size * a.chunks[c];
+					else if (C.delay == 1) acc += (int64_t)a.counts[q * a.npop + C.src] * a.chunks[c];
 					else if (t >= C.delay - 1) acc += (int64_t)C.src_nwords * a.chunks[c];
 				} else {
 					acc += (int64_t)a.counts[q * a.npop + C.src] * a.chunks[c];
@@ -3057,17 +3059,23 @@ __global__ void __launch_bounds__(kPersistThreads) k_persist(const __grid_consta
 				bool const weight_in = MODE == 1 && (C.plastic == SPICE_SYNAPSE_ISTDP || C.weight != 0.0f);
 				int64_t const slot   = t % a.D;
 				const uint32_t* bits = C.src_bits + ((t - C.delay + 1 + a.Hb) % a.Hb) * C.src_nwords;
+				constexpr int64_t L = kPersistPlasticChunk;
 				if (full) {  // unit: (source, chunk) of every row: catch-up, then the delivery if it spiked
 					int64_t const src = r / a.chunks[c];
 					bool const spiked = delivers && ((bits[src >> 5] >> (src & 31)) & 1u);
-					int64_t const e0 = C.off[src] + ch * kPersistChunk, e1 = min(C.off[src + 1], e0 + kPersistChunk);
+					int64_t const e0 = C.off[src] + ch * L, e1 = min(C.off[src + 1], e0 + L);
 					if (spiked && ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
 					plastic_row_chunk(C, e0, e1, t, C.ages[src], slot, spiked && weight_in, lane);
+				} else if (C.delay == 1) {  // unit: (spike, chunk) of step t, from the step's spike list
+					int32_t const src = C.src_list[(int64_t)q * C.src_size + r / a.chunks[c]];
+					int64_t const e0 = C.off[src] + ch * L, e1 = min(C.off[src + 1], e0 + L);
+					if (ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
+					plastic_row_chunk(C, e0, e1, t, C.ages[src], slot, weight_in, lane);
 				} else {  // unit: (bitmap word, chunk) of the spikes of step t - d + 1
 					int64_t const wd = r / a.chunks[c];
 					for (uint32_t m = bits[wd]; m; m &= m - 1) {
 						int64_t const src = 32 * wd + __ffs(m) - 1;
-						int64_t const e0 = C.off[src] + ch * kPersistChunk, e1 = min(C.off[src + 1], e0 + kPersistChunk);
+						int64_t const e0 = C.off[src] + ch * L, e1 = min(C.off[src + 1], e0 + L);
 						if (ch == 0 && lane == 0) ev += (unsigned long long)(C.off[src + 1] - C.off[src]);
 						plastic_row_chunk(C, e0, e1, t, C.ages[src], slot, weight_in, lane);
 					}
