@@ -58,20 +58,20 @@ WORKLOAD = "brunel_large_N5e5_p0.002_2000steps"
 # DRAM bytes (read + write) per synaptic event of the delivery kernels measured on this workload:
 # dram__bytes_read.sum + dram__bytes_write.sum of one full-size launch
 # (profiles/k_deliver_groups_brunel_N5e5_p0.002.md, profiles/k_deliver_staged_brunel_N5e5_p0.002.md,
-# profiles/k_deliver_rows16_k_window_brunel_N5e5_p0.002.md) divided by its events, keyed by delivery
+# profiles/k_deliver_rows16_brunel_N5e5_p0.002.md) divided by its events, keyed by delivery
 # mapping.  The bench's traffic per launch is this figure
 # times the launch's mean events (None for a mapping without a capture).
 DELIVER_DRAM_BYTES_PER_EVENT = {5: (62.261504e6 + 1.521152e6) / 11158496,
                                 8: (56.677376e6 + 0.970496e6) / 11158496,
                                 # mappings 15-21 read the same 16-bit target copy; measured on 17
-                                # (window 91, 10,415,589 events)
-                                15: (32.342528e6 + 0.064e6) / 10415589,
-                                16: (32.342528e6 + 0.064e6) / 10415589,
-                                17: (32.342528e6 + 0.064e6) / 10415589,
-                                18: (32.342528e6 + 0.064e6) / 10415589,
-                                19: (32.342528e6 + 0.064e6) / 10415589,
-                                20: (32.342528e6 + 0.064e6) / 10415589,
-                                21: (32.342528e6 + 0.064e6) / 10415589}
+                                # (window 30, 10,431,356 events)
+                                15: (32.3904e6 + 0.068352e6) / 10431356,
+                                16: (32.3904e6 + 0.068352e6) / 10431356,
+                                17: (32.3904e6 + 0.068352e6) / 10431356,
+                                18: (32.3904e6 + 0.068352e6) / 10431356,
+                                19: (32.3904e6 + 0.068352e6) / 10431356,
+                                20: (32.3904e6 + 0.068352e6) / 10431356,
+                                21: (32.3904e6 + 0.068352e6) / 10431356}
 DELIVER_KERNELS = {0: "k_deliver", 1: "k_deliver_tps", 2: "k_deliver_wps", 3: "k_deliver_tps<16-byte loads>",
                    4: "k_deliver_pipe", 5: "k_deliver_groups<4 lanes>", 6: "k_deliver_groups<8 lanes>",
                    7: "k_deliver_groups_occ", 8: "k_deliver_staged<2 in flight>",
