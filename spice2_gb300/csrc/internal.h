@@ -141,6 +141,8 @@ struct ConnDev {
 	const float* csc_w;       // weighted: weights in CSC order
 	const uint32_t* pull_orb; // [src_nwords] bit s: source s spiked in one of the pulled steps
 	const uint32_t* pull_wm;  // [src_size] bit k: source s spiked at (first pulled step + k - delay)
+	const int32_t* pull_act;  // the window's spiking sources of its (source, delay) set, and their number
+	const int* pull_nact;
 };
 
 // Window masks of one (source population, delay) pair of pulled connections (pull.cu).
@@ -150,6 +152,8 @@ struct PullSet {
 	const uint32_t* bits;  // the source's bitmap ring [Hb][nwords]
 	uint32_t* orb;         // [nwords]
 	uint32_t* wm;          // [size]
+	int32_t* act;          // [size] the window's spiking sources (any order), push-and-sort gather
+	int* nact;             // their number (emptied by k_ps_sort for the next window)
 };
 
 // A pulled connection whose spikes' events are counted (row lengths from its CSR).
@@ -318,7 +322,6 @@ struct spice_net {
 	int ps_nconn         = 0;
 	int* d_ps_conn       = nullptr;  // [ps_nconn] connection (by-target position) of each pulled connection
 	int* d_ps_pop        = nullptr;  // [ps_nconn] its pulled population
-	int64_t* d_ps_begin  = nullptr;  // [ps_nconn + 1] prefix of their source bitmap words
 	int64_t ps_units     = 0;
 };
 

@@ -84,8 +84,8 @@ struct PullArgs {
 	int ps_nconn;
 	const int* ps_conn;      // [ps_nconn] by-target position of each pulled connection
 	const int* ps_pop;       // [ps_nconn] its pulled population
-	const int64_t* ps_begin; // [ps_nconn + 1] prefix of the source bitmap words (work units)
-	int64_t ps_units;
+	int64_t ps_units;        // > 0: the push-and-sort gather is used (k_pull_masks lists the spiking sources)
+	int ps_grid;             // CTAs of the scatter (resident on every SM; warps stride over the rows)
 };
 cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<PullSet> const& sets,
                         std::vector<PullEvJob> const& ev);

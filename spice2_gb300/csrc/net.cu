@@ -765,11 +765,15 @@ int setup_pull(spice_net* n) {
 				ps.bits   = S.bits;
 				TRY(dalloc(n, &ps.orb, (size_t)std::max(S.nwords, 1)));
 				TRY(dalloc(n, &ps.wm, (size_t)std::max<int64_t>(S.size, 1)));
+				TRY(dalloc(n, &ps.act, (size_t)std::max<int64_t>(S.size, 1), false));
+				TRY(dalloc(n, &ps.nact, 1));  // zero
 				set = (int)n->pull_sets.size();
 				n->pull_sets.push_back(ps);
 			}
-			c.d.pull_orb = n->pull_sets[set].orb;
-			c.d.pull_wm  = n->pull_sets[set].wm;
+			c.d.pull_orb  = n->pull_sets[set].orb;
+			c.d.pull_wm   = n->pull_sets[set].wm;
+			c.d.pull_act  = n->pull_sets[set].act;
+			c.d.pull_nact = n->pull_sets[set].nact;
 			n->pull_ev.push_back({n->pops[c.d.src].d.nwords, n->pops[c.d.src].d.bits, c.d.off});
 		}
 		for (int f = d.pull_F; f < 3; f++) d.pull_field[f] = 0;
@@ -793,9 +797,9 @@ int setup_pull(spice_net* n) {
 		blk.push_back(blk.back() + pull_blocks_for(d.size));
 	}
 	n->pull_blocks = blk.back();
-	{  // push-and-sort gather: units (pulled connection, source bitmap word); rows must fit the sort key
+	{  // push-and-sort gather: units (pulled connection, spiking source); rows must fit the sort key
 		std::vector<int> ps_conn, ps_pop;
-		std::vector<int64_t> ps_begin(1, 0);
+		std::vector<int64_t> ps_begin(1, 0);  // source bitmap words per connection (their sum: the flag)
 		bool ok = !n->pull_pops.empty();
 		for (int pi : n->pull_pops) {
 			PopDev const& d = n->pops[pi].d;
@@ -820,10 +824,8 @@ int setup_pull(spice_net* n) {
 			}
 			TRY(dalloc(n, &n->d_ps_conn, std::max<size_t>(ps_conn.size(), 1), false));
 			TRY(dalloc(n, &n->d_ps_pop, std::max<size_t>(ps_pop.size(), 1), false));
-			TRY(dalloc(n, &n->d_ps_begin, ps_begin.size(), false));
 			CUDA_TRY(cudaMemcpy(n->d_ps_conn, ps_conn.data(), sizeof(int) * ps_conn.size(), cudaMemcpyHostToDevice));
 			CUDA_TRY(cudaMemcpy(n->d_ps_pop, ps_pop.data(), sizeof(int) * ps_pop.size(), cudaMemcpyHostToDevice));
-			CUDA_TRY(cudaMemcpy(n->d_ps_begin, ps_begin.data(), sizeof(int64_t) * ps_begin.size(), cudaMemcpyHostToDevice));
 		}
 	}
 	TRY(dalloc(n, &n->d_pull_pops, std::max<size_t>(n->pull_pops.size(), 1), false));
@@ -1741,8 +1743,8 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 				pa.ps_nconn    = n->ps_nconn;
 				pa.ps_conn     = n->d_ps_conn;
 				pa.ps_pop      = n->d_ps_pop;
-				pa.ps_begin    = n->d_ps_begin;
 				pa.ps_units    = n->ps_units;
+				pa.ps_grid     = 5 * std::max(n->sm_count, 1);
 				TRY(ev_begin(n, 4, &slot));
 				CUDA_TRY(launch_pull(n->stream, pa, n->pull_sets, n->pull_ev));
 				TRY(ev_end(n, slot));

@@ -134,16 +134,31 @@ __global__ void __launch_bounds__(kPullThreads) k_pull_masks(const __grid_consta
 		PullSet const S = a.sets[s];
 		int const nb    = (S.nwords + kPullThreads - 1) / kPullThreads;
 		if (b < nb) {
-			int const w = b * kPullThreads + threadIdx.x;
-			if (w >= S.nwords) return;
+			int const w      = b * kPullThreads + threadIdx.x;
+			bool const valid = w < S.nwords;
 			uint32_t x[kPullMaxWindow];
 			uint32_t any = 0;
 #pragma unroll
 			for (int k = 0; k < kPullMaxWindow; k++) {
 				int64_t const step = a.t + k - S.delay;
-				x[k]               = (k < a.K && step >= 0) ? S.bits[ring_step(step, a.Hb) * S.nwords + w] : 0u;
+				x[k]               = (valid && k < a.K && step >= 0) ? S.bits[ring_step(step, a.Hb) * S.nwords + w] : 0u;
 				any |= x[k];
 			}
+			if (a.ps_units > 0) {  // the word's spiking sources appended to the set's list (warp-aggregated)
+				int const lane = threadIdx.x & 31;
+				int const mine = __popc(any);
+				int incl       = mine;
+#pragma unroll
+				for (int d = 1; d < 32; d <<= 1) {
+					int const o = __shfl_up_sync(0xffffffffu, incl, d);
+					if (lane >= d) incl += o;
+				}
+				int base = 0;
+				if (lane == 31 && incl) base = atomicAdd(S.nact, incl);
+				base = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+				for (uint32_t r = any; r; r &= r - 1) S.act[base++] = 32 * w + __ffs(r) - 1;
+			}
+			if (!valid) return;
 			S.orb[w] = any;
 			uint32_t rest = any;
 			while (rest) {
@@ -347,60 +362,61 @@ __global__ void __launch_bounds__(kPullThreads) k_pull(const __grid_constant__ P
 // source, CSR order for duplicates), so both gathers give the same bins bit for bit.  A target with
 // more entries than its slots or its region takes the scan (pull_target) instead.
 
-// One warp per (pulled connection, source bitmap word).  Latency-bound (the slot reservations are
-// atomics with a result): at most 40 registers, so that six CTAs share an SM.
-__global__ void __launch_bounds__(kPullThreads, 6) k_ps_scatter(const __grid_constant__ PullArgs a) {
+// Warps stride over the rows of the window's spiking sources, connection after connection (the
+// sources listed by k_pull_masks; a connection's rows start at the warp after the previous
+// connection's last, so that the rows spread over all warps).  Latency-bound (the slot
+// reservations are atomics with a result): at most 48 registers, so that five CTAs share an SM.
+__global__ void __launch_bounds__(kPullThreads, 5) k_ps_scatter(const __grid_constant__ PullArgs a) {
 	int const lane  = threadIdx.x & 31;
-	int64_t const u = (int64_t)blockIdx.x * kPullWarps + (threadIdx.x >> 5);
-	if (u >= a.ps_units) return;
-	int lo = 0, hi = a.ps_nconn - 1;  // the pulled connection of unit u
-	while (lo < hi) {
-		int const mid = (lo + hi + 1) >> 1;
-		if (a.ps_begin[mid] <= u) lo = mid;
-		else hi = mid - 1;
-	}
-	int const cb     = a.ps_conn[lo];
-	ConnDev const& C = a.conns[cb];
-	PopDev const& P  = a.pops[a.ps_pop[lo]];
-	int64_t const wd = u - a.ps_begin[lo];
-	uint32_t bits    = C.pull_orb[wd];
-	if (!bits) return;
-	int const F = P.pull_F;
-	int f       = 0;
-	while (f + 1 < F && P.pull_field[f] != C.field) f++;
-	uint64_t const crank = (uint64_t)(cb - P.in_begin) << 50;
+	int64_t const gw = (int64_t)blockIdx.x * kPullWarps + (threadIdx.x >> 5);
+	int64_t const nw = (int64_t)gridDim.x * kPullWarps;
 	uint32_t const kmask = a.K >= 32 ? 0xffffffffu : (1u << a.K) - 1u;
-	for (; bits; bits &= bits - 1) {
-		int64_t const src = 32 * wd + __ffs(bits) - 1;
-		uint32_t const m  = C.pull_wm[src] & kmask;
-		if (!m) continue;
-		int64_t const e0 = C.off[src], e1 = C.off[src + 1];
-		uint64_t const sk = crank | ((uint64_t)src << 19);
-		int const nk = __popc(m);  // entries per synapse: one per step bit, reserved together
-		constexpr int U = 4;       // synapses per lane with their reservations in flight together
-		for (int64_t eb = e0 + lane; eb < e1; eb += 32 * U) {
-			int32_t j[U];
-			float w[U];
-			int pos[U];
+	int64_t pre = 0;  // rows of the connections before
+	for (int qc = 0; qc < a.ps_nconn; qc++) {
+		int const cb     = a.ps_conn[qc];
+		ConnDev const& C = a.conns[cb];
+		PopDev const& P  = a.pops[a.ps_pop[qc]];
+		int64_t const nrows = *C.pull_nact;
+		int64_t u = (gw - pre) % nw;
+		if (u < 0) u += nw;
+		pre += nrows;
+		if (u >= nrows) continue;
+		int const F = P.pull_F;
+		int f       = 0;
+		while (f + 1 < F && P.pull_field[f] != C.field) f++;
+		uint64_t const crank = (uint64_t)(cb - P.in_begin) << 50;
+		for (; u < nrows; u += nw) {
+			int64_t const src = C.pull_act[u];
+			uint32_t const m  = C.pull_wm[src] & kmask;
+			if (!m) continue;
+			int64_t const e0 = C.off[src], e1 = C.off[src + 1];
+			uint64_t const sk = crank | ((uint64_t)src << 19);
+			int const nk = __popc(m);  // entries per synapse: one per step bit, reserved together
+			constexpr int U = 4;       // synapses per lane with their reservations in flight together
+			for (int64_t eb = e0 + lane; eb < e1; eb += 32 * U) {
+				int32_t j[U];
+				float w[U];
+				int pos[U];
 #pragma unroll
-			for (int u = 0; u < U; u++)
-				if (eb + 32 * u < e1) {
-					j[u] = C.nb[eb + 32 * u];
-					w[u] = C.wts ? C.wts[eb + 32 * u] : C.weight;
-				}
+				for (int v = 0; v < U; v++)
+					if (eb + 32 * v < e1) {
+						j[v] = C.nb[eb + 32 * v];
+						w[v] = C.wts ? C.wts[eb + 32 * v] : C.weight;
+					}
 #pragma unroll
-			for (int u = 0; u < U; u++)
-				if (eb + 32 * u < e1) pos[u] = atomicAdd(P.pull_fill + j[u], nk);
+				for (int v = 0; v < U; v++)
+					if (eb + 32 * v < e1) pos[v] = atomicAdd(P.pull_fill + j[v], nk);
 #pragma unroll
-			for (int u = 0; u < U; u++) {
-				int64_t const e = eb + 32 * u;
-				if (e >= e1) break;
-				int q = pos[u];
-				for (uint32_t mm = m; mm; mm &= mm - 1, q++) {
-					if (q >= kPushSortSlots) break;
-					uint64_t const key = ((uint64_t)((__ffs(mm) - 1) * F + f) << 58) | sk | (uint64_t)(e - e0);
-					P.ps_slot[(int64_t)j[u] * kPushSortSlots + q] =
-					    make_uint4((uint32_t)key, (uint32_t)(key >> 32), __float_as_uint(w[u]), 0u);
+				for (int v = 0; v < U; v++) {
+					int64_t const e = eb + 32 * v;
+					if (e >= e1) break;
+					int q = pos[v];
+					for (uint32_t mm = m; mm; mm &= mm - 1, q++) {
+						if (q >= kPushSortSlots) break;
+						uint64_t const key = ((uint64_t)((__ffs(mm) - 1) * F + f) << 58) | sk | (uint64_t)(e - e0);
+						P.ps_slot[(int64_t)j[v] * kPushSortSlots + q] =
+						    make_uint4((uint32_t)key, (uint32_t)(key >> 32), __float_as_uint(w[v]), 0u);
+					}
 				}
 			}
 		}
@@ -417,6 +433,8 @@ __global__ void __launch_bounds__(kPullThreads) k_ps_sort(const __grid_constant_
 	__shared__ uint64_t key_s[kPullWarps][kPushSortSlots];
 	int const lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 	int const blk  = (int)blockIdx.x;
+	if (blk == 0)  // the scatter has read the lists: empty them for the next window
+		for (int s2 = threadIdx.x; s2 < a.nsets; s2 += blockDim.x) *a.sets[s2].nact = 0;
 	int q          = 0;
 	while (q + 1 < a.npull && blk >= a.pull_blk[q + 1]) q++;
 	int const pi    = a.pull_pops[q];
@@ -595,7 +613,7 @@ cudaError_t launch_pull(cudaStream_t stream, PullArgs const& a, std::vector<Pull
 	if (nb > 0) k_pull_masks<<<(unsigned)nb, kPullThreads, 0, stream>>>(a);
 	if (a.pull_blocks <= 0) return cudaGetLastError();
 	if (a.ps_units > 0) {  // push-and-sort
-		k_ps_scatter<<<(unsigned)((a.ps_units + kPullWarps - 1) / kPullWarps), kPullThreads, 0, stream>>>(a);
+		k_ps_scatter<<<(unsigned)a.ps_grid, kPullThreads, 0, stream>>>(a);
 		k_ps_sort<<<(unsigned)a.pull_blocks, kPullThreads, 0, stream>>>(a);
 	} else {
 		k_pull<<<(unsigned)a.pull_blocks, kPullThreads, 0, stream>>>(a);
