@@ -217,6 +217,11 @@ enum {
 	                                   update as predicated PTX (no branch inside a step)     */
 };
 int spice_set_tuning(spice_net* net, int knob, int64_t value);
+/* The knob's current value into *value: the caller's setting, the shape picked from the network's
+ * sizes once it is prepared, or (before that, for knobs the caller did not set) the value that
+ * stands until then.  SPICE_TUNE_PERSISTENT reads the knob as set (1: on, with the default CTAs
+ * per SM).  SPICE_TUNE_GRAPH_WINDOWS belongs to batches (spice_batch_set_tuning). */
+int spice_get_tuning(spice_net* net, int knob, int64_t* value);
 /* Upper bound on the steps fused into one neuron-update launch (default: the network's
  * minimum connection delay, the largest value that keeps the reference's semantics). */
 int spice_set_window(spice_net* net, int max_window);

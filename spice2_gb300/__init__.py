@@ -94,6 +94,7 @@ def _load():
         "spice_launch_count": [vp, P(i64)],
         "spice_get_stream": [vp, P(vp)],
         "spice_set_tuning": [vp, i32, i64],
+        "spice_get_tuning": [vp, i32, vp],
         "spice_synchronize": [vp],
         "spice_batch_create": [P(vp), i32, P(vp)],
         "spice_batch_destroy": [vp],
@@ -392,6 +393,20 @@ class snn:
             _check(lib().spice_set_tuning(self._h, 6, int(neuron_variant)))
         if launch_mode is not None:
             _check(lib().spice_set_tuning(self._h, 7, int(launch_mode)))
+
+    _TUNING_KNOBS = {"tile_bytes": 0, "deliver_threads": 1, "deliver_parts": 2, "deliver_algo": 3,
+                     "overlap_sources": 4, "neuron_variant": 6, "launch_mode": 7, "pull": 8, "source_steps": 9,
+                     "persistent": 10}
+
+    def get_tuning(self) -> dict:
+        """Every knob's current value (spice_get_tuning): the caller's settings, and once the network
+        is prepared (its first step) the launch shape picked from its sizes for the others."""
+        out = {}
+        for name, knob in self._TUNING_KNOBS.items():
+            v = C.c_int64()
+            _check(lib().spice_get_tuning(self._h, knob, C.byref(v)))
+            out[name] = v.value
+        return out
 
     # stepping
     def step(self):

@@ -2249,6 +2249,23 @@ extern "C" int spice_set_tuning(spice_net* n, int knob, int64_t value) {
 	return fail(SPICE_EINVAL, "unknown tuning knob");
 }
 
+extern "C" int spice_get_tuning(spice_net* n, int knob, int64_t* value) {
+	if (!n || !value) return fail(SPICE_EINVAL, "NULL argument");
+	switch (knob) {
+		case SPICE_TUNE_TILE_BYTES: *value = n->tile_bytes; return SPICE_OK;
+		case SPICE_TUNE_DELIVER_THREADS: *value = n->deliver_threads; return SPICE_OK;
+		case SPICE_TUNE_DELIVER_PARTS: *value = n->deliver_parts; return SPICE_OK;
+		case SPICE_TUNE_DELIVER_ALGO: *value = n->deliver_algo; return SPICE_OK;
+		case SPICE_TUNE_OVERLAP_SOURCES: *value = n->overlap_sources; return SPICE_OK;
+		case SPICE_TUNE_NEURON_VARIANT: *value = n->neuron_variant; return SPICE_OK;
+		case SPICE_TUNE_LAUNCH: *value = n->launch_mode; return SPICE_OK;
+		case SPICE_TUNE_PULL: *value = n->pull_all ? 1 : 0; return SPICE_OK;
+		case SPICE_TUNE_SOURCE_STEPS: *value = n->src_steps; return SPICE_OK;
+		case SPICE_TUNE_PERSISTENT: *value = n->persist_knob; return SPICE_OK;
+	}
+	return fail(SPICE_EINVAL, "unknown tuning knob (graph windows belong to batches)");
+}
+
 extern "C" int spice_get_stream(spice_net* n, void** out) {
 	if (!n || !out) return fail(SPICE_EINVAL, "NULL argument");
 	*out = (void*)n->stream;

@@ -210,6 +210,49 @@ def test_large_recorded_raster_equals_piecewise_recording(engine):
     assert n * 4 > (8 << 20)  # large enough for the threaded copy
 
 
+def _one_wave_tile(sizes, nslots, sms):
+    """The tile search of the default shape, restated: from 100 KiB down in 128-byte steps, the
+    largest tile (32-neuron multiples, 4 bytes per neuron) giving the most CTAs within one wave."""
+    best, tb = -1, 100 * 1024
+    for b in range(100 * 1024, 4 * 1024 - 1, -128):
+        tile = max(32, b // 4 // 32 * 32)
+        m = nslots * sum(-(-n // tile) for n in sizes)
+        if m > sms:
+            break
+        if m > best:
+            best, tb = m, b
+    return tb
+
+
+def test_default_shape_follows_the_network_sizes(engine):
+    """Knobs left unset are picked when the network is prepared: mapping 17, LIF window 9, the
+    largest tile <= 100 KiB giving the most (slot, tile) CTAs within one wave of the SMs, threads by
+    tile size; a caller's setting stands, and a tile too large for mapping 17's staging takes
+    mapping 1."""
+    import torch
+    sp = engine
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    big, _ = sp.brunel(500000, 0.002, 1)
+    assert big.get_tuning()["deliver_algo"] == 1  # the values that stand before preparation
+    big.run(0)
+    t = big.get_tuning()
+    assert (t["deliver_algo"], t["neuron_variant"], t["deliver_threads"]) == (17, 9, 768)
+    assert t["tile_bytes"] == _one_wave_tile([200000, 50000], 15, sms)
+    small, _ = sp.brunel(20000, 0.1, 1337)
+    small.run(0)
+    t = small.get_tuning()
+    assert (t["deliver_algo"], t["deliver_threads"]) == (17, 256)
+    assert t["tile_bytes"] == _one_wave_tile([8000, 2000], 15, sms)
+    own, _ = sp.brunel(20000, 0.1, 1337)
+    own.set_tuning(tile_bytes=200 * 1024, neuron_variant=4)
+    own.run(0)
+    t = own.get_tuning()
+    assert (t["tile_bytes"], t["deliver_algo"], t["neuron_variant"]) == (200 * 1024, 1, 4)
+    own.set_tuning(tile_bytes=64 * 1024)  # back within the staging budget: mapping 17 again
+    assert own.get_tuning()["deliver_algo"] == 17
+    own.run(30)
+
+
 @pytest.mark.parametrize("persistent", [0, 1])
 def test_pinned_caller_buffers_written_in_place(engine, persistent):
     """spice_run_record into pinned host buffers (written by the GPU while it steps) and into
