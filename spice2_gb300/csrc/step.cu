@@ -2038,16 +2038,26 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 			int64_t k = -1;
 			int src = 0;
 			if (lane < kConnBatch && ci < P.in_end) {  // the connection's fixed fields
-				ConnDev const& C = a.conns[ci];
-				k = sigma - (a.t0 + C.delay - 1);
-				if (k >= 0 && k < a.K && !C.plastic) {
+				// every field is loaded before the reach test, so that all the loads are one round trip
+				ConnDev const& C        = a.conns[ci];
+				int const delay         = C.delay;
+				int const plastic       = C.plastic;
+				int const csrc          = C.src;
+				const int32_t* const sl = C.src_list;
+				int64_t const ssize     = C.src_size;
+				const uint16_t* const n16 = C.nb16;
+				const int64_t* const bd = C.bounds;
+				int const wsel          = MODE == 0 ? C.word : C.fslot;
+				uint32_t const incw     = MODE == 0 ? C.inc : __float_as_uint(C.weight);
+				k = sigma - (a.t0 + delay - 1);
+				if (k >= 0 && k < a.K && !plastic) {
 					reach = true;
-					src   = C.src;
-					lst   = C.src_list + (a.list_k0 + k) * C.src_size;
-					nbp   = reinterpret_cast<const int4*>(C.nb16);
-					bnp   = C.bounds + t;
-					ai.x  = tile_addr + 4u * (uint32_t)(MODE == 0 ? C.word : C.fslot);
-					ai.y  = MODE == 0 ? C.inc : __float_as_uint(C.weight);
+					src   = csrc;
+					lst   = sl + (a.list_k0 + k) * ssize;
+					nbp   = reinterpret_cast<const int4*>(n16);
+					bnp   = bd + t;
+					ai.x  = tile_addr + 4u * (uint32_t)wsel;
+					ai.y  = incw;
 				}
 			}
 			if (cb == P.in_begin) {  // spike counts and lists: the previous launch's output
@@ -2097,16 +2107,45 @@ __device__ __forceinline__ void deliver_rows16(A const& a, PopDev const& P, int 
 		int const total = c_pre[nc];
 		for (int c0 = 0; c0 < total; c0 += STAGE) {
 			int const m = min(STAGE, total - c0);
-			for (int q = threadIdx.x; q < m; q += blockDim.x) {
-				int const g = c0 + q;
-				int j       = 0;
-				while (j + 1 < nc && c_pre[j + 1] <= g) j++;
-				const int64_t* bb = c_bnd[j] + (int64_t)__ldg(c_lst[j] + (g - c_pre[j])) * stride;
-				int64_t const b0  = __ldg(bb);
-				int const len     = (int)(__ldg(bb + 1) - b0);
-				st_ptr[q]         = c_nb[j] + (b0 >> 3);
-				st_lohi[q]        = (uint32_t)(b0 & 7) | ((uint32_t)((int)(b0 & 7) + len) << 3);
-				st_ai[q]          = c_ai[j];
+			// A thread stages up to R sub-rows per pass with all their loads in flight together: the
+			// R spike-list loads, then the 2 R bound loads that depend on them -- two load round trips
+			// per pass (one pass when STAGE <= R * blockDim.x) instead of two per sub-row.
+			constexpr int R = STAGE > 1024 ? 3 : 2;
+			for (int q0 = threadIdx.x; q0 < m; q0 += R * blockDim.x) {
+				int jr[R];
+				int32_t sr[R];
+#pragma unroll
+				for (int r = 0; r < R; r++) {
+					int const q = q0 + r * (int)blockDim.x;
+					int j       = 0;
+					sr[r]       = 0;
+					if (q < m) {
+						int const g = c0 + q;
+						while (j + 1 < nc && c_pre[j + 1] <= g) j++;
+						sr[r] = __ldg(c_lst[j] + (g - c_pre[j]));
+					}
+					jr[r] = j;
+				}
+				int64_t b0[R], b1[R];
+#pragma unroll
+				for (int r = 0; r < R; r++) {
+					b0[r] = b1[r] = 0;
+					if (q0 + r * (int)blockDim.x < m) {
+						const int64_t* bb = c_bnd[jr[r]] + (int64_t)sr[r] * stride;
+						b0[r]             = __ldg(bb);
+						b1[r]             = __ldg(bb + 1);
+					}
+				}
+#pragma unroll
+				for (int r = 0; r < R; r++) {
+					int const q = q0 + r * (int)blockDim.x;
+					if (q < m) {
+						int const len = (int)(b1[r] - b0[r]);
+						st_ptr[q]     = c_nb[jr[r]] + (b0[r] >> 3);
+						st_lohi[q]    = (uint32_t)(b0[r] & 7) | ((uint32_t)((int)(b0[r] & 7) + len) << 3);
+						st_ai[q]      = c_ai[jr[r]];
+					}
+				}
 			}
 			if (threadIdx.x == 0) s_next = 0;
 			__syncthreads();
