@@ -15,7 +15,8 @@ Printed JSON (one line, rank 0):
   roofline     the delivery kernel (dominant): algorithmic bytes per launch (8 B per synaptic
                event: int32 target + fp32 weight) / its mean CUDA-event duration, against
                MEASURED_PEAKS.json hbm_gbs; frac_at_4_bytes is the same against the 4-byte target
-               alone (a fixed_weight synapse has one weight per projection)
+               alone (a fixed_weight synapse has one weight per projection); frac_span the same
+               bytes over the launches' device spans (first CTA start to last CTA end)
   cpu_baseline the CPU restatement of the reference step loop (oracle/oracle_bench, the same
                algorithm as the reference's single-core path) timed on this host's cores
   atomic_mode  value with the fast atomic delivery mode (order-dependent float rounding)
@@ -749,6 +750,7 @@ def main():
     prof_events = net.events - pe0
     n_del, ms_del = net.kernel_stats(1)
     n_win, ms_win = net.kernel_stats(0)
+    n_span, ms_span = net.kernel_span(1)  # the same launches' device spans (first CTA start to last end)
     net.set_profiling(False)
     ms_max = _max_over_ranks(ms, ws)
     events_all = _sum_over_ranks(float(events), ws)
@@ -815,6 +817,8 @@ def main():
     ev_per_launch = prof_events / max(n_del, 1)
     t_launch = ms_del / max(n_del, 1) / 1e3
     achieved = bytes_per_event * ev_per_launch / t_launch / 1e9 if t_launch > 0 else None
+    t_span = ms_span / n_span / 1e3 if n_span > 0 else 0.0
+    achieved_span = bytes_per_event * ev_per_launch / t_span / 1e9 if t_span > 0 else None
     traffic = None
     if tuned["algo"] in DELIVER_DRAM_BYTES_PER_EVENT:
         traffic = DELIVER_DRAM_BYTES_PER_EVENT[tuned["algo"]] * ev_per_launch
@@ -893,7 +897,13 @@ def main():
                      "launches": n_del, "mean_launch_us": t_launch * 1e6,
                      "kernel_timing": "CUDA events around every delivery launch on the net's stream, over a "
                                       "second run of the timed steps (the headline is timed without them)",
-                     "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3},
+                     "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3,
+                     "kernel_span_us": t_span * 1e6 if n_span else None,
+                     "achieved_span": achieved_span,
+                     "frac_span": (achieved_span / peak) if achieved_span else None,
+                     "span_timing": "the same delivery launches from their first CTA's start to their last CTA's "
+                                    "end on the GPU's global timer; mean_launch_us - kernel_span_us is the fixed "
+                                    "cost of a launch and of the CUDA-event pair around it"},
         "cpu_baseline": cpu,
         "atomic_mode": atomic,
         "pull_mode": pull,

@@ -91,6 +91,7 @@ def _load():
         "spice_get_csc": [vp, i32, vp, vp],
         "spice_set_profiling": [vp, i32],
         "spice_kernel_stats": [vp, i32, P(i64), P(f64)],
+        "spice_kernel_span": [vp, i32, P(i64), P(f64)],
         "spice_launch_count": [vp, P(i64)],
         "spice_get_stream": [vp, P(vp)],
         "spice_set_tuning": [vp, i32, i64],
@@ -515,6 +516,13 @@ class snn:
     def kernel_stats(self, kind: int):
         n, ms = C.c_int64(), C.c_double()
         _check(lib().spice_kernel_stats(self._h, kind, C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def kernel_span(self, kind: int):
+        """Delivery launches (kind 1) since profiling was switched on: (launches, summed ms from the
+        first CTA's start to the last CTA's end on the device timer)."""
+        n, ms = C.c_int64(), C.c_double()
+        _check(lib().spice_kernel_span(self._h, kind, C.byref(n), C.byref(ms)))
         return n.value, ms.value
 
     def launch_count(self) -> int:

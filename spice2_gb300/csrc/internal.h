@@ -211,8 +211,10 @@ struct PendingGen {  // a fixed_probability connection whose adjacency is not ge
 };
 
 struct KernelStat {
-	int64_t launches = 0;
-	double ms        = 0;
+	int64_t launches      = 0;
+	double ms             = 0;
+	int64_t span_launches = 0;  // launches with a device span (first CTA start to last CTA end)
+	double span_ms        = 0;
 };
 
 }  // namespace spice_gb300
@@ -272,6 +274,8 @@ struct spice_net {
 	bool profiling = false;
 	std::vector<cudaEvent_t> ev_pool;
 	std::vector<std::pair<int, int>> ev_pending;  // (kind, event index of the start)
+	unsigned long long* d_span = nullptr;         // [event pool size]: per event pair, ~first CTA start and
+	                                              // last CTA end of a delivery launch (zeroed after each harvest)
 	size_t ev_used = 0;
 	spice_gb300::KernelStat stats[5];
 	int64_t launches = 0;

@@ -189,6 +189,7 @@ struct DeliverArgs {
 	                         // 8 / 9: 4 lanes per spike with sub-row descriptors staged in shared memory,
 	                         // 2 / 4 sub-rows in flight per group
 	int list_k0;             // first list slot of this window's parity
+	unsigned long long* span;  // profiling: [0] earliest CTA start, [1] latest CTA end (global ns); else null
 };
 // One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.
 cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int threads);

@@ -109,22 +109,45 @@ float kahan_next(spice_net* n) {  // kahan_sum<float>::operator+= then the reset
 }
 
 // ---- profiling ----
+constexpr size_t kEventPool = 4096;  // CUDA events of the profiling pool (two per launch)
+
+// Reads every recorded pair (complete once the streams are idle) into the per-kind statistics, with
+// the device spans of the delivery launches, and empties the pool.
+int harvest(spice_net* n) {
+	if (n->ev_pending.empty()) return SPICE_OK;
+	CUDA_TRY(cudaStreamSynchronize(n->stream));
+	if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
+	std::vector<unsigned long long> span;
+	if (n->d_span) {
+		span.resize(kEventPool);
+		CUDA_TRY(cudaMemcpy(span.data(), n->d_span, sizeof(unsigned long long) * kEventPool, cudaMemcpyDeviceToHost));
+	}
+	for (auto const& pr : n->ev_pending) {
+		float ms = 0;
+		CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
+		KernelStat& st = n->stats[pr.first];
+		st.ms += ms;
+		st.launches++;
+		if (!span.empty() && pr.second + 1 < (int)kEventPool && span[pr.second] && span[pr.second + 1]) {
+			unsigned long long const t0 = ~span[pr.second], t1 = span[pr.second + 1];  // start kept complemented
+			if (t1 >= t0) {
+				st.span_ms += (double)(t1 - t0) * 1e-6;
+				st.span_launches++;
+			}
+		}
+	}
+	n->ev_pending.clear();
+	n->ev_used = 0;
+	if (n->d_span) CUDA_TRY(cudaMemsetAsync(n->d_span, 0, sizeof(unsigned long long) * kEventPool, n->stream));
+	return SPICE_OK;
+}
+
 int ev_begin(spice_net* n, int kind, int* slot, cudaStream_t st = nullptr) {
 	*slot = -1;
 	if (!n->profiling) return SPICE_OK;
 	if (n->ev_used + 2 > n->ev_pool.size()) {
-		// harvest: every recorded pair is complete once the streams are idle
-		CUDA_TRY(cudaStreamSynchronize(n->stream));
-		if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
-		for (auto const& pr : n->ev_pending) {
-			float ms = 0;
-			CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
-			n->stats[pr.first].ms += ms;
-			n->stats[pr.first].launches++;
-		}
-		n->ev_pending.clear();
-		n->ev_used = 0;
-		while (n->ev_pool.size() < 4096) {
+		TRY(harvest(n));
+		while (n->ev_pool.size() < kEventPool) {
 			cudaEvent_t e;
 			CUDA_TRY(cudaEventCreate(&e));
 			n->ev_pool.push_back(e);
@@ -139,21 +162,6 @@ int ev_begin(spice_net* n, int kind, int* slot, cudaStream_t st = nullptr) {
 
 int ev_end(spice_net* n, int slot, cudaStream_t st = nullptr) {
 	if (slot >= 0) CUDA_TRY(cudaEventRecord(n->ev_pool[slot + 1], st ? st : n->stream));
-	return SPICE_OK;
-}
-
-int harvest(spice_net* n) {
-	if (n->ev_pending.empty()) return SPICE_OK;
-	CUDA_TRY(cudaStreamSynchronize(n->stream));
-	if (n->stream_src) CUDA_TRY(cudaStreamSynchronize(n->stream_src));
-	for (auto const& pr : n->ev_pending) {
-		float ms = 0;
-		CUDA_TRY(cudaEventElapsedTime(&ms, n->ev_pool[pr.second], n->ev_pool[pr.second + 1]));
-		n->stats[pr.first].ms += ms;
-		n->stats[pr.first].launches++;
-	}
-	n->ev_pending.clear();
-	n->ev_used = 0;
 	return SPICE_OK;
 }
 
@@ -1704,6 +1712,7 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			da.algo           = n->deliver_algo;
 			da.pdl            = fused ? 1 : 0;
 			TRY(ev_begin(n, 1, &slot));
+			da.span = (slot >= 0 && n->d_span) ? n->d_span + slot : nullptr;  // profiled: the launch's device span
 			CUDA_TRY(launch_deliver(n->stream, da, n->deliver_threads));
 			if (n->plastic)  // spikes of age d - 1 (snn.cpp:21-25), from the source's bitmap ring
 				for (auto const& c : n->conns)
@@ -2093,12 +2102,14 @@ extern "C" int spice_set_profiling(spice_net* n, int on) {
 	TRY(harvest(n));
 	n->profiling = on != 0;
 	for (auto& s : n->stats) s = KernelStat{};
-	if (n->profiling)
-		while (n->ev_pool.size() < 4096) {
+	if (n->profiling) {
+		while (n->ev_pool.size() < kEventPool) {
 			cudaEvent_t e;
 			CUDA_TRY(cudaEventCreate(&e));
 			n->ev_pool.push_back(e);
 		}
+		if (!n->d_span) TRY(dalloc(n, &n->d_span, kEventPool));  // zeroed
+	}
 	return SPICE_OK;
 }
 
@@ -2123,6 +2134,15 @@ extern "C" int spice_kernel_stats(spice_net* n, int kind, int64_t* launches, dou
 	TRY(harvest(n));
 	if (launches) *launches = n->stats[kind].launches;
 	if (ms) *ms = n->stats[kind].ms;
+	return SPICE_OK;
+}
+
+extern "C" int spice_kernel_span(spice_net* n, int kind, int64_t* launches, double* ms) {
+	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
+	if (kind < 0 || kind > 4) return fail(SPICE_EINVAL, "unknown kernel kind");
+	TRY(harvest(n));
+	if (launches) *launches = n->stats[kind].span_launches;
+	if (ms) *ms = n->stats[kind].span_ms;
 	return SPICE_OK;
 }
 

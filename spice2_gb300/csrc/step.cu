@@ -2292,6 +2292,25 @@ __device__ __forceinline__ void deliver_wps(A const& a, PopDev const& P, int t, 
 	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
+// Device span of a profiled delivery launch (DeliverArgs::span, null otherwise; both words zeroed
+// before): the earliest CTA start (complemented) and the latest CTA end on the GPU's global
+// nanosecond timer, so that the launch's own duration can be told from the fixed cost of the
+// CUDA-event pair around it.
+__device__ __forceinline__ unsigned long long global_ns() {
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+__device__ __forceinline__ void span_begin(DeliverArgs const& a) {  // kept complemented: max of ~t = min of t
+	if (a.span && threadIdx.x == 0) atomicMax(a.span, ~global_ns());
+}
+__device__ __forceinline__ void span_end(DeliverArgs const& a) {
+	if (a.span) {  // uniform: every thread of the CTA is here
+		__syncthreads();
+		if (threadIdx.x == 0) atomicMax(a.span + 1, global_ns());
+	}
+}
+
 // Plain-net delivery kernels: block -> (part, slot si, tile g over all target populations).
 struct DeliverItem {
 	int part, si, Q, t;
@@ -2328,74 +2347,96 @@ __device__ __forceinline__ DeliverItem deliver_item(DeliverArgs const& a) {
 
 template <int MODE>
 __global__ void __launch_bounds__(1024) k_deliver(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_flat<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE, bool VEC>
 __global__ void k_deliver_tps(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_tps<MODE, VEC>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE>
 __global__ void k_deliver_pipe(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_tps_pipe<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE, int G>
 __global__ void k_deliver_groups(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_groups<MODE, G>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE, int SF>
 __global__ void k_deliver_staged(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_staged<MODE, SF>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE, int SF, int U>
 __global__ void __launch_bounds__(SF > 2 || SF * U > 8 ? 768 : 1024, 1) k_deliver_staged_vec(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_staged_vec<MODE, SF, U>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE>
 __global__ void __launch_bounds__(1024, 1) k_deliver_rows(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_rows<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE, int SF, int U, bool TMA>
 __global__ void __launch_bounds__(SF > 1 ? 768 : 1024, 1) k_deliver_rows16(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item<false>(a);  // deliver_rows16 waits after its prologue
 	deliver_rows16<MODE, SF, U, TMA>(a, a.pops[it.Q], it.t, it.si, it.part);
 	clear_counts_next(a);
+	span_end(a);
 }
 
 // The compact-target row mapping at two 512-thread CTAs per SM (at most 64 registers, 1024 staged
 // sub-rows): one CTA's staging, barriers and flush overlap the other's reductions.
 template <int MODE, int SF, int U>
 __global__ void __launch_bounds__(512, 2) k_deliver_rows16_occ(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item<false>(a);
 	deliver_rows16<MODE, SF, U, false, 1024>(a, a.pops[it.Q], it.t, it.si, it.part);
 	clear_counts_next(a);
+	span_end(a);
 }
 
 // The 4-lane mapping with at most 32 registers per thread: four 512-thread CTAs (all 64 warps)
 // resident per SM, for windows whose (slot, tile) items fit one wave at that occupancy.
 template <int MODE>
 __global__ void __launch_bounds__(512, 4) k_deliver_groups_occ(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_groups<MODE, 4>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 template <int MODE>
 __global__ void __launch_bounds__(1024) k_deliver_wps(const __grid_constant__ DeliverArgs a) {
+	span_begin(a);
 	DeliverItem const it = deliver_item(a);
 	deliver_wps<MODE>(a, a.pops[it.Q], it.t, it.si, it.part);
+	span_end(a);
 }
 
 // Targets as indices within their delivery tile (tile <= 65536 neurons), in CSR order.

@@ -253,6 +253,26 @@ def test_default_shape_follows_the_network_sizes(engine):
     own.run(30)
 
 
+def test_delivery_spans_lie_inside_their_event_pairs(engine):
+    """With profiling on, each delivery launch also reports its device span (first CTA start to last
+    CTA end on the global timer), which is shorter than the CUDA-event time around the launch; the
+    raster and V stay the reference's bit for bit."""
+    g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
+    N, seed, steps = (int(x) for x in g["meta"])
+    net, pops = engine.brunel(N, float(g["p"][0]), seed)
+    net.set_profiling(True)
+    counts, idx = _raster_flat(net.run_record(steps))
+    n_ev, ms_ev = net.kernel_stats(1)
+    n_sp, ms_sp = net.kernel_span(1)
+    assert net.kernel_span(0) == (0, 0.0)  # spans are recorded for the delivery only
+    net.set_profiling(False)
+    assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
+    for k in (1, 2):
+        assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
+    assert n_ev > 0 and 0 < n_sp <= n_ev
+    assert 0 < ms_sp < ms_ev
+
+
 @pytest.mark.parametrize("persistent", [0, 1])
 def test_pinned_caller_buffers_written_in_place(engine, persistent):
     """spice_run_record into pinned host buffers (written by the GPU while it steps) and into
