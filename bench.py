@@ -751,6 +751,7 @@ def main():
     n_del, ms_del = net.kernel_stats(1)
     n_win, ms_win = net.kernel_stats(0)
     n_span, ms_span = net.kernel_span(1)  # the same launches' device spans (first CTA start to last end)
+    n_wspan, ms_wspan = net.kernel_span(0)
     net.set_profiling(False)
     ms_max = _max_over_ranks(ms, ws)
     events_all = _sum_over_ranks(float(events), ws)
@@ -898,6 +899,7 @@ def main():
                      "kernel_timing": "CUDA events around every delivery launch on the net's stream, over a "
                                       "second run of the timed steps (the headline is timed without them)",
                      "neuron_kernel_mean_us": ms_win / max(n_win, 1) * 1e3,
+                     "neuron_kernel_span_us": ms_wspan / n_wspan * 1e3 if n_wspan else None,
                      "kernel_span_us": t_span * 1e6 if n_span else None,
                      "achieved_span": achieved_span,
                      "frac_span": (achieved_span / peak) if achieved_span else None,

@@ -298,10 +298,12 @@ int spice_set_profiling(spice_net* net, int on);
  * (Poisson / external trains).  Returns the number of launches and their summed device time (ms)
  * since profiling was switched on. */
 int spice_kernel_stats(spice_net* net, int kind, int64_t* launches_out, double* ms_out);
-/* The same launches' device spans, kind 1 (spike delivery) only: per launch, from the first of its
- * CTAs to start to the last to finish on the GPU's global timer, summed (ms), and the number of
- * launches with a span -- the launch's own duration without the fixed cost of the CUDA-event pair
- * around it.  No counterpart in the reference (it has no device).  Other kinds report 0 launches. */
+/* The same launches' device spans, kinds 0 (neuron update, with the sources and raster blocks of
+ * its grid) and 1 (spike delivery): per launch, from the first of its CTAs to start to the last to
+ * finish on the GPU's global timer, summed (ms), and the number of launches with a span -- the
+ * launch's own duration without the fixed cost of the CUDA-event pair around it.  No counterpart
+ * in the reference (it has no device).  Other kinds, the persistent steps and user-model launches
+ * report no spans. */
 int spice_kernel_span(spice_net* net, int kind, int64_t* launches_out, double* ms_out);
 /* Number of kernels this library launched on the net's stream so far. */
 int spice_launch_count(spice_net* net, int64_t* launches_out);

@@ -519,8 +519,9 @@ class snn:
         return n.value, ms.value
 
     def kernel_span(self, kind: int):
-        """Delivery launches (kind 1) since profiling was switched on: (launches, summed ms from the
-        first CTA's start to the last CTA's end on the device timer)."""
+        """Neuron-update (kind 0) or delivery (kind 1) launches since profiling was switched on:
+        (launches with a span, summed ms from the first CTA's start to the last CTA's end on the
+        device timer)."""
         n, ms = C.c_int64(), C.c_double()
         _check(lib().spice_kernel_span(self._h, kind, C.byref(n), C.byref(ms)))
         return n.value, ms.value

@@ -154,6 +154,7 @@ struct WindowArgs {
 	int blk_per_step[kMaxPops];  // Poisson / external: CTAs per step
 	int src_steps;               // Poisson: consecutive steps each source CTA draws (>= 1)
 	int64_t ext_pos[kMaxPops];   // external: train position of step t0
+	unsigned long long* span;    // profiling: [0] ~earliest CTA start, [1] latest CTA end (global ns); else null
 };
 cudaError_t launch_neurons(cudaStream_t stream, WindowArgs const& a, int nblocks);
 struct RasterArgs;
@@ -189,7 +190,7 @@ struct DeliverArgs {
 	                         // 8 / 9: 4 lanes per spike with sub-row descriptors staged in shared memory,
 	                         // 2 / 4 sub-rows in flight per group
 	int list_k0;             // first list slot of this window's parity
-	unsigned long long* span;  // profiling: [0] earliest CTA start, [1] latest CTA end (global ns); else null
+	unsigned long long* span;  // profiling: [0] ~earliest CTA start, [1] latest CTA end (global ns); else null
 };
 // One CTA per (input slot, target tile): shared-memory accumulation, then a coalesced flush.
 cudaError_t launch_deliver(cudaStream_t stream, DeliverArgs const& a, int threads);

@@ -1647,8 +1647,10 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			bool const fused = n->launch_mode == 1 && !user_src && !user_st;
 			if (fused) {
 				TRY(ev_begin(n, 0, &slot));
+				wa.span = (slot >= 0 && n->d_span) ? n->d_span + slot : nullptr;  // profiled: the grid's device span
 				// the first window of a chunk follows the chunk's host-to-device copies: a plain launch
 				CUDA_TRY(launch_window(n->stream, wa, nb, ws, nbs, raster_pending ? &pending : nullptr, j > 0));
+				wa.span = nullptr;
 				TRY(ev_end(n, slot));
 				if (nb + nbs > 0 || raster_pending) n->launches++;
 				raster_pending = false;
@@ -1666,7 +1668,9 @@ int run_steps(spice_net* n, int64_t steps, bool record, int64_t* rows_done_out) 
 			}
 			if (!fused) {
 				TRY(ev_begin(n, 0, &slot));
+				wa.span = (slot >= 0 && n->d_span && !user_st) ? n->d_span + slot : nullptr;  // profiled
 				CUDA_TRY(launch_neurons(n->stream, wa, nb));
+				wa.span = nullptr;
 				if (user_st) TRY(launch_user_pops(n, wa, j, true, false, n->stream));
 				TRY(ev_end(n, slot));
 				if (nb > 0) n->launches++;

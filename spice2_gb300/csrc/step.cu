@@ -382,6 +382,25 @@ __device__ __forceinline__ float add_n_warp(float v, float w, uint32_t n) {
 	return v;
 }
 
+// Device span of a profiled launch (DeliverArgs::span, WindowArgs::span; null otherwise, both words
+// zeroed before): the earliest CTA start (complemented: the max of ~t is the min of t) and the latest
+// CTA end on the GPU's global nanosecond timer, so that the launch's own duration can be told from
+// the fixed cost of the CUDA-event pair around it.  span_close is reached by every thread of the CTA.
+__device__ __forceinline__ unsigned long long global_ns() {
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+__device__ __forceinline__ void span_open(unsigned long long* sp) {
+	if (sp && threadIdx.x == 0) atomicMax(sp, ~global_ns());
+}
+__device__ __forceinline__ void span_close(unsigned long long* sp) {
+	if (sp) {  // uniform
+		__syncthreads();
+		if (threadIdx.x == 0) atomicMax(sp + 1, global_ns());
+	}
+}
+
 // The Brunel LIF window (deterministic mode, every input group adds to V through a 16-bit counter
 // of word 0): the input words of 16 consecutive slots are loaded up front, then the steps run.
 // Same arithmetic, in the same order, as window_neurons<0, true, false>; dt comes from shared
@@ -1060,7 +1079,9 @@ __device__ __forceinline__ void neurons_block(WindowArgs const& a, int b) {
 // that each keeps its own register count.
 template <int MODE, bool ONLY_FAST, int VAR>
 __global__ void __launch_bounds__(kThreads, ONLY_FAST ? kNeuronBlocksPerSM : 1) k_neurons(const __grid_constant__ WindowArgs a) {
+	span_open(a.span);
 	neurons_block<MODE, ONLY_FAST, VAR>(a, (int)blockIdx.x);
+	span_close(a.span);
 }
 
 // Populations without inputs (Poisson, external trains): one CTA per (step, chunk).  They depend on
@@ -1103,11 +1124,13 @@ __global__ void __launch_bounds__(kThreads, ONLY_FAST ? kNeuronBlocksPerSM : 1) 
 	// each block kind waits for the previous launch where it first reads that launch's output; the
 	// raster blocks read only final data (the previous window's bitmaps and counts)
 	griddep_launch();
+	span_open(a.span);
 	int const nrb = REC ? r.K * r.npop : 0;  // raster blocks first: they start with the first wave
 	int const b   = (int)blockIdx.x;
 	if (REC && b < nrb) raster_block(r, b);  // the previous window's raster
 	else if (b < nrb + nb) neurons_block<MODE, ONLY_FAST, VAR>(a, b - nrb);
 	else sources_block(s, b - nrb - nb);
+	span_close(a.span);
 }
 
 // Writes a finished shared-memory tile into ring slot sigma mod D: a plain store when this CTA is
@@ -2292,24 +2315,8 @@ __device__ __forceinline__ void deliver_wps(A const& a, PopDev const& P, int t, 
 	flush_tile<MODE>(a, P, tbase, words, sigma, tile_sm);
 }
 
-// Device span of a profiled delivery launch (DeliverArgs::span, null otherwise; both words zeroed
-// before): the earliest CTA start (complemented) and the latest CTA end on the GPU's global
-// nanosecond timer, so that the launch's own duration can be told from the fixed cost of the
-// CUDA-event pair around it.
-__device__ __forceinline__ unsigned long long global_ns() {
-	unsigned long long t;
-	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-	return t;
-}
-__device__ __forceinline__ void span_begin(DeliverArgs const& a) {  // kept complemented: max of ~t = min of t
-	if (a.span && threadIdx.x == 0) atomicMax(a.span, ~global_ns());
-}
-__device__ __forceinline__ void span_end(DeliverArgs const& a) {
-	if (a.span) {  // uniform: every thread of the CTA is here
-		__syncthreads();
-		if (threadIdx.x == 0) atomicMax(a.span + 1, global_ns());
-	}
-}
+__device__ __forceinline__ void span_begin(DeliverArgs const& a) { span_open(a.span); }
+__device__ __forceinline__ void span_end(DeliverArgs const& a) { span_close(a.span); }
 
 // Plain-net delivery kernels: block -> (part, slot si, tile g over all target populations).
 struct DeliverItem {

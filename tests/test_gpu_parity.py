@@ -254,9 +254,9 @@ def test_default_shape_follows_the_network_sizes(engine):
 
 
 def test_delivery_spans_lie_inside_their_event_pairs(engine):
-    """With profiling on, each delivery launch also reports its device span (first CTA start to last
-    CTA end on the global timer), which is shorter than the CUDA-event time around the launch; the
-    raster and V stay the reference's bit for bit."""
+    """With profiling on, each neuron-update and delivery launch also reports its device span (first
+    CTA start to last CTA end on the global timer), which is shorter than the CUDA-event time around
+    the launch; the raster and V stay the reference's bit for bit."""
     g = np.load(os.path.join(GOLDEN, "brunel_n5000.npz"))
     N, seed, steps = (int(x) for x in g["meta"])
     net, pops = engine.brunel(N, float(g["p"][0]), seed)
@@ -264,13 +264,17 @@ def test_delivery_spans_lie_inside_their_event_pairs(engine):
     counts, idx = _raster_flat(net.run_record(steps))
     n_ev, ms_ev = net.kernel_stats(1)
     n_sp, ms_sp = net.kernel_span(1)
-    assert net.kernel_span(0) == (0, 0.0)  # spans are recorded for the delivery only
+    n_wev, ms_wev = net.kernel_stats(0)
+    n_wsp, ms_wsp = net.kernel_span(0)
+    assert net.kernel_span(2) == (0, 0.0)  # raster extraction: no spans
     net.set_profiling(False)
     assert np.array_equal(counts, g["counts"]) and np.array_equal(idx, g["idx"])
     for k in (1, 2):
         assert np.array_equal(pops[k].get_neurons()["V"].view(np.uint32), g[f"V{k}"].view(np.uint32))
     assert n_ev > 0 and 0 < n_sp <= n_ev
     assert 0 < ms_sp < ms_ev
+    assert n_wev > 0 and 0 < n_wsp <= n_wev
+    assert 0 < ms_wsp < ms_wev
 
 
 @pytest.mark.parametrize("persistent", [0, 1])
