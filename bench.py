@@ -22,7 +22,8 @@ Printed JSON (one line, rank 0):
   atomic_mode  value with the fast atomic delivery mode (order-dependent float rounding)
   pull_mode    the deterministic pull path (every population gathers its inputs over the CSC
                adjacency, as per-synapse weights need) on the same network: events/s, synapses
-               scanned/s, the pull kernels' roofline (4 B source index per synapse scanned), and
+               covered/s, the gather kernels' roofline (8 B per delivered event), the scan-equivalent
+               figure (the 4-byte CSC source index of every synapse covered per window), and
                whether its states equal the push path's bit for bit
   batched      the batched sweep (256 Brunel networks, N log-uniform in [5e3, 8e4], 1000 steps):
                events/s as one batch and as the plain path network after network, their ratio,
@@ -523,6 +524,12 @@ def pull_bench(steps: int, warmup: int, peak: float):
            "roofline": {"bound": "hbm", "kernel": "k_pull_masks + k_ps_scatter + k_ps_sort", "bytes_per_event": 8,
                         "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": (achieved / peak) if achieved else None},
+           # the survey's pull-mode figure: synapses whose inputs are settled per second at the 4-byte
+           # CSC source index a scan of every synapse would read per window (the gather reads only
+           # the active ones), against the same bandwidth
+           "scan_equivalent": {"bytes_per_synapse": 4, "achieved": 4 * synapses * windows / (ms / 1e3) / 1e9,
+                               "peak": peak, "unit": "GB/s",
+                               "frac": 4 * synapses * windows / (ms / 1e3) / 1e9 / peak},
            "bit_identical_to_push": bool(same), "build_seconds": build_s,
            "config": "Large Brunel N=5e5 p=0.002 seed 1, every population pulled (SPICE_TUNE_PULL), deterministic"}
     net.close()
