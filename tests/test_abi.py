@@ -97,3 +97,12 @@ def test_autotune_candidates_are_valid_launch_shapes():
         assert 0 <= algo < n_algos
     assert sorted(bench.DELIVER_KERNELS) == list(range(n_algos))
     assert set(bench.DELIVER_DRAM_BYTES_PER_EVENT) <= set(range(n_algos))
+
+
+def test_kernel_timing_entry_points_refuse_a_null_net(engine):
+    """The event-pair and device-span readers check their handle before touching a device."""
+    import ctypes as C
+    n, ms = C.c_int64(7), C.c_double(7.0)
+    for fn in ("spice_kernel_stats", "spice_kernel_span"):
+        rc = getattr(engine.lib(), fn)(None, 1, C.byref(n), C.byref(ms))
+        assert rc == engine.EINVAL and b"NULL" in engine.lib().spice_last_error()
