@@ -824,7 +824,9 @@ int setup_pull(spice_net* n) {
 		}
 		n->ps_ok    = ok;
 		n->ps_nconn = (int)ps_conn.size();
-		n->ps_units = ok ? ps_begin.back() : 0;
+		// (pulled populations without neurons have nothing to gather: no lists are kept for them,
+		// since k_ps_sort, which empties the lists, runs only over target blocks)
+		n->ps_units = (ok && blk.back() > 0) ? ps_begin.back() : 0;
 		if (ok) {
 			for (int pi : n->pull_pops) {  // the targets' entry slots
 				PopDev& d = n->pops[pi].d;

@@ -156,7 +156,8 @@ __global__ void __launch_bounds__(kPullThreads) k_pull_masks(const __grid_consta
 				int base = 0;
 				if (lane == 31 && incl) base = atomicAdd(S.nact, incl);
 				base = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
-				for (uint32_t r = any; r; r &= r - 1) S.act[base++] = 32 * w + __ffs(r) - 1;
+				for (uint32_t r = any; r; r &= r - 1, base++)  // (a list holds each source at most once)
+					if (base < S.size) S.act[base] = 32 * w + __ffs(r) - 1;
 			}
 			if (!valid) return;
 			S.orb[w] = any;

@@ -169,6 +169,31 @@ def test_pull_forced_on_brunel(engine, oracle_lib):
     assert net.events == push.events
 
 
+@pytest.mark.parametrize("fed", [True, False])
+def test_pulled_population_without_neurons(engine, fed):
+    """A pulled population of size 0 (the reference allows empty populations), beside a pulled one
+    with neurons (fed) or as the only pulled one: many windows run without error and the other
+    population matches the push path bit for bit."""
+    sp = engine
+    nets = []
+    for pull in (False, True):
+        net = sp.snn(1e-4, 15e-4, [3])
+        P = net.add_population(sp.poisson(20.0), 2000)
+        E = net.add_population(sp.lif(), 0)
+        I = net.add_population(sp.lif(), 400)
+        net.connect(P, E, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(0.02))
+        if fed:
+            net.connect(P, I, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(0.02))
+            net.connect(I, I, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(-0.01))
+        if pull:
+            net.set_tuning(pull=True)
+        net.run(1500)
+        nets.append((net, I))
+    (a, ia), (b, ib) = nets
+    assert np.array_equal(a.get_state(ia, sp.FIELD_V).view(np.uint32), b.get_state(ib, sp.FIELD_V).view(np.uint32))
+    assert a.events == b.events
+
+
 def test_pull_ungrouped_bins(engine, oracle_lib):
     """Sources firing at several steps of one window (Poisson at 3 kHz, windows of 16 steps): the
     bins overflow the targets' regions and the neuron update walks the active list instead; still
