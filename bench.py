@@ -524,9 +524,9 @@ def pull_bench(steps: int, warmup: int, peak: float):
            "roofline": {"bound": "hbm", "kernel": "k_pull_masks + k_ps_scatter + k_ps_sort", "bytes_per_event": 8,
                         "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": (achieved / peak) if achieved else None},
-           # the survey's pull-mode figure: synapses whose inputs are settled per second at the 4-byte
-           # CSC source index a scan of every synapse would read per window (the gather reads only
-           # the active ones), against the same bandwidth
+           # pull mode in synapses scanned per second: synapses whose inputs are settled per second at
+           # the 4-byte CSC source index a scan of every synapse would read per window (the gather
+           # reads only the active ones), against the same bandwidth
            "scan_equivalent": {"bytes_per_synapse": 4, "achieved": 4 * synapses * windows / (ms / 1e3) / 1e9,
                                "peak": peak, "unit": "GB/s",
                                "frac": 4 * synapses * windows / (ms / 1e3) / 1e9 / peak},
