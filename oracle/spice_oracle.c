@@ -340,6 +340,8 @@ static int conn_common(spo_net* n, int src, int dst, float delay, int field) {
 int spo_connect(spo_net* n, int src, int dst, double p, float delay, int field, float weight) {
 	if (conn_common(n, src, dst, delay, field)) return -1;
 	if (!(0 <= p && p <= 1)) return fail("Assertion failed (topology.cpp:79): 0 <= p && p <= 1");
+	/* the csr of an empty source has no offsets (csr.h:70), which generate refuses (topology.cpp:82) */
+	if (n->pops[src].size == 0) return fail("Assertion failed (topology.cpp:82): offsets.size() > src_count");
 	spo_conn* c = &n->conns[n->nconn];
 	memset(c, 0, sizeof *c);
 	c->src = src; c->dst = dst; c->field = field; c->weight = weight;
@@ -384,6 +386,8 @@ static int cmp_u64(const void* a, const void* b) {
 int spo_connect_adj(spo_net* n, int src, int dst, int64_t m, const int32_t* pairs, float delay,
                     int field, float weight) {
 	if (conn_common(n, src, dst, delay, field)) return -1;
+	/* the csr of an empty source has no offsets (csr.h:70), which Topology::generate refuses (topology.cpp:48) */
+	if (n->pops[src].size == 0) return fail("Assertion failed (topology.cpp:48): offsets.size() > src_count");
 	spo_conn* c = &n->conns[n->nconn];
 	memset(c, 0, sizeof *c);
 	c->src = src; c->dst = dst; c->field = field; c->weight = weight;

@@ -427,6 +427,8 @@ extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, d
 	int d = 0;
 	TRY(conn_common(n, src, dst, delay, &d));
 	if (!(0 <= p && p <= 1)) return pre_failed("topology.cpp:79", "0 <= p && p <= 1");
+	// the csr of an empty source has no offsets (csr.h:70), which generate refuses (topology.cpp:82)
+	if (n->pops[src].d.size == 0) return pre_failed("topology.cpp:82", "offsets.size() > src_count");
 	Conn c{};
 	memset(&c.d, 0, sizeof c.d);
 	TRY(parse_synapse(n, dst, synapse, params, np, c));
@@ -450,6 +452,8 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	int d = 0;
 	TRY(conn_common(n, src, dst, delay, &d));
 	if (npairs < 0 || (npairs > 0 && !pairs)) return fail(SPICE_EINVAL, "bad pairs");
+	// the csr of an empty source has no offsets (csr.h:70), which Topology::generate refuses (topology.cpp:48)
+	if (n->pops[src].d.size == 0) return pre_failed("topology.cpp:48", "offsets.size() > src_count");
 	Conn c{};
 	memset(&c.d, 0, sizeof c.d);
 	TRY(parse_synapse(n, dst, synapse, params, np, c));

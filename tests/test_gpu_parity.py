@@ -353,13 +353,21 @@ def test_csr_custom_adjacency(engine):
 
 
 def test_empty_and_zero_sized(engine):
+    """Empty populations: one as the source of a connection fails the reference's precondition at
+    connect (its CSR has no offsets: topology.cpp:82 for fixed_probability, :48 for adj_list); one as
+    the target, and a connection without synapses, step and deliver nothing."""
     sp = engine
     net = sp.snn(1e-4, 15e-4, [3])
     P = net.add_population(sp.poisson(), 0)
     E = net.add_population(sp.lif(), 0)
     F = net.add_population(sp.lif(), 5)
-    net.connect(P, E, sp.fixed_probability(0.5), 15e-4, sp.fixed_weight(1.0))
-    net.connect(P, F, sp.fixed_probability(0.5), 15e-4, sp.fixed_weight(1.0))
+    Q = net.add_population(sp.poisson(), 50)
+    with pytest.raises(sp.LogicError, match=r"topology\.cpp:82\): offsets\.size\(\) > src_count"):
+        net.connect(P, F, sp.fixed_probability(0.5), 15e-4, sp.fixed_weight(1.0))
+    with pytest.raises(sp.LogicError, match=r"topology\.cpp:48\): offsets\.size\(\) > src_count"):
+        net.connect(P, F, sp.adj_list(), 15e-4, sp.fixed_weight(1.0))
+    net.connect(Q, E, sp.fixed_probability(0.5), 15e-4, sp.fixed_weight(1.0))
+    net.connect(Q, F, sp.fixed_probability(0.0), 15e-4, sp.fixed_weight(1.0))
     net.run(40)
     assert net.spikes(P, 0).size == 0 and net.spikes(F, 3).size == 0
     assert net.events == 0

@@ -334,3 +334,43 @@ def test_oracle_vs_live_reference(oracle_lib, N, p, seed, steps):
         assert net.last_dt == res["dt"][t]
     for k in (1, 2):
         assert np.array_equal(net.state(pops[k], 0).view(np.uint32), st[k][0].view(np.uint32))
+
+
+def test_connection_from_an_empty_population_is_refused(oracle_lib):
+    """An empty source population has a CSR without offsets (csr.h:70), which generate refuses
+    (topology.cpp:82 for fixed_probability, topology.cpp:48 for adj_list); an empty target is kept."""
+    o = oracle_lib
+    net = o.Net(1e-4, 15e-4, [5])
+    P = net.add_population(o.POISSON, 0, (20.0,))
+    E = net.add_population(o.LIF, 0)
+    F = net.add_population(o.LIF, 40)
+    with pytest.raises(RuntimeError, match=r"Assertion failed \(topology\.cpp:82\): offsets\.size\(\) > src_count"):
+        net.connect(P, F, 0.5, 15e-4, 0.1)
+    with pytest.raises(RuntimeError, match=r"Assertion failed \(topology\.cpp:48\): offsets\.size\(\) > src_count"):
+        net.connect_adj(P, F, [], 15e-4, 0.1)
+    net.connect(F, E, 0.5, 15e-4, 0.1)
+    net.run(20)
+    assert net.events == 0
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+def test_empty_source_refused_like_the_reference(oracle_lib):
+    """The reference binary fails the same precondition, with the same message, for a connection from
+    an empty population."""
+    import subprocess
+    import tempfile
+    o = oracle_lib
+    spec = ["0.0001 0.0015 77 10 0", "pop poisson 0 20", "pop lif 30", "conn 0 1 0.1 0.0015 0.02"]
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "spec.txt")
+        open(path, "w").write("\n".join(spec) + "\n")
+        r = subprocess.run([o.REF_DRIVER, "net", path, os.path.join(d, "out.bin")], capture_output=True, text=True)
+    assert r.returncode != 0
+    assert "Assertion failed (topology.cpp:82): offsets.size() > src_count" in r.stdout + r.stderr
+    net = o.Net(1e-4, 15e-4, [77])
+    P = net.add_population(o.POISSON, 0, (20.0,))
+    L = net.add_population(o.LIF, 30)
+    with pytest.raises(RuntimeError, match=r"topology\.cpp:82\): offsets\.size\(\) > src_count"):
+        net.connect(P, L, 0.1, 15e-4, 0.02)
+
