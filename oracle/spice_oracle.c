@@ -161,7 +161,7 @@ float spo_kahan_step(spo_kahan* k, float delta) {
  * fixed_probability (topology.cpp:73-112)
  * ---------------------------------------------------------------------------------------- */
 
-/* fixed_probability::size() / src_count: floor(dst*p + 3*sqrt(dst*p*(1-p))) (topology.cpp:73-76). */
+/* fixed_probability::size() / src_count: floor(dst*p + 3*sqrt(dst*p*(1-p))) (topology.cpp:75-78). */
 int64_t spo_fp_max_degree(int64_t dst_count, double p) {
 	double m = (double)dst_count * p;
 	return (int64_t)(m + 3 * sqrt(m * (1 - p)));
@@ -246,7 +246,7 @@ struct spo_net {
 };
 
 spo_net* spo_net_create(float dt, float max_delay, const uint32_t* seeds, int nseeds) {
-	if (nseeds <= 0) { fail("Please provide at least 1 seed to seed_seq"); return NULL; }
+	if (nseeds <= 0) { fail("Assertion failed (random.h:151): il.size() > 0 && \"Please provide at least 1 seed to seed_seq\""); return NULL; }
 	spo_net* n = (spo_net*)calloc(1, sizeof(spo_net));
 	n->dt        = dt;
 	/* snn(dt, max_delay, seed): _max_delay(std::round(max_delay / dt)) (snn.h:18-19) */
@@ -339,7 +339,7 @@ static int conn_common(spo_net* n, int src, int dst, float delay, int field) {
 
 int spo_connect(spo_net* n, int src, int dst, double p, float delay, int field, float weight) {
 	if (conn_common(n, src, dst, delay, field)) return -1;
-	if (!(0 <= p && p <= 1)) return fail("Assertion failed (topology.cpp:79): 0 <= p && p <= 1");
+	if (!(0 <= p && p <= 1)) return fail("Assertion failed (topology.cpp:73): 0 <= p && p <= 1");
 	/* the csr of an empty source has no offsets (csr.h:70), which generate refuses (topology.cpp:82) */
 	if (n->pops[src].size == 0) return fail("Assertion failed (topology.cpp:82): offsets.size() > src_count");
 	spo_conn* c = &n->conns[n->nconn];
@@ -393,13 +393,31 @@ int spo_connect_adj(spo_net* n, int src, int dst, int64_t m, const int32_t* pair
 	c->src = src; c->dst = dst; c->field = field; c->weight = weight;
 	c->delay = (int64_t)roundf(delay / n->dt);
 	int64_t S = n->pops[src].size;
-	/* adj_list::generate sorts src<<32|dst and streams the edges (topology.cpp:56-71, 12-32) */
+	/* adj_list::connect checks each edge (topology.cpp:56-58); adj_list::generate sorts src<<32|dst
+	 * and streams the edges into offsets of S + 1 entries (topology.cpp:15-32, 65-71), with the
+	 * stream's checks in its order */
 	uint64_t* e = (uint64_t*)malloc(sizeof(uint64_t) * (size_t)(m + 1));
 	for (int64_t i = 0; i < m; i++) {
-		if (pairs[2 * i] < 0 || pairs[2 * i] >= S) { free(e); return fail("edge source out of range"); }
+		if (pairs[2 * i] < 0) { free(e); return fail("Assertion failed (topology.cpp:57): 0 <= src && src < std::numeric_limits<Int32>::max()"); }
+		if (pairs[2 * i + 1] < 0) { free(e); return fail("Assertion failed (topology.cpp:58): 0 <= dst && dst < std::numeric_limits<Int32>::max()"); }
 		e[i] = ((uint64_t)(uint32_t)pairs[2 * i] << 32) | (uint32_t)pairs[2 * i + 1];
 	}
 	qsort(e, (size_t)m, sizeof(uint64_t), cmp_u64);
+	{
+		int64_t at = 0; /* edge_stream::_src */
+		for (int64_t i = 0; i < m; i++) {
+			int64_t first = (int64_t)(e[i] >> 32);
+			if (!(at < S + 1)) { free(e); return fail("Assertion failed (topology.cpp:16): _src < _offsets.size()"); }
+			if (!(first < S + 1)) { free(e); return fail("Assertion failed (topology.cpp:18): edge.first < _offsets.size()"); }
+			if (at <= first) at = first + 1;
+		}
+		if (!(at < S + 1)) { free(e); return fail("Assertion failed (topology.cpp:29): _src < _offsets.size()"); }
+		for (int64_t i = 0; i < m; i++) /* a target beyond the population fails the delivery's check */
+			if ((int64_t)(e[i] & 0xffffffffu) >= n->pops[dst].size) {
+				free(e);
+				return fail("Assertion failed (synapse_population.h:119): edge.first < dst_neurons.size()");
+			}
+	}
 	c->off = (int64_t*)calloc((size_t)S + 1, sizeof(int64_t));
 	c->nb  = (int32_t*)malloc(sizeof(int32_t) * (size_t)(m + 1));
 	int64_t s = 0;

@@ -253,7 +253,7 @@ __global__ void k_fill(const double* __restrict__ gaps, const int64_t* __restric
 unsigned long long g_gen_fallbacks = 0;
 
 int64_t fp_max_degree(int64_t dst_count, double p) {
-	// fixed_probability::size() / src_count (topology.cpp:73-76, 90)
+	// fixed_probability::size() / src_count (topology.cpp:75-78, 90)
 	double const m = (double)dst_count * p;
 	return (int64_t)(m + 3 * sqrt(m * (1 - p)));
 }

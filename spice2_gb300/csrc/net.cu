@@ -191,7 +191,7 @@ extern "C" int spice_net_create(float dt, float max_delay, const uint32_t* seeds
 	if (!out) return fail(SPICE_EINVAL, "out must not be NULL");
 	*out = nullptr;
 	if (nseeds <= 0 || !seeds)
-		return pre_failed("random.h:153", "il.size() > 0 && \"Please provide at least 1 seed to seed_seq\"");
+		return pre_failed("random.h:151", "il.size() > 0 && \"Please provide at least 1 seed to seed_seq\"");
 	auto* n = new spice_net();
 	n->dt   = dt;
 	// _max_delay(std::round(max_delay / dt)) (snn.h:18-19)
@@ -250,7 +250,7 @@ extern "C" int spice_add_population(spice_net* n, int model, int64_t size, const
 	if (model < POISSON || model > EXTERNAL) return fail(SPICE_EINVAL, "unknown neuron model");
 	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
 	if (!(n->max_delay >= 1)) return pre_failed("neuron_population.h:108", "max_delay >= 1");
-	if (size >= INT32_MAX) return pre_failed("topology.cpp:51", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
+	if (size >= INT32_MAX) return pre_failed("topology.cpp:35", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
 	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
 	if (np < 0 || (np > 0 && !params)) return fail(SPICE_EINVAL, "bad params");
 	Pop p{};
@@ -292,7 +292,7 @@ extern "C" int spice_add_user_population(spice_net* n, int64_t size, int statefu
 	if (n->prepared) return fail(SPICE_ESTATE, "populations must be added before the network first steps");
 	if (!fn) return fail(SPICE_EINVAL, "a user population needs an update function");
 	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
-	if (size >= INT32_MAX) return pre_failed("topology.cpp:51", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
+	if (size >= INT32_MAX) return pre_failed("topology.cpp:35", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
 	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
 	if (stateful && (neuron_bytes <= 0 || !init_neuron))
 		return fail(SPICE_EINVAL, "a stateful user model needs its neuron struct size and initial value");
@@ -426,7 +426,7 @@ extern "C" int spice_connect_fixed_probability(spice_net* n, int src, int dst, d
                                                const float* params, int np, int* conn_out) {
 	int d = 0;
 	TRY(conn_common(n, src, dst, delay, &d));
-	if (!(0 <= p && p <= 1)) return pre_failed("topology.cpp:79", "0 <= p && p <= 1");
+	if (!(0 <= p && p <= 1)) return pre_failed("topology.cpp:73", "0 <= p && p <= 1");
 	// the csr of an empty source has no offsets (csr.h:70), which generate refuses (topology.cpp:82)
 	if (n->pops[src].d.size == 0) return pre_failed("topology.cpp:82", "offsets.size() > src_count");
 	Conn c{};
@@ -458,15 +458,29 @@ extern "C" int spice_connect_adj_list(spice_net* n, int src, int dst, const int3
 	memset(&c.d, 0, sizeof c.d);
 	TRY(parse_synapse(n, dst, synapse, params, np, c));
 	int64_t const S = n->pops[src].d.size, Dn = n->pops[dst].d.size;
-	// adj_list::generate: sort src<<32|dst, stream the edges (topology.cpp:56-71, 12-32)
+	// adj_list::connect checks each edge (topology.cpp:56-58); adj_list::generate sorts src<<32|dst and
+	// streams the edges into offsets of S + 1 entries (topology.cpp:15-32, 65-71), with the stream's
+	// checks in its order: an edge from row S or beyond fails them, as in the reference
 	std::vector<uint64_t> e((size_t)npairs);
 	for (int64_t i = 0; i < npairs; i++) {
 		int32_t const a = pairs[2 * i], b = pairs[2 * i + 1];
-		if (a < 0 || a >= S) return pre_failed("topology.cpp:15", "edge.first < _offsets.size()");
-		if (b < 0 || b >= Dn) return pre_failed("synapse_population.h:119", "edge.first < dst_neurons.size()");
+		if (a < 0) return pre_failed("topology.cpp:57", "0 <= src && src < std::numeric_limits<Int32>::max()");
+		if (b < 0) return pre_failed("topology.cpp:58", "0 <= dst && dst < std::numeric_limits<Int32>::max()");
 		e[i] = ((uint64_t)(uint32_t)a << 32) | (uint32_t)b;
 	}
 	std::sort(e.begin(), e.end());
+	{
+		int64_t at = 0;  // edge_stream::_src
+		for (uint64_t const x : e) {
+			int64_t const first = (int64_t)(x >> 32);
+			if (!(at < S + 1)) return pre_failed("topology.cpp:16", "_src < _offsets.size()");
+			if (!(first < S + 1)) return pre_failed("topology.cpp:18", "edge.first < _offsets.size()");
+			if (at <= first) at = first + 1;
+		}
+		if (!(at < S + 1)) return pre_failed("topology.cpp:29", "_src < _offsets.size()");  // flush
+	}
+	for (uint64_t const x : e)  // every source row is now below S
+		if ((int64_t)(x & 0xffffffffu) >= Dn) return pre_failed("synapse_population.h:119", "edge.first < dst_neurons.size()");
 	std::vector<int64_t> off((size_t)S + 1, 0);
 	std::vector<int32_t> nb((size_t)npairs);
 	int64_t s = 0;

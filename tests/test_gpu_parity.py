@@ -397,8 +397,13 @@ def test_errors_follow_the_reference(engine):
         net.connect(P, E, sp.fixed_probability(0.1), 0.0, sp.fixed_weight(1.0))
     with pytest.raises(sp.LogicError, match="may not exceed the maximum delay"):
         net.connect(P, E, sp.fixed_probability(0.1), 16e-4, sp.fixed_weight(1.0))
-    with pytest.raises(sp.LogicError, match=r"0 <= p && p <= 1"):
+    with pytest.raises(sp.LogicError, match=r"Assertion failed \(topology.cpp:73\): 0 <= p && p <= 1"):
         net.connect(P, E, sp.fixed_probability(1.5), 15e-4, sp.fixed_weight(1.0))
+    for first, where in ((10, "29"), (12, "18")):  # P has 10 neurons: its adjacency has 11 offsets
+        adj = sp.adj_list()
+        adj.connect(first, 0)
+        with pytest.raises(sp.LogicError, match=r"Assertion failed \(topology.cpp:" + where + r"\)"):
+            net.connect(P, E, adj, 15e-4, sp.fixed_weight(1.0))
     with pytest.raises(sp.LogicError, match="stateful"):
         net.connect(E, P, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(1.0))
     net.connect(P, E, sp.fixed_probability(0.1), 15e-4, sp.fixed_weight(1.0))

@@ -374,3 +374,73 @@ def test_empty_source_refused_like_the_reference(oracle_lib):
     with pytest.raises(RuntimeError, match=r"topology\.cpp:82\): offsets\.size\(\) > src_count"):
         net.connect(P, L, 0.1, 15e-4, 0.02)
 
+
+
+def _reference_error(spec_lines):
+    """The reference binary's error line for a network spec (None when it runs)."""
+    import subprocess
+    import tempfile
+    from oracle import oracle as o
+    with tempfile.TemporaryDirectory() as d:
+        path = os.path.join(d, "spec.txt")
+        open(path, "w").write("\n".join(spec_lines) + "\n")
+        r = subprocess.run([o.REF_DRIVER, "net", path, os.path.join(d, "out.bin")], capture_output=True, text=True)
+    if r.returncode == 0:
+        return None
+    return [ln for ln in (r.stdout + r.stderr).splitlines() if ln.startswith("Assertion failed")][0]
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+@pytest.mark.parametrize("pairs", [[(30, 0)], [(31, 0)], [(30, 0), (30, 1)], [(-1, 0)], [(0, -2)], [(3, 1), (29, 0)],
+                                   [(29, 2), (0, 0), (29, 2)]])
+def test_adj_list_checks_like_the_reference(oracle_lib, pairs):
+    """adj_list edges from rows at or beyond the source's size, and negative indices, fail the
+    reference's checks (topology.cpp:16, 18, 29, 57, 58) with its messages, in its order."""
+    o = oracle_lib
+    spec = ["0.0001 0.0015 77 10 0", "pop poisson 30 20", "pop lif 30",
+            "adj 0 1 0.0015 0.02 " + " ".join([str(len(pairs))] + [f"{a} {b}" for a, b in pairs])]
+    want = _reference_error(spec)
+    net = o.Net(1e-4, 15e-4, [77])
+    P = net.add_population(o.POISSON, 30, (20.0,))
+    L = net.add_population(o.LIF, 30)
+    if want is None:
+        net.connect_adj(P, L, pairs, 15e-4, 0.02)
+    else:
+        with pytest.raises(RuntimeError) as err:
+            net.connect_adj(P, L, pairs, 15e-4, 0.02)
+        assert str(err.value) == want
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+def test_probability_check_like_the_reference(oracle_lib):
+    """fixed_probability(p) outside [0, 1] fails the reference's constructor check (topology.cpp:73)."""
+    o = oracle_lib
+    want = _reference_error(["0.0001 0.0015 77 10 0", "pop poisson 30 20", "pop lif 30", "conn 0 1 1.5 0.0015 0.02"])
+    assert want == "Assertion failed (topology.cpp:73): 0 <= p && p <= 1"
+    net = o.Net(1e-4, 15e-4, [77])
+    P = net.add_population(o.POISSON, 30, (20.0,))
+    L = net.add_population(o.LIF, 30)
+    with pytest.raises(RuntimeError) as err:
+        net.connect(P, L, 1.5, 15e-4, 0.02)
+    assert str(err.value) == want
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+def test_adj_list_rows_after_the_last_edge_differ_from_the_reference(oracle_lib):
+    """A known difference: the reference's edge stream fills the offsets only up to the row after the
+    last edge's source (topology.cpp:15-32) and leaves the later ones 0, so an adj_list whose last
+    source is not the source's last row fails its CSR check (csr.h:76); the restatement (like the
+    engine) builds the CSR the edges describe."""
+    o = oracle_lib
+    want = _reference_error(["0.0001 0.0015 77 10 0", "pop poisson 30 20", "pop lif 30", "adj 0 1 0.0015 0.02 1 5 3"])
+    assert want == "Assertion failed (csr.h:76): std::is_sorted(_offsets.begin(), _offsets.end())"
+    net = o.Net(1e-4, 15e-4, [77])
+    P = net.add_population(o.POISSON, 30, (20.0,))
+    L = net.add_population(o.LIF, 30)
+    c = net.connect_adj(P, L, [(5, 3)], 15e-4, 0.02)
+    off, nb = net.csr_arrays(c, 30)
+    assert off.tolist() == [0] * 6 + [1] * 25 and nb.tolist() == [3]
+
