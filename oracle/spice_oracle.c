@@ -274,8 +274,14 @@ void spo_net_destroy(spo_net* n) {
 
 int spo_add_population(spo_net* n, int kind, int64_t size, const float* prm, int np) {
 	if (n->npop >= 16) return fail("too many populations");
-	if (size < 0) return fail("size >= 0");
-	if (n->max_delay < 1) return fail("max_delay >= 1");
+	/* a negative size as the reference's neuron adapters meet it: the stateless and per-population
+	 * adapters check it (neuron_population.h:35, :92); a stateful one's vector(size) throws first */
+	if (size < 0) {
+		if (kind == SPO_POISSON) return fail("Assertion failed (neuron_population.h:35): size >= 0");
+		if (kind == SPO_EXTERNAL) return fail("Assertion failed (neuron_population.h:92): size >= 0");
+		return fail("cannot create std::vector larger than max_size()");
+	}
+	if (n->max_delay < 1) return fail("Assertion failed (neuron_population.h:108): max_delay >= 1");
 	spo_pop* p = &n->pops[n->npop];
 	memset(p, 0, sizeof *p);
 	p->kind = kind;

@@ -243,12 +243,24 @@ extern "C" int spice_net_destroy(spice_net* n) {
 	return SPICE_OK;
 }
 
+namespace {
+// A negative population size as the reference's neuron adapters meet it: a stateless adapter checks
+// the size (neuron_population.h:35), a per-population one too (:92), and a stateful one's
+// std::vector<neuron>(size) throws std::length_error (a std::logic_error) before its own check.
+// kind: 0 stateless, 1 stateful, 2 per-population update.
+int negative_size(int kind) {
+	if (kind == 0) return pre_failed("neuron_population.h:35", "size >= 0");
+	if (kind == 2) return pre_failed("neuron_population.h:92", "size >= 0");
+	return fail(SPICE_EINVAL, "cannot create std::vector larger than max_size()");
+}
+}  // namespace
+
 extern "C" int spice_add_population(spice_net* n, int model, int64_t size, const float* params, int np,
                                     int* pop_out) {
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
 	if (n->prepared) return fail(SPICE_ESTATE, "populations must be added before the network first steps");
 	if (model < POISSON || model > EXTERNAL) return fail(SPICE_EINVAL, "unknown neuron model");
-	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
+	if (!(size >= 0)) return negative_size(model == POISSON ? 0 : model == EXTERNAL ? 2 : 1);
 	if (!(n->max_delay >= 1)) return pre_failed("neuron_population.h:108", "max_delay >= 1");
 	if (size >= INT32_MAX) return pre_failed("topology.cpp:35", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
 	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
@@ -291,7 +303,7 @@ extern "C" int spice_add_user_population(spice_net* n, int64_t size, int statefu
 	if (!n) return fail(SPICE_EINVAL, "net must not be NULL");
 	if (n->prepared) return fail(SPICE_ESTATE, "populations must be added before the network first steps");
 	if (!fn) return fail(SPICE_EINVAL, "a user population needs an update function");
-	if (!(size >= 0)) return pre_failed("neuron_population.h:34", "size >= 0");
+	if (!(size >= 0)) return negative_size(stateful ? 1 : 0);
 	if (size >= INT32_MAX) return pre_failed("topology.cpp:35", "0 <= src_count_ && src_count_ < std::numeric_limits<Int32>::max()");
 	if ((int)n->pops.size() >= kMaxPops) return fail(SPICE_EINVAL, "too many populations");
 	if (stateful && (neuron_bytes <= 0 || !init_neuron))

@@ -387,7 +387,8 @@ def _reference_error(spec_lines):
         r = subprocess.run([o.REF_DRIVER, "net", path, os.path.join(d, "out.bin")], capture_output=True, text=True)
     if r.returncode == 0:
         return None
-    return [ln for ln in (r.stdout + r.stderr).splitlines() if ln.startswith("Assertion failed")][0]
+    lines = [ln for ln in (r.stdout + r.stderr).splitlines() if ln.strip()]
+    return next((ln for ln in lines if ln.startswith("Assertion failed")), lines[0])
 
 
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
@@ -444,3 +445,21 @@ def test_adj_list_rows_after_the_last_edge_differ_from_the_reference(oracle_lib)
     off, nb = net.csr_arrays(c, 30)
     assert off.tolist() == [0] * 6 + [1] * 25 and nb.tolist() == [3]
 
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+@pytest.mark.parametrize("header,kind,size", [("0.0001 0.0015 77 10 0", "poisson", -5), ("0.0001 0.0015 77 10 0", "lif", -5),
+                                              ("0.0001 0.00001 77 10 0", "lif", 30)])
+def test_population_checks_like_the_reference(oracle_lib, header, kind, size):
+    """A negative size fails as the reference's neuron adapters fail it (a stateless adapter's check at
+    neuron_population.h:35; a stateful adapter's vector throws first); a maximum delay below one
+    step fails neuron_population.h:108."""
+    o = oracle_lib
+    want = _reference_error([header, f"pop {kind} {size}" + (" 20" if kind == "poisson" else "")])
+    assert want is not None
+    dt, max_delay = (float(x) for x in header.split()[:2])
+    net = o.Net(dt, max_delay, [77])
+    with pytest.raises(RuntimeError) as err:
+        net.add_population(o.POISSON if kind == "poisson" else o.LIF, size, (20.0,) if kind == "poisson" else ())
+    assert str(err.value) == want
