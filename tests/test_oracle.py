@@ -76,7 +76,8 @@ def test_csr_small_cases(oracle_lib):
 @pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
                                                     "ref_driver")), reason="reference driver not built here")
 @pytest.mark.parametrize("src,dst,p,seed", [(1, 1, 1.0, 5), (257, 1000, 0.013, 77), (4000, 300, 0.5, 9),
-                                            (3, 70000, 0.0007, 123), (1000, 1000, 0.999, 42), (50, 20, 0.0, 1)])
+                                            (3, 70000, 0.0007, 123), (1000, 1000, 0.999, 42), (50, 20, 0.0, 1),
+                                            (50, 0, 0.3, 2), (2, 5, 1.0, 3), (6000, 2, 0.5, 4)])
 def test_csr_vs_live_reference(oracle_lib, src, dst, p, seed):
     """fixed_probability adjacency of the restatement against the reference binary on shapes the
     fixtures do not hold (single synapse, near-empty and near-full rows, very sparse wide rows)."""
