@@ -487,3 +487,58 @@ def test_distributions_pass_the_reference_ks_tests(oracle_lib, seed):
             x = a + (b - a) * i * 0.01
             ks = max(ks, abs(1e-3 * np.count_nonzero(draws[1000 * i:1000 * (i + 1)] <= x) - cdf(x)))
         assert ks <= 0.06, ks
+
+
+def _random_net_spec(case):
+    """A small random network (seeded by `case`): 1-2 Poisson sources and 1-3 LIF populations, 3-7
+    fixed_probability projections into LIF populations with delays of 1..8 steps and weights of
+    either sign, 250 steps."""
+    rng = np.random.default_rng(1000 + case)
+    dt, max_delay = 1e-4, 8e-4
+    pops = [("poisson", int(rng.integers(50, 400)), float(rng.choice([10.0, 20.0, 40.0])))
+            for _ in range(int(rng.integers(1, 3)))]
+    pops += [("lif", int(rng.integers(20, 300)), None) for _ in range(int(rng.integers(1, 4)))]
+    lifs = [i for i, p in enumerate(pops) if p[0] == "lif"]
+    conns = []
+    for _ in range(int(rng.integers(3, 8))):
+        s, d = int(rng.integers(0, len(pops))), int(rng.choice(lifs))
+        p = float(np.float32(rng.choice([0.02, 0.05, 0.1, 0.3])))
+        delay = float(np.float32(int(rng.integers(1, 9)) * 1e-4))
+        w = float(np.float32(rng.choice([1, 1, -1]) * rng.uniform(0.002, 0.02)))
+        conns.append((s, d, p, delay, w))
+    seed = int(rng.integers(1, 1 << 31))
+    lines = [f"{dt!r} {max_delay!r} {seed} 250 0"]
+    lines += [f"pop poisson {n} {r!r}" if k == "poisson" else f"pop lif {n}" for k, n, r in pops]
+    lines += [f"conn {s} {d} {p!r} {delay!r} {w!r}" for s, d, p, delay, w in conns]
+    return dt, max_delay, seed, pops, conns, lines
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+@pytest.mark.parametrize("case", range(12))
+def test_random_networks_vs_live_reference(oracle_lib, case):
+    """Random small networks (population counts and sizes, rates, densities, delays of 1..8 steps,
+    signed weights, connection order) on the restatement and on the reference binary: every step's
+    raster and dt, the event count, and the final V / Tref of every LIF population, bit for bit."""
+    o = oracle_lib
+    dt, max_delay, seed, pops, conns, spec = _random_net_spec(case)
+    res = o.run_reference_net(spec)
+    lifs = [i for i, p in enumerate(pops) if p[0] == "lif"]
+    st, _, _ = o.reference_states(res, lifs)
+    net = o.Net(dt, max_delay, [seed])
+    for k, n, r in pops:
+        net.add_population(o.POISSON if k == "poisson" else o.LIF, n, (r,) if k == "poisson" else ())
+    for s, d, p, delay, w in conns:
+        net.connect(s, d, p, delay, w)
+    spikes = 0
+    for t in range(250):
+        net.step()
+        assert net.last_dt == res["dt"][t]
+        for k in range(len(pops)):
+            got = net.spikes(k, 0)
+            assert np.array_equal(got, res["raster"][t][k]), (t, k)
+            spikes += got.size
+    assert spikes > 0
+    for k in lifs:
+        assert np.array_equal(net.state(k, 0).view(np.uint32), st[k][0].view(np.uint32))
+        assert np.array_equal(net.state(k, 3), st[k][1])
