@@ -542,3 +542,45 @@ def test_random_networks_vs_live_reference(oracle_lib, case):
     for k in lifs:
         assert np.array_equal(net.state(k, 0).view(np.uint32), st[k][0].view(np.uint32))
         assert np.array_equal(net.state(k, 3), st[k][1])
+
+
+@pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "_ref",
+                                                    "ref_driver")), reason="reference driver not built here")
+@pytest.mark.parametrize("case", range(8))
+def test_random_conductance_networks_vs_live_reference(oracle_lib, case):
+    """Random small networks of the conductance LIF (samples/vogels.cpp, as the reference's fast-math
+    build computes it): Poisson drive and recurrent excitatory (Gex) and inhibitory (Gin) projections
+    with random densities, delays of 1..8 steps and weights; rasters and final V / Gex / Gin / Tref
+    bit for bit against the reference binary."""
+    o = oracle_lib
+    rng = np.random.default_rng(2000 + case)
+    dt, max_delay, steps = 1e-4, 8e-4, 300
+    pops = [("poisson", int(rng.integers(100, 400)), float(rng.choice([20.0, 40.0])))]
+    pops += [("lif_cond", int(rng.integers(30, 300)), None) for _ in range(int(rng.integers(1, 3)))]
+    conds = list(range(1, len(pops)))
+    conns = []
+    for _ in range(int(rng.integers(2, 6))):
+        s, d = int(rng.integers(0, len(pops))), int(rng.choice(conds))
+        field = 1 if s == 0 or rng.random() < 0.5 else 2
+        w = float(np.float32(rng.uniform(0.05, 0.5) if field == 1 else rng.uniform(0.1, 1.0)))
+        conns.append((s, d, float(np.float32(rng.choice([0.05, 0.1, 0.3]))),
+                      float(np.float32(int(rng.integers(1, 9)) * 1e-4)), w, field))
+    seed = int(rng.integers(1, 1 << 31))
+    spec = [f"{dt!r} {max_delay!r} {seed} {steps} 0"]
+    spec += [f"pop poisson {n} {r!r}" if k == "poisson" else f"pop lif_cond {n}" for k, n, r in pops]
+    spec += [f"conn {s} {d} {p!r} {delay!r} {w!r} {f}" for s, d, p, delay, w, f in conns]
+    res = o.run_reference_net(spec)
+    st, _, _ = o.reference_states(res, [], conds)
+    net = o.Net(dt, max_delay, [seed])
+    for k, n, r in pops:
+        net.add_population(o.POISSON if k == "poisson" else o.LIF_COND, n, (r,) if k == "poisson" else ())
+    for s, d, p, delay, w, f in conns:
+        net.connect(s, d, p, delay, w, f)
+    for t in range(steps):
+        net.step()
+        for k in range(len(pops)):
+            assert np.array_equal(net.spikes(k, 0), res["raster"][t][k]), (t, k)
+    for k in conds:
+        for field in range(3):
+            assert np.array_equal(net.state(k, field).view(np.uint32), st[k][field].view(np.uint32)), (k, field)
+        assert np.array_equal(net.state(k, 3), st[k][3])
